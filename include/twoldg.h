@@ -1,0 +1,145 @@
+/*
+ * twoldg.h -- C ABI of libtwoldg, the GB300 (sm_103a) implementation of the
+ * OLDG field right-hand side and RK4 time step of TreeWaveOLDG.jl.
+ *
+ * Plain C: no C++ or torch types in any signature, so Julia `ccall`, Python
+ * ctypes or any FFI can bind it. Every call returns an int status (0 = ok,
+ * else one of TWOLDG_E*); twoldg_last_error() gives the text of the most
+ * recent failure on the calling thread.
+ *
+ * Ownership: the caller owns the state vectors (device pointers in the
+ * reference's state layout (N^D, 2, nblocks), column-major, u then v per
+ * block, src/stepping.jl:24-25), so `pointer(::CuArray)` passes straight
+ * through. The library owns its ghost/face buffers, stage scratch, tables
+ * and one CUDA stream per problem; calls on one problem are not
+ * thread-safe. All calls are asynchronous on the problem's stream except
+ * those that return host scalars (energy, norm) and twoldg_synchronize.
+ */
+#ifndef TWOLDG_H
+#define TWOLDG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TWOLDG_OK 0
+#define TWOLDG_EINVAL 1     /* bad descriptor or argument (host-checked) */
+#define TWOLDG_ECUDA 2      /* a CUDA call failed */
+#define TWOLDG_ENOMEM 3     /* device allocation failed */
+#define TWOLDG_EUNSUP 4     /* valid but not supported by this build (e.g. order, block size) */
+
+#define TWOLDG_F64 0        /* plain FP64: the drop-in */
+#define TWOLDG_F32 1        /* FP32 fields and stencil */
+#define TWOLDG_F32C 2       /* FP32 fields, compensated (two-sum) RK4 accumulation */
+
+/*
+ * A forest of blocks in the form TreeAMR's Forest holds it (a brick of
+ * roots[d] root blocks per dimension, each leaf a block at `level` whose
+ * integer corner `corner[b*dim + d]` counts blocks of that level from the
+ * domain's low corner), with the element layout of the reference's
+ * element-centered field sets: N = elems * (order + 1) nodes per block and
+ * dimension, `elems` even (src/layout.jl:31-47). Faces are periodic,
+ * reflecting (solid wall: u, v even, d_d u odd; src/evolution.jl:1025-1027)
+ * per dimension; a forest may be refined with 2:1 face balance, and its
+ * coarse-fine faces get the element-local prolongation / restriction
+ * ghosts. Blocks are numbered in the caller's order, which is the state
+ * layout's block order.
+ */
+typedef struct twoldg_desc {
+    int32_t dim;             /* D = 1, 2 or 3 */
+    int32_t order;           /* P >= 1 */
+    int32_t elems;           /* E, even */
+    int32_t precision;       /* TWOLDG_F64 / TWOLDG_F32 / TWOLDG_F32C */
+    int32_t truncate;        /* 1: v held at degree P-1 (the paper's scheme) */
+    int32_t nblocks;
+    int32_t roots[3];
+    int32_t periodic[3];
+    int32_t reflecting[3];
+    double lo[3];
+    double hi[3];
+    const int32_t* level;    /* nblocks */
+    const int64_t* corner;   /* nblocks * dim */
+} twoldg_desc;
+
+typedef struct twoldg_problem twoldg_problem;
+
+const char* twoldg_last_error(void);
+const char* twoldg_version(void);
+
+/* Element tables of order P rounded once to float64 (precision 0) or float32
+ * (precision 1), for the host side's node positions and for tests:
+ * src/element.jl:129-170 (Element(T, P)). Arrays are row-major; `out` must
+ * hold table_size(P) words of the requested type. Sizes per order P:
+ * nodes, weights, offsets: P+1; stencil (P+1)(P+3); truncate (P+1)^2;
+ * topmode, topdual: P+1; duals (P+1)^2; prolong 2(P+1)^2; restrict 2(P+1)^2. */
+int twoldg_element_tables(int32_t order, int32_t precision, const char* name, void* out);
+
+/* WaveProblem(forest, el; truncate) -- src/evolution.jl:1043-1108.
+ * Builds the neighbour and coarse-fine face tables, uploads the tables and
+ * allocates the scratch. */
+int twoldg_problem_create(const twoldg_desc* desc, twoldg_problem** out);
+int twoldg_problem_destroy(twoldg_problem* p);
+
+/* Words of the state vector: N^D * 2 * nblocks. */
+int twoldg_state_words(const twoldg_problem* p, int64_t* words);
+/* Smallest block spacing (the finest level's) -- minimum_spacing(forest). */
+int twoldg_min_spacing(const twoldg_problem* p, double* h);
+
+/* wave_rhs!(du, u, p, t) -- src/evolution.jl:1367-1371: du = (v, sum_d D_d D_d u).
+ * Does not truncate, never writes u. */
+int twoldg_rhs(twoldg_problem* p, void* du, const void* u, double t);
+
+/* truncate_state!(u, p) -- src/evolution.jl:1383-1395: v <- (Pi x ... x Pi) v
+ * per element, in place; no-op when the problem does not truncate. */
+int twoldg_truncate(twoldg_problem* p, void* u);
+
+/* `nsteps` classic RK4 steps of size dt from time t, in place on u, with the
+ * truncation as stage and step limiter -- wave_integrator + solve!
+ * (src/stepping.jl:72-78, src/evolution.jl:1408-1430). The step is a CUDA
+ * graph, captured on the first call and re-captured when u or dt change.
+ * For TWOLDG_F32C the compensation words persist between calls on the same
+ * u and are cleared when u changes or by twoldg_reset_compensation. */
+int twoldg_rk4_step(twoldg_problem* p, void* u, double t, double dt, int32_t nsteps);
+int twoldg_reset_compensation(twoldg_problem* p);
+
+/* wave_energy(p, u) -- src/evolution.jl:1472-1489: 1/2 sum w (v^2 + sum_d (D_d u)^2),
+ * FP64 accumulation, deterministic order. Synchronous. */
+int twoldg_energy(twoldg_problem* p, const void* u, double t, double* energy);
+
+/* quadrature_norm(fs, el, u; p, vars) -- src/layout.jl:223-235, of u - ref
+ * when ref is not NULL. p >= 1, or p = 0 for the largest |value| (p = Inf).
+ * vars_mask bit 0 = u, bit 1 = v. FP64 accumulation. Synchronous. */
+int twoldg_norm(twoldg_problem* p, const void* u, const void* ref, int32_t pnorm, int32_t vars_mask,
+                double* out);
+
+/* modal_indicator(fs, el; mode, var) -- src/refinement.jl:147-155 (mode_kernel!
+ * :56-77): tau[e1..eD, b] = max over lines and m = 1..mode of
+ * (|c_m| (2m-1)!!/A)^(mode/m) / (2 mode - 1)!!, A the global peak |var|.
+ * var is 1 (u) or 2 (v); tau_dev holds E^D * nblocks words of the field type. */
+int twoldg_modal_indicator(twoldg_problem* p, const void* u, int32_t var, int32_t mode, void* tau_dev);
+/* mode_amplitude(fs, el; mode, var) -- src/refinement.jl:169-175. */
+int twoldg_mode_amplitude(twoldg_problem* p, const void* u, int32_t var, int32_t mode, void* tau_dev);
+
+/* Waits for all work queued on the problem's stream. */
+int twoldg_synchronize(twoldg_problem* p);
+
+/* Batched ensemble: n independent problems stepped together, the blocks of
+ * all of them as one work list per (dim, order, elems) group and one RK4
+ * step per CUDA graph launch. No reference counterpart (the reference runs
+ * one forest per WaveProblem); each member behaves as twoldg_rk4_step on its
+ * own problem. States are one device buffer: member k's state starts at word
+ * offsets[k] (as returned by twoldg_batch_offsets). */
+typedef struct twoldg_batch twoldg_batch;
+int twoldg_batch_create(int32_t n, const twoldg_desc* descs, twoldg_batch** out);
+int twoldg_batch_destroy(twoldg_batch* b);
+int twoldg_batch_offsets(const twoldg_batch* b, int64_t* offsets, int64_t* total_words);
+int twoldg_batch_rk4_step(twoldg_batch* b, void* u, const double* dt, int32_t nsteps);
+int twoldg_batch_synchronize(twoldg_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TWOLDG_H */

@@ -1,0 +1,498 @@
+/*
+ * oracle.c -- CPU oracle for the OLDG field step. TEST INFRASTRUCTURE ONLY:
+ * it is the checker for the CUDA library (tests/, __graft_entry__.smoke())
+ * and the timed CPU baseline (bench.py's cpu_baseline and --impl reference);
+ * nothing in the product links or calls it.
+ *
+ * A plain-C restatement of the reference's algorithm, written to share as
+ * little as possible with the CUDA path:
+ *   - wide derivative, gradient and Laplacian passes: src/evolution.jl:24-35,
+ *     67-110 (wide_derivative, gradient_kernel!, laplacian_kernel!), with the
+ *     stencil applied over its full (P+3)-wide window;
+ *   - ghosts: each ghost point finds its neighbour by locating the point just
+ *     across the face in a finest-level cell map (not by the library's face
+ *     table), then applies the documented TreeAMR element-local semantics
+ *     (reference CODE.md "The layout", "Reflecting walls", "The coupling"):
+ *     injection at equal level, mirror with u even and d_d u odd at walls,
+ *     and across coarse-fine faces the coarse element's Lagrange polynomial
+ *     evaluated at the fine node (I) or the adjoint restriction
+ *     R = M_c^-1 I^T M_f, both evaluated here from the nodes and weights;
+ *   - truncation: the dense projector el.truncate applied along each
+ *     dimension of each element (the matrix the reference's tests compare
+ *     the rank-one kernel against, test/evolution_tests.jl:83-103);
+ *   - RK4: the classic tableau, truncation as stage and step limiter
+ *     (src/evolution.jl:1408-1430), u^{n+1} = T(u + dt/6 (k1+2k2+2k3+k4));
+ *   - energy, norm: src/evolution.jl:1472-1489, src/layout.jl:100-122,223-235;
+ *   - modal indicator: src/refinement.jl:56-100, 147-179.
+ * Tables (nodes, weights, stencil, projector, duals) come from the caller:
+ * the tests load them from tests/golden/element_tables.json, an mpmath
+ * 512-bit restatement of src/element.jl.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef struct {
+    int D, P, E, nblocks, truncate;
+    int roots[3], periodic[3], reflecting[3];
+    double lo[3], hi[3];
+    const int32_t* level;
+    const int64_t* corner;
+    const double* nodes;     /* P+1 */
+    const double* weights;   /* P+1 */
+    const double* stencil;   /* (P+1) x (P+3) row-major */
+    const double* projector; /* (P+1) x (P+1) row-major */
+    const double* duals;     /* (P+1) x (P+1) row-major */
+} oracle_mesh;
+
+typedef struct {
+    const oracle_mesh* m;
+    int N, P1;
+    int64_t NN;       /* nodes per block */
+    int lmax;
+    int64_t grid[3];  /* finest cells per dim */
+    int32_t* owner;   /* finest cell -> leaf */
+    double cellw;     /* root block width (physical) */
+} ctx_t;
+
+static int64_t ipow64(int64_t b, int e) { int64_t r = 1; while (e-- > 0) r *= b; return r; }
+
+static int ctx_init(ctx_t* c, const oracle_mesh* m) {
+    c->m = m;
+    c->P1 = m->P + 1;
+    c->N = m->E * c->P1;
+    c->NN = ipow64(c->N, m->D);
+    c->lmax = 0;
+    for (int b = 0; b < m->nblocks; ++b) if (m->level[b] > c->lmax) c->lmax = m->level[b];
+    int64_t total = 1;
+    for (int k = 0; k < 3; ++k) {
+        c->grid[k] = k < m->D ? ((int64_t)m->roots[k] << c->lmax) : 1;
+        total *= c->grid[k];
+    }
+    c->owner = (int32_t*)malloc(sizeof(int32_t) * total);
+    if (!c->owner) return -1;
+    for (int64_t i = 0; i < total; ++i) c->owner[i] = -1;
+    for (int b = 0; b < m->nblocks; ++b) {
+        int64_t span = (int64_t)1 << (c->lmax - m->level[b]);
+        int64_t c0[3] = {0, 0, 0}, c1[3] = {1, 1, 1};
+        for (int k = 0; k < m->D; ++k) { c0[k] = m->corner[(int64_t)b * m->D + k] * span; c1[k] = c0[k] + span; }
+        for (int64_t z = c0[2]; z < c1[2]; ++z)
+            for (int64_t y = c0[1]; y < c1[1]; ++y)
+                for (int64_t x = c0[0]; x < c1[0]; ++x)
+                    c->owner[x + c->grid[0] * (y + c->grid[1] * z)] = b;
+    }
+    c->cellw = (m->hi[0] - m->lo[0]) / m->roots[0];
+    return 0;
+}
+
+/* The leaf containing point x (in root-block units), with periodic wrap;
+ * -1 outside a non-periodic domain. */
+static int locate(const ctx_t* c, const double* x) {
+    int64_t i[3] = {0, 0, 0};
+    for (int k = 0; k < c->m->D; ++k) {
+        double s = x[k] * (double)((int64_t)1 << c->lmax);
+        int64_t v = (int64_t)floor(s);
+        if (v < 0 || v >= c->grid[k]) {
+            if (!c->m->periodic[k]) return -1;
+            v = ((v % c->grid[k]) + c->grid[k]) % c->grid[k];
+        }
+        i[k] = v;
+    }
+    return c->owner[i[0] + c->grid[0] * (i[1] + c->grid[1] * i[2])];
+}
+
+static double block_width(const ctx_t* c, int b) { return 1.0 / (double)((int64_t)1 << c->m->level[b]); }
+static double block_origin(const ctx_t* c, int b, int k) {
+    return (double)c->m->corner[(int64_t)b * c->m->D + k] * block_width(c, b);
+}
+static double spacing(const ctx_t* c, int b) { return c->cellw * block_width(c, b) / c->N; }
+
+static int64_t oidx(const ctx_t* c, const int* x) {
+    int64_t r = 0, s = 1;
+    for (int k = 0; k < c->m->D; ++k) { r += x[k] * s; s *= c->N; }
+    return r;
+}
+
+static double lagrange(const double* xi, int n, int j, double x) {
+    double r = 1.0;
+    for (int k = 0; k < n; ++k) if (k != j) r *= (x - xi[k]) / (xi[j] - xi[k]);
+    return r;
+}
+
+/* The ghost across face (d, side) of block b at the face node whose
+ * tangential owned coordinates are x[k] (k != d), read from the owned field
+ * `f` (N^D per block). parity is the wall sign. */
+static double ghost_value(const ctx_t* c, int b, int d, int side, const int* x, const double* f, double parity) {
+    const oracle_mesh* m = c->m;
+    const int D = m->D, P1 = c->P1, N = c->N, E = m->E;
+    double w = block_width(c, b);
+    double ew = w / E;
+    double pt[3];
+    for (int k = 0; k < D; ++k) {
+        if (k == d) pt[k] = side ? block_origin(c, b, k) + w + 0.25 * ew : block_origin(c, b, k) - 0.25 * ew;
+        else pt[k] = block_origin(c, b, k) + ((x[k] / P1) + 0.5) * ew;
+    }
+    int nb = locate(c, pt);
+    if (nb < 0) {
+        /* reflecting wall: the mirror of this block's own face node */
+        int y[3] = {0, 0, 0};
+        for (int k = 0; k < D; ++k) y[k] = k == d ? (side ? N - 1 : 0) : x[k];
+        return parity * f[(int64_t)b * c->NN + oidx(c, y)];
+    }
+    int ln = m->level[nb], lb = m->level[b];
+    int y[3] = {0, 0, 0};
+    y[d] = side ? 0 : N - 1;
+    const double* fn = f + (int64_t)nb * c->NN;
+    if (ln == lb) {
+        for (int k = 0; k < D; ++k) if (k != d) y[k] = x[k];
+        return fn[oidx(c, y)];
+    }
+    double wn = block_width(c, nb), ewn = wn / E;
+    if (ln == lb - 1) {
+        /* fine ghost from the coarse neighbour: its element's polynomial at our node */
+        int ec[3] = {0, 0, 0};
+        double xi[3] = {0, 0, 0};
+        for (int k = 0; k < D; ++k) {
+            if (k == d) continue;
+            int e = x[k] / P1, i = x[k] % P1;
+            double center = block_origin(c, b, k) + (e + 0.5) * ew;
+            double rel = center - block_origin(c, nb, k);
+            /* periodic images never split a tangential coordinate: faces are inside the box tangentially */
+            ec[k] = (int)floor(rel / ewn);
+            double mid = block_origin(c, nb, k) + (ec[k] + 0.5) * ewn;
+            int half = center > mid ? 1 : 0;
+            xi[k] = (m->nodes[i] + (half ? 1.0 : -1.0)) / 2.0;
+        }
+        double acc = 0.0;
+        int tk[2], nt = 0;
+        for (int k = 0; k < D; ++k) if (k != d) tk[nt++] = k;
+        int64_t combos = ipow64(P1, nt);
+        for (int64_t q = 0; q < combos; ++q) {
+            double wgt = 1.0;
+            int64_t qq = q;
+            for (int a = 0; a < nt; ++a) {
+                int k = tk[a], j = (int)(qq % P1);
+                qq /= P1;
+                wgt *= lagrange(m->nodes, P1, j, xi[k]);
+                y[k] = ec[k] * P1 + j;
+            }
+            acc += wgt * fn[oidx(c, y)];
+        }
+        return acc;
+    }
+    /* coarse ghost from the fine neighbours: R = M_c^-1 I^T M_f over the
+     * 2(P+1) fine nodes of our element along each tangential dimension */
+    {
+        int tk[2], nt = 0;
+        for (int k = 0; k < D; ++k) if (k != d) tk[nt++] = k;
+        int ecur[3] = {0, 0, 0}, jn[3] = {0, 0, 0};
+        for (int a = 0; a < nt; ++a) { int k = tk[a]; ecur[k] = x[k] / P1; jn[k] = x[k] % P1; }
+        int64_t combos = ipow64(2 * P1, nt);
+        double acc = 0.0;
+        for (int64_t q = 0; q < combos; ++q) {
+            double wgt = 1.0;
+            double ptf[3];
+            int rr[3] = {0, 0, 0}, half[3] = {0, 0, 0};
+            int64_t qq = q;
+            for (int a = 0; a < nt; ++a) {
+                int k = tk[a];
+                int r = (int)(qq % (2 * P1));
+                qq /= 2 * P1;
+                rr[k] = r % P1;
+                half[k] = r / P1;
+                double xc = (m->nodes[rr[k]] + (half[k] ? 1.0 : -1.0)) / 2.0;
+                wgt *= lagrange(m->nodes, P1, jn[k], xc) * m->weights[rr[k]] / (2.0 * m->weights[jn[k]]);
+                ptf[k] = block_origin(c, b, k) + (ecur[k] + 0.25 + 0.5 * half[k]) * ew;
+            }
+            ptf[d] = pt[d];
+            int fb = locate(c, ptf);
+            if (fb < 0) return NAN;
+            int z[3] = {0, 0, 0};
+            z[d] = side ? 0 : N - 1;
+            for (int a = 0; a < nt; ++a) {
+                int k = tk[a];
+                double rel = ptf[k] - block_origin(c, fb, k);
+                int fe = (int)floor(rel / (block_width(c, fb) / E));
+                z[k] = fe * P1 + rr[k];
+            }
+            acc += wgt * f[(int64_t)fb * c->NN + oidx(c, z)];
+        }
+        return acc;
+    }
+}
+
+/* D_d a / h at every owned node of block b, with a's ghosts across the two
+ * faces normal to d (src/evolution.jl:24-35). */
+static void derivative_block(const ctx_t* c, int b, int d, const double* a, double parity, double* out) {
+    const oracle_mesh* m = c->m;
+    const int N = c->N, P1 = c->P1, PW = m->P + 3;
+    const double h = spacing(c, b);
+    const double* ab = a + (int64_t)b * c->NN;
+    int x[3] = {0, 0, 0};
+    for (int64_t n = 0; n < c->NN; ++n) {
+        int64_t r = n;
+        for (int k = 0; k < m->D; ++k) { x[k] = (int)(r % N); r /= N; }
+        int I = x[d];
+        int i = I % P1;
+        int start = I - i - 1;
+        double acc = 0.0;
+        for (int k = 0; k < PW; ++k) {
+            int pos = start + k;
+            double val;
+            if (pos < 0 || pos >= N) {
+                double coef = m->stencil[i * PW + k];
+                if (coef == 0.0) continue;
+                val = ghost_value(c, b, d, pos >= N, x, a, parity);
+            } else {
+                int y[3] = {x[0], x[1], x[2]};
+                y[d] = pos;
+                val = ab[oidx(c, y)];
+            }
+            acc += m->stencil[i * PW + k] * val;
+        }
+        out[n] = acc / h;
+    }
+}
+
+int oracle_rhs(const oracle_mesh* m, const double* u, double* du) {
+    ctx_t c;
+    if (ctx_init(&c, m)) return -1;
+    const int D = m->D;
+    const int64_t NN = c.NN, nb = m->nblocks;
+    double* ua = (double*)malloc(sizeof(double) * NN * nb);
+    double* g = (double*)malloc(sizeof(double) * NN * nb * D);
+    if (!ua || !g) { free(ua); free(g); free(c.owner); return -1; }
+#pragma omp parallel for schedule(dynamic)
+    for (int64_t b = 0; b < nb; ++b) memcpy(ua + b * NN, u + b * 2 * NN, sizeof(double) * NN);
+#pragma omp parallel for schedule(dynamic)
+    for (int64_t b = 0; b < nb; ++b)
+        for (int d = 0; d < D; ++d) derivative_block(&c, (int)b, d, ua, 1.0, g + (int64_t)d * NN * nb + b * NN);
+#pragma omp parallel
+    {
+        double* tmp = (double*)malloc(sizeof(double) * NN);
+#pragma omp for schedule(dynamic)
+        for (int64_t b = 0; b < nb; ++b) {
+            double* dv = du + b * 2 * NN + NN;
+            for (int64_t n = 0; n < NN; ++n) dv[n] = 0.0;
+            for (int d = 0; d < D; ++d) {
+                derivative_block(&c, (int)b, d, g + (int64_t)d * NN * nb, -1.0, tmp);
+                for (int64_t n = 0; n < NN; ++n) dv[n] += tmp[n];
+            }
+            memcpy(du + b * 2 * NN, u + b * 2 * NN + NN, sizeof(double) * NN);
+        }
+        free(tmp);
+    }
+    free(ua);
+    free(g);
+    free(c.owner);
+    return 0;
+}
+
+/* The reference's Laplacian divides the summed second derivatives by h once,
+ * with each gradient already divided by h: D_d(D_d u / h) / h. The routine
+ * above divides both passes' stencil sums by h, which is the same value. */
+
+static void truncate_with(const ctx_t* c, double* u) {
+    const oracle_mesh* m = c->m;
+    const int D = m->D, N = c->N, P1 = c->P1, E = m->E;
+    const int64_t NN = c->NN;
+    const int64_t nel = ipow64(E, D);
+#pragma omp parallel for schedule(dynamic)
+    for (int64_t b = 0; b < m->nblocks; ++b) {
+        double* v = u + b * 2 * NN + NN;
+        double line[16], out[16];
+        for (int64_t el = 0; el < nel; ++el) {
+            int base[3] = {0, 0, 0};
+            int64_t r = el;
+            for (int k = 0; k < D; ++k) { base[k] = (int)(r % E) * P1; r /= E; }
+            for (int d = 0; d < D; ++d) {
+                int64_t nl = ipow64(P1, D - 1);
+                for (int64_t l = 0; l < nl; ++l) {
+                    int x[3] = {base[0], base[1], base[2]};
+                    int64_t ll = l;
+                    for (int k = 0; k < D; ++k) if (k != d) { x[k] += (int)(ll % P1); ll /= P1; }
+                    for (int j = 0; j < P1; ++j) { int y[3] = {x[0], x[1], x[2]}; y[d] += j; line[j] = v[oidx(c, y)]; }
+                    for (int i = 0; i < P1; ++i) {
+                        double s = 0.0;
+                        for (int j = 0; j < P1; ++j) s += m->projector[i * P1 + j] * line[j];
+                        out[i] = s;
+                    }
+                    for (int i = 0; i < P1; ++i) { int y[3] = {x[0], x[1], x[2]}; y[d] += i; v[oidx(c, y)] = out[i]; }
+                }
+            }
+        }
+    }
+    (void)N;
+}
+
+int oracle_truncate(const oracle_mesh* m, double* u) {
+    if (!m->truncate) return 0;
+    ctx_t c;
+    c.m = m;
+    c.P1 = m->P + 1;
+    c.N = m->E * c.P1;
+    c.NN = ipow64(c.N, m->D);
+    truncate_with(&c, u);
+    return 0;
+}
+
+int oracle_rk4(const oracle_mesh* m, double* u, double dt, int nsteps) {
+    ctx_t c;
+    c.m = m;
+    c.P1 = m->P + 1;
+    c.N = m->E * c.P1;
+    c.NN = ipow64(c.N, m->D);
+    const int64_t W = 2 * c.NN * m->nblocks;
+    double* k1 = (double*)malloc(sizeof(double) * W);
+    double* k2 = (double*)malloc(sizeof(double) * W);
+    double* k3 = (double*)malloc(sizeof(double) * W);
+    double* k4 = (double*)malloc(sizeof(double) * W);
+    double* y = (double*)malloc(sizeof(double) * W);
+    if (!k1 || !k2 || !k3 || !k4 || !y) { free(k1); free(k2); free(k3); free(k4); free(y); return -1; }
+    int rc = 0;
+    for (int s = 0; s < nsteps && rc == 0; ++s) {
+        rc |= oracle_rhs(m, u, k1);
+#pragma omp parallel for
+        for (int64_t i = 0; i < W; ++i) y[i] = u[i] + dt / 2 * k1[i];
+        if (m->truncate) truncate_with(&c, y);
+        rc |= oracle_rhs(m, y, k2);
+#pragma omp parallel for
+        for (int64_t i = 0; i < W; ++i) y[i] = u[i] + dt / 2 * k2[i];
+        if (m->truncate) truncate_with(&c, y);
+        rc |= oracle_rhs(m, y, k3);
+#pragma omp parallel for
+        for (int64_t i = 0; i < W; ++i) y[i] = u[i] + dt * k3[i];
+        if (m->truncate) truncate_with(&c, y);
+        rc |= oracle_rhs(m, y, k4);
+#pragma omp parallel for
+        for (int64_t i = 0; i < W; ++i) u[i] = u[i] + dt / 6 * (k1[i] + 2 * k2[i] + 2 * k3[i] + k4[i]);
+        if (m->truncate) truncate_with(&c, u);
+    }
+    free(k1); free(k2); free(k3); free(k4); free(y);
+    return rc;
+}
+
+static double node_weight(const ctx_t* c, int b, int64_t n) {
+    const oracle_mesh* m = c->m;
+    double h = spacing(c, b), w = 1.0;
+    for (int k = 0; k < m->D; ++k) { w *= h * c->P1 / 2.0 * m->weights[(n % c->N) % c->P1]; n /= c->N; }
+    return w;
+}
+
+/* 1/2 sum w (v^2 + sum_d (D_d u)^2), summed block by block in order. */
+int oracle_energy(const oracle_mesh* m, const double* u, double* out) {
+    ctx_t c;
+    if (ctx_init(&c, m)) return -1;
+    const int D = m->D;
+    const int64_t NN = c.NN, nb = m->nblocks;
+    double* ua = (double*)malloc(sizeof(double) * NN * nb);
+    double* part = (double*)calloc(nb, sizeof(double));
+    if (!ua || !part) { free(ua); free(part); free(c.owner); return -1; }
+    for (int64_t b = 0; b < nb; ++b) memcpy(ua + b * NN, u + b * 2 * NN, sizeof(double) * NN);
+#pragma omp parallel
+    {
+        double* g = (double*)malloc(sizeof(double) * NN);
+#pragma omp for schedule(dynamic)
+        for (int64_t b = 0; b < nb; ++b) {
+            double s = 0.0;
+            const double* v = u + b * 2 * NN + NN;
+            for (int64_t n = 0; n < NN; ++n) s += node_weight(&c, (int)b, n) * v[n] * v[n];
+            for (int d = 0; d < D; ++d) {
+                derivative_block(&c, (int)b, d, ua, 1.0, g);
+                for (int64_t n = 0; n < NN; ++n) s += node_weight(&c, (int)b, n) * g[n] * g[n];
+            }
+            part[b] = 0.5 * s;
+        }
+        free(g);
+    }
+    double e = 0.0;
+    for (int64_t b = 0; b < nb; ++b) e += part[b];
+    *out = e;
+    free(ua);
+    free(part);
+    free(c.owner);
+    return 0;
+}
+
+/* Volume-normalised p-norm of u - ref (ref may be NULL); p = 0: largest |value|. */
+int oracle_norm(const oracle_mesh* m, const double* u, const double* ref, int p, int vars_mask, double* out) {
+    ctx_t c;
+    c.m = m;
+    c.P1 = m->P + 1;
+    c.N = m->E * c.P1;
+    c.NN = ipow64(c.N, m->D);
+    c.cellw = (m->hi[0] - m->lo[0]) / m->roots[0];
+    double num = 0.0, vol = 0.0;
+    for (int64_t b = 0; b < m->nblocks; ++b)
+        for (int var = 0; var < 2; ++var) {
+            if (!(vars_mask & (1 << var))) continue;
+            for (int64_t n = 0; n < c.NN; ++n) {
+                int64_t o = b * 2 * c.NN + var * c.NN + n;
+                double x = fabs(u[o] - (ref ? ref[o] : 0.0));
+                double w = node_weight(&c, (int)b, n);
+                if (p == 0) num = x > num ? x : num;
+                else num += w * pow(x, p);
+                vol += w;
+            }
+        }
+    *out = p == 0 ? num : (vol == 0 ? 0.0 : pow(num / vol, 1.0 / p));
+    return 0;
+}
+
+/* tau per element: post * max over lines in every dim and modes q of
+ * (weights[q] |sum_j duals[modes[q]][j] a_j| / peak)^pows[q]. */
+int oracle_modes(const oracle_mesh* m, const double* u, int var, int nq, const int* modes, const double* weights,
+                 const double* pows, double post, double* tau) {
+    const int D = m->D, P1 = m->P + 1, E = m->E, N = E * P1;
+    const int64_t NN = ipow64(N, D), nel = ipow64(E, D);
+    double peak = 0.0;
+    for (int64_t b = 0; b < m->nblocks; ++b)
+        for (int64_t n = 0; n < NN; ++n) {
+            double x = fabs(u[b * 2 * NN + (int64_t)var * NN + n]);
+            peak = x > peak ? x : peak;
+        }
+    double scale = peak == 0.0 ? 0.0 : 1.0 / peak;
+    for (int64_t b = 0; b < m->nblocks; ++b) {
+        const double* a = u + b * 2 * NN + (int64_t)var * NN;
+        for (int64_t el = 0; el < nel; ++el) {
+            int base[3] = {0, 0, 0};
+            int64_t r = el;
+            for (int k = 0; k < D; ++k) { base[k] = (int)(r % E) * P1; r /= E; }
+            double best = 0.0;
+            for (int d = 0; d < D; ++d) {
+                int64_t nl = ipow64(P1, D - 1);
+                for (int64_t l = 0; l < nl; ++l) {
+                    int x[3] = {base[0], base[1], base[2]};
+                    int64_t ll = l;
+                    for (int k = 0; k < D; ++k) if (k != d) { x[k] += (int)(ll % P1); ll /= P1; }
+                    for (int q = 0; q < nq; ++q) {
+                        double cq = 0.0;
+                        for (int j = 0; j < P1; ++j) {
+                            int y[3] = {x[0], x[1], x[2]};
+                            y[d] += j;
+                            int64_t o = 0, s = 1;
+                            for (int k = 0; k < D; ++k) { o += y[k] * s; s *= N; }
+                            cq += m->duals[modes[q] * P1 + j] * a[o];
+                        }
+                        double v = pow(weights[q] * scale * fabs(cq), pows[q]);
+                        best = v > best ? v : best;
+                    }
+                }
+            }
+            tau[b * nel + el] = post * best;
+        }
+    }
+    return 0;
+}
+
+int oracle_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

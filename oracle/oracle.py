@@ -1,0 +1,162 @@
+"""ctypes wrapper of the C oracle (oracle.c). Test infrastructure only.
+
+Tables come from tests/golden/element_tables.json (the mpmath restatement of
+the reference's Element), never from the library under test.
+"""
+import ctypes
+import json
+import os
+import struct
+
+import numpy as np
+
+from . import build as _build
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(os.path.dirname(HERE), "tests", "golden", "element_tables.json")
+
+
+class OracleMesh(ctypes.Structure):
+    _fields_ = [
+        ("D", ctypes.c_int), ("P", ctypes.c_int), ("E", ctypes.c_int), ("nblocks", ctypes.c_int),
+        ("truncate", ctypes.c_int), ("roots", ctypes.c_int * 3), ("periodic", ctypes.c_int * 3),
+        ("reflecting", ctypes.c_int * 3), ("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3),
+        ("level", ctypes.POINTER(ctypes.c_int32)), ("corner", ctypes.POINTER(ctypes.c_int64)),
+        ("nodes", ctypes.POINTER(ctypes.c_double)), ("weights", ctypes.POINTER(ctypes.c_double)),
+        ("stencil", ctypes.POINTER(ctypes.c_double)), ("projector", ctypes.POINTER(ctypes.c_double)),
+        ("duals", ctypes.POINTER(ctypes.c_double)),
+    ]
+
+
+_lib = None
+_tables = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(_build.build())
+        vp, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)
+        mp = ctypes.POINTER(OracleMesh)
+        L.oracle_rhs.argtypes = [mp, vp, vp]
+        L.oracle_truncate.argtypes = [mp, vp]
+        L.oracle_rk4.argtypes = [mp, vp, ctypes.c_double, ctypes.c_int]
+        L.oracle_energy.argtypes = [mp, vp, dp]
+        L.oracle_norm.argtypes = [mp, vp, vp, ctypes.c_int, ctypes.c_int, dp]
+        L.oracle_modes.argtypes = [mp, vp, ctypes.c_int, ctypes.c_int, vp, vp, vp, ctypes.c_double, vp]
+        L.oracle_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def golden_tables(P, kind="f64"):
+    """Tables of order P from the golden fixture, as float64 (or float32) arrays."""
+    global _tables
+    if _tables is None:
+        with open(GOLDEN) as f:
+            _tables = json.load(f)
+    raw = _tables["orders"][str(P)][kind]
+    out = {}
+    for k, v in raw.items():
+        if kind == "f64":
+            conv = lambda b: struct.unpack("<d", struct.pack("<Q", b))[0]
+        else:
+            conv = lambda b: struct.unpack("<f", struct.pack("<I", b))[0]
+        a = np.array([[conv(x) for x in row] for row in v] if isinstance(v[0], list) else [conv(x) for x in v])
+        out[k] = a.astype(np.float64 if kind == "f64" else np.float32)
+    return out
+
+
+class Oracle:
+    """The oracle over one forest (a twoldg Forest-like object with D, roots,
+    N, lo, hi, periodic, reflecting and leaves), in FP64."""
+
+    def __init__(self, forest, P, truncate=True):
+        self.forest = forest
+        self.P = P
+        self.D = forest.D
+        self.N = forest.N
+        self.E = forest.N // (P + 1)
+        self.NN = self.N ** self.D
+        self.nblocks = len(forest.leaves)
+        t = golden_tables(P)
+        self.tables = t
+        self._arrays = dict(
+            level=np.array([lv for lv, _ in forest.leaves], dtype=np.int32),
+            corner=np.array([c for _, c in forest.leaves], dtype=np.int64).reshape(-1),
+            nodes=np.ascontiguousarray(t["nodes"]), weights=np.ascontiguousarray(t["weights"]),
+            stencil=np.ascontiguousarray(t["stencil"]).reshape(-1),
+            projector=np.ascontiguousarray(t["truncate"]).reshape(-1),
+            duals=np.ascontiguousarray(t["duals"]).reshape(-1))
+        m = OracleMesh()
+        m.D, m.P, m.E, m.nblocks, m.truncate = self.D, P, self.E, self.nblocks, 1 if truncate else 0
+        for k in range(3):
+            m.roots[k] = forest.roots[k] if k < self.D else 1
+            m.periodic[k] = int(forest.periodic[k]) if k < self.D else 1
+            m.reflecting[k] = int(forest.reflecting[k]) if k < self.D else 0
+            m.lo[k] = forest.lo[k] if k < self.D else 0.0
+            m.hi[k] = forest.hi[k] if k < self.D else 1.0
+        a = self._arrays
+        m.level = a["level"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        m.corner = a["corner"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        for k in ("nodes", "weights", "stencil", "projector", "duals"):
+            setattr(m, k, a[k].ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        self.mesh = m
+
+    def _vec(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        if u.size != 2 * self.NN * self.nblocks:
+            raise ValueError("state size %d != %d" % (u.size, 2 * self.NN * self.nblocks))
+        return u
+
+    def rhs(self, u):
+        u = self._vec(u)
+        du = np.zeros_like(u)
+        if lib().oracle_rhs(ctypes.byref(self.mesh), u.ctypes.data, du.ctypes.data):
+            raise MemoryError("oracle_rhs failed")
+        return du
+
+    def truncate(self, u):
+        u = self._vec(u).copy()
+        lib().oracle_truncate(ctypes.byref(self.mesh), u.ctypes.data)
+        return u
+
+    def rk4(self, u, dt, nsteps):
+        u = self._vec(u).copy()
+        if lib().oracle_rk4(ctypes.byref(self.mesh), u.ctypes.data, float(dt), int(nsteps)):
+            raise MemoryError("oracle_rk4 failed")
+        return u
+
+    def energy(self, u):
+        u = self._vec(u)
+        e = ctypes.c_double()
+        lib().oracle_energy(ctypes.byref(self.mesh), u.ctypes.data, ctypes.byref(e))
+        return e.value
+
+    def norm(self, u, p=2, vars_mask=3, ref=None):
+        u = self._vec(u)
+        r = None if ref is None else self._vec(ref)
+        out = ctypes.c_double()
+        lib().oracle_norm(ctypes.byref(self.mesh), u.ctypes.data, None if r is None else r.ctypes.data,
+                          int(p), int(vars_mask), ctypes.byref(out))
+        return out.value
+
+    def modes(self, u, var, modes, weights, pows, post):
+        u = self._vec(u)
+        nq = len(modes)
+        mo = np.array(modes, dtype=np.int32)
+        w = np.array(weights, dtype=np.float64)
+        pw = np.array(pows, dtype=np.float64)
+        tau = np.zeros(self.nblocks * self.E ** self.D)
+        lib().oracle_modes(ctypes.byref(self.mesh), u.ctypes.data, int(var), nq, mo.ctypes.data, w.ctypes.data,
+                           pw.ctypes.data, float(post), tau.ctypes.data)
+        return tau
+
+    def modal_indicator(self, u, mode, var=1):
+        df = lambda m: float(np.prod(np.arange(1, 2 * m, 2))) if m > 0 else 1.0
+        modes = list(range(1, mode + 1))
+        return self.modes(u, var - 1, modes, [df(m) for m in modes], [mode / m for m in modes], 1.0 / df(mode))
+
+
+def threads():
+    return lib().oracle_threads()

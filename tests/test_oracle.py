@@ -1,0 +1,197 @@
+"""The oracle pinned: against the reference's dense-matrix reference
+(test/reference.jl via tests/dense.py), its property tests and its published
+convergence numbers. No GPU."""
+import math
+
+import numpy as np
+import pytest
+
+from cases import refined_forest, scrambled, state_from, smooth_data
+from dense import along, from_global, global_array, global_operators
+from oracle.oracle import Oracle, golden_tables
+from oracle_drivers import oracle_errors
+from twoldg.forest import wave_forest
+
+
+@pytest.mark.parametrize("D,P,E,roots", [(1, 3, 2, 3), (2, 2, 2, 3), (2, 3, 2, 2), (3, 1, 2, 3)])
+def test_rhs_is_the_global_operator(D, P, E, roots):
+    # test/evolution_tests.jl:22-59: du_u = v and du_v = sum_d along(Dm,d)^2 U to 1e-12
+    forest = wave_forest(np.float64, D, P, E, roots=roots)
+    o = Oracle(forest, P)
+    u = state_from(forest, P, smooth_data(D))
+    du = o.rhs(u)
+    t = golden_tables(P)
+    Dm, _, _ = global_operators(t["stencil"], t["truncate"], t["weights"], P, roots * E, forest.minimum_spacing())
+    lap = sum(along(Dm, d, D) @ along(Dm, d, D) for d in range(D))
+    U, V = global_array(forest, u, 0), global_array(forest, u, 1)
+    assert np.array_equal(global_array(forest, du, 0), V)
+    ref = lap @ U
+    assert np.abs(global_array(forest, du, 1) - ref).max() < 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("D,P,E,roots", [(1, 3, 2, 2), (2, 2, 2, 2), (2, 4, 2, 1), (3, 3, 2, 1)])
+def test_truncation_is_the_tensor_projector(D, P, E, roots):
+    # test/evolution_tests.jl:83-103
+    forest = wave_forest(np.float64, D, P, E, roots=roots)
+    o = Oracle(forest, P)
+    u = state_from(forest, P, smooth_data(D))
+    w = o.truncate(u)
+    t = golden_tables(P)
+    _, Pim, _ = global_operators(t["stencil"], t["truncate"], t["weights"], P, roots * E, 1.0)
+    Pi = Pim
+    for _ in range(D - 1):
+        Pi = np.kron(Pi, Pim)
+    V = global_array(forest, u, 1)
+    assert np.abs(global_array(forest, w, 1) - Pi @ V).max() < 1e-13 * np.abs(V).max()
+    assert np.array_equal(global_array(forest, w, 0), global_array(forest, u, 0))
+    assert np.abs(o.truncate(w) - w).max() < 1e-14 * np.abs(V).max()
+
+
+def test_rhs_neither_writes_u_nor_remembers():
+    # test/evolution_tests.jl:61-75
+    forest = wave_forest(np.float64, 2, 2, 2, roots=2)
+    o = Oracle(forest, 2)
+    u = state_from(forest, 2, smooth_data(2))
+    u0 = u.copy()
+    a = o.rhs(u)
+    o.rhs(2 * u)
+    b = o.rhs(u)
+    assert np.array_equal(u, u0) and np.array_equal(a, b)
+
+
+def _weights(o, forest, P):
+    t = golden_tables(P)
+    N, D = forest.N, forest.D
+    P1 = P + 1
+    out = []
+    for key in forest.leaves:
+        h = forest.spacing(key)
+        w1 = h * P1 / 2 * t["weights"][np.arange(N) % P1]
+        w = np.ones(1)
+        for _ in range(D):
+            w = np.kron(w1, w)
+        out.append(w)
+    return np.array(out)
+
+
+def _skew_residual(o, forest, P, a_u, b_u):
+    """<b, Lap a>_w - <Lap b, a>_w relative: the Laplacian's self-adjointness,
+    which is what makes the energy invariant (test/refined_tests.jl:82-143)."""
+    nb = len(forest.leaves)
+    NN = forest.N ** forest.D
+    def lap(x):
+        s = np.zeros((nb, 2, NN))
+        s[:, 0] = x
+        return o.rhs(s.reshape(-1)).reshape(nb, 2, NN)[:, 1]
+    w = _weights(o, forest, P)
+    la, lb = lap(a_u), lap(b_u)
+    lhs = np.sum(w * b_u * la)
+    rhs = np.sum(w * lb * a_u)
+    return abs(lhs - rhs) / (np.sum(np.abs(w * b_u * la)) + np.sum(np.abs(w * lb * a_u)))
+
+
+@pytest.mark.parametrize("D,P,reflecting", [(1, 3, False), (2, 2, False), (2, 3, True), (3, 2, False),
+                                            (3, 1, True)])
+def test_refined_laplacian_is_self_adjoint(D, P, reflecting):
+    # A coarse ghost that is not the adjoint of the fine one breaks this;
+    # measured residual ~1e-18 relative in the reference (CODE.md "The energy").
+    forest = refined_forest(D, P, reflecting)
+    assert len({lv for lv, _ in forest.leaves}) == 2
+    o = Oracle(forest, P)
+    n = len(forest.leaves) * forest.N ** D
+    a = scrambled(n, 0.1).reshape(len(forest.leaves), -1)
+    b = scrambled(n, 0.37).reshape(len(forest.leaves), -1)
+    assert _skew_residual(o, forest, P, a, b) < 1e-13
+
+
+@pytest.mark.parametrize("D,P", [(2, 3), (3, 3)])
+def test_refined_exact_to_degree_P_along_and_P_minus_1_across(D, P):
+    # test/refined_tests.jl:163-210 in the form the RHS exposes: the coarse
+    # ghost R is exact to degree P-1 tangentially (not P), so on a two-level
+    # forest the Laplacian is exact for data of degree P-1 in every dimension,
+    # and not for degree P across a coarse-fine face. Checked on the blocks
+    # around the refined middle, away from the periodic box's faces where a
+    # polynomial is not periodic.
+    forest = refined_forest(D, P)
+    o = Oracle(forest, P)
+    from cases import node_positions
+    x = node_positions(forest, P)
+    nb = len(forest.leaves)
+    inner = [b for b, (lv, c) in enumerate(forest.leaves)
+             if all(0.3 < (lo + hi) / 2 < 0.7 for lo, hi in forest.block_extent((lv, c)))]
+    assert inner
+    u = np.zeros((nb, 2, forest.N ** D))
+    u[:, 0] = sum((x[:, k] - 0.5) ** 2 for k in range(D))
+    du = o.rhs(u.reshape(-1)).reshape(nb, 2, -1)[:, 1]
+    assert np.abs(du[inner] - 2.0 * D).max() < 1e-9
+    # degree P tangentially is not reproduced by the coarse ghosts
+    u[:, 0] = (x[:, 0] - 0.5) ** P
+    du = o.rhs(u.reshape(-1)).reshape(nb, 2, -1)[:, 1]
+    assert np.abs(du - P * (P - 1) * (x[:, 0] - 0.5) ** (P - 2))[inner].max() > 1e-6
+
+
+def test_reflecting_wall_mirrors_with_parity():
+    # On a reflecting box the Neumann cos mode's u has zero normal gradient at
+    # the wall; the RHS of a field even about every wall is the global
+    # operator of the box mirrored into a periodic box of twice the side.
+    D, P, E, roots = 2, 3, 2, 2
+    fr = wave_forest(np.float64, D, P, E, roots=roots, reflecting=True)
+    fp = wave_forest(np.float64, D, P, E, roots=2 * roots, L=2.0)
+    orf, op = Oracle(fr, P), Oracle(fp, P)
+    f = lambda x, var: np.cos(math.pi * x[0]) * np.cos(2 * math.pi * x[1]) + 0.3 * np.cos(3 * math.pi * x[0]) * var
+    ur = state_from(fr, P, f)
+    # the mirrored field on [0,2)^2 with nodes mirrored as well: build it from the
+    # reflecting box's global array by reflection of node order
+    n = roots * fr.N
+    Ur = global_array(fr, ur, 0).reshape(n, n, order="F")
+    Vr = global_array(fr, ur, 1).reshape(n, n, order="F")
+    mirror = lambda A: np.block([[A, A[::-1, :]], [A[:, ::-1], A[::-1, ::-1]]]).T.T
+    def mir(A):
+        top = np.concatenate([A, A[::-1, :]], axis=0)
+        return np.concatenate([top, top[:, ::-1]], axis=1)
+    up = np.zeros(2 * len(fp.leaves) * fp.N ** D)
+    from_global(fp, mir(Ur).reshape(-1, order="F"), up, 0)
+    from_global(fp, mir(Vr).reshape(-1, order="F"), up, 1)
+    dr = global_array(fr, orf.rhs(ur), 1).reshape(n, n, order="F")
+    dp = global_array(fp, op.rhs(up), 1).reshape(2 * n, 2 * n, order="F")
+    assert np.abs(dr - dp[:n, :n]).max() < 1e-10 * np.abs(dp).max()
+    del mirror
+
+
+@pytest.mark.parametrize("D,P,row", [
+    (1, 3, (1.48e-2, 1.70e-3, 2.08e-4, 9.37e-2, 1.15e-2, 1.29e-3)),
+    (2, 3, (1.47e-2, 1.71e-3, 2.08e-4, 1.43e-1, 1.55e-2, 1.87e-3)),
+    (2, 4, (1.46e-3, 1.02e-4, 6.61e-6, 1.20e-2, 9.31e-4, 6.38e-5)),
+])
+def test_convergence_table(D, P, row):
+    # reference CODE.md:4124-4145 (truncated, E = 2, roots 2/4/8, cfl 1/2,
+    # quarter period): the published L2 errors of u and v, to the 3 digits printed
+    for i, roots in enumerate((2, 4, 8)):
+        r = oracle_errors(D, P, 2, roots)
+        assert r["eu"] == pytest.approx(row[i], rel=0.006), (roots, r["eu"])
+        assert r["ev"] == pytest.approx(row[3 + i], rel=0.006), (roots, r["ev"])
+
+
+def test_reflecting_convergence_table():
+    # reference CODE.md:4160-4169: D = 1, P = 3 reflecting, l2 4.23e-3 4.81e-4 6.0e-5
+    for roots, ref in zip((2, 4, 8), (4.23e-3, 4.81e-4, 6.0e-5)):
+        r = oracle_errors(1, 3, 2, roots, reflecting=True)
+        assert r["l2"] == pytest.approx(ref, rel=0.01)
+        assert r["energy"] <= r["energy0"]
+
+
+def test_energy_lost_at_rk4_rate():
+    # test/evolution_tests.jl:172-195
+    for D, P, truncate in ((1, 3, True), (2, 2, True), (2, 3, False)):
+        forest = wave_forest(np.float64, D, P, 2, roots=2)
+        o = Oracle(forest, P, truncate=truncate)
+        u0 = o.truncate(state_from(forest, P, smooth_data(D)))
+        losses = []
+        for cfl in (1.0, 0.5):
+            dt = cfl * forest.minimum_spacing() / (P + 1)
+            u = o.rk4(u0, dt, 200)
+            E0, E1 = o.energy(u0), o.energy(u)
+            assert E1 <= E0
+            losses.append((E0 - E1) / E0)
+        assert 0 < losses[1] < losses[0]
+        assert losses[0] / losses[1] > 2 ** 5

@@ -1,0 +1,534 @@
+// The C ABI (include/twoldg.h): problem and batch objects over the kernels.
+//
+// A "runner" holds one or more groups of blocks that share (D, P, E,
+// truncate), each group one work list for the templated kernels; a single
+// problem is a runner with one group, a batch a runner with one group per
+// distinct shape. One RK4 step is 4 x [coarse-fine ghosts (if any) ->
+// fused stage] per group, captured once in a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/twoldg.h"
+#include "mesh.h"
+#include "ops.h"
+#include "tables.h"
+
+using namespace twoldg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(TWOLDG_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                         \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+struct TableCache {
+    ElementTables<double> t64[kMaxP + 1];
+    ElementTables<float> t32[kMaxP + 1];
+    bool built[kMaxP + 1] = {};
+    bool get(int P) {
+        if (P < 1 || P > kMaxP) return false;
+        if (!built[P]) built[P] = build_tables(P, t64[P], t32[P]);
+        return built[P];
+    }
+};
+
+TableCache& tables() {
+    static TableCache c;
+    return c;
+}
+
+struct DevBuf {
+    void* p = nullptr;
+    ~DevBuf() { if (p) cudaFree(p); }
+    cudaError_t alloc(size_t bytes) {
+        if (p) { cudaFree(p); p = nullptr; }
+        if (bytes == 0) bytes = 16;
+        return cudaMalloc(&p, bytes);
+    }
+};
+
+struct Group {
+    int D = 0, P = 0, E = 0, truncate = 1;
+    int64_t NN = 0, F = 1;
+    std::vector<BlockItem> items;
+    std::vector<CfFace> cf;
+    std::vector<double> h;
+    std::unique_ptr<Ops> ops;
+    DevBuf d_items, d_cf, fu[2], fog[2], ugd, gfd, ggd, d_part, d_part2;
+    int nslots() const { return (int)items.size() * 2 * D; }
+};
+
+}  // namespace
+
+struct twoldg_runner {
+    int prec = 0;
+    size_t wsize = 8;
+    int nproblems = 0;
+    int64_t total_words = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<std::unique_ptr<Group>> groups;
+    std::vector<int64_t> offsets;   // per problem, words
+    std::vector<double> hmin;       // per problem
+    DevBuf y, acc, comp, d_dts;
+    std::vector<double> h_dts;
+    cudaGraphExec_t gexec = nullptr;
+    void* graph_u = nullptr;
+    void* comp_u = nullptr;
+
+    ~twoldg_runner() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    int setup(int n, const twoldg_desc* descs) {
+        if (n < 1 || !descs) return fail(TWOLDG_EINVAL, "no problem descriptors");
+        prec = descs[0].precision;
+        if (prec != TWOLDG_F64 && prec != TWOLDG_F32 && prec != TWOLDG_F32C)
+            return fail(TWOLDG_EINVAL, "precision must be TWOLDG_F64, TWOLDG_F32 or TWOLDG_F32C");
+        wsize = prec == TWOLDG_F64 ? 8 : 4;
+        nproblems = n;
+        std::map<std::tuple<int, int, int, int>, int> gidx;
+        for (int k = 0; k < n; ++k) {
+            const twoldg_desc& d = descs[k];
+            if (d.precision != prec) return fail(TWOLDG_EINVAL, "all members of a batch must share one precision");
+            Mesh m;
+            std::string err;
+            if (!build_mesh(d, m, err)) return fail(TWOLDG_EINVAL, err);
+            if (!tables().get(m.P))
+                return fail(TWOLDG_EUNSUP, "element order P = " + std::to_string(m.P) + " is not built (1..6)");
+            auto key = std::make_tuple(m.D, m.P, m.E, d.truncate ? 1 : 0);
+            auto gi = gidx.find(key);
+            Group* g;
+            if (gi == gidx.end()) {
+                gidx[key] = (int)groups.size();
+                groups.emplace_back(new Group());
+                g = groups.back().get();
+                g->D = m.D; g->P = m.P; g->E = m.E; g->truncate = d.truncate ? 1 : 0;
+                g->NN = m.NN;
+                for (int q = 0; q < m.D - 1; ++q) g->F *= m.N;
+                Ops* ops = nullptr;
+                if (m.D == 1) ops = make_ops_d1(prec, m.P, tables().t64[m.P], tables().t32[m.P]);
+                if (m.D == 2) ops = make_ops_d2(prec, m.P, tables().t64[m.P], tables().t32[m.P]);
+                if (m.D == 3) ops = make_ops_d3(prec, m.P, tables().t64[m.P], tables().t32[m.P]);
+                if (!ops) return fail(TWOLDG_EUNSUP, "no kernels for P = " + std::to_string(m.P) + " (built: 1..6)");
+                g->ops.reset(ops);
+            } else {
+                g = groups[gi->second].get();
+            }
+            const int64_t base = total_words;
+            const int slot0 = g->nslots();
+            for (auto it : m.items) {
+                it.off += base;
+                it.slot += slot0;
+                for (int f = 0; f < 6; ++f)
+                    if (it.nb[f] >= 0) it.nb[f] += slot0;
+                it.problem = k;
+                g->items.push_back(it);
+            }
+            for (auto c : m.cf) {
+                c.slot += slot0;
+                for (int q = 0; q < 4; ++q) c.src[q] += slot0;
+                g->cf.push_back(c);
+            }
+            g->h.insert(g->h.end(), m.h.begin(), m.h.end());
+            offsets.push_back(base);
+            hmin.push_back(m.hmin);
+            total_words += 2 * m.NN * m.nblocks;
+        }
+        for (auto& gp : groups) {
+            Group& g = *gp;
+            if (g.ops->stage_smem(g.E) > 227 * 1024)
+                return fail(TWOLDG_EUNSUP, "block of N = " + std::to_string(g.E * (g.P + 1)) + " nodes per dim in " +
+                                               std::to_string(g.D) + "D does not fit one CTA's shared memory");
+        }
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        for (auto& gp : groups) {
+            Group& g = *gp;
+            size_t fbytes = (size_t)g.nslots() * g.F * wsize;
+            CK(g.d_items.alloc(g.items.size() * sizeof(BlockItem)));
+            CK(cudaMemcpy(g.d_items.p, g.items.data(), g.items.size() * sizeof(BlockItem), cudaMemcpyHostToDevice));
+            CK(g.d_cf.alloc(g.cf.size() * sizeof(CfFace)));
+            if (!g.cf.empty())
+                CK(cudaMemcpy(g.d_cf.p, g.cf.data(), g.cf.size() * sizeof(CfFace), cudaMemcpyHostToDevice));
+            for (int i = 0; i < 2; ++i) {
+                CK(g.fu[i].alloc(fbytes));
+                CK(g.fog[i].alloc(fbytes));
+                CK(cudaMemset(g.fu[i].p, 0, fbytes));
+                CK(cudaMemset(g.fog[i].p, 0, fbytes));
+            }
+            size_t dbytes = g.cf.empty() ? 16 : fbytes;
+            CK(g.ugd.alloc(dbytes));
+            CK(g.gfd.alloc(dbytes));
+            CK(g.ggd.alloc(dbytes));
+            CK(g.d_part.alloc(g.items.size() * sizeof(double)));
+            CK(g.d_part2.alloc(g.items.size() * sizeof(double)));
+        }
+        size_t sbytes = (size_t)total_words * wsize;
+        if (y.alloc(sbytes) != cudaSuccess || acc.alloc(sbytes) != cudaSuccess)
+            return fail(TWOLDG_ENOMEM, "stage scratch allocation failed");
+        if (prec == TWOLDG_F32C) {
+            if (comp.alloc(sbytes) != cudaSuccess) return fail(TWOLDG_ENOMEM, "compensation allocation failed");
+            CK(cudaMemset(comp.p, 0, sbytes));
+        }
+        CK(d_dts.alloc(n * sizeof(double)));
+        h_dts.assign(n, 0.0);
+        CK(cudaMemcpy(d_dts.p, h_dts.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+        return TWOLDG_OK;
+    }
+
+    StagePtrs ptrs(Group& g, void* u, int in) {
+        StagePtrs p{};
+        p.u = u;
+        p.y = y.p;
+        p.acc = acc.p;
+        p.comp = comp.p;
+        p.du = nullptr;
+        p.fu_in = g.fu[in].p;
+        p.fog_in = g.fog[in].p;
+        p.fu_out = g.fu[1 - in].p;
+        p.fog_out = g.fog[1 - in].p;
+        p.ugd = g.ugd.p;
+        p.ggd = g.ggd.p;
+        p.dts = (const double*)d_dts.p;
+        p.partial = (double*)g.d_part.p;
+        return p;
+    }
+
+    int export_all(const void* u) {
+        for (auto& gp : groups) {
+            Group& g = *gp;
+            CK(g.ops->export_faces((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, u, g.fu[0].p,
+                                   g.fog[0].p, stream));
+        }
+        return TWOLDG_OK;
+    }
+
+    int cf_all(Group& g, int in) {
+        if (g.cf.empty()) return TWOLDG_OK;
+        CK(g.ops->cf_ghosts((const CfFace*)g.d_cf.p, (int)g.cf.size(), g.E, g.fu[in].p, g.fog[in].p, g.ugd.p,
+                            g.gfd.p, g.ggd.p, stream));
+        return TWOLDG_OK;
+    }
+
+    // One RK4 step, enqueued on `stream` (captured into the graph).
+    int enqueue_step(void* u) {
+        int in = 0;
+        for (int s = 1; s <= 4; ++s) {
+            for (auto& gp : groups) {
+                Group& g = *gp;
+                int r = cf_all(g, in);
+                if (r) return r;
+                StagePtrs p = ptrs(g, u, in);
+                CK(g.ops->stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, p, 0,
+                                stream));
+            }
+            in = 1 - in;
+        }
+        return TWOLDG_OK;
+    }
+
+    int rk4(void* u, const double* dts, int nsteps) {
+        if (!u) return fail(TWOLDG_EINVAL, "u is NULL");
+        if (nsteps < 0) return fail(TWOLDG_EINVAL, "nsteps is negative");
+        bool changed = false;
+        for (int k = 0; k < nproblems; ++k) {
+            if (!(dts[k] > 0) || !std::isfinite(dts[k])) return fail(TWOLDG_EINVAL, "dt must be positive and finite");
+            if (dts[k] != h_dts[k]) changed = true;
+        }
+        if (changed) {
+            std::copy(dts, dts + nproblems, h_dts.begin());
+            CK(cudaMemcpyAsync(d_dts.p, h_dts.data(), nproblems * sizeof(double), cudaMemcpyHostToDevice, stream));
+            CK(cudaStreamSynchronize(stream));
+        }
+        if (prec == TWOLDG_F32C && comp_u != u) {
+            CK(cudaMemsetAsync(comp.p, 0, (size_t)total_words * wsize, stream));
+            comp_u = u;
+        }
+        if (nsteps == 0) return TWOLDG_OK;
+        int r = export_all(u);
+        if (r) return r;
+        if (!gexec || graph_u != u) {
+            if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+            cudaGraph_t graph;
+            CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            r = enqueue_step(u);
+            cudaError_t e = cudaStreamEndCapture(stream, &graph);
+            if (r) { if (e == cudaSuccess) cudaGraphDestroy(graph); return r; }
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&gexec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) { gexec = nullptr; return cuda_fail(e, "cudaGraphInstantiate"); }
+            graph_u = u;
+        }
+        for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(gexec, stream));
+        CK(cudaGetLastError());
+        return TWOLDG_OK;
+    }
+};
+
+struct twoldg_problem : twoldg_runner {
+    int D = 0, P = 0, E = 0;
+    int truncate = 1;
+};
+
+struct twoldg_batch : twoldg_runner {};
+
+extern "C" {
+
+const char* twoldg_last_error(void) { return g_err.c_str(); }
+const char* twoldg_version(void) { return "twoldg 0.1 (sm_103a)"; }
+
+int twoldg_element_tables(int32_t order, int32_t precision, const char* name, void* out) {
+    if (!name || !out) return fail(TWOLDG_EINVAL, "name and out must not be NULL");
+    if (!tables().get(order)) return fail(TWOLDG_EINVAL, "order P must be 1.." + std::to_string(kMaxP));
+    auto pickv = [&](auto& t) -> const void* {
+        using V = typename std::decay_t<decltype(t.nodes)>;
+        static_assert(sizeof(V) > 0, "");
+        std::string n(name);
+        const auto* v = &t.nodes;
+        if (n == "nodes") v = &t.nodes;
+        else if (n == "weights") v = &t.weights;
+        else if (n == "offsets") v = &t.offsets;
+        else if (n == "stencil") v = &t.stencil;
+        else if (n == "truncate") v = &t.truncate;
+        else if (n == "topmode") v = &t.topmode;
+        else if (n == "topdual") v = &t.topdual;
+        else if (n == "duals") v = &t.duals;
+        else if (n == "prolong") v = &t.prolong;
+        else if (n == "restrict") v = &t.restrict_;
+        else return nullptr;
+        std::memcpy(out, v->data(), v->size() * sizeof((*v)[0]));
+        return out;
+    };
+    const void* r = precision == 0 ? pickv(tables().t64[order]) : pickv(tables().t32[order]);
+    if (!r) return fail(TWOLDG_EINVAL, std::string("unknown table ") + name);
+    return TWOLDG_OK;
+}
+
+int twoldg_problem_create(const twoldg_desc* desc, twoldg_problem** out) {
+    if (!desc || !out) return fail(TWOLDG_EINVAL, "desc and out must not be NULL");
+    *out = nullptr;
+    std::unique_ptr<twoldg_problem> p(new twoldg_problem());
+    int r = p->setup(1, desc);
+    if (r) return r;
+    p->D = desc->dim;
+    p->P = desc->order;
+    p->E = desc->elems;
+    p->truncate = desc->truncate ? 1 : 0;
+    *out = p.release();
+    return TWOLDG_OK;
+}
+
+int twoldg_problem_destroy(twoldg_problem* p) {
+    if (p) {
+        cudaStreamSynchronize(p->stream);
+        delete p;
+    }
+    return TWOLDG_OK;
+}
+
+int twoldg_state_words(const twoldg_problem* p, int64_t* words) {
+    if (!p || !words) return fail(TWOLDG_EINVAL, "NULL argument");
+    *words = p->total_words;
+    return TWOLDG_OK;
+}
+
+int twoldg_min_spacing(const twoldg_problem* p, double* h) {
+    if (!p || !h) return fail(TWOLDG_EINVAL, "NULL argument");
+    *h = p->hmin[0];
+    return TWOLDG_OK;
+}
+
+int twoldg_rhs(twoldg_problem* p, void* du, const void* u, double t) {
+    (void)t;
+    if (!p || !du || !u) return fail(TWOLDG_EINVAL, "NULL argument");
+    if (du == u) return fail(TWOLDG_EINVAL, "du and u must not alias: the right-hand side never writes u");
+    int r = p->export_all(u);
+    if (r) return r;
+    Group& g = *p->groups[0];
+    r = p->cf_all(g, 0);
+    if (r) return r;
+    StagePtrs s = p->ptrs(g, const_cast<void*>(u), 0);
+    s.du = du;
+    CK(g.ops->stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, 0, 0, s, 0, p->stream));
+    return TWOLDG_OK;
+}
+
+int twoldg_truncate(twoldg_problem* p, void* u) {
+    if (!p || !u) return fail(TWOLDG_EINVAL, "NULL argument");
+    Group& g = *p->groups[0];
+    if (!g.truncate) return TWOLDG_OK;
+    CK(g.ops->truncate((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, u, p->stream));
+    return TWOLDG_OK;
+}
+
+int twoldg_rk4_step(twoldg_problem* p, void* u, double t, double dt, int32_t nsteps) {
+    (void)t;
+    if (!p) return fail(TWOLDG_EINVAL, "NULL problem");
+    return p->rk4(u, &dt, nsteps);
+}
+
+int twoldg_reset_compensation(twoldg_problem* p) {
+    if (!p) return fail(TWOLDG_EINVAL, "NULL problem");
+    if (p->comp.p) CK(cudaMemsetAsync(p->comp.p, 0, (size_t)p->total_words * p->wsize, p->stream));
+    return TWOLDG_OK;
+}
+
+int twoldg_energy(twoldg_problem* p, const void* u, double t, double* energy) {
+    (void)t;
+    if (!p || !u || !energy) return fail(TWOLDG_EINVAL, "NULL argument");
+    int r = p->export_all(u);
+    if (r) return r;
+    Group& g = *p->groups[0];
+    r = p->cf_all(g, 0);
+    if (r) return r;
+    StagePtrs s = p->ptrs(g, const_cast<void*>(u), 0);
+    CK(g.ops->energy((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, p->stream));
+    std::vector<double> part(g.items.size());
+    CK(cudaMemcpyAsync(part.data(), g.d_part.p, part.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    double e = 0;
+    for (double x : part) e += x;
+    *energy = e;
+    return TWOLDG_OK;
+}
+
+int twoldg_norm(twoldg_problem* p, const void* u, const void* ref, int32_t pnorm, int32_t vars_mask, double* out) {
+    if (!p || !u || !out) return fail(TWOLDG_EINVAL, "NULL argument");
+    if (pnorm < 0) return fail(TWOLDG_EINVAL, "the norm takes an integer p >= 1, or 0 for the largest value");
+    if (vars_mask < 1 || vars_mask > 3) return fail(TWOLDG_EINVAL, "vars_mask must select u (1), v (2) or both (3)");
+    Group& g = *p->groups[0];
+    CK(g.ops->norm((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, u, ref, pnorm, vars_mask,
+                   (double*)g.d_part.p, (double*)g.d_part2.p, p->stream));
+    std::vector<double> num(g.items.size()), vol(g.items.size());
+    CK(cudaMemcpyAsync(num.data(), g.d_part.p, num.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaMemcpyAsync(vol.data(), g.d_part2.p, vol.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    if (pnorm == 0) {
+        double m = 0;
+        for (double x : num) m = std::fmax(m, x);
+        *out = m;
+        return TWOLDG_OK;
+    }
+    double a = 0, v = 0;
+    for (size_t i = 0; i < num.size(); ++i) { a += num[i]; v += vol[i]; }
+    *out = v == 0 ? 0.0 : std::pow(a / v, 1.0 / pnorm);
+    return TWOLDG_OK;
+}
+
+static int indicator(twoldg_problem* p, const void* u, int var, int nq, const int* modes, const double* weights,
+                     const double* pows, double post, void* tau) {
+    if (!p || !u || !tau) return fail(TWOLDG_EINVAL, "NULL argument");
+    if (var != 1 && var != 2) return fail(TWOLDG_EINVAL, "var must be 1 (u) or 2 (v)");
+    Group& g = *p->groups[0];
+    CK(g.ops->maxabs((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, u, var - 1, (double*)g.d_part.p,
+                     p->stream));
+    std::vector<double> part(g.items.size());
+    CK(cudaMemcpyAsync(part.data(), g.d_part.p, part.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    double peak = 0;
+    for (double x : part) peak = std::fmax(peak, x);
+    // A field that vanishes everywhere scores zero rather than NaN (src/refinement.jl:88-90).
+    double scale = peak == 0 ? 0.0 : 1.0 / peak;
+    std::vector<double> w(nq);
+    for (int q = 0; q < nq; ++q) w[q] = weights[q] * scale;
+    CK(g.ops->modes((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, u, var - 1, nq, modes, w.data(), pows,
+                    post, tau, p->stream));
+    return TWOLDG_OK;
+}
+
+static double doublefactorial(int m) {
+    double r = 1;
+    for (int k = 1; k <= 2 * m - 1; k += 2) r *= k;
+    return r;
+}
+
+int twoldg_modal_indicator(twoldg_problem* p, const void* u, int32_t var, int32_t mode, void* tau_dev) {
+    if (!p) return fail(TWOLDG_EINVAL, "NULL problem");
+    // check_mode: mode 0 says nothing about resolution; the truncated scheme's last moving mode is P-1
+    if (mode < 1 || mode > p->P)
+        return fail(TWOLDG_EINVAL, "mode = " + std::to_string(mode) + " must be one of 1 .. P = " + std::to_string(p->P));
+    std::vector<int> modes(mode);
+    std::vector<double> weights(mode), pows(mode);
+    for (int m = 1; m <= mode; ++m) {
+        modes[m - 1] = m;
+        weights[m - 1] = doublefactorial(m);
+        pows[m - 1] = (double)mode / m;
+    }
+    return indicator(p, u, var, mode, modes.data(), weights.data(), pows.data(), 1.0 / doublefactorial(mode), tau_dev);
+}
+
+int twoldg_mode_amplitude(twoldg_problem* p, const void* u, int32_t var, int32_t mode, void* tau_dev) {
+    if (!p) return fail(TWOLDG_EINVAL, "NULL problem");
+    if (mode < 0 || mode > p->P)
+        return fail(TWOLDG_EINVAL, "mode = " + std::to_string(mode) + " is not a Legendre mode of an element of order P = " +
+                                       std::to_string(p->P));
+    int m = mode;
+    double w = 1, pw = 1;
+    return indicator(p, u, var, 1, &m, &w, &pw, 1.0, tau_dev);
+}
+
+int twoldg_synchronize(twoldg_problem* p) {
+    if (!p) return fail(TWOLDG_EINVAL, "NULL problem");
+    CK(cudaStreamSynchronize(p->stream));
+    return TWOLDG_OK;
+}
+
+int twoldg_batch_create(int32_t n, const twoldg_desc* descs, twoldg_batch** out) {
+    if (!out) return fail(TWOLDG_EINVAL, "out must not be NULL");
+    *out = nullptr;
+    std::unique_ptr<twoldg_batch> b(new twoldg_batch());
+    int r = b->setup(n, descs);
+    if (r) return r;
+    *out = b.release();
+    return TWOLDG_OK;
+}
+
+int twoldg_batch_destroy(twoldg_batch* b) {
+    if (b) {
+        cudaStreamSynchronize(b->stream);
+        delete b;
+    }
+    return TWOLDG_OK;
+}
+
+int twoldg_batch_offsets(const twoldg_batch* b, int64_t* offsets, int64_t* total_words) {
+    if (!b) return fail(TWOLDG_EINVAL, "NULL batch");
+    if (offsets) std::copy(b->offsets.begin(), b->offsets.end(), offsets);
+    if (total_words) *total_words = b->total_words;
+    return TWOLDG_OK;
+}
+
+int twoldg_batch_rk4_step(twoldg_batch* b, void* u, const double* dt, int32_t nsteps) {
+    if (!b || !dt) return fail(TWOLDG_EINVAL, "NULL argument");
+    return b->rk4(u, dt, nsteps);
+}
+
+int twoldg_batch_synchronize(twoldg_batch* b) {
+    if (!b) return fail(TWOLDG_EINVAL, "NULL batch");
+    CK(cudaStreamSynchronize(b->stream));
+    return TWOLDG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,736 @@
+// Device code of the OLDG field step: one mesh block per CTA.
+//
+// State layout is the reference's (N^D, 2, nblocks), column-major, u then v
+// per block (src/stepping.jl:24-25): block b's u starts at b * 2 N^D, its v
+// N^D words later. Every kernel is templated on the field type T (float or
+// double), the dimension D and the element order P, so that the element
+// line contractions unroll with constant coefficients.
+//
+// Ghosts: the wide derivative (src/evolution.jl:24-35) reads one node past
+// its element along the dimension it differentiates, so a block needs its
+// neighbours' face nodes of u ("u ghosts") and, for the second application,
+// their face values of D_d u ("gradient ghosts"), faces only. Each stage
+// kernel exports, per block face, the face node of u (`fu`) and the part of
+// the face node's wide derivative that reads the block's own element
+// (`fog`, "own gradient"). A neighbour's gradient ghost is then
+//     (fog_nb + Wg * (the neighbour's own u ghost)) / h_nb,
+// and for a same-level or wall face that u ghost is this block's own face
+// node, so a stage needs only the previous stage's face exports and no
+// separate exchange pass. Coarse-fine faces are "dense": two small kernels
+// (cf_ghost_u, cf_ghost_g) fill their ghosts through the element-local
+// prolongation I and restriction R before the stage kernel runs.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels_types.h"
+
+namespace twoldg {
+
+constexpr int kMaxD = 3;
+
+enum : int { MODE_RHS = 0, MODE_STAGE1 = 1, MODE_STAGE4 = 4, MODE_ENERGY = 5 };
+
+template <typename T, int P>
+struct Tab {
+    T W[P + 1][P + 3];   // wide derivative per h, columns are nodes -1 .. P+1
+    T tm[P + 1];         // topmode
+    T td[P + 1];         // topdual
+    T wq[P + 1];         // Gauss-Lobatto weights on [-1, 1]
+};
+
+template <typename T, int P>
+struct CfTab {
+    T I[2 * (P + 1)][P + 1];
+    T R[P + 1][2 * (P + 1)];
+};
+
+template <typename T>
+struct StageArgs {
+    const BlockItem* items;
+    int nitems;
+    int E;
+    int mode;
+    int truncate;
+    T* u;            // u^n (stages) or the rhs input; receives u^{n+1} at stage 4
+    T* y;            // stage value
+    T* acc;          // increments accumulated over stages 1..3
+    T* comp;         // compensation words (compensated float path)
+    T* du;           // rhs output
+    const T* fu_in;
+    const T* fog_in;
+    T* fu_out;
+    T* fog_out;
+    const T* ugd;    // dense u ghosts (coarse-fine faces)
+    const T* ggd;    // dense gradient ghosts (coarse-fine faces)
+    const double* dts;
+    double* partial; // energy: one sum per item
+};
+
+__host__ __device__ constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1); }
+
+// Coordinates helpers. Owned node n = x0 + N x1 + N^2 x2.
+template <int D>
+struct Geo {
+    int N, S, NN, F, SS;
+    __device__ Geo(int N_) : N(N_), S(N_ + 2) {
+        NN = 1; F = 1; SS = 1;
+        for (int k = 0; k < D; ++k) { NN *= N; SS *= S; }
+        for (int k = 0; k < D - 1; ++k) F *= N;
+    }
+    __device__ int sstride(int d) const { int s = 1; for (int k = 0; k < d; ++k) s *= S; return s; }
+    __device__ int ostride(int d) const { int s = 1; for (int k = 0; k < d; ++k) s *= N; return s; }
+    // owned linear index -> padded smem index
+    __device__ int sidx_of_owned(int n) const {
+        int r = 0, s = 1;
+        for (int k = 0; k < D; ++k) { r += (n % N + 1) * s; n /= N; s *= S; }
+        return r;
+    }
+    // face tangential index t of a face normal to d, with x_d given -> padded smem index
+    __device__ int sidx_face(int d, int t, int xd) const {
+        int r = 0, s = 1;
+        for (int k = 0; k < D; ++k) {
+            int x;
+            if (k == d) x = xd; else { x = t % N; t /= N; }
+            r += (x + 1) * s;
+            s *= S;
+        }
+        return r;
+    }
+    // owned index of a face node
+    __device__ int oidx_face(int d, int t, int xd) const {
+        int r = 0, s = 1;
+        for (int k = 0; k < D; ++k) {
+            int x;
+            if (k == d) x = xd; else { x = t % N; t /= N; }
+            r += x * s;
+            s *= N;
+        }
+        return r;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Element-line contractions with the stencil's structural zeros skipped:
+// row i reads columns 1..P+1 (its element) except the diagonal i+1, which is
+// zero; only row 0 reads column 0 and only row P column P+2 (the faces).
+template <typename T, int P>
+__device__ __forceinline__ void line_derivative(const Tab<T, P>& tb, const T (&w)[P + 3], T (&out)[P + 1]) {
+#pragma unroll
+    for (int i = 0; i <= P; ++i) {
+        T acc = T(0);
+#pragma unroll
+        for (int k = 0; k < P + 3; ++k) {
+            if (k == i + 1) continue;
+            if (k == 0 && i != 0) continue;
+            if (k == P + 2 && i != P) continue;
+            acc += tb.W[i][k] * w[k];
+        }
+        out[i] = acc;
+    }
+}
+
+// Own-element part of the face row: low face row 0 over columns 1..P+1, high
+// face row P over columns 1..P+1, applied to the element's P+1 nodes.
+template <typename T, int P>
+__device__ __forceinline__ T own_face_part(const Tab<T, P>& tb, int side, const T (&e)[P + 1]) {
+    T acc = T(0);
+    if (side == 0) {
+#pragma unroll
+        for (int k = 1; k <= P + 1; ++k) if (k != 1) acc += tb.W[0][k] * e[k - 1];
+    } else {
+#pragma unroll
+        for (int k = 1; k <= P + 1; ++k) if (k != P + 1) acc += tb.W[P][k] * e[k - 1];
+    }
+    return acc;
+}
+
+template <typename T, int P>
+__device__ __forceinline__ T ghost_coef(const Tab<T, P>& tb, int side) {
+    return side == 0 ? tb.W[0][0] : tb.W[P][P + 2];
+}
+
+// Error-free sum (Knuth's TwoSum).
+template <typename T>
+__device__ __forceinline__ void two_sum(T a, T b, T& s, T& e) {
+    s = a + b;
+    T bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// ---------------------------------------------------------------------------
+// Face export of an arbitrary state (rk4 start, rhs, energy): per block face
+// the face node of u and the own part of its wide derivative.
+template <typename T, int D, int P>
+__global__ void export_faces_kernel(const BlockItem* items, int nitems, int E, const T* u, T* fu,
+                                    T* fog, Tab<T, P> tb) {
+    Geo<D> g(E * (P + 1));
+    const int perblock = 2 * D * g.F;
+    int64_t total = (int64_t)nitems * perblock;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int b = (int)(i / perblock);
+        int r = (int)(i % perblock);
+        int f = r / g.F, t = r % g.F;
+        int d = f >> 1, side = f & 1;
+        const BlockItem& it = items[b];
+        const T* ub = u + it.off;
+        int sd = g.ostride(d);
+        int x0 = side == 0 ? 0 : g.N - 1 - P;
+        int base = g.oidx_face(d, t, x0);
+        T e[P + 1];
+#pragma unroll
+        for (int k = 0; k <= P; ++k) e[k] = ub[base + k * sd];
+        int slot = it.slot + f;
+        fu[(int64_t)slot * g.F + t] = side == 0 ? e[0] : e[P];
+        fog[(int64_t)slot * g.F + t] = own_face_part<T, P>(tb, side, e);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Coarse-fine ghosts. Tangential dims of a face normal to d are the other
+// dims in increasing order; a face's tangential index t has the first of
+// them fastest. One thread per (cf face, t).
+template <typename T, int D, int P>
+__device__ __forceinline__ T cf_apply(const CfFace& c, int t, int N, int E, int F, const T* src,
+                                      const CfTab<T, P>& ct) {
+    constexpr int P1 = P + 1;
+    constexpr int DT = D - 1;
+    if constexpr (DT == 0) {
+        return src[(int64_t)c.src[0] * F];
+    } else {
+        int n[DT];
+        {
+            int tt = t;
+            for (int k = 0; k < DT; ++k) { n[k] = tt % N; tt /= N; }
+        }
+        const int halfE = E / 2;
+        if (c.kind == 0) {
+            // fine ghost from the coarse face: sum_j I[row][j] * coarse values
+            int row[DT], cb[DT];
+            for (int k = 0; k < DT; ++k) {
+                int e = n[k] / P1, i = n[k] % P1;
+                int q = (c.sub >> k) & 1;
+                row[k] = (e & 1) * P1 + i;
+                cb[k] = (q * halfE + e / 2) * P1;
+            }
+            const T* s = src + (int64_t)c.src[0] * F;
+            T acc = T(0);
+            if constexpr (DT == 1) {
+#pragma unroll
+                for (int j = 0; j < P1; ++j) acc += ct.I[row[0]][j] * s[cb[0] + j];
+            } else {
+#pragma unroll
+                for (int j2 = 0; j2 < P1; ++j2) {
+                    T a = T(0);
+#pragma unroll
+                    for (int j1 = 0; j1 < P1; ++j1) a += ct.I[row[0]][j1] * s[(cb[0] + j1) + N * (cb[1] + j2)];
+                    acc += ct.I[row[1]][j2] * a;
+                }
+            }
+            return acc;
+        } else {
+            // coarse ghost from the fine faces: sum_r R[j][r] * fine values
+            int j[DT], fb[DT], bits = 0;
+            for (int k = 0; k < DT; ++k) {
+                int ec = n[k] / P1;
+                j[k] = n[k] % P1;
+                int q = ec / halfE;
+                bits |= q << k;
+                fb[k] = 2 * (ec % halfE) * P1;
+            }
+            const T* s = src + (int64_t)c.src[bits] * F;
+            T acc = T(0);
+            if constexpr (DT == 1) {
+#pragma unroll
+                for (int r = 0; r < 2 * P1; ++r) acc += ct.R[j[0]][r] * s[fb[0] + r];
+            } else {
+#pragma unroll
+                for (int r2 = 0; r2 < 2 * P1; ++r2) {
+                    T a = T(0);
+#pragma unroll
+                    for (int r1 = 0; r1 < 2 * P1; ++r1) a += ct.R[j[0]][r1] * s[(fb[0] + r1) + N * (fb[1] + r2)];
+                    acc += ct.R[j[1]][r2] * a;
+                }
+            }
+            return acc;
+        }
+    }
+}
+
+template <typename T, int D, int P>
+__global__ void cf_ghost_u_kernel(const CfFace* cf, int ncf, int E, const T* fu, const T* fog, T* ugd,
+                                  T* gfd, Tab<T, P> tb, CfTab<T, P> ct) {
+    int N = E * (P + 1);
+    int F = ipow(N, D - 1);
+    int64_t total = (int64_t)ncf * F;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int c = (int)(i / F), t = (int)(i % F);
+        CfFace face = cf[c];
+        T ug = cf_apply<T, D, P>(face, t, N, E, F, fu, ct);
+        int64_t o = (int64_t)face.slot * F + t;
+        ugd[o] = ug;
+        gfd[o] = (fog[o] + ghost_coef<T, P>(tb, face.side) * ug) / T(face.h);
+    }
+}
+
+template <typename T, int D, int P>
+__global__ void cf_ghost_g_kernel(const CfFace* cf, int ncf, int E, const T* gfd, T* ggd, CfTab<T, P> ct) {
+    int N = E * (P + 1);
+    int F = ipow(N, D - 1);
+    int64_t total = (int64_t)ncf * F;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int c = (int)(i / F), t = (int)(i % F);
+        CfFace face = cf[c];
+        ggd[(int64_t)face.slot * F + t] = cf_apply<T, D, P>(face, t, N, E, F, gfd, ct);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Loads a block's u with its face ghosts into the padded smem array su.
+template <typename T, int D, int P>
+__device__ __forceinline__ void load_u_with_ghosts(const Geo<D>& g, const BlockItem& it, const T* ysrc,
+                                                   const StageArgs<T>& a, T* su) {
+    const T* yu = ysrc + it.off;
+    for (int n = threadIdx.x; n < g.NN; n += blockDim.x) su[g.sidx_of_owned(n)] = yu[n];
+    for (int i = threadIdx.x; i < 2 * D * g.F; i += blockDim.x) {
+        int f = i / g.F, t = i % g.F;
+        int d = f >> 1, side = f & 1;
+        T v;
+        if (it.flags & (1u << f)) v = a.ugd[(int64_t)(it.slot + f) * g.F + t];
+        else v = a.fu_in[(int64_t)it.nb[f] * g.F + t];
+        su[g.sidx_face(d, t, side == 0 ? -1 : g.N)] = v;
+    }
+}
+
+// Gradient along d at every owned node into sg (padded layout), scaled by 1/h,
+// and the gradient ghost planes normal to d.
+template <typename T, int D, int P>
+__device__ __forceinline__ void gradient_along(const Geo<D>& g, int E, int d, const BlockItem& it,
+                                               const StageArgs<T>& a, const Tab<T, P>& tb, const T* su,
+                                               T* sg, T inv_h) {
+    constexpr int P1 = P + 1;
+    const int sd = g.sstride(d);
+    const int nlines = E * g.F;
+    for (int L = threadIdx.x; L < nlines; L += blockDim.x) {
+        int t = L % g.F, e = L / g.F;
+        int base = g.sidx_face(d, t, e * P1);
+        T w[P + 3], out[P + 1];
+#pragma unroll
+        for (int k = 0; k < P + 3; ++k) w[k] = su[base + (k - 1) * sd];
+        line_derivative<T, P>(tb, w, out);
+#pragma unroll
+        for (int i = 0; i <= P; ++i) sg[base + i * sd] = out[i] * inv_h;
+    }
+    for (int i = threadIdx.x; i < 2 * g.F; i += blockDim.x) {
+        int side = i / g.F, t = i % g.F;
+        int f = 2 * d + side;
+        T v;
+        if (it.flags & (1u << f)) {
+            v = a.ggd[(int64_t)(it.slot + f) * g.F + t];
+        } else {
+            // the neighbour's face-node derivative: its own part plus its ghost
+            // coefficient times its u ghost, which is this block's face node
+            int nslot = it.nb[f];
+            int nside = nslot & 1;  // face index parity = side (slots are b*2D + f)
+            T own = su[g.sidx_face(d, t, side == 0 ? 0 : g.N - 1)];
+            T gnb = (a.fog_in[(int64_t)nslot * g.F + t] + ghost_coef<T, P>(tb, nside) * own) * inv_h;
+            v = (it.flags & (1u << (8 + f))) ? -gnb : gnb;
+        }
+        sg[g.sidx_face(d, t, side == 0 ? -1 : g.N)] = v;
+    }
+}
+
+// Laplacian term along d: slap[n] (+)= D_d(sg) at every owned node (not yet /h).
+template <typename T, int D, int P>
+__device__ __forceinline__ void laplacian_along(const Geo<D>& g, int E, int d, const Tab<T, P>& tb,
+                                                const T* sg, T* slap, bool first) {
+    constexpr int P1 = P + 1;
+    const int sd = g.sstride(d);
+    const int od = g.ostride(d);
+    const int nlines = E * g.F;
+    for (int L = threadIdx.x; L < nlines; L += blockDim.x) {
+        int t = L % g.F, e = L / g.F;
+        int base = g.sidx_face(d, t, e * P1);
+        int obase = g.oidx_face(d, t, e * P1);
+        T w[P + 3], out[P + 1];
+#pragma unroll
+        for (int k = 0; k < P + 3; ++k) w[k] = sg[base + (k - 1) * sd];
+        line_derivative<T, P>(tb, w, out);
+#pragma unroll
+        for (int i = 0; i <= P; ++i) {
+            if (first) slap[obase + i * od] = out[i];
+            else slap[obase + i * od] += out[i];
+        }
+    }
+}
+
+// Truncation of v (owned layout in sv), per element line along each d in
+// turn: c = sum_j topdual_j v_j; v_i -= topmode_i c (src/evolution.jl:222-264).
+// With COMP the subtraction is error-free into the compensation words sc.
+template <typename T, int D, int P, bool COMP>
+__device__ __forceinline__ void truncate_block(const Geo<D>& g, int E, const Tab<T, P>& tb, T* sv, T* sc) {
+    constexpr int P1 = P + 1;
+    const int nlines = E * g.F;
+    for (int d = 0; d < D; ++d) {
+        const int od = g.ostride(d);
+        for (int L = threadIdx.x; L < nlines; L += blockDim.x) {
+            int t = L % g.F, e = L / g.F;
+            int obase = g.oidx_face(d, t, e * P1);
+            T v[P1];
+            T c = T(0);
+#pragma unroll
+            for (int j = 0; j < P1; ++j) { v[j] = sv[obase + j * od]; c += tb.td[j] * v[j]; }
+            if (COMP) {
+                T cc = T(0);
+#pragma unroll
+                for (int j = 0; j < P1; ++j) cc += tb.td[j] * sc[obase + j * od];
+                c += cc;
+#pragma unroll
+                for (int i = 0; i < P1; ++i) {
+                    T s, err;
+                    two_sum(v[i], -(tb.tm[i] * c), s, err);
+                    sv[obase + i * od] = s;
+                    sc[obase + i * od] += err;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < P1; ++i) sv[obase + i * od] = v[i] - tb.tm[i] * c;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Face export from the padded su of the new stage value.
+template <typename T, int D, int P>
+__device__ __forceinline__ void export_from_smem(const Geo<D>& g, const BlockItem& it, const Tab<T, P>& tb,
+                                                 const T* su, T* fu, T* fog) {
+    for (int i = threadIdx.x; i < 2 * D * g.F; i += blockDim.x) {
+        int f = i / g.F, t = i % g.F;
+        int d = f >> 1, side = f & 1;
+        int sd = g.sstride(d);
+        int x0 = side == 0 ? 0 : g.N - 1 - P;
+        int base = g.sidx_face(d, t, x0);
+        T e[P + 1];
+#pragma unroll
+        for (int k = 0; k <= P; ++k) e[k] = su[base + k * sd];
+        int64_t o = (int64_t)(it.slot + f) * g.F + t;
+        fu[o] = side == 0 ? e[0] : e[P];
+        fog[o] = own_face_part<T, P>(tb, side, e);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The fused stage: k = f(Y) (u' = v, v' = sum_d D_d D_d u) for one block, the
+// classic RK4 combination of that stage, the truncation of the new v and
+// the face export of the new u. acc holds only increments (dt/6 k1 + dt/3 k2
+// + dt/3 k3), added to u^n at stage 4. mode MODE_RHS writes du = f(u) only.
+template <typename T, int D, int P, bool COMP>
+__global__ void __launch_bounds__(256) stage_kernel(StageArgs<T> a, Tab<T, P> tb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* smem = reinterpret_cast<T*>(smem_raw);
+    Geo<D> g(a.E * (P + 1));
+    T* su = smem;
+    T* sg = su + g.SS;
+    T* slap = sg + g.SS;
+    const int mode = a.mode;
+    const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
+
+    for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+        const BlockItem it = a.items[item];
+        const T inv_h = T(1) / T(it.h);
+        load_u_with_ghosts<T, D, P>(g, it, ysrc, a, su);
+        __syncthreads();
+        for (int d = 0; d < D; ++d) {
+            gradient_along<T, D, P>(g, a.E, d, it, a, tb, su, sg, inv_h);
+            __syncthreads();
+            laplacian_along<T, D, P>(g, a.E, d, tb, sg, slap, d == 0);
+            __syncthreads();
+        }
+        const T* yv = ysrc + it.off + g.NN;
+        if (mode == MODE_RHS) {
+            T* du = a.du + it.off;
+            for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
+                du[n] = yv[n];
+                du[g.NN + n] = slap[n] * inv_h;
+            }
+            __syncthreads();
+            continue;
+        }
+        const double dt = a.dts[it.problem];
+        const T* un = a.u + it.off;
+        T* acc = a.acc + it.off;
+        T* comp = COMP ? a.comp + it.off : nullptr;
+        T* sc = sg;  // compensation of v during the final truncation
+        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
+            T ku = yv[n];
+            T kv = slap[n] * inv_h;
+            T uu = un[n], uv = un[g.NN + n];
+            T nu, nv;
+            if (mode == 1) {
+                acc[n] = T(dt / 6) * ku;
+                acc[g.NN + n] = T(dt / 6) * kv;
+                nu = uu + T(dt / 2) * ku;
+                nv = uv + T(dt / 2) * kv;
+            } else if (mode == 2 || mode == 3) {
+                acc[n] += T(dt / 3) * ku;
+                acc[g.NN + n] += T(dt / 3) * kv;
+                T c = mode == 2 ? T(dt / 2) : T(dt);
+                nu = uu + c * ku;
+                nv = uv + c * kv;
+            } else {
+                T iu = acc[n] + T(dt / 6) * ku;
+                T iv = acc[g.NN + n] + T(dt / 6) * kv;
+                if (COMP) {
+                    T cu = comp[n] + iu, cv = comp[g.NN + n] + iv;
+                    T eu, ev;
+                    two_sum(uu, cu, nu, eu);
+                    two_sum(uv, cv, nv, ev);
+                    comp[n] = eu;
+                    sc[n] = ev;
+                } else {
+                    nu = uu + iu;
+                    nv = uv + iv;
+                }
+            }
+            su[g.sidx_of_owned(n)] = nu;
+            slap[n] = nv;
+        }
+        __syncthreads();
+        const bool final_comp = COMP && mode == MODE_STAGE4;
+        if (a.truncate) {
+            if (final_comp) truncate_block<T, D, P, true>(g, a.E, tb, slap, sc);
+            else truncate_block<T, D, P, false>(g, a.E, tb, slap, sc);
+        }
+        T* out = (mode == MODE_STAGE4 ? a.u : a.y) + it.off;
+        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
+            out[n] = su[g.sidx_of_owned(n)];
+            out[g.NN + n] = slap[n];
+            if (final_comp) comp[g.NN + n] = sc[n];
+        }
+        export_from_smem<T, D, P>(g, it, tb, su, a.fu_out, a.fog_out);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Energy (src/evolution.jl:1472-1489, flat): 1/2 sum_nodes w (v^2 + sum_d
+// (D_d u)^2), w = prod_d h (P+1)/2 w_hat(i_d). One FP64 partial per block.
+template <int D>
+__device__ __forceinline__ double block_reduce_sum(double v, double* red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    double s = 0;
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) s += red[w];
+    }
+    __syncthreads();
+    return s;
+}
+
+template <typename T, int D, int P>
+__global__ void __launch_bounds__(256) energy_kernel(StageArgs<T> a, Tab<T, P> tb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* smem = reinterpret_cast<T*>(smem_raw);
+    Geo<D> g(a.E * (P + 1));
+    T* su = smem;
+    double* red = reinterpret_cast<double*>(su + g.SS + (g.SS & 1));
+    constexpr int P1 = P + 1;
+    for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+        const BlockItem it = a.items[item];
+        const double h = it.h;
+        const T inv_h = T(1) / T(h);
+        load_u_with_ghosts<T, D, P>(g, it, a.u, a, su);
+        __syncthreads();
+        double local = 0;
+        const double wscale = h * P1 / 2.0;
+        const T* uv = a.u + it.off + g.NN;
+        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
+            double w = 1.0;
+            int m = n;
+            for (int k = 0; k < D; ++k) { w *= wscale * (double)tb.wq[(m % g.N) % P1]; m /= g.N; }
+            double v = (double)uv[n];
+            local += w * v * v;
+        }
+        for (int d = 0; d < D; ++d) {
+            const int sd = g.sstride(d);
+            const int nlines = a.E * g.F;
+            for (int L = threadIdx.x; L < nlines; L += blockDim.x) {
+                int t = L % g.F, e = L / g.F;
+                int base = g.sidx_face(d, t, e * P1);
+                double wt = 1.0;
+                {
+                    int tt = t;
+                    for (int k = 0; k < D; ++k) {
+                        if (k == d) continue;
+                        wt *= wscale * (double)tb.wq[(tt % g.N) % P1];
+                        tt /= g.N;
+                    }
+                }
+                T w[P + 3], out[P + 1];
+#pragma unroll
+                for (int k = 0; k < P + 3; ++k) w[k] = su[base + (k - 1) * sd];
+                line_derivative<T, P>(tb, w, out);
+#pragma unroll
+                for (int i = 0; i <= P; ++i) {
+                    double gv = (double)(out[i] * inv_h);
+                    local += wt * wscale * (double)tb.wq[i] * gv * gv;
+                }
+            }
+        }
+        double s = block_reduce_sum<D>(local, red);
+        if (threadIdx.x == 0) a.partial[item] = 0.5 * s;
+        __syncthreads();
+    }
+}
+
+// Quadrature p-norm parts (src/layout.jl:100-122, 223-235): per block
+// sum w |x - ref|^p over the selected variables and sum w * nvars; p = 0
+// means the largest |x - ref|.
+template <typename T, int D, int P>
+__global__ void norm_kernel(const BlockItem* items, int nitems, int E, const T* u, const T* ref, int p,
+                            int vars_mask, Tab<T, P> tb, double* part_num, double* part_vol) {
+    __shared__ double red[32];
+    constexpr int P1 = P + 1;
+    const int N = E * P1;
+    const int NN = ipow(N, D);
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const BlockItem it = items[item];
+        const double wscale = it.h * P1 / 2.0;
+        double num = 0, vol = 0;
+        for (int n = threadIdx.x; n < NN; n += blockDim.x) {
+            double w = 1.0;
+            int m = n;
+            for (int k = 0; k < D; ++k) { w *= wscale * (double)tb.wq[(m % N) % P1]; m /= N; }
+            for (int var = 0; var < 2; ++var) {
+                if (!(vars_mask & (1 << var))) continue;
+                int64_t o = it.off + (int64_t)var * NN + n;
+                double x = (double)u[o];
+                if (ref) x -= (double)ref[o];
+                x = fabs(x);
+                if (p == 0) num = fmax(num, x);
+                else if (p == 2) num += w * x * x;
+                else num += w * pow(x, (double)p);
+                vol += w;
+            }
+        }
+        double s;
+        if (p == 0) {
+            for (int o = 16; o > 0; o >>= 1) num = fmax(num, __shfl_down_sync(0xffffffffu, num, o));
+            int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+            if (lane == 0) red[wid] = num;
+            __syncthreads();
+            s = 0;
+            if (threadIdx.x == 0)
+                for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) s = fmax(s, red[w]);
+            __syncthreads();
+        } else {
+            s = block_reduce_sum<D>(num, red);
+        }
+        double v = block_reduce_sum<D>(vol, red);
+        if (threadIdx.x == 0) { part_num[item] = s; part_vol[item] = v; }
+        __syncthreads();
+    }
+}
+
+// Modal indicator (src/refinement.jl:56-77): per element the largest over
+// its lines in every dimension and over the modes q of
+// (weights[q] |sum_j duals[q][j] a_j|)^pows[q], times post.
+template <typename T, int P>
+struct ModeTab {
+    T dual[P + 1][P + 1];
+    T weight[P + 1];
+    T pw[P + 1];
+    int nq;
+    T post;
+};
+
+template <typename T, int D, int P>
+__global__ void mode_kernel(const BlockItem* items, int nitems, int E, const T* u, int var, ModeTab<T, P> mt,
+                            T* tau) {
+    constexpr int P1 = P + 1;
+    const int N = E * P1;
+    const int NN = ipow(N, D);
+    const int EE = ipow(E, D);
+    int64_t total = (int64_t)nitems * EE;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int b = (int)(i / EE), el = (int)(i % EE);
+        const T* a = u + items[b].off + (int64_t)var * NN;
+        int base = 0, s = 1;
+        {
+            int m = el;
+            for (int k = 0; k < D; ++k) { base += (m % E) * P1 * s; m /= E; s *= N; }
+        }
+        T best = T(0);
+        for (int d = 0; d < D; ++d) {
+            int sd = 1;
+            for (int k = 0; k < d; ++k) sd *= N;
+            const int nl = ipow(P1, D - 1);
+            for (int l = 0; l < nl; ++l) {
+                int off = 0, ll = l, st = 1;
+                for (int k = 0; k < D; ++k) {
+                    if (k != d) { off += (ll % P1) * st; ll /= P1; }
+                    st *= N;
+                }
+                T line[P1];
+#pragma unroll
+                for (int j = 0; j < P1; ++j) line[j] = a[base + off + j * sd];
+                for (int q = 0; q < mt.nq; ++q) {
+                    T c = T(0);
+#pragma unroll
+                    for (int j = 0; j < P1; ++j) c += mt.dual[q][j] * line[j];
+                    T x = mt.weight[q] * (c < T(0) ? -c : c);
+                    T v = mt.pw[q] == T(1) ? x : (T)pow((double)x, (double)mt.pw[q]);
+                    best = v > best ? v : best;
+                }
+            }
+        }
+        tau[i] = mt.post * best;
+    }
+}
+
+// Largest |u| of one variable, per block (the indicator's global scale).
+template <typename T, int D>
+__global__ void maxabs_kernel(const BlockItem* items, int nitems, int NN, const T* u, int var, double* part) {
+    __shared__ double red[32];
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const T* a = u + items[item].off + (int64_t)var * NN;
+        double m = 0;
+        for (int n = threadIdx.x; n < NN; n += blockDim.x) m = fmax(m, fabs((double)a[n]));
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+        int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        if (lane == 0) red[wid] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0;
+            for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) s = fmax(s, red[w]);
+            part[item] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// Standalone truncation of v (twoldg_truncate): one block per CTA, v staged
+// in shared memory.
+template <typename T, int D, int P>
+__global__ void truncate_kernel(const BlockItem* items, int nitems, int E, T* u, Tab<T, P> tb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sv = reinterpret_cast<T*>(smem_raw);
+    Geo<D> g(E * (P + 1));
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        T* v = u + items[item].off + g.NN;
+        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) sv[n] = v[n];
+        __syncthreads();
+        truncate_block<T, D, P, false>(g, E, tb, sv, nullptr);
+        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) v[n] = sv[n];
+        __syncthreads();
+    }
+}
+
+}  // namespace twoldg

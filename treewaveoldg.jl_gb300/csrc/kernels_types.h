@@ -1,0 +1,27 @@
+// Plain work-item structs shared by the host set-up and the kernels.
+#pragma once
+#include <stdint.h>
+
+namespace twoldg {
+
+// One mesh block as a work item of the stage and energy kernels.
+struct BlockItem {
+    int64_t off;        // word offset of the block's u in the state arrays
+    int32_t slot;       // face slot of this block's face 0; face f is slot + f
+    int32_t nb[6];      // face slot whose exports give face f's ghosts
+    uint32_t flags;     // bit f: face f is dense (coarse-fine); bit 8+f: gradient ghost odd
+    int32_t problem;    // index into the per-problem time steps
+    double h;           // the block's spacing
+};
+
+// A coarse-fine face: its ghosts are an I or R image of the other side.
+struct CfFace {
+    int32_t slot;       // the face slot whose ghosts this fills
+    int32_t kind;       // 0: fine ghost from coarse (I), 1: coarse ghost from fine (R)
+    int32_t src[4];     // kind 0: src[0] the coarse face; kind 1: fine faces by child bits
+    int32_t sub;        // kind 0: bit k = which half of the coarse face along tangential dim k
+    int32_t side;       // 0 low face, 1 high face
+    double h;           // spacing of the block owning `slot`
+};
+
+}  // namespace twoldg

@@ -1,0 +1,193 @@
+// Mesh compiler. The neighbour of a block across a face is found by the
+// leaf's integer coordinates, as TreeAMR's forest finds it: a block of the
+// same level at the adjacent corner, else its parent-level block (this block
+// is then the fine side of a coarse-fine face), else the 2^(D-1) children of
+// the adjacent corner that touch the face (this block is the coarse side).
+// A face outside the domain is periodic (wrapped) or a reflecting wall.
+//
+// Ghost semantics follow TreeAMR's element-local operators as the reference
+// documents them (CODE.md, "The layout", "Reflecting walls", "The coupling"):
+// same level and normal direction always injection of the neighbour's face
+// node; walls mirror the block's own face node with u even and d_d u odd;
+// across a coarse-fine face the fine ghost is the coarse element's
+// polynomial at the fine nodes (I) and the coarse ghost its adjoint
+// restriction R = M_c^-1 I^T M_f, tangentially.
+#include "mesh.h"
+
+#include <cmath>
+#include <map>
+#include <sstream>
+
+namespace twoldg {
+
+namespace {
+
+struct Key {
+    int level;
+    int64_t c[3];
+    bool operator<(const Key& o) const {
+        if (level != o.level) return level < o.level;
+        for (int k = 0; k < 3; ++k)
+            if (c[k] != o.c[k]) return c[k] < o.c[k];
+        return false;
+    }
+};
+
+}  // namespace
+
+bool build_mesh(const twoldg_desc& d, Mesh& m, std::string& err) {
+    std::ostringstream es;
+    const int D = d.dim;
+    if (D < 1 || D > 3) { es << "dim = " << D << " must be 1, 2 or 3"; err = es.str(); return false; }
+    if (d.order < 1) { es << "the element order P must be at least 1, got " << d.order; err = es.str(); return false; }
+    if (d.elems < 2 || d.elems % 2) {
+        es << "E = " << d.elems << " elements per block must be even and at least 2: a block of a refined forest "
+           << "covers half of its parent and has to cover whole elements of it (N must be a multiple of 2(P+1))";
+        err = es.str();
+        return false;
+    }
+    if (d.nblocks < 1 || !d.level || !d.corner) { err = "the forest has no blocks (nblocks, level, corner)"; return false; }
+    m.D = D;
+    m.P = d.order;
+    m.E = d.elems;
+    m.N = d.elems * (d.order + 1);
+    m.nblocks = d.nblocks;
+    m.NN = 1;
+    for (int k = 0; k < D; ++k) m.NN *= m.N;
+    double cell = 0;
+    for (int k = 0; k < D; ++k) {
+        if (d.roots[k] < 1) { es << "roots[" << k << "] = " << d.roots[k] << " must be positive"; err = es.str(); return false; }
+        if (!(d.hi[k] > d.lo[k])) { es << "extent " << k << " is empty"; err = es.str(); return false; }
+        if (d.periodic[k] && d.reflecting[k]) {
+            es << "dimension " << k << " is both periodic and reflecting"; err = es.str(); return false;
+        }
+        if (!d.periodic[k] && !d.reflecting[k]) {
+            es << "dimension " << k << " is neither periodic nor reflecting: the flat problem's outer faces are "
+               << "filled by periodicity or by the wall's mirror";
+            err = es.str();
+            return false;
+        }
+        double c = (d.hi[k] - d.lo[k]) / d.roots[k];
+        if (k == 0) cell = c;
+        else if (std::fabs(c - cell) > 1e-12 * cell) {
+            err = "root blocks must be cubes: one spacing per block, as the reference's per-block h";
+            return false;
+        }
+    }
+    std::map<Key, int> leaves;
+    double volume = 0;
+    for (int b = 0; b < d.nblocks; ++b) {
+        Key key{d.level[b], {0, 0, 0}};
+        if (key.level < 0 || key.level > 20) { es << "block " << b << " has level " << key.level; err = es.str(); return false; }
+        for (int k = 0; k < D; ++k) {
+            key.c[k] = d.corner[(int64_t)b * D + k];
+            int64_t ext = (int64_t)d.roots[k] << key.level;
+            if (key.c[k] < 0 || key.c[k] >= ext) {
+                es << "block " << b << " corner[" << k << "] = " << key.c[k] << " is outside [0, " << ext << ")";
+                err = es.str();
+                return false;
+            }
+        }
+        if (!leaves.emplace(key, b).second) { es << "block " << b << " duplicates another leaf"; err = es.str(); return false; }
+        volume += std::ldexp(1.0, -D * key.level);
+    }
+    double rootsvol = 1;
+    for (int k = 0; k < D; ++k) rootsvol *= d.roots[k];
+    if (std::fabs(volume - rootsvol) > 1e-9 * rootsvol) {
+        err = "the leaves do not tile the domain (their volume differs from the root blocks')";
+        return false;
+    }
+    m.h.resize(d.nblocks);
+    m.items.assign(d.nblocks, BlockItem{});
+    m.hmin = INFINITY;
+    for (int b = 0; b < d.nblocks; ++b) {
+        m.h[b] = cell / std::ldexp(1.0, d.level[b]) / m.N;
+        m.hmin = std::fmin(m.hmin, m.h[b]);
+        BlockItem& it = m.items[b];
+        it.off = (int64_t)b * 2 * m.NN;
+        it.slot = b * 2 * D;
+        it.flags = 0;
+        it.problem = 0;
+        it.h = m.h[b];
+        for (int f = 0; f < 6; ++f) it.nb[f] = -1;
+    }
+    auto slot = [&](int b, int f) { return b * 2 * D + f; };
+    for (int b = 0; b < d.nblocks; ++b) {
+        const int lv = d.level[b];
+        int64_t c[3] = {0, 0, 0};
+        for (int k = 0; k < D; ++k) c[k] = d.corner[(int64_t)b * D + k];
+        BlockItem& it = m.items[b];
+        for (int f = 0; f < 2 * D; ++f) {
+            const int dd = f / 2, side = f % 2;
+            Key n{lv, {c[0], c[1], c[2]}};
+            n.c[dd] += side ? 1 : -1;
+            const int64_t ext = (int64_t)d.roots[dd] << lv;
+            if (n.c[dd] < 0 || n.c[dd] >= ext) {
+                if (d.periodic[dd]) {
+                    n.c[dd] = (n.c[dd] + ext) % ext;
+                } else {
+                    it.nb[f] = slot(b, f);
+                    it.flags |= 1u << (8 + f);
+                    m.nwall++;
+                    continue;
+                }
+            }
+            auto same = leaves.find(n);
+            if (same != leaves.end()) {
+                it.nb[f] = slot(same->second, f ^ 1);
+                m.nsame++;
+                continue;
+            }
+            if (lv > 0) {
+                Key p{lv - 1, {0, 0, 0}};
+                for (int k = 0; k < D; ++k) p.c[k] = n.c[k] >> 1;
+                auto coarse = leaves.find(p);
+                if (coarse != leaves.end()) {
+                    CfFace cf{};
+                    cf.slot = slot(b, f);
+                    cf.kind = 0;
+                    cf.src[0] = slot(coarse->second, f ^ 1);
+                    int bit = 0;
+                    for (int k = 0; k < D; ++k) {
+                        if (k == dd) continue;
+                        cf.sub |= (int)(c[k] & 1) << bit;
+                        ++bit;
+                    }
+                    cf.side = side;
+                    cf.h = m.h[b];
+                    m.cf.push_back(cf);
+                    it.flags |= 1u << f;
+                    continue;
+                }
+            }
+            CfFace cf{};
+            cf.slot = slot(b, f);
+            cf.kind = 1;
+            cf.side = side;
+            cf.h = m.h[b];
+            bool ok = true;
+            for (int q = 0; q < (1 << (D - 1)); ++q) {
+                Key ch{lv + 1, {0, 0, 0}};
+                int bit = 0;
+                for (int k = 0; k < D; ++k) {
+                    if (k == dd) ch.c[k] = 2 * n.c[k] + (side ? 0 : 1);
+                    else { ch.c[k] = 2 * n.c[k] + ((q >> bit) & 1); ++bit; }
+                }
+                auto fine = leaves.find(ch);
+                if (fine == leaves.end()) { ok = false; break; }
+                cf.src[q] = slot(fine->second, f ^ 1);
+            }
+            if (!ok) {
+                es << "block " << b << " face " << f << " has no neighbour one level apart at most: the forest must "
+                   << "be 2:1 balanced across faces and tile the domain";
+                err = es.str();
+                return false;
+            }
+            m.cf.push_back(cf);
+            it.flags |= 1u << f;
+        }
+    }
+    return true;
+}
+
+}  // namespace twoldg

@@ -1,0 +1,62 @@
+// Host-side interface to the templated kernels: one Ops object per
+// (precision, dimension, order), created at problem set-up. Pointers are
+// device pointers of the problem's precision; sizes are in words.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels_types.h"
+#include "tables.h"
+
+namespace twoldg {
+
+enum Precision : int { PREC_F64 = 0, PREC_F32 = 1, PREC_F32C = 2 };
+
+struct StagePtrs {
+    void* u;
+    void* y;
+    void* acc;
+    void* comp;
+    void* du;
+    const void* fu_in;
+    const void* fog_in;
+    void* fu_out;
+    void* fog_out;
+    const void* ugd;
+    const void* ggd;
+    const double* dts;
+    double* partial;
+};
+
+class Ops {
+public:
+    virtual ~Ops() {}
+    // bytes of dynamic shared memory the stage kernel needs for E elements per dim
+    virtual size_t stage_smem(int E) const = 0;
+    virtual int stage_threads() const = 0;
+    virtual cudaError_t export_faces(const BlockItem* items, int nitems, int E, const void* u, void* fu,
+                                     void* fog, cudaStream_t s) const = 0;
+    virtual cudaError_t cf_ghosts(const CfFace* cf, int ncf, int E, const void* fu, const void* fog, void* ugd,
+                                  void* gfd, void* ggd, cudaStream_t s) const = 0;
+    virtual cudaError_t stage(const BlockItem* items, int nitems, int E, int mode, int truncate,
+                              const StagePtrs& p, int grid, cudaStream_t s) const = 0;
+    virtual cudaError_t energy(const BlockItem* items, int nitems, int E, const StagePtrs& p,
+                               cudaStream_t s) const = 0;
+    virtual cudaError_t norm(const BlockItem* items, int nitems, int E, const void* u, const void* ref, int p,
+                             int vars_mask, double* num, double* vol, cudaStream_t s) const = 0;
+    virtual cudaError_t truncate(const BlockItem* items, int nitems, int E, void* u, cudaStream_t s) const = 0;
+    virtual cudaError_t maxabs(const BlockItem* items, int nitems, int E, const void* u, int var, double* part,
+                               cudaStream_t s) const = 0;
+    // modes[0..nq): Legendre modes; weights/pows per mode; post factor; result tau (E^D per block)
+    virtual cudaError_t modes(const BlockItem* items, int nitems, int E, const void* u, int var, int nq,
+                              const int* modes, const double* weights, const double* pows, double post,
+                              void* tau, cudaStream_t s) const = 0;
+};
+
+// Factories, one per dimension (separate translation units). Return
+// nullptr when (prec, P) has no instantiation.
+Ops* make_ops_d1(int prec, int P, const ElementTables<double>& t64, const ElementTables<float>& t32);
+Ops* make_ops_d2(int prec, int P, const ElementTables<double>& t64, const ElementTables<float>& t32);
+Ops* make_ops_d3(int prec, int P, const ElementTables<double>& t64, const ElementTables<float>& t32);
+
+}  // namespace twoldg

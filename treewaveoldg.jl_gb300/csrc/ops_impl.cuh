@@ -1,0 +1,209 @@
+// The templated Ops implementation: fills the constant tables once and
+// launches the kernels of kernels.cuh with them.
+#pragma once
+#include <algorithm>
+
+#include "kernels.cuh"
+#include "ops.h"
+
+namespace twoldg {
+
+constexpr int kStageThreads = 256;
+constexpr int kMaxGrid = 152 * 64;
+
+template <typename T>
+inline const ElementTables<T>& pick(const ElementTables<double>& a, const ElementTables<float>& b);
+template <>
+inline const ElementTables<double>& pick<double>(const ElementTables<double>& a, const ElementTables<float>&) {
+    return a;
+}
+template <>
+inline const ElementTables<float>& pick<float>(const ElementTables<double>&, const ElementTables<float>& b) {
+    return b;
+}
+
+inline int grid_for(int64_t work, int threads) {
+    int64_t g = (work + threads - 1) / threads;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(g, kMaxGrid));
+}
+
+template <typename T, int D, int P, bool COMP>
+class OpsImpl : public Ops {
+    Tab<T, P> tb_;
+    CfTab<T, P> ct_;
+    ElementTables<T> et_;
+
+public:
+    int max_smem_ = 0;
+
+    explicit OpsImpl(const ElementTables<T>& t) : et_(t) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&max_smem_, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaFuncSetAttribute(stage_kernel<T, D, P, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
+        cudaFuncSetAttribute(energy_kernel<T, D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
+        cudaFuncSetAttribute(truncate_kernel<T, D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
+        cudaGetLastError();
+        const int P1 = P + 1, PW = P + 3;
+        for (int i = 0; i < P1; ++i) {
+            for (int k = 0; k < PW; ++k) tb_.W[i][k] = t.stencil[i * PW + k];
+            tb_.tm[i] = t.topmode[i];
+            tb_.td[i] = t.topdual[i];
+            tb_.wq[i] = t.weights[i];
+        }
+        for (int r = 0; r < 2 * P1; ++r)
+            for (int j = 0; j < P1; ++j) {
+                ct_.I[r][j] = t.prolong[r * P1 + j];
+                ct_.R[j][r] = t.restrict_[j * 2 * P1 + r];
+            }
+    }
+
+    static size_t smem_words(int E) {
+        size_t N = (size_t)E * (P + 1), S = N + 2, NN = 1, SS = 1;
+        for (int k = 0; k < D; ++k) { NN *= N; SS *= S; }
+        return 2 * SS + NN;
+    }
+    size_t stage_smem(int E) const override { return smem_words(E) * sizeof(T); }
+    int stage_threads() const override { return kStageThreads; }
+
+    cudaError_t export_faces(const BlockItem* items, int nitems, int E, const void* u, void* fu, void* fog,
+                             cudaStream_t s) const override {
+        int64_t F = 1;
+        for (int k = 0; k < D - 1; ++k) F *= (int64_t)E * (P + 1);
+        int64_t work = (int64_t)nitems * 2 * D * F;
+        export_faces_kernel<T, D, P><<<grid_for(work, 256), 256, 0, s>>>(
+            items, nitems, E, (const T*)u, (T*)fu, (T*)fog, tb_);
+        return cudaGetLastError();
+    }
+
+    cudaError_t cf_ghosts(const CfFace* cf, int ncf, int E, const void* fu, const void* fog, void* ugd, void* gfd,
+                          void* ggd, cudaStream_t s) const override {
+        if (ncf == 0) return cudaSuccess;
+        int64_t F = 1;
+        for (int k = 0; k < D - 1; ++k) F *= (int64_t)E * (P + 1);
+        int g = grid_for((int64_t)ncf * F, 256);
+        cf_ghost_u_kernel<T, D, P><<<g, 256, 0, s>>>(cf, ncf, E, (const T*)fu, (const T*)fog, (T*)ugd, (T*)gfd,
+                                                    tb_, ct_);
+        cf_ghost_g_kernel<T, D, P><<<g, 256, 0, s>>>(cf, ncf, E, (const T*)gfd, (T*)ggd, ct_);
+        return cudaGetLastError();
+    }
+
+    cudaError_t stage(const BlockItem* items, int nitems, int E, int mode, int truncate, const StagePtrs& p,
+                      int grid, cudaStream_t s) const override {
+        StageArgs<T> a;
+        a.items = items;
+        a.nitems = nitems;
+        a.E = E;
+        a.mode = mode;
+        a.truncate = truncate;
+        a.u = (T*)p.u;
+        a.y = (T*)p.y;
+        a.acc = (T*)p.acc;
+        a.comp = (T*)p.comp;
+        a.du = (T*)p.du;
+        a.fu_in = (const T*)p.fu_in;
+        a.fog_in = (const T*)p.fog_in;
+        a.fu_out = (T*)p.fu_out;
+        a.fog_out = (T*)p.fog_out;
+        a.ugd = (const T*)p.ugd;
+        a.ggd = (const T*)p.ggd;
+        a.dts = p.dts;
+        a.partial = p.partial;
+        size_t smem = stage_smem(E);
+        auto kern = stage_kernel<T, D, P, COMP>;
+        if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
+        if (grid <= 0) grid = std::min(nitems, kMaxGrid);
+        kern<<<grid, kStageThreads, smem, s>>>(a, tb_);
+        return cudaGetLastError();
+    }
+
+    cudaError_t energy(const BlockItem* items, int nitems, int E, const StagePtrs& p,
+                       cudaStream_t s) const override {
+        StageArgs<T> a{};
+        a.items = items;
+        a.nitems = nitems;
+        a.E = E;
+        a.u = (T*)p.u;
+        a.fu_in = (const T*)p.fu_in;
+        a.fog_in = (const T*)p.fog_in;
+        a.ugd = (const T*)p.ugd;
+        a.ggd = (const T*)p.ggd;
+        a.partial = p.partial;
+        size_t N = (size_t)E * (P + 1), SS = 1;
+        for (int k = 0; k < D; ++k) SS *= N + 2;
+        size_t smem = (SS + 1) * sizeof(T) + 32 * sizeof(double) + 16;
+        auto kern = energy_kernel<T, D, P>;
+        if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
+        kern<<<std::min(nitems, kMaxGrid), 256, smem, s>>>(a, tb_);
+        return cudaGetLastError();
+    }
+
+    cudaError_t norm(const BlockItem* items, int nitems, int E, const void* u, const void* ref, int p,
+                     int vars_mask, double* num, double* vol, cudaStream_t s) const override {
+        norm_kernel<T, D, P><<<std::min(nitems, kMaxGrid), 256, 0, s>>>(
+            items, nitems, E, (const T*)u, (const T*)ref, p, vars_mask, tb_, num, vol);
+        return cudaGetLastError();
+    }
+
+    cudaError_t truncate(const BlockItem* items, int nitems, int E, void* u, cudaStream_t s) const override {
+        size_t N = (size_t)E * (P + 1), NN = 1;
+        for (int k = 0; k < D; ++k) NN *= N;
+        size_t smem = NN * sizeof(T);
+        auto kern = truncate_kernel<T, D, P>;
+        if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
+        kern<<<std::min(nitems, kMaxGrid), 256, smem, s>>>(items, nitems, E, (T*)u, tb_);
+        return cudaGetLastError();
+    }
+
+    cudaError_t maxabs(const BlockItem* items, int nitems, int E, const void* u, int var, double* part,
+                       cudaStream_t s) const override {
+        int NN = 1;
+        for (int k = 0; k < D; ++k) NN *= E * (P + 1);
+        maxabs_kernel<T, D><<<std::min(nitems, kMaxGrid), 256, 0, s>>>(items, nitems, NN, (const T*)u, var, part);
+        return cudaGetLastError();
+    }
+
+    cudaError_t modes(const BlockItem* items, int nitems, int E, const void* u, int var, int nq, const int* modes,
+                      const double* weights, const double* pows, double post, void* tau,
+                      cudaStream_t s) const override {
+        if (nq < 1 || nq > P + 1) return cudaErrorInvalidValue;
+        ModeTab<T, P> mt{};
+        for (int q = 0; q < nq; ++q) {
+            for (int j = 0; j <= P; ++j) mt.dual[q][j] = et_.duals[modes[q] * (P + 1) + j];
+            mt.weight[q] = (T)weights[q];
+            mt.pw[q] = (T)pows[q];
+        }
+        mt.nq = nq;
+        mt.post = (T)post;
+        int64_t EE = 1;
+        for (int k = 0; k < D; ++k) EE *= E;
+        mode_kernel<T, D, P><<<grid_for((int64_t)nitems * EE, 128), 128, 0, s>>>(items, nitems, E, (const T*)u,
+                                                                                 var, mt, (T*)tau);
+        return cudaGetLastError();
+    }
+};
+
+template <int D, int P>
+Ops* make_ops_p(int prec, const ElementTables<double>& t64, const ElementTables<float>& t32) {
+    switch (prec) {
+        case PREC_F64: return new OpsImpl<double, D, P, false>(t64);
+        case PREC_F32: return new OpsImpl<float, D, P, false>(t32);
+        case PREC_F32C: return new OpsImpl<float, D, P, true>(t32);
+        default: return nullptr;
+    }
+}
+
+template <int D>
+Ops* make_ops_dim(int prec, int P, const ElementTables<double>& t64, const ElementTables<float>& t32) {
+    switch (P) {
+        case 1: return make_ops_p<D, 1>(prec, t64, t32);
+        case 2: return make_ops_p<D, 2>(prec, t64, t32);
+        case 3: return make_ops_p<D, 3>(prec, t64, t32);
+        case 4: return make_ops_p<D, 4>(prec, t64, t32);
+        case 5: return make_ops_p<D, 5>(prec, t64, t32);
+        case 6: return make_ops_p<D, 6>(prec, t64, t32);
+        default: return nullptr;
+    }
+}
+
+}  // namespace twoldg

@@ -1,0 +1,18 @@
+"""twoldg: the GB300-native OLDG field step of TreeWaveOLDG.jl.
+
+A Python mirror of the reference package's API for the field right-hand
+side and RK4 step (src/evolution.jl, src/stepping.jl, src/sinewave.jl,
+src/refinement.jl) over the C ABI of libtwoldg (include/twoldg.h), whose
+sm_103a kernels do all the arithmetic.
+"""
+from .nativebuild import build, lib_path
+from .element import Element, element_table
+from .forest import Forest, nested_cubes, refine_regions, wave_forest
+from .problem import (WaveIntegrator, WaveProblem, check_layout, initial_state, oldg_timestep,
+                      quadrature_norm, solve, truncate_stage, truncate_state, wave_energy, wave_integrator,
+                      wave_norm, wave_rhs)
+from .drivers import (convergence_rate, reflect_errors, reflect_exact, reflect_omega, wave_errors,
+                      wave_exact, wave_omega)
+from .indicator import modal_indicator, mode_amplitude
+
+__all__ = [n for n in dir() if not n.startswith("_")]

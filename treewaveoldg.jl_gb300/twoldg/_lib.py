@@ -1,0 +1,92 @@
+"""ctypes binding of libtwoldg (include/twoldg.h).
+
+The library is the only compute path: if it is not built, or the process has
+no CUDA device, the calls that need it raise instead of falling back to any
+CPU implementation.
+"""
+import ctypes
+import os
+
+from . import nativebuild as _build
+
+TWOLDG_OK, TWOLDG_EINVAL, TWOLDG_ECUDA, TWOLDG_ENOMEM, TWOLDG_EUNSUP = range(5)
+F64, F32, F32C = 0, 1, 2
+
+# Every function include/twoldg.h declares; tests check the library exports them.
+EXPORTS = [
+    "twoldg_last_error", "twoldg_version", "twoldg_element_tables",
+    "twoldg_problem_create", "twoldg_problem_destroy", "twoldg_state_words", "twoldg_min_spacing",
+    "twoldg_rhs", "twoldg_truncate", "twoldg_rk4_step", "twoldg_reset_compensation",
+    "twoldg_energy", "twoldg_norm", "twoldg_modal_indicator", "twoldg_mode_amplitude",
+    "twoldg_synchronize", "twoldg_batch_create", "twoldg_batch_destroy", "twoldg_batch_offsets",
+    "twoldg_batch_rk4_step", "twoldg_batch_synchronize",
+]
+
+
+class Desc(ctypes.Structure):
+    """twoldg_desc."""
+    _fields_ = [
+        ("dim", ctypes.c_int32), ("order", ctypes.c_int32), ("elems", ctypes.c_int32),
+        ("precision", ctypes.c_int32), ("truncate", ctypes.c_int32), ("nblocks", ctypes.c_int32),
+        ("roots", ctypes.c_int32 * 3), ("periodic", ctypes.c_int32 * 3),
+        ("reflecting", ctypes.c_int32 * 3), ("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3),
+        ("level", ctypes.POINTER(ctypes.c_int32)), ("corner", ctypes.POINTER(ctypes.c_int64)),
+    ]
+
+
+class TwoldgError(RuntimeError):
+    """A failure reported by libtwoldg (CUDA error, allocation, unsupported shape)."""
+
+
+_lib = None
+
+
+def lib():
+    """The loaded library; builds nothing, raises if it is missing."""
+    global _lib
+    if _lib is None:
+        path = _build.lib_path()
+        if not os.path.exists(path):
+            raise TwoldgError("libtwoldg.so is not built (%s): run __graft_entry__.build()" % path)
+        L = ctypes.CDLL(path)
+        vp, i32, i64, d = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+        sig = {
+            "twoldg_last_error": (ctypes.c_char_p, []),
+            "twoldg_version": (ctypes.c_char_p, []),
+            "twoldg_element_tables": (ctypes.c_int, [i32, i32, ctypes.c_char_p, vp]),
+            "twoldg_problem_create": (ctypes.c_int, [ctypes.POINTER(Desc), ctypes.POINTER(vp)]),
+            "twoldg_problem_destroy": (ctypes.c_int, [vp]),
+            "twoldg_state_words": (ctypes.c_int, [vp, ctypes.POINTER(i64)]),
+            "twoldg_min_spacing": (ctypes.c_int, [vp, ctypes.POINTER(d)]),
+            "twoldg_rhs": (ctypes.c_int, [vp, vp, vp, d]),
+            "twoldg_truncate": (ctypes.c_int, [vp, vp]),
+            "twoldg_rk4_step": (ctypes.c_int, [vp, vp, d, d, i32]),
+            "twoldg_reset_compensation": (ctypes.c_int, [vp]),
+            "twoldg_energy": (ctypes.c_int, [vp, vp, d, ctypes.POINTER(d)]),
+            "twoldg_norm": (ctypes.c_int, [vp, vp, vp, i32, i32, ctypes.POINTER(d)]),
+            "twoldg_modal_indicator": (ctypes.c_int, [vp, vp, i32, i32, vp]),
+            "twoldg_mode_amplitude": (ctypes.c_int, [vp, vp, i32, i32, vp]),
+            "twoldg_synchronize": (ctypes.c_int, [vp]),
+            "twoldg_batch_create": (ctypes.c_int, [i32, ctypes.POINTER(Desc), ctypes.POINTER(vp)]),
+            "twoldg_batch_destroy": (ctypes.c_int, [vp]),
+            "twoldg_batch_offsets": (ctypes.c_int, [vp, ctypes.POINTER(i64), ctypes.POINTER(i64)]),
+            "twoldg_batch_rk4_step": (ctypes.c_int, [vp, vp, ctypes.POINTER(d), i32]),
+            "twoldg_batch_synchronize": (ctypes.c_int, [vp]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    """Raise the library's error for a non-zero status: ValueError for a
+    rejected argument (the reference's ArgumentError), TwoldgError else."""
+    if rc == TWOLDG_OK:
+        return
+    msg = lib().twoldg_last_error().decode(errors="replace")
+    if rc == TWOLDG_EINVAL:
+        raise ValueError(msg)
+    raise TwoldgError("libtwoldg error %d: %s" % (rc, msg))
