@@ -1,0 +1,347 @@
+"""Benchmark: RK4 node-steps/s of the OLDG field step on one GB300.
+
+Workload (default): the 3D periodic uniform forest, P = 3, E = 4, roots = 16
+(4096 blocks of 16^3, 256^3 = 16.8M nodes), the standing sine mode with
+wavenumbers (1, 2, 3), dt = 0.5 h/(P+1), h = 1/256. A step is one RK4 step
+of the whole forest (4 fused stage launches replayed from a CUDA graph).
+
+Arms: the plain FP64 path (the drop-in) and the FP32-field path with FP64
+energy/time and compensated (two-sum) RK accumulation, the headline
+`value`. Both run 100 steps from the same initial data outside the timed
+region to state the L2 / Linf error against the exact solution and against
+the FP64 run, and the energy drift.
+
+--impl reference times the reference's CPU algorithm (the C oracle port,
+all host threads) on a bounded sample of the same workload; the reference
+itself is Julia and is not installed on this machine.
+
+Under torchrun (N > 1) every rank runs an independent replica (the path
+does not shard on one box: replicas only), a barrier brackets the timed
+region, and the time is the max over ranks.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "treewaveoldg.jl_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "node-steps/s on 1 GB300: mixed-precision batched vs plain FP64, at equal L2 error"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--roots", type=int, default=16)
+    ap.add_argument("--accuracy-steps", type=int, default=100)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._p = None
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", "-i", str(self.index),
+               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+               "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"]
+        try:
+            self._p = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self._p = None
+        return self
+
+    def _read(self):
+        for line in self._p.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self._p is not None:
+            self._p.terminate()
+            try:
+                self._p.wait(timeout=5)
+            except Exception:
+                self._p.kill()
+
+    def summary(self):
+        sm = [float(s[0]) for s in self.samples if len(s) >= 7 and s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if len(s) >= 7 and s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples if len(s) >= 7 for i in range(4) if s[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def c2_problem(twoldg, roots, precision):
+    dtype = np.float64 if precision == "f64" else np.float32
+    forest = twoldg.wave_forest(dtype, 3, 3, 4, roots=roots)
+    p = twoldg.WaveProblem(forest, twoldg.Element(dtype, 3), precision=precision)
+    return forest, p
+
+
+def c2_initial(x, var, T):
+    twopi = T(2 * math.pi)
+    u = np.sin(twopi * x[0]) * np.sin(twopi * T(2) * x[1]) * np.sin(twopi * T(3) * x[2])
+    return u if var == 1 else np.zeros_like(u)
+
+
+def c2_exact(x, var, t, T):
+    om = 2 * math.pi * math.sqrt(14.0)
+    s = np.sin(2 * math.pi * x[0]) * np.sin(4 * math.pi * x[1]) * np.sin(6 * math.pi * x[2])
+    return (math.cos(om * t) * s if var == 1 else -om * math.sin(om * t) * s).astype(T)
+
+
+def run_arm(twoldg, torch, precision, roots, steps, warmup, clocks_index):
+    T = np.float64 if precision == "f64" else np.float32
+    forest, p = c2_problem(twoldg, roots, precision)
+    u0 = twoldg.initial_state(p, lambda x, var: c2_initial(x, var, T))
+    dt = 0.5 * forest.minimum_spacing() / 4
+    lib = twoldg._lib.lib()
+    u = u0.clone()
+    ptr = ctypes.c_void_p(u.data_ptr())
+    stream = torch.cuda.ExternalStream(lib.twoldg_stream(p.handle))
+    torch.cuda.synchronize()
+    twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ptr, 0.0, dt, warmup))
+    p.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(clocks_index) as clk:
+        ev0.record(stream)
+        twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ptr, 0.0, dt, steps))
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    ms = max_over_ranks(ms)
+    # per-stage launch durations (events between the stage launches)
+    st = (ctypes.c_float * 4)()
+    prof = []
+    for _ in range(5):
+        twoldg._lib.check(lib.twoldg_profile_step(p.handle, ptr, dt, st))
+        prof.append(list(st))
+    stage_ms = np.min(np.array(prof), axis=0)
+    return dict(forest=forest, p=p, u0=u0, dt=dt, ms=ms, stage_ms=stage_ms, clocks=clk.summary(),
+                nodes=p.state_words // 2)
+
+
+def accuracy(twoldg, torch, arm, nsteps, ref64=None):
+    p, T = arm["p"], arm["p"].dtype.type
+    u = arm["u0"].clone()
+    if p.precision == "f32c":
+        twoldg._lib.check(twoldg._lib.lib().twoldg_reset_compensation(p.handle))
+    e0 = twoldg.wave_energy(p, u)
+    integ = twoldg.wave_integrator(p, u, 0.0, nsteps * arm["dt"], arm["dt"], alias_u0=True)
+    integ.nsteps = nsteps
+    integ.solve()
+    e1 = twoldg.wave_energy(p, u)
+    t = nsteps * arm["dt"]
+    ue = p.to_device(p.fill_at_nodes(lambda x, var: c2_exact(x, var, t, T)))
+    out = dict(l2=twoldg.quadrature_norm(p, u, 2, ref=ue), linf=twoldg.quadrature_norm(p, u, math.inf, ref=ue),
+               energy_drift=abs(e1 - e0) / e0, steps=nsteps)
+    if ref64 is not None:
+        r = ref64.to(u.dtype)
+        out["l2_vs_fp64"] = twoldg.quadrature_norm(p, u, 2, ref=r)
+        out["linf_vs_fp64"] = twoldg.quadrature_norm(p, u, math.inf, ref=r)
+    return out, u
+
+
+def e2e(twoldg, torch, arm, steps):
+    """The same metric through the public API with host buffers: every step
+    copies the state from pinned host memory, steps it, and reads it back."""
+    p = arm["p"]
+    host = arm["u0"].cpu().pin_memory()
+    dev = torch.empty_like(arm["u0"])
+    lib = twoldg._lib.lib()
+    ptr = ctypes.c_void_p(dev.data_ptr())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        dev.copy_(host, non_blocking=True)
+        torch.cuda.synchronize()
+        twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ptr, 0.0, arm["dt"], 1))
+        p.synchronize()
+        host.copy_(dev, non_blocking=True)
+        torch.cuda.synchronize()
+    sec = max_over_ranks(time.perf_counter() - t0)
+    nbytes = dev.numel() * dev.element_size()
+    return dict(value=arm["nodes"] * steps / sec * world(), unit="node-steps/s",
+                h2d_bytes_per_step=nbytes, d2h_bytes_per_step=nbytes)
+
+
+# --- multi-rank plumbing (replicas) -------------------------------------------
+_dist = None
+
+
+def world():
+    return int(os.environ.get("WORLD_SIZE", "1"))
+
+
+def rank():
+    return int(os.environ.get("RANK", "0"))
+
+
+def init_dist(torch):
+    global _dist
+    if world() > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        _dist = dist
+
+
+def barrier():
+    if _dist is not None:
+        _dist.barrier()
+
+
+def max_over_ranks(x):
+    if _dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], device="cuda" if torch.cuda.is_available() else "cpu")
+    _dist.all_reduce(t, op=_dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --- CPU baseline: the oracle port on a bounded sample --------------------------
+def cpu_sample(steps=10):
+    from oracle import oracle as orc
+    import twoldg
+    forest = twoldg.wave_forest(np.float64, 3, 3, 4, roots=8)
+    o = orc.Oracle(forest, 3)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from cases import state_from
+    u = o.truncate(state_from(forest, 3, lambda x, var: c2_initial(x, var, np.float64)))
+    dt = 0.5 * forest.minimum_spacing() / 4
+    o.rk4(u, dt, 1)  # warm-up (page-in, thread pool)
+    t0 = time.perf_counter()
+    o.rk4(u, dt, steps)
+    sec = time.perf_counter() - t0
+    nodes = len(forest.leaves) * forest.N ** 3
+    return dict(value=nodes * steps / sec, unit="node-steps/s", cores=orc.threads(), kind="port",
+                sample="%d RK4 step(s) of the 3D P=3 E=4 periodic standing mode on 8^3 blocks of 16^3 "
+                       "(%d nodes, the 256^3 box's block shape), FP64, OpenMP over blocks" % (steps, nodes))
+
+
+def reference_arm(args):
+    if rank() != 0:
+        return
+    import torch  # noqa: F401
+    sample = None
+    times = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(1)
+        if i >= args.warmup:
+            times.append(r["value"])
+        sample = r
+    value = float(np.median(times))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "node-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "3D periodic uniform forest, P=3, E=4, standing mode (1,2,3); each step "
+                                   "one RK4 step of an 8^3-block sample of the 16^3 root blocks"},
+            "cpu_baseline": {"value": value, "unit": "node-steps/s", "cores": sample["cores"], "kind": "port",
+                             "sample": sample["sample"]},
+            "e2e": {"value": value, "unit": "node-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference (Julia + TreeAMR + CUDA.jl) cannot run on this machine; its CPU algorithm "
+                    "is timed through the C oracle port"}
+    print(json.dumps(line))
+
+
+def traffic_from_profiles(precision):
+    path = os.path.join(ROOT, "profiles", "stage_kernel_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    return d.get(precision)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    import torch
+    import twoldg
+    init_dist(torch)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    twoldg.build()
+    arms = {}
+    for prec in ("f64", "f32c"):
+        arms[prec] = run_arm(twoldg, torch, prec, args.roots, args.steps, args.warmup, local)
+    acc64, u64 = accuracy(twoldg, torch, arms["f64"], args.accuracy_steps)
+    acc32, _ = accuracy(twoldg, torch, arms["f32c"], args.accuracy_steps, ref64=u64)
+    ee = e2e(twoldg, torch, arms["f32c"], max(3, args.steps // 4))
+    hbm, peak_kind = peaks()
+    head = arms["f32c"]
+    nodes = head["nodes"]
+    value = nodes * args.steps / (head["ms"] / 1e3) * world()
+    v64 = nodes * args.steps / (arms["f64"]["ms"] / 1e3) * world()
+    # algorithmic bytes per node-step: 34 words (+4 compensation words for f32c)
+    bytes_ns = {"f64": 272.0, "f32c": 152.0}
+    stage = head["stage_ms"]
+    achieved = bytes_ns["f32c"] * nodes / 4 / (float(np.mean(stage)) / 1e3) / 1e9
+    traffic = traffic_from_profiles("f32c")
+    line = {
+        "metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world(), "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "3D periodic uniform forest, P=3, E=4, roots=%d (%d blocks of 16^3, %d nodes), "
+                               "standing sine mode (1,2,3), dt=0.5h/(P+1), FP32 fields + compensated RK4"
+                               % (args.roots, len(head["forest"].leaves), nodes),
+                   "precision": "f32c", "parallelism": "replicas" if world() > 1 else "single",
+                   "l2_flush": "inputs larger than L2 (state %.0f MB + stage scratch)" % (nodes * 8 / 1e6)},
+        "fp64": {"value": v64, "ms_per_step": arms["f64"]["ms"] / args.steps,
+                 "stage_ms": [float(x) for x in arms["f64"]["stage_ms"]],
+                 "roofline_frac": bytes_ns["f64"] * nodes / 4 / (float(np.mean(arms["f64"]["stage_ms"])) / 1e3)
+                 / 1e9 / hbm},
+        "speedup_vs_fp64": value / v64,
+        "accuracy": {"fp64": acc64, "f32c": acc32},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "peak_kind": peak_kind, "kernel": "stage_kernel<float,3,3,true>",
+                     "stage_ms": [float(x) for x in stage]},
+        "clocks": head["clocks"],
+        "e2e": ee,
+        "gpu_launches": 1 + 4 * args.steps,
+    }
+    if rank() == 0 and world() == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sample(10)
+    if rank() == 0:
+        print(json.dumps(line))
+    if _dist is not None:
+        _dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -122,6 +122,14 @@ int twoldg_modal_indicator(twoldg_problem* p, const void* u, int32_t var, int32_
 /* mode_amplitude(fs, el; mode, var) -- src/refinement.jl:169-175. */
 int twoldg_mode_amplitude(twoldg_problem* p, const void* u, int32_t var, int32_t mode, void* tau_dev);
 
+/* Diagnostics (no reference counterpart): runs one RK4 step of size dt on u
+ * without the graph, with CUDA events between the four stages, and returns
+ * each stage's duration in milliseconds (stage_ms[4]). Synchronous. */
+int twoldg_profile_step(twoldg_problem* p, void* u, double dt, float* stage_ms);
+/* The problem's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or events against the library's. */
+void* twoldg_stream(twoldg_problem* p);
+
 /* Waits for all work queued on the problem's stream. */
 int twoldg_synchronize(twoldg_problem* p);
 

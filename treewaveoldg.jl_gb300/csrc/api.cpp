@@ -489,6 +489,37 @@ int twoldg_mode_amplitude(twoldg_problem* p, const void* u, int32_t var, int32_t
     return indicator(p, u, var, 1, &m, &w, &pw, 1.0, tau_dev);
 }
 
+int twoldg_profile_step(twoldg_problem* p, void* u, double dt, float* stage_ms) {
+    if (!p || !u || !stage_ms) return fail(TWOLDG_EINVAL, "NULL argument");
+    double dts = dt;
+    // make sure dt is on the device (rk4 with zero steps uploads it)
+    int r = p->rk4(u, &dts, 0);
+    if (r) return r;
+    r = p->export_all(u);
+    if (r) return r;
+    cudaEvent_t ev[5];
+    for (int i = 0; i < 5; ++i) CK(cudaEventCreate(&ev[i]));
+    int in = 0;
+    CK(cudaEventRecord(ev[0], p->stream));
+    for (int s = 1; s <= 4; ++s) {
+        for (auto& gp : p->groups) {
+            Group& g = *gp;
+            r = p->cf_all(g, in);
+            if (r) return r;
+            StagePtrs sp = p->ptrs(g, u, in);
+            CK(g.ops->stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, sp, 0, p->stream));
+        }
+        in = 1 - in;
+        CK(cudaEventRecord(ev[s], p->stream));
+    }
+    CK(cudaEventSynchronize(ev[4]));
+    for (int s = 0; s < 4; ++s) CK(cudaEventElapsedTime(&stage_ms[s], ev[s], ev[s + 1]));
+    for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
+    return TWOLDG_OK;
+}
+
+void* twoldg_stream(twoldg_problem* p) { return p ? (void*)p->stream : nullptr; }
+
 int twoldg_synchronize(twoldg_problem* p) {
     if (!p) return fail(TWOLDG_EINVAL, "NULL problem");
     CK(cudaStreamSynchronize(p->stream));

@@ -19,7 +19,7 @@ EXPORTS = [
     "twoldg_rhs", "twoldg_truncate", "twoldg_rk4_step", "twoldg_reset_compensation",
     "twoldg_energy", "twoldg_norm", "twoldg_modal_indicator", "twoldg_mode_amplitude",
     "twoldg_synchronize", "twoldg_batch_create", "twoldg_batch_destroy", "twoldg_batch_offsets",
-    "twoldg_batch_rk4_step", "twoldg_batch_synchronize",
+    "twoldg_batch_rk4_step", "twoldg_batch_synchronize", "twoldg_profile_step", "twoldg_stream",
 ]
 
 
@@ -72,6 +72,8 @@ def lib():
             "twoldg_batch_offsets": (ctypes.c_int, [vp, ctypes.POINTER(i64), ctypes.POINTER(i64)]),
             "twoldg_batch_rk4_step": (ctypes.c_int, [vp, vp, ctypes.POINTER(d), i32]),
             "twoldg_batch_synchronize": (ctypes.c_int, [vp]),
+            "twoldg_profile_step": (ctypes.c_int, [vp, vp, d, ctypes.POINTER(ctypes.c_float)]),
+            "twoldg_stream": (vp, [vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)

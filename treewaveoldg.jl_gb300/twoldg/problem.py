@@ -255,6 +255,18 @@ def oldg_timestep(p, cfl):
     return T(cfl) * T(p.forest.minimum_spacing()) / T(p.P + 1)
 
 
+def chunk_count(T, span, chunk):
+    """ceil(span / chunk), except that a quotient within a few ulp of an
+    integer m gives m (src/precision.jl:30-49, chunk_count), in type T."""
+    T = np.dtype(T).type
+    r = T(T(span) / T(chunk))
+    m = np.round(r)
+    tol = 4 * (np.spacing(r) + np.spacing(T(span)) / T(chunk))
+    if m >= 1 and abs(r - m) <= tol:
+        return int(m)
+    return int(math.ceil(r))
+
+
 class WaveIntegrator:
     """The RK4 integrator of wave_integrator (src/stepping.jl:72-78):
     truncation as stage and step limiter, fixed dt, ceil((t1-t0)/dt) steps.
@@ -269,8 +281,7 @@ class WaveIntegrator:
         self.t = float(t0)
         self.t1 = float(t1)
         self.dt = float(dt)
-        T = p.dtype.type
-        self.nsteps = int(math.ceil(T(T(t1) - T(t0)) / T(dt)))
+        self.nsteps = chunk_count(p.dtype.type, float(t1) - float(t0), float(dt))
         self.nstep = 0
 
     def _advance(self, n):
