@@ -142,14 +142,16 @@ def test_indicator_vanishes_below_its_degree(native):
 
 @pytest.mark.parametrize("case", [CASES[3], CASES[6], CASES[10]], ids=ids)
 def test_f32_paths_against_f64_oracle(native, case):
-    # float32 fields: the RHS to float32 rounding of the stencil sums, and a
+    # float32 fields: the RHS to float32 rounding of the input and of the
+    # stencil sums, which two stencil applications amplify by about
+    # (|W|_1 / h)^2 |u| / |Lap u| (4e-5 measured at h = 1/80), so 2e-4; and a
     # short RK4 run (plain and compensated) to 5e-6 of the state's scale.
     forest, p, o, u = build(case, dtype=np.float32, precision="f32")
     u0 = o.truncate(u)
     du = p.statevector()
     native.wave_rhs(du, dev(p, u0), p, 0.0)
     ref = o.rhs(u0)
-    assert rel(du.cpu().numpy(), ref) < 2e-5
+    assert rel(du.cpu().numpy(), ref) < 2e-4
     dt = 0.5 * forest.minimum_spacing() / (case[1] + 1)
     ref = o.rk4(u0, dt, 10)
     for prec in ("f32", "f32c"):
