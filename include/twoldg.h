@@ -133,6 +133,19 @@ void* twoldg_stream(twoldg_problem* p);
 /* Waits for all work queued on the problem's stream. */
 int twoldg_synchronize(twoldg_problem* p);
 
+/* The right-hand side of twoldg_rhs without any device allocation, for
+ * callers that cannot call cudaMalloc (a host that lends the library only
+ * buffers it manages itself: a fixed arena, a pool that forbids growth, an
+ * embedding runtime whose allocator must not be bypassed). No counterpart in
+ * the reference. It takes the forest's descriptor instead of a problem and
+ * keeps its scratch (work items, face exports, coarse-fine ghosts) in one
+ * file-scope device array of 16 MiB per GPU, held until exit; a forest that
+ * needs more is rejected with TWOLDG_EINVAL. The first call on a device looks
+ * the array up (cudaGetSymbolAddress) and should come before any stream
+ * capture. Calls share the array: calls that overlap on the GPU race.
+ * Asynchronous on `stream` (a cudaStream_t; NULL is the default stream). */
+int twoldg_rhs_static(const twoldg_desc* desc, void* du, const void* u, double t, void* stream);
+
 /* Batched ensemble: n independent problems stepped together, the blocks of
  * all of them as one work list per (dim, order, elems) group and one RK4
  * step per CUDA graph launch. No reference counterpart (the reference runs

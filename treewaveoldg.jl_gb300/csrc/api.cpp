@@ -81,6 +81,17 @@ struct Group {
 
 }  // namespace
 
+namespace twoldg {
+// Shared with noalloc.cu, which keeps no state of its own besides its scratch.
+int static_rhs_fail(int code, const std::string& msg) { return fail(code, msg); }
+bool static_rhs_tables(int P, const ElementTables<double>** t64, const ElementTables<float>** t32) {
+    if (!tables().get(P)) return false;
+    *t64 = &tables().t64[P];
+    *t32 = &tables().t32[P];
+    return true;
+}
+}  // namespace twoldg
+
 struct twoldg_runner {
     int prec = 0;
     size_t wsize = 8;

@@ -20,6 +20,7 @@ EXPORTS = [
     "twoldg_energy", "twoldg_norm", "twoldg_modal_indicator", "twoldg_mode_amplitude",
     "twoldg_synchronize", "twoldg_batch_create", "twoldg_batch_destroy", "twoldg_batch_offsets",
     "twoldg_batch_rk4_step", "twoldg_batch_synchronize", "twoldg_profile_step", "twoldg_stream",
+    "twoldg_rhs_static",
 ]
 
 
@@ -74,6 +75,7 @@ def lib():
             "twoldg_batch_synchronize": (ctypes.c_int, [vp]),
             "twoldg_profile_step": (ctypes.c_int, [vp, vp, d, ctypes.POINTER(ctypes.c_float)]),
             "twoldg_stream": (vp, [vp]),
+            "twoldg_rhs_static": (ctypes.c_int, [ctypes.POINTER(Desc), vp, vp, d, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
