@@ -27,6 +27,8 @@ CASES = [
     (3, 2, 2, 3, False, True),
     (3, 3, 2, 2, True, ((0.0, 0.5), (0.0, 0.5), (0.0, 0.5))),
     (1, 3, 2, 4, False, True),
+    (2, 2, 6, 2, False, False),     # E = 6: the run-time-shape kernel
+    (3, 1, 6, 1, True, False),
 ]
 
 

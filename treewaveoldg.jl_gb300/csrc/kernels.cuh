@@ -289,34 +289,149 @@ __global__ void cf_ghost_g_kernel(const CfFace* cf, int ncf, int E, const T* gfd
 }
 
 // ---------------------------------------------------------------------------
-// Loads a block's u with its face ghosts into the padded smem array su.
-template <typename T, int D, int P>
-__device__ __forceinline__ void load_u_with_ghosts(const Geo<D>& g, const BlockItem& it, const T* ysrc,
+// Block tiles. A block's u with its face ghosts lives in shared memory in a
+// padded layout with an odd x pitch (N+3), so that element lines along x,
+// which consecutive threads take at consecutive y, hit distinct banks; the
+// gradient along the current d uses the same layout, and the Laplacian
+// accumulator / new v a ghost-free layout with x pitch N+1 (odd). A shape
+// is either compile-time (ShapeC: N = E(P+1) known, all index arithmetic
+// folds to shifts and multiplies) or run-time (ShapeR, for other E).
+template <int D, int P, int E_>
+struct ShapeC {
+    static constexpr int E = E_;
+    static constexpr int P1 = P + 1;
+    static constexpr int N = E_ * (P + 1);
+    static constexpr int F = ipow(N, D - 1);
+    static constexpr int NN = ipow(N, D);
+    static constexpr int SX = N + 3, SY = N + 2;
+    static constexpr int SS = D == 1 ? SX : D == 2 ? SX * SY : SX * SY * SY;
+    static constexpr int LX = N + 1;
+    static constexpr int LS = LX * ipow(N, D - 1);
+    __device__ ShapeC(int) {}
+    __device__ static constexpr int sstride(int d) { return d == 0 ? 1 : d == 1 ? SX : SX * SY; }
+    __device__ static constexpr int lstride(int d) { return d == 0 ? 1 : d == 1 ? LX : LX * N; }
+};
+
+template <int D, int P>
+struct ShapeR {
+    static constexpr int P1 = P + 1;
+    int E, N, F, NN, SX, SY, SS, LX, LS;
+    __device__ ShapeR(int E_) : E(E_) {
+        N = E_ * P1;
+        F = 1;
+        for (int k = 0; k < D - 1; ++k) F *= N;
+        NN = F * N;
+        SX = N + 3;
+        SY = N + 2;
+        SS = D == 1 ? SX : D == 2 ? SX * SY : SX * SY * SY;
+        LX = N + 1;
+        LS = LX * F;
+    }
+    __device__ int sstride(int d) const { return d == 0 ? 1 : d == 1 ? SX : SX * SY; }
+    __device__ int lstride(int d) const { return d == 0 ? 1 : d == 1 ? LX : LX * N; }
+};
+
+// Coordinates of the node with tangential index t on the plane x_d = xd.
+template <int D, class G>
+__device__ __forceinline__ void plane_coords(const G& g, int d, int t, int xd, int (&x)[3]) {
+    x[0] = x[1] = x[2] = 0;
+    if (D == 1) { x[0] = xd; return; }
+    if (D == 2) {
+        if (d == 0) { x[0] = xd; x[1] = t; } else { x[0] = t; x[1] = xd; }
+        return;
+    }
+    const int a = t % g.N, b = t / g.N;
+    if (d == 0) { x[0] = xd; x[1] = a; x[2] = b; }
+    else if (d == 1) { x[0] = a; x[1] = xd; x[2] = b; }
+    else { x[0] = a; x[1] = b; x[2] = xd; }
+}
+
+template <int D, class G>
+__device__ __forceinline__ void owned_coords(const G& g, int n, int (&x)[3]) {
+    x[0] = n % g.N;
+    x[1] = D > 1 ? (n / g.N) % g.N : 0;
+    x[2] = D > 2 ? n / (g.N * g.N) : 0;
+}
+
+template <int D, class G>
+__device__ __forceinline__ int sidx(const G& g, const int (&x)[3]) {
+    int r = x[0] + 1;
+    if (D > 1) r += g.SX * (x[1] + 1);
+    if (D > 2) r += g.SX * g.SY * (x[2] + 1);
+    return r;
+}
+
+template <int D, class G>
+__device__ __forceinline__ int lidx(const G& g, const int (&x)[3]) {
+    int r = x[0];
+    if (D > 1) r += g.LX * x[1];
+    if (D > 2) r += g.LX * g.N * x[2];
+    return r;
+}
+
+// 16-byte vectors for the state streams.
+template <typename T>
+struct V16;
+template <>
+struct V16<float> { using type = float4; static constexpr int n = 4; };
+template <>
+struct V16<double> { using type = double2; static constexpr int n = 2; };
+
+template <typename T, int D, class G>
+__device__ __forceinline__ constexpr bool vec_ok(const G& g) {
+    return (g.N % V16<T>::n) == 0;
+}
+
+// u of the block (owned layout in global memory) into the padded su, and its
+// face ghosts: from the dense coarse-fine planes, or the neighbour's export.
+template <typename T, int D, class G>
+__device__ __forceinline__ void load_u_with_ghosts(const G& g, const BlockItem& it, const T* ysrc,
                                                    const StageArgs<T>& a, T* su) {
     const T* yu = ysrc + it.off;
-    for (int n = threadIdx.x; n < g.NN; n += blockDim.x) su[g.sidx_of_owned(n)] = yu[n];
+    constexpr int VW = V16<T>::n;
+    if (vec_ok<T, D>(g)) {
+        using V = typename V16<T>::type;
+        const V* src = reinterpret_cast<const V*>(yu);
+        for (int i = threadIdx.x; i < g.NN / VW; i += blockDim.x) {
+            V v = src[i];
+            int x[3];
+            owned_coords<D>(g, i * VW, x);
+            int s0 = sidx<D>(g, x);
+            const T* e = reinterpret_cast<const T*>(&v);
+#pragma unroll
+            for (int k = 0; k < VW; ++k) su[s0 + k] = e[k];
+        }
+    } else {
+        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
+            int x[3];
+            owned_coords<D>(g, n, x);
+            su[sidx<D>(g, x)] = yu[n];
+        }
+    }
     for (int i = threadIdx.x; i < 2 * D * g.F; i += blockDim.x) {
         int f = i / g.F, t = i % g.F;
         int d = f >> 1, side = f & 1;
         T v;
         if (it.flags & (1u << f)) v = a.ugd[(int64_t)(it.slot + f) * g.F + t];
         else v = a.fu_in[(int64_t)it.nb[f] * g.F + t];
-        su[g.sidx_face(d, t, side == 0 ? -1 : g.N)] = v;
+        int x[3];
+        plane_coords<D>(g, d, t, side == 0 ? -1 : g.N, x);
+        su[sidx<D>(g, x)] = v;
     }
 }
 
-// Gradient along d at every owned node into sg (padded layout), scaled by 1/h,
-// and the gradient ghost planes normal to d.
-template <typename T, int D, int P>
-__device__ __forceinline__ void gradient_along(const Geo<D>& g, int E, int d, const BlockItem& it,
-                                               const StageArgs<T>& a, const Tab<T, P>& tb, const T* su,
-                                               T* sg, T inv_h) {
+// Gradient along d at every owned node into sg (padded), scaled by 1/h, and
+// the two gradient ghost planes normal to d.
+template <typename T, int D, int P, class G>
+__device__ __forceinline__ void gradient_along(const G& g, int d, const BlockItem& it, const StageArgs<T>& a,
+                                               const Tab<T, P>& tb, const T* su, T* sg, T inv_h) {
     constexpr int P1 = P + 1;
     const int sd = g.sstride(d);
-    const int nlines = E * g.F;
-    for (int L = threadIdx.x; L < nlines; L += blockDim.x) {
+    for (int L = threadIdx.x; L < g.E * g.F; L += blockDim.x) {
         int t = L % g.F, e = L / g.F;
-        int base = g.sidx_face(d, t, e * P1);
+        int x[3];
+        plane_coords<D>(g, d, t, e * P1, x);
+        int base = sidx<D>(g, x);
         T w[P + 3], out[P + 1];
 #pragma unroll
         for (int k = 0; k < P + 3; ++k) w[k] = su[base + (k - 1) * sd];
@@ -327,6 +442,7 @@ __device__ __forceinline__ void gradient_along(const Geo<D>& g, int E, int d, co
     for (int i = threadIdx.x; i < 2 * g.F; i += blockDim.x) {
         int side = i / g.F, t = i % g.F;
         int f = 2 * d + side;
+        int x[3];
         T v;
         if (it.flags & (1u << f)) {
             v = a.ggd[(int64_t)(it.slot + f) * g.F + t];
@@ -334,70 +450,72 @@ __device__ __forceinline__ void gradient_along(const Geo<D>& g, int E, int d, co
             // the neighbour's face-node derivative: its own part plus its ghost
             // coefficient times its u ghost, which is this block's face node
             int nslot = it.nb[f];
-            int nside = nslot & 1;  // face index parity = side (slots are b*2D + f)
-            T own = su[g.sidx_face(d, t, side == 0 ? 0 : g.N - 1)];
+            int nside = nslot & 1;  // slots are b*2D + f, so the parity is the side
+            plane_coords<D>(g, d, t, side == 0 ? 0 : g.N - 1, x);
+            T own = su[sidx<D>(g, x)];
             T gnb = (a.fog_in[(int64_t)nslot * g.F + t] + ghost_coef<T, P>(tb, nside) * own) * inv_h;
             v = (it.flags & (1u << (8 + f))) ? -gnb : gnb;
         }
-        sg[g.sidx_face(d, t, side == 0 ? -1 : g.N)] = v;
+        plane_coords<D>(g, d, t, side == 0 ? -1 : g.N, x);
+        sg[sidx<D>(g, x)] = v;
     }
 }
 
-// Laplacian term along d: slap[n] (+)= D_d(sg) at every owned node (not yet /h).
-template <typename T, int D, int P>
-__device__ __forceinline__ void laplacian_along(const Geo<D>& g, int E, int d, const Tab<T, P>& tb,
-                                                const T* sg, T* slap, bool first) {
+// Laplacian term along d: sl (+)= D_d(sg) at every owned node (not yet /h).
+template <typename T, int D, int P, class G>
+__device__ __forceinline__ void laplacian_along(const G& g, int d, const Tab<T, P>& tb, const T* sg, T* sl,
+                                                bool first) {
     constexpr int P1 = P + 1;
-    const int sd = g.sstride(d);
-    const int od = g.ostride(d);
-    const int nlines = E * g.F;
-    for (int L = threadIdx.x; L < nlines; L += blockDim.x) {
+    const int sd = g.sstride(d), ld = g.lstride(d);
+    for (int L = threadIdx.x; L < g.E * g.F; L += blockDim.x) {
         int t = L % g.F, e = L / g.F;
-        int base = g.sidx_face(d, t, e * P1);
-        int obase = g.oidx_face(d, t, e * P1);
+        int x[3];
+        plane_coords<D>(g, d, t, e * P1, x);
+        int base = sidx<D>(g, x), lb = lidx<D>(g, x);
         T w[P + 3], out[P + 1];
 #pragma unroll
         for (int k = 0; k < P + 3; ++k) w[k] = sg[base + (k - 1) * sd];
         line_derivative<T, P>(tb, w, out);
 #pragma unroll
         for (int i = 0; i <= P; ++i) {
-            if (first) slap[obase + i * od] = out[i];
-            else slap[obase + i * od] += out[i];
+            if (first) sl[lb + i * ld] = out[i];
+            else sl[lb + i * ld] += out[i];
         }
     }
 }
 
-// Truncation of v (owned layout in sv), per element line along each d in
+// Truncation of v (ghost-free layout sv), per element line along each d in
 // turn: c = sum_j topdual_j v_j; v_i -= topmode_i c (src/evolution.jl:222-264).
 // With COMP the subtraction is error-free into the compensation words sc.
-template <typename T, int D, int P, bool COMP>
-__device__ __forceinline__ void truncate_block(const Geo<D>& g, int E, const Tab<T, P>& tb, T* sv, T* sc) {
+template <typename T, int D, int P, bool COMP, class G>
+__device__ __forceinline__ void truncate_block(const G& g, const Tab<T, P>& tb, T* sv, T* sc) {
     constexpr int P1 = P + 1;
-    const int nlines = E * g.F;
     for (int d = 0; d < D; ++d) {
-        const int od = g.ostride(d);
-        for (int L = threadIdx.x; L < nlines; L += blockDim.x) {
+        const int ld = g.lstride(d);
+        for (int L = threadIdx.x; L < g.E * g.F; L += blockDim.x) {
             int t = L % g.F, e = L / g.F;
-            int obase = g.oidx_face(d, t, e * P1);
+            int x[3];
+            plane_coords<D>(g, d, t, e * P1, x);
+            int lb = lidx<D>(g, x);
             T v[P1];
             T c = T(0);
 #pragma unroll
-            for (int j = 0; j < P1; ++j) { v[j] = sv[obase + j * od]; c += tb.td[j] * v[j]; }
+            for (int j = 0; j < P1; ++j) { v[j] = sv[lb + j * ld]; c += tb.td[j] * v[j]; }
             if (COMP) {
                 T cc = T(0);
 #pragma unroll
-                for (int j = 0; j < P1; ++j) cc += tb.td[j] * sc[obase + j * od];
+                for (int j = 0; j < P1; ++j) cc += tb.td[j] * sc[lb + j * ld];
                 c += cc;
 #pragma unroll
                 for (int i = 0; i < P1; ++i) {
                     T s, err;
                     two_sum(v[i], -(tb.tm[i] * c), s, err);
-                    sv[obase + i * od] = s;
-                    sc[obase + i * od] += err;
+                    sv[lb + i * ld] = s;
+                    sc[lb + i * ld] += err;
                 }
             } else {
 #pragma unroll
-                for (int i = 0; i < P1; ++i) sv[obase + i * od] = v[i] - tb.tm[i] * c;
+                for (int i = 0; i < P1; ++i) sv[lb + i * ld] = v[i] - tb.tm[i] * c;
             }
         }
         __syncthreads();
@@ -405,15 +523,16 @@ __device__ __forceinline__ void truncate_block(const Geo<D>& g, int E, const Tab
 }
 
 // Face export from the padded su of the new stage value.
-template <typename T, int D, int P>
-__device__ __forceinline__ void export_from_smem(const Geo<D>& g, const BlockItem& it, const Tab<T, P>& tb,
-                                                 const T* su, T* fu, T* fog) {
+template <typename T, int D, int P, class G>
+__device__ __forceinline__ void export_from_smem(const G& g, const BlockItem& it, const Tab<T, P>& tb, const T* su,
+                                                 T* fu, T* fog) {
     for (int i = threadIdx.x; i < 2 * D * g.F; i += blockDim.x) {
         int f = i / g.F, t = i % g.F;
         int d = f >> 1, side = f & 1;
         int sd = g.sstride(d);
-        int x0 = side == 0 ? 0 : g.N - 1 - P;
-        int base = g.sidx_face(d, t, x0);
+        int x[3];
+        plane_coords<D>(g, d, t, side == 0 ? 0 : g.N - 1 - P, x);
+        int base = sidx<D>(g, x);
         T e[P + 1];
 #pragma unroll
         for (int k = 0; k <= P; ++k) e[k] = su[base + k * sd];
@@ -423,96 +542,219 @@ __device__ __forceinline__ void export_from_smem(const Geo<D>& g, const BlockIte
     }
 }
 
-// ---------------------------------------------------------------------------
-// The fused stage: k = f(Y) (u' = v, v' = sum_d D_d D_d u) for one block, the
-// classic RK4 combination of that stage, the truncation of the new v and
-// the face export of the new u. acc holds only increments (dt/6 k1 + dt/3 k2
-// + dt/3 k3), added to u^n at stage 4. mode MODE_RHS writes du = f(u) only.
+// The pointwise stage combination of VW consecutive nodes (along x, in one
+// row) starting at owned index n0: k = (Y_v, lap/h), the classic RK4 update
+// of stage `mode`, u-part into su, v-part into sl (and its compensation into
+// sc at stage 4 with COMP).
+template <typename T, bool COMP, int VW>
+__device__ __forceinline__ void stage_points(int mode, double dt, const T* yv, const T* un_u, const T* un_v,
+                                             T* acc_u, T* acc_v, T* comp_u, const T* comp_v_in, const T* sl_in,
+                                             T inv_h, T (&nu)[VW], T (&nv)[VW], T (&cv)[VW]) {
+#pragma unroll
+    for (int k = 0; k < VW; ++k) {
+        T ku = yv[k];
+        T kv = sl_in[k] * inv_h;
+        T uu = un_u[k], uv = un_v[k];
+        if (mode == 1) {
+            acc_u[k] = T(dt / 6) * ku;
+            acc_v[k] = T(dt / 6) * kv;
+            nu[k] = uu + T(dt / 2) * ku;
+            nv[k] = uv + T(dt / 2) * kv;
+        } else if (mode == 2 || mode == 3) {
+            acc_u[k] += T(dt / 3) * ku;
+            acc_v[k] += T(dt / 3) * kv;
+            T c = mode == 2 ? T(dt / 2) : T(dt);
+            nu[k] = uu + c * ku;
+            nv[k] = uv + c * kv;
+        } else {
+            T iu = acc_u[k] + T(dt / 6) * ku;
+            T iv = acc_v[k] + T(dt / 6) * kv;
+            if (COMP) {
+                T cu = comp_u[k] + iu, cvv = comp_v_in[k] + iv;
+                T eu, ev;
+                two_sum(uu, cu, nu[k], eu);
+                two_sum(uv, cvv, nv[k], ev);
+                comp_u[k] = eu;
+                cv[k] = ev;
+            } else {
+                nu[k] = uu + iu;
+                nv[k] = uv + iv;
+            }
+        }
+    }
+}
+
+template <typename T, int VW>
+struct Pack {
+    T v[VW];
+};
+
+template <typename T, int VW>
+__device__ __forceinline__ Pack<T, VW> ldv(const T* p) {
+    Pack<T, VW> r;
+    if constexpr (VW == V16<T>::n) {
+        using V = typename V16<T>::type;
+        V x = *reinterpret_cast<const V*>(p);
+        const T* e = reinterpret_cast<const T*>(&x);
+#pragma unroll
+        for (int k = 0; k < VW; ++k) r.v[k] = e[k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < VW; ++k) r.v[k] = p[k];
+    }
+    return r;
+}
+
+template <typename T, int VW>
+__device__ __forceinline__ void stv(T* p, const T (&a)[VW]) {
+    if constexpr (VW == V16<T>::n) {
+        using V = typename V16<T>::type;
+        V x;
+        T* e = reinterpret_cast<T*>(&x);
+#pragma unroll
+        for (int k = 0; k < VW; ++k) e[k] = a[k];
+        *reinterpret_cast<V*>(p) = x;
+    } else {
+#pragma unroll
+        for (int k = 0; k < VW; ++k) p[k] = a[k];
+    }
+}
+
+// One block of the fused stage: k = f(Y) (u' = v, v' = sum_d D_d D_d u), the
+// RK4 combination of that stage, the truncation of the new v and the face
+// export of the new u. acc holds only increments (dt/6 k1 + dt/3 k2 + dt/3
+// k3), added to u^n at stage 4. mode MODE_RHS writes du = f(u) only.
+template <typename T, int D, int P, bool COMP, class G, int VW>
+__device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, const Tab<T, P>& tb,
+                                            const BlockItem& it, T* su, T* sg, T* sl) {
+    const int mode = a.mode;
+    const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
+    const T inv_h = T(1) / T(it.h);
+    load_u_with_ghosts<T, D>(g, it, ysrc, a, su);
+    __syncthreads();
+    for (int d = 0; d < D; ++d) {
+        gradient_along<T, D, P>(g, d, it, a, tb, su, sg, inv_h);
+        __syncthreads();
+        laplacian_along<T, D, P>(g, d, tb, sg, sl, d == 0);
+        __syncthreads();
+    }
+    const T* yv = ysrc + it.off + g.NN;
+    if (mode == MODE_RHS) {
+        T* du = a.du + it.off;
+        for (int i = threadIdx.x; i < g.NN / VW; i += blockDim.x) {
+            const int n0 = i * VW;
+            int x[3];
+            owned_coords<D>(g, n0, x);
+            const int l0 = lidx<D>(g, x);
+            Pack<T, VW> v = ldv<T, VW>(yv + n0);
+            T lap[VW];
+#pragma unroll
+            for (int k = 0; k < VW; ++k) lap[k] = sl[l0 + k] * inv_h;
+            stv<T, VW>(du + n0, v.v);
+            stv<T, VW>(du + g.NN + n0, lap);
+        }
+        __syncthreads();
+        return;
+    }
+    const double dt = a.dts[it.problem];
+    const T* un = a.u + it.off;
+    T* acc = a.acc + it.off;
+    T* comp = COMP ? a.comp + it.off : nullptr;
+    T* sc = sg;  // compensation of v during the final truncation (ghost-free layout)
+    for (int i = threadIdx.x; i < g.NN / VW; i += blockDim.x) {
+        const int n0 = i * VW;
+        int x[3];
+        owned_coords<D>(g, n0, x);
+        const int s0 = sidx<D>(g, x), l0 = lidx<D>(g, x);
+        Pack<T, VW> y = ldv<T, VW>(yv + n0);
+        Pack<T, VW> uu = ldv<T, VW>(un + n0);
+        Pack<T, VW> uv = ldv<T, VW>(un + g.NN + n0);
+        Pack<T, VW> au, av, cu, cvi;
+        if (mode != 1) {
+            au = ldv<T, VW>(acc + n0);
+            av = ldv<T, VW>(acc + g.NN + n0);
+        }
+        if (COMP && mode == MODE_STAGE4) {
+            cu = ldv<T, VW>(comp + n0);
+            cvi = ldv<T, VW>(comp + g.NN + n0);
+        }
+        T lap[VW];
+#pragma unroll
+        for (int k = 0; k < VW; ++k) lap[k] = sl[l0 + k];
+        T nu[VW], nv[VW], cv[VW];
+        stage_points<T, COMP, VW>(mode, dt, y.v, uu.v, uv.v, au.v, av.v, cu.v, cvi.v, lap, inv_h, nu, nv, cv);
+        if (mode != MODE_STAGE4) {
+            stv<T, VW>(acc + n0, au.v);
+            stv<T, VW>(acc + g.NN + n0, av.v);
+        }
+        if (COMP && mode == MODE_STAGE4) stv<T, VW>(comp + n0, cu.v);
+#pragma unroll
+        for (int k = 0; k < VW; ++k) {
+            su[s0 + k] = nu[k];
+            sl[l0 + k] = nv[k];
+            if (COMP && mode == MODE_STAGE4) sc[l0 + k] = cv[k];
+        }
+    }
+    __syncthreads();
+    const bool final_comp = COMP && mode == MODE_STAGE4;
+    if (a.truncate) {
+        if (final_comp) truncate_block<T, D, P, true>(g, tb, sl, sc);
+        else truncate_block<T, D, P, false>(g, tb, sl, sc);
+    }
+    T* out = (mode == MODE_STAGE4 ? a.u : a.y) + it.off;
+    for (int i = threadIdx.x; i < g.NN / VW; i += blockDim.x) {
+        const int n0 = i * VW;
+        int x[3];
+        owned_coords<D>(g, n0, x);
+        const int s0 = sidx<D>(g, x), l0 = lidx<D>(g, x);
+        T ou[VW], ov[VW], oc[VW];
+#pragma unroll
+        for (int k = 0; k < VW; ++k) {
+            ou[k] = su[s0 + k];
+            ov[k] = sl[l0 + k];
+            if (final_comp) oc[k] = sc[l0 + k];
+        }
+        stv<T, VW>(out + n0, ou);
+        stv<T, VW>(out + g.NN + n0, ov);
+        if (final_comp) stv<T, VW>(comp + g.NN + n0, oc);
+    }
+    export_from_smem<T, D, P>(g, it, tb, su, a.fu_out, a.fog_out);
+    __syncthreads();
+}
+
+template <typename T, int D, class G>
+__host__ __device__ constexpr size_t block_smem_words(const G& g) {
+    return 2 * (size_t)g.SS + (size_t)g.LS;
+}
+
+// Stage kernel with a compile-time shape (E known).
+template <typename T, int D, int P, int E, bool COMP, int NT>
+__global__ void __launch_bounds__(NT) stage_kernel_c(StageArgs<T> a, Tab<T, P> tb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using G = ShapeC<D, P, E>;
+    G g(E);
+    T* su = reinterpret_cast<T*>(smem_raw);
+    T* sg = su + G::SS;
+    T* sl = sg + G::SS;
+    constexpr int VW = (G::N % V16<T>::n == 0) ? V16<T>::n : 1;
+    for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+        const BlockItem& it = a.items[item];
+        stage_block<T, D, P, COMP, G, VW>(g, a, tb, it, su, sg, sl);
+    }
+}
+
+// Stage kernel for any E (run-time shape, scalar I/O).
 template <typename T, int D, int P, bool COMP>
 __global__ void __launch_bounds__(256) stage_kernel(StageArgs<T> a, Tab<T, P> tb) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* smem = reinterpret_cast<T*>(smem_raw);
-    Geo<D> g(a.E * (P + 1));
-    T* su = smem;
+    using G = ShapeR<D, P>;
+    G g(a.E);
+    T* su = reinterpret_cast<T*>(smem_raw);
     T* sg = su + g.SS;
-    T* slap = sg + g.SS;
-    const int mode = a.mode;
-    const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
-
+    T* sl = sg + g.SS;
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
-        const BlockItem it = a.items[item];
-        const T inv_h = T(1) / T(it.h);
-        load_u_with_ghosts<T, D, P>(g, it, ysrc, a, su);
-        __syncthreads();
-        for (int d = 0; d < D; ++d) {
-            gradient_along<T, D, P>(g, a.E, d, it, a, tb, su, sg, inv_h);
-            __syncthreads();
-            laplacian_along<T, D, P>(g, a.E, d, tb, sg, slap, d == 0);
-            __syncthreads();
-        }
-        const T* yv = ysrc + it.off + g.NN;
-        if (mode == MODE_RHS) {
-            T* du = a.du + it.off;
-            for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
-                du[n] = yv[n];
-                du[g.NN + n] = slap[n] * inv_h;
-            }
-            __syncthreads();
-            continue;
-        }
-        const double dt = a.dts[it.problem];
-        const T* un = a.u + it.off;
-        T* acc = a.acc + it.off;
-        T* comp = COMP ? a.comp + it.off : nullptr;
-        T* sc = sg;  // compensation of v during the final truncation
-        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
-            T ku = yv[n];
-            T kv = slap[n] * inv_h;
-            T uu = un[n], uv = un[g.NN + n];
-            T nu, nv;
-            if (mode == 1) {
-                acc[n] = T(dt / 6) * ku;
-                acc[g.NN + n] = T(dt / 6) * kv;
-                nu = uu + T(dt / 2) * ku;
-                nv = uv + T(dt / 2) * kv;
-            } else if (mode == 2 || mode == 3) {
-                acc[n] += T(dt / 3) * ku;
-                acc[g.NN + n] += T(dt / 3) * kv;
-                T c = mode == 2 ? T(dt / 2) : T(dt);
-                nu = uu + c * ku;
-                nv = uv + c * kv;
-            } else {
-                T iu = acc[n] + T(dt / 6) * ku;
-                T iv = acc[g.NN + n] + T(dt / 6) * kv;
-                if (COMP) {
-                    T cu = comp[n] + iu, cv = comp[g.NN + n] + iv;
-                    T eu, ev;
-                    two_sum(uu, cu, nu, eu);
-                    two_sum(uv, cv, nv, ev);
-                    comp[n] = eu;
-                    sc[n] = ev;
-                } else {
-                    nu = uu + iu;
-                    nv = uv + iv;
-                }
-            }
-            su[g.sidx_of_owned(n)] = nu;
-            slap[n] = nv;
-        }
-        __syncthreads();
-        const bool final_comp = COMP && mode == MODE_STAGE4;
-        if (a.truncate) {
-            if (final_comp) truncate_block<T, D, P, true>(g, a.E, tb, slap, sc);
-            else truncate_block<T, D, P, false>(g, a.E, tb, slap, sc);
-        }
-        T* out = (mode == MODE_STAGE4 ? a.u : a.y) + it.off;
-        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
-            out[n] = su[g.sidx_of_owned(n)];
-            out[g.NN + n] = slap[n];
-            if (final_comp) comp[g.NN + n] = sc[n];
-        }
-        export_from_smem<T, D, P>(g, it, tb, su, a.fu_out, a.fog_out);
-        __syncthreads();
+        const BlockItem& it = a.items[item];
+        stage_block<T, D, P, COMP, G, 1>(g, a, tb, it, su, sg, sl);
     }
 }
 
@@ -536,42 +778,38 @@ __device__ __forceinline__ double block_reduce_sum(double v, double* red) {
 template <typename T, int D, int P>
 __global__ void __launch_bounds__(256) energy_kernel(StageArgs<T> a, Tab<T, P> tb) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* smem = reinterpret_cast<T*>(smem_raw);
-    Geo<D> g(a.E * (P + 1));
-    T* su = smem;
+    using G = ShapeR<D, P>;
+    G g(a.E);
+    T* su = reinterpret_cast<T*>(smem_raw);
     double* red = reinterpret_cast<double*>(su + g.SS + (g.SS & 1));
     constexpr int P1 = P + 1;
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
-        const BlockItem it = a.items[item];
+        const BlockItem& it = a.items[item];
         const double h = it.h;
         const T inv_h = T(1) / T(h);
-        load_u_with_ghosts<T, D, P>(g, it, a.u, a, su);
+        load_u_with_ghosts<T, D>(g, it, a.u, a, su);
         __syncthreads();
         double local = 0;
         const double wscale = h * P1 / 2.0;
         const T* uv = a.u + it.off + g.NN;
         for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
+            int x[3];
+            owned_coords<D>(g, n, x);
             double w = 1.0;
-            int m = n;
-            for (int k = 0; k < D; ++k) { w *= wscale * (double)tb.wq[(m % g.N) % P1]; m /= g.N; }
+            for (int k = 0; k < D; ++k) w *= wscale * (double)tb.wq[x[k] % P1];
             double v = (double)uv[n];
             local += w * v * v;
         }
         for (int d = 0; d < D; ++d) {
             const int sd = g.sstride(d);
-            const int nlines = a.E * g.F;
-            for (int L = threadIdx.x; L < nlines; L += blockDim.x) {
+            for (int L = threadIdx.x; L < g.E * g.F; L += blockDim.x) {
                 int t = L % g.F, e = L / g.F;
-                int base = g.sidx_face(d, t, e * P1);
+                int x[3];
+                plane_coords<D>(g, d, t, e * P1, x);
+                int base = sidx<D>(g, x);
                 double wt = 1.0;
-                {
-                    int tt = t;
-                    for (int k = 0; k < D; ++k) {
-                        if (k == d) continue;
-                        wt *= wscale * (double)tb.wq[(tt % g.N) % P1];
-                        tt /= g.N;
-                    }
-                }
+                for (int k = 0; k < D; ++k)
+                    if (k != d) wt *= wscale * (double)tb.wq[x[k] % P1];
                 T w[P + 3], out[P + 1];
 #pragma unroll
                 for (int k = 0; k < P + 3; ++k) w[k] = su[base + (k - 1) * sd];
@@ -717,18 +955,27 @@ __global__ void maxabs_kernel(const BlockItem* items, int nitems, int NN, const 
 }
 
 // Standalone truncation of v (twoldg_truncate): one block per CTA, v staged
-// in shared memory.
+// in shared memory in the ghost-free layout.
 template <typename T, int D, int P>
 __global__ void truncate_kernel(const BlockItem* items, int nitems, int E, T* u, Tab<T, P> tb) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sv = reinterpret_cast<T*>(smem_raw);
-    Geo<D> g(E * (P + 1));
+    using G = ShapeR<D, P>;
+    G g(E);
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         T* v = u + items[item].off + g.NN;
-        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) sv[n] = v[n];
+        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
+            int x[3];
+            owned_coords<D>(g, n, x);
+            sv[lidx<D>(g, x)] = v[n];
+        }
         __syncthreads();
-        truncate_block<T, D, P, false>(g, E, tb, sv, nullptr);
-        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) v[n] = sv[n];
+        truncate_block<T, D, P, false>(g, tb, sv, nullptr);
+        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
+            int x[3];
+            owned_coords<D>(g, n, x);
+            v[n] = sv[lidx<D>(g, x)];
+        }
         __syncthreads();
     }
 }

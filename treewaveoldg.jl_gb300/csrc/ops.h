@@ -34,6 +34,8 @@ public:
     // bytes of dynamic shared memory the stage kernel needs for E elements per dim
     virtual size_t stage_smem(int E) const = 0;
     virtual int stage_threads() const = 0;
+    // threads per CTA of the stage kernel (0 = the shape's default); the autotuner sets it
+    virtual void set_threads(int t) = 0;
     virtual cudaError_t export_faces(const BlockItem* items, int nitems, int E, const void* u, void* fu,
                                      void* fog, cudaStream_t s) const = 0;
     virtual cudaError_t cf_ghosts(const CfFace* cf, int ncf, int E, const void* fu, const void* fog, void* ugd,

@@ -41,6 +41,10 @@ public:
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&max_smem_, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaFuncSetAttribute(stage_kernel<T, D, P, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
+        cudaFuncSetAttribute(stage_kernel_c<T, D, P, 2, COMP, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             max_smem_);
+        cudaFuncSetAttribute(stage_kernel_c<T, D, P, 4, COMP, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             max_smem_);
         cudaFuncSetAttribute(energy_kernel<T, D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         cudaFuncSetAttribute(truncate_kernel<T, D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         cudaGetLastError();
@@ -58,13 +62,29 @@ public:
             }
     }
 
-    static size_t smem_words(int E) {
-        size_t N = (size_t)E * (P + 1), S = N + 2, NN = 1, SS = 1;
-        for (int k = 0; k < D; ++k) { NN *= N; SS *= S; }
-        return 2 * SS + NN;
+    // padded u / gradient arrays: x pitch N+3, other dims N+2; ghost-free v: x pitch N+1
+    static size_t padded_words(int E) {
+        size_t N = (size_t)E * (P + 1), SS = N + 3;
+        for (int k = 1; k < D; ++k) SS *= N + 2;
+        return SS;
+    }
+    static size_t plain_words(int E) {
+        size_t N = (size_t)E * (P + 1), LS = N + 1;
+        for (int k = 1; k < D; ++k) LS *= N;
+        return LS;
+    }
+    static size_t smem_words(int E) { return 2 * padded_words(E) + plain_words(E); }
+    int threads_ = 0;  // 0: the default for the shape
+    void set_threads(int t) override { threads_ = t; }
+    int default_threads(int E) const {
+        size_t N = (size_t)E * (P + 1), NN = 1;
+        for (int k = 0; k < D; ++k) NN *= N;
+        if (NN >= 2048) return sizeof(T) == 8 ? 512 : 256;
+        if (NN >= 256) return 128;
+        return 64;
     }
     size_t stage_smem(int E) const override { return smem_words(E) * sizeof(T); }
-    int stage_threads() const override { return kStageThreads; }
+    int stage_threads() const override { return threads_ ? threads_ : kStageThreads; }
 
     cudaError_t export_faces(const BlockItem* items, int nitems, int E, const void* u, void* fu, void* fog,
                              cudaStream_t s) const override {
@@ -110,10 +130,19 @@ public:
         a.dts = p.dts;
         a.partial = p.partial;
         size_t smem = stage_smem(E);
-        auto kern = stage_kernel<T, D, P, COMP>;
         if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
         if (grid <= 0) grid = std::min(nitems, kMaxGrid);
-        kern<<<grid, kStageThreads, smem, s>>>(a, tb_);
+        // the vector path needs 16-byte aligned state pointers
+        uintptr_t al = (uintptr_t)p.u | (uintptr_t)p.y | (uintptr_t)p.acc | (uintptr_t)p.comp | (uintptr_t)p.du;
+        const bool aligned = (al & 15) == 0;
+        int nt = threads_ ? threads_ : default_threads(E);
+        if (aligned && E == 2) {
+            stage_kernel_c<T, D, P, 2, COMP, 512><<<grid, nt, smem, s>>>(a, tb_);
+        } else if (aligned && E == 4) {
+            stage_kernel_c<T, D, P, 4, COMP, 512><<<grid, nt, smem, s>>>(a, tb_);
+        } else {
+            stage_kernel<T, D, P, COMP><<<grid, std::min(nt, 256), smem, s>>>(a, tb_);
+        }
         return cudaGetLastError();
     }
 
@@ -129,9 +158,7 @@ public:
         a.ugd = (const T*)p.ugd;
         a.ggd = (const T*)p.ggd;
         a.partial = p.partial;
-        size_t N = (size_t)E * (P + 1), SS = 1;
-        for (int k = 0; k < D; ++k) SS *= N + 2;
-        size_t smem = (SS + 1) * sizeof(T) + 32 * sizeof(double) + 16;
+        size_t smem = (padded_words(E) + 1) * sizeof(T) + 32 * sizeof(double) + 16;
         auto kern = energy_kernel<T, D, P>;
         if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
         kern<<<std::min(nitems, kMaxGrid), 256, smem, s>>>(a, tb_);
@@ -146,9 +173,7 @@ public:
     }
 
     cudaError_t truncate(const BlockItem* items, int nitems, int E, void* u, cudaStream_t s) const override {
-        size_t N = (size_t)E * (P + 1), NN = 1;
-        for (int k = 0; k < D; ++k) NN *= N;
-        size_t smem = NN * sizeof(T);
+        size_t smem = plain_words(E) * sizeof(T);
         auto kern = truncate_kernel<T, D, P>;
         if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
         kern<<<std::min(nitems, kMaxGrid), 256, smem, s>>>(items, nitems, E, (T*)u, tb_);
