@@ -379,7 +379,10 @@ struct V16<double> { using type = double2; static constexpr int n = 2; };
 
 template <typename T, int D, class G>
 __device__ __forceinline__ constexpr bool vec_ok(const G& g) {
-    return (g.N % V16<T>::n) == 0;
+    // 16-byte global loads scatter into shared memory at a stride of their
+    // width, which conflicts 4-way; scalar loads are conflict-free and cost
+    // less than the replays, so the vector path stays off.
+    return false;
 }
 
 // u of the block (owned layout in global memory) into the padded su, and its
@@ -546,8 +549,19 @@ __device__ __forceinline__ void export_from_smem(const G& g, const BlockItem& it
 // row) starting at owned index n0: k = (Y_v, lap/h), the classic RK4 update
 // of stage `mode`, u-part into su, v-part into sl (and its compensation into
 // sc at stage 4 with COMP).
+// The stage's coefficients in T, computed once per block from the FP64 dt:
+// ca multiplies k into the accumulator, cn into the next stage value.
+template <typename T>
+struct RkCoef {
+    T ca, cn;
+    __device__ RkCoef(int mode, double dt) {
+        ca = mode == 1 || mode == 4 ? T(dt / 6) : T(dt / 3);
+        cn = mode == 3 ? T(dt) : T(dt / 2);
+    }
+};
+
 template <typename T, bool COMP, int VW>
-__device__ __forceinline__ void stage_points(int mode, double dt, const T* yv, const T* un_u, const T* un_v,
+__device__ __forceinline__ void stage_points(int mode, RkCoef<T> rc, const T* yv, const T* un_u, const T* un_v,
                                              T* acc_u, T* acc_v, T* comp_u, const T* comp_v_in, const T* sl_in,
                                              T inv_h, T (&nu)[VW], T (&nv)[VW], T (&cv)[VW]) {
 #pragma unroll
@@ -556,19 +570,18 @@ __device__ __forceinline__ void stage_points(int mode, double dt, const T* yv, c
         T kv = sl_in[k] * inv_h;
         T uu = un_u[k], uv = un_v[k];
         if (mode == 1) {
-            acc_u[k] = T(dt / 6) * ku;
-            acc_v[k] = T(dt / 6) * kv;
-            nu[k] = uu + T(dt / 2) * ku;
-            nv[k] = uv + T(dt / 2) * kv;
+            acc_u[k] = rc.ca * ku;
+            acc_v[k] = rc.ca * kv;
+            nu[k] = uu + rc.cn * ku;
+            nv[k] = uv + rc.cn * kv;
         } else if (mode == 2 || mode == 3) {
-            acc_u[k] += T(dt / 3) * ku;
-            acc_v[k] += T(dt / 3) * kv;
-            T c = mode == 2 ? T(dt / 2) : T(dt);
-            nu[k] = uu + c * ku;
-            nv[k] = uv + c * kv;
+            acc_u[k] += rc.ca * ku;
+            acc_v[k] += rc.ca * kv;
+            nu[k] = uu + rc.cn * ku;
+            nv[k] = uv + rc.cn * kv;
         } else {
-            T iu = acc_u[k] + T(dt / 6) * ku;
-            T iv = acc_v[k] + T(dt / 6) * kv;
+            T iu = acc_u[k] + rc.ca * ku;
+            T iv = acc_v[k] + rc.ca * kv;
             if (COMP) {
                 T cu = comp_u[k] + iu, cvv = comp_v_in[k] + iv;
                 T eu, ev;
@@ -656,7 +669,7 @@ __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, c
         __syncthreads();
         return;
     }
-    const double dt = a.dts[it.problem];
+    const RkCoef<T> rc(mode, a.dts[it.problem]);
     const T* un = a.u + it.off;
     T* acc = a.acc + it.off;
     T* comp = COMP ? a.comp + it.off : nullptr;
@@ -682,7 +695,7 @@ __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, c
 #pragma unroll
         for (int k = 0; k < VW; ++k) lap[k] = sl[l0 + k];
         T nu[VW], nv[VW], cv[VW];
-        stage_points<T, COMP, VW>(mode, dt, y.v, uu.v, uv.v, au.v, av.v, cu.v, cvi.v, lap, inv_h, nu, nv, cv);
+        stage_points<T, COMP, VW>(mode, rc, y.v, uu.v, uv.v, au.v, av.v, cu.v, cvi.v, lap, inv_h, nu, nv, cv);
         if (mode != MODE_STAGE4) {
             stv<T, VW>(acc + n0, au.v);
             stv<T, VW>(acc + g.NN + n0, av.v);
@@ -722,21 +735,34 @@ __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, c
     __syncthreads();
 }
 
-template <typename T, int D, class G>
-__host__ __device__ constexpr size_t block_smem_words(const G& g) {
-    return 2 * (size_t)g.SS + (size_t)g.LS;
-}
 
-// Stage kernel with a compile-time shape (E known).
-template <typename T, int D, int P, int E, bool COMP, int NT>
-__global__ void __launch_bounds__(NT) stage_kernel_c(StageArgs<T> a, Tab<T, P> tb) {
+// Threads per CTA and the CTAs per SM the register budget is sized for, from
+// the shape: as many CTAs as the shared memory allows (at most 4, so that a
+// thread keeps at least 64 registers), 512 threads for large FP64 blocks.
+template <typename T, int D, int P, int E>
+struct StageLaunch {
+    using G = ShapeC<D, P, E>;
+    static constexpr int NT = (sizeof(T) == 8 && G::NN >= 2048) ? 512 : 256;
+    static constexpr size_t bytes = (2 * (size_t)G::SS + (size_t)G::LS) * sizeof(T) + 1024;
+    static constexpr int by_smem = (int)((227 * 1024) / bytes);
+    static constexpr int by_regs = 65536 / (NT * 64);
+    static constexpr int MINB = by_smem < 1 ? 1 : (by_smem < by_regs ? by_smem : by_regs);
+};
+
+// Stage kernel with a compile-time shape (E known). The pointwise phases
+// touch shared memory one node per thread (consecutive threads, consecutive
+// words: no bank conflicts with the odd pitches), with coalesced scalar
+// global accesses.
+template <typename T, int D, int P, int E, bool COMP>
+__global__ void __launch_bounds__(StageLaunch<T, D, P, E>::NT, StageLaunch<T, D, P, E>::MINB)
+    stage_kernel_c(StageArgs<T> a, Tab<T, P> tb) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using G = ShapeC<D, P, E>;
     G g(E);
     T* su = reinterpret_cast<T*>(smem_raw);
     T* sg = su + G::SS;
     T* sl = sg + G::SS;
-    constexpr int VW = (G::N % V16<T>::n == 0) ? V16<T>::n : 1;
+    constexpr int VW = 1;
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         const BlockItem& it = a.items[item];
         stage_block<T, D, P, COMP, G, VW>(g, a, tb, it, su, sg, sl);

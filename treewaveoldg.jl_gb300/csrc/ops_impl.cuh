@@ -41,10 +41,12 @@ public:
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&max_smem_, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaFuncSetAttribute(stage_kernel<T, D, P, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
-        cudaFuncSetAttribute(stage_kernel_c<T, D, P, 2, COMP, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             max_smem_);
-        cudaFuncSetAttribute(stage_kernel_c<T, D, P, 4, COMP, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             max_smem_);
+        cudaFuncSetAttribute(stage_kernel_c<T, D, P, 2, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
+        cudaFuncSetAttribute(stage_kernel_c<T, D, P, 4, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
+        // the stage kernels hold whole blocks in shared memory: take the largest carveout
+        cudaFuncSetAttribute(stage_kernel<T, D, P, COMP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cudaFuncSetAttribute(stage_kernel_c<T, D, P, 2, COMP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cudaFuncSetAttribute(stage_kernel_c<T, D, P, 4, COMP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         cudaFuncSetAttribute(energy_kernel<T, D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         cudaFuncSetAttribute(truncate_kernel<T, D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         cudaGetLastError();
@@ -137,9 +139,9 @@ public:
         const bool aligned = (al & 15) == 0;
         int nt = threads_ ? threads_ : default_threads(E);
         if (aligned && E == 2) {
-            stage_kernel_c<T, D, P, 2, COMP, 512><<<grid, nt, smem, s>>>(a, tb_);
+            stage_kernel_c<T, D, P, 2, COMP><<<grid, std::min(nt, StageLaunch<T, D, P, 2>::NT), smem, s>>>(a, tb_);
         } else if (aligned && E == 4) {
-            stage_kernel_c<T, D, P, 4, COMP, 512><<<grid, nt, smem, s>>>(a, tb_);
+            stage_kernel_c<T, D, P, 4, COMP><<<grid, std::min(nt, StageLaunch<T, D, P, 4>::NT), smem, s>>>(a, tb_);
         } else {
             stage_kernel<T, D, P, COMP><<<grid, std::min(nt, 256), smem, s>>>(a, tb_);
         }
