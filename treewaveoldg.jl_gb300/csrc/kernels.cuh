@@ -385,9 +385,18 @@ __device__ __forceinline__ constexpr bool vec_ok(const G& g) {
     return false;
 }
 
+// The thread count of a block loop: the compile-time NT of a fixed-shape
+// kernel (so that trip counts and per-thread coordinates fold), or the
+// launch's for NT = 0.
+template <int NT>
+__device__ __forceinline__ int nthreads() {
+    if constexpr (NT > 0) return NT;
+    else return (int)blockDim.x;
+}
+
 // u of the block (owned layout in global memory) into the padded su, and its
 // face ghosts: from the dense coarse-fine planes, or the neighbour's export.
-template <typename T, int D, class G>
+template <typename T, int D, int NT, class G>
 __device__ __forceinline__ void load_u_with_ghosts(const G& g, const BlockItem& it, const T* ysrc,
                                                    const StageArgs<T>& a, T* su) {
     const T* yu = ysrc + it.off;
@@ -395,7 +404,8 @@ __device__ __forceinline__ void load_u_with_ghosts(const G& g, const BlockItem& 
     if (vec_ok<T, D>(g)) {
         using V = typename V16<T>::type;
         const V* src = reinterpret_cast<const V*>(yu);
-        for (int i = threadIdx.x; i < g.NN / VW; i += blockDim.x) {
+        #pragma unroll 4
+        for (int i = threadIdx.x; i < g.NN / VW; i += nthreads<NT>()) {
             V v = src[i];
             int x[3];
             owned_coords<D>(g, i * VW, x);
@@ -405,13 +415,15 @@ __device__ __forceinline__ void load_u_with_ghosts(const G& g, const BlockItem& 
             for (int k = 0; k < VW; ++k) su[s0 + k] = e[k];
         }
     } else {
-        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
+        #pragma unroll 4
+        for (int n = threadIdx.x; n < g.NN; n += nthreads<NT>()) {
             int x[3];
             owned_coords<D>(g, n, x);
             su[sidx<D>(g, x)] = yu[n];
         }
     }
-    for (int i = threadIdx.x; i < 2 * D * g.F; i += blockDim.x) {
+    #pragma unroll 4
+    for (int i = threadIdx.x; i < 2 * D * g.F; i += nthreads<NT>()) {
         int f = i / g.F, t = i % g.F;
         int d = f >> 1, side = f & 1;
         T v;
@@ -425,12 +437,13 @@ __device__ __forceinline__ void load_u_with_ghosts(const G& g, const BlockItem& 
 
 // Gradient along d at every owned node into sg (padded), scaled by 1/h, and
 // the two gradient ghost planes normal to d.
-template <typename T, int D, int P, class G>
+template <typename T, int D, int P, int NT, class G>
 __device__ __forceinline__ void gradient_along(const G& g, int d, const BlockItem& it, const StageArgs<T>& a,
                                                const Tab<T, P>& tb, const T* su, T* sg, T inv_h) {
     constexpr int P1 = P + 1;
     const int sd = g.sstride(d);
-    for (int L = threadIdx.x; L < g.E * g.F; L += blockDim.x) {
+    #pragma unroll 4
+    for (int L = threadIdx.x; L < g.E * g.F; L += nthreads<NT>()) {
         int t = L % g.F, e = L / g.F;
         int x[3];
         plane_coords<D>(g, d, t, e * P1, x);
@@ -442,7 +455,8 @@ __device__ __forceinline__ void gradient_along(const G& g, int d, const BlockIte
 #pragma unroll
         for (int i = 0; i <= P; ++i) sg[base + i * sd] = out[i] * inv_h;
     }
-    for (int i = threadIdx.x; i < 2 * g.F; i += blockDim.x) {
+    #pragma unroll 4
+    for (int i = threadIdx.x; i < 2 * g.F; i += nthreads<NT>()) {
         int side = i / g.F, t = i % g.F;
         int f = 2 * d + side;
         int x[3];
@@ -465,12 +479,13 @@ __device__ __forceinline__ void gradient_along(const G& g, int d, const BlockIte
 }
 
 // Laplacian term along d: sl (+)= D_d(sg) at every owned node (not yet /h).
-template <typename T, int D, int P, class G>
+template <typename T, int D, int P, int NT, class G>
 __device__ __forceinline__ void laplacian_along(const G& g, int d, const Tab<T, P>& tb, const T* sg, T* sl,
                                                 bool first) {
     constexpr int P1 = P + 1;
     const int sd = g.sstride(d), ld = g.lstride(d);
-    for (int L = threadIdx.x; L < g.E * g.F; L += blockDim.x) {
+    #pragma unroll 4
+    for (int L = threadIdx.x; L < g.E * g.F; L += nthreads<NT>()) {
         int t = L % g.F, e = L / g.F;
         int x[3];
         plane_coords<D>(g, d, t, e * P1, x);
@@ -490,12 +505,13 @@ __device__ __forceinline__ void laplacian_along(const G& g, int d, const Tab<T, 
 // Truncation of v (ghost-free layout sv), per element line along each d in
 // turn: c = sum_j topdual_j v_j; v_i -= topmode_i c (src/evolution.jl:222-264).
 // With COMP the subtraction is error-free into the compensation words sc.
-template <typename T, int D, int P, bool COMP, class G>
+template <typename T, int D, int P, bool COMP, int NT, class G>
 __device__ __forceinline__ void truncate_block(const G& g, const Tab<T, P>& tb, T* sv, T* sc) {
     constexpr int P1 = P + 1;
     for (int d = 0; d < D; ++d) {
         const int ld = g.lstride(d);
-        for (int L = threadIdx.x; L < g.E * g.F; L += blockDim.x) {
+        #pragma unroll 4
+        for (int L = threadIdx.x; L < g.E * g.F; L += nthreads<NT>()) {
             int t = L % g.F, e = L / g.F;
             int x[3];
             plane_coords<D>(g, d, t, e * P1, x);
@@ -526,10 +542,11 @@ __device__ __forceinline__ void truncate_block(const G& g, const Tab<T, P>& tb, 
 }
 
 // Face export from the padded su of the new stage value.
-template <typename T, int D, int P, class G>
+template <typename T, int D, int P, int NT, class G>
 __device__ __forceinline__ void export_from_smem(const G& g, const BlockItem& it, const Tab<T, P>& tb, const T* su,
                                                  T* fu, T* fog) {
-    for (int i = threadIdx.x; i < 2 * D * g.F; i += blockDim.x) {
+    #pragma unroll 4
+    for (int i = threadIdx.x; i < 2 * D * g.F; i += nthreads<NT>()) {
         int f = i / g.F, t = i % g.F;
         int d = f >> 1, side = f & 1;
         int sd = g.sstride(d);
@@ -637,24 +654,25 @@ __device__ __forceinline__ void stv(T* p, const T (&a)[VW]) {
 // RK4 combination of that stage, the truncation of the new v and the face
 // export of the new u. acc holds only increments (dt/6 k1 + dt/3 k2 + dt/3
 // k3), added to u^n at stage 4. mode MODE_RHS writes du = f(u) only.
-template <typename T, int D, int P, bool COMP, class G, int VW>
+template <typename T, int D, int P, bool COMP, int NT, class G, int VW>
 __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, const Tab<T, P>& tb,
                                             const BlockItem& it, T* su, T* sg, T* sl) {
     const int mode = a.mode;
     const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
     const T inv_h = T(1) / T(it.h);
-    load_u_with_ghosts<T, D>(g, it, ysrc, a, su);
+    load_u_with_ghosts<T, D, NT>(g, it, ysrc, a, su);
     __syncthreads();
     for (int d = 0; d < D; ++d) {
-        gradient_along<T, D, P>(g, d, it, a, tb, su, sg, inv_h);
+        gradient_along<T, D, P, NT>(g, d, it, a, tb, su, sg, inv_h);
         __syncthreads();
-        laplacian_along<T, D, P>(g, d, tb, sg, sl, d == 0);
+        laplacian_along<T, D, P, NT>(g, d, tb, sg, sl, d == 0);
         __syncthreads();
     }
     const T* yv = ysrc + it.off + g.NN;
     if (mode == MODE_RHS) {
         T* du = a.du + it.off;
-        for (int i = threadIdx.x; i < g.NN / VW; i += blockDim.x) {
+        #pragma unroll 4
+        for (int i = threadIdx.x; i < g.NN / VW; i += nthreads<NT>()) {
             const int n0 = i * VW;
             int x[3];
             owned_coords<D>(g, n0, x);
@@ -670,52 +688,66 @@ __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, c
         return;
     }
     const RkCoef<T> rc(mode, a.dts[it.problem]);
-    const T* un = a.u + it.off;
-    T* acc = a.acc + it.off;
-    T* comp = COMP ? a.comp + it.off : nullptr;
+    const T* __restrict__ un = a.u + it.off;
+    T* __restrict__ acc = a.acc + it.off;
+    T* __restrict__ comp = COMP ? a.comp + it.off : nullptr;
+    const T* __restrict__ yvr = yv;
     T* sc = sg;  // compensation of v during the final truncation (ghost-free layout)
-    for (int i = threadIdx.x; i < g.NN / VW; i += blockDim.x) {
-        const int n0 = i * VW;
-        int x[3];
-        owned_coords<D>(g, n0, x);
-        const int s0 = sidx<D>(g, x), l0 = lidx<D>(g, x);
-        Pack<T, VW> y = ldv<T, VW>(yv + n0);
-        Pack<T, VW> uu = ldv<T, VW>(un + n0);
-        Pack<T, VW> uv = ldv<T, VW>(un + g.NN + n0);
-        Pack<T, VW> au, av, cu, cvi;
-        if (mode != 1) {
-            au = ldv<T, VW>(acc + n0);
-            av = ldv<T, VW>(acc + g.NN + n0);
-        }
-        if (COMP && mode == MODE_STAGE4) {
-            cu = ldv<T, VW>(comp + n0);
-            cvi = ldv<T, VW>(comp + g.NN + n0);
-        }
-        T lap[VW];
+    // Batches of B nodes per thread: every global load of a batch is issued
+    // before the first use, so each thread keeps several in flight.
+    constexpr int B = 4;
+    const int nt = nthreads<NT>();
+    for (int j0 = 0; j0 * nt < g.NN; j0 += B) {
+        T y[B], uu[B], uv[B], au[B], av[B], cu[B], cvi[B];
 #pragma unroll
-        for (int k = 0; k < VW; ++k) lap[k] = sl[l0 + k];
-        T nu[VW], nv[VW], cv[VW];
-        stage_points<T, COMP, VW>(mode, rc, y.v, uu.v, uv.v, au.v, av.v, cu.v, cvi.v, lap, inv_h, nu, nv, cv);
-        if (mode != MODE_STAGE4) {
-            stv<T, VW>(acc + n0, au.v);
-            stv<T, VW>(acc + g.NN + n0, av.v);
+        for (int q = 0; q < B; ++q) {
+            const int n = threadIdx.x + (j0 + q) * nt;
+            if (n < g.NN) {
+                y[q] = yvr[n];
+                uu[q] = un[n];
+                uv[q] = un[g.NN + n];
+                if (mode != 1) {
+                    au[q] = acc[n];
+                    av[q] = acc[g.NN + n];
+                }
+                if (COMP && mode == MODE_STAGE4) {
+                    cu[q] = comp[n];
+                    cvi[q] = comp[g.NN + n];
+                }
+            }
         }
-        if (COMP && mode == MODE_STAGE4) stv<T, VW>(comp + n0, cu.v);
 #pragma unroll
-        for (int k = 0; k < VW; ++k) {
-            su[s0 + k] = nu[k];
-            sl[l0 + k] = nv[k];
-            if (COMP && mode == MODE_STAGE4) sc[l0 + k] = cv[k];
+        for (int q = 0; q < B; ++q) {
+            const int n = threadIdx.x + (j0 + q) * nt;
+            if (n < g.NN) {
+                int x[3];
+                owned_coords<D>(g, n, x);
+                const int s0 = sidx<D>(g, x), l0 = lidx<D>(g, x);
+                T lap[1] = {sl[l0]};
+                T nu[1], nv[1], cv[1];
+                T yq[1] = {y[q]}, uuq[1] = {uu[q]}, uvq[1] = {uv[q]}, auq[1] = {au[q]}, avq[1] = {av[q]},
+                  cuq[1] = {cu[q]}, cviq[1] = {cvi[q]};
+                stage_points<T, COMP, 1>(mode, rc, yq, uuq, uvq, auq, avq, cuq, cviq, lap, inv_h, nu, nv, cv);
+                if (mode != MODE_STAGE4) {
+                    acc[n] = auq[0];
+                    acc[g.NN + n] = avq[0];
+                }
+                if (COMP && mode == MODE_STAGE4) comp[n] = cuq[0];
+                su[s0] = nu[0];
+                sl[l0] = nv[0];
+                if (COMP && mode == MODE_STAGE4) sc[l0] = cv[0];
+            }
         }
     }
     __syncthreads();
     const bool final_comp = COMP && mode == MODE_STAGE4;
     if (a.truncate) {
-        if (final_comp) truncate_block<T, D, P, true>(g, tb, sl, sc);
-        else truncate_block<T, D, P, false>(g, tb, sl, sc);
+        if (final_comp) truncate_block<T, D, P, true, NT>(g, tb, sl, sc);
+        else truncate_block<T, D, P, false, NT>(g, tb, sl, sc);
     }
     T* out = (mode == MODE_STAGE4 ? a.u : a.y) + it.off;
-    for (int i = threadIdx.x; i < g.NN / VW; i += blockDim.x) {
+    #pragma unroll 4
+    for (int i = threadIdx.x; i < g.NN / VW; i += nthreads<NT>()) {
         const int n0 = i * VW;
         int x[3];
         owned_coords<D>(g, n0, x);
@@ -731,7 +763,7 @@ __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, c
         stv<T, VW>(out + g.NN + n0, ov);
         if (final_comp) stv<T, VW>(comp + g.NN + n0, oc);
     }
-    export_from_smem<T, D, P>(g, it, tb, su, a.fu_out, a.fog_out);
+    export_from_smem<T, D, P, NT>(g, it, tb, su, a.fu_out, a.fog_out);
     __syncthreads();
 }
 
@@ -765,7 +797,7 @@ __global__ void __launch_bounds__(StageLaunch<T, D, P, E>::NT, StageLaunch<T, D,
     constexpr int VW = 1;
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         const BlockItem& it = a.items[item];
-        stage_block<T, D, P, COMP, G, VW>(g, a, tb, it, su, sg, sl);
+        stage_block<T, D, P, COMP, StageLaunch<T, D, P, E>::NT, G, VW>(g, a, tb, it, su, sg, sl);
     }
 }
 
@@ -780,7 +812,7 @@ __global__ void __launch_bounds__(256) stage_kernel(StageArgs<T> a, Tab<T, P> tb
     T* sl = sg + g.SS;
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         const BlockItem& it = a.items[item];
-        stage_block<T, D, P, COMP, G, 1>(g, a, tb, it, su, sg, sl);
+        stage_block<T, D, P, COMP, 0, G, 1>(g, a, tb, it, su, sg, sl);
     }
 }
 
@@ -813,7 +845,7 @@ __global__ void __launch_bounds__(256) energy_kernel(StageArgs<T> a, Tab<T, P> t
         const BlockItem& it = a.items[item];
         const double h = it.h;
         const T inv_h = T(1) / T(h);
-        load_u_with_ghosts<T, D>(g, it, a.u, a, su);
+        load_u_with_ghosts<T, D, 0>(g, it, a.u, a, su);
         __syncthreads();
         double local = 0;
         const double wscale = h * P1 / 2.0;
@@ -996,7 +1028,7 @@ __global__ void truncate_kernel(const BlockItem* items, int nitems, int E, T* u,
             sv[lidx<D>(g, x)] = v[n];
         }
         __syncthreads();
-        truncate_block<T, D, P, false>(g, tb, sv, nullptr);
+        truncate_block<T, D, P, false, 0>(g, tb, sv, nullptr);
         for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
             int x[3];
             owned_coords<D>(g, n, x);
