@@ -769,12 +769,15 @@ __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, c
 
 
 // Threads per CTA and the CTAs per SM the register budget is sized for, from
-// the shape: as many CTAs as the shared memory allows (at most 4, so that a
-// thread keeps at least 64 registers), 512 threads for large FP64 blocks.
+// the shape: 64 to 256 threads by block size (512 for large FP64 blocks), and
+// as many CTAs as the shared memory allows, at most 65536 / (64 NT) so that a
+// thread keeps at least 64 registers.
 template <typename T, int D, int P, int E>
 struct StageLaunch {
     using G = ShapeC<D, P, E>;
-    static constexpr int NT = (sizeof(T) == 8 && G::NN >= 2048) ? 512 : 256;
+    // the fixed-shape kernel must be launched with exactly NT threads: its
+    // block loops stride by this constant
+    static constexpr int NT = G::NN >= 2048 ? (sizeof(T) == 8 ? 512 : 256) : G::NN >= 512 ? 128 : 64;
     static constexpr size_t bytes = (2 * (size_t)G::SS + (size_t)G::LS) * sizeof(T) + 1024;
     static constexpr int by_smem = (int)((227 * 1024) / bytes);
     static constexpr int by_regs = 65536 / (NT * 64);

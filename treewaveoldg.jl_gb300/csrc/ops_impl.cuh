@@ -139,9 +139,9 @@ public:
         const bool aligned = (al & 15) == 0;
         int nt = threads_ ? threads_ : default_threads(E);
         if (aligned && E == 2) {
-            stage_kernel_c<T, D, P, 2, COMP><<<grid, std::min(nt, StageLaunch<T, D, P, 2>::NT), smem, s>>>(a, tb_);
+            stage_kernel_c<T, D, P, 2, COMP><<<grid, StageLaunch<T, D, P, 2>::NT, smem, s>>>(a, tb_);
         } else if (aligned && E == 4) {
-            stage_kernel_c<T, D, P, 4, COMP><<<grid, std::min(nt, StageLaunch<T, D, P, 4>::NT), smem, s>>>(a, tb_);
+            stage_kernel_c<T, D, P, 4, COMP><<<grid, StageLaunch<T, D, P, 4>::NT, smem, s>>>(a, tb_);
         } else {
             stage_kernel<T, D, P, COMP><<<grid, std::min(nt, 256), smem, s>>>(a, tb_);
         }
