@@ -5,6 +5,7 @@
 
 #include "kernels.cuh"
 #include "ops.h"
+#include "stage3d.cuh"
 
 namespace twoldg {
 
@@ -43,6 +44,10 @@ public:
         cudaFuncSetAttribute(stage_kernel<T, D, P, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         cudaFuncSetAttribute(stage_kernel_c<T, D, P, 2, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         cudaFuncSetAttribute(stage_kernel_c<T, D, P, 4, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
+        if constexpr (D == 3) {
+            set_attrs(stage3d_kernel<T, P, 2, COMP>);
+            set_attrs(stage3d_kernel<T, P, 4, COMP>);
+        }
         // the stage kernels hold whole blocks in shared memory: take the largest carveout
         cudaFuncSetAttribute(stage_kernel<T, D, P, COMP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         cudaFuncSetAttribute(stage_kernel_c<T, D, P, 2, COMP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
@@ -76,6 +81,11 @@ public:
         return LS;
     }
     static size_t smem_words(int E) { return 2 * padded_words(E) + plain_words(E); }
+    template <typename K>
+    void set_attrs(K kern) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    }
     int threads_ = 0;  // 0: the default for the shape
     void set_threads(int t) override { threads_ = t; }
     int default_threads(int E) const {
@@ -138,6 +148,16 @@ public:
         uintptr_t al = (uintptr_t)p.u | (uintptr_t)p.y | (uintptr_t)p.acc | (uintptr_t)p.comp | (uintptr_t)p.du;
         const bool aligned = (al & 15) == 0;
         int nt = threads_ ? threads_ : default_threads(E);
+        if constexpr (D == 3) {
+            if (aligned && E == 2 && Stage3D<T, P, 2>::usable) {
+                stage3d_kernel<T, P, 2, COMP><<<grid, Stage3D<T, P, 2>::NT, smem, s>>>(a, tb_);
+                return cudaGetLastError();
+            }
+            if (aligned && E == 4 && Stage3D<T, P, 4>::usable) {
+                stage3d_kernel<T, P, 4, COMP><<<grid, Stage3D<T, P, 4>::NT, smem, s>>>(a, tb_);
+                return cudaGetLastError();
+            }
+        }
         if (aligned && E == 2) {
             stage_kernel_c<T, D, P, 2, COMP><<<grid, StageLaunch<T, D, P, 2>::NT, smem, s>>>(a, tb_);
         } else if (aligned && E == 4) {
