@@ -6,6 +6,7 @@
 #include "kernels.cuh"
 #include "ops.h"
 #include "stage3d.cuh"
+#include "stage3r.cuh"
 
 namespace twoldg {
 
@@ -47,6 +48,8 @@ public:
         if constexpr (D == 3) {
             set_attrs(stage3d_kernel<T, P, 2, COMP>);
             set_attrs(stage3d_kernel<T, P, 4, COMP>);
+            set_attrs(stage3r_kernel<T, P, 2, COMP>);
+            set_attrs(stage3r_kernel<T, P, 4, COMP>);
         }
         // the stage kernels hold whole blocks in shared memory: take the largest carveout
         cudaFuncSetAttribute(stage_kernel<T, D, P, COMP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
@@ -149,6 +152,16 @@ public:
         const bool aligned = (al & 15) == 0;
         int nt = threads_ ? threads_ : default_threads(E);
         if constexpr (D == 3) {
+            if (aligned && E == 2 && Stage3R<T, P, 2, COMP>::usable) {
+                using S = Stage3R<T, P, 2, COMP>;
+                stage3r_kernel<T, P, 2, COMP><<<grid, S::NT, S::words * sizeof(T), s>>>(a, tb_);
+                return cudaGetLastError();
+            }
+            if (aligned && E == 4 && Stage3R<T, P, 4, COMP>::usable) {
+                using S = Stage3R<T, P, 4, COMP>;
+                stage3r_kernel<T, P, 4, COMP><<<grid, S::NT, S::words * sizeof(T), s>>>(a, tb_);
+                return cudaGetLastError();
+            }
             if (aligned && E == 2 && Stage3D<T, P, 2>::usable) {
                 stage3d_kernel<T, P, 2, COMP><<<grid, Stage3D<T, P, 2>::NT, smem, s>>>(a, tb_);
                 return cudaGetLastError();

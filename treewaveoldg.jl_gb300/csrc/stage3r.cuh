@@ -1,0 +1,294 @@
+// The fused RK stage for 3D blocks with a compile-time shape, whole element
+// lines in registers. One thread per (a, b) position of the block's N x N
+// cross-section; in direction d a thread owns the complete line of N nodes
+// at its tangential position (all E elements), so it holds the line of u,
+// its gradient D_d u / h (with the two gradient ghosts) and the Laplacian
+// term D_d D_d u in registers: the gradient never goes through shared memory.
+// The z direction is the thread's own column, loaded from global memory
+// straight into registers, so it touches shared memory only to add its
+// Laplacian term; x and y lines read u from the padded shared copy and add
+// their terms into the ghost-free accumulator.
+//
+// The RK combination runs element by element along the column, where the
+// truncation along z is applied in registers; along x and y it is applied
+// afterwards in shared memory. The dimensions commute, so this is the same
+// projector as the generic kernel's (which applies x, y, z in turn) up to
+// rounding.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace twoldg {
+
+template <typename T, int P, int E, bool COMP>
+struct Stage3R {
+    static constexpr int P1 = P + 1;
+    static constexpr int N = E * P1;
+    static constexpr int F = N * N;
+    static constexpr int NN = N * F;
+    static constexpr int SX = N + 3, SY = N + 2, SXY = SX * SY;  // padded u
+    static constexpr int SS = SXY * SY;
+    static constexpr int LX = N + 1, LXY = LX * N;               // ghost-free accumulator / v
+    static constexpr int LS = LXY * N;
+    static constexpr int NT = F;
+    // u, the accumulator / new v, and (compensated) the compensation of v
+    static constexpr size_t words = (size_t)SS + (size_t)LS + (COMP ? (size_t)LS : 0);
+    static constexpr size_t bytes = words * sizeof(T) + 1024;
+    static constexpr int by_smem = (int)((227 * 1024) / bytes);
+    static constexpr int by_regs = 65536 / (NT * 80) > 0 ? 65536 / (NT * 80) : 1;
+    static constexpr int MINB = by_smem < 1 ? 1 : (by_smem < by_regs ? by_smem : by_regs);
+    static constexpr bool usable = F >= 64 && F <= 1024 && F % 32 == 0;
+};
+
+// Derivative of a whole line held in registers: in[0] and in[N+1] are the
+// values beyond the two faces (ghosts), in[1..N] the line; out[i] is the wide
+// derivative at node i, scaled by s.
+template <typename T, int P, int E>
+__device__ __forceinline__ void line_full(const Tab<T, P>& tb, const T (&in)[E * (P + 1) + 2],
+                                          T (&out)[E * (P + 1)], T s) {
+    constexpr int P1 = P + 1;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        T w[P + 3], o[P + 1];
+#pragma unroll
+        for (int k = 0; k < P + 3; ++k) w[k] = in[e * P1 + k];
+        line_derivative<T, P>(tb, w, o);
+#pragma unroll
+        for (int i = 0; i < P1; ++i) out[e * P1 + i] = o[i] * s;
+    }
+}
+
+// The gradient ghost of face f at this thread's face point: the dense
+// coarse-fine plane, or the neighbour's own part plus its ghost coefficient
+// times its u ghost, which is this block's own face node `own`.
+template <typename T, int P>
+__device__ __forceinline__ T grad_ghost(const StageArgs<T>& a, const Tab<T, P>& tb, const BlockItem& it, int f,
+                                        int F, int tid, T own, T inv_h) {
+    if (it.flags & (1u << f)) return a.ggd[(int64_t)(it.slot + f) * F + tid];
+    const int nslot = it.nb[f];
+    const T gnb = (a.fog_in[(int64_t)nslot * F + tid] + ghost_coef<T, P>(tb, nslot & 1) * own) * inv_h;
+    return (it.flags & (1u << (8 + f))) ? -gnb : gnb;
+}
+
+template <typename T, int P, int E, bool COMP>
+__global__ void __launch_bounds__(Stage3R<T, P, E, COMP>::NT, Stage3R<T, P, E, COMP>::MINB)
+    stage3r_kernel(StageArgs<T> a, Tab<T, P> tb) {
+    using S = Stage3R<T, P, E, COMP>;
+    constexpr int P1 = S::P1, N = S::N, F = S::F, NN = S::NN;
+    constexpr int SX = S::SX, SXY = S::SXY, LX = S::LX, LXY = S::LXY;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* su = reinterpret_cast<T*>(smem_raw);
+    T* sl = su + S::SS;
+    T* sc = sl + S::LS;  // compensated only
+    const int tid = threadIdx.x;
+    const int ca = tid % N, cb = tid / N;
+    // padded index of x_d = 0 on this thread's line along d, and the strides
+    const int s0 = 1 + SX * (ca + 1) + SXY * (cb + 1);   // x-line (x1, x2) = (ca, cb)
+    const int s1 = (ca + 1) + SX + SXY * (cb + 1);       // y-line (x0, x2) = (ca, cb)
+    const int s2 = (ca + 1) + SX * (cb + 1) + SXY;       // z-line (x0, x1) = (ca, cb)
+    const int l0 = LX * ca + LXY * cb;
+    const int l1 = ca + LXY * cb;
+    const int l2 = ca + LX * cb;
+    const int mode = a.mode;
+    const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
+
+    for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+        const BlockItem& it = a.items[item];
+        const T inv_h = T(1) / T(it.h);
+        const T* yu = ysrc + it.off;
+        // ---- z: the column in registers, straight from global memory
+        {
+            T line[N + 2];
+#pragma unroll
+            for (int j = 0; j < N; ++j) line[1 + j] = yu[tid + F * j];
+#pragma unroll
+            for (int j = 0; j < N; ++j) su[s2 + SXY * j] = line[1 + j];
+            // u ghosts: x and y faces into shared memory, z faces into the line
+#pragma unroll
+            for (int f = 0; f < 6; ++f) {
+                const int d = f >> 1, side = f & 1;
+                T v;
+                if (it.flags & (1u << f)) v = a.ugd[(int64_t)(it.slot + f) * F + tid];
+                else v = a.fu_in[(int64_t)it.nb[f] * F + tid];
+                if (d == 2) line[side ? N + 1 : 0] = v;
+                else if (d == 0) su[s0 + (side ? N : -1)] = v;
+                else su[s1 + (side ? N : -1) * SX] = v;
+            }
+            T g[N + 2], gi[N], lap[N];
+            line_full<T, P, E>(tb, line, gi, inv_h);
+#pragma unroll
+            for (int j = 0; j < N; ++j) g[1 + j] = gi[j];
+            g[0] = grad_ghost<T, P>(a, tb, it, 4, F, tid, line[1], inv_h);
+            g[N + 1] = grad_ghost<T, P>(a, tb, it, 5, F, tid, line[N], inv_h);
+            line_full<T, P, E>(tb, g, lap, T(1));
+#pragma unroll
+            for (int j = 0; j < N; ++j) sl[l2 + LXY * j] = lap[j];
+        }
+        __syncthreads();
+        // ---- x and y lines from the shared copy of u
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {
+            const int sb = d == 0 ? s0 : s1;
+            const int ss = d == 0 ? 1 : SX;
+            const int lb = d == 0 ? l0 : l1;
+            const int ls = d == 0 ? 1 : LX;
+            T line[N + 2], g[N + 2], gi[N], lap[N];
+#pragma unroll
+            for (int k = 0; k < N + 2; ++k) line[k] = su[sb + (k - 1) * ss];
+            line_full<T, P, E>(tb, line, gi, inv_h);
+#pragma unroll
+            for (int j = 0; j < N; ++j) g[1 + j] = gi[j];
+            g[0] = grad_ghost<T, P>(a, tb, it, 2 * d, F, tid, line[1], inv_h);
+            g[N + 1] = grad_ghost<T, P>(a, tb, it, 2 * d + 1, F, tid, line[N], inv_h);
+            line_full<T, P, E>(tb, g, lap, T(1));
+#pragma unroll
+            for (int j = 0; j < N; ++j) sl[lb + ls * j] += lap[j];
+            __syncthreads();
+        }
+        const T* yv = ysrc + it.off + NN;
+        if (mode == MODE_RHS) {
+            T* du = a.du + it.off;
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                du[tid + F * j] = yv[tid + F * j];
+                du[NN + tid + F * j] = sl[l2 + LXY * j] * inv_h;
+            }
+            __syncthreads();
+            continue;
+        }
+        // ---- the RK combination along the column, element by element, with the
+        // truncation along z in registers
+        const RkCoef<T> rc(mode, a.dts[it.problem]);
+        const T* __restrict__ un = a.u + it.off;
+        T* __restrict__ acc = a.acc + it.off;
+        T* __restrict__ comp = COMP ? a.comp + it.off : nullptr;
+        const bool final_comp = COMP && mode == MODE_STAGE4;
+#pragma unroll
+        for (int ez = 0; ez < E; ++ez) {
+            T y[P1], uu[P1], uv[P1], au[P1], av[P1], cu[P1], cvi[P1];
+#pragma unroll
+            for (int q = 0; q < P1; ++q) {
+                const int n = tid + F * (ez * P1 + q);
+                y[q] = yv[n];
+                uu[q] = un[n];
+                uv[q] = un[NN + n];
+                if (mode != 1) {
+                    au[q] = acc[n];
+                    av[q] = acc[NN + n];
+                }
+                if (final_comp) {
+                    cu[q] = comp[n];
+                    cvi[q] = comp[NN + n];
+                }
+            }
+            T nu[P1], nv[P1], cv[P1];
+#pragma unroll
+            for (int q = 0; q < P1; ++q) {
+                const int j = ez * P1 + q;
+                T lap[1] = {sl[l2 + LXY * j]};
+                T o_u[1], o_v[1], o_c[1];
+                T yq[1] = {y[q]}, uuq[1] = {uu[q]}, uvq[1] = {uv[q]}, auq[1] = {au[q]}, avq[1] = {av[q]},
+                  cuq[1] = {cu[q]}, cviq[1] = {cvi[q]};
+                stage_points<T, COMP, 1>(mode, rc, yq, uuq, uvq, auq, avq, cuq, cviq, lap, inv_h, o_u, o_v, o_c);
+                au[q] = auq[0];
+                av[q] = avq[0];
+                cu[q] = cuq[0];
+                nu[q] = o_u[0];
+                nv[q] = o_v[0];
+                cv[q] = o_c[0];
+            }
+            if (a.truncate) {
+                T c = T(0);
+#pragma unroll
+                for (int q = 0; q < P1; ++q) c += tb.td[q] * nv[q];
+                if (final_comp) {
+                    T cc = T(0);
+#pragma unroll
+                    for (int q = 0; q < P1; ++q) cc += tb.td[q] * cv[q];
+                    c += cc;
+#pragma unroll
+                    for (int q = 0; q < P1; ++q) {
+                        T s, err;
+                        two_sum(nv[q], -(tb.tm[q] * c), s, err);
+                        nv[q] = s;
+                        cv[q] += err;
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < P1; ++q) nv[q] = nv[q] - tb.tm[q] * c;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < P1; ++q) {
+                const int j = ez * P1 + q;
+                const int n = tid + F * j;
+                if (mode != MODE_STAGE4) {
+                    acc[n] = au[q];
+                    acc[NN + n] = av[q];
+                }
+                if (final_comp) comp[n] = cu[q];
+                su[s2 + SXY * j] = nu[q];
+                sl[l2 + LXY * j] = nv[q];
+                if (final_comp) sc[l2 + LXY * j] = cv[q];
+            }
+        }
+        __syncthreads();
+        // ---- face export of the new u (reads su only)
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+            const int d = f >> 1, side = f & 1;
+            const int sd = d == 0 ? 1 : d == 1 ? SX : SXY;
+            const int base = (d == 0 ? s0 : d == 1 ? s1 : s2) + (side ? N - 1 - P : 0) * sd;
+            T e[P + 1];
+#pragma unroll
+            for (int k = 0; k <= P; ++k) e[k] = su[base + k * sd];
+            const int64_t o = (int64_t)(it.slot + f) * F + tid;
+            a.fu_out[o] = side == 0 ? e[0] : e[P];
+            a.fog_out[o] = own_face_part<T, P>(tb, side, e);
+        }
+        // ---- truncation along x, then y, in shared memory
+        if (a.truncate) {
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                const int lb = d == 0 ? l0 : l1;
+                const int ls = d == 0 ? 1 : LX;
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const int b0 = lb + e * P1 * ls;
+                    T v[P1];
+                    T c = T(0);
+#pragma unroll
+                    for (int q = 0; q < P1; ++q) { v[q] = sl[b0 + q * ls]; c += tb.td[q] * v[q]; }
+                    if (final_comp) {
+                        T cc = T(0);
+#pragma unroll
+                        for (int q = 0; q < P1; ++q) cc += tb.td[q] * sc[b0 + q * ls];
+                        c += cc;
+#pragma unroll
+                        for (int q = 0; q < P1; ++q) {
+                            T s, err;
+                            two_sum(v[q], -(tb.tm[q] * c), s, err);
+                            sl[b0 + q * ls] = s;
+                            sc[b0 + q * ls] += err;
+                        }
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < P1; ++q) sl[b0 + q * ls] = v[q] - tb.tm[q] * c;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // ---- the new state of the column
+        T* out = (mode == MODE_STAGE4 ? a.u : a.y) + it.off;
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            out[tid + F * j] = su[s2 + SXY * j];
+            out[NN + tid + F * j] = sl[l2 + LXY * j];
+            if (final_comp) comp[NN + tid + F * j] = sc[l2 + LXY * j];
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace twoldg
