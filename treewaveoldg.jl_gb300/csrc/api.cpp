@@ -101,8 +101,9 @@ struct twoldg_runner {
     std::vector<std::unique_ptr<Group>> groups;
     std::vector<int64_t> offsets;   // per problem, words
     std::vector<double> hmin;       // per problem
-    DevBuf y, acc, comp, d_dts;
-    std::vector<double> h_dts;
+    DevBuf y, acc, comp, d_rk;
+    std::vector<double> h_dts;                 // the dt each problem's coefficients were made for
+    std::vector<unsigned char> h_rk;           // per problem dt/6, dt/3, dt/2, dt in the field type
     cudaGraphExec_t gexec = nullptr;
     void* graph_u = nullptr;
     void* comp_u = nullptr;
@@ -202,9 +203,10 @@ struct twoldg_runner {
             if (comp.alloc(sbytes) != cudaSuccess) return fail(TWOLDG_ENOMEM, "compensation allocation failed");
             CK(cudaMemset(comp.p, 0, sbytes));
         }
-        CK(d_dts.alloc(n * sizeof(double)));
+        CK(d_rk.alloc(n * 4 * wsize));
         h_dts.assign(n, 0.0);
-        CK(cudaMemcpy(d_dts.p, h_dts.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+        h_rk.assign(n * 4 * wsize, 0);
+        CK(cudaMemcpy(d_rk.p, h_rk.data(), h_rk.size(), cudaMemcpyHostToDevice));
         return TWOLDG_OK;
     }
 
@@ -221,7 +223,7 @@ struct twoldg_runner {
         p.fog_out = g.fog[1 - in].p;
         p.ugd = g.ugd.p;
         p.ggd = g.ggd.p;
-        p.dts = (const double*)d_dts.p;
+        p.rk = d_rk.p;
         p.partial = (double*)g.d_part.p;
         return p;
     }
@@ -269,7 +271,15 @@ struct twoldg_runner {
         }
         if (changed) {
             std::copy(dts, dts + nproblems, h_dts.begin());
-            CK(cudaMemcpyAsync(d_dts.p, h_dts.data(), nproblems * sizeof(double), cudaMemcpyHostToDevice, stream));
+            for (int k = 0; k < nproblems; ++k) {
+                const double c[4] = {dts[k] / 6, dts[k] / 3, dts[k] / 2, dts[k]};
+                for (int q = 0; q < 4; ++q) {
+                    unsigned char* dst = h_rk.data() + (k * 4 + q) * wsize;
+                    if (wsize == 8) std::memcpy(dst, &c[q], 8);
+                    else { float f = (float)c[q]; std::memcpy(dst, &f, 4); }
+                }
+            }
+            CK(cudaMemcpyAsync(d_rk.p, h_rk.data(), h_rk.size(), cudaMemcpyHostToDevice, stream));
             CK(cudaStreamSynchronize(stream));
         }
         if (prec == TWOLDG_F32C && comp_u != u) {

@@ -63,7 +63,7 @@ struct StageArgs {
     T* fog_out;
     const T* ugd;    // dense u ghosts (coarse-fine faces)
     const T* ggd;    // dense gradient ghosts (coarse-fine faces)
-    const double* dts;
+    const T* rk;     // per problem: dt/6, dt/3, dt/2, dt, rounded once to T on the host
     double* partial; // energy: one sum per item
 };
 
@@ -566,14 +566,15 @@ __device__ __forceinline__ void export_from_smem(const G& g, const BlockItem& it
 // row) starting at owned index n0: k = (Y_v, lap/h), the classic RK4 update
 // of stage `mode`, u-part into su, v-part into sl (and its compensation into
 // sc at stage 4 with COMP).
-// The stage's coefficients in T, computed once per block from the FP64 dt:
-// ca multiplies k into the accumulator, cn into the next stage value.
+// The stage's coefficients: ca multiplies k into the accumulator, cn into
+// the next stage value. The host forms dt/6, dt/3, dt/2 and dt in FP64 and
+// rounds each once to T.
 template <typename T>
 struct RkCoef {
     T ca, cn;
-    __device__ RkCoef(int mode, double dt) {
-        ca = mode == 1 || mode == 4 ? T(dt / 6) : T(dt / 3);
-        cn = mode == 3 ? T(dt) : T(dt / 2);
+    __device__ RkCoef(int mode, const T* rk) {
+        ca = mode == 1 || mode == 4 ? rk[0] : rk[1];
+        cn = mode == 3 ? rk[3] : rk[2];
     }
 };
 
@@ -687,7 +688,7 @@ __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, c
         __syncthreads();
         return;
     }
-    const RkCoef<T> rc(mode, a.dts[it.problem]);
+    const RkCoef<T> rc(mode, a.rk + 4 * it.problem);
     const T* __restrict__ un = a.u + it.off;
     T* __restrict__ acc = a.acc + it.off;
     T* __restrict__ comp = COMP ? a.comp + it.off : nullptr;

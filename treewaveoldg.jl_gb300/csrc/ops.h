@@ -24,7 +24,7 @@ struct StagePtrs {
     void* fog_out;
     const void* ugd;
     const void* ggd;
-    const double* dts;
+    const void* rk;    // per problem 4 RK coefficients in the field type
     double* partial;
 };
 

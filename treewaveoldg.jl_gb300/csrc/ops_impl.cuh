@@ -5,7 +5,6 @@
 
 #include "kernels.cuh"
 #include "ops.h"
-#include "stage3d.cuh"
 #include "stage3r.cuh"
 
 namespace twoldg {
@@ -46,8 +45,6 @@ public:
         cudaFuncSetAttribute(stage_kernel_c<T, D, P, 2, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         cudaFuncSetAttribute(stage_kernel_c<T, D, P, 4, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         if constexpr (D == 3) {
-            set_attrs(stage3d_kernel<T, P, 2, COMP>);
-            set_attrs(stage3d_kernel<T, P, 4, COMP>);
             set_attrs(stage3r_kernel<T, P, 2, COMP>);
             set_attrs(stage3r_kernel<T, P, 4, COMP>);
         }
@@ -142,7 +139,7 @@ public:
         a.fog_out = (T*)p.fog_out;
         a.ugd = (const T*)p.ugd;
         a.ggd = (const T*)p.ggd;
-        a.dts = p.dts;
+        a.rk = (const T*)p.rk;
         a.partial = p.partial;
         size_t smem = stage_smem(E);
         if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
@@ -160,14 +157,6 @@ public:
             if (aligned && E == 4 && Stage3R<T, P, 4, COMP>::usable) {
                 using S = Stage3R<T, P, 4, COMP>;
                 stage3r_kernel<T, P, 4, COMP><<<grid, S::NT, S::words * sizeof(T), s>>>(a, tb_);
-                return cudaGetLastError();
-            }
-            if (aligned && E == 2 && Stage3D<T, P, 2>::usable) {
-                stage3d_kernel<T, P, 2, COMP><<<grid, Stage3D<T, P, 2>::NT, smem, s>>>(a, tb_);
-                return cudaGetLastError();
-            }
-            if (aligned && E == 4 && Stage3D<T, P, 4>::usable) {
-                stage3d_kernel<T, P, 4, COMP><<<grid, Stage3D<T, P, 4>::NT, smem, s>>>(a, tb_);
                 return cudaGetLastError();
             }
         }

@@ -58,16 +58,16 @@ __device__ __forceinline__ void line_full(const Tab<T, P>& tb, const T (&in)[E *
     }
 }
 
-// The gradient ghost of face f at this thread's face point: the dense
-// coarse-fine plane, or the neighbour's own part plus its ghost coefficient
-// times its u ghost, which is this block's own face node `own`.
+// The gradient ghost of face f at this thread's face point, from the value
+// prefetched for it: the dense coarse-fine plane's, or the neighbour's own
+// part `pre` plus its ghost coefficient times its u ghost, which is this
+// block's own face node `own`.
 template <typename T, int P>
-__device__ __forceinline__ T grad_ghost(const StageArgs<T>& a, const Tab<T, P>& tb, const BlockItem& it, int f,
-                                        int F, int tid, T own, T inv_h) {
-    if (it.flags & (1u << f)) return a.ggd[(int64_t)(it.slot + f) * F + tid];
-    const int nslot = it.nb[f];
-    const T gnb = (a.fog_in[(int64_t)nslot * F + tid] + ghost_coef<T, P>(tb, nslot & 1) * own) * inv_h;
-    return (it.flags & (1u << (8 + f))) ? -gnb : gnb;
+__device__ __forceinline__ T grad_ghost(const Tab<T, P>& tb, uint32_t flags, int nslot, int f, T pre, T own,
+                                        T inv_h) {
+    if (flags & (1u << f)) return pre;
+    const T gnb = (pre + ghost_coef<T, P>(tb, nslot & 1) * own) * inv_h;
+    return (flags & (1u << (8 + f))) ? -gnb : gnb;
 }
 
 template <typename T, int P, int E, bool COMP>
@@ -94,32 +94,45 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP>::NT, Stage3R<T, P, E, C
 
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         const BlockItem& it = a.items[item];
+        const uint32_t flags = it.flags;
+        const int slot = it.slot;
+        int nb[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) nb[f] = it.nb[f];
         const T inv_h = T(1) / T(it.h);
         const T* yu = ysrc + it.off;
-        // ---- z: the column in registers, straight from global memory
-        {
-            T line[N + 2];
+        // every global load of the block's prologue at once: the column, the u
+        // ghosts and the neighbours' gradient parts at this face point
+        T line[N + 2];
 #pragma unroll
-            for (int j = 0; j < N; ++j) line[1 + j] = yu[tid + F * j];
+        for (int j = 0; j < N; ++j) line[1 + j] = yu[tid + F * j];
+        T ug[6], gp[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+            if (flags & (1u << f)) {
+                ug[f] = a.ugd[(int64_t)(slot + f) * F + tid];
+                gp[f] = a.ggd[(int64_t)(slot + f) * F + tid];
+            } else {
+                ug[f] = a.fu_in[(int64_t)nb[f] * F + tid];
+                gp[f] = a.fog_in[(int64_t)nb[f] * F + tid];
+            }
+        }
+        // ---- z: the column in registers
+        {
 #pragma unroll
             for (int j = 0; j < N; ++j) su[s2 + SXY * j] = line[1 + j];
-            // u ghosts: x and y faces into shared memory, z faces into the line
-#pragma unroll
-            for (int f = 0; f < 6; ++f) {
-                const int d = f >> 1, side = f & 1;
-                T v;
-                if (it.flags & (1u << f)) v = a.ugd[(int64_t)(it.slot + f) * F + tid];
-                else v = a.fu_in[(int64_t)it.nb[f] * F + tid];
-                if (d == 2) line[side ? N + 1 : 0] = v;
-                else if (d == 0) su[s0 + (side ? N : -1)] = v;
-                else su[s1 + (side ? N : -1) * SX] = v;
-            }
+            su[s0 - 1] = ug[0];
+            su[s0 + N] = ug[1];
+            su[s1 - SX] = ug[2];
+            su[s1 + N * SX] = ug[3];
+            line[0] = ug[4];
+            line[N + 1] = ug[5];
             T g[N + 2], gi[N], lap[N];
             line_full<T, P, E>(tb, line, gi, inv_h);
 #pragma unroll
             for (int j = 0; j < N; ++j) g[1 + j] = gi[j];
-            g[0] = grad_ghost<T, P>(a, tb, it, 4, F, tid, line[1], inv_h);
-            g[N + 1] = grad_ghost<T, P>(a, tb, it, 5, F, tid, line[N], inv_h);
+            g[0] = grad_ghost<T, P>(tb, flags, nb[4], 4, gp[4], line[1], inv_h);
+            g[N + 1] = grad_ghost<T, P>(tb, flags, nb[5], 5, gp[5], line[N], inv_h);
             line_full<T, P, E>(tb, g, lap, T(1));
 #pragma unroll
             for (int j = 0; j < N; ++j) sl[l2 + LXY * j] = lap[j];
@@ -132,14 +145,14 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP>::NT, Stage3R<T, P, E, C
             const int ss = d == 0 ? 1 : SX;
             const int lb = d == 0 ? l0 : l1;
             const int ls = d == 0 ? 1 : LX;
-            T line[N + 2], g[N + 2], gi[N], lap[N];
+            T g[N + 2], gi[N], lap[N];
 #pragma unroll
             for (int k = 0; k < N + 2; ++k) line[k] = su[sb + (k - 1) * ss];
             line_full<T, P, E>(tb, line, gi, inv_h);
 #pragma unroll
             for (int j = 0; j < N; ++j) g[1 + j] = gi[j];
-            g[0] = grad_ghost<T, P>(a, tb, it, 2 * d, F, tid, line[1], inv_h);
-            g[N + 1] = grad_ghost<T, P>(a, tb, it, 2 * d + 1, F, tid, line[N], inv_h);
+            g[0] = grad_ghost<T, P>(tb, flags, nb[2 * d], 2 * d, gp[2 * d], line[1], inv_h);
+            g[N + 1] = grad_ghost<T, P>(tb, flags, nb[2 * d + 1], 2 * d + 1, gp[2 * d + 1], line[N], inv_h);
             line_full<T, P, E>(tb, g, lap, T(1));
 #pragma unroll
             for (int j = 0; j < N; ++j) sl[lb + ls * j] += lap[j];
@@ -158,7 +171,7 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP>::NT, Stage3R<T, P, E, C
         }
         // ---- the RK combination along the column, element by element, with the
         // truncation along z in registers
-        const RkCoef<T> rc(mode, a.dts[it.problem]);
+        const RkCoef<T> rc(mode, a.rk + 4 * it.problem);
         const T* __restrict__ un = a.u + it.off;
         T* __restrict__ acc = a.acc + it.off;
         T* __restrict__ comp = COMP ? a.comp + it.off : nullptr;
@@ -242,7 +255,7 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP>::NT, Stage3R<T, P, E, C
             T e[P + 1];
 #pragma unroll
             for (int k = 0; k <= P; ++k) e[k] = su[base + k * sd];
-            const int64_t o = (int64_t)(it.slot + f) * F + tid;
+            const int64_t o = (int64_t)(slot + f) * F + tid;
             a.fu_out[o] = side == 0 ? e[0] : e[P];
             a.fog_out[o] = own_face_part<T, P>(tb, side, e);
         }
