@@ -281,12 +281,17 @@ def reference_arm(args):
 
 
 def traffic_from_profiles(precision):
-    path = os.path.join(ROOT, "profiles", "stage_kernel_traffic.json")
+    """DRAM bytes per stage launch measured by ncu for this workload
+    (profiles/stage_kernel_traffic.txt: "<precision> <bytes>" lines)."""
+    path = os.path.join(ROOT, "profiles", "stage_kernel_traffic.txt")
     if not os.path.exists(path):
         return None
     with open(path) as f:
-        d = json.load(f)
-    return d.get(precision)
+        for line in f:
+            parts = line.split()
+            if len(parts) == 2 and parts[0] == precision:
+                return float(parts[1])
+    return None
 
 
 def main():
@@ -341,7 +346,8 @@ def main():
         "speedup_vs_fp64": value / v64,
         "accuracy": {"fp64": acc64, "f32c": acc32},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "peak_kind": peak_kind, "kernel": "stage_kernel<float,3,3,true>",
+                     "traffic": traffic, "peak_kind": peak_kind, "kernel": "stage3r_kernel<float,3,4,compensated>",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per stage launch, profiles/stage3r_f32c_256cube.md",
                      "stage_ms": [float(x) for x in stage]},
         "clocks": head["clocks"],
         "e2e": ee,
