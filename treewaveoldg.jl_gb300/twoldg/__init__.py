@@ -14,5 +14,6 @@ from .problem import (WaveIntegrator, WaveProblem, check_layout, initial_state, 
 from .drivers import (convergence_rate, reflect_errors, reflect_exact, reflect_omega, wave_errors,
                       wave_exact, wave_omega)
 from .indicator import modal_indicator, mode_amplitude
+from .batch import Batch, fill_batch, sine_ensemble
 
 __all__ = [n for n in dir() if not n.startswith("_")]
