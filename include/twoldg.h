@@ -61,6 +61,20 @@ typedef struct twoldg_desc {
     double hi[3];
     const int32_t* level;    /* nblocks */
     const int64_t* corner;   /* nblocks * dim */
+    /* Optional diagonal metric (a geometry such as the polar annulus,
+     * src/evolution.jl:513-708): NULL for the flat problem. coef holds, per
+     * block, the node values of sqrt(g), A_1 .. A_D with A_d = sqrt(g) g^dd,
+     * laid out (N^D, 1 + D, nblocks) column-major like the state; the gradient
+     * then holds the flux A_d D_d u and the Laplacian divides by sqrt(g).
+     * trunc_modes / trunc_duals hold the truncation's rank-one pair of every
+     * element line, orthogonal in the sqrt(g)-factor-weighted inner product
+     * (MetricTruncation, src/evolution.jl:556-622): for each dimension d, block
+     * b and element index e along d, P+1 values, laid out (P+1, E, nblocks, D)
+     * column-major. Both are rounded once to the field type. A problem with a
+     * metric takes no coarse-fine faces and no batching. */
+    const double* coef;
+    const double* trunc_modes;
+    const double* trunc_duals;
 } twoldg_desc;
 
 typedef struct twoldg_problem twoldg_problem;

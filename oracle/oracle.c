@@ -47,6 +47,12 @@ typedef struct {
     const double* stencil;   /* (P+1) x (P+3) row-major */
     const double* projector; /* (P+1) x (P+1) row-major */
     const double* duals;     /* (P+1) x (P+1) row-major */
+    /* diagonal metric (NULL: flat): node values sqrt(g), A_1..A_D per block,
+     * (N^D, 1+D, nblocks) column-major; and the sqrt(g) factor along each
+     * element line at its nodes, (P+1, E, nblocks, D), from which the oracle
+     * builds the line's orthogonal projector itself */
+    const double* coef;
+    const double* line_weights;
 } oracle_mesh;
 
 typedef struct {
@@ -227,7 +233,8 @@ static double ghost_value(const ctx_t* c, int b, int d, int side, const int* x, 
 
 /* D_d a / h at every owned node of block b, with a's ghosts across the two
  * faces normal to d (src/evolution.jl:24-35). */
-static void derivative_block(const ctx_t* c, int b, int d, const double* a, double parity, double* out) {
+static void derivative_block(const ctx_t* c, int b, int d, const double* a, double parity, double* out,
+                             const double* scale) {
     const oracle_mesh* m = c->m;
     const int N = c->N, P1 = c->P1, PW = m->P + 3;
     const double h = spacing(c, b);
@@ -255,6 +262,7 @@ static void derivative_block(const ctx_t* c, int b, int d, const double* a, doub
             acc += m->stencil[i * PW + k] * val;
         }
         out[n] = acc / h;
+        if (scale) out[n] *= scale[n];
     }
 }
 
@@ -270,7 +278,9 @@ int oracle_rhs(const oracle_mesh* m, const double* u, double* du) {
     for (int64_t b = 0; b < nb; ++b) memcpy(ua + b * NN, u + b * 2 * NN, sizeof(double) * NN);
 #pragma omp parallel for schedule(dynamic)
     for (int64_t b = 0; b < nb; ++b)
-        for (int d = 0; d < D; ++d) derivative_block(&c, (int)b, d, ua, 1.0, g + (int64_t)d * NN * nb + b * NN);
+        for (int d = 0; d < D; ++d)
+            derivative_block(&c, (int)b, d, ua, 1.0, g + (int64_t)d * NN * nb + b * NN,
+                             m->coef ? m->coef + (b * (1 + D) + 1 + d) * NN : NULL);
 #pragma omp parallel
     {
         double* tmp = (double*)malloc(sizeof(double) * NN);
@@ -279,9 +289,12 @@ int oracle_rhs(const oracle_mesh* m, const double* u, double* du) {
             double* dv = du + b * 2 * NN + NN;
             for (int64_t n = 0; n < NN; ++n) dv[n] = 0.0;
             for (int d = 0; d < D; ++d) {
-                derivative_block(&c, (int)b, d, g + (int64_t)d * NN * nb, -1.0, tmp);
+                derivative_block(&c, (int)b, d, g + (int64_t)d * NN * nb, -1.0, tmp, NULL);
                 for (int64_t n = 0; n < NN; ++n) dv[n] += tmp[n];
             }
+            /* on a geometry: sqrt(g) v' = sum_d D_d F_d */
+            if (m->coef)
+                for (int64_t n = 0; n < NN; ++n) dv[n] /= m->coef[b * (1 + D) * NN + n];
             memcpy(du + b * 2 * NN, u + b * 2 * NN + NN, sizeof(double) * NN);
         }
         free(tmp);
@@ -295,6 +308,54 @@ int oracle_rhs(const oracle_mesh* m, const double* u, double* du) {
 /* The reference's Laplacian divides the summed second derivatives by h once,
  * with each gradient already divided by h: D_d(D_d u / h) / h. The routine
  * above divides both passes' stencil sums by h, which is the same value. */
+
+/* The line's projector onto degree < P orthogonal in sum_i w_i a_i f_i g_i:
+ * Pi = I - phi (x) dual with phi = L_P less its projection on L_0..L_{P-1},
+ * dual = w a phi / gamma (src/evolution.jl:578-622), in long double. */
+static void line_projector(const oracle_mesh* m, const double* a, double* Pi) {
+    const int P = m->P, P1 = P + 1;
+    long double L[16][16], G[16][17], phi[16], c[16];
+    for (int i = 0; i < P1; ++i) {
+        long double x = m->nodes[i];
+        L[0][i] = 1.0L;
+        if (P >= 1) L[1][i] = x;
+        for (int k = 2; k <= P; ++k) L[k][i] = ((2 * k - 1) * x * L[k - 1][i] - (k - 1) * L[k - 2][i]) / k;
+    }
+    for (int k = 0; k < P; ++k) {
+        for (int l = 0; l < P; ++l) {
+            long double s = 0;
+            for (int i = 0; i < P1; ++i) s += (long double)m->weights[i] * a[i] * L[k][i] * L[l][i];
+            G[k][l] = s;
+        }
+        long double r = 0;
+        for (int i = 0; i < P1; ++i) r += (long double)m->weights[i] * a[i] * L[P][i] * L[k][i];
+        G[k][P] = r;
+    }
+    for (int k = 0; k < P; ++k) { /* Gaussian elimination with partial pivoting */
+        int piv = k;
+        for (int r = k + 1; r < P; ++r) if (fabsl(G[r][k]) > fabsl(G[piv][k])) piv = r;
+        for (int j = 0; j <= P; ++j) { long double t = G[k][j]; G[k][j] = G[piv][j]; G[piv][j] = t; }
+        for (int r = k + 1; r < P; ++r) {
+            long double f = G[r][k] / G[k][k];
+            for (int j = k; j <= P; ++j) G[r][j] -= f * G[k][j];
+        }
+    }
+    for (int k = P - 1; k >= 0; --k) {
+        long double s = G[k][P];
+        for (int j = k + 1; j < P; ++j) s -= G[k][j] * c[j];
+        c[k] = s / G[k][k];
+    }
+    long double gamma = 0;
+    for (int i = 0; i < P1; ++i) {
+        long double v = L[P][i];
+        for (int k = 0; k < P; ++k) v -= c[k] * L[k][i];
+        phi[i] = v;
+        gamma += (long double)m->weights[i] * a[i] * v * v;
+    }
+    for (int i = 0; i < P1; ++i)
+        for (int j = 0; j < P1; ++j)
+            Pi[i * P1 + j] = (double)((i == j ? 1.0L : 0.0L) - phi[i] * m->weights[j] * a[j] * phi[j] / gamma);
+}
 
 static void truncate_with(const ctx_t* c, double* u) {
     const oracle_mesh* m = c->m;
@@ -311,6 +372,14 @@ static void truncate_with(const ctx_t* c, double* u) {
             for (int k = 0; k < D; ++k) { base[k] = (int)(r % E) * P1; r /= E; }
             for (int d = 0; d < D; ++d) {
                 int64_t nl = ipow64(P1, D - 1);
+                double Pline[256];
+                const double* Pm = m->projector;
+                if (m->line_weights) {
+                    /* the line's own projector: element index along d is base[d] / P1 */
+                    const double* a = m->line_weights + (int64_t)P1 * (base[d] / P1 + (int64_t)E * (b + (int64_t)m->nblocks * d));
+                    line_projector(m, a, Pline);
+                    Pm = Pline;
+                }
                 for (int64_t l = 0; l < nl; ++l) {
                     int x[3] = {base[0], base[1], base[2]};
                     int64_t ll = l;
@@ -318,7 +387,7 @@ static void truncate_with(const ctx_t* c, double* u) {
                     for (int j = 0; j < P1; ++j) { int y[3] = {x[0], x[1], x[2]}; y[d] += j; line[j] = v[oidx(c, y)]; }
                     for (int i = 0; i < P1; ++i) {
                         double s = 0.0;
-                        for (int j = 0; j < P1; ++j) s += m->projector[i * P1 + j] * line[j];
+                        for (int j = 0; j < P1; ++j) s += Pm[i * P1 + j] * line[j];
                         out[i] = s;
                     }
                     for (int i = 0; i < P1; ++i) { int y[3] = {x[0], x[1], x[2]}; y[d] += i; v[oidx(c, y)] = out[i]; }
@@ -400,10 +469,13 @@ int oracle_energy(const oracle_mesh* m, const double* u, double* out) {
         for (int64_t b = 0; b < nb; ++b) {
             double s = 0.0;
             const double* v = u + b * 2 * NN + NN;
-            for (int64_t n = 0; n < NN; ++n) s += node_weight(&c, (int)b, n) * v[n] * v[n];
+            const double* cf = m->coef ? m->coef + b * (1 + D) * NN : NULL;
+            for (int64_t n = 0; n < NN; ++n) s += (cf ? cf[n] : 1.0) * node_weight(&c, (int)b, n) * v[n] * v[n];
             for (int d = 0; d < D; ++d) {
-                derivative_block(&c, (int)b, d, ua, 1.0, g);
-                for (int64_t n = 0; n < NN; ++n) s += node_weight(&c, (int)b, n) * g[n] * g[n];
+                /* on a geometry the flux F_d = A_d D_d u enters as F_d^2 / A_d */
+                derivative_block(&c, (int)b, d, ua, 1.0, g, cf ? cf + (1 + d) * NN : NULL);
+                for (int64_t n = 0; n < NN; ++n)
+                    s += node_weight(&c, (int)b, n) * g[n] * g[n] / (cf ? cf[(1 + d) * NN + n] : 1.0);
             }
             part[b] = 0.5 * s;
         }
@@ -434,6 +506,7 @@ int oracle_norm(const oracle_mesh* m, const double* u, const double* ref, int p,
                 int64_t o = b * 2 * c.NN + var * c.NN + n;
                 double x = fabs(u[o] - (ref ? ref[o] : 0.0));
                 double w = node_weight(&c, (int)b, n);
+                if (m->coef) w *= m->coef[b * (1 + m->D) * c.NN + n];
                 if (p == 0) num = x > num ? x : num;
                 else num += w * pow(x, p);
                 vol += w;

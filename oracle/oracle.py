@@ -24,7 +24,8 @@ class OracleMesh(ctypes.Structure):
         ("level", ctypes.POINTER(ctypes.c_int32)), ("corner", ctypes.POINTER(ctypes.c_int64)),
         ("nodes", ctypes.POINTER(ctypes.c_double)), ("weights", ctypes.POINTER(ctypes.c_double)),
         ("stencil", ctypes.POINTER(ctypes.c_double)), ("projector", ctypes.POINTER(ctypes.c_double)),
-        ("duals", ctypes.POINTER(ctypes.c_double)),
+        ("duals", ctypes.POINTER(ctypes.c_double)), ("coef", ctypes.POINTER(ctypes.c_double)),
+        ("line_weights", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -71,7 +72,10 @@ class Oracle:
     """The oracle over one forest (a twoldg Forest-like object with D, roots,
     N, lo, hi, periodic, reflecting and leaves), in FP64."""
 
-    def __init__(self, forest, P, truncate=True):
+    def __init__(self, forest, P, truncate=True, coef=None, line_weights=None):
+        """coef: (nblocks, 1+D, N^D) metric node values; line_weights: (D,
+        nblocks, E, P+1) sqrt(g) factors along each element line (a
+        diagonal-metric geometry), or None for the flat problem."""
         self.forest = forest
         self.P = P
         self.D = forest.D
@@ -101,6 +105,11 @@ class Oracle:
         m.corner = a["corner"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
         for k in ("nodes", "weights", "stencil", "projector", "duals"):
             setattr(m, k, a[k].ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        if coef is not None:
+            a["coef"] = np.ascontiguousarray(coef, dtype=np.float64).reshape(-1)
+            a["line_weights"] = np.ascontiguousarray(line_weights, dtype=np.float64).reshape(-1)
+            m.coef = a["coef"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            m.line_weights = a["line_weights"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
         self.mesh = m
 
     def _vec(self, u):

@@ -76,6 +76,11 @@ struct Group {
     std::vector<double> h;
     std::unique_ptr<Ops> ops;
     DevBuf d_items, d_cf, fu[2], fog[2], ugd, gfd, ggd, d_part, d_part2;
+    bool metric = false;
+    std::vector<double> coef;             // per item (1 + D) N^D, then converted to the field type
+    std::vector<std::vector<double>> trm, trd;  // per member: (P+1, E, nblocks, D)
+    std::vector<int> member_blocks;
+    DevBuf d_coef, d_trm, d_trd;
     int nslots() const { return (int)items.size() * 2 * D; }
 };
 
@@ -129,7 +134,13 @@ struct twoldg_runner {
             if (!build_mesh(d, m, err)) return fail(TWOLDG_EINVAL, err);
             if (!tables().get(m.P))
                 return fail(TWOLDG_EUNSUP, "element order P = " + std::to_string(m.P) + " is not built (1..6)");
-            auto key = std::make_tuple(m.D, m.P, m.E, d.truncate ? 1 : 0);
+            const bool metric = d.coef != nullptr;
+            if (metric && (!d.trunc_modes || !d.trunc_duals))
+                return fail(TWOLDG_EINVAL, "a metric (coef) needs its truncation pairs (trunc_modes, trunc_duals)");
+            if (metric && !m.cf.empty())
+                return fail(TWOLDG_EINVAL, "a geometry takes refinement only in an affine patch, which a diagonal "
+                                           "metric's coefficients do not describe: no coarse-fine faces with coef");
+            auto key = std::make_tuple(m.D, m.P, m.E, (d.truncate ? 1 : 0) + (metric ? 2 : 0));
             auto gi = gidx.find(key);
             Group* g;
             if (gi == gidx.end()) {
@@ -137,6 +148,7 @@ struct twoldg_runner {
                 groups.emplace_back(new Group());
                 g = groups.back().get();
                 g->D = m.D; g->P = m.P; g->E = m.E; g->truncate = d.truncate ? 1 : 0;
+                g->metric = metric;
                 g->NN = m.NN;
                 for (int q = 0; q < m.D - 1; ++q) g->F *= m.N;
                 Ops* ops = nullptr;
@@ -164,6 +176,14 @@ struct twoldg_runner {
                 g->cf.push_back(c);
             }
             g->h.insert(g->h.end(), m.h.begin(), m.h.end());
+            if (metric) {
+                const size_t nc = (size_t)(1 + m.D) * m.NN * m.nblocks;
+                g->coef.insert(g->coef.end(), d.coef, d.coef + nc);
+                const size_t nt = (size_t)(m.P + 1) * m.E * m.nblocks * m.D;
+                g->trm.emplace_back(d.trunc_modes, d.trunc_modes + nt);
+                g->trd.emplace_back(d.trunc_duals, d.trunc_duals + nt);
+                g->member_blocks.push_back(m.nblocks);
+            }
             offsets.push_back(base);
             hmin.push_back(m.hmin);
             total_words += 2 * m.NN * m.nblocks;
@@ -195,6 +215,29 @@ struct twoldg_runner {
             CK(g.ggd.alloc(dbytes));
             CK(g.d_part.alloc(g.items.size() * sizeof(double)));
             CK(g.d_part2.alloc(g.items.size() * sizeof(double)));
+            if (g.metric) {
+                // the per-line tables of every member into the group's (P+1, E, nitems, D) layout
+                const int P1 = g.P + 1, nit = (int)g.items.size();
+                std::vector<double> tm((size_t)P1 * g.E * nit * g.D), td(tm.size());
+                int item0 = 0;
+                for (size_t mbr = 0; mbr < g.member_blocks.size(); ++mbr) {
+                    const int nb = g.member_blocks[mbr];
+                    for (int dd = 0; dd < g.D; ++dd)
+                        for (int b = 0; b < nb; ++b)
+                            for (int e = 0; e < g.E; ++e)
+                                for (int i = 0; i < P1; ++i) {
+                                    size_t src = i + (size_t)P1 * (e + (size_t)g.E * (b + (size_t)nb * dd));
+                                    size_t dst = i + (size_t)P1 * (e + (size_t)g.E * (item0 + b + (size_t)nit * dd));
+                                    tm[dst] = g.trm[mbr][src];
+                                    td[dst] = g.trd[mbr][src];
+                                }
+                    item0 += nb;
+                }
+                int r = upload_t(g.d_coef, g.coef);
+                if (!r) r = upload_t(g.d_trm, tm);
+                if (!r) r = upload_t(g.d_trd, td);
+                if (r) return r;
+            }
         }
         size_t sbytes = (size_t)total_words * wsize;
         if (y.alloc(sbytes) != cudaSuccess || acc.alloc(sbytes) != cudaSuccess)
@@ -207,6 +250,18 @@ struct twoldg_runner {
         h_dts.assign(n, 0.0);
         h_rk.assign(n * 4 * wsize, 0);
         CK(cudaMemcpy(d_rk.p, h_rk.data(), h_rk.size(), cudaMemcpyHostToDevice));
+        return TWOLDG_OK;
+    }
+
+    // doubles -> the field type, rounded once, onto the device
+    int upload_t(DevBuf& buf, const std::vector<double>& v) {
+        CK(buf.alloc(v.size() * wsize));
+        if (wsize == 8) {
+            CK(cudaMemcpy(buf.p, v.data(), v.size() * 8, cudaMemcpyHostToDevice));
+        } else {
+            std::vector<float> f(v.begin(), v.end());
+            CK(cudaMemcpy(buf.p, f.data(), f.size() * 4, cudaMemcpyHostToDevice));
+        }
         return TWOLDG_OK;
     }
 
@@ -225,6 +280,9 @@ struct twoldg_runner {
         p.ggd = g.ggd.p;
         p.rk = d_rk.p;
         p.partial = (double*)g.d_part.p;
+        p.coef = g.metric ? g.d_coef.p : nullptr;
+        p.trm = g.metric ? g.d_trm.p : nullptr;
+        p.trd = g.metric ? g.d_trd.p : nullptr;
         return p;
     }
 
@@ -400,7 +458,8 @@ int twoldg_truncate(twoldg_problem* p, void* u) {
     if (!p || !u) return fail(TWOLDG_EINVAL, "NULL argument");
     Group& g = *p->groups[0];
     if (!g.truncate) return TWOLDG_OK;
-    CK(g.ops->truncate((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, u, p->stream));
+    CK(g.ops->truncate((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, u,
+                       g.metric ? g.d_trm.p : nullptr, g.metric ? g.d_trd.p : nullptr, p->stream));
     return TWOLDG_OK;
 }
 
@@ -441,7 +500,7 @@ int twoldg_norm(twoldg_problem* p, const void* u, const void* ref, int32_t pnorm
     if (vars_mask < 1 || vars_mask > 3) return fail(TWOLDG_EINVAL, "vars_mask must select u (1), v (2) or both (3)");
     Group& g = *p->groups[0];
     CK(g.ops->norm((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, u, ref, pnorm, vars_mask,
-                   (double*)g.d_part.p, (double*)g.d_part2.p, p->stream));
+                   (double*)g.d_part.p, (double*)g.d_part2.p, g.metric ? g.d_coef.p : nullptr, p->stream));
     std::vector<double> num(g.items.size()), vol(g.items.size());
     CK(cudaMemcpyAsync(num.data(), g.d_part.p, num.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
     CK(cudaMemcpyAsync(vol.data(), g.d_part2.p, vol.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));

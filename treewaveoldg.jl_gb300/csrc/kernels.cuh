@@ -65,6 +65,11 @@ struct StageArgs {
     const T* ggd;    // dense gradient ghosts (coarse-fine faces)
     const T* rk;     // per problem: dt/6, dt/3, dt/2, dt, rounded once to T on the host
     double* partial; // energy: one sum per item
+    // diagonal metric (NULL: flat): per item (N^D, 1 + D) node values sqrt(g), A_1..A_D,
+    // and the per-line truncation pairs (P+1, E, nitems, D)
+    const T* coef;
+    const T* trm;
+    const T* trd;
 };
 
 __host__ __device__ constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1); }
@@ -369,6 +374,14 @@ __device__ __forceinline__ int lidx(const G& g, const int (&x)[3]) {
     return r;
 }
 
+template <int D, class G>
+__device__ __forceinline__ int oidx(const G& g, const int (&x)[3]) {
+    int r = x[0];
+    if (D > 1) r += g.N * x[1];
+    if (D > 2) r += g.N * g.N * x[2];
+    return r;
+}
+
 // 16-byte vectors for the state streams.
 template <typename T>
 struct V16;
@@ -436,13 +449,18 @@ __device__ __forceinline__ void load_u_with_ghosts(const G& g, const BlockItem& 
 }
 
 // Gradient along d at every owned node into sg (padded), scaled by 1/h, and
-// the two gradient ghost planes normal to d.
+// the two gradient ghost planes normal to d. With a diagonal metric the
+// gradient set holds the flux A_d D_d u / h (src/evolution.jl:67-90), and a
+// ghost is the neighbour's flux at its face node, with the neighbour's A_d.
 template <typename T, int D, int P, int NT, class G>
-__device__ __forceinline__ void gradient_along(const G& g, int d, const BlockItem& it, const StageArgs<T>& a,
-                                               const Tab<T, P>& tb, const T* su, T* sg, T inv_h) {
+__device__ __forceinline__ void gradient_along(const G& g, int d, const BlockItem& it, int item,
+                                               const StageArgs<T>& a, const Tab<T, P>& tb, const T* su, T* sg,
+                                               T inv_h) {
     constexpr int P1 = P + 1;
     const int sd = g.sstride(d);
-    #pragma unroll 4
+    const int od = d == 0 ? 1 : d == 1 ? g.N : g.N * g.N;
+    const T* Ad = a.coef ? a.coef + ((int64_t)item * (1 + D) + 1 + d) * g.NN : nullptr;
+#pragma unroll 4
     for (int L = threadIdx.x; L < g.E * g.F; L += nthreads<NT>()) {
         int t = L % g.F, e = L / g.F;
         int x[3];
@@ -452,10 +470,16 @@ __device__ __forceinline__ void gradient_along(const G& g, int d, const BlockIte
 #pragma unroll
         for (int k = 0; k < P + 3; ++k) w[k] = su[base + (k - 1) * sd];
         line_derivative<T, P>(tb, w, out);
+        if (Ad) {
+            const int ob = oidx<D>(g, x);
 #pragma unroll
-        for (int i = 0; i <= P; ++i) sg[base + i * sd] = out[i] * inv_h;
+            for (int i = 0; i <= P; ++i) sg[base + i * sd] = Ad[ob + i * od] * (out[i] * inv_h);
+        } else {
+#pragma unroll
+            for (int i = 0; i <= P; ++i) sg[base + i * sd] = out[i] * inv_h;
+        }
     }
-    #pragma unroll 4
+#pragma unroll 4
     for (int i = threadIdx.x; i < 2 * g.F; i += nthreads<NT>()) {
         int side = i / g.F, t = i % g.F;
         int f = 2 * d + side;
@@ -471,6 +495,12 @@ __device__ __forceinline__ void gradient_along(const G& g, int d, const BlockIte
             plane_coords<D>(g, d, t, side == 0 ? 0 : g.N - 1, x);
             T own = su[sidx<D>(g, x)];
             T gnb = (a.fog_in[(int64_t)nslot * g.F + t] + ghost_coef<T, P>(tb, nside) * own) * inv_h;
+            if (a.coef) {
+                int xn[3];
+                plane_coords<D>(g, d, t, nside ? g.N - 1 : 0, xn);
+                const int nitem = nslot / (2 * D);
+                gnb = a.coef[((int64_t)nitem * (1 + D) + 1 + d) * g.NN + oidx<D>(g, xn)] * gnb;
+            }
             v = (it.flags & (1u << (8 + f))) ? -gnb : gnb;
         }
         plane_coords<D>(g, d, t, side == 0 ? -1 : g.N, x);
@@ -506,35 +536,47 @@ __device__ __forceinline__ void laplacian_along(const G& g, int d, const Tab<T, 
 // turn: c = sum_j topdual_j v_j; v_i -= topmode_i c (src/evolution.jl:222-264).
 // With COMP the subtraction is error-free into the compensation words sc.
 template <typename T, int D, int P, bool COMP, int NT, class G>
-__device__ __forceinline__ void truncate_block(const G& g, const Tab<T, P>& tb, T* sv, T* sc) {
+__device__ __forceinline__ void truncate_block(const G& g, const Tab<T, P>& tb, T* sv, T* sc,
+                                               const T* trm = nullptr, const T* trd = nullptr, int item = 0,
+                                               int nitems = 0) {
     constexpr int P1 = P + 1;
     for (int d = 0; d < D; ++d) {
         const int ld = g.lstride(d);
-        #pragma unroll 4
+#pragma unroll 4
         for (int L = threadIdx.x; L < g.E * g.F; L += nthreads<NT>()) {
             int t = L % g.F, e = L / g.F;
             int x[3];
             plane_coords<D>(g, d, t, e * P1, x);
             int lb = lidx<D>(g, x);
+            // the line's rank-one pair: the element's, or on a geometry the line's own
+            T tm[P1], td[P1];
+            if (trm) {
+                const int64_t o = (int64_t)P1 * (e + (int64_t)g.E * (item + (int64_t)nitems * d));
+#pragma unroll
+                for (int j = 0; j < P1; ++j) { tm[j] = trm[o + j]; td[j] = trd[o + j]; }
+            } else {
+#pragma unroll
+                for (int j = 0; j < P1; ++j) { tm[j] = tb.tm[j]; td[j] = tb.td[j]; }
+            }
             T v[P1];
             T c = T(0);
 #pragma unroll
-            for (int j = 0; j < P1; ++j) { v[j] = sv[lb + j * ld]; c += tb.td[j] * v[j]; }
+            for (int j = 0; j < P1; ++j) { v[j] = sv[lb + j * ld]; c += td[j] * v[j]; }
             if (COMP) {
                 T cc = T(0);
 #pragma unroll
-                for (int j = 0; j < P1; ++j) cc += tb.td[j] * sc[lb + j * ld];
+                for (int j = 0; j < P1; ++j) cc += td[j] * sc[lb + j * ld];
                 c += cc;
 #pragma unroll
                 for (int i = 0; i < P1; ++i) {
                     T s, err;
-                    two_sum(v[i], -(tb.tm[i] * c), s, err);
+                    two_sum(v[i], -(tm[i] * c), s, err);
                     sv[lb + i * ld] = s;
                     sc[lb + i * ld] += err;
                 }
             } else {
 #pragma unroll
-                for (int i = 0; i < P1; ++i) sv[lb + i * ld] = v[i] - tb.tm[i] * c;
+                for (int i = 0; i < P1; ++i) sv[lb + i * ld] = v[i] - tm[i] * c;
             }
         }
         __syncthreads();
@@ -657,14 +699,14 @@ __device__ __forceinline__ void stv(T* p, const T (&a)[VW]) {
 // k3), added to u^n at stage 4. mode MODE_RHS writes du = f(u) only.
 template <typename T, int D, int P, bool COMP, int NT, class G, int VW>
 __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, const Tab<T, P>& tb,
-                                            const BlockItem& it, T* su, T* sg, T* sl) {
+                                            const BlockItem& it, int item, T* su, T* sg, T* sl) {
     const int mode = a.mode;
     const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
     const T inv_h = T(1) / T(it.h);
     load_u_with_ghosts<T, D, NT>(g, it, ysrc, a, su);
     __syncthreads();
     for (int d = 0; d < D; ++d) {
-        gradient_along<T, D, P, NT>(g, d, it, a, tb, su, sg, inv_h);
+        gradient_along<T, D, P, NT>(g, d, it, item, a, tb, su, sg, inv_h);
         __syncthreads();
         laplacian_along<T, D, P, NT>(g, d, tb, sg, sl, d == 0);
         __syncthreads();
@@ -681,7 +723,11 @@ __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, c
             Pack<T, VW> v = ldv<T, VW>(yv + n0);
             T lap[VW];
 #pragma unroll
-            for (int k = 0; k < VW; ++k) lap[k] = sl[l0 + k] * inv_h;
+            for (int k = 0; k < VW; ++k) {
+                lap[k] = sl[l0 + k] * inv_h;
+                // a geometry's Laplacian is divided by sqrt(g) (src/evolution.jl:67-110)
+                if (a.coef) lap[k] = lap[k] / a.coef[(int64_t)item * (1 + D) * g.NN + n0 + k];
+            }
             stv<T, VW>(du + n0, v.v);
             stv<T, VW>(du + g.NN + n0, lap);
         }
@@ -725,6 +771,7 @@ __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, c
                 owned_coords<D>(g, n, x);
                 const int s0 = sidx<D>(g, x), l0 = lidx<D>(g, x);
                 T lap[1] = {sl[l0]};
+                if (a.coef) lap[0] = lap[0] / a.coef[(int64_t)item * (1 + D) * g.NN + n];
                 T nu[1], nv[1], cv[1];
                 T yq[1] = {y[q]}, uuq[1] = {uu[q]}, uvq[1] = {uv[q]}, auq[1] = {au[q]}, avq[1] = {av[q]},
                   cuq[1] = {cu[q]}, cviq[1] = {cvi[q]};
@@ -743,8 +790,8 @@ __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, c
     __syncthreads();
     const bool final_comp = COMP && mode == MODE_STAGE4;
     if (a.truncate) {
-        if (final_comp) truncate_block<T, D, P, true, NT>(g, tb, sl, sc);
-        else truncate_block<T, D, P, false, NT>(g, tb, sl, sc);
+        if (final_comp) truncate_block<T, D, P, true, NT>(g, tb, sl, sc, a.trm, a.trd, item, a.nitems);
+        else truncate_block<T, D, P, false, NT>(g, tb, sl, sc, a.trm, a.trd, item, a.nitems);
     }
     T* out = (mode == MODE_STAGE4 ? a.u : a.y) + it.off;
     #pragma unroll 4
@@ -801,7 +848,7 @@ __global__ void __launch_bounds__(StageLaunch<T, D, P, E>::NT, StageLaunch<T, D,
     constexpr int VW = 1;
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         const BlockItem& it = a.items[item];
-        stage_block<T, D, P, COMP, StageLaunch<T, D, P, E>::NT, G, VW>(g, a, tb, it, su, sg, sl);
+        stage_block<T, D, P, COMP, StageLaunch<T, D, P, E>::NT, G, VW>(g, a, tb, it, item, su, sg, sl);
     }
 }
 
@@ -816,7 +863,7 @@ __global__ void __launch_bounds__(256) stage_kernel(StageArgs<T> a, Tab<T, P> tb
     T* sl = sg + g.SS;
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         const BlockItem& it = a.items[item];
-        stage_block<T, D, P, COMP, 0, G, 1>(g, a, tb, it, su, sg, sl);
+        stage_block<T, D, P, COMP, 0, G, 1>(g, a, tb, it, item, su, sg, sl);
     }
 }
 
@@ -854,13 +901,15 @@ __global__ void __launch_bounds__(256) energy_kernel(StageArgs<T> a, Tab<T, P> t
         double local = 0;
         const double wscale = h * P1 / 2.0;
         const T* uv = a.u + it.off + g.NN;
+        // on a geometry: 1/2 sum w (sqrt(g) v^2 + sum_d F_d^2 / A_d), F_d = A_d D_d u
+        const T* cf = a.coef ? a.coef + (int64_t)item * (1 + D) * g.NN : nullptr;
         for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
             int x[3];
             owned_coords<D>(g, n, x);
             double w = 1.0;
             for (int k = 0; k < D; ++k) w *= wscale * (double)tb.wq[x[k] % P1];
             double v = (double)uv[n];
-            local += w * v * v;
+            local += (cf ? (double)cf[n] : 1.0) * w * v * v;
         }
         for (int d = 0; d < D; ++d) {
             const int sd = g.sstride(d);
@@ -876,10 +925,13 @@ __global__ void __launch_bounds__(256) energy_kernel(StageArgs<T> a, Tab<T, P> t
 #pragma unroll
                 for (int k = 0; k < P + 3; ++k) w[k] = su[base + (k - 1) * sd];
                 line_derivative<T, P>(tb, w, out);
+                const int ob = oidx<D>(g, x);
+                const int od = d == 0 ? 1 : d == 1 ? g.N : g.N * g.N;
 #pragma unroll
                 for (int i = 0; i <= P; ++i) {
                     double gv = (double)(out[i] * inv_h);
-                    local += wt * wscale * (double)tb.wq[i] * gv * gv;
+                    double Ad = cf ? (double)cf[(1 + d) * g.NN + ob + i * od] : 1.0;
+                    local += Ad * wt * wscale * (double)tb.wq[i] * gv * gv;
                 }
             }
         }
@@ -894,7 +946,7 @@ __global__ void __launch_bounds__(256) energy_kernel(StageArgs<T> a, Tab<T, P> t
 // means the largest |x - ref|.
 template <typename T, int D, int P>
 __global__ void norm_kernel(const BlockItem* items, int nitems, int E, const T* u, const T* ref, int p,
-                            int vars_mask, Tab<T, P> tb, double* part_num, double* part_vol) {
+                            int vars_mask, Tab<T, P> tb, double* part_num, double* part_vol, const T* coef) {
     __shared__ double red[32];
     constexpr int P1 = P + 1;
     const int N = E * P1;
@@ -907,6 +959,8 @@ __global__ void norm_kernel(const BlockItem* items, int nitems, int E, const T* 
             double w = 1.0;
             int m = n;
             for (int k = 0; k < D; ++k) { w *= wscale * (double)tb.wq[(m % N) % P1]; m /= N; }
+            // on a geometry the norm is weighted by sqrt(g): the physical volume
+            if (coef) w *= (double)coef[(int64_t)item * (1 + D) * NN + n];
             for (int var = 0; var < 2; ++var) {
                 if (!(vars_mask & (1 << var))) continue;
                 int64_t o = it.off + (int64_t)var * NN + n;
@@ -1019,7 +1073,8 @@ __global__ void maxabs_kernel(const BlockItem* items, int nitems, int NN, const 
 // Standalone truncation of v (twoldg_truncate): one block per CTA, v staged
 // in shared memory in the ghost-free layout.
 template <typename T, int D, int P>
-__global__ void truncate_kernel(const BlockItem* items, int nitems, int E, T* u, Tab<T, P> tb) {
+__global__ void truncate_kernel(const BlockItem* items, int nitems, int E, T* u, Tab<T, P> tb, const T* trm,
+                                const T* trd) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sv = reinterpret_cast<T*>(smem_raw);
     using G = ShapeR<D, P>;
@@ -1032,7 +1087,7 @@ __global__ void truncate_kernel(const BlockItem* items, int nitems, int E, T* u,
             sv[lidx<D>(g, x)] = v[n];
         }
         __syncthreads();
-        truncate_block<T, D, P, false, 0>(g, tb, sv, nullptr);
+        truncate_block<T, D, P, false, 0>(g, tb, sv, nullptr, trm, trd, item, nitems);
         for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
             int x[3];
             owned_coords<D>(g, n, x);

@@ -67,6 +67,7 @@ extern "C" int twoldg_rhs_static(const twoldg_desc* desc, void* du, const void* 
         }
         base = g_scratch_ptr[dev];
     }
+    if (desc->coef) return static_rhs_fail(TWOLDG_EUNSUP, "twoldg_rhs_static serves flat problems (coef = NULL)");
     Mesh m;
     std::string err;
     if (!build_mesh(*desc, m, err)) return static_rhs_fail(TWOLDG_EINVAL, err);

@@ -26,6 +26,9 @@ struct StagePtrs {
     const void* ggd;
     const void* rk;    // per problem 4 RK coefficients in the field type
     double* partial;
+    const void* coef;  // diagonal metric node values (NULL: flat)
+    const void* trm;   // per-line truncation pairs (NULL: the element's)
+    const void* trd;
 };
 
 class Ops {
@@ -45,8 +48,9 @@ public:
     virtual cudaError_t energy(const BlockItem* items, int nitems, int E, const StagePtrs& p,
                                cudaStream_t s) const = 0;
     virtual cudaError_t norm(const BlockItem* items, int nitems, int E, const void* u, const void* ref, int p,
-                             int vars_mask, double* num, double* vol, cudaStream_t s) const = 0;
-    virtual cudaError_t truncate(const BlockItem* items, int nitems, int E, void* u, cudaStream_t s) const = 0;
+                             int vars_mask, double* num, double* vol, const void* coef, cudaStream_t s) const = 0;
+    virtual cudaError_t truncate(const BlockItem* items, int nitems, int E, void* u, const void* trm,
+                                 const void* trd, cudaStream_t s) const = 0;
     virtual cudaError_t maxabs(const BlockItem* items, int nitems, int E, const void* u, int var, double* part,
                                cudaStream_t s) const = 0;
     // modes[0..nq): Legendre modes; weights/pows per mode; post factor; result tau (E^D per block)

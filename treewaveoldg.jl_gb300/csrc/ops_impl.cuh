@@ -141,6 +141,9 @@ public:
         a.ggd = (const T*)p.ggd;
         a.rk = (const T*)p.rk;
         a.partial = p.partial;
+        a.coef = (const T*)p.coef;
+        a.trm = (const T*)p.trm;
+        a.trd = (const T*)p.trd;
         size_t smem = stage_smem(E);
         if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
         if (grid <= 0) grid = std::min(nitems, kMaxGrid);
@@ -148,13 +151,14 @@ public:
         uintptr_t al = (uintptr_t)p.u | (uintptr_t)p.y | (uintptr_t)p.acc | (uintptr_t)p.comp | (uintptr_t)p.du;
         const bool aligned = (al & 15) == 0;
         int nt = threads_ ? threads_ : default_threads(E);
+        // the whole-lines-in-registers 3D kernel serves flat problems
         if constexpr (D == 3) {
-            if (aligned && E == 2 && Stage3R<T, P, 2, COMP>::usable) {
+            if (!p.coef && aligned && E == 2 && Stage3R<T, P, 2, COMP>::usable) {
                 using S = Stage3R<T, P, 2, COMP>;
                 stage3r_kernel<T, P, 2, COMP><<<grid, S::NT, S::words * sizeof(T), s>>>(a, tb_);
                 return cudaGetLastError();
             }
-            if (aligned && E == 4 && Stage3R<T, P, 4, COMP>::usable) {
+            if (!p.coef && aligned && E == 4 && Stage3R<T, P, 4, COMP>::usable) {
                 using S = Stage3R<T, P, 4, COMP>;
                 stage3r_kernel<T, P, 4, COMP><<<grid, S::NT, S::words * sizeof(T), s>>>(a, tb_);
                 return cudaGetLastError();
@@ -182,6 +186,7 @@ public:
         a.ugd = (const T*)p.ugd;
         a.ggd = (const T*)p.ggd;
         a.partial = p.partial;
+        a.coef = (const T*)p.coef;
         size_t smem = (padded_words(E) + 1) * sizeof(T) + 32 * sizeof(double) + 16;
         auto kern = energy_kernel<T, D, P>;
         if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
@@ -190,17 +195,19 @@ public:
     }
 
     cudaError_t norm(const BlockItem* items, int nitems, int E, const void* u, const void* ref, int p,
-                     int vars_mask, double* num, double* vol, cudaStream_t s) const override {
+                     int vars_mask, double* num, double* vol, const void* coef, cudaStream_t s) const override {
         norm_kernel<T, D, P><<<std::min(nitems, kMaxGrid), 256, 0, s>>>(
-            items, nitems, E, (const T*)u, (const T*)ref, p, vars_mask, tb_, num, vol);
+            items, nitems, E, (const T*)u, (const T*)ref, p, vars_mask, tb_, num, vol, (const T*)coef);
         return cudaGetLastError();
     }
 
-    cudaError_t truncate(const BlockItem* items, int nitems, int E, void* u, cudaStream_t s) const override {
+    cudaError_t truncate(const BlockItem* items, int nitems, int E, void* u, const void* trm, const void* trd,
+                         cudaStream_t s) const override {
         size_t smem = plain_words(E) * sizeof(T);
         auto kern = truncate_kernel<T, D, P>;
         if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
-        kern<<<std::min(nitems, kMaxGrid), 256, smem, s>>>(items, nitems, E, (T*)u, tb_);
+        kern<<<std::min(nitems, kMaxGrid), 256, smem, s>>>(items, nitems, E, (T*)u, tb_, (const T*)trm,
+                                                          (const T*)trd);
         return cudaGetLastError();
     }
 

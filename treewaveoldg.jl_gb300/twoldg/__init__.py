@@ -15,5 +15,7 @@ from .drivers import (convergence_rate, reflect_errors, reflect_exact, reflect_o
                       wave_exact, wave_omega)
 from .indicator import modal_indicator, mode_amplitude
 from .batch import Batch, fill_batch, sine_ensemble
+from .geometry import (PolarAnnulus, annulus_errors, annulus_exact, annulus_forest, annulus_wavenumber,
+                       metric_tables, projector_mode)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

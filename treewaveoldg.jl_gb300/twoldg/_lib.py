@@ -32,6 +32,8 @@ class Desc(ctypes.Structure):
         ("roots", ctypes.c_int32 * 3), ("periodic", ctypes.c_int32 * 3),
         ("reflecting", ctypes.c_int32 * 3), ("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3),
         ("level", ctypes.POINTER(ctypes.c_int32)), ("corner", ctypes.POINTER(ctypes.c_int64)),
+        ("coef", ctypes.POINTER(ctypes.c_double)), ("trunc_modes", ctypes.POINTER(ctypes.c_double)),
+        ("trunc_duals", ctypes.POINTER(ctypes.c_double)),
     ]
 
 

@@ -41,8 +41,9 @@ def check_layout(forest, el):
                          "elements of it, so N must be a multiple of 2(P+1) = %d" % (forest.N, E, el.P, 2 * P1))
 
 
-def make_desc(forest, el, truncate, precision):
-    """The twoldg_desc of a forest; returns (desc, keepalive arrays)."""
+def make_desc(forest, el, truncate, precision, metric=None):
+    """The twoldg_desc of a forest (and of a diagonal metric's tables, from
+    geometry.metric_tables); returns (desc, keepalive arrays)."""
     D = forest.D
     levels = np.array([lv for lv, _ in forest.leaves], dtype=np.int32)
     corners = np.array([c for _, c in forest.leaves], dtype=np.int64).reshape(-1)
@@ -61,7 +62,15 @@ def make_desc(forest, el, truncate, precision):
         d.hi[k] = forest.hi[k] if k < D else 1.0
     d.level = levels.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
     d.corner = corners.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
-    return d, (levels, corners)
+    keep = [levels, corners]
+    if metric is not None:
+        coef, modes, duals = metric[:3]
+        dp = ctypes.POINTER(ctypes.c_double)
+        d.coef = coef.ctypes.data_as(dp)
+        d.trunc_modes = modes.ctypes.data_as(dp)
+        d.trunc_duals = duals.ctypes.data_as(dp)
+        keep += [coef, modes, duals]
+    return d, tuple(keep)
 
 
 class WaveProblem:
@@ -72,7 +81,7 @@ class WaveProblem:
     RK4 accumulation). By default it follows the element's type.
     """
 
-    def __init__(self, forest, el, truncate=True, precision=None, device="cuda"):
+    def __init__(self, forest, el, truncate=True, precision=None, device="cuda", geometry=None):
         check_layout(forest, el)
         if precision is None:
             precision = "f64" if el.T == np.float64 else "f32"
@@ -93,7 +102,14 @@ class WaveProblem:
         self.NN = self.N ** self.D
         self.dtype = el.T
         self.device = device
-        self._desc, self._keep = make_desc(forest, el, truncate, _PREC[precision])
+        self.geometry = geometry
+        self.metric = None
+        self.hspeed = None
+        if geometry is not None:
+            from .geometry import metric_tables
+            self.metric = metric_tables(forest, Element(np.float64, el.P), geometry)
+            self.hspeed = self.metric[3]
+        self._desc, self._keep = make_desc(forest, el, truncate, _PREC[precision], self.metric)
         h = ctypes.c_void_p()
         _lib.check(_lib.lib().twoldg_problem_create(ctypes.byref(self._desc), ctypes.byref(h)))
         self._h = h
@@ -250,9 +266,12 @@ def wave_norm(p, u, pnorm=2, vars=(1, 2)):
 
 
 def oldg_timestep(p, cfl):
-    """oldg_timestep(p; cfl) = cfl h_min / (P+1) (src/evolution.jl:1528-1531), in T."""
+    """oldg_timestep(p; cfl) = cfl h_min / (P+1) (src/evolution.jl:1528-1531),
+    in T; on a geometry h_min is the smallest block spacing over the block's
+    largest logical wave speed."""
     T = p.dtype.type
-    return T(cfl) * T(p.forest.minimum_spacing()) / T(p.P + 1)
+    h = p.forest.minimum_spacing() if p.hspeed is None else p.hspeed
+    return T(cfl) * T(h) / T(p.P + 1)
 
 
 def chunk_count(T, span, chunk):
