@@ -75,6 +75,37 @@ typedef struct twoldg_desc {
     const double* coef;
     const double* trunc_modes;
     const double* trunc_duals;
+    /* The metric's kind: 0 flat (coef NULL), 1 diagonal (coef: sqrt(g), A_d),
+     * 2 full (a geometry whose glues may swap axes, such as the seven-patch
+     * ball, src/evolution.jl:112-220, D = 3 only): coef then holds sqrt(g) and
+     * the area vectors S[d][i] = sqrt(g) d xi^d / d x^i at 1 + D d + i,
+     * (N^D, 1 + D^2, nblocks), and the gradient crosses faces as Cartesian
+     * components. */
+    int32_t metric;
+    /* An explicit face table for a forest of glued patches (NULL: the brick
+     * of roots above): face_nb[b*2D + f] is the block across face f of block
+     * b, or -1 for a face on the domain's boundary, which takes the Dirichlet
+     * data below; face_code[b*2D + f] = (the neighbour's face) | (o << 4),
+     * where o maps this face's tangential point (a, b) to the neighbour's:
+     * bit 0 swaps a and b, bit 1 then reverses the first, bit 2 the second. */
+    const int32_t* face_nb;
+    const int32_t* face_code;
+    /* The full metric's truncation (ElementTruncation, src/evolution.jl:723-899):
+     * elem_slot[b] = 0 takes the element's tensor projector (a block of an
+     * affine patch), s >= 1 the tables s - 1 of elem_w ((P+1)^D, E^D, elem_ntab:
+     * quadrature weights times sqrt(g)) and elem_chol (P^D, P^D, E^D, elem_ntab:
+     * the upper Cholesky factor U of the Gram matrix, G = U^T U), column-major. */
+    const int32_t* elem_slot;
+    const double* elem_w;
+    const double* elem_chol;
+    int32_t elem_ntab;
+    /* Dirichlet data on boundary faces: the plane wave u = sin(k . x - |k| t +
+     * phi) (src/sevenpatch.jl:9-36); bnd_x holds, for every face slot b*2D + f,
+     * the physical positions of its face nodes, (N^(D-1), 3) per slot (only the
+     * boundary faces' are read). */
+    double wave_k[3];
+    double wave_phi;
+    const double* bnd_x;
 } twoldg_desc;
 
 typedef struct twoldg_problem twoldg_problem;

@@ -53,6 +53,21 @@ typedef struct {
      * builds the line's orthogonal projector itself */
     const double* coef;
     const double* line_weights;
+    /* full metric (metric == 2, D = 3): coef holds sqrt(g), S[d][i] (10 per
+     * node); the explicit face table of a glued forest (face_nb, face_code as
+     * in the library's descriptor); elem_slot[b] != 0 marks blocks whose
+     * truncation is the sqrt(g)-orthogonal projection per element (solved
+     * here from the nodes, weights and sqrt(g)); Dirichlet data: the plane wave
+     * (wave_k, wave_phi) at the boundary face nodes' positions bnd_x ((3, N^2)
+     * per slot); t the time of the state */
+    int metric;
+    const int32_t* face_nb;
+    const int32_t* face_code;
+    const int32_t* elem_slot;
+    const double* bnd_x;
+    double wave_k[3];
+    double wave_phi;
+    double t;
 } oracle_mesh;
 
 typedef struct {
@@ -568,4 +583,338 @@ int oracle_threads(void) {
 #else
     return 1;
 #endif
+}
+
+
+/* ------------------------------------------------------------------------- */
+/* The full metric (src/evolution.jl:112-220, 266-425, 1110-1127).           */
+
+static int oriented_t(int t, int N, int code) {
+    int a = t % N, b = t / N;
+    if (code & 1) { int s = a; a = b; b = s; }
+    if (code & 2) a = N - 1 - a;
+    if (code & 4) b = N - 1 - b;
+    return a + N * b;
+}
+
+/* Owned coordinates of face f's node at tangential t (other dims in
+ * increasing order, first fastest) with x_d = xd. */
+static void face_node(int N, int f, int t, int xd, int* x) {
+    int d = f / 2, k2 = 0;
+    int tt[2] = {t % N, t / N};
+    for (int k = 0; k < 3; ++k) x[k] = k == d ? xd : tt[k2++];
+}
+
+static double wave_phase(const oracle_mesh* m, const double* X, int F, int t, double time) {
+    double om = sqrt(m->wave_k[0] * m->wave_k[0] + m->wave_k[1] * m->wave_k[1] + m->wave_k[2] * m->wave_k[2]);
+    return m->wave_k[0] * X[t] + m->wave_k[1] * X[F + t] + m->wave_k[2] * X[2 * F + t] - om * time + m->wave_phi;
+}
+
+/* The ghost of field `f` (ncomp components of N^3 per block, component
+ * stride `cs`) across face `face` of block b at tangential t: the
+ * neighbour's face node, oriented; or NAN for a boundary face. */
+static double full_ghost(const oracle_mesh* m, int N, int64_t NN, const double* f, int64_t bstride, int comp,
+                         int64_t cs, int b, int face, int t) {
+    int nb = m->face_nb[b * 6 + face];
+    if (nb < 0) return NAN;
+    int code = m->face_code[b * 6 + face];
+    int nf = code & 15, o = (code >> 4) & 7;
+    int t2 = oriented_t(t, N, o);
+    int x[3];
+    face_node(N, nf, t2, (nf & 1) ? N - 1 : 0, x);
+    (void)NN;
+    return f[nb * bstride + comp * cs + x[0] + N * (x[1] + N * x[2])];
+}
+
+/* V = grad u at every node of every block, (3, N^3) per block. */
+static void full_gradient(const oracle_mesh* m, const double* u, double* V) {
+    const int P = m->P, P1 = P + 1, PW = P + 3, N = m->E * P1;
+    const int64_t NN = (int64_t)N * N * N, F = (int64_t)N * N;
+    const double h = 1.0 / N;
+#pragma omp parallel for schedule(dynamic)
+    for (int b = 0; b < m->nblocks; ++b) {
+        const double* cf = m->coef + (int64_t)b * 10 * NN;
+        for (int64_t n = 0; n < NN; ++n) {
+            int x[3] = {(int)(n % N), (int)((n / N) % N), (int)(n / F)};
+            double De[3];
+            for (int e = 0; e < 3; ++e) {
+                int i = x[e] % P1, start = x[e] - i - 1;
+                double acc = 0;
+                for (int k = 0; k < PW; ++k) {
+                    double coefk = m->stencil[i * PW + k];
+                    if (coefk == 0.0) continue;
+                    int pos = start + k;
+                    double val;
+                    if (pos < 0 || pos >= N) {
+                        int face = 2 * e + (pos >= N), t = 0, k2 = 0;
+                        int tt[2];
+                        for (int q = 0; q < 3; ++q) if (q != e) tt[k2++] = x[q];
+                        t = tt[0] + N * tt[1];
+                        val = full_ghost(m, N, NN, u, 2 * NN, 0, 0, b, face, t);
+                        if (isnan(val)) {
+                            const double* X = m->bnd_x + ((int64_t)b * 6 + face) * 3 * F;
+                            val = sin(wave_phase(m, X, (int)F, t, m->t));
+                        }
+                    } else {
+                        int y[3] = {x[0], x[1], x[2]};
+                        y[e] = pos;
+                        val = u[(int64_t)b * 2 * NN + y[0] + N * (y[1] + N * y[2])];
+                    }
+                    acc += coefk * val;
+                }
+                De[e] = acc / h;
+            }
+            for (int ci = 0; ci < 3; ++ci) {
+                double s = 0;
+                for (int e = 0; e < 3; ++e) s += cf[(1 + 3 * e + ci) * NN + n] * De[e];
+                V[(int64_t)b * 3 * NN + ci * NN + n] = s / cf[n];
+            }
+        }
+    }
+}
+
+int oracle_rhs_full(const oracle_mesh* m, const double* u, double* du) {
+    const int P = m->P, P1 = P + 1, PW = P + 3, N = m->E * P1;
+    const int64_t NN = (int64_t)N * N * N, F = (int64_t)N * N;
+    const double h = 1.0 / N;
+    double* V = (double*)malloc(sizeof(double) * 3 * NN * m->nblocks);
+    if (!V) return -1;
+    full_gradient(m, u, V);
+#pragma omp parallel for schedule(dynamic)
+    for (int b = 0; b < m->nblocks; ++b) {
+        const double* cf = m->coef + (int64_t)b * 10 * NN;
+        for (int64_t n = 0; n < NN; ++n) {
+            int x[3] = {(int)(n % N), (int)((n / N) % N), (int)(n / F)};
+            double lap = 0;
+            for (int d = 0; d < 3; ++d) {
+                int i = x[d] % P1, start = x[d] - i - 1;
+                double acc = 0;
+                for (int k = 0; k < PW; ++k) {
+                    double coefk = m->stencil[i * PW + k];
+                    if (coefk == 0.0) continue;
+                    int pos = start + k;
+                    int y[3] = {x[0], x[1], x[2]};
+                    double Vw[3];
+                    int64_t sn;                      /* the node whose S[d] forms the flux */
+                    if (pos < 0 || pos >= N) {
+                        int face = 2 * d + (pos >= N), k2 = 0, tt[2];
+                        for (int q = 0; q < 3; ++q) if (q != d) tt[k2++] = x[q];
+                        int t = tt[0] + N * tt[1];
+                        y[d] = pos < 0 ? 0 : N - 1;
+                        sn = y[0] + N * (y[1] + N * y[2]);
+                        if (m->face_nb[b * 6 + face] < 0) {
+                            const double* X = m->bnd_x + ((int64_t)b * 6 + face) * 3 * F;
+                            double c = cos(wave_phase(m, X, (int)F, t, m->t));
+                            for (int ci = 0; ci < 3; ++ci) Vw[ci] = m->wave_k[ci] * c;
+                        } else {
+                            for (int ci = 0; ci < 3; ++ci)
+                                Vw[ci] = full_ghost(m, N, NN, V, 3 * NN, ci, NN, b, face, t);
+                        }
+                    } else {
+                        y[d] = pos;
+                        sn = y[0] + N * (y[1] + N * y[2]);
+                        for (int ci = 0; ci < 3; ++ci) Vw[ci] = V[(int64_t)b * 3 * NN + ci * NN + sn];
+                    }
+                    double Fd = 0;
+                    for (int ci = 0; ci < 3; ++ci) Fd += cf[(1 + 3 * d + ci) * NN + sn] * Vw[ci];
+                    acc += coefk * Fd;
+                }
+                lap += acc / h;
+            }
+            du[(int64_t)b * 2 * NN + n] = u[(int64_t)b * 2 * NN + NN + n];
+            du[(int64_t)b * 2 * NN + NN + n] = lap / cf[n];
+        }
+    }
+    free(V);
+    return 0;
+}
+
+/* The sqrt(g)-orthogonal projection onto Q_{P-1} of one element's v:
+ * solve (Psi^T W Psi) z = Psi^T W v, v = Psi z, in long double. */
+static void full_project_element(const oracle_mesh* m, const double* cf, double* v, int N, const int* base) {
+    const int P = m->P, P1 = P + 1, n3 = P1 * P1 * P1, m3 = P * P * P;
+    long double L[16][16];
+    for (int i = 0; i < P1; ++i) {
+        long double x = m->nodes[i];
+        L[0][i] = 1.0L;
+        if (P >= 1) L[1][i] = x;
+        for (int k = 2; k <= P; ++k) L[k][i] = ((2 * k - 1) * x * L[k - 1][i] - (k - 1) * L[k - 2][i]) / k;
+    }
+    long double* Gm = (long double*)malloc(sizeof(long double) * m3 * (m3 + 1));
+    if (!Gm) return;
+#define G(i, j) Gm[(i) * (m3 + 1) + (j)]
+    long double W[1000];
+    int64_t idx[1000];
+    for (int nn = 0; nn < n3; ++nn) {
+        int n0 = nn % P1, n1 = (nn / P1) % P1, n2 = nn / (P1 * P1);
+        idx[nn] = (base[0] + n0) + (int64_t)N * ((base[1] + n1) + (int64_t)N * (base[2] + n2));
+        W[nn] = (long double)m->weights[n0] * m->weights[n1] * m->weights[n2] * cf[idx[nn]];
+    }
+    for (int q = 0; q < m3; ++q) {
+        int q0 = q % P, q1 = (q / P) % P, q2 = q / (P * P);
+        for (int r = 0; r < m3; ++r) {
+            int r0 = r % P, r1 = (r / P) % P, r2 = r / (P * P);
+            long double s = 0;
+            for (int nn = 0; nn < n3; ++nn) {
+                int n0 = nn % P1, n1 = (nn / P1) % P1, n2 = nn / (P1 * P1);
+                s += L[q0][n0] * L[q1][n1] * L[q2][n2] * W[nn] * L[r0][n0] * L[r1][n1] * L[r2][n2];
+            }
+            G(q, r) = s;
+        }
+        long double c = 0;
+        for (int nn = 0; nn < n3; ++nn) {
+            int n0 = nn % P1, n1 = (nn / P1) % P1, n2 = nn / (P1 * P1);
+            c += L[q0][n0] * L[q1][n1] * L[q2][n2] * W[nn] * v[idx[nn]];
+        }
+        G(q, m3) = c;
+    }
+    for (int k = 0; k < m3; ++k) {
+        int piv = k;
+        for (int r = k + 1; r < m3; ++r) if (fabsl(G(r, k)) > fabsl(G(piv, k))) piv = r;
+        if (piv != k)
+            for (int j = 0; j <= m3; ++j) { long double t = G(k, j); G(k, j) = G(piv, j); G(piv, j) = t; }
+        for (int r = k + 1; r < m3; ++r) {
+            long double f = G(r, k) / G(k, k);
+            for (int j = k; j <= m3; ++j) G(r, j) -= f * G(k, j);
+        }
+    }
+    long double z[729];
+    for (int k = m3 - 1; k >= 0; --k) {
+        long double s = G(k, m3);
+        for (int j = k + 1; j < m3; ++j) s -= G(k, j) * z[j];
+        z[k] = s / G(k, k);
+    }
+#undef G
+    free(Gm);
+    for (int nn = 0; nn < n3; ++nn) {
+        int n0 = nn % P1, n1 = (nn / P1) % P1, n2 = nn / (P1 * P1);
+        long double s = 0;
+        for (int q = 0; q < m3; ++q) {
+            int q0 = q % P, q1 = (q / P) % P, q2 = q / (P * P);
+            s += L[q0][n0] * L[q1][n1] * L[q2][n2] * z[q];
+        }
+        v[idx[nn]] = (double)s;
+    }
+}
+
+/* The tensor projector on the affine blocks and the element projection on
+ * the others, from the state before truncation (`orig`). */
+static void full_truncate_from(const oracle_mesh* m, const double* orig, double* u) {
+    const int P1 = m->P + 1, E = m->E, N = E * P1;
+    const int64_t NN = (int64_t)N * N * N;
+    ctx_t c;
+    c.m = m;
+    c.P1 = P1;
+    c.N = N;
+    c.NN = NN;
+    memcpy(u, orig, sizeof(double) * 2 * NN * m->nblocks);
+    truncate_with(&c, u);
+#pragma omp parallel for schedule(dynamic)
+    for (int b = 0; b < m->nblocks; ++b) {
+        if (!m->elem_slot[b]) continue;
+        double* v = u + (int64_t)b * 2 * NN + NN;
+        memcpy(v, orig + (int64_t)b * 2 * NN + NN, sizeof(double) * NN);
+        const double* cf = m->coef + (int64_t)b * 10 * NN;
+        for (int e2 = 0; e2 < E; ++e2)
+            for (int e1 = 0; e1 < E; ++e1)
+                for (int e0 = 0; e0 < E; ++e0) {
+                    int base[3] = {e0 * P1, e1 * P1, e2 * P1};
+                    full_project_element(m, cf, v, N, base);
+                }
+    }
+}
+
+int oracle_truncate_full2(const oracle_mesh* m, double* u) {
+    if (!m->truncate) return 0;
+    const int64_t W = 2 * (int64_t)m->E * (m->P + 1) * m->E * (m->P + 1) * m->E * (m->P + 1) * m->nblocks;
+    double* orig = (double*)malloc(sizeof(double) * W);
+    if (!orig) return -1;
+    memcpy(orig, u, sizeof(double) * W);
+    full_truncate_from(m, orig, u);
+    free(orig);
+    return 0;
+}
+
+int oracle_rk4_full(oracle_mesh* m, double* u, double t0, double dt, int nsteps) {
+    const int64_t NN = (int64_t)m->E * (m->P + 1) * m->E * (m->P + 1) * m->E * (m->P + 1);
+    const int64_t W = 2 * NN * m->nblocks;
+    double* k1 = (double*)malloc(sizeof(double) * W);
+    double* k2 = (double*)malloc(sizeof(double) * W);
+    double* k3 = (double*)malloc(sizeof(double) * W);
+    double* k4 = (double*)malloc(sizeof(double) * W);
+    double* y = (double*)malloc(sizeof(double) * W);
+    if (!k1 || !k2 || !k3 || !k4 || !y) { free(k1); free(k2); free(k3); free(k4); free(y); return -1; }
+    int rc = 0;
+    for (int s = 0; s < nsteps && rc == 0; ++s) {
+        const double t = t0 + s * dt;
+        m->t = t;
+        rc |= oracle_rhs_full(m, u, k1);
+        for (int64_t i = 0; i < W; ++i) y[i] = u[i] + dt / 2 * k1[i];
+        rc |= oracle_truncate_full2(m, y);
+        m->t = t + dt / 2;
+        rc |= oracle_rhs_full(m, y, k2);
+        for (int64_t i = 0; i < W; ++i) y[i] = u[i] + dt / 2 * k2[i];
+        rc |= oracle_truncate_full2(m, y);
+        rc |= oracle_rhs_full(m, y, k3);
+        for (int64_t i = 0; i < W; ++i) y[i] = u[i] + dt * k3[i];
+        rc |= oracle_truncate_full2(m, y);
+        m->t = t + dt;
+        rc |= oracle_rhs_full(m, y, k4);
+        for (int64_t i = 0; i < W; ++i) u[i] = u[i] + dt / 6 * (k1[i] + 2 * k2[i] + 2 * k3[i] + k4[i]);
+        rc |= oracle_truncate_full2(m, u);
+    }
+    free(k1); free(k2); free(k3); free(k4); free(y);
+    return rc;
+}
+
+/* 1/2 sum w sqrt(g) (v^2 + |V|^2), block by block in order. */
+int oracle_energy_full(const oracle_mesh* m, const double* u, double* out) {
+    const int P1 = m->P + 1, N = m->E * P1;
+    const int64_t NN = (int64_t)N * N * N;
+    double* V = (double*)malloc(sizeof(double) * 3 * NN * m->nblocks);
+    if (!V) return -1;
+    full_gradient(m, u, V);
+    const double h = 1.0 / N;
+    double e = 0;
+    for (int b = 0; b < m->nblocks; ++b) {
+        const double* cf = m->coef + (int64_t)b * 10 * NN;
+        double s = 0;
+        for (int64_t n = 0; n < NN; ++n) {
+            double w = 1;
+            int64_t r = n;
+            for (int k = 0; k < 3; ++k) { w *= h * P1 / 2.0 * m->weights[(r % N) % P1]; r /= N; }
+            double vv = u[(int64_t)b * 2 * NN + NN + n];
+            double q = vv * vv;
+            for (int ci = 0; ci < 3; ++ci) q += V[(int64_t)b * 3 * NN + ci * NN + n] * V[(int64_t)b * 3 * NN + ci * NN + n];
+            s += w * cf[n] * q;
+        }
+        e += 0.5 * s;
+    }
+    *out = e;
+    free(V);
+    return 0;
+}
+
+/* sqrt(g)-weighted p-norm of u - ref (p = 0: largest |value|). */
+int oracle_norm_full(const oracle_mesh* m, const double* u, const double* ref, int p, int vars_mask, double* out) {
+    const int P1 = m->P + 1, N = m->E * P1;
+    const int64_t NN = (int64_t)N * N * N;
+    const double h = 1.0 / N;
+    double num = 0, vol = 0;
+    for (int b = 0; b < m->nblocks; ++b)
+        for (int var = 0; var < 2; ++var) {
+            if (!(vars_mask & (1 << var))) continue;
+            for (int64_t n = 0; n < NN; ++n) {
+                int64_t o = (int64_t)b * 2 * NN + var * NN + n;
+                double x = fabs(u[o] - (ref ? ref[o] : 0.0));
+                double w = m->coef[(int64_t)b * 10 * NN + n];
+                int64_t r = n;
+                for (int k = 0; k < 3; ++k) { w *= h * P1 / 2.0 * m->weights[(r % N) % P1]; r /= N; }
+                if (p == 0) num = x > num ? x : num;
+                else num += w * pow(x, p);
+                vol += w;
+            }
+        }
+    *out = p == 0 ? num : (vol == 0 ? 0.0 : pow(num / vol, 1.0 / p));
+    return 0;
 }

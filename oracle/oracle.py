@@ -25,7 +25,10 @@ class OracleMesh(ctypes.Structure):
         ("nodes", ctypes.POINTER(ctypes.c_double)), ("weights", ctypes.POINTER(ctypes.c_double)),
         ("stencil", ctypes.POINTER(ctypes.c_double)), ("projector", ctypes.POINTER(ctypes.c_double)),
         ("duals", ctypes.POINTER(ctypes.c_double)), ("coef", ctypes.POINTER(ctypes.c_double)),
-        ("line_weights", ctypes.POINTER(ctypes.c_double)),
+        ("line_weights", ctypes.POINTER(ctypes.c_double)), ("metric", ctypes.c_int),
+        ("face_nb", ctypes.POINTER(ctypes.c_int32)), ("face_code", ctypes.POINTER(ctypes.c_int32)),
+        ("elem_slot", ctypes.POINTER(ctypes.c_int32)), ("bnd_x", ctypes.POINTER(ctypes.c_double)),
+        ("wave_k", ctypes.c_double * 3), ("wave_phi", ctypes.c_double), ("t", ctypes.c_double),
     ]
 
 
@@ -46,6 +49,11 @@ def lib():
         L.oracle_norm.argtypes = [mp, vp, vp, ctypes.c_int, ctypes.c_int, dp]
         L.oracle_modes.argtypes = [mp, vp, ctypes.c_int, ctypes.c_int, vp, vp, vp, ctypes.c_double, vp]
         L.oracle_threads.restype = ctypes.c_int
+        L.oracle_rhs_full.argtypes = [mp, vp, vp]
+        L.oracle_truncate_full2.argtypes = [mp, vp]
+        L.oracle_rk4_full.argtypes = [mp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int]
+        L.oracle_energy_full.argtypes = [mp, vp, dp]
+        L.oracle_norm_full.argtypes = [mp, vp, vp, ctypes.c_int, ctypes.c_int, dp]
         _lib = L
     return _lib
 
@@ -169,3 +177,81 @@ class Oracle:
 
 def threads():
     return lib().oracle_threads()
+
+
+class BallOracle(Oracle):
+    """The oracle on a ball forest (full metric, glue, Dirichlet plane wave):
+    coef (sqrt(g), S) from the geometry, the face table, the blocks whose
+    truncation is the per-element projection; the projections themselves are
+    solved by the oracle."""
+
+    def __init__(self, forest, P, tables, wave, truncate=True):
+        self.forest = forest
+        self.P = P
+        self.D = 3
+        self.N = forest.N
+        self.E = forest.N // (P + 1)
+        self.NN = self.N ** 3
+        self.nblocks = forest.nleaves()
+        t = golden_tables(P)
+        a = dict(nodes=np.ascontiguousarray(t["nodes"]), weights=np.ascontiguousarray(t["weights"]),
+                 stencil=np.ascontiguousarray(t["stencil"]).reshape(-1),
+                 projector=np.ascontiguousarray(t["truncate"]).reshape(-1),
+                 duals=np.ascontiguousarray(t["duals"]).reshape(-1),
+                 level=np.zeros(self.nblocks, dtype=np.int32),
+                 corner=np.zeros(3 * self.nblocks, dtype=np.int64),
+                 coef=np.ascontiguousarray(tables["coef"], dtype=np.float64),
+                 face_nb=np.ascontiguousarray(forest.face_nb, dtype=np.int32),
+                 face_code=np.ascontiguousarray(forest.face_code, dtype=np.int32),
+                 elem_slot=np.ascontiguousarray(tables["elem_slot"], dtype=np.int32),
+                 bnd_x=np.ascontiguousarray(tables["bnd_x"], dtype=np.float64))
+        self._arrays = a
+        m = OracleMesh()
+        m.D, m.P, m.E, m.nblocks, m.truncate = 3, P, self.E, self.nblocks, 1 if truncate else 0
+        for k in range(3):
+            m.roots[k], m.periodic[k], m.reflecting[k], m.lo[k], m.hi[k] = 1, 0, 0, 0.0, 1.0
+            m.wave_k[k] = wave.k[k]
+        m.wave_phi = wave.phi
+        m.metric = 2
+        dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int32)
+        m.level = a["level"].ctypes.data_as(ip)
+        m.corner = a["corner"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        for k in ("nodes", "weights", "stencil", "projector", "duals", "coef", "bnd_x"):
+            setattr(m, k, a[k].ctypes.data_as(dp))
+        for k in ("face_nb", "face_code", "elem_slot"):
+            setattr(m, k, a[k].ctypes.data_as(ip))
+        self.mesh = m
+
+    def rhs(self, u, t=0.0):
+        u = self._vec(u)
+        du = np.zeros_like(u)
+        self.mesh.t = t
+        if lib().oracle_rhs_full(ctypes.byref(self.mesh), u.ctypes.data, du.ctypes.data):
+            raise MemoryError("oracle_rhs_full failed")
+        return du
+
+    def truncate(self, u):
+        u = self._vec(u).copy()
+        lib().oracle_truncate_full2(ctypes.byref(self.mesh), u.ctypes.data)
+        return u
+
+    def rk4(self, u, dt, nsteps, t0=0.0):
+        u = self._vec(u).copy()
+        if lib().oracle_rk4_full(ctypes.byref(self.mesh), u.ctypes.data, float(t0), float(dt), int(nsteps)):
+            raise MemoryError("oracle_rk4_full failed")
+        return u
+
+    def energy(self, u, t=0.0):
+        u = self._vec(u)
+        e = ctypes.c_double()
+        self.mesh.t = t
+        lib().oracle_energy_full(ctypes.byref(self.mesh), u.ctypes.data, ctypes.byref(e))
+        return e.value
+
+    def norm(self, u, p=2, vars_mask=3, ref=None):
+        u = self._vec(u)
+        r = None if ref is None else self._vec(ref)
+        out = ctypes.c_double()
+        lib().oracle_norm_full(ctypes.byref(self.mesh), u.ctypes.data, None if r is None else r.ctypes.data,
+                               int(p), int(vars_mask), ctypes.byref(out))
+        return out.value

@@ -1,0 +1,95 @@
+"""The seven-patch ball (full metric, quarter-turn glue, Dirichlet sphere):
+the host geometry and glue, and the oracle against the reference's published
+table. No GPU."""
+import numpy as np
+import pytest
+
+from ball_cases import ball_setup, oracle_sevenpatch_errors
+from twoldg.ball import face_plane_logical, orient, sevenpatch_forest
+from twoldg.element import Element
+
+
+def test_ball_forest_and_glue_continuity():
+    # 8 + 6 * 8 blocks at roots (2, 2); 448 at (4, 4); every glued face's
+    # nodes coincide with the neighbour's under the face table's orientation
+    # (the property the reference fixes the quarter turns by)
+    for roots, nb, nbnd in (((2, 2), 56, 24), ((4, 4), 448, 96)):
+        f, geo = sevenpatch_forest(np.float64, 3, 2, roots=roots)
+        assert f.nleaves() == nb
+        assert (f.face_nb < 0).sum() == nbnd
+    f, geo = sevenpatch_forest(np.float64, 2, 2, roots=(2, 2))
+    offs = Element(np.float64, 2).offsets.astype(np.float64)
+    N = f.N
+    A, B = np.meshgrid(np.arange(N), np.arange(N), indexing="xy")
+    A, B = A.reshape(-1), B.reshape(-1)
+    quarter_turns = 0
+    for b, (p, c) in enumerate(f.blocks):
+        for face in range(6):
+            nb = f.face_nb[b * 6 + face]
+            if nb < 0:
+                X = np.stack(geo.position(face_plane_logical(c, N, offs, face), p), axis=-1)
+                assert np.allclose(np.linalg.norm(X, axis=1), geo.R1)
+                continue
+            code = f.face_code[b * 6 + face]
+            nf, o = code & 15, code >> 4
+            quarter_turns += (o & 1)
+            pn, cn = f.blocks[nb]
+            X1 = np.stack(geo.position(face_plane_logical(c, N, offs, face), p), axis=-1)
+            X2 = np.stack(geo.position(face_plane_logical(cn, N, offs, nf), pn), axis=-1)
+            a2, b2 = orient(A, B, o, N)
+            assert np.allclose(X1, X2[a2 + N * b2], atol=1e-12)
+    assert quarter_turns > 0
+
+
+def test_frame_is_the_inverse_jacobian():
+    f, geo = sevenpatch_forest(np.float64, 2, 2, roots=(2, 2))
+    xi = (np.array([0.3, 1.7]), np.array([0.9, 0.2]), np.array([1.1, 1.5]))
+    for p in range(7):
+        J, S = geo.frame(xi, p)
+        eps = 1e-6
+        x0 = np.array(geo.position(xi, p))
+        Jm = np.empty((2, 3, 3))
+        for j in range(3):
+            xp = list(xi)
+            xp[j] = xi[j] + eps
+            Jm[:, :, j] = ((np.array(geo.position(tuple(xp), p)) - x0) / eps).T
+        assert np.allclose(J, np.abs(np.linalg.det(Jm)), rtol=1e-5)
+        for k in range(2):
+            assert np.allclose(S[k] @ Jm[k], J[k] * np.eye(3), atol=1e-4 * J[k])
+
+
+@pytest.mark.parametrize("P,row", [(2, (6.07e-2, 7.81e-2, 0.016)), (3, (8.83e-3, 1.14e-2, 0.035))])
+def test_sevenpatch_published_table(P, row):
+    # reference CODE.md:4247-4252: k = (1.1, -0.7, 0.5), phi = 0.3, Lc = 1,
+    # R1 = 3, t = 1, roots (2, 2), E = 2, truncated, cfl 1/2: sqrt(g)-weighted
+    # L2 errors of u and v, and 1 - E1/E0 (the energy the wave carries out)
+    r = oracle_sevenpatch_errors(P, 2, (2, 2))
+    assert r["u"] == pytest.approx(row[0], rel=0.01)
+    assert r["v"] == pytest.approx(row[1], rel=0.01)
+    assert 1 - r["energy"] / r["energy0"] == pytest.approx(row[2], abs=0.0015)
+
+
+def test_ball_laplacian_is_self_adjoint_away_from_the_sphere():
+    # with homogeneous data (a field vanishing on the sphere's ghosts), the
+    # full-metric Laplacian is self-adjoint in sqrt(g)-weighted quadrature over
+    # the cube and its glued shells: checked on fields supported inside |x| < 1.5
+    forest, geo, wave, tables, o = ball_setup(2, 2, (2, 2), truncate=False, k=(0.0, 0.0, 0.0), phi=0.0)
+    from ball_cases import physical_nodes
+    X = physical_nodes(forest, tables)
+    r = np.linalg.norm(X, axis=1)
+    bump = lambda c: np.where(r < 1.5, np.cos(np.pi * r / 3.0) ** 4, 0.0) * (1 + 0.3 * X[:, c])
+    nb, NN = forest.nleaves(), forest.N ** 3
+
+    def lap(a):
+        s = np.zeros((nb, 2, NN))
+        s[:, 0] = a
+        return o.rhs(s.reshape(-1)).reshape(nb, 2, NN)[:, 1]
+    P1 = 3
+    N = forest.N
+    wq = Element(np.float64, 2).weights
+    w1 = (1.0 / N) * P1 / 2 * wq[np.arange(N) % P1]
+    w = np.kron(np.kron(w1, w1), w1)[None, :] * tables["coef"].reshape(nb, 10, NN)[:, 0]
+    a, b = bump(0), bump(1)
+    la, lb = lap(a), lap(b)
+    lhs, rhs = np.sum(w * b * la), np.sum(w * lb * a)
+    assert abs(lhs - rhs) < 1e-10 * np.sum(np.abs(w * b * la))

@@ -77,10 +77,16 @@ struct Group {
     std::unique_ptr<Ops> ops;
     DevBuf d_items, d_cf, fu[2], fog[2], ugd, gfd, ggd, d_part, d_part2;
     bool metric = false;
-    std::vector<double> coef;             // per item (1 + D) N^D, then converted to the field type
+    int full = 0;                         // 1: the full metric's two-pass stage
+    std::vector<double> coef;             // per item (1 + D) N^D (or 1 + D^2: full), then the field type
     std::vector<std::vector<double>> trm, trd;  // per member: (P+1, E, nblocks, D)
     std::vector<int> member_blocks;
     DevBuf d_coef, d_trm, d_trd;
+    // full metric
+    DevBuf d_V, d_fv, d_bndx, d_eslot, d_ew, d_echol;
+    std::vector<double> bndx, ew, echol;
+    std::vector<int> eslot;
+    double wave_k[3] = {0, 0, 0}, wave_phi = 0;
     int nslots() const { return (int)items.size() * 2 * D; }
 };
 
@@ -106,7 +112,8 @@ struct twoldg_runner {
     std::vector<std::unique_ptr<Group>> groups;
     std::vector<int64_t> offsets;   // per problem, words
     std::vector<double> hmin;       // per problem
-    DevBuf y, acc, comp, d_rk;
+    DevBuf y, acc, comp, d_rk, d_tinfo;
+    std::vector<double> h_tinfo;               // per problem: t_n, dt (the full metric's stage times)
     std::vector<double> h_dts;                 // the dt each problem's coefficients were made for
     std::vector<unsigned char> h_rk;           // per problem dt/6, dt/3, dt/2, dt in the field type
     cudaGraphExec_t gexec = nullptr;
@@ -135,12 +142,19 @@ struct twoldg_runner {
             if (!tables().get(m.P))
                 return fail(TWOLDG_EUNSUP, "element order P = " + std::to_string(m.P) + " is not built (1..6)");
             const bool metric = d.coef != nullptr;
-            if (metric && (!d.trunc_modes || !d.trunc_duals))
+            const int full = d.metric == 2 ? 1 : 0;
+            if (full) {
+                if (m.D != 3) return fail(TWOLDG_EINVAL, "the full metric is three-dimensional");
+                if (!d.coef || !d.elem_slot || !d.bnd_x)
+                    return fail(TWOLDG_EINVAL, "a full metric needs coef, elem_slot and bnd_x");
+                if (n != 1) return fail(TWOLDG_EUNSUP, "a full-metric problem is stepped alone, not in a batch");
+            }
+            if (metric && !full && (!d.trunc_modes || !d.trunc_duals))
                 return fail(TWOLDG_EINVAL, "a metric (coef) needs its truncation pairs (trunc_modes, trunc_duals)");
             if (metric && !m.cf.empty())
                 return fail(TWOLDG_EINVAL, "a geometry takes refinement only in an affine patch, which a diagonal "
                                            "metric's coefficients do not describe: no coarse-fine faces with coef");
-            auto key = std::make_tuple(m.D, m.P, m.E, (d.truncate ? 1 : 0) + (metric ? 2 : 0));
+            auto key = std::make_tuple(m.D, m.P, m.E, (d.truncate ? 1 : 0) + (metric ? 2 : 0) + (full ? 4 : 0));
             auto gi = gidx.find(key);
             Group* g;
             if (gi == gidx.end()) {
@@ -149,6 +163,7 @@ struct twoldg_runner {
                 g = groups.back().get();
                 g->D = m.D; g->P = m.P; g->E = m.E; g->truncate = d.truncate ? 1 : 0;
                 g->metric = metric;
+                g->full = full;
                 g->NN = m.NN;
                 for (int q = 0; q < m.D - 1; ++q) g->F *= m.N;
                 Ops* ops = nullptr;
@@ -176,7 +191,22 @@ struct twoldg_runner {
                 g->cf.push_back(c);
             }
             g->h.insert(g->h.end(), m.h.begin(), m.h.end());
-            if (metric) {
+            if (full) {
+                const size_t nc = (size_t)(1 + m.D * m.D) * m.NN * m.nblocks;
+                g->coef.insert(g->coef.end(), d.coef, d.coef + nc);
+                size_t F = 1;
+                for (int q = 0; q < m.D - 1; ++q) F *= m.N;
+                g->bndx.assign(d.bnd_x, d.bnd_x + (size_t)m.nblocks * 2 * m.D * 3 * F);
+                g->eslot.assign(d.elem_slot, d.elem_slot + m.nblocks);
+                const size_t P1 = m.P + 1, ne = (size_t)m.E * m.E * m.E;
+                const size_t n3 = P1 * P1 * P1, m3 = (size_t)m.P * m.P * m.P;
+                if (d.elem_ntab > 0) {
+                    g->ew.assign(d.elem_w, d.elem_w + n3 * ne * d.elem_ntab);
+                    g->echol.assign(d.elem_chol, d.elem_chol + m3 * m3 * ne * d.elem_ntab);
+                }
+                for (int q = 0; q < 3; ++q) g->wave_k[q] = d.wave_k[q];
+                g->wave_phi = d.wave_phi;
+            } else if (metric) {
                 const size_t nc = (size_t)(1 + m.D) * m.NN * m.nblocks;
                 g->coef.insert(g->coef.end(), d.coef, d.coef + nc);
                 const size_t nt = (size_t)(m.P + 1) * m.E * m.nblocks * m.D;
@@ -215,7 +245,19 @@ struct twoldg_runner {
             CK(g.ggd.alloc(dbytes));
             CK(g.d_part.alloc(g.items.size() * sizeof(double)));
             CK(g.d_part2.alloc(g.items.size() * sizeof(double)));
-            if (g.metric) {
+            if (g.full) {
+                int r = upload_t(g.d_coef, g.coef);
+                if (!r) r = upload_t(g.d_ew, g.ew.empty() ? std::vector<double>(1, 0.0) : g.ew);
+                if (!r) r = upload_t(g.d_echol, g.echol.empty() ? std::vector<double>(1, 0.0) : g.echol);
+                if (r) return r;
+                CK(g.d_V.alloc((size_t)g.items.size() * 3 * g.NN * wsize));
+                CK(g.d_fv.alloc((size_t)g.nslots() * 3 * g.F * wsize));
+                CK(cudaMemset(g.d_fv.p, 0, (size_t)g.nslots() * 3 * g.F * wsize));
+                CK(g.d_bndx.alloc(g.bndx.size() * sizeof(double)));
+                CK(cudaMemcpy(g.d_bndx.p, g.bndx.data(), g.bndx.size() * sizeof(double), cudaMemcpyHostToDevice));
+                CK(g.d_eslot.alloc(g.eslot.size() * sizeof(int)));
+                CK(cudaMemcpy(g.d_eslot.p, g.eslot.data(), g.eslot.size() * sizeof(int), cudaMemcpyHostToDevice));
+            } else if (g.metric) {
                 // the per-line tables of every member into the group's (P+1, E, nitems, D) layout
                 const int P1 = g.P + 1, nit = (int)g.items.size();
                 std::vector<double> tm((size_t)P1 * g.E * nit * g.D), td(tm.size());
@@ -247,6 +289,9 @@ struct twoldg_runner {
             CK(cudaMemset(comp.p, 0, sbytes));
         }
         CK(d_rk.alloc(n * 4 * wsize));
+        CK(d_tinfo.alloc(n * 2 * sizeof(double)));
+        h_tinfo.assign(n * 2, 0.0);
+        CK(cudaMemcpy(d_tinfo.p, h_tinfo.data(), n * 2 * sizeof(double), cudaMemcpyHostToDevice));
         h_dts.assign(n, 0.0);
         h_rk.assign(n * 4 * wsize, 0);
         CK(cudaMemcpy(d_rk.p, h_rk.data(), h_rk.size(), cudaMemcpyHostToDevice));
@@ -286,6 +331,46 @@ struct twoldg_runner {
         return p;
     }
 
+    FmPtrs fptrs(Group& g, void* u, int in) {
+        FmPtrs p{};
+        p.u = u;
+        p.y = y.p;
+        p.acc = acc.p;
+        p.comp = comp.p;
+        p.fu_in = g.fu[in].p;
+        p.fu_out = g.fu[1 - in].p;
+        p.V = g.d_V.p;
+        p.fv = g.d_fv.p;
+        p.coef = g.d_coef.p;
+        p.rk = d_rk.p;
+        p.tinfo = (const double*)d_tinfo.p;
+        p.bnd_x = (const double*)g.d_bndx.p;
+        for (int q = 0; q < 3; ++q) p.wave_k[q] = g.wave_k[q];
+        p.wave_phi = g.wave_phi;
+        p.eslot = (const int*)g.d_eslot.p;
+        p.ew = g.d_ew.p;
+        p.echol = g.d_echol.p;
+        p.partial = (double*)g.d_part.p;
+        return p;
+    }
+
+    // the full metric's stage times: t_n and dt of every problem
+    int set_time(double t, const double* dts) {
+        for (int k = 0; k < nproblems; ++k) {
+            h_tinfo[2 * k] = t;
+            h_tinfo[2 * k + 1] = dts ? dts[k] : 0.0;
+        }
+        CK(cudaMemcpyAsync(d_tinfo.p, h_tinfo.data(), h_tinfo.size() * sizeof(double), cudaMemcpyHostToDevice,
+                           stream));
+        return TWOLDG_OK;
+    }
+
+    bool any_full() const {
+        for (auto& g : groups)
+            if (g->full) return true;
+        return false;
+    }
+
     int export_all(const void* u) {
         for (auto& gp : groups) {
             Group& g = *gp;
@@ -308,6 +393,13 @@ struct twoldg_runner {
         for (int s = 1; s <= 4; ++s) {
             for (auto& gp : groups) {
                 Group& g = *gp;
+                if (g.full) {
+                    FmPtrs fp = fptrs(g, u, in);
+                    CK(g.ops->fm_gradient((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, fp, stream));
+                    CK(g.ops->fm_stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, fp,
+                                       stream));
+                    continue;
+                }
                 int r = cf_all(g, in);
                 if (r) return r;
                 StagePtrs p = ptrs(g, u, in);
@@ -316,10 +408,16 @@ struct twoldg_runner {
             }
             in = 1 - in;
         }
+        if (any_full()) {
+            fm_advance_time(stream);
+            CK(cudaGetLastError());
+        }
         return TWOLDG_OK;
     }
 
-    int rk4(void* u, const double* dts, int nsteps) {
+    void fm_advance_time(cudaStream_t s);
+
+    int rk4(void* u, const double* dts, int nsteps, double t0 = 0.0) {
         if (!u) return fail(TWOLDG_EINVAL, "u is NULL");
         if (nsteps < 0) return fail(TWOLDG_EINVAL, "nsteps is negative");
         bool changed = false;
@@ -344,6 +442,10 @@ struct twoldg_runner {
             CK(cudaMemsetAsync(comp.p, 0, (size_t)total_words * wsize, stream));
             comp_u = u;
         }
+        if (any_full()) {
+            int rr = set_time(t0, dts);
+            if (rr) return rr;
+        }
         if (nsteps == 0) return TWOLDG_OK;
         int r = export_all(u);
         if (r) return r;
@@ -365,6 +467,12 @@ struct twoldg_runner {
         return TWOLDG_OK;
     }
 };
+
+namespace twoldg {
+void fm_advance_time_launch(double* tinfo, int nproblems, cudaStream_t s);
+}
+
+void twoldg_runner::fm_advance_time(cudaStream_t s) { fm_advance_time_launch((double*)d_tinfo.p, nproblems, s); }
 
 struct twoldg_problem : twoldg_runner {
     int D = 0, P = 0, E = 0;
@@ -440,12 +548,20 @@ int twoldg_min_spacing(const twoldg_problem* p, double* h) {
 }
 
 int twoldg_rhs(twoldg_problem* p, void* du, const void* u, double t) {
-    (void)t;
     if (!p || !du || !u) return fail(TWOLDG_EINVAL, "NULL argument");
     if (du == u) return fail(TWOLDG_EINVAL, "du and u must not alias: the right-hand side never writes u");
     int r = p->export_all(u);
     if (r) return r;
     Group& g = *p->groups[0];
+    if (g.full) {
+        r = p->set_time(t, nullptr);
+        if (r) return r;
+        FmPtrs fp = p->fptrs(g, const_cast<void*>(u), 0);
+        fp.du = du;
+        CK(g.ops->fm_gradient((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, 0, fp, p->stream));
+        CK(g.ops->fm_stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, 0, 0, fp, p->stream));
+        return TWOLDG_OK;
+    }
     r = p->cf_all(g, 0);
     if (r) return r;
     StagePtrs s = p->ptrs(g, const_cast<void*>(u), 0);
@@ -458,15 +574,19 @@ int twoldg_truncate(twoldg_problem* p, void* u) {
     if (!p || !u) return fail(TWOLDG_EINVAL, "NULL argument");
     Group& g = *p->groups[0];
     if (!g.truncate) return TWOLDG_OK;
+    if (g.full) {
+        FmPtrs fp = p->fptrs(g, u, 0);
+        CK(g.ops->fm_truncate((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, fp, p->stream));
+        return TWOLDG_OK;
+    }
     CK(g.ops->truncate((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, u,
                        g.metric ? g.d_trm.p : nullptr, g.metric ? g.d_trd.p : nullptr, p->stream));
     return TWOLDG_OK;
 }
 
 int twoldg_rk4_step(twoldg_problem* p, void* u, double t, double dt, int32_t nsteps) {
-    (void)t;
     if (!p) return fail(TWOLDG_EINVAL, "NULL problem");
-    return p->rk4(u, &dt, nsteps);
+    return p->rk4(u, &dt, nsteps, t);
 }
 
 int twoldg_reset_compensation(twoldg_problem* p) {
@@ -476,15 +596,22 @@ int twoldg_reset_compensation(twoldg_problem* p) {
 }
 
 int twoldg_energy(twoldg_problem* p, const void* u, double t, double* energy) {
-    (void)t;
     if (!p || !u || !energy) return fail(TWOLDG_EINVAL, "NULL argument");
     int r = p->export_all(u);
     if (r) return r;
     Group& g = *p->groups[0];
-    r = p->cf_all(g, 0);
-    if (r) return r;
-    StagePtrs s = p->ptrs(g, const_cast<void*>(u), 0);
-    CK(g.ops->energy((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, p->stream));
+    if (g.full) {
+        r = p->set_time(t, nullptr);
+        if (r) return r;
+        FmPtrs fp = p->fptrs(g, const_cast<void*>(u), 0);
+        CK(g.ops->fm_gradient((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, 5, fp, p->stream));
+        CK(g.ops->fm_energy((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, fp, p->stream));
+    } else {
+        r = p->cf_all(g, 0);
+        if (r) return r;
+        StagePtrs s = p->ptrs(g, const_cast<void*>(u), 0);
+        CK(g.ops->energy((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, p->stream));
+    }
     std::vector<double> part(g.items.size());
     CK(cudaMemcpyAsync(part.data(), g.d_part.p, part.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
     CK(cudaStreamSynchronize(p->stream));
@@ -500,7 +627,8 @@ int twoldg_norm(twoldg_problem* p, const void* u, const void* ref, int32_t pnorm
     if (vars_mask < 1 || vars_mask > 3) return fail(TWOLDG_EINVAL, "vars_mask must select u (1), v (2) or both (3)");
     Group& g = *p->groups[0];
     CK(g.ops->norm((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, u, ref, pnorm, vars_mask,
-                   (double*)g.d_part.p, (double*)g.d_part2.p, g.metric ? g.d_coef.p : nullptr, p->stream));
+                   (double*)g.d_part.p, (double*)g.d_part2.p, g.metric ? g.d_coef.p : nullptr,
+                   g.full ? 1 + g.D * g.D : 1 + g.D, p->stream));
     std::vector<double> num(g.items.size()), vol(g.items.size());
     CK(cudaMemcpyAsync(num.data(), g.d_part.p, num.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
     CK(cudaMemcpyAsync(vol.data(), g.d_part2.p, vol.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));

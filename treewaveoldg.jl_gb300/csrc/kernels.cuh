@@ -946,7 +946,8 @@ __global__ void __launch_bounds__(256) energy_kernel(StageArgs<T> a, Tab<T, P> t
 // means the largest |x - ref|.
 template <typename T, int D, int P>
 __global__ void norm_kernel(const BlockItem* items, int nitems, int E, const T* u, const T* ref, int p,
-                            int vars_mask, Tab<T, P> tb, double* part_num, double* part_vol, const T* coef) {
+                            int vars_mask, Tab<T, P> tb, double* part_num, double* part_vol, const T* coef,
+                            int ncoef) {
     __shared__ double red[32];
     constexpr int P1 = P + 1;
     const int N = E * P1;
@@ -960,7 +961,7 @@ __global__ void norm_kernel(const BlockItem* items, int nitems, int E, const T* 
             int m = n;
             for (int k = 0; k < D; ++k) { w *= wscale * (double)tb.wq[(m % N) % P1]; m /= N; }
             // on a geometry the norm is weighted by sqrt(g): the physical volume
-            if (coef) w *= (double)coef[(int64_t)item * (1 + D) * NN + n];
+            if (coef) w *= (double)coef[(int64_t)item * ncoef * NN + n];
             for (int var = 0; var < 2; ++var) {
                 if (!(vars_mask & (1 << var))) continue;
                 int64_t o = it.off + (int64_t)var * NN + n;

@@ -11,6 +11,7 @@ struct BlockItem {
     int32_t nb[6];      // face slot whose exports give face f's ghosts
     uint32_t flags;     // bit f: face f is dense (coarse-fine); bit 8+f: gradient ghost odd
     int32_t problem;    // index into the per-problem time steps
+    uint32_t orient;    // 3 bits per face: the face plane's orientation across a glue
     double h;           // the block's spacing
 };
 

@@ -35,6 +35,48 @@ struct Key {
 
 }  // namespace
 
+// An explicit face table (a forest of glued patches): neighbours, faces and
+// orientations as given; a face with no neighbour is a boundary face.
+static bool build_explicit(const twoldg_desc& d, Mesh& m, std::string& err) {
+    std::ostringstream es;
+    const int D = d.dim;
+    m.h.resize(d.nblocks);
+    m.items.assign(d.nblocks, BlockItem{});
+    m.hmin = INFINITY;
+    const double cell = (d.hi[0] - d.lo[0]) / d.roots[0];
+    for (int b = 0; b < d.nblocks; ++b) {
+        if (d.level[b] != 0) { err = "a forest with an explicit face table takes level-0 blocks only"; return false; }
+        m.h[b] = cell / m.N;
+        m.hmin = std::fmin(m.hmin, m.h[b]);
+        BlockItem& it = m.items[b];
+        it.off = (int64_t)b * 2 * m.NN;
+        it.slot = b * 2 * D;
+        it.h = m.h[b];
+        for (int f = 0; f < 6; ++f) it.nb[f] = -1;
+        for (int f = 0; f < 2 * D; ++f) {
+            const int nb = d.face_nb[b * 2 * D + f];
+            const int code = d.face_code[b * 2 * D + f];
+            if (nb < 0) { m.nwall++; continue; }
+            const int nf = code & 15, o = (code >> 4) & 7;
+            if (nb >= d.nblocks || nf >= 2 * D) {
+                es << "block " << b << " face " << f << " names block " << nb << " face " << nf;
+                err = es.str();
+                return false;
+            }
+            if (d.face_nb[nb * 2 * D + nf] != b) {
+                es << "block " << b << " face " << f << " and block " << nb << " face " << nf
+                   << " do not name each other";
+                err = es.str();
+                return false;
+            }
+            it.nb[f] = nb * 2 * D + nf;
+            it.orient |= (uint32_t)o << (3 * f);
+            m.nsame++;
+        }
+    }
+    return true;
+}
+
 bool build_mesh(const twoldg_desc& d, Mesh& m, std::string& err) {
     std::ostringstream es;
     const int D = d.dim;
@@ -61,7 +103,7 @@ bool build_mesh(const twoldg_desc& d, Mesh& m, std::string& err) {
         if (d.periodic[k] && d.reflecting[k]) {
             es << "dimension " << k << " is both periodic and reflecting"; err = es.str(); return false;
         }
-        if (!d.periodic[k] && !d.reflecting[k]) {
+        if (!d.face_nb && !d.periodic[k] && !d.reflecting[k]) {
             es << "dimension " << k << " is neither periodic nor reflecting: the flat problem's outer faces are "
                << "filled by periodicity or by the wall's mirror";
             err = es.str();
@@ -73,6 +115,10 @@ bool build_mesh(const twoldg_desc& d, Mesh& m, std::string& err) {
             err = "root blocks must be cubes: one spacing per block, as the reference's per-block h";
             return false;
         }
+    }
+    if (d.face_nb) {
+        if (!d.face_code) { err = "face_nb needs face_code"; return false; }
+        return build_explicit(d, m, err);
     }
     std::map<Key, int> leaves;
     double volume = 0;

@@ -31,6 +31,29 @@ struct StagePtrs {
     const void* trd;
 };
 
+// Buffers and data of the full-metric passes (fullmetric.cuh).
+struct FmPtrs {
+    void* u;
+    void* y;
+    void* acc;
+    void* comp;
+    void* du;
+    const void* fu_in;
+    void* fu_out;
+    void* V;
+    void* fv;
+    const void* coef;
+    const void* rk;
+    const double* tinfo;
+    const double* bnd_x;
+    double wave_k[3];
+    double wave_phi;
+    const int* eslot;
+    const void* ew;
+    const void* echol;
+    double* partial;
+};
+
 class Ops {
 public:
     virtual ~Ops() {}
@@ -47,10 +70,21 @@ public:
                               const StagePtrs& p, int grid, cudaStream_t s) const = 0;
     virtual cudaError_t energy(const BlockItem* items, int nitems, int E, const StagePtrs& p,
                                cudaStream_t s) const = 0;
+    // coef: sqrt(g) at variable 0 of ncoef per node (NULL: flat)
     virtual cudaError_t norm(const BlockItem* items, int nitems, int E, const void* u, const void* ref, int p,
-                             int vars_mask, double* num, double* vol, const void* coef, cudaStream_t s) const = 0;
+                             int vars_mask, double* num, double* vol, const void* coef, int ncoef,
+                             cudaStream_t s) const = 0;
     virtual cudaError_t truncate(const BlockItem* items, int nitems, int E, void* u, const void* trm,
                                  const void* trd, cudaStream_t s) const = 0;
+    // full metric (D = 3): mode 0 rhs, 1..4 RK stages, 5 energy; returns cudaErrorNotSupported for D != 3
+    virtual cudaError_t fm_gradient(const BlockItem* items, int nitems, int E, int mode, const FmPtrs& p,
+                                    cudaStream_t s) const = 0;
+    virtual cudaError_t fm_stage(const BlockItem* items, int nitems, int E, int mode, int truncate,
+                                 const FmPtrs& p, cudaStream_t s) const = 0;
+    virtual cudaError_t fm_truncate(const BlockItem* items, int nitems, int E, const FmPtrs& p,
+                                    cudaStream_t s) const = 0;
+    virtual cudaError_t fm_energy(const BlockItem* items, int nitems, int E, const FmPtrs& p,
+                                  cudaStream_t s) const = 0;
     virtual cudaError_t maxabs(const BlockItem* items, int nitems, int E, const void* u, int var, double* part,
                                cudaStream_t s) const = 0;
     // modes[0..nq): Legendre modes; weights/pows per mode; post factor; result tau (E^D per block)

@@ -2,10 +2,12 @@
 // launches the kernels of kernels.cuh with them.
 #pragma once
 #include <algorithm>
+#include <cmath>
 
 #include "kernels.cuh"
 #include "ops.h"
 #include "stage3r.cuh"
+#include "fullmetric.cuh"
 
 namespace twoldg {
 
@@ -47,6 +49,22 @@ public:
         if constexpr (D == 3) {
             set_attrs(stage3r_kernel<T, P, 2, COMP>);
             set_attrs(stage3r_kernel<T, P, 4, COMP>);
+            set_attrs(fm_gradient_kernel<T, P>);
+            set_attrs(fm_stage_kernel<T, P, COMP>);
+            set_attrs(fm_truncate_kernel<T, P>);
+            // Legendre L_q, q < P, at the Gauss-Lobatto nodes, for the full metric's truncation
+            for (int i = 0; i <= P; ++i) {
+                double x = (double)t.nodes[i], l0 = 1, l1 = x;
+                for (int q = 0; q < P; ++q) {
+                    double lq = q == 0 ? l0 : q == 1 ? l1 : 0;
+                    if (q >= 2) {
+                        double a = 1, b = x;
+                        for (int kk = 2; kk <= q; ++kk) { double c = ((2 * kk - 1) * x * b - (kk - 1) * a) / kk; a = b; b = c; }
+                        lq = b;
+                    }
+                    ft_.L[q][i] = (T)lq;
+                }
+            }
         }
         // the stage kernels hold whole blocks in shared memory: take the largest carveout
         cudaFuncSetAttribute(stage_kernel<T, D, P, COMP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
@@ -195,9 +213,10 @@ public:
     }
 
     cudaError_t norm(const BlockItem* items, int nitems, int E, const void* u, const void* ref, int p,
-                     int vars_mask, double* num, double* vol, const void* coef, cudaStream_t s) const override {
+                     int vars_mask, double* num, double* vol, const void* coef, int ncoef,
+                     cudaStream_t s) const override {
         norm_kernel<T, D, P><<<std::min(nitems, kMaxGrid), 256, 0, s>>>(
-            items, nitems, E, (const T*)u, (const T*)ref, p, vars_mask, tb_, num, vol, (const T*)coef);
+            items, nitems, E, (const T*)u, (const T*)ref, p, vars_mask, tb_, num, vol, (const T*)coef, ncoef);
         return cudaGetLastError();
     }
 
@@ -209,6 +228,84 @@ public:
         kern<<<std::min(nitems, kMaxGrid), 256, smem, s>>>(items, nitems, E, (T*)u, tb_, (const T*)trm,
                                                           (const T*)trd);
         return cudaGetLastError();
+    }
+
+    // ---- full metric (3D)
+    FmTab<T, P> ft_;
+    FmArgs<T> fm_args(const BlockItem* items, int nitems, int E, int mode, int truncate, const FmPtrs& p) const {
+        FmArgs<T> a{};
+        a.items = items;
+        a.nitems = nitems;
+        a.E = E;
+        a.mode = mode;
+        a.truncate = truncate;
+        a.u = (T*)p.u;
+        a.y = (T*)p.y;
+        a.acc = (T*)p.acc;
+        a.comp = (T*)p.comp;
+        a.du = (T*)p.du;
+        a.fu_in = (const T*)p.fu_in;
+        a.fu_out = (T*)p.fu_out;
+        a.V = (T*)p.V;
+        a.fv = (T*)p.fv;
+        a.coef = (const T*)p.coef;
+        a.rk = (const T*)p.rk;
+        a.tinfo = p.tinfo;
+        a.bnd_x = p.bnd_x;
+        for (int q = 0; q < 3; ++q) a.wave.k[q] = p.wave_k[q];
+        a.wave.omega = std::sqrt(p.wave_k[0] * p.wave_k[0] + p.wave_k[1] * p.wave_k[1] + p.wave_k[2] * p.wave_k[2]);
+        a.wave.phi = p.wave_phi;
+        a.eslot = p.eslot;
+        a.ew = (const T*)p.ew;
+        a.echol = (const T*)p.echol;
+        a.partial = p.partial;
+        return a;
+    }
+    static size_t fm_grad_smem(int E) { return (padded_words(E) + 3 * plain_words(E)) * sizeof(T); }
+    static size_t fm_stage_smem(int E) {
+        size_t m3 = (size_t)P * P * P, EE = (size_t)E * E * E;
+        return (padded_words(E) + 2 * plain_words(E) + EE * m3) * sizeof(T);
+    }
+    cudaError_t fm_gradient(const BlockItem* items, int nitems, int E, int mode, const FmPtrs& p,
+                            cudaStream_t s) const override {
+        if constexpr (D != 3) return cudaErrorNotSupported;
+        else {
+            size_t smem = fm_grad_smem(E);
+            if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
+            fm_gradient_kernel<T, P><<<std::min(nitems, kMaxGrid), 256, smem, s>>>(
+                fm_args(items, nitems, E, mode, 0, p), tb_);
+            return cudaGetLastError();
+        }
+    }
+    cudaError_t fm_stage(const BlockItem* items, int nitems, int E, int mode, int truncate, const FmPtrs& p,
+                         cudaStream_t s) const override {
+        if constexpr (D != 3) return cudaErrorNotSupported;
+        else {
+            size_t smem = fm_stage_smem(E);
+            if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
+            fm_stage_kernel<T, P, COMP><<<std::min(nitems, kMaxGrid), 256, smem, s>>>(
+                fm_args(items, nitems, E, mode, truncate, p), tb_, ft_);
+            return cudaGetLastError();
+        }
+    }
+    cudaError_t fm_truncate(const BlockItem* items, int nitems, int E, const FmPtrs& p,
+                            cudaStream_t s) const override {
+        if constexpr (D != 3) return cudaErrorNotSupported;
+        else {
+            size_t smem = (plain_words(E) + (size_t)E * E * E * P * P * P) * sizeof(T);
+            if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
+            fm_truncate_kernel<T, P><<<std::min(nitems, kMaxGrid), 256, smem, s>>>(
+                fm_args(items, nitems, E, 0, 1, p), tb_, ft_);
+            return cudaGetLastError();
+        }
+    }
+    cudaError_t fm_energy(const BlockItem* items, int nitems, int E, const FmPtrs& p, cudaStream_t s) const override {
+        if constexpr (D != 3) return cudaErrorNotSupported;
+        else {
+            fm_energy_kernel<T, P><<<std::min(nitems, kMaxGrid), 256, 0, s>>>(fm_args(items, nitems, E, 5, 0, p),
+                                                                              tb_);
+            return cudaGetLastError();
+        }
     }
 
     cudaError_t maxabs(const BlockItem* items, int nitems, int E, const void* u, int var, double* part,

@@ -34,6 +34,11 @@ class Desc(ctypes.Structure):
         ("level", ctypes.POINTER(ctypes.c_int32)), ("corner", ctypes.POINTER(ctypes.c_int64)),
         ("coef", ctypes.POINTER(ctypes.c_double)), ("trunc_modes", ctypes.POINTER(ctypes.c_double)),
         ("trunc_duals", ctypes.POINTER(ctypes.c_double)),
+        ("metric", ctypes.c_int32), ("face_nb", ctypes.POINTER(ctypes.c_int32)),
+        ("face_code", ctypes.POINTER(ctypes.c_int32)), ("elem_slot", ctypes.POINTER(ctypes.c_int32)),
+        ("elem_w", ctypes.POINTER(ctypes.c_double)), ("elem_chol", ctypes.POINTER(ctypes.c_double)),
+        ("elem_ntab", ctypes.c_int32), ("wave_k", ctypes.c_double * 3), ("wave_phi", ctypes.c_double),
+        ("bnd_x", ctypes.POINTER(ctypes.c_double)),
     ]
 
 

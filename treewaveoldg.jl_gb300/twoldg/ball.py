@@ -1,0 +1,455 @@
+"""The seven-patch ball: a full-metric geometry with quarter-turn glue.
+
+SevenPatchBall (src/geometry.jl:270-553) maps a cube [-Lc, Lc]^3 (patch 1,
+n^3 roots) and six shells over its faces (patches 2-7, m roots along the
+radial dimension k and n along the others) onto the ball |x| <= R1. The
+shells' metric is neither diagonal nor separable, so the problem holds the
+gradient in Cartesian components, V = grad u, and the flux through a face
+normal to d is S[d] . V with the area vectors S[d] = sqrt(g) grad xi^d
+(src/evolution.jl:112-220). The outer sphere takes Dirichlet data: the plane
+wave u = sin(k . x - |k| t + phi) (src/sevenpatch.jl:9-59).
+
+The forest here is explicit: seven patches of root blocks, and for every
+block face its neighbour block, the neighbour's face and the orientation
+of the face plane across the glue, found by matching the physical
+positions of the face nodes on both sides (the glue's axis maps are quarter
+turns between shells; continuity of the physical coordinates across every
+glued face is what fixes them). Faces on the sphere are boundary faces.
+"""
+import math
+
+import numpy as np
+
+
+class Dual:
+    """Forward-mode dual numbers over numpy arrays: a value and its
+    derivatives with respect to the three logical coordinates."""
+
+    __array_priority__ = 1000
+
+    def __init__(self, v, d):
+        self.v = np.asarray(v, dtype=np.float64)
+        self.d = [np.asarray(x, dtype=np.float64) for x in d]
+
+    @staticmethod
+    def lift(x):
+        return x if isinstance(x, Dual) else Dual(x, [np.zeros_like(np.asarray(x, dtype=np.float64))] * 3)
+
+    def __add__(self, o):
+        o = Dual.lift(o)
+        return Dual(self.v + o.v, [a + b for a, b in zip(self.d, o.d)])
+
+    __radd__ = __add__
+
+    def __neg__(self):
+        return Dual(-self.v, [-a for a in self.d])
+
+    def __sub__(self, o):
+        return self + (-Dual.lift(o))
+
+    def __rsub__(self, o):
+        return Dual.lift(o) + (-self)
+
+    def __mul__(self, o):
+        o = Dual.lift(o)
+        return Dual(self.v * o.v, [a * o.v + self.v * b for a, b in zip(self.d, o.d)])
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, o):
+        o = Dual.lift(o)
+        return Dual(self.v / o.v, [(a * o.v - self.v * b) / (o.v * o.v) for a, b in zip(self.d, o.d)])
+
+    def __rtruediv__(self, o):
+        return Dual.lift(o) / self
+
+
+def dsqrt(x):
+    if not isinstance(x, Dual):
+        return np.sqrt(x)
+    s = np.sqrt(x.v)
+    return Dual(s, [a / (2 * s) for a in x.d])
+
+
+def dexp(x):
+    if not isinstance(x, Dual):
+        return np.exp(x)
+    e = np.exp(x.v)
+    return Dual(e, [a * e for a in x.d])
+
+
+# the shells' cube faces (k, s), in patch order 2-7 (src/geometry.jl:366)
+SHELLS = ((0, -1), (0, 1), (1, -1), (1, 1), (2, -1), (2, 1))
+
+
+class SevenPatchBall:
+    """The seven-patch ball map (src/geometry.jl:270-455), dimensions 0-based."""
+
+    def __init__(self, Lc, R1, roots, grading=0.0):
+        if not Lc > 0:
+            raise ValueError("the cube's half-width Lc must be positive, got %r" % (Lc,))
+        if not R1 > math.sqrt(3) * Lc:
+            raise ValueError("the outer radius R1 = %r must exceed sqrt(3) Lc = %r, so that the cube's corners "
+                             "lie inside the sphere and every shell maps one to one" % (R1, math.sqrt(3) * Lc))
+        if not all(r > 0 for r in roots):
+            raise ValueError("every patch of the ball needs a positive number of roots, got %r" % (roots,))
+        self.Lc, self.R1 = float(Lc), float(R1)
+        self.roots = tuple(int(r) for r in roots)
+        self.grading = float(grading)
+
+    def patch_roots(self, p):
+        n, m = self.roots
+        if p == 0:
+            return (n, n, n)
+        k, _ = SHELLS[p - 1]
+        return tuple(m if j == k else n for j in range(3))
+
+    def shell_fraction(self, eta):
+        a = self.grading
+        if a == 0:
+            return eta
+        return (dexp(a * eta) - 1) / (math.exp(a) - 1)
+
+    def position(self, xi, p):
+        """Physical position of logical xi (a 3-tuple of arrays or Duals) of patch p (0-based)."""
+        n, m = self.roots
+        Lc = self.Lc
+        if p == 0:
+            return tuple((2 * Lc / n) * xi[j] - Lc for j in range(3))
+        k, s = SHELLS[p - 1]
+        f = [s * Lc * (xi[j] * 0 + 1) if j == k else Lc * (2 * xi[j] / n - 1) for j in range(3)]
+        eta = xi[k] / m if s == 1 else 1 - xi[k] / m
+        rho = self.shell_fraction(eta)
+        norm = dsqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2])
+        return tuple((1 - rho) * f[j] + (rho * self.R1 / norm) * f[j] for j in range(3))
+
+    def frame(self, xi, p):
+        """sqrt(g) and the area vectors S[d][i] = sqrt(g) d xi^d / d x^i at logical xi
+        (src/geometry.jl:402-409), by forward-mode differentiation of the map."""
+        shape = np.shape(xi[0])
+        duals = [Dual(xi[j], [np.ones(shape) if q == j else np.zeros(shape) for q in range(3)]) for j in range(3)]
+        x = self.position(duals, p)
+        Jm = np.empty(shape + (3, 3))
+        for i in range(3):
+            xi_ = Dual.lift(x[i])
+            for j in range(3):
+                Jm[..., i, j] = np.broadcast_to(xi_.d[j], shape)
+        J = np.abs(np.linalg.det(Jm))
+        Ji = np.linalg.inv(Jm)               # Ji[d, i] = d xi^d / d x^i
+        S = J[..., None, None] * Ji          # S[..., d, i]
+        return J, S
+
+    def outer_radius(self):
+        return self.R1
+
+
+class BallForest:
+    """The forest of the ball: seven patches of root blocks (level 0) and
+    the explicit face table. Blocks are ordered patch by patch, and within a
+    patch by corner with the first dimension fastest."""
+
+    def __init__(self, geo, N):
+        self.geo = geo
+        self.D = 3
+        self.N = int(N)
+        self.blocks = []                    # (patch, corner)
+        for p in range(7):
+            r = geo.patch_roots(p)
+            for c2 in range(r[2]):
+                for c1 in range(r[1]):
+                    for c0 in range(r[0]):
+                        self.blocks.append((p, (c0, c1, c2)))
+        self.leaves = [(0, c) for _, c in self.blocks]   # level 0, for layout helpers
+        self.face_nb = None
+        self.face_code = None
+
+    def nleaves(self):
+        return len(self.blocks)
+
+    def spacing(self, key=None):
+        return 1.0 / self.N                 # every root block has logical extent 1
+
+    def minimum_spacing(self):
+        return 1.0 / self.N
+
+
+def face_plane_logical(corner, N, offs, f):
+    """Logical coordinates (3 arrays of N^2) of the face-node plane of face f of
+    a block at integer corner; tangential dims in increasing order, first fastest."""
+    P1 = len(offs)
+    n = np.arange(N)
+    x1d = (n // P1) * P1 + offs[n % P1]
+    d, side = f // 2, f % 2
+    tang = [k for k in range(3) if k != d]
+    a, b = np.meshgrid(x1d, x1d, indexing="xy")   # a varies fastest along columns
+    coords = [None] * 3
+    coords[tang[0]] = corner[tang[0]] + a.reshape(-1) / N
+    coords[tang[1]] = corner[tang[1]] + b.reshape(-1) / N
+    coords[d] = np.full(N * N, float(corner[d] + (1 if side else 0)))
+    return coords
+
+
+def orient(a, b, code, N):
+    """The neighbour's tangential indices of our face point (a, b): bit 0
+    swaps the two, bit 1 reverses the first, bit 2 the second."""
+    if code & 1:
+        a, b = b, a
+    if code & 2:
+        a = N - 1 - a
+    if code & 4:
+        b = N - 1 - b
+    return a, b
+
+
+def build_ball_faces(forest, offsets):
+    """The face table of a ball forest by matching face-node positions."""
+    geo, N = forest.geo, forest.N
+    nb = forest.nleaves()
+    face_nb = np.full(nb * 6, -1, dtype=np.int32)
+    face_code = np.zeros(nb * 6, dtype=np.int32)
+    index = {blk: i for i, blk in enumerate(forest.blocks)}
+    pos = {}
+    centre = {}
+    for bi, (p, c) in enumerate(forest.blocks):
+        for f in range(6):
+            x = geo.position(face_plane_logical(c, N, offsets, f), p)
+            X = np.stack([np.asarray(v) for v in x], axis=-1)
+            pos[(bi, f)] = X
+            centre[(bi, f)] = X.mean(axis=0)
+    # same-patch neighbours first
+    for bi, (p, c) in enumerate(forest.blocks):
+        r = geo.patch_roots(p)
+        for f in range(6):
+            d, side = f // 2, f % 2
+            cn = list(c)
+            cn[d] += 1 if side else -1
+            if 0 <= cn[d] < r[d]:
+                face_nb[bi * 6 + f] = index[(p, tuple(cn))]
+                face_code[bi * 6 + f] = (f ^ 1)
+    # glued faces: the unmatched faces whose face-node centres coincide
+    open_faces = [(bi, f) for bi in range(nb) for f in range(6) if face_nb[bi * 6 + f] < 0]
+    keys = {}
+    scale = geo.R1
+    for bf in open_faces:
+        key = tuple(np.round(centre[bf] / scale, 9))
+        keys.setdefault(key, []).append(bf)
+    nn = np.arange(N)
+    A, B = np.meshgrid(nn, nn, indexing="xy")
+    A, B = A.reshape(-1), B.reshape(-1)
+    for key, group in keys.items():
+        if len(group) == 1:
+            continue                       # an outer (sphere) face
+        if len(group) != 2:
+            raise ValueError("faces %r meet at one centre" % (group,))
+        (b1, f1), (b2, f2) = group
+        X1, X2 = pos[(b1, f1)], pos[(b2, f2)]
+        found = None
+        for code in range(8):
+            a2, bb2 = orient(A, B, code, N)
+            if np.allclose(X1, X2[a2 + N * bb2], atol=1e-10 * scale):
+                found = code
+                break
+        if found is None:
+            raise ValueError("glued faces (%d, %d) and (%d, %d) do not match" % (b1, f1, b2, f2))
+        face_nb[b1 * 6 + f1] = b2
+        face_code[b1 * 6 + f1] = f2 | (found << 4)
+        # the inverse orientation for the other side
+        inv = None
+        for code in range(8):
+            a1, bb1 = orient(A, B, code, N)
+            if np.allclose(X2, X1[a1 + N * bb1], atol=1e-10 * scale):
+                inv = code
+                break
+        face_nb[b2 * 6 + f2] = b1
+        face_code[b2 * 6 + f2] = f1 | (inv << 4)
+    forest.face_nb = face_nb
+    forest.face_code = face_code
+    return face_nb, face_code
+
+
+def sevenpatch_forest(T, P, E, roots=(2, 2), Lc=1.0, R1=3.0, grading=0.0):
+    """The ball forest and its map (src/geometry.jl:525-538)."""
+    from .element import Element
+    if E % 2:
+        raise ValueError("E = %d elements of order P = %d per block is odd, and E must be even" % (E, P))
+    geo = SevenPatchBall(Lc, R1, roots, grading)
+    forest = BallForest(geo, E * (P + 1))
+    build_ball_faces(forest, Element(np.float64, P).offsets.astype(np.float64))
+    return forest, geo
+
+
+def node_logical(forest, P, offsets):
+    """Logical coordinates (nblocks, 3, N^3) of every node, patch-local."""
+    N = forest.N
+    P1 = P + 1
+    n = np.arange(N)
+    x1d = (n // P1) * P1 + offsets[n % P1]
+    grids = np.indices([N] * 3).reshape(3, -1)[::-1]
+    out = np.empty((forest.nleaves(), 3, N ** 3))
+    for b, (p, c) in enumerate(forest.blocks):
+        for k in range(3):
+            out[b, k] = c[k] + x1d[grids[k]] / N
+    return out
+
+
+class PlaneWave:
+    """u = sin(k . x - |k| t + phi) (src/sevenpatch.jl:9-59)."""
+
+    def __init__(self, k, phi):
+        self.k = tuple(float(x) for x in k)
+        self.omega = math.sqrt(sum(x * x for x in self.k))
+        self.phi = float(phi)
+
+    def state(self, X, t, var):
+        th = sum(self.k[j] * X[j] for j in range(3)) - self.omega * t + self.phi
+        return np.sin(th) if var == 1 else -self.omega * np.cos(th)
+
+
+def legendre_at(P, x):
+    L = [np.ones_like(x), np.asarray(x, dtype=np.float64)]
+    for k in range(2, P + 1):
+        L.append(((2 * k - 1) * x * L[k - 1] - (k - 1) * L[k - 2]) / k)
+    return np.array(L[:P + 1])
+
+
+def ball_tables(forest, P, wave=None):
+    """The full metric's host tables for a ball forest, in float64
+    (src/evolution.jl:723-1018): coef (nblocks, 1 + 9, N^3) = sqrt(g) and
+    S[d][i] at 1 + 3d + i; the per-element truncation of the shells (elem_slot,
+    W_e = w_hat sqrt(g) and the upper Cholesky factor of G = Psi^T W Psi);
+    the boundary face nodes' positions per slot (3, N^2); and the time step's
+    spacing over speed."""
+    from .element import Element
+    geo, N = forest.geo, forest.N
+    el = Element(np.float64, P)
+    P1 = P + 1
+    E = N // P1
+    offs = el.offsets.astype(np.float64)
+    xl = node_logical(forest, P, offs)                 # (nb, 3, N^3)
+    nb = forest.nleaves()
+    NN = N ** 3
+    coef = np.empty((nb, 10, NN))
+    hspeed = math.inf
+    h = 1.0 / N
+    for b, (p, c) in enumerate(forest.blocks):
+        J, S = geo.frame(tuple(xl[b, k] for k in range(3)), p)
+        coef[b, 0] = J
+        for d in range(3):
+            for i in range(3):
+                coef[b, 1 + 3 * d + i] = S[:, d, i]
+        g = np.einsum("ndi,nei->nde", S, S) / (J ** 2)[:, None, None]
+        speed = np.sqrt(np.max(np.linalg.eigvalsh(g), axis=1)).max()
+        hspeed = min(hspeed, h / speed)
+    # per-element truncation tables for the shells (the cube is affine: slot 0)
+    L = legendre_at(P, el.nodes.astype(np.float64))   # (P+1 modes, P+1 nodes)
+    nodes = np.array([(n0, n1, n2) for n2 in range(P1) for n1 in range(P1) for n0 in range(P1)])
+    basis = np.array([(q0, q1, q2) for q2 in range(P) for q1 in range(P) for q0 in range(P)])
+    Psi = L[basis[:, 0]][:, nodes[:, 0]] * L[basis[:, 1]][:, nodes[:, 1]] * L[basis[:, 2]][:, nodes[:, 2]]
+    Psi = Psi.T                                        # (n3, m3)
+    what = el.weights[nodes[:, 0]] * el.weights[nodes[:, 1]] * el.weights[nodes[:, 2]]
+    slot = np.zeros(nb, dtype=np.int32)
+    ws, chols = [], []
+    for b, (p, c) in enumerate(forest.blocks):
+        if p == 0:
+            continue
+        slot[b] = len(ws) + 1
+        Wb = np.empty((E ** 3, P1 ** 3))
+        Cb = np.empty((E ** 3, P ** 3, P ** 3))
+        for e2 in range(E):
+            for e1 in range(E):
+                for e0 in range(E):
+                    e = e0 + E * (e1 + E * e2)
+                    idx = (e0 * P1 + nodes[:, 0]) + N * (e1 * P1 + nodes[:, 1]) + N * N * (e2 * P1 + nodes[:, 2])
+                    W = what * coef[b, 0, idx]
+                    G = Psi.T @ (W[:, None] * Psi)
+                    U = np.linalg.cholesky(G).T            # upper, G = U^T U
+                    Wb[e] = W
+                    Cb[e] = U
+        ws.append(Wb)
+        chols.append(Cb)
+    # (n3, E^3, ntab) column-major == (ntab, E^3, n3) row-major; U column-major per element
+    ew = np.ascontiguousarray(np.array(ws)).reshape(-1) if ws else np.zeros(1)
+    echol = np.ascontiguousarray(np.array(chols).transpose(0, 1, 3, 2)).reshape(-1) if chols else np.zeros(1)
+    # boundary face nodes' positions per slot, (3, N^2)
+    bnd = np.zeros((nb * 6, 3, N * N))
+    for b, (p, c) in enumerate(forest.blocks):
+        for f in range(6):
+            if forest.face_nb[b * 6 + f] < 0:
+                x = geo.position(face_plane_logical(c, N, offs, f), p)
+                bnd[b * 6 + f] = np.stack([np.asarray(v) for v in x])
+    return dict(coef=np.ascontiguousarray(coef.reshape(-1)), elem_slot=slot, elem_w=ew, elem_chol=echol,
+                ntab=len(ws), bnd_x=np.ascontiguousarray(bnd.reshape(-1)), hspeed=hspeed, xl=xl)
+
+
+def ball_desc(forest, P, truncate, precision, tables, wave):
+    """The twoldg_desc of a ball problem (an explicit face table and the full metric)."""
+    import ctypes
+    from . import _lib
+    nb = forest.nleaves()
+    d = _lib.Desc()
+    d.dim, d.order, d.elems = 3, P, forest.N // (P + 1)
+    d.precision = precision
+    d.truncate = 1 if truncate else 0
+    d.nblocks = nb
+    for k in range(3):
+        d.roots[k] = 1
+        d.periodic[k] = 0
+        d.reflecting[k] = 0
+        d.lo[k] = 0.0
+        d.hi[k] = 1.0
+    levels = np.zeros(nb, dtype=np.int32)
+    corners = np.zeros(nb * 3, dtype=np.int64)
+    ip, dp = ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)
+    d.level = levels.ctypes.data_as(ip)
+    d.corner = corners.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    d.metric = 2
+    d.coef = tables["coef"].ctypes.data_as(dp)
+    d.face_nb = forest.face_nb.ctypes.data_as(ip)
+    d.face_code = forest.face_code.ctypes.data_as(ip)
+    d.elem_slot = tables["elem_slot"].ctypes.data_as(ip)
+    d.elem_w = tables["elem_w"].ctypes.data_as(dp)
+    d.elem_chol = tables["elem_chol"].ctypes.data_as(dp)
+    d.elem_ntab = tables["ntab"]
+    for k in range(3):
+        d.wave_k[k] = wave.k[k]
+    d.wave_phi = wave.phi
+    d.bnd_x = tables["bnd_x"].ctypes.data_as(dp)
+    keep = (levels, corners, tables, forest.face_nb, forest.face_code)
+    return d, keep
+
+
+def sevenpatch_exact(geo, wave, t, forest=None):
+    """u and v = du/dt of the plane wave at time t (src/sevenpatch.jl:38-59), as a
+    callback f(x, var) of physical positions."""
+    def f(x, var):
+        return wave.state(x, t, var)
+    return f
+
+
+def sevenpatch_errors(T=np.float64, P=3, E=2, roots=(2, 2), Lc=1.0, R1=3.0, k=(1.1, -0.7, 0.5), phi=0.3, cfl=0.5,
+                      tend=1.0, truncate=True, precision=None):
+    """sevenpatch_errors (src/sevenpatch.jl:61-117): the plane wave on the ball
+    to tend with itself as the Dirichlet data on the sphere; sqrt(g)-weighted L2
+    errors of u and v together and apart, Linf, the cube's physical spacing,
+    the step count and the energies."""
+    from .element import Element
+    from .problem import WaveProblem, initial_state, oldg_timestep, quadrature_norm, wave_energy, wave_integrator
+    T = np.dtype(T)
+    forest, geo = sevenpatch_forest(T, P, E, roots=roots, Lc=Lc, R1=R1)
+    wave = PlaneWave(k, phi)
+    problem = WaveProblem(forest, Element(T, P), truncate=truncate, geometry=geo, boundary=wave,
+                          precision=precision)
+    t_end = float(T.type(tend))
+    u0 = initial_state(problem, sevenpatch_exact(geo, wave, 0.0))
+    nsteps = int(math.ceil(T.type(t_end) / oldg_timestep(problem, cfl)))
+    dt = float(T.type(T.type(t_end) / T.type(nsteps)))
+    integ = wave_integrator(problem, u0, 0.0, t_end, dt)
+    integ.nsteps = nsteps
+    integ.solve()
+    u = integ.u
+    ue = problem.to_device(problem.fill_at_nodes(sevenpatch_exact(geo, wave, t_end)))
+    h = forest.minimum_spacing() * 2 * geo.Lc / geo.roots[0]
+    return dict(l2=quadrature_norm(problem, u, 2, ref=ue), l2u=quadrature_norm(problem, u, 2, (1,), ref=ue),
+                l2v=quadrature_norm(problem, u, 2, (2,), ref=ue), linf=quadrature_norm(problem, u, math.inf, ref=ue),
+                h=h, he=(P + 1) * h, nsteps=nsteps, dt=dt, tend=t_end, nblocks=forest.nleaves(),
+                energy0=wave_energy(problem, u0, t=0.0), energy=wave_energy(problem, u, t=t_end))

@@ -81,7 +81,7 @@ class WaveProblem:
     RK4 accumulation). By default it follows the element's type.
     """
 
-    def __init__(self, forest, el, truncate=True, precision=None, device="cuda", geometry=None):
+    def __init__(self, forest, el, truncate=True, precision=None, device="cuda", geometry=None, boundary=None):
         check_layout(forest, el)
         if precision is None:
             precision = "f64" if el.T == np.float64 else "f32"
@@ -103,13 +103,29 @@ class WaveProblem:
         self.dtype = el.T
         self.device = device
         self.geometry = geometry
+        self.boundary = boundary
         self.metric = None
         self.hspeed = None
-        if geometry is not None:
-            from .geometry import metric_tables
-            self.metric = metric_tables(forest, Element(np.float64, el.P), geometry)
-            self.hspeed = self.metric[3]
-        self._desc, self._keep = make_desc(forest, el, truncate, _PREC[precision], self.metric)
+        self.full = False
+        from .ball import BallForest
+        if isinstance(forest, BallForest):
+            # a full-metric geometry with glue (the seven-patch ball): Dirichlet data required
+            from .ball import ball_desc, ball_tables
+            if boundary is None:
+                raise ValueError("the geometry has outer faces, and no data were given for them: pass "
+                                 "boundary = PlaneWave(k, phi), the Dirichlet data on the sphere")
+            self.full = True
+            self.metric = ball_tables(forest, el.P, boundary)
+            self.hspeed = self.metric["hspeed"]
+            self._desc, self._keep = ball_desc(forest, el.P, truncate, _PREC[precision], self.metric, boundary)
+        else:
+            if boundary is not None:
+                raise ValueError("Dirichlet data (boundary) are taken by a full geometry only")
+            if geometry is not None:
+                from .geometry import metric_tables
+                self.metric = metric_tables(forest, Element(np.float64, el.P), geometry)
+                self.hspeed = self.metric[3]
+            self._desc, self._keep = make_desc(forest, el, truncate, _PREC[precision], self.metric)
         h = ctypes.c_void_p()
         _lib.check(_lib.lib().twoldg_problem_create(ctypes.byref(self._desc), ctypes.byref(h)))
         self._h = h
@@ -146,8 +162,17 @@ class WaveProblem:
     def node_coordinates(self):
         """Positions of every owned node, shape (nblocks, D, N^D), in the
         element's type: lo + h (B N + q(P+1) + offsets[i]) per dimension
-        (src/layout.jl:59-76), with B the block's integer corner."""
+        (src/layout.jl:59-76), with B the block's integer corner; on the ball,
+        the physical positions of the patches' nodes."""
         T = self.dtype.type
+        if self.full:
+            xl = self.metric["xl"]
+            out = np.empty(xl.shape, dtype=self.dtype)
+            for b, (p, c) in enumerate(self.forest.blocks):
+                x = self.forest.geo.position(tuple(xl[b, k] for k in range(3)), p)
+                for k in range(3):
+                    out[b, k] = np.asarray(x[k])
+            return out
         P1 = self.P + 1
         n = np.arange(self.N)
         local = (n // P1) * P1  # element start, integer
