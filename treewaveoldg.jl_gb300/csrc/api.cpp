@@ -119,9 +119,18 @@ struct twoldg_runner {
     cudaGraphExec_t gexec = nullptr;
     void* graph_u = nullptr;
     void* comp_u = nullptr;
+    // Shape groups of a batch never exchange data, so each group's four
+    // stages are one independent branch of the step's graph: side[i] carries
+    // group i+1's branch, joined back to `stream` by join[i].
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> join;
+    cudaEvent_t fork = nullptr;
 
     ~twoldg_runner() {
         if (gexec) cudaGraphExecDestroy(gexec);
+        for (auto e : join) cudaEventDestroy(e);
+        for (auto st : side) cudaStreamDestroy(st);
+        if (fork) cudaEventDestroy(fork);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -225,6 +234,17 @@ struct twoldg_runner {
                                                std::to_string(g.D) + "D does not fit one CTA's shared memory");
         }
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        if (groups.size() > 1) {
+            CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+            for (size_t i = 1; i < groups.size(); ++i) {
+                cudaStream_t st;
+                cudaEvent_t ev;
+                CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+                side.push_back(st);
+                CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+                join.push_back(ev);
+            }
+        }
         for (auto& gp : groups) {
             Group& g = *gp;
             size_t fbytes = (size_t)g.nslots() * g.F * wsize;
@@ -387,27 +407,39 @@ struct twoldg_runner {
         return TWOLDG_OK;
     }
 
-    // One RK4 step, enqueued on `stream` (captured into the graph).
-    int enqueue_step(void* u) {
+    // One RK4 step of group g, its four stages enqueued on st.
+    int enqueue_group(Group& g, void* u, cudaStream_t st) {
         int in = 0;
         for (int s = 1; s <= 4; ++s) {
-            for (auto& gp : groups) {
-                Group& g = *gp;
-                if (g.full) {
-                    FmPtrs fp = fptrs(g, u, in);
-                    CK(g.ops->fm_gradient((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, fp, stream));
-                    CK(g.ops->fm_stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, fp,
-                                       stream));
-                    continue;
-                }
-                int r = cf_all(g, in);
-                if (r) return r;
+            if (g.full) {
+                FmPtrs fp = fptrs(g, u, in);
+                CK(g.ops->fm_gradient((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, fp, st));
+                CK(g.ops->fm_stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, fp, st));
+            } else {
+                if (!g.cf.empty())
+                    CK(g.ops->cf_ghosts((const CfFace*)g.d_cf.p, (int)g.cf.size(), g.E, g.fu[in].p, g.fog[in].p,
+                                        g.ugd.p, g.gfd.p, g.ggd.p, st));
                 StagePtrs p = ptrs(g, u, in);
-                CK(g.ops->stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, p, 0,
-                                stream));
+                CK(g.ops->stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, p, 0, st));
             }
             in = 1 - in;
         }
+        return TWOLDG_OK;
+    }
+
+    // One RK4 step, enqueued on `stream` (captured into the graph): group 0
+    // on `stream`, every other group on its side stream between a fork and
+    // a join, so that the graph runs the groups' chains side by side.
+    int enqueue_step(void* u) {
+        if (groups.size() > 1) CK(cudaEventRecord(fork, stream));
+        for (size_t i = 0; i < groups.size(); ++i) {
+            cudaStream_t st = i == 0 ? stream : side[i - 1];
+            if (i > 0) CK(cudaStreamWaitEvent(st, fork, 0));
+            int r = enqueue_group(*groups[i], u, st);
+            if (r) return r;
+            if (i > 0) CK(cudaEventRecord(join[i - 1], st));
+        }
+        for (size_t i = 1; i < groups.size(); ++i) CK(cudaStreamWaitEvent(stream, join[i - 1], 0));
         if (any_full()) {
             fm_advance_time(stream);
             CK(cudaGetLastError());
