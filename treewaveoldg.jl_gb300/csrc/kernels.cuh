@@ -155,6 +155,39 @@ __device__ __forceinline__ T ghost_coef(const Tab<T, P>& tb, int side) {
     return side == 0 ? tb.W[0][0] : tb.W[P][P + 2];
 }
 
+// Bulk prefetch of a contiguous range into L2 (cp.async.bulk.prefetch.L2,
+// sm_90 and later): one instruction per 64 KiB, no registers or shared memory
+// held, nothing to wait for. The instruction wants a 16-byte aligned start
+// and a multiple of 16 bytes; other ranges are left to the plain loads.
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    if ((a & 15) || (bytes & 15)) return;
+    for (size_t o = 0; o < bytes; o += 65536) {
+        const uint32_t n = (uint32_t)(bytes - o < 65536 ? bytes - o : 65536);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a + o), "r"(n) : "memory");
+    }
+}
+
+// The prefetches of one block's stage: its own RK operands (the stage input
+// y, u^n, the accumulator and the compensation, as far as the stage reads
+// them) and the next block this CTA takes, so that DRAM streams while the
+// CTA computes. One thread issues them.
+template <typename T>
+__device__ __forceinline__ void prefetch_stage(const StageArgs<T>& a, int item, int64_t words) {
+    const int mode = a.mode;
+    const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
+    const int64_t off = a.items[item].off;
+    const size_t b = (size_t)words * sizeof(T);
+    prefetch_l2(ysrc + off, b);
+    if (mode != MODE_RHS && mode != MODE_STAGE1) {
+        prefetch_l2(a.u + off, b);
+        prefetch_l2(a.acc + off, b);
+        if (mode == MODE_STAGE4 && a.comp) prefetch_l2(a.comp + off, b);
+    }
+    const int nxt = item + gridDim.x;
+    if (nxt < a.nitems) prefetch_l2(ysrc + a.items[nxt].off, b);
+}
+
 // Error-free sum (Knuth's TwoSum).
 template <typename T>
 __device__ __forceinline__ void two_sum(T a, T b, T& s, T& e) {
@@ -703,6 +736,7 @@ __device__ __forceinline__ void stage_block(const G& g, const StageArgs<T>& a, c
     const int mode = a.mode;
     const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
     const T inv_h = T(1) / T(it.h);
+    if (threadIdx.x == 0) prefetch_stage<T>(a, item, 2 * (int64_t)g.NN);
     load_u_with_ghosts<T, D, NT>(g, it, ysrc, a, su);
     __syncthreads();
     for (int d = 0; d < D; ++d) {

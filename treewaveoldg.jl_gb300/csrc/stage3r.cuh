@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP>::NT, Stage3R<T, P, E, C
         for (int f = 0; f < 6; ++f) nb[f] = it.nb[f];
         const T inv_h = T(1) / T(it.h);
         const T* yu = ysrc + it.off;
+        if (tid == 0) prefetch_stage<T>(a, item, 2 * (int64_t)NN);
         // every global load of the block's prologue at once: the column, the u
         // ghosts and the neighbours' gradient parts at this face point
         T line[N + 2];
