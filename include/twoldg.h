@@ -18,6 +18,7 @@
 #ifndef TWOLDG_H
 #define TWOLDG_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -171,6 +172,20 @@ int twoldg_mode_amplitude(twoldg_problem* p, const void* u, int32_t var, int32_t
  * without the graph, with CUDA events between the four stages, and returns
  * each stage's duration in milliseconds (stage_ms[4]). Synchronous. */
 int twoldg_profile_step(twoldg_problem* p, void* u, double dt, float* stage_ms);
+/* The autotuner (no reference counterpart: the reference launches its
+ * kernels with a fixed workgroup size). For every (dim, P, E) group of the
+ * problem it times the stage kernel's launch layouts -- which kernel (the
+ * register-line 3D kernel, the fixed-shape or the run-time-shape kernel),
+ * threads per CTA, and one CTA per block or a persistent grid of 1 or 2
+ * waves of resident CTAs -- on stages 1 to 3 of a step of size dt from u
+ * (u itself is not changed), and keeps the fastest for the problem's later
+ * steps. cache: NULL, or the path of a JSON file of earlier choices keyed by
+ * precision, dim, P, E, metric and the block count's bit length; choices
+ * found there are taken without timing and new ones are written back.
+ * report (may be NULL) receives one line per group with the choice and its
+ * time per stage launch in microseconds. Synchronous. */
+int twoldg_autotune(twoldg_problem* p, void* u, double dt, const char* cache, char* report, size_t report_len);
+
 /* The problem's CUDA stream (a cudaStream_t), for callers that order their
  * own work or events against the library's. */
 void* twoldg_stream(twoldg_problem* p);
@@ -202,6 +217,9 @@ int twoldg_batch_create(int32_t n, const twoldg_desc* descs, twoldg_batch** out)
 int twoldg_batch_destroy(twoldg_batch* b);
 int twoldg_batch_offsets(const twoldg_batch* b, int64_t* offsets, int64_t* total_words);
 int twoldg_batch_rk4_step(twoldg_batch* b, void* u, const double* dt, int32_t nsteps);
+/* twoldg_autotune for a batch: dt[n] per problem, one choice per shape group. */
+int twoldg_batch_autotune(twoldg_batch* b, void* u, const double* dt, const char* cache, char* report,
+                          size_t report_len);
 int twoldg_batch_synchronize(twoldg_batch* b);
 
 #ifdef __cplusplus

@@ -9,9 +9,12 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <map>
 #include <memory>
+#include <sstream>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -449,6 +452,117 @@ struct twoldg_runner {
 
     void fm_advance_time(cudaStream_t s);
 
+    // The autotuner: for every shape group, time each launch layout the
+    // group's kernels offer on stages 1 to 3 of a step from u (which they do
+    // not change: they write only the stage scratch and the face planes) and
+    // keep the fastest. Layouts found in the cache file (a JSON object, one
+    // entry per line, as this function writes it) are taken without timing;
+    // new ones are added to it. report receives the chosen layouts in the
+    // same form.
+    int autotune(void* u, const double* dts, const char* cache, std::string& report) {
+        int r = rk4(u, dts, 0);
+        if (r) return r;
+        r = export_all(u);
+        if (r) return r;
+        std::map<std::string, std::string> lines;  // key -> the entry's text
+        std::map<std::string, Launch> known;
+        if (cache) {
+            std::ifstream in(cache);
+            std::string line;
+            while (std::getline(in, line)) {
+                const size_t q0 = line.find('"'), q1 = line.find('"', q0 + 1);
+                if (q0 == std::string::npos || q1 == std::string::npos) continue;
+                Launch l{};
+                if (std::sscanf(line.c_str() + q1 + 1, ": {\"kernel\": %d, \"threads\": %d, \"waves\": %d", &l.kernel,
+                                &l.threads, &l.waves) != 3)
+                    continue;
+                const std::string key = line.substr(q0 + 1, q1 - q0 - 1);
+                known[key] = l;
+                std::string body = line.substr(q0);
+                while (!body.empty() && (body.back() == ',' || body.back() == ' ' || body.back() == '\r')) body.pop_back();
+                lines[key] = body;
+            }
+        }
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        const char* pname = prec == TWOLDG_F64 ? "f64" : prec == TWOLDG_F32 ? "f32" : "f32c";
+        std::ostringstream rep;
+        int rc = TWOLDG_OK;
+        for (auto& gp : groups) {
+            Group& g = *gp;
+            if (g.full) continue;
+            const int nit = (int)g.items.size();
+            int size_class = 0;
+            while ((1 << size_class) <= nit) ++size_class;
+            char keyb[128];
+            std::snprintf(keyb, sizeof keyb, "%s d%d p%d e%d %s n%d", pname, g.D, g.P, g.E,
+                          g.metric ? "diag" : "flat", size_class);
+            const std::string key = keyb;
+            auto kn = known.find(key);
+            if (kn != known.end()) {
+                g.ops->set_launch(kn->second, g.E, !g.metric);
+                rep << lines[key] << "\n";
+                continue;
+            }
+            Launch cand[32];
+            const int nc = g.ops->launch_candidates(g.E, !g.metric, cand, 32);
+            float best = INFINITY;
+            Launch bl{0, 0, 0};
+            auto run3 = [&]() -> cudaError_t {
+                int in = 0;
+                for (int s = 1; s <= 3; ++s) {
+                    StagePtrs sp = ptrs(g, u, in);
+                    cudaError_t e = g.ops->stage((const BlockItem*)g.d_items.p, nit, g.E, s, g.truncate, sp, 0, stream);
+                    if (e != cudaSuccess) return e;
+                    in = 1 - in;
+                }
+                return cudaSuccess;
+            };
+            for (int c = 0; c < nc; ++c) {
+                g.ops->set_launch(cand[c], g.E, !g.metric);
+                if (run3() != cudaSuccess || run3() != cudaSuccess) { cudaGetLastError(); continue; }
+                const int reps = 5;
+                cudaEventRecord(e0, stream);
+                bool ok = true;
+                for (int q = 0; q < reps && ok; ++q) ok = run3() == cudaSuccess;
+                cudaEventRecord(e1, stream);
+                cudaError_t e = cudaEventSynchronize(e1);
+                if (e != cudaSuccess) { rc = cuda_fail(e, "autotune"); break; }
+                if (!ok) { cudaGetLastError(); continue; }
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                ms /= reps * 3;
+                if (ms < best) { best = ms; bl = cand[c]; }
+            }
+            if (rc) break;
+            g.ops->set_launch(bl, g.E, !g.metric);
+            char body[256];
+            std::snprintf(body, sizeof body, "\"%s\": {\"kernel\": %d, \"threads\": %d, \"waves\": %d, \"us\": %.2f}",
+                          key.c_str(), bl.kernel, bl.threads, bl.waves, (double)best * 1e3);
+            lines[key] = body;
+            rep << body << "\n";
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (rc) return rc;
+        if (gexec) {
+            cudaGraphExecDestroy(gexec);
+            gexec = nullptr;
+        }
+        graph_u = nullptr;
+        if (cache) {
+            std::ofstream out(cache, std::ios::trunc);
+            if (!out) return fail(TWOLDG_EINVAL, std::string("cannot write the autotuner cache ") + cache);
+            out << "{\n";
+            size_t i = 0;
+            for (auto& kv : lines) out << "  " << kv.second << (++i < lines.size() ? ",\n" : "\n");
+            out << "}\n";
+        }
+        report = rep.str();
+        return TWOLDG_OK;
+    }
+
     int rk4(void* u, const double* dts, int nsteps, double t0 = 0.0) {
         if (!u) return fail(TWOLDG_EINVAL, "u is NULL");
         if (nsteps < 0) return fail(TWOLDG_EINVAL, "nsteps is negative");
@@ -794,6 +908,32 @@ int twoldg_batch_offsets(const twoldg_batch* b, int64_t* offsets, int64_t* total
 int twoldg_batch_rk4_step(twoldg_batch* b, void* u, const double* dt, int32_t nsteps) {
     if (!b || !dt) return fail(TWOLDG_EINVAL, "NULL argument");
     return b->rk4(u, dt, nsteps);
+}
+
+static int tune_report(const std::string& rep, char* report, size_t report_len) {
+    if (report && report_len) {
+        const size_t n = std::min(rep.size(), report_len - 1);
+        std::memcpy(report, rep.data(), n);
+        report[n] = 0;
+    }
+    return TWOLDG_OK;
+}
+
+int twoldg_autotune(twoldg_problem* p, void* u, double dt, const char* cache, char* report, size_t report_len) {
+    if (!p || !u) return fail(TWOLDG_EINVAL, "NULL argument");
+    std::string rep;
+    int r = p->autotune(u, &dt, cache, rep);
+    if (r) return r;
+    return tune_report(rep, report, report_len);
+}
+
+int twoldg_batch_autotune(twoldg_batch* b, void* u, const double* dt, const char* cache, char* report,
+                          size_t report_len) {
+    if (!b || !u || !dt) return fail(TWOLDG_EINVAL, "NULL argument");
+    std::string rep;
+    int r = b->autotune(u, dt, cache, rep);
+    if (r) return r;
+    return tune_report(rep, report, report_len);
 }
 
 int twoldg_batch_synchronize(twoldg_batch* b) {

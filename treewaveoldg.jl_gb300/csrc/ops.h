@@ -54,14 +54,28 @@ struct FmPtrs {
     double* partial;
 };
 
+// A launch layout of the stage kernel. kernel: 0 the shape's default, 1 the
+// register-line 3D kernel, 2 the fixed-shape kernel, 3 the run-time-shape
+// kernel; threads: threads per CTA of kernel 3 (0: by block size); waves: 0
+// one CTA per block, k > 0 at most k times the CTAs the device holds at once,
+// each CTA looping over blocks (so that its prefetch of the next block pays).
+struct Launch {
+    int kernel;
+    int threads;
+    int waves;
+};
+
 class Ops {
 public:
     virtual ~Ops() {}
     // bytes of dynamic shared memory the stage kernel needs for E elements per dim
     virtual size_t stage_smem(int E) const = 0;
-    virtual int stage_threads() const = 0;
-    // threads per CTA of the stage kernel (0 = the shape's default); the autotuner sets it
-    virtual void set_threads(int t) = 0;
+    // the stage kernel's launch layout (the autotuner sets it, before a graph is captured)
+    virtual void set_launch(const Launch& l, int E, bool flat) = 0;
+    virtual Launch launch() const = 0;
+    // the layouts worth timing for blocks of E elements per dimension; flat:
+    // no metric coefficients. Returns how many were written (at most max).
+    virtual int launch_candidates(int E, bool flat, Launch* out, int max) const = 0;
     virtual cudaError_t export_faces(const BlockItem* items, int nitems, int E, const void* u, void* fu,
                                      void* fog, cudaStream_t s) const = 0;
     virtual cudaError_t cf_ghosts(const CfFace* cf, int ncf, int E, const void* fu, const void* fog, void* ugd,

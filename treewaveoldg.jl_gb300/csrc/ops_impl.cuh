@@ -11,7 +11,6 @@
 
 namespace twoldg {
 
-constexpr int kStageThreads = 256;
 constexpr int kMaxGrid = 152 * 64;
 
 template <typename T>
@@ -43,6 +42,7 @@ public:
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&max_smem_, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev);
         cudaFuncSetAttribute(stage_kernel<T, D, P, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         cudaFuncSetAttribute(stage_kernel_c<T, D, P, 2, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         cudaFuncSetAttribute(stage_kernel_c<T, D, P, 4, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
@@ -104,8 +104,9 @@ public:
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     }
-    int threads_ = 0;  // 0: the default for the shape
-    void set_threads(int t) override { threads_ = t; }
+    Launch launch_{0, 0, 0};
+    int grid_cap_ = 0;  // 0: one CTA per block (at most kMaxGrid)
+    int nsm_ = 0;
     int default_threads(int E) const {
         size_t N = (size_t)E * (P + 1), NN = 1;
         for (int k = 0; k < D; ++k) NN *= N;
@@ -114,7 +115,81 @@ public:
         return 64;
     }
     size_t stage_smem(int E) const override { return smem_words(E) * sizeof(T); }
-    int stage_threads() const override { return threads_ ? threads_ : kStageThreads; }
+
+    // the kernel that runs for a requested one: the register-line kernel for
+    // flat 3D blocks of E = 2 or 4 whose cross-section fits a CTA, the
+    // fixed-shape kernel for E = 2 or 4, the run-time-shape kernel always;
+    // 0 or a kernel the shape cannot take means the first that it can
+    int resolve(int kernel, int E, bool flat, bool aligned) const {
+        bool line = false;
+        if constexpr (D == 3) {
+            line = flat && aligned && ((E == 2 && Stage3R<T, P, 2, COMP>::usable) ||
+                                       (E == 4 && Stage3R<T, P, 4, COMP>::usable));
+        }
+        const bool fixed = aligned && (E == 2 || E == 4);
+        if (kernel == 1 && line) return 1;
+        if (kernel == 2 && fixed) return 2;
+        if (kernel == 3) return 3;
+        return line ? 1 : fixed ? 2 : 3;
+    }
+    int run_threads(int kernel, int E) const {
+        if (kernel == 1) return E * (P + 1) * E * (P + 1);
+        if (kernel == 2) return E == 2 ? StageLaunch<T, D, P, 2>::NT : StageLaunch<T, D, P, 4>::NT;
+        return std::min(launch_.threads ? launch_.threads : default_threads(E), 256);
+    }
+    // CTAs of the resolved kernel one SM holds at once
+    int resident(int kernel, int threads, int E) const {
+        int n = 0;
+        if constexpr (D == 3) {
+            if (kernel == 1) {
+                if (E == 2)
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage3r_kernel<T, P, 2, COMP>, threads,
+                                                                  Stage3R<T, P, 2, COMP>::words * sizeof(T));
+                else
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage3r_kernel<T, P, 4, COMP>, threads,
+                                                                  Stage3R<T, P, 4, COMP>::words * sizeof(T));
+                return n;
+            }
+        }
+        if (kernel == 2) {
+            if (E == 2)
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage_kernel_c<T, D, P, 2, COMP>, threads,
+                                                              stage_smem(E));
+            else
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage_kernel_c<T, D, P, 4, COMP>, threads,
+                                                              stage_smem(E));
+            return n;
+        }
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage_kernel<T, D, P, COMP>, threads, stage_smem(E));
+        return n;
+    }
+    void set_launch(const Launch& l, int E, bool flat) override {
+        launch_ = l;
+        grid_cap_ = 0;
+        if (l.waves > 0) {
+            const int k = resolve(l.kernel, E, flat, true);
+            const int r = resident(k, run_threads(k, E), E);
+            cudaGetLastError();
+            grid_cap_ = std::max(1, l.waves * std::max(r, 1) * std::max(nsm_, 1));
+        }
+    }
+    Launch launch() const override { return launch_; }
+    int launch_candidates(int E, bool flat, Launch* out, int max) const override {
+        int n = 0;
+        auto add = [&](int k, int t, int w) {
+            if (n < max) out[n++] = Launch{k, t, w};
+        };
+        for (int k = 1; k <= 3; ++k) {
+            if (resolve(k, E, flat, true) != k) continue;
+            if (k < 3) {
+                for (int w = 0; w <= 2; ++w) add(k, 0, w);
+            } else {
+                for (int t : {64, 128, 256})
+                    for (int w = 0; w <= 1; ++w) add(k, t, w);
+            }
+        }
+        return n;
+    }
 
     cudaError_t export_faces(const BlockItem* items, int nitems, int E, const void* u, void* fu, void* fog,
                              cudaStream_t s) const override {
@@ -164,30 +239,29 @@ public:
         a.trd = (const T*)p.trd;
         size_t smem = stage_smem(E);
         if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
-        if (grid <= 0) grid = std::min(nitems, kMaxGrid);
-        // the vector path needs 16-byte aligned state pointers
+        if (grid <= 0) grid = std::min(nitems, grid_cap_ > 0 ? grid_cap_ : kMaxGrid);
+        // the fixed-shape kernels need 16-byte aligned state pointers
         uintptr_t al = (uintptr_t)p.u | (uintptr_t)p.y | (uintptr_t)p.acc | (uintptr_t)p.comp | (uintptr_t)p.du;
         const bool aligned = (al & 15) == 0;
-        int nt = threads_ ? threads_ : default_threads(E);
-        // the whole-lines-in-registers 3D kernel serves flat problems
+        const int k = resolve(launch_.kernel, E, !p.coef, aligned);
         if constexpr (D == 3) {
-            if (!p.coef && aligned && E == 2 && Stage3R<T, P, 2, COMP>::usable) {
+            if (k == 1 && E == 2) {
                 using S = Stage3R<T, P, 2, COMP>;
                 stage3r_kernel<T, P, 2, COMP><<<grid, S::NT, S::words * sizeof(T), s>>>(a, tb_);
                 return cudaGetLastError();
             }
-            if (!p.coef && aligned && E == 4 && Stage3R<T, P, 4, COMP>::usable) {
+            if (k == 1 && E == 4) {
                 using S = Stage3R<T, P, 4, COMP>;
                 stage3r_kernel<T, P, 4, COMP><<<grid, S::NT, S::words * sizeof(T), s>>>(a, tb_);
                 return cudaGetLastError();
             }
         }
-        if (aligned && E == 2) {
+        if (k == 2 && E == 2) {
             stage_kernel_c<T, D, P, 2, COMP><<<grid, StageLaunch<T, D, P, 2>::NT, smem, s>>>(a, tb_);
-        } else if (aligned && E == 4) {
+        } else if (k == 2 && E == 4) {
             stage_kernel_c<T, D, P, 4, COMP><<<grid, StageLaunch<T, D, P, 4>::NT, smem, s>>>(a, tb_);
         } else {
-            stage_kernel<T, D, P, COMP><<<grid, std::min(nt, 256), smem, s>>>(a, tb_);
+            stage_kernel<T, D, P, COMP><<<grid, run_threads(3, E), smem, s>>>(a, tb_);
         }
         return cudaGetLastError();
     }

@@ -20,7 +20,7 @@ EXPORTS = [
     "twoldg_energy", "twoldg_norm", "twoldg_modal_indicator", "twoldg_mode_amplitude",
     "twoldg_synchronize", "twoldg_batch_create", "twoldg_batch_destroy", "twoldg_batch_offsets",
     "twoldg_batch_rk4_step", "twoldg_batch_synchronize", "twoldg_profile_step", "twoldg_stream",
-    "twoldg_rhs_static",
+    "twoldg_rhs_static", "twoldg_autotune", "twoldg_batch_autotune",
 ]
 
 
@@ -83,6 +83,9 @@ def lib():
             "twoldg_profile_step": (ctypes.c_int, [vp, vp, d, ctypes.POINTER(ctypes.c_float)]),
             "twoldg_stream": (vp, [vp]),
             "twoldg_rhs_static": (ctypes.c_int, [ctypes.POINTER(Desc), vp, vp, d, vp]),
+            "twoldg_autotune": (ctypes.c_int, [vp, vp, d, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]),
+            "twoldg_batch_autotune": (ctypes.c_int, [vp, vp, ctypes.POINTER(d), ctypes.c_char_p, ctypes.c_char_p,
+                                                     ctypes.c_size_t]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -90,6 +93,13 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def tune_report(text):
+    """The autotuner's report lines ('"key": {"kernel": k, ...}') as a dict."""
+    import json
+    body = ",".join(line for line in text.splitlines() if line.strip())
+    return json.loads("{" + body + "}") if body else {}
 
 
 def check(rc):

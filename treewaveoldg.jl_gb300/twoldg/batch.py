@@ -60,6 +60,19 @@ class Batch:
     def synchronize(self):
         _lib.check(_lib.lib().twoldg_batch_synchronize(self._h))
 
+    def autotune(self, u, dts, cache=None):
+        """Time the stage kernel's launch layouts of every shape group on u
+        (unchanged) with steps dts and keep the fastest; cache: a JSON file of
+        earlier choices, read and extended. Returns {group key: choice}."""
+        import torch
+        torch.cuda.synchronize()
+        arr = (ctypes.c_double * len(dts))(*[float(x) for x in dts])
+        buf = ctypes.create_string_buffer(1 << 16)
+        _lib.check(_lib.lib().twoldg_batch_autotune(self._h, ctypes.c_void_p(u.data_ptr()), arr,
+                                                    None if cache is None else str(cache).encode(), buf,
+                                                    len(buf)))
+        return _lib.tune_report(buf.value.decode())
+
 
 def sine_ensemble(n, seed=0, dtype=np.float64, P_range=(2, 5), E_choices=(2, 4), roots_range=(4, 16)):
     """n 2D periodic problems: P uniform in P_range, E in E_choices, roots

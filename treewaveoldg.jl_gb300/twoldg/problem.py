@@ -204,6 +204,18 @@ class WaveProblem:
     def synchronize(self):
         _lib.check(_lib.lib().twoldg_synchronize(self._h))
 
+    def autotune(self, u, dt, cache=None):
+        """Time the stage kernel's launch layouts (kernel, threads per CTA,
+        grid) of every (dim, P, E) group on u, which is not changed, with step
+        dt, and keep the fastest for later steps; cache: a JSON file of
+        earlier choices, read and extended. Returns {group key: choice}."""
+        _check_state(self, u)
+        _torch().cuda.synchronize()
+        buf = ctypes.create_string_buffer(1 << 16)
+        _lib.check(_lib.lib().twoldg_autotune(self._h, ctypes.c_void_p(u.data_ptr()), float(dt),
+                                              None if cache is None else str(cache).encode(), buf, len(buf)))
+        return _lib.tune_report(buf.value.decode())
+
 
 def _check_state(p, u):
     torch = _torch()
