@@ -53,9 +53,11 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner (untimed, before the warm-up) and run the default launch layouts")
-    ap.add_argument("--workload", default="box256", choices=["box256", "nested"],
+    ap.add_argument("--workload", default="box256", choices=["box256", "nested", "c1", "ball"],
                     help="box256: the 256^3 periodic box (the headline); nested: the 3D reflecting box with "
-                         "three nested refinement levels (P=3, E=2, roots=8) and a Gaussian pulse")
+                         "three nested refinement levels (P=3, E=2, roots=8) and a Gaussian pulse; c1: the 2D "
+                         "periodic P=4, E=2, roots=8 box to a quarter period at CFL 0.25; ball: the seven-patch "
+                         "ball, P=3, E=2, roots=(4,4), plane wave with Dirichlet sphere, to t=6")
     return ap.parse_args()
 
 
@@ -264,6 +266,86 @@ def batched(twoldg, torch, steps, warmup, accuracy_steps, n=512):
     return out
 
 
+# --- the small configurations: whole runs to t_end, FP64 against FP32 + compensated ---------
+def small_problem(twoldg, prec):
+    """(problem, u0, dt, nsteps, t_end, exact(t) -> device state) of the c1 or ball workload."""
+    T = np.float64 if prec == "f64" else np.float32
+    if WORKLOAD == "c1":
+        forest = twoldg.wave_forest(T, 2, 4, 2, roots=8)
+        p = twoldg.WaveProblem(forest, twoldg.Element(T, 4), precision=prec)
+        u0 = twoldg.initial_state(p, twoldg.wave_exact(2, 1.0, 1, 0.0, T))
+        t_end, cfl = 0.25 * 2 * math.pi / twoldg.wave_omega(2, 1.0, 1), 0.25
+
+        def exact(t):
+            return p.to_device(p.fill_at_nodes(twoldg.wave_exact(2, 1.0, 1, t, T)))
+    else:
+        forest, geo = twoldg.sevenpatch_forest(T, 3, 2, roots=(4, 4), Lc=1.0, R1=3.0)
+        k = np.array([1.1, -0.7, 0.5])
+        wave = twoldg.PlaneWave(2 * math.pi * k / np.linalg.norm(k), 0.3)
+        p = twoldg.WaveProblem(forest, twoldg.Element(T, 3), geometry=geo, boundary=wave, precision=prec)
+        u0 = twoldg.initial_state(p, twoldg.sevenpatch_exact(geo, wave, 0.0))
+        t_end, cfl = 6.0, 0.5
+
+        def exact(t):
+            return p.to_device(p.fill_at_nodes(twoldg.sevenpatch_exact(geo, wave, t)))
+    nsteps = int(math.ceil(T(t_end) / twoldg.oldg_timestep(p, cfl)))
+    dt = float(T(T(t_end) / T(nsteps)))
+    return p, u0, dt, nsteps, float(T(t_end)), exact
+
+
+def small_config(args, twoldg, torch):
+    """Both arms of a small configuration: node-steps/s of the whole run to
+    t_end (CUDA events on the library's stream, after a warm-up run), the L2
+    and Linf errors against the exact solution and against the FP64 run, and
+    the energy drift."""
+    lib = twoldg._lib.lib()
+    arms, final = {}, {}
+    for prec in ("f64", "f32c"):
+        p, u0, dt, nsteps, t_end, exact = small_problem(twoldg, prec)
+        u = u0.clone()
+        layout = p.autotune(u, dt) if TUNE else {}
+        stream = torch.cuda.ExternalStream(lib.twoldg_stream(p.handle))
+        best = math.inf
+        for rep in range(1 + max(1, args.steps // 50)):
+            u = u0.clone()
+            if prec == "f32c":
+                twoldg._lib.check(lib.twoldg_reset_compensation(p.handle))
+            torch.cuda.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ctypes.c_void_p(u.data_ptr()), 0.0, dt, nsteps))
+            ev1.record(stream)
+            ev1.synchronize()
+            if rep > 0:
+                best = min(best, ev0.elapsed_time(ev1))
+        nodes = p.state_words // 2
+        ue = exact(t_end)
+        e0, e1 = twoldg.wave_energy(p, u0, t=0.0), twoldg.wave_energy(p, u, t=t_end)
+        arms[prec] = {"value": nodes * nsteps / (best / 1e3), "ms_per_step": best / nsteps, "nsteps": nsteps,
+                      "nodes": nodes, "layout": layout,
+                      "l2": twoldg.quadrature_norm(p, u, 2, ref=ue),
+                      "linf": twoldg.quadrature_norm(p, u, math.inf, ref=ue),
+                      "energy_drift": abs(e1 - e0) / abs(e0)}
+        final[prec] = (p, u)
+    p32, u32 = final["f32c"]
+    r = final["f64"][1].to(u32.dtype)
+    arms["f32c"]["l2_vs_fp64"] = twoldg.quadrature_norm(p32, u32, 2, ref=r)
+    arms["f32c"]["linf_vs_fp64"] = twoldg.quadrature_norm(p32, u32, math.inf, ref=r)
+    head = arms["f32c"]
+    name = ("2D periodic box, P=4, E=2, roots=8 (6400 nodes), sin(2 pi x) sin(2 pi y) to a quarter period at "
+            "CFL 0.25" if WORKLOAD == "c1" else
+            "seven-patch ball, P=3, E=2, roots=(4,4), Lc=1, R1=3 (%d nodes), plane wave |k|=2 pi, phi=0.3, "
+            "Dirichlet sphere, to t=6 at CFL 0.5" % head["nodes"])
+    line = {"metric": METRIC, "value": head["value"], "unit": "node-steps/s", "n_gpus": 1,
+            "steps": head["nsteps"], "warmup": 1, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": name, "precision": "f32c",
+                       "l2_flush": "none: the state fits in L2 (a whole run to t_end is timed)"},
+            "fp64": arms["f64"], "f32c": arms["f32c"], "speedup_vs_fp64": head["value"] / arms["f64"]["value"],
+            "roofline": None, "gpu_launches": None}
+    print(json.dumps(line))
+
+
 # --- multi-rank plumbing (replicas) -------------------------------------------
 _dist = None
 
@@ -371,6 +453,9 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     twoldg.build()
+    if WORKLOAD in ("c1", "ball"):
+        small_config(args, twoldg, torch)
+        return
     arms = {}
     wanted = args.arms.split(",")
     for prec in ("f64", "f32c"):

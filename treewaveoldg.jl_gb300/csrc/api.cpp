@@ -90,6 +90,13 @@ struct Group {
     std::vector<double> bndx, ew, echol;
     std::vector<int> eslot;
     double wave_k[3] = {0, 0, 0}, wave_phi = 0;
+    int boundary = 0;
+    double kappa = 0, inv_r = 0;
+    // the factored truncation: per block slot, per factored block its radial
+    // dimension, pair and angular table index, the angular tables
+    DevBuf d_fslot, d_fradial, d_frm, d_frd, d_faslot, d_faw, d_fachol;
+    std::vector<int> fslot, fradial, faslot;
+    std::vector<double> frm, frd, faw, fachol;
     int nslots() const { return (int)items.size() * 2 * D; }
 };
 
@@ -160,6 +167,14 @@ struct twoldg_runner {
                 if (!d.coef || !d.elem_slot || !d.bnd_x)
                     return fail(TWOLDG_EINVAL, "a full metric needs coef, elem_slot and bnd_x");
                 if (n != 1) return fail(TWOLDG_EUNSUP, "a full-metric problem is stepped alone, not in a batch");
+                if (d.boundary != 0 && d.boundary != 1)
+                    return fail(TWOLDG_EINVAL, "boundary must be 0 (Dirichlet plane wave) or 1 (radiative)");
+                if (d.boundary == 1 && !(d.kappa >= 0))
+                    return fail(TWOLDG_EINVAL, "kappa = " + std::to_string(d.kappa) +
+                                                   " is negative, and a radiative boundary with kappa < 0 feeds "
+                                                   "energy in: take kappa >= 0, 1 for Sommerfeld's condition");
+                if (d.boundary == 1 && !(d.inv_r >= 0))
+                    return fail(TWOLDG_EINVAL, "inv_r must be 1/R >= 0, or 0 without the u/R term");
             }
             if (metric && !full && (!d.trunc_modes || !d.trunc_duals))
                 return fail(TWOLDG_EINVAL, "a metric (coef) needs its truncation pairs (trunc_modes, trunc_duals)");
@@ -218,6 +233,40 @@ struct twoldg_runner {
                 }
                 for (int q = 0; q < 3; ++q) g->wave_k[q] = d.wave_k[q];
                 g->wave_phi = d.wave_phi;
+                g->boundary = d.boundary;
+                g->kappa = d.kappa;
+                g->inv_r = d.inv_r;
+                g->fslot.assign(m.nblocks, 0);
+                if (d.fac_slot) {
+                    int nf = 0;
+                    for (int b = 0; b < m.nblocks; ++b) {
+                        const int f = d.fac_slot[b];
+                        if (f < 0 || f > m.nblocks) return fail(TWOLDG_EINVAL, "fac_slot out of range");
+                        if (f > 0 && d.elem_slot[b] != 0)
+                            return fail(TWOLDG_EINVAL, "block " + std::to_string(b) +
+                                                           " has both per-element and factored truncation tables");
+                        g->fslot[b] = f;
+                        nf = std::max(nf, f);
+                    }
+                    if (nf > 0) {
+                        if (!d.fac_radial || !d.fac_rmodes || !d.fac_rduals || !d.fac_aslot || !d.fac_aw ||
+                            !d.fac_achol || d.fac_ntab < 1)
+                            return fail(TWOLDG_EINVAL, "fac_slot names factored blocks but their tables are missing");
+                        g->fradial.assign(d.fac_radial, d.fac_radial + nf);
+                        g->faslot.assign(d.fac_aslot, d.fac_aslot + nf);
+                        for (int f = 0; f < nf; ++f)
+                            if (g->fradial[f] < 0 || g->fradial[f] > 2 || g->faslot[f] < 0 ||
+                                g->faslot[f] >= d.fac_ntab)
+                                return fail(TWOLDG_EINVAL, "factored block " + std::to_string(f) +
+                                                               " has a bad radial dimension or angular table");
+                        const size_t nr = P1 * m.E * nf, n2 = P1 * P1, m2 = (size_t)m.P * m.P;
+                        const size_t e2 = (size_t)m.E * m.E;
+                        g->frm.assign(d.fac_rmodes, d.fac_rmodes + nr);
+                        g->frd.assign(d.fac_rduals, d.fac_rduals + nr);
+                        g->faw.assign(d.fac_aw, d.fac_aw + n2 * e2 * d.fac_ntab);
+                        g->fachol.assign(d.fac_achol, d.fac_achol + m2 * m2 * e2 * d.fac_ntab);
+                    }
+                }
             } else if (metric) {
                 const size_t nc = (size_t)(1 + m.D) * m.NN * m.nblocks;
                 g->coef.insert(g->coef.end(), d.coef, d.coef + nc);
@@ -280,6 +329,21 @@ struct twoldg_runner {
                 CK(cudaMemcpy(g.d_bndx.p, g.bndx.data(), g.bndx.size() * sizeof(double), cudaMemcpyHostToDevice));
                 CK(g.d_eslot.alloc(g.eslot.size() * sizeof(int)));
                 CK(cudaMemcpy(g.d_eslot.p, g.eslot.data(), g.eslot.size() * sizeof(int), cudaMemcpyHostToDevice));
+                CK(g.d_fslot.alloc(g.fslot.size() * sizeof(int)));
+                CK(cudaMemcpy(g.d_fslot.p, g.fslot.data(), g.fslot.size() * sizeof(int), cudaMemcpyHostToDevice));
+                if (!g.fradial.empty()) {
+                    CK(g.d_fradial.alloc(g.fradial.size() * sizeof(int)));
+                    CK(cudaMemcpy(g.d_fradial.p, g.fradial.data(), g.fradial.size() * sizeof(int),
+                                  cudaMemcpyHostToDevice));
+                    CK(g.d_faslot.alloc(g.faslot.size() * sizeof(int)));
+                    CK(cudaMemcpy(g.d_faslot.p, g.faslot.data(), g.faslot.size() * sizeof(int),
+                                  cudaMemcpyHostToDevice));
+                    int rr = upload_t(g.d_frm, g.frm);
+                    if (!rr) rr = upload_t(g.d_frd, g.frd);
+                    if (!rr) rr = upload_t(g.d_faw, g.faw);
+                    if (!rr) rr = upload_t(g.d_fachol, g.fachol);
+                    if (rr) return rr;
+                }
             } else if (g.metric) {
                 // the per-line tables of every member into the group's (P+1, E, nitems, D) layout
                 const int P1 = g.P + 1, nit = (int)g.items.size();
@@ -371,6 +435,16 @@ struct twoldg_runner {
         for (int q = 0; q < 3; ++q) p.wave_k[q] = g.wave_k[q];
         p.wave_phi = g.wave_phi;
         p.eslot = (const int*)g.d_eslot.p;
+        p.boundary = g.boundary;
+        p.kappa = g.kappa;
+        p.inv_r = g.inv_r;
+        p.fslot = (const int*)g.d_fslot.p;
+        p.fradial = (const int*)g.d_fradial.p;
+        p.frm = g.d_frm.p;
+        p.frd = g.d_frd.p;
+        p.faslot = (const int*)g.d_faslot.p;
+        p.faw = g.d_faw.p;
+        p.fachol = g.d_fachol.p;
         p.ew = g.d_ew.p;
         p.echol = g.d_echol.p;
         p.partial = (double*)g.d_part.p;
@@ -410,22 +484,27 @@ struct twoldg_runner {
         return TWOLDG_OK;
     }
 
+    // Stage s of group g (reading the face planes `in`), enqueued on st.
+    int enqueue_stage(Group& g, void* u, int s, int in, cudaStream_t st) {
+        if (g.full) {
+            FmPtrs fp = fptrs(g, u, in);
+            CK(g.ops->fm_gradient((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, fp, st));
+            CK(g.ops->fm_stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, fp, st));
+            return TWOLDG_OK;
+        }
+        if (!g.cf.empty())
+            CK(g.ops->cf_ghosts((const CfFace*)g.d_cf.p, (int)g.cf.size(), g.E, g.fu[in].p, g.fog[in].p, g.ugd.p,
+                                g.gfd.p, g.ggd.p, st));
+        StagePtrs p = ptrs(g, u, in);
+        CK(g.ops->stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, p, 0, st));
+        return TWOLDG_OK;
+    }
+
     // One RK4 step of group g, its four stages enqueued on st.
     int enqueue_group(Group& g, void* u, cudaStream_t st) {
-        int in = 0;
         for (int s = 1; s <= 4; ++s) {
-            if (g.full) {
-                FmPtrs fp = fptrs(g, u, in);
-                CK(g.ops->fm_gradient((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, fp, st));
-                CK(g.ops->fm_stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, fp, st));
-            } else {
-                if (!g.cf.empty())
-                    CK(g.ops->cf_ghosts((const CfFace*)g.d_cf.p, (int)g.cf.size(), g.E, g.fu[in].p, g.fog[in].p,
-                                        g.ugd.p, g.gfd.p, g.ggd.p, st));
-                StagePtrs p = ptrs(g, u, in);
-                CK(g.ops->stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, p, 0, st));
-            }
-            in = 1 - in;
+            int r = enqueue_stage(g, u, s, (s - 1) & 1, st);
+            if (r) return r;
         }
         return TWOLDG_OK;
     }
@@ -853,18 +932,17 @@ int twoldg_profile_step(twoldg_problem* p, void* u, double dt, float* stage_ms) 
     if (r) return r;
     cudaEvent_t ev[5];
     for (int i = 0; i < 5; ++i) CK(cudaEventCreate(&ev[i]));
-    int in = 0;
     CK(cudaEventRecord(ev[0], p->stream));
     for (int s = 1; s <= 4; ++s) {
         for (auto& gp : p->groups) {
-            Group& g = *gp;
-            r = p->cf_all(g, in);
+            r = p->enqueue_stage(*gp, u, s, (s - 1) & 1, p->stream);
             if (r) return r;
-            StagePtrs sp = p->ptrs(g, u, in);
-            CK(g.ops->stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, sp, 0, p->stream));
         }
-        in = 1 - in;
         CK(cudaEventRecord(ev[s], p->stream));
+    }
+    if (p->any_full()) {
+        p->fm_advance_time(p->stream);
+        CK(cudaGetLastError());
     }
     CK(cudaEventSynchronize(ev[4]));
     for (int s = 0; s < 4; ++s) CK(cudaEventElapsedTime(&stage_ms[s], ev[s], ev[s + 1]));
