@@ -107,6 +107,37 @@ typedef struct twoldg_desc {
     double wave_k[3];
     double wave_phi;
     const double* bnd_x;
+    /* The boundary faces' condition: 0 the Dirichlet plane wave above; 1 the
+     * radiative, maximally dissipative condition n . grad u = -(kappa du/dt +
+     * inv_r u) (RadiativeBoundary, src/evolution.jl:1129-1260): u's ghost is
+     * the face node's own u, and the gradient's ghost makes the flux through
+     * the face F* = -sigma |S[d]| (kappa v + inv_r u), sigma = -1 on a low
+     * face and +1 on a high one. kappa >= 0; inv_r = 1/R, or 0 without the u/R
+     * term. The energy then carries the boundary's own term,
+     * 1/2 inv_r sum w |S[d]| u^2 over the boundary faces' nodes. */
+    int32_t boundary;
+    double kappa;
+    double inv_r;
+    /* The factored truncation (FactoredTruncation, src/evolution.jl:759-899)
+     * of blocks whose sqrt(g) is a radial factor along one dimension times an
+     * angular factor across it (the thirteen-patch ball's outer shells), NULL
+     * when there are none: fac_slot[b] = 0 for any other block and f + 1 for the
+     * factored block f; fac_radial[f] its radial dimension (0-based);
+     * fac_rmodes / fac_rduals (P+1, E, nfac) the rank-one pair along it per
+     * element index; fac_aslot[f] its angular tables among fac_ntab: fac_aw
+     * ((P+1)^2, E^2, fac_ntab), the in-plane quadrature weights times the
+     * angular factor, and fac_achol (P^2, P^2, E^2, fac_ntab), the upper
+     * Cholesky factor of the in-plane Gram matrix; in-plane nodes, elements
+     * and modes run over the two dimensions across the radial one in
+     * increasing order, the first fastest. Such a block has elem_slot 0. */
+    const int32_t* fac_slot;
+    const int32_t* fac_radial;
+    const double* fac_rmodes;
+    const double* fac_rduals;
+    const int32_t* fac_aslot;
+    const double* fac_aw;
+    const double* fac_achol;
+    int32_t fac_ntab;
 } twoldg_desc;
 
 typedef struct twoldg_problem twoldg_problem;

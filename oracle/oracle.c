@@ -68,6 +68,11 @@ typedef struct {
     double wave_k[3];
     double wave_phi;
     double t;
+    /* the boundary faces' condition: 0 the Dirichlet plane wave, 1 radiative
+     * (src/evolution.jl:1129-1260): u's ghost is the face node's u, and the
+     * face's flux is F* = -sigma |S[d]| (kappa v + inv_r u) */
+    int boundary;
+    double kappa, inv_r;
 } oracle_mesh;
 
 typedef struct {
@@ -651,7 +656,11 @@ static void full_gradient(const oracle_mesh* m, const double* u, double* V) {
                         for (int q = 0; q < 3; ++q) if (q != e) tt[k2++] = x[q];
                         t = tt[0] + N * tt[1];
                         val = full_ghost(m, N, NN, u, 2 * NN, 0, 0, b, face, t);
-                        if (isnan(val)) {
+                        if (isnan(val) && m->boundary == 1) {
+                            int y[3] = {x[0], x[1], x[2]};
+                            y[e] = pos < 0 ? 0 : N - 1;
+                            val = u[(int64_t)b * 2 * NN + y[0] + N * (y[1] + N * y[2])];
+                        } else if (isnan(val)) {
                             const double* X = m->bnd_x + ((int64_t)b * 6 + face) * 3 * F;
                             val = sin(wave_phase(m, X, (int)F, t, m->t));
                         }
@@ -702,6 +711,20 @@ int oracle_rhs_full(const oracle_mesh* m, const double* u, double* du) {
                         int t = tt[0] + N * tt[1];
                         y[d] = pos < 0 ? 0 : N - 1;
                         sn = y[0] + N * (y[1] + N * y[2]);
+                        if (m->face_nb[b * 6 + face] < 0 && m->boundary == 1) {
+                            /* the ghost's flux 2 F* - F: the central flux is F* */
+                            double Fo = 0, S2 = 0;
+                            for (int ci = 0; ci < 3; ++ci) {
+                                double Sc = cf[(1 + 3 * d + ci) * NN + sn];
+                                Fo += Sc * V[(int64_t)b * 3 * NN + ci * NN + sn];
+                                S2 += Sc * Sc;
+                            }
+                            double sigma = pos >= N ? 1.0 : -1.0;
+                            double us = u[(int64_t)b * 2 * NN + sn], vs = u[(int64_t)b * 2 * NN + NN + sn];
+                            double Fstar = -sigma * sqrt(S2) * (m->kappa * vs + m->inv_r * us);
+                            acc += coefk * (2 * Fstar - Fo);
+                            continue;
+                        }
                         if (m->face_nb[b * 6 + face] < 0) {
                             const double* X = m->bnd_x + ((int64_t)b * 6 + face) * 3 * F;
                             double c = cos(wave_phase(m, X, (int)F, t, m->t));
@@ -887,6 +910,23 @@ int oracle_energy_full(const oracle_mesh* m, const double* u, double* out) {
             double q = vv * vv;
             for (int ci = 0; ci < 3; ++ci) q += V[(int64_t)b * 3 * NN + ci * NN + n] * V[(int64_t)b * 3 * NN + ci * NN + n];
             s += w * cf[n] * q;
+        }
+        /* a radiative boundary's own energy: inv_r sum w |S[d]| u^2 over its faces' nodes */
+        if (m->boundary == 1 && m->inv_r != 0) {
+            for (int face = 0; face < 6; ++face) {
+                if (m->face_nb[b * 6 + face] >= 0) continue;
+                int d = face / 2;
+                for (int t = 0; t < N * N; ++t) {
+                    int x[3];
+                    face_node(N, face, t, (face & 1) ? N - 1 : 0, x);
+                    int64_t n = x[0] + (int64_t)N * (x[1] + (int64_t)N * x[2]);
+                    double w = 1, S2 = 0;
+                    for (int q = 0; q < 3; ++q) if (q != d) w *= h * P1 / 2.0 * m->weights[x[q] % P1];
+                    for (int ci = 0; ci < 3; ++ci) S2 += cf[(1 + 3 * d + ci) * NN + n] * cf[(1 + 3 * d + ci) * NN + n];
+                    double uu = u[(int64_t)b * 2 * NN + n];
+                    s += w * sqrt(S2) * m->inv_r * uu * uu;
+                }
+            }
         }
         e += 0.5 * s;
     }

@@ -29,6 +29,7 @@ class OracleMesh(ctypes.Structure):
         ("face_nb", ctypes.POINTER(ctypes.c_int32)), ("face_code", ctypes.POINTER(ctypes.c_int32)),
         ("elem_slot", ctypes.POINTER(ctypes.c_int32)), ("bnd_x", ctypes.POINTER(ctypes.c_double)),
         ("wave_k", ctypes.c_double * 3), ("wave_phi", ctypes.c_double), ("t", ctypes.c_double),
+        ("boundary", ctypes.c_int), ("kappa", ctypes.c_double), ("inv_r", ctypes.c_double),
     ]
 
 
@@ -180,12 +181,15 @@ def threads():
 
 
 class BallOracle(Oracle):
-    """The oracle on a ball forest (full metric, glue, Dirichlet plane wave):
-    coef (sqrt(g), S) from the geometry, the face table, the blocks whose
-    truncation is the per-element projection; the projections themselves are
-    solved by the oracle."""
+    """The oracle on a ball forest (full metric, glue, Dirichlet plane wave or
+    radiative boundary): coef (sqrt(g), S) from the geometry, the face table,
+    the blocks whose truncation is the sqrt(g)-orthogonal projection per
+    element (every block off the affine cube, the factored ones included:
+    the oracle solves each element's projection from sqrt(g) itself, so the
+    factored tables are checked against it); `radiative` is (kappa, inv_r)
+    or None."""
 
-    def __init__(self, forest, P, tables, wave, truncate=True):
+    def __init__(self, forest, P, tables, wave, truncate=True, radiative=None):
         self.forest = forest
         self.P = P
         self.D = 3
@@ -203,16 +207,19 @@ class BallOracle(Oracle):
                  coef=np.ascontiguousarray(tables["coef"], dtype=np.float64),
                  face_nb=np.ascontiguousarray(forest.face_nb, dtype=np.int32),
                  face_code=np.ascontiguousarray(forest.face_code, dtype=np.int32),
-                 elem_slot=np.ascontiguousarray(tables["elem_slot"], dtype=np.int32),
+                 elem_slot=np.ascontiguousarray((np.asarray(tables["elem_slot"]) != 0) |
+                                                (np.asarray(tables.get("fac_slot", 0)) != 0), dtype=np.int32),
                  bnd_x=np.ascontiguousarray(tables["bnd_x"], dtype=np.float64))
         self._arrays = a
         m = OracleMesh()
         m.D, m.P, m.E, m.nblocks, m.truncate = 3, P, self.E, self.nblocks, 1 if truncate else 0
         for k in range(3):
             m.roots[k], m.periodic[k], m.reflecting[k], m.lo[k], m.hi[k] = 1, 0, 0, 0.0, 1.0
-            m.wave_k[k] = wave.k[k]
-        m.wave_phi = wave.phi
+            m.wave_k[k] = wave.k[k] if wave is not None else 0.0
+        m.wave_phi = wave.phi if wave is not None else 0.0
         m.metric = 2
+        if radiative is not None:
+            m.boundary, m.kappa, m.inv_r = 1, float(radiative[0]), float(radiative[1])
         dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int32)
         m.level = a["level"].ctypes.data_as(ip)
         m.corner = a["corner"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64))

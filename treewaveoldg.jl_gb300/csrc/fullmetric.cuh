@@ -53,6 +53,20 @@ struct FmArgs {
     const T* ew;        // ((P+1)^3, E^3, ntab)
     const T* echol;     // (P^3, P^3, E^3, ntab), upper factor U, G = U^T U
     double* partial;    // energy
+    // the boundary faces' condition: 0 Dirichlet (the wave), 1 radiative
+    int boundary;
+    T kappa;
+    T inv_r;
+    // the factored truncation: per item 0 or 1 + its factored index f; per f
+    // the radial dimension, the pair (P+1, E, nf), the angular table index;
+    // the angular tables ((P+1)^2, E^2, ntab) and (P^2, P^2, E^2, ntab)
+    const int* fslot;
+    const int* fradial;
+    const T* frm;
+    const T* frd;
+    const int* faslot;
+    const T* faw;
+    const T* fachol;
 };
 
 template <typename T, int P>
@@ -101,7 +115,13 @@ __global__ void __launch_bounds__(256) fm_gradient_kernel(FmArgs<T> a, Tab<T, P>
             const int f = i / g.F, tt = i % g.F;
             const int d = f >> 1, side = f & 1;
             T v;
-            if (it.nb[f] < 0) {
+            if (it.nb[f] < 0 && a.boundary == 1) {
+                // radiative: the face node's own u, so that the wide derivative's
+                // face correction vanishes there (src/evolution.jl:1213-1221)
+                int xo[3];
+                plane_coords<3>(g, d, tt, side == 0 ? 0 : g.N - 1, xo);
+                v = yu[oidx<3>(g, xo)];
+            } else if (it.nb[f] < 0) {
                 // Dirichlet: the data at the boundary face node's position
                 const double* X = a.bnd_x + (int64_t)(it.slot + f) * 3 * g.F;
                 const double th = a.wave.k[0] * X[tt] + a.wave.k[1] * X[g.F + tt] + a.wave.k[2] * X[2 * g.F + tt] -
@@ -225,6 +245,102 @@ __device__ __forceinline__ void fm_project_block(const G& g, const FmArgs<T>& a,
     __syncthreads();
 }
 
+// The factored truncation of one block (src/evolution.jl:308-382): along the
+// radial dimension k the rank-one pair of each element line, then on each of
+// an element's P+1 planes across k the 2D sqrt(g)-orthogonal projection with
+// the angular tables: c = Psi^T W v, U^T y = c, U z = y, v = Psi z. The two
+// act on different indices and their product is the projection onto Q_{P-1}.
+// cbuf holds (P+1) P^2 coefficients per element.
+template <typename T, int P, class G>
+__device__ __forceinline__ void fm_project_factored(const G& g, const FmArgs<T>& a, const FmTab<T, P>& ft, int f,
+                                                    T* sv, T* cbuf) {
+    constexpr int P1 = P + 1, n2 = P1 * P1, m2 = P * P;
+    const int E = g.E, EE = E * E * E, E2 = E * E;
+    const int k = a.fradial[f], A = a.faslot[f];
+    const int d0 = k == 0 ? 1 : 0, d1 = k == 2 ? 1 : 2;
+    // along k: v -= mode (dual . v) on every element line
+    for (int i = threadIdx.x; i < EE * n2; i += blockDim.x) {
+        const int e = i / n2, nn = i % n2;
+        const int ex[3] = {e % E, (e / E) % E, e / E2};
+        const T* rm = a.frm + ((int64_t)f * E + ex[k]) * P1;
+        const T* rd = a.frd + ((int64_t)f * E + ex[k]) * P1;
+        int x[3];
+        x[d0] = ex[d0] * P1 + nn % P1;
+        x[d1] = ex[d1] * P1 + nn / P1;
+        x[k] = ex[k] * P1;
+        const int l0 = lidx<3>(g, x), ls = g.lstride(k);
+        T c = T(0);
+#pragma unroll
+        for (int j = 0; j < P1; ++j) c += rd[j] * sv[l0 + j * ls];
+#pragma unroll
+        for (int j = 0; j < P1; ++j) sv[l0 + j * ls] -= rm[j] * c;
+    }
+    __syncthreads();
+    // across k, plane by plane: c = Psi^T W v
+    for (int i = threadIdx.x; i < EE * P1 * m2; i += blockDim.x) {
+        const int q = i % m2, j = (i / m2) % P1, e = i / (m2 * P1);
+        const int ex[3] = {e % E, (e / E) % E, e / E2};
+        const int ea = ex[d0] + E * ex[d1];
+        const T* W = a.faw + ((int64_t)A * E2 + ea) * n2;
+        const int q0 = q % P, q1 = q / P;
+        T c = T(0);
+        for (int nn = 0; nn < n2; ++nn) {
+            const int na = nn % P1, nb = nn / P1;
+            int x[3];
+            x[d0] = ex[d0] * P1 + na;
+            x[d1] = ex[d1] * P1 + nb;
+            x[k] = ex[k] * P1 + j;
+            c += ft.L[q0][na] * ft.L[q1][nb] * W[nn] * sv[lidx<3>(g, x)];
+        }
+        cbuf[i] = c;
+    }
+    __syncthreads();
+    for (int u = threadIdx.x; u < EE * P1; u += blockDim.x) {
+        const int e = u / P1;
+        const int ex[3] = {e % E, (e / E) % E, e / E2};
+        const int ea = ex[d0] + E * ex[d1];
+        T* c = cbuf + u * m2;
+        const T* U = a.fachol + ((int64_t)A * E2 + ea) * m2 * m2;   // U[r][q] at r + m2 q
+        for (int q = 0; q < m2; ++q) {            // U^T y = c
+            T s = c[q];
+            for (int r = 0; r < q; ++r) s -= U[r + m2 * q] * c[r];
+            c[q] = s / U[q + m2 * q];
+        }
+        for (int q = m2 - 1; q >= 0; --q) {       // U z = y
+            T s = c[q];
+            for (int r = q + 1; r < m2; ++r) s -= U[q + m2 * r] * c[r];
+            c[q] = s / U[q + m2 * q];
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < EE * P1 * n2; i += blockDim.x) {
+        const int nn = i % n2, j = (i / n2) % P1, e = i / (n2 * P1);
+        const int ex[3] = {e % E, (e / E) % E, e / E2};
+        const int na = nn % P1, nb = nn / P1;
+        const T* c = cbuf + (e * P1 + j) * m2;
+        T z = T(0);
+        for (int q = 0; q < m2; ++q) z += ft.L[q % P][na] * ft.L[q / P][nb] * c[q];
+        int x[3];
+        x[d0] = ex[d0] * P1 + na;
+        x[d1] = ex[d1] * P1 + nb;
+        x[k] = ex[k] * P1 + j;
+        sv[lidx<3>(g, x)] = z;
+    }
+    __syncthreads();
+}
+
+// The truncation of one block of the full metric: the element's tensor
+// projector (affine patch), the per-element projection, or the factored one.
+template <typename T, int P, class G>
+__device__ __forceinline__ void fm_truncate_block(const G& g, const FmArgs<T>& a, const Tab<T, P>& tb,
+                                                  const FmTab<T, P>& ft, int item, T* sv, T* cbuf) {
+    const int s = a.eslot[item];
+    const int f = a.fslot ? a.fslot[item] : 0;
+    if (s > 0) fm_project_block<T, P>(g, a, ft, s - 1, sv, cbuf);
+    else if (f > 0) fm_project_factored<T, P>(g, a, ft, f - 1, sv, cbuf);
+    else truncate_block<T, 3, P, false, 0>(g, tb, sv, nullptr);
+}
+
 template <typename T, int P, bool COMP>
 __global__ void __launch_bounds__(256) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb, FmTab<T, P> ft) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -262,6 +378,23 @@ __global__ void __launch_bounds__(256) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb
                 plane_coords<3>(g, d, tt, side == 0 ? 0 : g.N - 1, xo);
                 plane_coords<3>(g, d, tt, side == 0 ? -1 : g.N, xg);
                 const int o = oidx<3>(g, xo);
+                if (it.nb[f] < 0 && a.boundary == 1) {
+                    // radiative: the ghost's flux 2 F* - F, so that the central
+                    // flux through the face is F* = -sigma |S[d]| (kappa v + u / R)
+                    // (src/evolution.jl:1232-1260)
+                    T F = T(0), S2 = T(0);
+#pragma unroll
+                    for (int ci = 0; ci < 3; ++ci) {
+                        const T Sc = cf[(1 + 3 * d + ci) * g.NN + o];
+                        F += Sc * Vb[ci * g.NN + o];
+                        S2 += Sc * Sc;
+                    }
+                    const T* yo = ysrc + it.off;
+                    const T sigma = side ? T(1) : T(-1);
+                    const T Fstar = -sigma * sqrt(S2) * (a.kappa * yo[g.NN + o] + a.inv_r * yo[o]);
+                    sF[sidx<3>(g, xg)] = T(2) * Fstar - F;
+                    continue;
+                }
                 T Vg[3];
                 if (it.nb[f] < 0) {
                     const double* X = a.bnd_x + (int64_t)(it.slot + f) * 3 * g.F;
@@ -334,14 +467,8 @@ __global__ void __launch_bounds__(256) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb
         }
         __syncthreads();
         if (a.truncate) {
-            const int s = a.eslot[item];
-            if (s == 0) {
-                truncate_block<T, 3, P, false, 0>(g, tb, sl, nullptr);
-                if (final_comp) truncate_block<T, 3, P, false, 0>(g, tb, sc, nullptr);
-            } else {
-                fm_project_block<T, P>(g, a, ft, s - 1, sl, cbuf);
-                if (final_comp) fm_project_block<T, P>(g, a, ft, s - 1, sc, cbuf);
-            }
+            fm_truncate_block<T, P>(g, a, tb, ft, item, sl, cbuf);
+            if (final_comp) fm_truncate_block<T, P>(g, a, tb, ft, item, sc, cbuf);
         }
         for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
             int x[3];
@@ -377,9 +504,7 @@ __global__ void __launch_bounds__(256) fm_truncate_kernel(FmArgs<T> a, Tab<T, P>
             sv[lidx<3>(g, x)] = v[n];
         }
         __syncthreads();
-        const int s = a.eslot[item];
-        if (s == 0) truncate_block<T, 3, P, false, 0>(g, tb, sv, nullptr);
-        else fm_project_block<T, P>(g, a, ft, s - 1, sv, cbuf);
+        fm_truncate_block<T, P>(g, a, tb, ft, item, sv, cbuf);
         for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
             int x[3];
             owned_coords<3>(g, n, x);
@@ -412,6 +537,28 @@ __global__ void __launch_bounds__(256) fm_energy_kernel(FmArgs<T> a, Tab<T, P> t
             double s = (double)v[n] * (double)v[n];
             for (int ci = 0; ci < 3; ++ci) s += (double)Vb[ci * g.NN + n] * (double)Vb[ci * g.NN + n];
             local += w * (double)cf[n] * s;
+        }
+        // a radiative boundary's own energy, 1/2 inv_r sum w |S[d]| u^2 over its
+        // faces' nodes (src/evolution.jl:1265-1288)
+        if (a.boundary == 1 && a.inv_r != T(0)) {
+            const T* uu = a.u + it.off;
+            for (int i = threadIdx.x; i < 6 * g.F; i += blockDim.x) {
+                const int f = i / g.F, tt = i % g.F;
+                if (it.nb[f] >= 0) continue;
+                const int d = f >> 1, side = f & 1;
+                int x[3];
+                plane_coords<3>(g, d, tt, side == 0 ? 0 : g.N - 1, x);
+                const int o = oidx<3>(g, x);
+                double w = 1.0;
+                for (int q = 0; q < 3; ++q)
+                    if (q != d) w *= wscale * (double)tb.wq[x[q] % P1];
+                double S2 = 0;
+                for (int ci = 0; ci < 3; ++ci) {
+                    const double Sc = (double)cf[(1 + 3 * d + ci) * g.NN + o];
+                    S2 += Sc * Sc;
+                }
+                local += w * sqrt(S2) * (double)uu[o] * (double)uu[o] * (double)a.inv_r;
+            }
         }
         double s = block_reduce_sum<3>(local, red);
         if (threadIdx.x == 0) a.partial[item] = 0.5 * s;

@@ -52,6 +52,16 @@ struct FmPtrs {
     const void* ew;
     const void* echol;
     double* partial;
+    int boundary;       // 0 Dirichlet plane wave, 1 radiative
+    double kappa;
+    double inv_r;
+    const int* fslot;   // factored truncation (fullmetric.cuh)
+    const int* fradial;
+    const void* frm;
+    const void* frd;
+    const int* faslot;
+    const void* faw;
+    const void* fachol;
 };
 
 // A launch layout of the stage kernel. kernel: 0 the shape's default, 1 the

@@ -333,13 +333,22 @@ public:
         a.ew = (const T*)p.ew;
         a.echol = (const T*)p.echol;
         a.partial = p.partial;
+        a.boundary = p.boundary;
+        a.kappa = (T)p.kappa;
+        a.inv_r = (T)p.inv_r;
+        a.fslot = p.fslot;
+        a.fradial = p.fradial;
+        a.frm = (const T*)p.frm;
+        a.frd = (const T*)p.frd;
+        a.faslot = p.faslot;
+        a.faw = (const T*)p.faw;
+        a.fachol = (const T*)p.fachol;
         return a;
     }
     static size_t fm_grad_smem(int E) { return (padded_words(E) + 3 * plain_words(E)) * sizeof(T); }
-    static size_t fm_stage_smem(int E) {
-        size_t m3 = (size_t)P * P * P, EE = (size_t)E * E * E;
-        return (padded_words(E) + 2 * plain_words(E) + EE * m3) * sizeof(T);
-    }
+    // coefficients per element: P^3 (per-element projection) or (P+1) P^2 (factored)
+    static size_t fm_cbuf_words(int E) { return (size_t)E * E * E * (P + 1) * P * P; }
+    static size_t fm_stage_smem(int E) { return (padded_words(E) + 2 * plain_words(E) + fm_cbuf_words(E)) * sizeof(T); }
     cudaError_t fm_gradient(const BlockItem* items, int nitems, int E, int mode, const FmPtrs& p,
                             cudaStream_t s) const override {
         if constexpr (D != 3) return cudaErrorNotSupported;
@@ -366,7 +375,7 @@ public:
                             cudaStream_t s) const override {
         if constexpr (D != 3) return cudaErrorNotSupported;
         else {
-            size_t smem = (plain_words(E) + (size_t)E * E * E * P * P * P) * sizeof(T);
+            size_t smem = (plain_words(E) + fm_cbuf_words(E)) * sizeof(T);
             if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
             fm_truncate_kernel<T, P><<<std::min(nitems, kMaxGrid), 256, smem, s>>>(
                 fm_args(items, nitems, E, 0, 1, p), tb_, ft_);

@@ -17,6 +17,7 @@ from .indicator import modal_indicator, mode_amplitude
 from .batch import Batch, fill_batch, sine_ensemble
 from .geometry import (PolarAnnulus, annulus_errors, annulus_exact, annulus_forest, annulus_wavenumber,
                        metric_tables, projector_mode)
-from .ball import BallForest, PlaneWave, SevenPatchBall, sevenpatch_errors, sevenpatch_exact, sevenpatch_forest
+from .ball import (BallForest, OutgoingPulse, PlaneWave, RadiativeBoundary, SevenPatchBall, ThirteenPatchBall,
+                   radiative_errors, sevenpatch_errors, sevenpatch_exact, sevenpatch_forest, thirteenpatch_forest)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

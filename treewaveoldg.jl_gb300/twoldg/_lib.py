@@ -39,6 +39,11 @@ class Desc(ctypes.Structure):
         ("elem_w", ctypes.POINTER(ctypes.c_double)), ("elem_chol", ctypes.POINTER(ctypes.c_double)),
         ("elem_ntab", ctypes.c_int32), ("wave_k", ctypes.c_double * 3), ("wave_phi", ctypes.c_double),
         ("bnd_x", ctypes.POINTER(ctypes.c_double)),
+        ("boundary", ctypes.c_int32), ("kappa", ctypes.c_double), ("inv_r", ctypes.c_double),
+        ("fac_slot", ctypes.POINTER(ctypes.c_int32)), ("fac_radial", ctypes.POINTER(ctypes.c_int32)),
+        ("fac_rmodes", ctypes.POINTER(ctypes.c_double)), ("fac_rduals", ctypes.POINTER(ctypes.c_double)),
+        ("fac_aslot", ctypes.POINTER(ctypes.c_int32)), ("fac_aw", ctypes.POINTER(ctypes.c_double)),
+        ("fac_achol", ctypes.POINTER(ctypes.c_double)), ("fac_ntab", ctypes.c_int32),
     ]
 
 

@@ -124,27 +124,123 @@ class SevenPatchBall:
         return tuple((1 - rho) * f[j] + (rho * self.R1 / norm) * f[j] for j in range(3))
 
     def frame(self, xi, p):
-        """sqrt(g) and the area vectors S[d][i] = sqrt(g) d xi^d / d x^i at logical xi
-        (src/geometry.jl:402-409), by forward-mode differentiation of the map."""
-        shape = np.shape(xi[0])
-        duals = [Dual(xi[j], [np.ones(shape) if q == j else np.zeros(shape) for q in range(3)]) for j in range(3)]
-        x = self.position(duals, p)
-        Jm = np.empty(shape + (3, 3))
-        for i in range(3):
-            xi_ = Dual.lift(x[i])
-            for j in range(3):
-                Jm[..., i, j] = np.broadcast_to(xi_.d[j], shape)
-        J = np.abs(np.linalg.det(Jm))
-        Ji = np.linalg.inv(Jm)               # Ji[d, i] = d xi^d / d x^i
-        S = J[..., None, None] * Ji          # S[..., d, i]
-        return J, S
+        return map_frame(self, xi, p)
 
     def outer_radius(self):
         return self.R1
 
+    npatches = 7
+
+    def affine_patch(self, p):
+        return p == 0
+
+    def factored_dim(self, p):
+        """The dimension along which sqrt(g) splits on patch p, or -1: on no
+        patch of the seven-patch ball (src/geometry.jl:123-135)."""
+        return -1
+
+
+def map_frame(geo, xi, p):
+    """sqrt(g) and the area vectors S[d][i] = sqrt(g) d xi^d / d x^i at logical xi
+    of patch p (src/geometry.jl:402-409, 655-662), by forward-mode
+    differentiation of the geometry's map."""
+    shape = np.shape(xi[0])
+    duals = [Dual(xi[j], [np.ones(shape) if q == j else np.zeros(shape) for q in range(3)]) for j in range(3)]
+    x = geo.position(duals, p)
+    Jm = np.empty(shape + (3, 3))
+    for i in range(3):
+        xi_ = Dual.lift(x[i])
+        for j in range(3):
+            Jm[..., i, j] = np.broadcast_to(xi_.d[j], shape)
+    J = np.abs(np.linalg.det(Jm))
+    Ji = np.linalg.inv(Jm)               # Ji[d, i] = d xi^d / d x^i
+    S = J[..., None, None] * Ji          # S[..., d, i]
+    return J, S
+
+
+class ThirteenPatchBall:
+    """The thirteen-patch ball (src/geometry.jl:555-717), patches 0-based:
+    the seven-patch ball out to the middle sphere |x| = Rm (patches 0-6,
+    roots (n, m)), and six outer shells over the same cube faces (patches
+    7-12, m' roots along the radial dimension k and n across it) whose
+    radial coordinate is exactly radial: c_k = s, c_j = 2 xi_j / n - 1,
+    rho = xi_k / m' (s = 1) or 1 - xi_k / m' (s = -1), x = (Rm + (R1 - Rm) rho)
+    c / |c|. On an outer shell sqrt(g) = r^2 r' (2/n)^2 (1 + c_a^2 + c_b^2)^(-3/2),
+    a radial factor times an angular one that is the same on all six."""
+
+    npatches = 13
+
+    def __init__(self, Lc, Rm, R1, roots):
+        if not Lc > 0:
+            raise ValueError("the cube's half-width Lc must be positive, got %r" % (Lc,))
+        if not Rm > math.sqrt(3) * Lc:
+            raise ValueError("the middle radius Rm = %r must exceed sqrt(3) Lc = %r, so that the cube's corners lie "
+                             "inside the middle sphere and every inner shell maps one to one"
+                             % (Rm, math.sqrt(3) * Lc))
+        if not R1 > Rm:
+            raise ValueError("the outer radius R1 = %r must exceed the middle radius Rm = %r" % (R1, Rm))
+        if len(roots) != 3:
+            raise ValueError("the thirteen-patch ball takes roots = (n, m, m'), the cube's per side and the inner "
+                             "and outer shells' radial ones, got %r" % (tuple(roots),))
+        if not all(r > 0 for r in roots):
+            raise ValueError("every patch of the ball needs a positive number of roots along each dimension, "
+                             "got %r" % (tuple(roots),))
+        self.Lc, self.Rm, self.R1 = float(Lc), float(Rm), float(R1)
+        self.roots = tuple(int(r) for r in roots)
+        self.inner = SevenPatchBall(Lc, Rm, self.roots[:2])
+
+    def patch_roots(self, p):
+        if p < 7:
+            return self.inner.patch_roots(p)
+        n, _, m2 = self.roots
+        k, _ = SHELLS[p - 7]
+        return tuple(m2 if j == k else n for j in range(3))
+
+    def outer_radius_at(self, xk, s):
+        m2 = self.roots[2]
+        rho = xk / m2 if s == 1 else 1 - xk / m2
+        return self.Rm + (self.R1 - self.Rm) * rho
+
+    def position(self, xi, p):
+        if p < 7:
+            return self.inner.position(xi, p)
+        n = self.roots[0]
+        k, s = SHELLS[p - 7]
+        c = [s * (xi[j] * 0 + 1) if j == k else 2 * xi[j] / n - 1 for j in range(3)]
+        norm = dsqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2])
+        r = self.outer_radius_at(xi[k], s)
+        return tuple((r / norm) * c[j] for j in range(3))
+
+    def frame(self, xi, p):
+        return map_frame(self, xi, p)
+
+    def outer_radius(self):
+        return self.R1
+
+    def affine_patch(self, p):
+        return p == 0
+
+    def factored_dim(self, p):
+        """The radial dimension of an outer shell, along which sqrt(g) splits
+        (src/geometry.jl:671); -1 elsewhere."""
+        return SHELLS[p - 7][0] if p >= 7 else -1
+
+    def radial_volume(self, xk, p):
+        """r^2 r' at the radial coordinate xk of outer shell p (src/geometry.jl:675-679)."""
+        _, s = SHELLS[p - 7]
+        r = self.outer_radius_at(xk, s)
+        return r * r * ((self.R1 - self.Rm) / self.roots[2])
+
+    def angular_volume(self, xa, xb):
+        """(2/n)^2 (1 + c_a^2 + c_b^2)^(-3/2), the gnomonic area element, at the two
+        coordinates across the radial one (src/geometry.jl:681-687)."""
+        n = self.roots[0]
+        ca, cb = 2 * xa / n - 1, 2 * xb / n - 1
+        q = 1 + ca * ca + cb * cb
+        return (2.0 / n) ** 2 / (q * np.sqrt(q))
 
 class BallForest:
-    """The forest of the ball: seven patches of root blocks (level 0) and
+    """The forest of a ball: its patches' root blocks (level 0) and
     the explicit face table. Blocks are ordered patch by patch, and within a
     patch by corner with the first dimension fastest."""
 
@@ -153,7 +249,7 @@ class BallForest:
         self.D = 3
         self.N = int(N)
         self.blocks = []                    # (patch, corner)
-        for p in range(7):
+        for p in range(geo.npatches):
             r = geo.patch_roots(p)
             for c2 in range(r[2]):
                 for c1 in range(r[1]):
@@ -278,6 +374,32 @@ def sevenpatch_forest(T, P, E, roots=(2, 2), Lc=1.0, R1=3.0, grading=0.0):
     return forest, geo
 
 
+def thirteenpatch_forest(T, P, E, roots=(2, 1, 1), Lc=1.0, Rm=2.0, R1=3.0):
+    """The thirteen-patch ball's forest and its map (src/geometry.jl:719-751):
+    roots = (n, m, m'), the cube's per side and the inner and outer shells'
+    radial ones."""
+    from .element import Element
+    if E % 2:
+        raise ValueError("E = %d elements of order P = %d per block is odd, and E must be even" % (E, P))
+    if len(tuple(roots)) != 3:
+        raise ValueError("the thirteen-patch ball takes roots = (n, m, m'), the cube's per side and the inner "
+                         "and outer shells' radial ones, got %r" % (tuple(roots),))
+    geo = ThirteenPatchBall(Lc, Rm, R1, roots)
+    forest = BallForest(geo, E * (P + 1))
+    build_ball_faces(forest, Element(np.float64, P).offsets.astype(np.float64))
+    return forest, geo
+
+
+def ball_forest(T, P, E, roots, Lc, R1, Rm=None, grading=0.0):
+    """The seven-patch ball, or with a middle radius Rm the thirteen-patch one
+    (src/sevenpatch.jl:119-128)."""
+    if Rm is None:
+        return sevenpatch_forest(T, P, E, roots=roots, Lc=Lc, R1=R1, grading=grading)
+    if grading != 0:
+        raise ValueError("the thirteen-patch ball's inner shells are ungraded: grading must be 0 with Rm")
+    return thirteenpatch_forest(T, P, E, roots=roots, Lc=Lc, Rm=Rm, R1=R1)
+
+
 def node_logical(forest, P, offsets):
     """Logical coordinates (nblocks, 3, N^3) of every node, patch-local."""
     N = forest.N
@@ -303,6 +425,52 @@ class PlaneWave:
     def state(self, X, t, var):
         th = sum(self.k[j] * X[j] for j in range(3)) - self.omega * t + self.phi
         return np.sin(th) if var == 1 else -self.omega * np.cos(th)
+
+
+class RadiativeBoundary:
+    """The radiative, maximally dissipative condition on a ball's outer
+    sphere (src/evolution.jl:1129-1160): n . grad u = -(kappa du/dt + u/R),
+    R the geometry's outer radius; inverse_r = False drops the u/R term.
+    kappa = 1 with u/R is Sommerfeld's condition; kappa = 0 without it a wall
+    that holds the normal derivative at zero."""
+
+    def __init__(self, kappa=1.0, inverse_r=True):
+        if not kappa >= 0:
+            raise ValueError("kappa = %r is negative, and a radiative boundary with kappa < 0 feeds energy in: "
+                             "take kappa >= 0, kappa = 1 for Sommerfeld's condition" % (kappa,))
+        self.kappa = float(kappa)
+        self.inverse_r = bool(inverse_r)
+
+
+class OutgoingPulse:
+    """u = (f(t - r) - f(t + r)) / r with f(s) = exp(-s^2/w^2), a solution of the
+    wave equation regular at the origin, and v = du/dt (src/sevenpatch.jl:130-177);
+    below r = w/1000 the series in r through r^4."""
+
+    def __init__(self, w):
+        self.w = float(w)
+
+    def state(self, X, t, var):
+        w = self.w
+        X = [np.asarray(x, dtype=np.float64) for x in X]
+        r = np.sqrt(X[0] ** 2 + X[1] ** 2 + X[2] ** 2)
+        f = lambda s: np.exp(-(s / w) ** 2)
+        df = lambda s: -2 * s / w ** 2 * f(s)
+        rs = np.where(r > w / 1000, r, 1.0)
+        if var == 1:
+            far = (f(t - rs) - f(t + rs)) / rs
+        else:
+            far = (df(t - rs) - df(t + rs)) / rs
+        y = t / w
+        H = (2 * y, 4 * y ** 2 - 2, 8 * y ** 3 - 12 * y, 16 * y ** 4 - 48 * y ** 2 + 12,
+             32 * y ** 5 - 160 * y ** 3 + 120 * y, 64 * y ** 6 - 480 * y ** 4 + 720 * y ** 2 - 120)
+        dn = lambda k: (-1 / w) ** k * H[k - 1] * f(t)
+        r2 = r * r
+        if var == 1:
+            near = -2 * (dn(1) + r2 * dn(3) / 6 + r2 ** 2 * dn(5) / 120)
+        else:
+            near = -2 * (dn(2) + r2 * dn(4) / 6 + r2 ** 2 * dn(6) / 120)
+        return np.where(r > w / 1000, far, near)
 
 
 def legendre_at(P, x):
@@ -340,7 +508,8 @@ def ball_tables(forest, P, wave=None):
         g = np.einsum("ndi,nei->nde", S, S) / (J ** 2)[:, None, None]
         speed = np.sqrt(np.max(np.linalg.eigvalsh(g), axis=1)).max()
         hspeed = min(hspeed, h / speed)
-    # per-element truncation tables for the shells (the cube is affine: slot 0)
+    # per-element truncation tables for the shells whose sqrt(g) does not
+    # factorize (the cube is affine: slot 0; factored shells: fac_slot)
     L = legendre_at(P, el.nodes.astype(np.float64))   # (P+1 modes, P+1 nodes)
     nodes = np.array([(n0, n1, n2) for n2 in range(P1) for n1 in range(P1) for n0 in range(P1)])
     basis = np.array([(q0, q1, q2) for q2 in range(P) for q1 in range(P) for q0 in range(P)])
@@ -350,7 +519,7 @@ def ball_tables(forest, P, wave=None):
     slot = np.zeros(nb, dtype=np.int32)
     ws, chols = [], []
     for b, (p, c) in enumerate(forest.blocks):
-        if p == 0:
+        if geo.affine_patch(p) or geo.factored_dim(p) >= 0:
             continue
         slot[b] = len(ws) + 1
         Wb = np.empty((E ** 3, P1 ** 3))
@@ -370,6 +539,7 @@ def ball_tables(forest, P, wave=None):
     # (n3, E^3, ntab) column-major == (ntab, E^3, n3) row-major; U column-major per element
     ew = np.ascontiguousarray(np.array(ws)).reshape(-1) if ws else np.zeros(1)
     echol = np.ascontiguousarray(np.array(chols).transpose(0, 1, 3, 2)).reshape(-1) if chols else np.zeros(1)
+    fac = factored_tables(forest, P, el)
     # boundary face nodes' positions per slot, (3, N^2)
     bnd = np.zeros((nb * 6, 3, N * N))
     for b, (p, c) in enumerate(forest.blocks):
@@ -377,12 +547,86 @@ def ball_tables(forest, P, wave=None):
             if forest.face_nb[b * 6 + f] < 0:
                 x = geo.position(face_plane_logical(c, N, offs, f), p)
                 bnd[b * 6 + f] = np.stack([np.asarray(v) for v in x])
-    return dict(coef=np.ascontiguousarray(coef.reshape(-1)), elem_slot=slot, elem_w=ew, elem_chol=echol,
-                ntab=len(ws), bnd_x=np.ascontiguousarray(bnd.reshape(-1)), hspeed=hspeed, xl=xl)
+    out = dict(coef=np.ascontiguousarray(coef.reshape(-1)), elem_slot=slot, elem_w=ew, elem_chol=echol,
+               ntab=len(ws), bnd_x=np.ascontiguousarray(bnd.reshape(-1)), hspeed=hspeed, xl=xl)
+    out.update(fac)
+    return out
+
+
+def factored_tables(forest, P, el):
+    """The factored truncation's tables (src/evolution.jl:840-899) for the
+    blocks of patches whose sqrt(g) splits as R(x_k) Omega(x_across): per such
+    block f its radial dimension k and the rank-one pair (projector_mode in
+    the weight w_hat R) of each element along k; per distinct position
+    across k the in-plane weights w_hat_a w_hat_b Omega and the upper Cholesky
+    factor of the in-plane Gram matrix, shared by every block of a radial
+    column and by all shells of one angular factor. Float64, rounded once to
+    the field type by the library."""
+    from .geometry import projector_mode
+    geo, N = forest.geo, forest.N
+    P1 = P + 1
+    E = N // P1
+    nb = forest.nleaves()
+    wq = el.weights.astype(np.float64)
+    offs = el.offsets.astype(np.float64)
+    n = np.arange(N)
+    x1d = (n // P1) * P1 + offs[n % P1]
+    fslot = np.zeros(nb, dtype=np.int32)
+    radial, rmodes, rduals, aslot = [], [], [], []
+    keys = {}
+    firsts = []
+    for b, (p, c) in enumerate(forest.blocks):
+        k = geo.factored_dim(p)
+        if geo.affine_patch(p) or k < 0:
+            continue
+        fslot[b] = len(radial) + 1
+        radial.append(k)
+        rm = np.empty((E, P1))
+        rd = np.empty((E, P1))
+        for e in range(E):
+            R = geo.radial_volume(c[k] + x1d[e * P1:(e + 1) * P1] / N, p)
+            phi = projector_mode(el.nodes.astype(np.float64), wq, R, P)
+            gamma = np.sum(wq * R * phi ** 2)
+            rm[e] = phi
+            rd[e] = wq * R * phi / gamma
+        rmodes.append(rm)
+        rduals.append(rd)
+        across = tuple(c[j] for j in range(3) if j != k)
+        if across not in keys:
+            keys[across] = len(keys)
+            firsts.append(across)
+        aslot.append(keys[across])
+    if not radial:
+        return dict(fac_slot=fslot, fac_radial=None, fac_rmodes=None, fac_rduals=None, fac_aslot=None,
+                    fac_aw=None, fac_achol=None, fac_ntab=0)
+    L = legendre_at(P, el.nodes.astype(np.float64))
+    nodes2 = np.array([(na, nb_) for nb_ in range(P1) for na in range(P1)])
+    basis2 = np.array([(q0, q1) for q1 in range(P) for q0 in range(P)])
+    Psi = (L[basis2[:, 0]][:, nodes2[:, 0]] * L[basis2[:, 1]][:, nodes2[:, 1]]).T      # (n2, m2)
+    w2 = wq[nodes2[:, 0]] * wq[nodes2[:, 1]]
+    aw = np.empty((len(firsts), E * E, P1 * P1))
+    ach = np.empty((len(firsts), E * E, P * P, P * P))
+    for A, (ca, cb) in enumerate(firsts):
+        for eb in range(E):
+            for ea in range(E):
+                xa = ca + x1d[ea * P1 + nodes2[:, 0]] / N
+                xb = cb + x1d[eb * P1 + nodes2[:, 1]] / N
+                W = w2 * geo.angular_volume(xa, xb)
+                G = Psi.T @ (W[:, None] * Psi)
+                U = np.linalg.cholesky(G).T
+                aw[A, ea + E * eb] = W
+                ach[A, ea + E * eb] = U
+    return dict(fac_slot=fslot, fac_radial=np.array(radial, dtype=np.int32),
+                fac_rmodes=np.ascontiguousarray(np.array(rmodes)).reshape(-1),
+                fac_rduals=np.ascontiguousarray(np.array(rduals)).reshape(-1),
+                fac_aslot=np.array(aslot, dtype=np.int32),
+                fac_aw=np.ascontiguousarray(aw).reshape(-1),
+                fac_achol=np.ascontiguousarray(ach.transpose(0, 1, 3, 2)).reshape(-1), fac_ntab=len(firsts))
 
 
 def ball_desc(forest, P, truncate, precision, tables, wave):
-    """The twoldg_desc of a ball problem (an explicit face table and the full metric)."""
+    """The twoldg_desc of a ball problem (an explicit face table and the full
+    metric); `wave` is the Dirichlet PlaneWave or a RadiativeBoundary."""
     import ctypes
     from . import _lib
     nb = forest.nleaves()
@@ -410,10 +654,24 @@ def ball_desc(forest, P, truncate, precision, tables, wave):
     d.elem_w = tables["elem_w"].ctypes.data_as(dp)
     d.elem_chol = tables["elem_chol"].ctypes.data_as(dp)
     d.elem_ntab = tables["ntab"]
-    for k in range(3):
-        d.wave_k[k] = wave.k[k]
-    d.wave_phi = wave.phi
+    if isinstance(wave, RadiativeBoundary):
+        d.boundary = 1
+        d.kappa = wave.kappa
+        d.inv_r = 1.0 / forest.geo.outer_radius() if wave.inverse_r else 0.0
+    else:
+        for k in range(3):
+            d.wave_k[k] = wave.k[k]
+        d.wave_phi = wave.phi
     d.bnd_x = tables["bnd_x"].ctypes.data_as(dp)
+    if tables.get("fac_ntab", 0) > 0:
+        d.fac_slot = tables["fac_slot"].ctypes.data_as(ip)
+        d.fac_radial = tables["fac_radial"].ctypes.data_as(ip)
+        d.fac_rmodes = tables["fac_rmodes"].ctypes.data_as(dp)
+        d.fac_rduals = tables["fac_rduals"].ctypes.data_as(dp)
+        d.fac_aslot = tables["fac_aslot"].ctypes.data_as(ip)
+        d.fac_aw = tables["fac_aw"].ctypes.data_as(dp)
+        d.fac_achol = tables["fac_achol"].ctypes.data_as(dp)
+        d.fac_ntab = tables["fac_ntab"]
     keep = (levels, corners, tables, forest.face_nb, forest.face_code)
     return d, keep
 
@@ -427,7 +685,7 @@ def sevenpatch_exact(geo, wave, t, forest=None):
 
 
 def sevenpatch_errors(T=np.float64, P=3, E=2, roots=(2, 2), Lc=1.0, R1=3.0, k=(1.1, -0.7, 0.5), phi=0.3, cfl=0.5,
-                      tend=1.0, truncate=True, precision=None):
+                      tend=1.0, truncate=True, precision=None, Rm=None):
     """sevenpatch_errors (src/sevenpatch.jl:61-117): the plane wave on the ball
     to tend with itself as the Dirichlet data on the sphere; sqrt(g)-weighted L2
     errors of u and v together and apart, Linf, the cube's physical spacing,
@@ -435,7 +693,7 @@ def sevenpatch_errors(T=np.float64, P=3, E=2, roots=(2, 2), Lc=1.0, R1=3.0, k=(1
     from .element import Element
     from .problem import WaveProblem, initial_state, oldg_timestep, quadrature_norm, wave_energy, wave_integrator
     T = np.dtype(T)
-    forest, geo = sevenpatch_forest(T, P, E, roots=roots, Lc=Lc, R1=R1)
+    forest, geo = ball_forest(T, P, E, roots, Lc, R1, Rm=Rm)
     wave = PlaneWave(k, phi)
     problem = WaveProblem(forest, Element(T, P), truncate=truncate, geometry=geo, boundary=wave,
                           precision=precision)
@@ -448,6 +706,36 @@ def sevenpatch_errors(T=np.float64, P=3, E=2, roots=(2, 2), Lc=1.0, R1=3.0, k=(1
     integ.solve()
     u = integ.u
     ue = problem.to_device(problem.fill_at_nodes(sevenpatch_exact(geo, wave, t_end)))
+    h = forest.minimum_spacing() * 2 * geo.Lc / geo.roots[0]
+    return dict(l2=quadrature_norm(problem, u, 2, ref=ue), l2u=quadrature_norm(problem, u, 2, (1,), ref=ue),
+                l2v=quadrature_norm(problem, u, 2, (2,), ref=ue), linf=quadrature_norm(problem, u, math.inf, ref=ue),
+                h=h, he=(P + 1) * h, nsteps=nsteps, dt=dt, tend=t_end, nblocks=forest.nleaves(),
+                energy0=wave_energy(problem, u0, t=0.0), energy=wave_energy(problem, u, t=t_end))
+
+
+def radiative_errors(T=np.float64, P=3, E=2, roots=(2, 2), Lc=1.0, R1=3.0, w=0.5, kappa=1.0, inverse_r=True,
+                     cfl=0.5, tend=2.0, truncate=True, precision=None, Rm=None):
+    """radiative_errors (src/sevenpatch.jl:186-237): the outgoing pulse of width
+    w from the origin to tend under a radiative boundary of kappa (and u/R) on
+    the outer sphere; sqrt(g)-weighted L2 errors of u and v together and apart,
+    Linf, the cube's physical spacing, the step count and the energies, the
+    boundary's own term included."""
+    from .element import Element
+    from .problem import WaveProblem, initial_state, oldg_timestep, quadrature_norm, wave_energy, wave_integrator
+    T = np.dtype(T)
+    forest, geo = ball_forest(T, P, E, roots, Lc, R1, Rm=Rm)
+    pulse = OutgoingPulse(w)
+    problem = WaveProblem(forest, Element(T, P), truncate=truncate, geometry=geo,
+                          boundary=RadiativeBoundary(kappa, inverse_r), precision=precision)
+    t_end = float(T.type(tend))
+    u0 = initial_state(problem, lambda x, var: pulse.state(x, 0.0, var))
+    nsteps = int(math.ceil(T.type(t_end) / oldg_timestep(problem, cfl)))
+    dt = float(T.type(T.type(t_end) / T.type(nsteps)))
+    integ = wave_integrator(problem, u0, 0.0, t_end, dt)
+    integ.nsteps = nsteps
+    integ.solve()
+    u = integ.u
+    ue = problem.to_device(problem.fill_at_nodes(lambda x, var: pulse.state(x, t_end, var)))
     h = forest.minimum_spacing() * 2 * geo.Lc / geo.roots[0]
     return dict(l2=quadrature_norm(problem, u, 2, ref=ue), l2u=quadrature_norm(problem, u, 2, (1,), ref=ue),
                 l2v=quadrature_norm(problem, u, 2, (2,), ref=ue), linf=quadrature_norm(problem, u, math.inf, ref=ue),

@@ -113,7 +113,8 @@ class WaveProblem:
             from .ball import ball_desc, ball_tables
             if boundary is None:
                 raise ValueError("the geometry has outer faces, and no data were given for them: pass "
-                                 "boundary = PlaneWave(k, phi), the Dirichlet data on the sphere")
+                                 "boundary = PlaneWave(k, phi), the Dirichlet data on the sphere, or a "
+                                 "RadiativeBoundary")
             self.full = True
             self.metric = ball_tables(forest, el.P, boundary)
             self.hspeed = self.metric["hspeed"]
