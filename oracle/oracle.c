@@ -73,6 +73,9 @@ typedef struct {
      * face's flux is F* = -sigma |S[d]| (kappa v + inv_r u) */
     int boundary;
     double kappa, inv_r;
+    /* the per-element projections' LU factors with partial pivoting, built by
+     * oracle_full_prepare (NULL: each projection factors its own Gram matrix) */
+    void* cache;
 } oracle_mesh;
 
 typedef struct {
@@ -752,22 +755,22 @@ int oracle_rhs_full(const oracle_mesh* m, const double* u, double* du) {
     return 0;
 }
 
-/* The sqrt(g)-orthogonal projection onto Q_{P-1} of one element's v:
- * solve (Psi^T W Psi) z = Psi^T W v, v = Psi z, in long double. */
-static void full_project_element(const oracle_mesh* m, const double* cf, double* v, int N, const int* base) {
-    const int P = m->P, P1 = P + 1, n3 = P1 * P1 * P1, m3 = P * P * P;
-    long double L[16][16];
+/* Legendre L_q at the nodes, q <= P, in long double. */
+static void legendre_nodes(const oracle_mesh* m, long double L[16][16]) {
+    const int P = m->P, P1 = P + 1;
     for (int i = 0; i < P1; ++i) {
         long double x = m->nodes[i];
         L[0][i] = 1.0L;
         if (P >= 1) L[1][i] = x;
         for (int k = 2; k <= P; ++k) L[k][i] = ((2 * k - 1) * x * L[k - 1][i] - (k - 1) * L[k - 2][i]) / k;
     }
-    long double* Gm = (long double*)malloc(sizeof(long double) * m3 * (m3 + 1));
-    if (!Gm) return;
-#define G(i, j) Gm[(i) * (m3 + 1) + (j)]
-    long double W[1000];
-    int64_t idx[1000];
+}
+
+/* The Gram matrix Psi^T W Psi of one element (m3 x m3, row stride m3 + 1),
+ * its weights W and node indices. */
+static void element_gram(const oracle_mesh* m, const double* cf, int N, const int* base, long double L[16][16],
+                         long double* Gm, long double* W, int64_t* idx) {
+    const int P = m->P, P1 = P + 1, n3 = P1 * P1 * P1, m3 = P * P * P;
     for (int nn = 0; nn < n3; ++nn) {
         int n0 = nn % P1, n1 = (nn / P1) % P1, n2 = nn / (P1 * P1);
         idx[nn] = (base[0] + n0) + (int64_t)N * ((base[1] + n1) + (int64_t)N * (base[2] + n2));
@@ -782,33 +785,56 @@ static void full_project_element(const oracle_mesh* m, const double* cf, double*
                 int n0 = nn % P1, n1 = (nn / P1) % P1, n2 = nn / (P1 * P1);
                 s += L[q0][n0] * L[q1][n1] * L[q2][n2] * W[nn] * L[r0][n0] * L[r1][n1] * L[r2][n2];
             }
-            G(q, r) = s;
+            Gm[q * (m3 + 1) + r] = s;
         }
+    }
+}
+
+/* Gaussian elimination with partial pivoting of the m3 x m3 part of Gm (row
+ * stride m3 + 1), in place: the multipliers below the diagonal, the row
+ * swaps in piv. */
+static void lu_factor(long double* Gm, int m3, int* piv) {
+#define G(i, j) Gm[(i) * (m3 + 1) + (j)]
+    for (int k = 0; k < m3; ++k) {
+        int p = k;
+        for (int r = k + 1; r < m3; ++r) if (fabsl(G(r, k)) > fabsl(G(p, k))) p = r;
+        piv[k] = p;
+        if (p != k)
+            for (int j = 0; j < m3; ++j) { long double t = G(k, j); G(k, j) = G(p, j); G(p, j) = t; }
+        for (int r = k + 1; r < m3; ++r) {
+            long double f = G(r, k) / G(k, k);
+            G(r, k) = f;
+            for (int j = k + 1; j < m3; ++j) G(r, j) -= f * G(k, j);
+        }
+    }
+#undef G
+}
+
+/* v <- Psi z with (Psi^T W Psi) z = Psi^T W v, through the LU factors. */
+static void lu_project(const oracle_mesh* m, const long double* Gm, const int* piv, const long double* W,
+                       const int64_t* idx, long double L[16][16], double* v) {
+    const int P = m->P, P1 = P + 1, n3 = P1 * P1 * P1, m3 = P * P * P;
+#define G(i, j) Gm[(i) * (m3 + 1) + (j)]
+    long double z[729];
+    for (int q = 0; q < m3; ++q) {
+        int q0 = q % P, q1 = (q / P) % P, q2 = q / (P * P);
         long double c = 0;
         for (int nn = 0; nn < n3; ++nn) {
             int n0 = nn % P1, n1 = (nn / P1) % P1, n2 = nn / (P1 * P1);
             c += L[q0][n0] * L[q1][n1] * L[q2][n2] * W[nn] * v[idx[nn]];
         }
-        G(q, m3) = c;
+        z[q] = c;
     }
     for (int k = 0; k < m3; ++k) {
-        int piv = k;
-        for (int r = k + 1; r < m3; ++r) if (fabsl(G(r, k)) > fabsl(G(piv, k))) piv = r;
-        if (piv != k)
-            for (int j = 0; j <= m3; ++j) { long double t = G(k, j); G(k, j) = G(piv, j); G(piv, j) = t; }
-        for (int r = k + 1; r < m3; ++r) {
-            long double f = G(r, k) / G(k, k);
-            for (int j = k; j <= m3; ++j) G(r, j) -= f * G(k, j);
-        }
+        if (piv[k] != k) { long double t = z[k]; z[k] = z[piv[k]]; z[piv[k]] = t; }
+        for (int r = k + 1; r < m3; ++r) z[r] -= G(r, k) * z[k];
     }
-    long double z[729];
     for (int k = m3 - 1; k >= 0; --k) {
-        long double s = G(k, m3);
+        long double s = z[k];
         for (int j = k + 1; j < m3; ++j) s -= G(k, j) * z[j];
         z[k] = s / G(k, k);
     }
 #undef G
-    free(Gm);
     for (int nn = 0; nn < n3; ++nn) {
         int n0 = nn % P1, n1 = (nn / P1) % P1, n2 = nn / (P1 * P1);
         long double s = 0;
@@ -818,6 +844,81 @@ static void full_project_element(const oracle_mesh* m, const double* cf, double*
         }
         v[idx[nn]] = (double)s;
     }
+}
+
+/* Per projected element (blocks in order, elements e0 fastest): the LU
+ * factors and pivots, the weights and node indices. */
+typedef struct {
+    int nelem;
+    int64_t* first;      /* per block: its first element's index, or -1 */
+    long double* lu;     /* m3 (m3 + 1) per element */
+    int* piv;            /* m3 per element */
+    long double* w;      /* n3 per element */
+    int64_t* idx;        /* n3 per element */
+} proj_cache_t;
+
+/* The sqrt(g)-orthogonal projection onto Q_{P-1} of one element's v:
+ * solve (Psi^T W Psi) z = Psi^T W v, v = Psi z, in long double. */
+static void full_project_element(const oracle_mesh* m, const double* cf, double* v, int N, const int* base) {
+    const int P = m->P, m3 = P * P * P;
+    long double L[16][16];
+    legendre_nodes(m, L);
+    long double* Gm = (long double*)malloc(sizeof(long double) * m3 * (m3 + 1));
+    int* piv = (int*)malloc(sizeof(int) * m3);
+    if (!Gm || !piv) { free(Gm); free(piv); return; }
+    long double W[1000];
+    int64_t idx[1000];
+    element_gram(m, cf, N, base, L, Gm, W, idx);
+    lu_factor(Gm, m3, piv);
+    lu_project(m, Gm, piv, W, idx, L, v);
+    free(Gm);
+    free(piv);
+}
+
+int oracle_full_prepare(oracle_mesh* m) {
+    const int P = m->P, P1 = P + 1, E = m->E, N = E * P1;
+    const int n3 = P1 * P1 * P1, m3 = P * P * P, EE = E * E * E;
+    const int64_t NN = (int64_t)N * N * N;
+    proj_cache_t* c = (proj_cache_t*)calloc(1, sizeof(proj_cache_t));
+    if (!c) return -1;
+    c->first = (int64_t*)malloc(sizeof(int64_t) * m->nblocks);
+    int nel = 0;
+    for (int b = 0; b < m->nblocks; ++b) {
+        c->first[b] = m->elem_slot[b] ? nel : -1;
+        if (m->elem_slot[b]) nel += EE;
+    }
+    c->nelem = nel;
+    c->lu = (long double*)malloc(sizeof(long double) * (size_t)nel * m3 * (m3 + 1) + 1);
+    c->piv = (int*)malloc(sizeof(int) * (size_t)nel * m3 + 1);
+    c->w = (long double*)malloc(sizeof(long double) * (size_t)nel * n3 + 1);
+    c->idx = (int64_t*)malloc(sizeof(int64_t) * (size_t)nel * n3 + 1);
+    if (!c->first || !c->lu || !c->piv || !c->w || !c->idx) {
+        free(c->first); free(c->lu); free(c->piv); free(c->w); free(c->idx); free(c);
+        return -1;
+    }
+    long double L[16][16];
+    legendre_nodes(m, L);
+#pragma omp parallel for schedule(dynamic)
+    for (int b = 0; b < m->nblocks; ++b) {
+        if (c->first[b] < 0) continue;
+        const double* cf = m->coef + (int64_t)b * 10 * NN;
+        for (int e = 0; e < EE; ++e) {
+            const int64_t k = c->first[b] + e;
+            int base[3] = {(e % E) * P1, ((e / E) % E) * P1, (e / (E * E)) * P1};
+            long double* Gm = c->lu + k * m3 * (m3 + 1);
+            element_gram(m, cf, N, base, L, Gm, c->w + k * n3, c->idx + k * n3);
+            lu_factor(Gm, m3, c->piv + k * m3);
+        }
+    }
+    m->cache = c;
+    return 0;
+}
+
+void oracle_full_release(oracle_mesh* m) {
+    proj_cache_t* c = (proj_cache_t*)m->cache;
+    if (!c) return;
+    free(c->first); free(c->lu); free(c->piv); free(c->w); free(c->idx); free(c);
+    m->cache = NULL;
 }
 
 /* The tensor projector on the affine blocks and the element projection on
@@ -832,17 +933,27 @@ static void full_truncate_from(const oracle_mesh* m, const double* orig, double*
     c.NN = NN;
     memcpy(u, orig, sizeof(double) * 2 * NN * m->nblocks);
     truncate_with(&c, u);
+    const proj_cache_t* pc = (const proj_cache_t*)m->cache;
+    const int P = m->P, m3 = P * P * P, n3 = P1 * P1 * P1;
 #pragma omp parallel for schedule(dynamic)
     for (int b = 0; b < m->nblocks; ++b) {
         if (!m->elem_slot[b]) continue;
         double* v = u + (int64_t)b * 2 * NN + NN;
         memcpy(v, orig + (int64_t)b * 2 * NN + NN, sizeof(double) * NN);
         const double* cf = m->coef + (int64_t)b * 10 * NN;
+        long double L[16][16];
+        legendre_nodes(m, L);
         for (int e2 = 0; e2 < E; ++e2)
             for (int e1 = 0; e1 < E; ++e1)
                 for (int e0 = 0; e0 < E; ++e0) {
                     int base[3] = {e0 * P1, e1 * P1, e2 * P1};
-                    full_project_element(m, cf, v, N, base);
+                    if (pc) {
+                        const int64_t k = pc->first[b] + e0 + E * (e1 + E * e2);
+                        lu_project(m, pc->lu + k * m3 * (m3 + 1), pc->piv + k * m3, pc->w + k * n3,
+                                   pc->idx + k * n3, L, v);
+                    } else {
+                        full_project_element(m, cf, v, N, base);
+                    }
                 }
     }
 }

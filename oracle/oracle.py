@@ -30,6 +30,7 @@ class OracleMesh(ctypes.Structure):
         ("elem_slot", ctypes.POINTER(ctypes.c_int32)), ("bnd_x", ctypes.POINTER(ctypes.c_double)),
         ("wave_k", ctypes.c_double * 3), ("wave_phi", ctypes.c_double), ("t", ctypes.c_double),
         ("boundary", ctypes.c_int), ("kappa", ctypes.c_double), ("inv_r", ctypes.c_double),
+        ("cache", ctypes.c_void_p),
     ]
 
 
@@ -53,6 +54,9 @@ def lib():
         L.oracle_rhs_full.argtypes = [mp, vp, vp]
         L.oracle_truncate_full2.argtypes = [mp, vp]
         L.oracle_rk4_full.argtypes = [mp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int]
+        L.oracle_full_prepare.argtypes = [mp]
+        L.oracle_full_release.argtypes = [mp]
+        L.oracle_full_release.restype = None
         L.oracle_energy_full.argtypes = [mp, vp, dp]
         L.oracle_norm_full.argtypes = [mp, vp, vp, ctypes.c_int, ctypes.c_int, dp]
         _lib = L
@@ -228,6 +232,14 @@ class BallOracle(Oracle):
         for k in ("face_nb", "face_code", "elem_slot"):
             setattr(m, k, a[k].ctypes.data_as(ip))
         self.mesh = m
+        # factor every projected element's Gram matrix once (long double LU)
+        if lib().oracle_full_prepare(ctypes.byref(m)):
+            raise MemoryError("oracle_full_prepare failed")
+
+    def __del__(self):
+        m = getattr(self, "mesh", None)
+        if m is not None and m.cache:
+            lib().oracle_full_release(ctypes.byref(m))
 
     def rhs(self, u, t=0.0):
         u = self._vec(u)

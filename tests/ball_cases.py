@@ -1,17 +1,22 @@
-"""The seven-patch ball run on the oracle (test infrastructure)."""
+"""The seven- and thirteen-patch balls run on the oracle (test infrastructure)."""
 import math
 
 import numpy as np
 
 from oracle.oracle import BallOracle
-from twoldg.ball import PlaneWave, ball_tables, node_logical, sevenpatch_forest
+from twoldg.ball import PlaneWave, ball_forest, ball_tables, node_logical, sevenpatch_forest
 
 
-def ball_setup(P, E, roots, truncate=True, k=(1.1, -0.7, 0.5), phi=0.3):
-    forest, geo = sevenpatch_forest(np.float64, P, E, roots=roots)
+def ball_setup(P, E, roots, truncate=True, k=(1.1, -0.7, 0.5), phi=0.3, Rm=None, radiative=None, Lc=1.0, R1=3.0):
+    """A ball (the thirteen-patch one with Rm), its tables and its oracle;
+    radiative = (kappa, inverse_r) replaces the Dirichlet wave."""
+    forest, geo = ball_forest(np.float64, P, E, roots, Lc, R1, Rm=Rm)
     wave = PlaneWave(k, phi)
     tables = ball_tables(forest, P, wave)
-    o = BallOracle(forest, P, tables, wave, truncate=truncate)
+    rad = None
+    if radiative is not None:
+        rad = (radiative[0], 1.0 / geo.outer_radius() if radiative[1] else 0.0)
+    o = BallOracle(forest, P, tables, wave, truncate=truncate, radiative=rad)
     return forest, geo, wave, tables, o
 
 
@@ -34,8 +39,8 @@ def ball_state(forest, tables, f):
     return u.reshape(-1)
 
 
-def oracle_sevenpatch_errors(P, E, roots, cfl=0.5, tend=1.0, truncate=True):
-    forest, geo, wave, tables, o = ball_setup(P, E, roots, truncate)
+def oracle_sevenpatch_errors(P, E, roots, cfl=0.5, tend=1.0, truncate=True, Rm=None):
+    forest, geo, wave, tables, o = ball_setup(P, E, roots, truncate, Rm=Rm)
     u0 = ball_state(forest, tables, lambda x, v: wave.state(x, 0.0, v))
     if truncate:
         u0 = o.truncate(u0)
@@ -45,3 +50,20 @@ def oracle_sevenpatch_errors(P, E, roots, cfl=0.5, tend=1.0, truncate=True):
     ue = ball_state(forest, tables, lambda x, v: wave.state(x, tend, v))
     return dict(u=o.norm(u, 2, 1, ue), v=o.norm(u, 2, 2, ue), l2=o.norm(u, 2, 3, ue), nsteps=nsteps,
                 energy0=o.energy(u0, 0.0), energy=o.energy(u, tend))
+
+
+def oracle_radiative_errors(P, E, roots, kappa=1.0, inverse_r=True, w=0.5, cfl=0.5, tend=2.0, truncate=True,
+                            Rm=None):
+    """radiative_errors on the oracle: the outgoing pulse of width w under a
+    radiative sphere; L2 errors and the energies (the boundary's term included)."""
+    from twoldg.ball import OutgoingPulse
+    forest, geo, wave, tables, o = ball_setup(P, E, roots, truncate, Rm=Rm, radiative=(kappa, inverse_r))
+    pulse = OutgoingPulse(w)
+    u0 = ball_state(forest, tables, lambda x, v: pulse.state(x, 0.0, v))
+    if truncate:
+        u0 = o.truncate(u0)
+    nsteps = int(math.ceil(tend / (cfl * tables["hspeed"] / (P + 1))))
+    dt = tend / nsteps
+    u = o.rk4(u0, dt, nsteps, 0.0)
+    ue = ball_state(forest, tables, lambda x, v: pulse.state(x, tend, v))
+    return dict(l2=o.norm(u, 2, 3, ue), nsteps=nsteps, energy0=o.energy(u0, 0.0), energy=o.energy(u, tend))
