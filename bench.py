@@ -53,11 +53,13 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner (untimed, before the warm-up) and run the default launch layouts")
-    ap.add_argument("--workload", default="box256", choices=["box256", "nested", "c1", "ball"],
+    ap.add_argument("--workload", default="box256", choices=["box256", "nested", "c1", "ball", "ball13"],
                     help="box256: the 256^3 periodic box (the headline); nested: the 3D reflecting box with "
                          "three nested refinement levels (P=3, E=2, roots=8) and a Gaussian pulse; c1: the 2D "
                          "periodic P=4, E=2, roots=8 box to a quarter period at CFL 0.25; ball: the seven-patch "
-                         "ball, P=3, E=2, roots=(4,4), plane wave with Dirichlet sphere, to t=6")
+                         "ball, P=3, E=2, roots=(4,4), plane wave with Dirichlet sphere, to t=6; ball13: the "
+                         "reference's benchmark ball, thirteen patches, roots (4,4,44), E=4, P=3, Lc=4, Rm=12, "
+                         "R1=100, radiative sphere (19.1M nodes)")
     return ap.parse_args()
 
 
@@ -346,6 +348,61 @@ def small_config(args, twoldg, torch):
     print(json.dumps(line))
 
 
+def ball_benchmark(args, twoldg, torch):
+    """The reference's benchmark ball (bin/ball_benchmark.jl): the
+    thirteen-patch ball of 4672 blocks of 16^3 (roots (4, 4, 44), Lc = 4,
+    Rm = 12, R1 = 100), P = 3, Sommerfeld's radiative sphere, truncation on,
+    the state sin(1), sin(2), ... truncated; K RK4 steps at cfl 1/2 timed with
+    CUDA events on the library's stream, FP64 and FP32 + compensated, and the
+    FP32 run's L2 distance from the FP64 one after the warm-up and timed steps."""
+    lib = twoldg._lib.lib()
+    forest, geo = twoldg.thirteenpatch_forest(np.float64, 3, 4, roots=(4, 4, 44), Lc=4.0, Rm=12.0, R1=100.0)
+    arms, final = {}, {}
+    for prec in ("f64", "f32c"):
+        T = np.float64 if prec == "f64" else np.float32
+        p = twoldg.WaveProblem(forest, twoldg.Element(T, 3), geometry=geo, boundary=twoldg.RadiativeBoundary(),
+                               precision=prec)
+        u = torch.from_numpy(np.sin(np.arange(1, p.state_words + 1, dtype=np.float64)).astype(T)).cuda()
+        twoldg.truncate_state(u, p)
+        dt = float(twoldg.oldg_timestep(p, 0.5))
+        ptr = ctypes.c_void_p(u.data_ptr())
+        stream = torch.cuda.ExternalStream(lib.twoldg_stream(p.handle))
+        torch.cuda.synchronize()
+        twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ptr, 0.0, dt, args.warmup))
+        p.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with Clocks(0) as clk:
+            ev0.record(stream)
+            twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ptr, args.warmup * dt, dt, args.steps))
+            ev1.record(stream)
+            ev1.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        nodes = p.state_words // 2
+        st = (ctypes.c_float * 4)()
+        v = u.clone()
+        twoldg._lib.check(lib.twoldg_profile_step(p.handle, ctypes.c_void_p(v.data_ptr()), dt, st))
+        arms[prec] = {"value": nodes * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                      "ns_per_node_step": ms * 1e6 / args.steps / nodes, "stage_ms": [float(x) for x in st],
+                      "nodes": nodes, "dt": dt, "clocks": clk.summary()}
+        final[prec] = (p, u)
+        if prec == "f32c":
+            p32, u32 = p, u
+    r = final["f64"][1].to(torch.float32)
+    arms["f32c"]["l2_vs_fp64"] = float(twoldg.quadrature_norm(p32, u32, 2, ref=r))
+    head = arms["f32c"]
+    line = {"metric": METRIC, "value": head["value"], "unit": "node-steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "the benchmark ball: thirteen-patch, roots (4,4,44), E=4, P=3, Lc=4, Rm=12, "
+                                   "R1=100 (4672 blocks of 16^3, %d nodes), Sommerfeld radiative sphere, "
+                                   "truncation on, state sin(1..n) truncated, cfl 1/2" % head["nodes"],
+                       "precision": "f32c", "l2_flush": "inputs larger than L2"},
+            "fp64": arms["f64"], "f32c": arms["f32c"], "speedup_vs_fp64": head["value"] / arms["f64"]["value"],
+            "reference_h200_ns_per_node_step": {"f64": 2.84, "f32": 1.92, "source": "CODE.md:5108-5122"},
+            "clocks": head["clocks"], "roofline": None, "gpu_launches": 1 + 9 * args.steps}
+    print(json.dumps(line))
+
+
 # --- multi-rank plumbing (replicas) -------------------------------------------
 _dist = None
 
@@ -455,6 +512,9 @@ def main():
     twoldg.build()
     if WORKLOAD in ("c1", "ball"):
         small_config(args, twoldg, torch)
+        return
+    if WORKLOAD == "ball13":
+        ball_benchmark(args, twoldg, torch)
         return
     arms = {}
     wanted = args.arms.split(",")

@@ -184,8 +184,15 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP>::NT, Stage3R<T, P, E, C
             for (int q = 0; q < P1; ++q) {
                 const int n = tid + F * (ez * P1 + q);
                 y[q] = yv[n];
-                uu[q] = un[n];
-                uv[q] = un[NN + n];
+                if (mode == MODE_STAGE1) {
+                    // the stage input is u^n: its u is the column in shared
+                    // memory, its v the value just loaded
+                    uu[q] = su[s2 + SXY * (ez * P1 + q)];
+                    uv[q] = y[q];
+                } else {
+                    uu[q] = un[n];
+                    uv[q] = un[NN + n];
+                }
                 if (mode != 1) {
                     au[q] = acc[n];
                     av[q] = acc[NN + n];

@@ -488,6 +488,9 @@ def ball_tables(forest, P, wave=None):
     the boundary face nodes' positions per slot (3, N^2); and the time step's
     spacing over speed."""
     from .element import Element
+    cache = forest.__dict__.setdefault("_tables", {})
+    if P in cache:
+        return cache[P]
     geo, N = forest.geo, forest.N
     el = Element(np.float64, P)
     P1 = P + 1
@@ -550,6 +553,7 @@ def ball_tables(forest, P, wave=None):
     out = dict(coef=np.ascontiguousarray(coef.reshape(-1)), elem_slot=slot, elem_w=ew, elem_chol=echol,
                ntab=len(ws), bnd_x=np.ascontiguousarray(bnd.reshape(-1)), hspeed=hspeed, xl=xl)
     out.update(fac)
+    cache[P] = out       # one forest, one set of tables: problems of any precision share them
     return out
 
 
