@@ -203,6 +203,21 @@ int twoldg_mode_amplitude(twoldg_problem* p, const void* u, int32_t var, int32_t
  * without the graph, with CUDA events between the four stages, and returns
  * each stage's duration in milliseconds (stage_ms[4]). Synchronous. */
 int twoldg_profile_step(twoldg_problem* p, void* u, double dt, float* stage_ms);
+/* The regrid transfer (TreeAMR's element-set regrid, which the reference's
+ * regrid! / adaptive_blast run on the host: src/blast.jl, CODE.md "Adaptive
+ * refinement"): the state u_from of the flat forest `from` moved onto the
+ * forest `to`, which shares dim, order, elems, precision, roots and extents
+ * and differs from it by at most one level per block. A block of `to` that
+ * is a leaf of `from` is copied; a child of a `from` leaf gets the parent
+ * element's polynomial at its nodes (the prolongation I in every
+ * dimension); the parent of 2^D `from` leaves gets their L2 projection in
+ * the Gauss-Lobatto inner product (R = M_c^-1 I^T M_f in every dimension).
+ * Both keep sum w u of each variable; coarsening brings back v's top modes,
+ * so a truncated scheme truncates after it. u_from and u_to are device
+ * buffers in the two forests' state layouts; stream is a cudaStream_t or
+ * NULL. Synchronous. */
+int twoldg_transfer(const twoldg_desc* from, const void* u_from, const twoldg_desc* to, void* u_to, void* stream);
+
 /* The autotuner (no reference counterpart: the reference launches its
  * kernels with a fixed workgroup size). For every (dim, P, E) group of the
  * problem it times the stage kernel's launch layouts -- which kernel (the

@@ -274,3 +274,89 @@ class BallOracle(Oracle):
         lib().oracle_norm_full(ctypes.byref(self.mesh), u.ctypes.data, None if r is None else r.ctypes.data,
                                int(p), int(vars_mask), ctypes.byref(out))
         return out.value
+
+
+# --- the regrid transfer, restated (test infrastructure) ----------------------
+def transfer_operators(P):
+    """The 1D prolongation I (2(P+1) x (P+1): the coarse element's Lagrange
+    polynomial at the nodes of its two halves) and the L2 restriction
+    R = M_c^-1 I^T M_f in the Gauss-Lobatto inner product ((P+1) x 2(P+1)),
+    evaluated here from the golden nodes and weights in long double."""
+    t = golden_tables(P)
+    x = np.array(t["nodes"], dtype=np.longdouble)
+    w = np.array(t["weights"], dtype=np.longdouble)
+    P1 = P + 1
+    I = np.zeros((2 * P1, P1), dtype=np.longdouble)
+    for h in range(2):
+        for i in range(P1):
+            xf = (x[i] + 2 * h - 1) / 2
+            for j in range(P1):
+                lj = np.longdouble(1)
+                for m in range(P1):
+                    if m != j:
+                        lj *= (xf - x[m]) / (x[j] - x[m])
+                I[h * P1 + i, j] = lj
+    wf = np.concatenate([w / 2, w / 2])
+    R = (I * wf[:, None]).T / w[:, None]
+    return I.astype(np.float64), R.astype(np.float64)
+
+
+def _along(A, op, d, D):
+    """Apply a matrix along dimension d of a block array (axis D-1-d)."""
+    ax = D - 1 - d
+    return np.moveaxis(np.tensordot(op, A, axes=([1], [ax])), 0, ax)
+
+
+def oracle_transfer(old_leaves, u_old, new_leaves, D, P, E):
+    """The state on leaves `old_leaves` ((level, corner) per block, the state
+    layout's order) moved onto `new_leaves`: copy, refine by I, coarsen by R,
+    dimension by dimension."""
+    P1, N = P + 1, E * (P + 1)
+    NN = N ** D
+    I, R = transfer_operators(P)
+    half = E // 2
+    index = {k: b for b, k in enumerate(old_leaves)}
+    u_old = np.asarray(u_old, dtype=np.float64).reshape(len(old_leaves), 2, *([N] * D))
+    out = np.empty((len(new_leaves), 2) + (N,) * D)
+    # refine: fine node i of the half s takes row (ef % 2) P1 + i % P1 of I over coarse element s E/2 + ef/2
+    up = []
+    for s in range(2):
+        op = np.zeros((N, N))
+        for i in range(N):
+            ef = i // P1
+            ec = s * half + ef // 2
+            op[i, ec * P1:(ec + 1) * P1] = I[(ef % 2) * P1 + i % P1]
+        up.append(op)
+    # coarsen: coarse node i of element ec reads R's row over the two fine
+    # elements 2 (ec % (E/2)) and the next of the child half ec // (E/2)
+    down = np.zeros((N, 2 * N))
+    for i in range(N):
+        ec = i // P1
+        h = ec // half
+        f0 = h * N + 2 * (ec % half) * P1
+        down[i, f0:f0 + 2 * P1] = R[i % P1]
+    for b, (lv, c) in enumerate(new_leaves):
+        if (lv, c) in index:
+            out[b] = u_old[index[(lv, c)]]
+            continue
+        parent = (lv - 1, tuple(x >> 1 for x in c))
+        if lv > 0 and parent in index:
+            A = u_old[index[parent]]
+            for var in range(2):
+                X = A[var]
+                for d in range(D):
+                    X = _along(X, up[c[d] & 1], d, D)
+                out[b, var] = X
+            continue
+        kids = {}
+        for q in np.ndindex(*([2] * D)):
+            kids[q] = index[(lv + 1, tuple(2 * c[d] + q[d] for d in range(D)))]
+        for var in range(2):
+            big = np.empty((2 * N,) * D)
+            for q, kb in kids.items():
+                sl = tuple(slice(q[D - 1 - ax] * N, (q[D - 1 - ax] + 1) * N) for ax in range(D))
+                big[sl] = u_old[kb, var]
+            for d in range(D):
+                big = _along(big, down, d, D)
+            out[b, var] = big
+    return out.reshape(-1)

@@ -958,6 +958,89 @@ int twoldg_synchronize(twoldg_problem* p) {
     return TWOLDG_OK;
 }
 
+int twoldg_transfer(const twoldg_desc* from, const void* u_from, const twoldg_desc* to, void* u_to, void* stream) {
+    if (!from || !to || !u_from || !u_to) return fail(TWOLDG_EINVAL, "NULL argument");
+    if (from->dim != to->dim || from->order != to->order || from->elems != to->elems ||
+        from->precision != to->precision)
+        return fail(TWOLDG_EINVAL, "the two forests must share dim, order, elems and precision");
+    const int D = from->dim, P = from->order, E = from->elems;
+    if (D < 1 || D > 3) return fail(TWOLDG_EINVAL, "dim must be 1, 2 or 3");
+    if (E < 2 || E % 2) return fail(TWOLDG_EINVAL, "E must be even: a child block covers half its parent's elements");
+    for (int k = 0; k < D; ++k)
+        if (from->roots[k] != to->roots[k] || from->lo[k] != to->lo[k] || from->hi[k] != to->hi[k])
+            return fail(TWOLDG_EINVAL, "the two forests must share roots and extents");
+    if (from->coef || to->coef || from->face_nb || to->face_nb)
+        return fail(TWOLDG_EUNSUP, "the transfer moves the state of flat brick forests");
+    if (!tables().get(P)) return fail(TWOLDG_EUNSUP, "no kernels for P = " + std::to_string(P) + " (built: 1..6)");
+    const int prec = from->precision;
+    const int64_t N = (int64_t)E * (P + 1);
+    int64_t NN = 1;
+    for (int k = 0; k < D; ++k) NN *= N;
+    // the old leaves by (level, corner)
+    std::map<std::vector<int64_t>, int> old;
+    for (int b = 0; b < from->nblocks; ++b) {
+        std::vector<int64_t> key(1 + D);
+        key[0] = from->level[b];
+        for (int k = 0; k < D; ++k) key[1 + k] = from->corner[(int64_t)b * D + k];
+        old[key] = b;
+    }
+    std::vector<TransferItem> items(to->nblocks);
+    for (int b = 0; b < to->nblocks; ++b) {
+        TransferItem& it = items[b];
+        it.dst = (int64_t)b * 2 * NN;
+        std::vector<int64_t> key(1 + D);
+        key[0] = to->level[b];
+        for (int k = 0; k < D; ++k) key[1 + k] = to->corner[(int64_t)b * D + k];
+        auto same = old.find(key);
+        if (same != old.end()) {
+            it.mode = 0;
+            it.src[0] = (int64_t)same->second * 2 * NN;
+            continue;
+        }
+        if (key[0] > 0) {
+            std::vector<int64_t> pk(key);
+            pk[0] -= 1;
+            int sub = 0;
+            for (int k = 0; k < D; ++k) {
+                sub |= (int)(key[1 + k] & 1) << k;
+                pk[1 + k] = key[1 + k] >> 1;
+            }
+            auto par = old.find(pk);
+            if (par != old.end()) {
+                it.mode = 1;
+                it.sub = sub;
+                it.src[0] = (int64_t)par->second * 2 * NN;
+                continue;
+            }
+        }
+        bool all = true;
+        for (int q = 0; q < (1 << D) && all; ++q) {
+            std::vector<int64_t> ck(key);
+            ck[0] += 1;
+            for (int k = 0; k < D; ++k) ck[1 + k] = 2 * key[1 + k] + ((q >> k) & 1);
+            auto ch = old.find(ck);
+            if (ch == old.end()) all = false;
+            else it.src[q] = (int64_t)ch->second * 2 * NN;
+        }
+        if (!all)
+            return fail(TWOLDG_EINVAL, "block " + std::to_string(b) + " of the new forest is neither a leaf of the old "
+                                       "one, nor a child of one, nor the parent of 2^D of them");
+        it.mode = 2;
+    }
+    std::unique_ptr<Ops> ops;
+    if (D == 1) ops.reset(make_ops_d1(prec, P, tables().t64[P], tables().t32[P]));
+    if (D == 2) ops.reset(make_ops_d2(prec, P, tables().t64[P], tables().t32[P]));
+    if (D == 3) ops.reset(make_ops_d3(prec, P, tables().t64[P], tables().t32[P]));
+    if (!ops) return fail(TWOLDG_EINVAL, "precision must be TWOLDG_F64, TWOLDG_F32 or TWOLDG_F32C");
+    cudaStream_t st = (cudaStream_t)stream;
+    DevBuf d_items;
+    CK(d_items.alloc(items.size() * sizeof(TransferItem)));
+    CK(cudaMemcpyAsync(d_items.p, items.data(), items.size() * sizeof(TransferItem), cudaMemcpyHostToDevice, st));
+    CK(ops->transfer((const TransferItem*)d_items.p, (int)items.size(), E, u_from, u_to, st));
+    CK(cudaStreamSynchronize(st));
+    return TWOLDG_OK;
+}
+
 int twoldg_batch_create(int32_t n, const twoldg_desc* descs, twoldg_batch** out) {
     if (!out) return fail(TWOLDG_EINVAL, "out must not be NULL");
     *out = nullptr;

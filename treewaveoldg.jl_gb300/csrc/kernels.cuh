@@ -327,6 +327,88 @@ __global__ void cf_ghost_g_kernel(const CfFace* cf, int ncf, int E, const T* gfd
 }
 
 // ---------------------------------------------------------------------------
+// The regrid transfer (TreeAMR's element-set regrid, which the reference's
+// regrid! runs on the host): one CTA per new block, both variables, by
+// direct tensor sums of the 1D operators. Refining evaluates the coarse
+// element's polynomial at the fine nodes (I along every dimension);
+// coarsening is the L2 projection in the Gauss-Lobatto inner product (R =
+// M_c^-1 I^T M_f along every dimension). Both keep sum w u.
+template <typename T, int D, int P>
+__global__ void __launch_bounds__(256) transfer_kernel(const TransferItem* items, int nitems, int E, const T* src,
+                                                       T* dst, CfTab<T, P> ct) {
+    constexpr int P1 = P + 1;
+    const int N = E * P1, halfE = E / 2;
+    int NN = 1;
+    for (int k = 0; k < D; ++k) NN *= N;
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const TransferItem it = items[item];
+        for (int i = threadIdx.x; i < 2 * NN; i += blockDim.x) {
+            const int var = i / NN, n = i % NN;
+            int x[3] = {0, 0, 0};
+            {
+                int r = n;
+                for (int k = 0; k < D; ++k) { x[k] = r % N; r /= N; }
+            }
+            T out;
+            if (it.mode == 0) {
+                out = src[it.src[0] + i];
+            } else if (it.mode == 1) {
+                // the child's node x: fine element ef = x / P1 of the half `sub` of the
+                // parent, row (ef & 1) P1 + x % P1 of I over the parent element's nodes
+                int row[3] = {0, 0, 0}, cb[3] = {0, 0, 0};
+                for (int k = 0; k < D; ++k) {
+                    const int ef = x[k] / P1;
+                    row[k] = (ef & 1) * P1 + x[k] % P1;
+                    cb[k] = (((it.sub >> k) & 1) * halfE + ef / 2) * P1;
+                }
+                const T* s = src + it.src[0] + (int64_t)var * NN;
+                T acc = T(0);
+                const int J1 = D > 1 ? P1 : 1, J2 = D > 2 ? P1 : 1;
+                for (int j2 = 0; j2 < J2; ++j2)
+                    for (int j1 = 0; j1 < J1; ++j1) {
+                        T w12 = T(1);
+                        if (D > 1) w12 *= ct.I[row[1]][j1];
+                        if (D > 2) w12 *= ct.I[row[2]][j2];
+                        const int64_t base = (cb[0]) + (int64_t)N * ((cb[1] + j1) + (int64_t)N * (cb[2] + j2));
+                        T a = T(0);
+#pragma unroll
+                        for (int j0 = 0; j0 < P1; ++j0) a += ct.I[row[0]][j0] * s[base + j0];
+                        acc += w12 * a;
+                    }
+                out = acc;
+            } else {
+                // the coarse node x: element ec = x / P1 in the half h = ec / (E/2) of
+                // the block, covered by the child of those halves, whose fine elements
+                // 2 (ec % (E/2)) and the next carry R's 2 P1 columns
+                int row[3] = {0, 0, 0}, fb[3] = {0, 0, 0}, child = 0;
+                for (int k = 0; k < D; ++k) {
+                    const int ec = x[k] / P1;
+                    row[k] = x[k] % P1;
+                    child |= (ec / halfE) << k;
+                    fb[k] = 2 * (ec % halfE) * P1;
+                }
+                const T* s = src + it.src[child] + (int64_t)var * NN;
+                T acc = T(0);
+                const int J1 = D > 1 ? 2 * P1 : 1, J2 = D > 2 ? 2 * P1 : 1;
+                for (int j2 = 0; j2 < J2; ++j2)
+                    for (int j1 = 0; j1 < J1; ++j1) {
+                        T w12 = T(1);
+                        if (D > 1) w12 *= ct.R[row[1]][j1];
+                        if (D > 2) w12 *= ct.R[row[2]][j2];
+                        const int64_t base = fb[0] + (int64_t)N * ((fb[1] + j1) + (int64_t)N * (fb[2] + j2));
+                        T a = T(0);
+#pragma unroll
+                        for (int j0 = 0; j0 < 2 * P1; ++j0) a += ct.R[row[0]][j0] * s[base + j0];
+                        acc += w12 * a;
+                    }
+                out = acc;
+            }
+            dst[it.dst + i] = out;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Block tiles. A block's u with its face ghosts lives in shared memory in a
 // padded layout with an odd x pitch (N+3), so that element lines along x,
 // which consecutive threads take at consecutive y, hit distinct banks; the

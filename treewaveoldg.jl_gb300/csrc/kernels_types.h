@@ -25,4 +25,14 @@ struct CfFace {
     double h;           // spacing of the block owning `slot`
 };
 
+// One block of a regrid transfer: the new block at dst (words), from the old
+// leaf src[0] (copy), from its parent src[0] as child `sub` (bit d: the
+// upper half along d; refine), or from its 2^D children src[bits] (coarsen).
+struct TransferItem {
+    int64_t dst;
+    int64_t src[8];
+    int32_t mode;       // 0 copy, 1 refine, 2 coarsen
+    int32_t sub;
+};
+
 }  // namespace twoldg

@@ -88,6 +88,9 @@ public:
     virtual int launch_candidates(int E, bool flat, Launch* out, int max) const = 0;
     virtual cudaError_t export_faces(const BlockItem* items, int nitems, int E, const void* u, void* fu,
                                      void* fog, cudaStream_t s) const = 0;
+    // the regrid transfer of both variables, one new block per item
+    virtual cudaError_t transfer(const TransferItem* items, int nitems, int E, const void* src, void* dst,
+                                 cudaStream_t s) const = 0;
     virtual cudaError_t cf_ghosts(const CfFace* cf, int ncf, int E, const void* fu, const void* fog, void* ugd,
                                   void* gfd, void* ggd, cudaStream_t s) const = 0;
     virtual cudaError_t stage(const BlockItem* items, int nitems, int E, int mode, int truncate,

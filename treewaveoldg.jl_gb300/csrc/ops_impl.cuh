@@ -201,6 +201,14 @@ public:
         return cudaGetLastError();
     }
 
+    cudaError_t transfer(const TransferItem* items, int nitems, int E, const void* src, void* dst,
+                         cudaStream_t s) const override {
+        if (nitems == 0) return cudaSuccess;
+        transfer_kernel<T, D, P><<<std::min(nitems, kMaxGrid), 256, 0, s>>>(items, nitems, E, (const T*)src,
+                                                                          (T*)dst, ct_);
+        return cudaGetLastError();
+    }
+
     cudaError_t cf_ghosts(const CfFace* cf, int ncf, int E, const void* fu, const void* fog, void* ugd, void* gfd,
                           void* ggd, cudaStream_t s) const override {
         if (ncf == 0) return cudaSuccess;
