@@ -47,8 +47,8 @@ public:
         cudaFuncSetAttribute(stage_kernel_c<T, D, P, 2, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         cudaFuncSetAttribute(stage_kernel_c<T, D, P, 4, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
         if constexpr (D == 3) {
-            set_attrs(stage3r_kernel<T, P, 2, COMP>);
-            set_attrs(stage3r_kernel<T, P, 4, COMP>);
+            set_attrs3r<2>();
+            set_attrs3r<4>();
             set_attrs(fm_gradient_kernel<T, P>);
             set_attrs(fm_stage_kernel<T, P, COMP>);
             set_attrs(fm_truncate_kernel<T, P>);
@@ -253,16 +253,8 @@ public:
         const bool aligned = (al & 15) == 0;
         const int k = resolve(launch_.kernel, E, !p.coef, aligned);
         if constexpr (D == 3) {
-            if (k == 1 && E == 2) {
-                using S = Stage3R<T, P, 2, COMP>;
-                stage3r_kernel<T, P, 2, COMP><<<grid, S::NT, S::words * sizeof(T), s>>>(a, tb_);
-                return cudaGetLastError();
-            }
-            if (k == 1 && E == 4) {
-                using S = Stage3R<T, P, 4, COMP>;
-                stage3r_kernel<T, P, 4, COMP><<<grid, S::NT, S::words * sizeof(T), s>>>(a, tb_);
-                return cudaGetLastError();
-            }
+            if (k == 1 && E == 2) return launch3r<2>(a, grid, mode, s);
+            if (k == 1 && E == 4) return launch3r<4>(a, grid, mode, s);
         }
         if (k == 2 && E == 2) {
             stage_kernel_c<T, D, P, 2, COMP><<<grid, StageLaunch<T, D, P, 2>::NT, smem, s>>>(a, tb_);
@@ -272,6 +264,42 @@ public:
             stage_kernel<T, D, P, COMP><<<grid, run_threads(3, E), smem, s>>>(a, tb_);
         }
         return cudaGetLastError();
+    }
+
+    // The register-line kernel: stage 4 of the compensated path with the
+    // compensation array, stage 1 in the lean variant where that fits one more
+    // CTA per SM, every other stage without the compensation array.
+    template <int E>
+    cudaError_t launch3r(const StageArgs<T>& a, int grid, int mode, cudaStream_t s) const {
+        if constexpr (D == 3) {
+            using SL = Stage3R<T, P, E, false, true>;
+            using S0 = Stage3R<T, P, E, false>;
+            using SC = Stage3R<T, P, E, true>;
+            if constexpr (COMP) {
+                if (mode == MODE_STAGE4) {
+                    stage3r_kernel<T, P, E, true><<<grid, SC::NT, SC::words * sizeof(T), s>>>(a, tb_);
+                    return cudaGetLastError();
+                }
+            }
+            if constexpr (SL::MINB > S0::MINB) {
+                if (mode == MODE_STAGE1)
+                    stage3r_kernel<T, P, E, false, true><<<grid, SL::NT, SL::words * sizeof(T), s>>>(a, tb_);
+                else
+                    stage3r_kernel<T, P, E, false><<<grid, S0::NT, S0::words * sizeof(T), s>>>(a, tb_);
+            } else {
+                stage3r_kernel<T, P, E, false><<<grid, S0::NT, S0::words * sizeof(T), s>>>(a, tb_);
+            }
+        }
+        return cudaGetLastError();
+    }
+    template <int E>
+    void set_attrs3r() {
+        if constexpr (D == 3) {
+            if constexpr (COMP) set_attrs(stage3r_kernel<T, P, E, true>);
+            set_attrs(stage3r_kernel<T, P, E, false>);
+            if constexpr (Stage3R<T, P, E, false, true>::MINB > Stage3R<T, P, E, false>::MINB)
+                set_attrs(stage3r_kernel<T, P, E, false, true>);
+        }
     }
 
     cudaError_t energy(const BlockItem* items, int nitems, int E, const StagePtrs& p,

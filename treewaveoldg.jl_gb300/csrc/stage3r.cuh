@@ -20,22 +20,56 @@
 
 namespace twoldg {
 
-template <typename T, int P, int E, bool COMP>
+// A pitch of at least `lo` words that keeps 16-byte shared accesses
+// conflict-free when consecutive threads step by it: a multiple of the
+// vector width whose byte offset, in 4-byte banks modulo 32, is 4, 12, 20 or
+// 28 (the eight threads of a 16-byte phase then take disjoint bank quads).
+template <typename T>
+constexpr int vec_pitch(int lo) {
+    constexpr int VW = 16 / sizeof(T);
+    for (int x = lo;; ++x) {
+        if (x % VW) continue;
+        const int b = (int)((x * sizeof(T) / 4) % 32);
+        if (b == 4 || b == 12 || b == 20 || b == 28) return x;
+    }
+}
+
+// A plane stride of at least `lo` words, a multiple of the vector width,
+// whose byte offset is 64 modulo 128: the two 16-thread rows of a warp that
+// walk along a plane then fall in opposite halves of the banks.
+template <typename T>
+constexpr int half_bank_stride(int lo) {
+    constexpr int VW = 16 / sizeof(T);
+    for (int x = lo;; ++x)
+        if (x % VW == 0 && (x * sizeof(T)) % 128 == 64) return x;
+}
+
+template <typename T, int P, int E, bool COMP, bool LEAN = false>
 struct Stage3R {
     static constexpr int P1 = P + 1;
     static constexpr int N = E * P1;
     static constexpr int F = N * N;
     static constexpr int NN = N * F;
-    static constexpr int SX = N + 3, SY = N + 2, SXY = SX * SY;  // padded u
-    static constexpr int SS = SXY * SY;
-    static constexpr int LX = N + 1, LXY = LX * N;               // ghost-free accumulator / v
+    static constexpr int VW = 16 / sizeof(T);
+    // padded u: x pitch SX (the two x ghosts and 16-byte rows), y pitch SXY
+    // over N + 2 rows (the two y ghosts); z planes 0 .. N-1 only, since the
+    // z ghosts stay in registers
+    static constexpr int SX = vec_pitch<T>(N + 3), SY = N + 2;
+    static constexpr int SXY = half_bank_stride<T>(SX * SY);
+    static constexpr int SS = SXY * N;
+    // ghost-free accumulator / new v: x pitch LX, plane stride LXY
+    static constexpr int LX = vec_pitch<T>(N), LXY = half_bank_stride<T>(LX * N);
     static constexpr int LS = LXY * N;
     static constexpr int NT = F;
     // u, the accumulator / new v, and (compensated) the compensation of v
     static constexpr size_t words = (size_t)SS + (size_t)LS + (COMP ? (size_t)LS : 0);
     static constexpr size_t bytes = words * sizeof(T) + 1024;
     static constexpr int by_smem = (int)((227 * 1024) / bytes);
-    static constexpr int by_regs = 65536 / (NT * 80) > 0 ? 65536 / (NT * 80) : 1;
+    // registers a thread may use: 80, or 64 in the lean variant that stage 1
+    // runs where that lets one more CTA onto an SM (stage 1 moves the least
+    // data and waits the longest; the others run best at 80)
+    static constexpr int REGS = LEAN ? 64 : 80;
+    static constexpr int by_regs = 65536 / (NT * REGS) > 0 ? 65536 / (NT * REGS) : 1;
     static constexpr int MINB = by_smem < 1 ? 1 : (by_smem < by_regs ? by_smem : by_regs);
     static constexpr bool usable = F >= 64 && F <= 1024 && F % 32 == 0;
 };
@@ -70,11 +104,11 @@ __device__ __forceinline__ T grad_ghost(const Tab<T, P>& tb, uint32_t flags, int
     return (flags & (1u << (8 + f))) ? -gnb : gnb;
 }
 
-template <typename T, int P, int E, bool COMP>
-__global__ void __launch_bounds__(Stage3R<T, P, E, COMP>::NT, Stage3R<T, P, E, COMP>::MINB)
+template <typename T, int P, int E, bool COMP, bool LEAN = false>
+__global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P, E, COMP, LEAN>::MINB)
     stage3r_kernel(StageArgs<T> a, Tab<T, P> tb) {
-    using S = Stage3R<T, P, E, COMP>;
-    constexpr int P1 = S::P1, N = S::N, F = S::F, NN = S::NN;
+    using S = Stage3R<T, P, E, COMP, LEAN>;
+    constexpr int P1 = S::P1, N = S::N, F = S::F, NN = S::NN, VW = S::VW;
     constexpr int SX = S::SX, SXY = S::SXY, LX = S::LX, LXY = S::LXY;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* su = reinterpret_cast<T*>(smem_raw);
@@ -83,9 +117,10 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP>::NT, Stage3R<T, P, E, C
     const int tid = threadIdx.x;
     const int ca = tid % N, cb = tid / N;
     // padded index of x_d = 0 on this thread's line along d, and the strides
-    const int s0 = 1 + SX * (ca + 1) + SXY * (cb + 1);   // x-line (x1, x2) = (ca, cb)
-    const int s1 = (ca + 1) + SX + SXY * (cb + 1);       // y-line (x0, x2) = (ca, cb)
-    const int s2 = (ca + 1) + SX * (cb + 1) + SXY;       // z-line (x0, x1) = (ca, cb)
+    // padded index of (x0, x1, x2) is (x0 + 1) + SX (x1 + 1) + SXY x2
+    const int s0 = 1 + SX * (ca + 1) + SXY * cb;         // x-line (x1, x2) = (ca, cb)
+    const int s1 = (ca + 1) + SX + SXY * cb;             // y-line (x0, x2) = (ca, cb)
+    const int s2 = (ca + 1) + SX * (cb + 1);             // z-line (x0, x1) = (ca, cb)
     const int l0 = LX * ca + LXY * cb;
     const int l1 = ca + LXY * cb;
     const int l2 = ca + LX * cb;
@@ -147,16 +182,43 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP>::NT, Stage3R<T, P, E, C
             const int lb = d == 0 ? l0 : l1;
             const int ls = d == 0 ? 1 : LX;
             T g[N + 2], gi[N], lap[N];
+            if (d == 0) {
+                // the x line is contiguous and 16-byte aligned: vector loads
+                using V = typename V16<T>::type;
 #pragma unroll
-            for (int k = 0; k < N + 2; ++k) line[k] = su[sb + (k - 1) * ss];
+                for (int k = 0; k + VW <= N + 2; k += VW) {
+                    const V v = *reinterpret_cast<const V*>(su + sb - 1 + k);
+                    const T* e = reinterpret_cast<const T*>(&v);
+#pragma unroll
+                    for (int q = 0; q < VW; ++q) line[k + q] = e[q];
+                }
+#pragma unroll
+                for (int k = (N + 2) / VW * VW; k < N + 2; ++k) line[k] = su[sb - 1 + k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < N + 2; ++k) line[k] = su[sb + (k - 1) * ss];
+            }
             line_full<T, P, E>(tb, line, gi, inv_h);
 #pragma unroll
             for (int j = 0; j < N; ++j) g[1 + j] = gi[j];
             g[0] = grad_ghost<T, P>(tb, flags, nb[2 * d], 2 * d, gp[2 * d], line[1], inv_h);
             g[N + 1] = grad_ghost<T, P>(tb, flags, nb[2 * d + 1], 2 * d + 1, gp[2 * d + 1], line[N], inv_h);
             line_full<T, P, E>(tb, g, lap, T(1));
+            if (d == 0 && N % VW == 0) {
+                using V = typename V16<T>::type;
 #pragma unroll
-            for (int j = 0; j < N; ++j) sl[lb + ls * j] += lap[j];
+                for (int j = 0; j < N; j += VW) {
+                    V* pv = reinterpret_cast<V*>(sl + lb + j);
+                    V v = *pv;
+                    T* e = reinterpret_cast<T*>(&v);
+#pragma unroll
+                    for (int q = 0; q < VW; ++q) e[q] += lap[j + q];
+                    *pv = v;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < N; ++j) sl[lb + ls * j] += lap[j];
+            }
             __syncthreads();
         }
         const T* yv = ysrc + it.off + NN;
