@@ -86,7 +86,7 @@ struct Group {
     std::vector<int> member_blocks;
     DevBuf d_coef, d_trm, d_trd;
     // full metric
-    DevBuf d_V, d_fv, d_bndx, d_eslot, d_ew, d_echol;
+    DevBuf d_V, d_fv, d_bndx, d_eslot, d_ew, d_echol, d_M;
     std::vector<double> bndx, ew, echol;
     std::vector<int> eslot;
     double wave_k[3] = {0, 0, 0}, wave_phi = 0;
@@ -318,7 +318,23 @@ struct twoldg_runner {
             CK(g.d_part.alloc(g.items.size() * sizeof(double)));
             CK(g.d_part2.alloc(g.items.size() * sizeof(double)));
             if (g.full) {
+                // sqrt(g) g^de = S[d] . S[e] / sqrt(g) per node, the gradient pass's
+                // flux coefficients, formed once in double and rounded once
+                std::vector<double> M((size_t)6 * g.NN * g.items.size());
+                const int pairs[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+                for (size_t b = 0; b < g.items.size(); ++b)
+                    for (int64_t n = 0; n < g.NN; ++n) {
+                        const double* cb = g.coef.data() + b * 10 * g.NN;
+                        const double J = cb[n];
+                        for (int k = 0; k < 6; ++k) {
+                            double s = 0;
+                            for (int i = 0; i < 3; ++i)
+                                s += cb[(1 + 3 * pairs[k][0] + i) * g.NN + n] * cb[(1 + 3 * pairs[k][1] + i) * g.NN + n];
+                            M[(b * 6 + k) * g.NN + n] = s / J;
+                        }
+                    }
                 int r = upload_t(g.d_coef, g.coef);
+                if (!r) r = upload_t(g.d_M, M);
                 if (!r) r = upload_t(g.d_ew, g.ew.empty() ? std::vector<double>(1, 0.0) : g.ew);
                 if (!r) r = upload_t(g.d_echol, g.echol.empty() ? std::vector<double>(1, 0.0) : g.echol);
                 if (r) return r;
@@ -429,6 +445,7 @@ struct twoldg_runner {
         p.V = g.d_V.p;
         p.fv = g.d_fv.p;
         p.coef = g.d_coef.p;
+        p.M = g.d_M.p;
         p.rk = d_rk.p;
         p.tinfo = (const double*)d_tinfo.p;
         p.bnd_x = (const double*)g.d_bndx.p;

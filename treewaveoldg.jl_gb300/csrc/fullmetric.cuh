@@ -1,18 +1,21 @@
 // The full-metric field step (3D): a geometry whose glues may swap axes,
-// such as the seven-patch ball (src/evolution.jl:112-220, 266-425,
-// 1110-1127). The gradient crosses faces as Cartesian components
-// V = grad u, all three in one field with a ghost plane on every face, so
-// a stage is two passes:
-//   fm_gradient_kernel: V_i = sum_e S[e][i] D_e u / (h sqrt(g)) at every node
-//     (u's face ghosts from the neighbours' exported face nodes, oriented
-//     across the glue, or the Dirichlet data on the domain's boundary), and
-//     V's face planes for the neighbours;
-//   fm_stage_kernel: sqrt(g) v' = sum_d D_d F^d with the flux F^d = S[d] . V
-//     formed at every point of the window along d, the ghost's with the face
-//     node's own S[d]; then the RK combination, the sqrt(g)-orthogonal
-//     truncation of v per element (Cholesky solves, or the element's tensor
-//     projector on an affine patch) and u's face export.
-// coef holds, per block, (N^3, 10): sqrt(g), then S[d][i] at 1 + 3d + i.
+// such as the seven- and thirteen-patch balls (src/evolution.jl:112-220,
+// 266-425, 1110-1299). The gradient crosses faces as Cartesian components
+// V = grad u, so a stage is two passes:
+//   fm_gradient_kernel: the logical derivatives D_e u at every node (u's face
+//     ghosts from the neighbours' exported face nodes, oriented across the
+//     glue, the Dirichlet data, or the radiative face's own node), then the
+//     fluxes F^d = S[d] . V = sum_e M^de D_e u / h with M^de = S[d] . S[e] /
+//     sqrt(g) = sqrt(g) g^de, three words per node, and V = sum_e S[e] D_e u /
+//     (h sqrt(g)) only on the face planes, for the neighbours;
+//   fm_stage_kernel: sqrt(g) v' = sum_d D_d F^d with the ghost's flux formed
+//     from the neighbour's V with this face node's own S[d] (or the Dirichlet
+//     gradient, or the radiative 2F* - F); then the RK combination, the
+//     sqrt(g)-orthogonal truncation of v per element (Cholesky solves, the
+//     factored projection, or the element's tensor projector on an affine
+//     patch) and u's face export.
+// coef holds, per block, (N^3, 10): sqrt(g), then S[d][i] at 1 + 3d + i; M
+// (N^3, 6): M^00, M^11, M^22, M^01, M^02, M^12, formed by the host from coef.
 #pragma once
 
 #include "kernels.cuh"
@@ -41,9 +44,10 @@ struct FmArgs {
     T* du;
     const T* fu_in;     // u face exports of the current stage value (N^2 per slot)
     T* fu_out;
-    T* V;               // (N^3, 3) per item
+    T* V;               // (N^3, 3) per item: the fluxes F^d (V itself in the energy pass)
     T* fv;              // V face planes: (3, N^2) per slot
     const T* coef;      // (N^3, 10) per item
+    const T* M;         // (N^3, 6) per item
     const T* rk;        // per problem dt/6, dt/3, dt/2, dt
     const double* tinfo;  // per problem: t_n, dt (FP64)
     const double* bnd_x;  // per slot: (3, N^2) physical positions of boundary face nodes
@@ -90,6 +94,11 @@ __device__ __forceinline__ int oriented(int t, int N, unsigned code) {
 
 __device__ __forceinline__ unsigned face_orient(const BlockItem& it, int f) { return (it.orient >> (3 * f)) & 7u; }
 
+__device__ __forceinline__ int sym_index(int d, int e) {
+    // M^de in the order 00, 11, 22, 01, 02, 12
+    return d == e ? d : d + e + 2;
+}
+
 // ---------------------------------------------------------------------------
 template <typename T, int P>
 __global__ void __launch_bounds__(256) fm_gradient_kernel(FmArgs<T> a, Tab<T, P> tb) {
@@ -98,7 +107,7 @@ __global__ void __launch_bounds__(256) fm_gradient_kernel(FmArgs<T> a, Tab<T, P>
     G g(a.E);
     constexpr int P1 = P + 1;
     T* su = reinterpret_cast<T*>(smem_raw);
-    T* sv = su + g.SS;               // V, ghost-free layout, 3 components
+    T* sD = su + g.SS;               // D_e u, ghost-free layout, e = 0, 1, 2
     const int mode = a.mode;
     const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1 || mode == MODE_ENERGY) ? a.u : a.y;
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
@@ -135,57 +144,79 @@ __global__ void __launch_bounds__(256) fm_gradient_kernel(FmArgs<T> a, Tab<T, P>
             su[sidx<3>(g, xg)] = v;
         }
         __syncthreads();
-        const T* cf = a.coef + (int64_t)item * 10 * g.NN;
-        for (int n = threadIdx.x; n < 3 * g.LS; n += blockDim.x) sv[n] = T(0);
+        // D_e u along every element line of every direction (one pass: the
+        // three directions write three arrays)
+        for (int L = threadIdx.x; L < 3 * g.E * g.F; L += blockDim.x) {
+            const int e = L / (g.E * g.F), r = L % (g.E * g.F);
+            const int tt = r % g.F, el = r / g.F;
+            const int sd = g.sstride(e), ld = g.lstride(e);
+            int x[3];
+            plane_coords<3>(g, e, tt, el * P1, x);
+            const int base = sidx<3>(g, x), lb = lidx<3>(g, x);
+            T w[P + 3], out[P + 1];
+#pragma unroll
+            for (int k = 0; k < P + 3; ++k) w[k] = su[base + (k - 1) * sd];
+            line_derivative<T, P>(tb, w, out);
+            T* dst = sD + e * g.LS;
+#pragma unroll
+            for (int q = 0; q <= P; ++q) dst[lb + q * ld] = out[q];
+        }
         __syncthreads();
-        // V_i += S[e][i] D_e u / h, line by line along e
-        for (int e = 0; e < 3; ++e) {
-            const int sd = g.sstride(e);
-            const int od = e == 0 ? 1 : e == 1 ? g.N : g.N * g.N;
-            const int ld = g.lstride(e);
-            for (int L = threadIdx.x; L < g.E * g.F; L += blockDim.x) {
-                const int tt = L % g.F, el = L / g.F;
+        const T* cf = a.coef + (int64_t)item * 10 * g.NN;
+        T* Vg = a.V + (int64_t)item * 3 * g.NN;
+        if (mode == MODE_ENERGY) {
+            // V = sum_e S[e] D_e u / (h sqrt(g)) at every node, for the energy
+            for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
                 int x[3];
-                plane_coords<3>(g, e, tt, el * P1, x);
-                const int base = sidx<3>(g, x), ob = oidx<3>(g, x), lb = lidx<3>(g, x);
-                T w[P + 3], out[P + 1];
+                owned_coords<3>(g, n, x);
+                const int l = lidx<3>(g, x);
+                const T De[3] = {sD[l] * inv_h, sD[g.LS + l] * inv_h, sD[2 * g.LS + l] * inv_h};
+                const T J = cf[n];
 #pragma unroll
-                for (int k = 0; k < P + 3; ++k) w[k] = su[base + (k - 1) * sd];
-                line_derivative<T, P>(tb, w, out);
+                for (int ci = 0; ci < 3; ++ci) {
+                    T s = T(0);
 #pragma unroll
-                for (int q = 0; q <= P; ++q) {
-                    const T De = out[q] * inv_h;
-                    const int o = ob + q * od;
-#pragma unroll
-                    for (int ci = 0; ci < 3; ++ci) sv[ci * g.LS + lb + q * ld] += cf[(1 + 3 * e + ci) * g.NN + o] * De;
+                    for (int e = 0; e < 3; ++e) s += cf[(1 + 3 * e + ci) * g.NN + n] * De[e];
+                    Vg[ci * g.NN + n] = s / J;
                 }
             }
-            __syncthreads();
-        }
-        T* Vg = a.V + (int64_t)item * 3 * g.NN;
-        for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
-            int x[3];
-            owned_coords<3>(g, n, x);
-            const int l = lidx<3>(g, x);
-            const T J = cf[n];
+        } else {
+            // the fluxes F^d = sum_e M^de D_e u / h at every node
+            const T* Mb = a.M + (int64_t)item * 6 * g.NN;
+            for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
+                int x[3];
+                owned_coords<3>(g, n, x);
+                const int l = lidx<3>(g, x);
+                const T De[3] = {sD[l] * inv_h, sD[g.LS + l] * inv_h, sD[2 * g.LS + l] * inv_h};
+                T m[6];
 #pragma unroll
-            for (int ci = 0; ci < 3; ++ci) {
-                const T val = sv[ci * g.LS + l] / J;
-                sv[ci * g.LS + l] = val;
-                Vg[ci * g.NN + n] = val;
+                for (int k = 0; k < 6; ++k) m[k] = Mb[k * g.NN + n];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    T s = T(0);
+#pragma unroll
+                    for (int e = 0; e < 3; ++e) s += m[sym_index(d, e)] * De[e];
+                    Vg[d * g.NN + n] = s;
+                }
             }
         }
-        __syncthreads();
-        // V's face planes for the neighbours
+        // V on the face planes for the neighbours
         for (int i = threadIdx.x; i < 6 * g.F; i += blockDim.x) {
             const int f = i / g.F, tt = i % g.F;
             const int d = f >> 1, side = f & 1;
             int x[3];
             plane_coords<3>(g, d, tt, side == 0 ? 0 : g.N - 1, x);
-            const int l = lidx<3>(g, x);
+            const int l = lidx<3>(g, x), n = oidx<3>(g, x);
+            const T De[3] = {sD[l] * inv_h, sD[g.LS + l] * inv_h, sD[2 * g.LS + l] * inv_h};
+            const T J = cf[n];
             T* o = a.fv + (int64_t)(it.slot + f) * 3 * g.F;
 #pragma unroll
-            for (int ci = 0; ci < 3; ++ci) o[ci * g.F + tt] = sv[ci * g.LS + l];
+            for (int ci = 0; ci < 3; ++ci) {
+                T s = T(0);
+#pragma unroll
+                for (int e = 0; e < 3; ++e) s += cf[(1 + 3 * e + ci) * g.NN + n] * De[e];
+                o[ci * g.F + tt] = s / J;
+            }
         }
         __syncthreads();
     }
@@ -358,17 +389,14 @@ __global__ void __launch_bounds__(256) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb
         const T inv_h = T(1) / T(it.h);
         const double t = stage_time(a.tinfo, it.problem, mode);
         const T* cf = a.coef + (int64_t)item * 10 * g.NN;
-        const T* Vb = a.V + (int64_t)item * 3 * g.NN;
+        const T* Fb = a.V + (int64_t)item * 3 * g.NN;
         for (int d = 0; d < 3; ++d) {
             const int sd = g.sstride(d), ld = g.lstride(d);
-            // F^d = S[d] . V at the owned nodes
+            // F^d at the owned nodes, from the gradient pass
             for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
                 int x[3];
                 owned_coords<3>(g, n, x);
-                T F = T(0);
-#pragma unroll
-                for (int ci = 0; ci < 3; ++ci) F += cf[(1 + 3 * d + ci) * g.NN + n] * Vb[ci * g.NN + n];
-                sF[sidx<3>(g, x)] = F;
+                sF[sidx<3>(g, x)] = Fb[d * g.NN + n];
             }
             // ... and at the two ghost planes along d, with the face node's S[d]
             for (int i = threadIdx.x; i < 2 * g.F; i += blockDim.x) {
@@ -382,11 +410,11 @@ __global__ void __launch_bounds__(256) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb
                     // radiative: the ghost's flux 2 F* - F, so that the central
                     // flux through the face is F* = -sigma |S[d]| (kappa v + u / R)
                     // (src/evolution.jl:1232-1260)
-                    T F = T(0), S2 = T(0);
+                    const T F = Fb[d * g.NN + o];
+                    T S2 = T(0);
 #pragma unroll
                     for (int ci = 0; ci < 3; ++ci) {
                         const T Sc = cf[(1 + 3 * d + ci) * g.NN + o];
-                        F += Sc * Vb[ci * g.NN + o];
                         S2 += Sc * Sc;
                     }
                     const T* yo = ysrc + it.off;

@@ -43,6 +43,7 @@ struct FmPtrs {
     void* V;
     void* fv;
     const void* coef;
+    const void* M;      // sqrt(g) g^de per node, 6 per node (00, 11, 22, 01, 02, 12)
     const void* rk;
     const double* tinfo;
     const double* bnd_x;

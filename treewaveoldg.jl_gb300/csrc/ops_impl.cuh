@@ -359,6 +359,7 @@ public:
         a.V = (T*)p.V;
         a.fv = (T*)p.fv;
         a.coef = (const T*)p.coef;
+        a.M = (const T*)p.M;
         a.rk = (const T*)p.rk;
         a.tinfo = p.tinfo;
         a.bnd_x = p.bnd_x;
