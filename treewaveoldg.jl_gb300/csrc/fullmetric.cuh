@@ -115,6 +115,11 @@ __global__ void __launch_bounds__(256) fm_gradient_kernel(FmArgs<T> a, Tab<T, P>
         const T inv_h = T(1) / T(it.h);
         const double t = stage_time(a.tinfo, it.problem, mode == MODE_ENERGY ? 0 : mode);
         const T* yu = ysrc + it.off;
+        if (threadIdx.x == 0) {
+            // the flux coefficients and sqrt(g) stream into L2 while u loads
+            prefetch_l2(a.M + (int64_t)item * 6 * g.NN, 6 * (size_t)g.NN * sizeof(T));
+            prefetch_l2(a.coef + (int64_t)item * 10 * g.NN, (size_t)g.NN * sizeof(T));
+        }
         for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
             int x[3];
             owned_coords<3>(g, n, x);
@@ -226,8 +231,8 @@ __global__ void __launch_bounds__(256) fm_gradient_kernel(FmArgs<T> a, Tab<T, P>
 // layout `sv`, element at x = base): c = Psi^T W v, U^T y = c, U z = y, v = Psi z
 // (src/evolution.jl:384-425). cbuf holds P^3 coefficients per element.
 template <typename T, int P, class G>
-__device__ __forceinline__ void fm_project_block(const G& g, const FmArgs<T>& a, const FmTab<T, P>& ft, int slot,
-                                                 T* sv, T* cbuf) {
+__device__ __forceinline__ void fm_project_block(const G& g, const FmArgs<T>& a, const T* L, int slot, T* sv,
+                                                 T* cbuf) {
     constexpr int P1 = P + 1, n3 = P1 * P1 * P1, m3 = P * P * P;
     const int EE = g.E * g.E * g.E;
     const T* W = a.ew + (int64_t)slot * n3 * EE;
@@ -240,7 +245,7 @@ __device__ __forceinline__ void fm_project_block(const G& g, const FmArgs<T>& a,
         for (int nn = 0; nn < n3; ++nn) {
             const int n0 = nn % P1, n1 = (nn / P1) % P1, n2 = nn / (P1 * P1);
             const int x[3] = {e0 * P1 + n0, e1 * P1 + n1, e2 * P1 + n2};
-            c += ft.L[q0][n0] * ft.L[q1][n1] * ft.L[q2][n2] * W[(int64_t)e * n3 + nn] * sv[lidx<3>(g, x)];
+            c += L[q0 * P1 + n0] * L[q1 * P1 + n1] * L[q2 * P1 + n2] * W[(int64_t)e * n3 + nn] * sv[lidx<3>(g, x)];
         }
         cbuf[i] = c;
     }
@@ -268,7 +273,7 @@ __device__ __forceinline__ void fm_project_block(const G& g, const FmArgs<T>& a,
         T z = T(0);
         for (int q = 0; q < m3; ++q) {
             const int q0 = q % P, q1 = (q / P) % P, q2 = q / (P * P);
-            z += ft.L[q0][n0] * ft.L[q1][n1] * ft.L[q2][n2] * c[q];
+            z += L[q0 * P1 + n0] * L[q1 * P1 + n1] * L[q2 * P1 + n2] * c[q];
         }
         const int x[3] = {e0 * P1 + n0, e1 * P1 + n1, e2 * P1 + n2};
         sv[lidx<3>(g, x)] = z;
@@ -282,80 +287,98 @@ __device__ __forceinline__ void fm_project_block(const G& g, const FmArgs<T>& a,
 // the angular tables: c = Psi^T W v, U^T y = c, U z = y, v = Psi z. The two
 // act on different indices and their product is the projection onto Q_{P-1}.
 // cbuf holds (P+1) P^2 coefficients per element.
+// The node of an element with index jk along dimension k and (ja, jb) along
+// the two others in increasing order, as an index into the ghost-free
+// layout; selects only, so that nothing indexes a local array at run time.
+template <class G>
+__device__ __forceinline__ int node_across(const G& g, int k, int jk, int ja, int jb) {
+    int x[3];
+    x[0] = k == 0 ? jk : ja;
+    x[1] = k == 1 ? jk : (k == 0 ? ja : jb);
+    x[2] = k == 2 ? jk : jb;
+    return lidx<3>(g, x);
+}
+
+__device__ __forceinline__ int pick3(int k, int a0, int a1, int a2) { return k == 0 ? a0 : k == 1 ? a1 : a2; }
+
 template <typename T, int P, class G>
-__device__ __forceinline__ void fm_project_factored(const G& g, const FmArgs<T>& a, const FmTab<T, P>& ft, int f,
-                                                    T* sv, T* cbuf) {
+__device__ __forceinline__ void fm_project_factored(const G& g, const FmArgs<T>& a, const T* L, int f, T* sv,
+                                                    T* cbuf) {
     constexpr int P1 = P + 1, n2 = P1 * P1, m2 = P * P;
     const int E = g.E, EE = E * E * E, E2 = E * E;
     const int k = a.fradial[f], A = a.faslot[f];
     const int d0 = k == 0 ? 1 : 0, d1 = k == 2 ? 1 : 2;
+    const int ls = g.lstride(k);
     // along k: v -= mode (dual . v) on every element line
     for (int i = threadIdx.x; i < EE * n2; i += blockDim.x) {
         const int e = i / n2, nn = i % n2;
-        const int ex[3] = {e % E, (e / E) % E, e / E2};
-        const T* rm = a.frm + ((int64_t)f * E + ex[k]) * P1;
-        const T* rd = a.frd + ((int64_t)f * E + ex[k]) * P1;
-        int x[3];
-        x[d0] = ex[d0] * P1 + nn % P1;
-        x[d1] = ex[d1] * P1 + nn / P1;
-        x[k] = ex[k] * P1;
-        const int l0 = lidx<3>(g, x), ls = g.lstride(k);
+        const int e0 = e % E, e1 = (e / E) % E, e2 = e / E2;
+        const int ek = pick3(k, e0, e1, e2), ea = pick3(d0, e0, e1, e2), eb = pick3(d1, e0, e1, e2);
+        const T* rm = a.frm + ((int64_t)f * E + ek) * P1;
+        const T* rd = a.frd + ((int64_t)f * E + ek) * P1;
+        const int l0 = node_across(g, k, ek * P1, ea * P1 + nn % P1, eb * P1 + nn / P1);
+        T v[P1];
         T c = T(0);
 #pragma unroll
-        for (int j = 0; j < P1; ++j) c += rd[j] * sv[l0 + j * ls];
+        for (int j = 0; j < P1; ++j) { v[j] = sv[l0 + j * ls]; c += rd[j] * v[j]; }
 #pragma unroll
-        for (int j = 0; j < P1; ++j) sv[l0 + j * ls] -= rm[j] * c;
+        for (int j = 0; j < P1; ++j) sv[l0 + j * ls] = v[j] - rm[j] * c;
     }
     __syncthreads();
     // across k, plane by plane: c = Psi^T W v
     for (int i = threadIdx.x; i < EE * P1 * m2; i += blockDim.x) {
         const int q = i % m2, j = (i / m2) % P1, e = i / (m2 * P1);
-        const int ex[3] = {e % E, (e / E) % E, e / E2};
-        const int ea = ex[d0] + E * ex[d1];
-        const T* W = a.faw + ((int64_t)A * E2 + ea) * n2;
+        const int e0 = e % E, e1 = (e / E) % E, e2 = e / E2;
+        const int ek = pick3(k, e0, e1, e2), ea = pick3(d0, e0, e1, e2), eb = pick3(d1, e0, e1, e2);
+        const T* W = a.faw + ((int64_t)A * E2 + ea + E * eb) * n2;
         const int q0 = q % P, q1 = q / P;
         T c = T(0);
-        for (int nn = 0; nn < n2; ++nn) {
-            const int na = nn % P1, nb = nn / P1;
-            int x[3];
-            x[d0] = ex[d0] * P1 + na;
-            x[d1] = ex[d1] * P1 + nb;
-            x[k] = ex[k] * P1 + j;
-            c += ft.L[q0][na] * ft.L[q1][nb] * W[nn] * sv[lidx<3>(g, x)];
-        }
+#pragma unroll
+        for (int nb = 0; nb < P1; ++nb)
+#pragma unroll
+            for (int na = 0; na < P1; ++na)
+                c += L[q0 * P1 + na] * L[q1 * P1 + nb] * W[na + P1 * nb] *
+                     sv[node_across(g, k, ek * P1 + j, ea * P1 + na, eb * P1 + nb)];
         cbuf[i] = c;
     }
     __syncthreads();
     for (int u = threadIdx.x; u < EE * P1; u += blockDim.x) {
         const int e = u / P1;
-        const int ex[3] = {e % E, (e / E) % E, e / E2};
-        const int ea = ex[d0] + E * ex[d1];
+        const int e0 = e % E, e1 = (e / E) % E, e2 = e / E2;
+        const int ea = pick3(d0, e0, e1, e2), eb = pick3(d1, e0, e1, e2);
         T* c = cbuf + u * m2;
-        const T* U = a.fachol + ((int64_t)A * E2 + ea) * m2 * m2;   // U[r][q] at r + m2 q
+        const T* U = a.fachol + ((int64_t)A * E2 + ea + E * eb) * m2 * m2;   // U[r][q] at r + m2 q
+        T z[m2];
+#pragma unroll
+        for (int q = 0; q < m2; ++q) z[q] = c[q];
+#pragma unroll
         for (int q = 0; q < m2; ++q) {            // U^T y = c
-            T s = c[q];
-            for (int r = 0; r < q; ++r) s -= U[r + m2 * q] * c[r];
-            c[q] = s / U[q + m2 * q];
+            T s = z[q];
+#pragma unroll
+            for (int r = 0; r < q; ++r) s -= U[r + m2 * q] * z[r];
+            z[q] = s / U[q + m2 * q];
         }
+#pragma unroll
         for (int q = m2 - 1; q >= 0; --q) {       // U z = y
-            T s = c[q];
-            for (int r = q + 1; r < m2; ++r) s -= U[q + m2 * r] * c[r];
-            c[q] = s / U[q + m2 * q];
+            T s = z[q];
+#pragma unroll
+            for (int r = q + 1; r < m2; ++r) s -= U[q + m2 * r] * z[r];
+            z[q] = s / U[q + m2 * q];
         }
+#pragma unroll
+        for (int q = 0; q < m2; ++q) c[q] = z[q];
     }
     __syncthreads();
     for (int i = threadIdx.x; i < EE * P1 * n2; i += blockDim.x) {
         const int nn = i % n2, j = (i / n2) % P1, e = i / (n2 * P1);
-        const int ex[3] = {e % E, (e / E) % E, e / E2};
+        const int e0 = e % E, e1 = (e / E) % E, e2 = e / E2;
+        const int ek = pick3(k, e0, e1, e2), ea = pick3(d0, e0, e1, e2), eb = pick3(d1, e0, e1, e2);
         const int na = nn % P1, nb = nn / P1;
         const T* c = cbuf + (e * P1 + j) * m2;
         T z = T(0);
-        for (int q = 0; q < m2; ++q) z += ft.L[q % P][na] * ft.L[q / P][nb] * c[q];
-        int x[3];
-        x[d0] = ex[d0] * P1 + na;
-        x[d1] = ex[d1] * P1 + nb;
-        x[k] = ex[k] * P1 + j;
-        sv[lidx<3>(g, x)] = z;
+#pragma unroll
+        for (int q = 0; q < m2; ++q) z += L[(q % P) * P1 + na] * L[(q / P) * P1 + nb] * c[q];
+        sv[node_across(g, k, ek * P1 + j, ea * P1 + na, eb * P1 + nb)] = z;
     }
     __syncthreads();
 }
@@ -363,17 +386,32 @@ __device__ __forceinline__ void fm_project_factored(const G& g, const FmArgs<T>&
 // The truncation of one block of the full metric: the element's tensor
 // projector (affine patch), the per-element projection, or the factored one.
 template <typename T, int P, class G>
-__device__ __forceinline__ void fm_truncate_block(const G& g, const FmArgs<T>& a, const Tab<T, P>& tb,
-                                                  const FmTab<T, P>& ft, int item, T* sv, T* cbuf) {
+__device__ __forceinline__ void fm_truncate_block(const G& g, const FmArgs<T>& a, const Tab<T, P>& tb, const T* L,
+                                                  int item, T* sv, T* cbuf) {
     const int s = a.eslot[item];
     const int f = a.fslot ? a.fslot[item] : 0;
-    if (s > 0) fm_project_block<T, P>(g, a, ft, s - 1, sv, cbuf);
-    else if (f > 0) fm_project_factored<T, P>(g, a, ft, f - 1, sv, cbuf);
+    if (s > 0) fm_project_block<T, P>(g, a, L, s - 1, sv, cbuf);
+    else if (f > 0) fm_project_factored<T, P>(g, a, L, f - 1, sv, cbuf);
     else truncate_block<T, 3, P, false, 0>(g, tb, sv, nullptr);
 }
 
+// The Legendre table in shared memory (a kernel-parameter array indexed at
+// run time would be copied to local memory): L[q (P+1) + i] = L_q(node i).
+template <typename T, int P>
+__device__ __forceinline__ void stage_legendre(const FmTab<T, P>& ft, T* L) {
+    for (int i = threadIdx.x; i < P * (P + 1); i += blockDim.x) {
+        const int q = i / (P + 1), n = i % (P + 1);
+#pragma unroll
+        for (int qq = 0; qq < P; ++qq)
+#pragma unroll
+            for (int nn = 0; nn <= P; ++nn)
+                if (qq == q && nn == n) L[i] = ft.L[qq][nn];
+    }
+    __syncthreads();
+}
+
 template <typename T, int P, bool COMP>
-__global__ void __launch_bounds__(256) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb, FmTab<T, P> ft) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb, FmTab<T, P> ft) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using G = ShapeR<3, P>;
     G g(a.E);
@@ -382,6 +420,8 @@ __global__ void __launch_bounds__(256) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb
     T* sl = sF + g.SS;                        // Laplacian accumulator, then the new v
     T* sc = sl + g.LS;                        // compensation of v (COMP)
     T* cbuf = sc + g.LS;                      // truncation coefficients
+    __shared__ T sLeg[P * (P + 1)];
+    stage_legendre<T, P>(ft, sLeg);
     const int mode = a.mode;
     const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
@@ -390,6 +430,26 @@ __global__ void __launch_bounds__(256) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb
         const double t = stage_time(a.tinfo, it.problem, mode);
         const T* cf = a.coef + (int64_t)item * 10 * g.NN;
         const T* Fb = a.V + (int64_t)item * 3 * g.NN;
+        if (threadIdx.x == 0) {
+            // everything the block reads after its fluxes: sqrt(g), the RK
+            // operands and its truncation tables, into L2 while the fluxes load
+            const size_t b = (size_t)g.NN * sizeof(T);
+            prefetch_l2(Fb, 3 * b);
+            prefetch_l2(cf, b);
+            prefetch_l2(ysrc + it.off, 2 * b);
+            if (mode != MODE_RHS && mode != MODE_STAGE1) {
+                prefetch_l2(a.u + it.off, 2 * b);
+                prefetch_l2(a.acc + it.off, 2 * b);
+                if (COMP && mode == MODE_STAGE4) prefetch_l2(a.comp + it.off, 2 * b);
+            }
+            const int es = a.eslot[item];
+            if (a.truncate && es > 0) {
+                constexpr int n3 = (P + 1) * (P + 1) * (P + 1), m3 = P * P * P;
+                const size_t EE = (size_t)g.E * g.E * g.E;
+                prefetch_l2(a.ew + (int64_t)(es - 1) * n3 * EE, n3 * EE * sizeof(T));
+                prefetch_l2(a.echol + (int64_t)(es - 1) * m3 * m3 * EE, (size_t)m3 * m3 * EE * sizeof(T));
+            }
+        }
         for (int d = 0; d < 3; ++d) {
             const int sd = g.sstride(d), ld = g.lstride(d);
             // F^d at the owned nodes, from the gradient pass
@@ -495,8 +555,8 @@ __global__ void __launch_bounds__(256) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb
         }
         __syncthreads();
         if (a.truncate) {
-            fm_truncate_block<T, P>(g, a, tb, ft, item, sl, cbuf);
-            if (final_comp) fm_truncate_block<T, P>(g, a, tb, ft, item, sc, cbuf);
+            fm_truncate_block<T, P>(g, a, tb, sLeg, item, sl, cbuf);
+            if (final_comp) fm_truncate_block<T, P>(g, a, tb, sLeg, item, sc, cbuf);
         }
         for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
             int x[3];
@@ -524,6 +584,8 @@ __global__ void __launch_bounds__(256) fm_truncate_kernel(FmArgs<T> a, Tab<T, P>
     G g(a.E);
     T* sv = reinterpret_cast<T*>(smem_raw);
     T* cbuf = sv + g.LS;
+    __shared__ T sLeg[P * (P + 1)];
+    stage_legendre<T, P>(ft, sLeg);
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         T* v = a.u + a.items[item].off + g.NN;
         for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
@@ -532,7 +594,7 @@ __global__ void __launch_bounds__(256) fm_truncate_kernel(FmArgs<T> a, Tab<T, P>
             sv[lidx<3>(g, x)] = v[n];
         }
         __syncthreads();
-        fm_truncate_block<T, P>(g, a, tb, ft, item, sv, cbuf);
+        fm_truncate_block<T, P>(g, a, tb, sLeg, item, sv, cbuf);
         for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
             int x[3];
             owned_coords<3>(g, n, x);

@@ -43,9 +43,9 @@ public:
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&max_smem_, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(stage_kernel<T, D, P, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
-        cudaFuncSetAttribute(stage_kernel_c<T, D, P, 2, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
-        cudaFuncSetAttribute(stage_kernel_c<T, D, P, 4, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
+        set_attrs(stage_kernel<T, D, P, COMP>);
+        set_attrs(stage_kernel_c<T, D, P, 2, COMP>);
+        set_attrs(stage_kernel_c<T, D, P, 4, COMP>);
         if constexpr (D == 3) {
             set_attrs3r<2>();
             set_attrs3r<4>();
@@ -66,12 +66,9 @@ public:
                 }
             }
         }
-        // the stage kernels hold whole blocks in shared memory: take the largest carveout
-        cudaFuncSetAttribute(stage_kernel<T, D, P, COMP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        cudaFuncSetAttribute(stage_kernel_c<T, D, P, 2, COMP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        cudaFuncSetAttribute(stage_kernel_c<T, D, P, 4, COMP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        cudaFuncSetAttribute(energy_kernel<T, D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
-        cudaFuncSetAttribute(truncate_kernel<T, D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
+        // the energy and truncation kernels stage blocks in shared memory too
+        set_attrs(energy_kernel<T, D, P>);
+        set_attrs(truncate_kernel<T, D, P>);
         cudaGetLastError();
         const int P1 = P + 1, PW = P + 3;
         for (int i = 0; i < P1; ++i) {
@@ -99,9 +96,14 @@ public:
         return LS;
     }
     static size_t smem_words(int E) { return 2 * padded_words(E) + plain_words(E); }
+    // the kernels hold whole blocks in shared memory: the largest carveout, and
+    // as dynamic shared memory the opt-in maximum less the kernel's own static
     template <typename K>
     void set_attrs(K kern) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_);
+        cudaFuncAttributes fa{};
+        cudaFuncGetAttributes(&fa, kern);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             max_smem_ - (int)fa.sharedSizeBytes);
         cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     }
     Launch launch_{0, 0, 0};
