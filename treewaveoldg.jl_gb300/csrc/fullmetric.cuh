@@ -348,25 +348,16 @@ __device__ __forceinline__ void fm_project_factored(const G& g, const FmArgs<T>&
         const int ea = pick3(d0, e0, e1, e2), eb = pick3(d1, e0, e1, e2);
         T* c = cbuf + u * m2;
         const T* U = a.fachol + ((int64_t)A * E2 + ea + E * eb) * m2 * m2;   // U[r][q] at r + m2 q
-        T z[m2];
-#pragma unroll
-        for (int q = 0; q < m2; ++q) z[q] = c[q];
-#pragma unroll
         for (int q = 0; q < m2; ++q) {            // U^T y = c
-            T s = z[q];
-#pragma unroll
-            for (int r = 0; r < q; ++r) s -= U[r + m2 * q] * z[r];
-            z[q] = s / U[q + m2 * q];
+            T s = c[q];
+            for (int r = 0; r < q; ++r) s -= U[r + m2 * q] * c[r];
+            c[q] = s / U[q + m2 * q];
         }
-#pragma unroll
         for (int q = m2 - 1; q >= 0; --q) {       // U z = y
-            T s = z[q];
-#pragma unroll
-            for (int r = q + 1; r < m2; ++r) s -= U[q + m2 * r] * z[r];
-            z[q] = s / U[q + m2 * q];
+            T s = c[q];
+            for (int r = q + 1; r < m2; ++r) s -= U[q + m2 * r] * c[r];
+            c[q] = s / U[q + m2 * q];
         }
-#pragma unroll
-        for (int q = 0; q < m2; ++q) c[q] = z[q];
     }
     __syncthreads();
     for (int i = threadIdx.x; i < EE * P1 * n2; i += blockDim.x) {
@@ -411,7 +402,7 @@ __device__ __forceinline__ void stage_legendre(const FmTab<T, P>& ft, T* L) {
 }
 
 template <typename T, int P, bool COMP>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb, FmTab<T, P> ft) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 4) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb, FmTab<T, P> ft) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using G = ShapeR<3, P>;
     G g(a.E);
