@@ -51,6 +51,9 @@ def parse():
                     help="comma list of the precisions to run; the headline needs f32c (profiling runs one)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--ball-roots", default="4,4,44",
+                    help="ball13: the roots (n, m, m') of the thirteen-patch ball (the benchmark ball's 4,4,44; "
+                         "a smaller m' for profiling)")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner (untimed, before the warm-up) and run the default launch layouts")
     ap.add_argument("--workload", default="box256", choices=["box256", "nested", "c1", "ball", "ball13"],
@@ -356,7 +359,8 @@ def ball_benchmark(args, twoldg, torch):
     CUDA events on the library's stream, FP64 and FP32 + compensated, and the
     FP32 run's L2 distance from the FP64 one after the warm-up and timed steps."""
     lib = twoldg._lib.lib()
-    forest, geo = twoldg.thirteenpatch_forest(np.float64, 3, 4, roots=(4, 4, 44), Lc=4.0, Rm=12.0, R1=100.0)
+    roots = tuple(int(x) for x in args.ball_roots.split(","))
+    forest, geo = twoldg.thirteenpatch_forest(np.float64, 3, 4, roots=roots, Lc=4.0, Rm=12.0, R1=100.0)
     arms, final = {}, {}
     for prec in ("f64", "f32c"):
         T = np.float64 if prec == "f64" else np.float32
@@ -393,9 +397,10 @@ def ball_benchmark(args, twoldg, torch):
     line = {"metric": METRIC, "value": head["value"], "unit": "node-steps/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "the benchmark ball: thirteen-patch, roots (4,4,44), E=4, P=3, Lc=4, Rm=12, "
-                                   "R1=100 (4672 blocks of 16^3, %d nodes), Sommerfeld radiative sphere, "
-                                   "truncation on, state sin(1..n) truncated, cfl 1/2" % head["nodes"],
+            "config": {"workload": "the benchmark ball: thirteen-patch, roots %s, E=4, P=3, Lc=4, Rm=12, "
+                                   "R1=100 (%d blocks of 16^3, %d nodes), Sommerfeld radiative sphere, "
+                                   "truncation on, state sin(1..n) truncated, cfl 1/2"
+                                   % (roots, forest.nleaves(), head["nodes"]),
                        "precision": "f32c", "l2_flush": "inputs larger than L2"},
             "fp64": arms["f64"], "f32c": arms["f32c"], "speedup_vs_fp64": head["value"] / arms["f64"]["value"],
             "reference_h200_ns_per_node_step": {"f64": 2.84, "f32": 1.92, "source": "CODE.md:5108-5122"},
