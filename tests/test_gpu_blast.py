@@ -1,0 +1,89 @@
+"""The blast wave through libtwoldg: the uniform runs against the reference's
+published errors, and the adaptive driver's promises (the ring refined to
+the cap, the energy changed only at regrids and little there, the uniform
+run's accuracy at the cap for fewer node-steps). Marked gpu."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ADAPTIVE = dict(P=3, E=2, roots=4, maxlevel_cap=2, refine_tol=1e-2, coarsen_tol=1e-5, chunk=0.05, t_end=0.2)
+
+
+@pytest.fixture(scope="module")
+def adaptive_run(native):
+    from twoldg.blast import adaptive_blast
+    return adaptive_blast(**ADAPTIVE)
+
+
+@pytest.mark.parametrize("P,roots,t,linf", [(3, 16, 0.2, 5.59e-2), (4, 16, 0.2, 5.43e-3)])
+def test_uniform_blast_published_errors(native, P, roots, t, linf):
+    # reference CODE.md:4935-4937; the FP32 + compensated run within 1e-3 of it
+    from twoldg.blast import uniform_blast
+    r = uniform_blast(np.float64, P=P, E=2, roots=roots, t_end=t)
+    assert r["err"] == pytest.approx(linf, rel=0.01)
+    r32 = uniform_blast(np.float32, P=P, E=2, roots=roots, t_end=t, precision="f32c")
+    assert r32["err"] == pytest.approx(r["err"], rel=2e-3)
+
+
+def test_adaptive_blast_refines_the_ring_to_the_cap(adaptive_run):
+    # test/adaptive_tests.jl:296-323
+    r = adaptive_run
+    sigma, t = 0.08, ADAPTIVE["t_end"]
+    assert r["converged"]
+    assert r["maxlevel"] == ADAPTIVE["maxlevel_cap"]
+    assert r["nregrids"] >= 2
+    f = r["forest"]
+    dist = lambda a, b: math.hypot(a - 0.5, b - 0.5)
+    ring, coarse = [], []
+    for key in f.leaves:
+        ext = f.block_extent(key)
+        corners = [dist(a, b) for a in ext[0] for b in ext[1]]
+        if min(corners) <= t + sigma and max(corners) >= t - sigma:
+            ring.append(key)
+        if key[0] < ADAPTIVE["maxlevel_cap"]:
+            coarse.append(key)
+    assert ring and all(lv == ADAPTIVE["maxlevel_cap"] for lv, _ in ring)
+    assert coarse
+    for key in coarse:
+        ext = f.block_extent(key)
+        assert dist((ext[0][0] + ext[0][1]) / 2, (ext[1][0] + ext[1][1]) / 2) > t + 2 * sigma
+
+
+def test_adaptive_blast_energy_changes_only_at_regrids(adaptive_run):
+    # test/adaptive_tests.jl:325-347: within a chunk only RK4 loses energy;
+    # a regrid changes it by how far the data jump across the faces it moves
+    r = adaptive_run
+    for c in r["chunks"]:
+        assert 0 <= (c["energy_start"] - c["energy_end"]) / c["energy_start"] < 2e-9
+    for a, b in zip(r["chunks"][:-1], r["chunks"][1:]):
+        if a["regridded"]:
+            assert abs(b["energy_start"] - a["energy_end"]) < 1e-10 * r["energy0"]
+        else:
+            assert b["energy_start"] == a["energy_end"]
+    assert sum(c["regridded"] for c in r["chunks"]) == r["nregrids"]
+    assert not r["chunks"][-1]["regridded"]
+    assert r["chunks"][-1]["t"] == ADAPTIVE["t_end"]
+
+
+def test_adaptive_blast_matches_the_uniform_run_at_less_work(adaptive_run):
+    # test/adaptive_tests.jl:349-373: the error of the uniform run at the
+    # cap's spacing, for at most 82 % of its node-steps
+    from twoldg.blast import uniform_blast
+    r = adaptive_run
+    u = uniform_blast(np.float64, P=3, E=2, roots=ADAPTIVE["roots"] * 2 ** ADAPTIVE["maxlevel_cap"],
+                      t_end=ADAPTIVE["t_end"])
+    assert r["err"] < 1.01 * u["err"]
+    assert r["l2"] < 1.01 * u["l2"]
+    assert r["node_steps"] < 0.82 * u["nodes"] * u["nsteps"]
+    assert r["h"] == u["h"]
+    # the published row (CODE.md:4915): L-infinity and L2 ratios 1.000, 0.79
+    # of the node-steps, 160 blocks after the initial adaptation and 244 at
+    # the end, 3 of 3 regrids changing the mesh
+    assert r["err"] / u["err"] == pytest.approx(1.000, abs=0.0015)
+    assert r["l2"] / u["l2"] == pytest.approx(1.000, abs=0.0015)
+    assert r["node_steps"] / (u["nodes"] * u["nsteps"]) == pytest.approx(0.79, abs=0.01)
+    assert r["chunks"][0]["nblocks"] == 160 and r["forest"].nleaves() == 244
+    assert r["nregrids"] == 3

@@ -52,6 +52,13 @@ def test_regrid_refines_coarsens_and_balances():
     flags = [COARSEN if lv == 1 else KEEP for lv, _ in g.leaves]
     flags[g.leaves.index((1, (2, 2)))] = KEEP
     assert sorted(regrid(g, flags).leaves) == sorted(g.leaves)
+    # a KEEP box asks for its own level around it: a coarser leaf it reaches
+    # is refined, one at the same level is only held
+    flags = [KEEP] * g.nleaves()
+    flags[g.leaves.index((1, (3, 3)))] = (KEEP, ((0, 6), (0, 6)))
+    k = regrid(g, flags, buffer=1)
+    assert (1, (2, 4)) in k.leaves and (0, (1, 2)) not in k.leaves
+    assert (1, (2, 2)) in k.leaves
     # refining next to a refined block keeps 2:1 balance
     flags = [REFINE if k == (1, (3, 3)) else KEEP for k in g.leaves]
     r = regrid(g, flags)

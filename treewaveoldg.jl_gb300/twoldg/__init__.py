@@ -20,4 +20,7 @@ from .geometry import (PolarAnnulus, annulus_errors, annulus_exact, annulus_fore
 from .ball import (BallForest, OutgoingPulse, PlaneWave, RadiativeBoundary, SevenPatchBall, ThirteenPatchBall,
                    radiative_errors, sevenpatch_errors, sevenpatch_exact, sevenpatch_forest, thirteenpatch_forest)
 
+from .regrid import COARSEN, KEEP, REFINE, refine_flags, refine_mark, regrid, transfer_state
+from .blast import adaptive_blast, blast_exact, blast_initial, blast_reference, refinement_buffer, uniform_blast
+
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -71,8 +71,9 @@ def _flag_kind(f):
 def regrid(forest, flags, buffer=0):
     """The forest regridded by one flag per leaf (REFINE, KEEP or COARSEN, or
     (flag, box)): a flagged box dilated by `buffer` points of its block's
-    spacing recruits the leaves it reaches (they are not coarsened, and are
-    refined with a REFINE block of their level or coarser); a complete set of
+    spacing asks for its block's level around it (one more with REFINE), so
+    the leaves it reaches are not coarsened and a coarser one is refined, and
+    the margin travels with the feature; a complete set of
     2^D sibling leaves all flagged COARSEN and not recruited is merged when
     no leaf beside their parent is finer than they are; then the forest is
     refined back to 2:1 balance. Returns a new Forest; each of its blocks is
@@ -101,7 +102,7 @@ def regrid(forest, flags, buffer=0):
             oe = extents[q]
             if all(oe[d][0] < box[d][1] and box[d][0] < oe[d][1] for d in range(D)):
                 hold.add(other)
-                if f[0] == REFINE and other[0] <= key[0]:
+                if other[0] < key[0] + (1 if f[0] == REFINE else 0):
                     refine.add(other)
     new = Forest.__new__(Forest)
     new.__dict__.update({k: v for k, v in forest.__dict__.items() if not k.startswith("_tables")})
