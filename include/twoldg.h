@@ -203,6 +203,16 @@ int twoldg_mode_amplitude(twoldg_problem* p, const void* u, int32_t var, int32_t
  * without the graph, with CUDA events between the four stages, and returns
  * each stage's duration in milliseconds (stage_ms[4]). Synchronous. */
 int twoldg_profile_step(twoldg_problem* p, void* u, double dt, float* stage_ms);
+/* The extraction's gather (sphere_values / plane_values, src/extraction.jl:
+ * 216-245): out[j] = sum_q weights[q + nper j] * u[index[q + nper j] + (var-1)
+ * N^D] for j < npoints, the element polynomials of variable var (1: u, 2: v)
+ * at located points. index (int64, positions in the state vector for
+ * variable 1), weights and out are device arrays, weights and out of the
+ * problem's field type; the host builds the stencils (the points' elements
+ * and Lagrange weights). Asynchronous on the problem's stream. */
+int twoldg_gather(twoldg_problem* p, const void* u, int32_t var, int64_t npoints, int32_t nper,
+                  const int64_t* index, const void* weights, void* out);
+
 /* The regrid transfer (TreeAMR's element-set regrid, which the reference's
  * regrid! / adaptive_blast run on the host: src/blast.jl, CODE.md "Adaptive
  * refinement"): the state u_from of the flat forest `from` moved onto the

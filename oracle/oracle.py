@@ -360,3 +360,53 @@ def oracle_transfer(old_leaves, u_old, new_leaves, D, P, E):
                 big = _along(big, down, d, D)
             out[b, var] = big
     return out.reshape(-1)
+
+
+# --- the extraction's reading, restated (test infrastructure) -----------------
+def oracle_point_values(forest, P, u, points, var=1, locate=None):
+    """The element polynomial of variable `var` at physical points of a brick
+    (or, with `locate(x) -> (block, local coordinates in [0, 1]^D)`, of any
+    forest): the block found by scanning the leaves' extents, the element by
+    the position in it, the value by the Lagrange form through the golden
+    Gauss-Lobatto nodes in long double."""
+    t = golden_tables(P)
+    nodes = np.array(t["nodes"], dtype=np.longdouble)
+    D, N = forest.D, forest.N
+    P1, E, NN = P + 1, N // (P + 1), N ** D
+    u = np.asarray(u, dtype=np.float64).reshape(-1, 2, *([N] * D))
+    out = np.empty(len(points))
+    for j, x in enumerate(points):
+        if locate is None:
+            b, local = None, None
+            for q, key in enumerate(forest.leaves):
+                ext = forest.block_extent(key)
+                if all(ext[d][0] <= x[d] <= ext[d][1] for d in range(D)):
+                    b, local = q, [(x[d] - ext[d][0]) / (ext[d][1] - ext[d][0]) for d in range(D)]
+                    if forest.leaves[q][0] == max(lv for lv, _ in forest.leaves):
+                        break
+            if b is None:
+                raise ValueError("point %r is outside the forest" % (tuple(x),))
+        else:
+            b, local = locate(x)
+        acc = np.longdouble(0)
+        e = [min(int(local[d] * E), E - 1) for d in range(D)]
+        z = [np.longdouble(2) * (np.longdouble(local[d]) * E - e[d]) - 1 for d in range(D)]
+        L = []
+        for d in range(D):
+            row = []
+            for i in range(P1):
+                v = np.longdouble(1)
+                for m in range(P1):
+                    if m != i:
+                        v *= (z[d] - nodes[m]) / (nodes[i] - nodes[m])
+                row.append(v)
+            L.append(row)
+        for I in np.ndindex(*([P1] * D)):
+            J = I[::-1]
+            w = np.longdouble(1)
+            for d in range(D):
+                w *= L[d][J[d]]
+            idx = tuple(e[d] * P1 + J[d] for d in range(D))[::-1]
+            acc += w * np.longdouble(u[(b, var - 1) + idx])
+        out[j] = float(acc)
+    return out

@@ -975,6 +975,17 @@ int twoldg_synchronize(twoldg_problem* p) {
     return TWOLDG_OK;
 }
 
+int twoldg_gather(twoldg_problem* p, const void* u, int32_t var, int64_t npoints, int32_t nper,
+                  const int64_t* index, const void* weights, void* out) {
+    if (!p || !u || (npoints > 0 && (!index || !weights || !out))) return fail(TWOLDG_EINVAL, "NULL argument");
+    if (var != 1 && var != 2) return fail(TWOLDG_EINVAL, "var must be 1 (u) or 2 (v)");
+    if (npoints < 0 || nper < 1) return fail(TWOLDG_EINVAL, "npoints must be >= 0 and nper >= 1");
+    if (p->groups.empty()) return fail(TWOLDG_EINVAL, "the problem has no blocks");
+    Group& g = *p->groups[0];
+    CK(g.ops->gather(u, (var - 1) * g.NN, npoints, nper, index, weights, out, p->stream));
+    return TWOLDG_OK;
+}
+
 int twoldg_transfer(const twoldg_desc* from, const void* u_from, const twoldg_desc* to, void* u_to, void* stream) {
     if (!from || !to || !u_from || !u_to) return fail(TWOLDG_EINVAL, "NULL argument");
     if (from->dim != to->dim || from->order != to->order || from->elems != to->elems ||

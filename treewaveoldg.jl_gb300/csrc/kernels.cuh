@@ -327,6 +327,20 @@ __global__ void cf_ghost_g_kernel(const CfFace* cf, int ncf, int E, const T* gfd
 }
 
 // ---------------------------------------------------------------------------
+// The stencil gather of the extraction (src/extraction.jl:216-245): out[j] =
+// sum_q w[q, j] u[index[q, j] + varoff], one thread per point.
+template <typename T>
+__global__ void __launch_bounds__(256) gather_kernel(const T* u, int64_t varoff, int64_t npoints, int nper,
+                                                     const int64_t* index, const T* w, T* out) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < npoints;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        T s = T(0);
+        for (int q = 0; q < nper; ++q) s += w[j * nper + q] * u[index[j * nper + q] + varoff];
+        out[j] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // The regrid transfer (TreeAMR's element-set regrid, which the reference's
 // regrid! runs on the host): one CTA per new block, both variables, by
 // direct tensor sums of the 1D operators. Refining evaluates the coarse

@@ -89,6 +89,9 @@ public:
     virtual int launch_candidates(int E, bool flat, Launch* out, int max) const = 0;
     virtual cudaError_t export_faces(const BlockItem* items, int nitems, int E, const void* u, void* fu,
                                      void* fog, cudaStream_t s) const = 0;
+    // the extraction's stencil gather: out[j] = sum_q w[q,j] u[index[q,j] + varoff]
+    virtual cudaError_t gather(const void* u, int64_t varoff, int64_t npoints, int nper, const int64_t* index,
+                               const void* w, void* out, cudaStream_t s) const = 0;
     // the regrid transfer of both variables, one new block per item
     virtual cudaError_t transfer(const TransferItem* items, int nitems, int E, const void* src, void* dst,
                                  cudaStream_t s) const = 0;

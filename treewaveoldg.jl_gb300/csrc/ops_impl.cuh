@@ -203,6 +203,14 @@ public:
         return cudaGetLastError();
     }
 
+    cudaError_t gather(const void* u, int64_t varoff, int64_t npoints, int nper, const int64_t* index,
+                       const void* w, void* out, cudaStream_t s) const override {
+        if (npoints == 0) return cudaSuccess;
+        gather_kernel<T><<<grid_for(npoints, 256), 256, 0, s>>>((const T*)u, varoff, npoints, nper, index,
+                                                                 (const T*)w, (T*)out);
+        return cudaGetLastError();
+    }
+
     cudaError_t transfer(const TransferItem* items, int nitems, int E, const void* src, void* dst,
                          cudaStream_t s) const override {
         if (nitems == 0) return cudaSuccess;

@@ -23,4 +23,7 @@ from .ball import (BallForest, OutgoingPulse, PlaneWave, RadiativeBoundary, Seve
 from .regrid import COARSEN, KEEP, REFINE, refine_flags, refine_mark, regrid, transfer_state
 from .blast import adaptive_blast, blast_exact, blast_initial, blast_reference, refinement_buffer, uniform_blast
 
+from .extraction import (PlaneExtraction, SphereExtraction, ball_patch_point, harmonic_modes, plane_values,
+                         sphere_modes, sphere_rule, sphere_values, spherical_harmonics)
+
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -20,7 +20,7 @@ EXPORTS = [
     "twoldg_energy", "twoldg_norm", "twoldg_modal_indicator", "twoldg_mode_amplitude",
     "twoldg_synchronize", "twoldg_batch_create", "twoldg_batch_destroy", "twoldg_batch_offsets",
     "twoldg_batch_rk4_step", "twoldg_batch_synchronize", "twoldg_profile_step", "twoldg_stream",
-    "twoldg_rhs_static", "twoldg_autotune", "twoldg_batch_autotune", "twoldg_transfer",
+    "twoldg_rhs_static", "twoldg_autotune", "twoldg_batch_autotune", "twoldg_transfer", "twoldg_gather",
 ]
 
 
@@ -90,6 +90,7 @@ def lib():
             "twoldg_rhs_static": (ctypes.c_int, [ctypes.POINTER(Desc), vp, vp, d, vp]),
             "twoldg_autotune": (ctypes.c_int, [vp, vp, d, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]),
             "twoldg_transfer": (ctypes.c_int, [ctypes.POINTER(Desc), vp, ctypes.POINTER(Desc), vp, vp]),
+            "twoldg_gather": (ctypes.c_int, [vp, vp, i32, i64, i32, vp, vp, vp]),
             "twoldg_batch_autotune": (ctypes.c_int, [vp, vp, ctypes.POINTER(d), ctypes.c_char_p, ctypes.c_char_p,
                                                      ctypes.c_size_t]),
         }
