@@ -175,7 +175,9 @@ int twoldg_truncate(twoldg_problem* p, void* u);
 /* `nsteps` classic RK4 steps of size dt from time t, in place on u, with the
  * truncation as stage and step limiter -- wave_integrator + solve!
  * (src/stepping.jl:72-78, src/evolution.jl:1408-1430). The step is a CUDA
- * graph, captured on the first call and re-captured when u or dt change.
+ * graph captured on the first call for a state pointer; the graphs of the
+ * four most recently used pointers are kept (a caller may alternate state
+ * buffers), and a new dt changes only the coefficients the graph reads.
  * For TWOLDG_F32C the compensation words persist between calls on the same
  * u and are cleared when u changes or by twoldg_reset_compensation. */
 int twoldg_rk4_step(twoldg_problem* p, void* u, double t, double dt, int32_t nsteps);

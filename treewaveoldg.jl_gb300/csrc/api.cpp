@@ -126,8 +126,11 @@ struct twoldg_runner {
     std::vector<double> h_tinfo;               // per problem: t_n, dt (the full metric's stage times)
     std::vector<double> h_dts;                 // the dt each problem's coefficients were made for
     std::vector<unsigned char> h_rk;           // per problem dt/6, dt/3, dt/2, dt in the field type
-    cudaGraphExec_t gexec = nullptr;
-    void* graph_u = nullptr;
+    // the captured step graphs, keyed by the state pointer they were captured
+    // for (a caller that alternates a few state buffers keeps them all),
+    // most recently used first
+    static constexpr int kGraphs = 4;
+    std::vector<std::pair<void*, cudaGraphExec_t>> graphs;
     void* comp_u = nullptr;
     // Shape groups of a batch never exchange data, so each group's four
     // stages are one independent branch of the step's graph: side[i] carries
@@ -137,7 +140,7 @@ struct twoldg_runner {
     cudaEvent_t fork = nullptr;
 
     ~twoldg_runner() {
-        if (gexec) cudaGraphExecDestroy(gexec);
+        drop_graphs();
         for (auto e : join) cudaEventDestroy(e);
         for (auto st : side) cudaStreamDestroy(st);
         if (fork) cudaEventDestroy(fork);
@@ -548,6 +551,11 @@ struct twoldg_runner {
 
     void fm_advance_time(cudaStream_t s);
 
+    void drop_graphs() {
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        graphs.clear();
+    }
+
     // The autotuner: for every shape group, time each launch layout the
     // group's kernels offer on stages 1 to 3 of a step from u (which they do
     // not change: they write only the stage scratch and the face planes) and
@@ -642,11 +650,7 @@ struct twoldg_runner {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (rc) return rc;
-        if (gexec) {
-            cudaGraphExecDestroy(gexec);
-            gexec = nullptr;
-        }
-        graph_u = nullptr;
+        drop_graphs();
         if (cache) {
             std::ofstream out(cache, std::ios::trunc);
             if (!out) return fail(TWOLDG_EINVAL, std::string("cannot write the autotuner cache ") + cache);
@@ -691,8 +695,14 @@ struct twoldg_runner {
         if (nsteps == 0) return TWOLDG_OK;
         int r = export_all(u);
         if (r) return r;
-        if (!gexec || graph_u != u) {
-            if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        cudaGraphExec_t gexec = nullptr;
+        for (size_t i = 0; i < graphs.size(); ++i)
+            if (graphs[i].first == u) {
+                gexec = graphs[i].second;
+                std::rotate(graphs.begin(), graphs.begin() + i, graphs.begin() + i + 1);
+                break;
+            }
+        if (!gexec) {
             cudaGraph_t graph;
             CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
             r = enqueue_step(u);
@@ -701,8 +711,12 @@ struct twoldg_runner {
             if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
             e = cudaGraphInstantiate(&gexec, graph, 0);
             cudaGraphDestroy(graph);
-            if (e != cudaSuccess) { gexec = nullptr; return cuda_fail(e, "cudaGraphInstantiate"); }
-            graph_u = u;
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+            if ((int)graphs.size() == kGraphs) {
+                cudaGraphExecDestroy(graphs.back().second);
+                graphs.pop_back();
+            }
+            graphs.insert(graphs.begin(), {u, gexec});
         }
         for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(gexec, stream));
         CK(cudaGetLastError());
