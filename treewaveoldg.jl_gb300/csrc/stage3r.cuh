@@ -239,6 +239,11 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
         T* __restrict__ acc = a.acc + it.off;
         T* __restrict__ comp = COMP ? a.comp + it.off : nullptr;
         const bool final_comp = COMP && mode == MODE_STAGE4;
+        // the new u is final here (the truncation acts on v only): stages 1-3
+        // store it from registers as each element is done; stage 4, which
+        // writes u^n in place, stores it with v at the end (measured faster)
+        T* out = (mode == MODE_STAGE4 ? a.u : a.y) + it.off;
+        const bool early_u = mode != MODE_STAGE4;
 #pragma unroll
         for (int ez = 0; ez < E; ++ez) {
             T y[P1], uu[P1], uv[P1], au[P1], av[P1], cu[P1], cvi[P1];
@@ -310,6 +315,7 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
                     acc[NN + n] = av[q];
                 }
                 if (final_comp) comp[n] = cu[q];
+                if (early_u) out[n] = nu[q];
                 su[s2 + SXY * j] = nu[q];
                 sl[l2 + LXY * j] = nv[q];
                 if (final_comp) sc[l2 + LXY * j] = cv[q];
@@ -362,11 +368,10 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
                 __syncthreads();
             }
         }
-        // ---- the new state of the column
-        T* out = (mode == MODE_STAGE4 ? a.u : a.y) + it.off;
+        // ---- the new v of the column (and in stage 4 its u)
 #pragma unroll
         for (int j = 0; j < N; ++j) {
-            out[tid + F * j] = su[s2 + SXY * j];
+            if (!early_u) out[tid + F * j] = su[s2 + SXY * j];
             out[NN + tid + F * j] = sl[l2 + LXY * j];
             if (final_comp) comp[NN + tid + F * j] = sc[l2 + LXY * j];
         }
