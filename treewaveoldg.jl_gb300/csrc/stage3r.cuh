@@ -320,11 +320,19 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
                 sl[l2 + LXY * j] = nv[q];
                 if (final_comp) sc[l2 + LXY * j] = cv[q];
             }
+            // the column's own z faces from the first and the last element,
+            // still in registers
+            if (ez == 0 || ez == E - 1) {
+                const int side = ez == 0 ? 0 : 1;
+                const int64_t o = (int64_t)(slot + 4 + side) * F + tid;
+                a.fu_out[o] = side == 0 ? nu[0] : nu[P];
+                a.fog_out[o] = own_face_part<T, P>(tb, side, nu);
+            }
         }
         __syncthreads();
-        // ---- face export of the new u (reads su only)
+        // ---- face export of the new u on the x and y faces (reads su only)
 #pragma unroll
-        for (int f = 0; f < 6; ++f) {
+        for (int f = 0; f < 4; ++f) {
             const int d = f >> 1, side = f & 1;
             const int sd = d == 0 ? 1 : d == 1 ? SX : SXY;
             const int base = (d == 0 ? s0 : d == 1 ? s1 : s2) + (side ? N - 1 - P : 0) * sd;
