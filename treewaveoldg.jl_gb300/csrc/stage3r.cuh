@@ -104,6 +104,73 @@ __device__ __forceinline__ T grad_ghost(const Tab<T, P>& tb, uint32_t flags, int
     return (flags & (1u << (8 + f))) ? -gnb : gnb;
 }
 
+// The truncation of the E element lines of a thread's line in shared memory
+// (base b, stride ls), with the compensation's two-sum in stage 4; VEC: the
+// line is contiguous and each element's P+1 nodes are whole 16-byte words.
+template <typename T, int P, int E, bool VEC>
+__device__ __forceinline__ void truncate_lines(const Tab<T, P>& tb, T* sl, T* sc, int b, int ls, bool final_comp) {
+    constexpr int P1 = P + 1, VW = 16 / sizeof(T);
+    using V = typename V16<T>::type;
+    auto load = [&](const T* p, int b0, T (&v)[P1]) {
+        if constexpr (VEC) {
+#pragma unroll
+            for (int k = 0; k < P1; k += VW) {
+                const V t = *reinterpret_cast<const V*>(p + b0 + k);
+                const T* e = reinterpret_cast<const T*>(&t);
+#pragma unroll
+                for (int q = 0; q < VW; ++q) v[k + q] = e[q];
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < P1; ++q) v[q] = p[b0 + q * ls];
+        }
+    };
+    auto store = [&](T* p, int b0, const T (&v)[P1]) {
+        if constexpr (VEC) {
+#pragma unroll
+            for (int k = 0; k < P1; k += VW) {
+                V t;
+                T* e = reinterpret_cast<T*>(&t);
+#pragma unroll
+                for (int q = 0; q < VW; ++q) e[q] = v[k + q];
+                *reinterpret_cast<V*>(p + b0 + k) = t;
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < P1; ++q) p[b0 + q * ls] = v[q];
+        }
+    };
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int b0 = b + e * P1 * ls;
+        T v[P1];
+        load(sl, b0, v);
+        T c = T(0);
+#pragma unroll
+        for (int q = 0; q < P1; ++q) c += tb.td[q] * v[q];
+        if (final_comp) {
+            T w[P1];
+            load(sc, b0, w);
+            T cc = T(0);
+#pragma unroll
+            for (int q = 0; q < P1; ++q) cc += tb.td[q] * w[q];
+            c += cc;
+#pragma unroll
+            for (int q = 0; q < P1; ++q) {
+                T s, err;
+                two_sum(v[q], -(tb.tm[q] * c), s, err);
+                v[q] = s;
+                w[q] += err;
+            }
+            store(sc, b0, w);
+        } else {
+#pragma unroll
+            for (int q = 0; q < P1; ++q) v[q] = v[q] - tb.tm[q] * c;
+        }
+        store(sl, b0, v);
+    }
+}
+
 template <typename T, int P, int E, bool COMP, bool LEAN = false>
 __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P, E, COMP, LEAN>::MINB)
     stage3r_kernel(StageArgs<T> a, Tab<T, P> tb) {
@@ -345,36 +412,10 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
         }
         // ---- truncation along x, then y, in shared memory
         if (a.truncate) {
-#pragma unroll
-            for (int d = 0; d < 2; ++d) {
-                const int lb = d == 0 ? l0 : l1;
-                const int ls = d == 0 ? 1 : LX;
-#pragma unroll
-                for (int e = 0; e < E; ++e) {
-                    const int b0 = lb + e * P1 * ls;
-                    T v[P1];
-                    T c = T(0);
-#pragma unroll
-                    for (int q = 0; q < P1; ++q) { v[q] = sl[b0 + q * ls]; c += tb.td[q] * v[q]; }
-                    if (final_comp) {
-                        T cc = T(0);
-#pragma unroll
-                        for (int q = 0; q < P1; ++q) cc += tb.td[q] * sc[b0 + q * ls];
-                        c += cc;
-#pragma unroll
-                        for (int q = 0; q < P1; ++q) {
-                            T s, err;
-                            two_sum(v[q], -(tb.tm[q] * c), s, err);
-                            sl[b0 + q * ls] = s;
-                            sc[b0 + q * ls] += err;
-                        }
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < P1; ++q) sl[b0 + q * ls] = v[q] - tb.tm[q] * c;
-                    }
-                }
-                __syncthreads();
-            }
+            truncate_lines<T, P, E, (P1 % VW == 0)>(tb, sl, sc, l0, 1, final_comp);
+            __syncthreads();
+            truncate_lines<T, P, E, false>(tb, sl, sc, l1, LX, final_comp);
+            __syncthreads();
         }
         // ---- the new v of the column (and in stage 4 its u)
 #pragma unroll
