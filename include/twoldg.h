@@ -264,6 +264,81 @@ int twoldg_synchronize(twoldg_problem* p);
  * Asynchronous on `stream` (a cudaStream_t; NULL is the default stream). */
 int twoldg_rhs_static(const twoldg_desc* desc, void* du, const void* u, double t, void* stream);
 
+/* ---- The particle-grid transfer (src/transfer.jl) ----
+ *
+ * project_source!(du, p, t, S, particles; ball, rnear, factor, var) --
+ * src/transfer.jl:918-944: du[var] += factor (P S), (P S)_n = (1/w_n)
+ * int_{element(n)} S phi_n, over the elements of the blocks that the
+ * source's ball meets. Elements within rnear h_e of a particle take the
+ * nested rule split at its support (Gauss inside, Johnston and Elliott's sinh
+ * rule outside, src/transfer.jl:343-455), those within rfar h_e a graded
+ * tensor Gauss rule (band by distance, :107-170), the rest the far tensor
+ * Gauss rule of q = P + 3 points (:520-680). The host plans the elements and
+ * the nested rule's points (projection_plan, host_elements and
+ * nested_points, :984-1022, :1257-1285, :1380-1415); the device evaluates
+ * and contracts. The reference's device hook for the source evaluation,
+ * launch_points! (ext/TreeWaveOLDGCUDAExt.jl:23-30, src/transfer.jl:636),
+ * runs a user closure at every point: here the caller either evaluates S
+ * itself at the points twoldg_transfer_points lists and passes the values
+ * (twoldg_project_values), or takes the built-in particle density
+ * (twoldg_project_density, particle_density, src/particle.jl:117-127). */
+typedef struct twoldg_particle {
+    double z[3];       /* centre, physical coordinates */
+    double v[3];       /* velocity, |v| < 1 */
+    double ell;        /* size: the support is |L(v)(x - z)| <= ell */
+    double charge;     /* Q of the built-in density source */
+} twoldg_particle;
+
+typedef struct twoldg_transfer_desc {
+    const double* origins;   /* nblocks x dim: each block's origin in the particles' frame
+                                (physical coordinates; ParticleFrame, src/transfer.jl:705-766) */
+    const double* spacings;  /* nblocks: each block's node spacing in that frame */
+    const int32_t* levels;   /* nblocks: refinement levels (the finest-level checks), or NULL */
+    const uint8_t* mask;     /* nblocks: 1 for a block of the frame's patch, or NULL for all */
+    double h_e;              /* the finest element width in that frame (frame_he) */
+    double ball_centre[3];   /* the source's ball: elements that miss it are skipped */
+    double ball_radius;
+    const twoldg_particle* particles;  /* at most 8 */
+    int32_t nparticles;
+    double rnear;            /* nested rule within rnear h_e (0 <= rnear <= rfar) */
+    /* the quadrature; 0 (or NULL) takes the reference's defaults
+     * (TransferTables, src/transfer.jl:139-170) */
+    int32_t q;               /* far rule points per dimension: P + 3 */
+    int32_t nsinh, nmid, ninner;       /* 48, 16, 24 */
+    int32_t nbands;                    /* graded bands: 4 */
+    const double* band_from;           /* (1, 2, 3, 4) h_e */
+    const int32_t* band_points;        /* (14, 10, 8, 7) */
+    double rfar;                       /* 9 h_e */
+} twoldg_transfer_desc;
+
+typedef struct twoldg_transfer_plan twoldg_transfer_plan;
+
+/* Plans a projection onto problem p's state (flat layout, dim 1..3): checks
+ * the refusals of the reference (rnear outside [0, rfar], two supports in one
+ * element, the ball or a support on a level below the finest), classifies the
+ * elements and lists the nested rule's points. Synchronous. */
+int twoldg_transfer_plan_create(twoldg_problem* p, const twoldg_transfer_desc* desc, twoldg_transfer_plan** out);
+int twoldg_transfer_plan_destroy(twoldg_transfer_plan* plan);
+/* counts[8]: far elements, far points, graded elements, graded points,
+ * near elements, near points, near chunks, all points. */
+int twoldg_transfer_plan_counts(const twoldg_transfer_plan* plan, int64_t* counts);
+/* Every point the plan evaluates S at, as (dim, npoints) in the field type,
+ * into the device array xs: the far and graded elements' Gauss points
+ * element by element (dimension 1 fastest), then the nested rule's points.
+ * Asynchronous on the problem's stream. */
+int twoldg_transfer_points(twoldg_transfer_plan* plan, void* xs);
+/* du[var] += factor P S with S's values at the listed points (a device
+ * array of the field type, npoints long); var 1 (u) or 2 (v). Asynchronous. */
+int twoldg_project_values(twoldg_transfer_plan* plan, const void* values, void* du, double factor, int32_t var);
+/* The same with S the particles' density sum_k Q_k rho0(|L(v_k)(x - z_k)|),
+ * evaluated on the device (dim 3). Asynchronous. */
+int twoldg_project_density(twoldg_transfer_plan* plan, void* du, double factor, int32_t var);
+/* A transfer table of order P in float64 (precision 0) or float32 (1):
+ * "bary" (P+1), and of the q-point Gauss-Legendre rule "gauss_nodes" (q),
+ * "gauss_weights" (q), "lagrange" (q x (P+1)), "contract" ((P+1) x q); built
+ * in double-double and rounded once (TransferTables, src/transfer.jl:139-170). */
+int twoldg_transfer_table(int32_t order, int32_t precision, const char* name, int32_t q, void* out);
+
 /* Batched ensemble: n independent problems stepped together, the blocks of
  * all of them as one work list per (dim, order, elems) group and one RK4
  * step per CUDA graph launch. No reference counterpart (the reference runs

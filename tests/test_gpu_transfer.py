@@ -1,0 +1,293 @@
+"""The particle-grid transfer on the GPU, through the C ABI: the projection
+of the particles' density and of a caller's source against the oracle, and
+the reference's own assertions (test/transfer_tests.jl) through the device:
+the nested rule integrates a particle to 1e-12 at any size and speed, the
+projection is consistent at order P and adjoint to the reconstruction, and
+it does not jump as a particle crosses r_near or a face."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import transfer as T
+from transfer_cases import exact_moment, irregular, poly, reference_integral
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(D, P, roots, dtype=np.float64, E=2):
+    import twoldg
+    f = twoldg.wave_forest(dtype, D, P, E, roots=roots)
+    return twoldg.WaveProblem(f, twoldg.Element(dtype, P))
+
+
+def _mesh(p):
+    """The oracle's view of problem p's forest, in the state's block order."""
+    f = p.forest
+    origins = [[f.block_extent(k)[d][0] for d in range(p.D)] for k in f.leaves]
+    spacings = [f.spacing(k) for k in f.leaves]
+    return T.Mesh(origins, spacings, p.P, p.E)
+
+
+def _node_weights(p):
+    """w_n of every node of the state vector, for var 1 and var 2 alike."""
+    P1 = p.P + 1
+    w1 = np.tile(T.Tables(p.P).weights, p.E)
+    out = np.empty((p.nblocks, p.NN))
+    for b, k in enumerate(p.forest.leaves):
+        h = p.forest.spacing(k)
+        w = np.ones(1)
+        for _ in range(p.D):
+            w = ((w1 * h * P1 / 2)[:, None] * w[None, :]).reshape(-1)
+        out[b] = w
+    return np.repeat(out[:, None, :], 2, axis=1).reshape(-1)
+
+
+def _inner(p, a, b, var):
+    w = _node_weights(p).reshape(p.nblocks, 2, p.NN)[:, var - 1]
+    a = np.asarray(a, dtype=np.float64).reshape(p.nblocks, 2, p.NN)[:, var - 1]
+    b = np.asarray(b, dtype=np.float64).reshape(p.nblocks, 2, p.NN)[:, var - 1]
+    return float(np.sum(w * a * b))
+
+
+def _host(u):
+    return u.double().cpu().numpy()
+
+
+def test_density_projection_matches_the_oracle(native):
+    from twoldg import ParticleSupport, project_source
+    D, P = 3, 3
+    p = _problem(D, P, 2)
+    z = np.array([0.53, 0.47, 0.51])
+    v = np.array([0.1, -0.15, 0.05])
+    ell, Q = 0.02, 0.3
+    ball = (z, 0.45)
+    du = p.statevector()
+    project_source(du, p, "density", [ParticleSupport(z, v, ell, charge=Q)], ball, rnear=1.0, factor=0.7, var=2)
+    got = _host(du)
+    ref = T.project_source(np.zeros(p.state_words), _mesh(p), T.Tables(P),
+                           lambda X: T.particle_density(X, z, v, ell, Q), [T.Support(z, v, ell)], ball,
+                           rnear=1.0, factor=0.7, var=2, he=0.25)
+    assert np.abs(ref).max() > 0
+    assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+    assert np.all(got.reshape(p.nblocks, 2, -1)[:, 0] == 0)
+
+
+@pytest.mark.parametrize("D,P", [(1, 3), (2, 2), (3, 3)])
+def test_caller_source_projection_matches_the_oracle(native, D, P):
+    # the source of test/transfer_tests.jl:295-328, evaluated by the caller
+    # at the plan's points (the launch_points! role)
+    import torch
+    from twoldg import ParticleSupport, TransferPlan
+    p = _problem(D, P, 2)
+    z = np.array([0.5 + 0.03 * (d + 1) for d in range(D)])
+    v = np.array([0.1 / (d + 1) for d in range(D)])
+    s = ParticleSupport(z, v, 0.01)
+    rnear = 1.5 if D < 3 else 1.0
+    plan = TransferPlan(p, [s], (z, 1.0), rnear)
+    assert plan.counts["near_elements"] > 2 ** D
+
+    zt = torch.tensor(z, dtype=torch.float64, device="cuda")
+
+    def S(xs):
+        return 1 / (((xs - zt[:, None]) ** 2).sum(0) + 1e-4) + xs[0]
+
+    du = p.statevector()
+    plan.project(du, S, factor=1.0, var=2)
+    got = _host(du)
+
+    def Sn(X):
+        return 1 / (np.sum((X - z[None, :]) ** 2, axis=1) + 1e-4) + X[:, 0]
+
+    ref = T.project_source(np.zeros(p.state_words), _mesh(p), T.Tables(P), Sn, [T.Support(z, v, 0.01)], (z, 1.0),
+                           rnear=rnear, factor=1.0, var=2)
+    assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("ratio", [1e-1, 1e-2, 1e-3, 1e-4])
+@pytest.mark.parametrize("moving", [False, True])
+def test_near_rule_integrates_the_particle_at_any_size(native, ratio, moving):
+    # test/transfer_tests.jl:172-214 through the device
+    from twoldg import ParticleSupport, TransferPlan
+    p = _problem(3, 3, 1)
+    he = 0.5
+    ell = ratio * he
+    Q = 1e-3
+    v = np.array([0.1, -0.15, 0.05]) if moving else np.zeros(3)
+    z = np.array([0.5, 0.5, 0.5]) + ell * np.array([0.3, -0.2, 0.1])
+    plan = TransferPlan(p, [ParticleSupport(z, v, ell, charge=Q)], (z, 2 * ell))
+    assert plan.counts["near_elements"] == 8 and plan.counts["far_elements"] == 0
+    du = p.statevector()
+    plan.project(du, "density", factor=1.0, var=1)
+    got = _host(du)
+    gamma = 1 / math.sqrt(1 - v @ v)
+    assert _inner(p, got, np.ones_like(got), 1) == pytest.approx(Q / gamma, rel=1e-12)
+    g = p.fill_at_nodes(lambda x, var: poly(np.stack([x[0].reshape(-1), x[1].reshape(-1), x[2].reshape(-1)],
+                                                     axis=1)).reshape(x[0].shape)).reshape(-1)
+    assert _inner(p, got, g, 1) == pytest.approx(exact_moment(poly, Q, ell, z, v), rel=1e-12)
+
+
+def test_float32_density_keeps_the_charge(native):
+    from twoldg import ParticleSupport, project_source
+    p = _problem(3, 3, 1, dtype=np.float32)
+    ell, Q = 5e-3, 1e-3
+    v = np.array([0.1, -0.15, 0.05])
+    z = np.array([0.5, 0.5, 0.5]) + ell * np.array([0.3, -0.2, 0.1])
+    du = p.statevector()
+    project_source(du, p, "density", [ParticleSupport(z, v, ell, charge=Q)], (z, 2 * ell), factor=1.0, var=1)
+    got = _host(du)
+    gamma = 1 / math.sqrt(1 - v @ v)
+    assert _inner(p, got, np.ones_like(got), 1) == pytest.approx(Q / gamma, rel=1e-5)
+
+
+def _projection_error(D, P, roots):
+    import torch
+    from twoldg import project_source
+    p = _problem(D, P, roots)
+
+    def S(xs):
+        out = torch.sin(2 * math.pi * xs[0])
+        for d in range(1, D):
+            out = out * torch.cos(2 * math.pi * xs[d])
+        return out + 0.3
+
+    du = p.statevector()
+    project_source(du, p, S, [], (np.full(D, 0.5), 2.0), factor=1.0)
+
+    def Sn(x, var):
+        out = np.sin(2 * np.pi * x[0])
+        for d in range(1, D):
+            out = out * np.cos(2 * np.pi * x[d])
+        return (out + 0.3) if var == 2 else 0 * out
+
+    err = _host(du) - p.fill_at_nodes(Sn).reshape(-1)
+    one = np.ones_like(err)
+    return math.sqrt(_inner(p, err, err, 2) / _inner(p, one, one, 2))
+
+
+def test_projection_is_consistent_at_order_P(native):
+    # test/transfer_tests.jl:108-133 through the device
+    for D, P in ((1, 2), (1, 3), (1, 4), (2, 2), (2, 3), (2, 4)):
+        errs = [_projection_error(D, P, r) for r in (2, 4, 8)]
+        rate = np.polyfit(np.log([1 / 2, 1 / 4, 1 / 8]), np.log(errs), 1)[0]
+        assert rate > P - 0.1, (D, P, errs)
+    e = [_projection_error(3, 2, r) for r in (2, 4)]
+    assert math.log2(e[0] / e[1]) > 2 - 0.2
+
+
+def test_projection_is_adjoint_to_the_reconstruction_2d(native):
+    # test/transfer_tests.jl:135-170, D = 2: <P S, g>_w = int S g_h for a bump
+    # straddling a face (the nested rule split at its support), a Lorentzian
+    # peak (the sinh rule) and a smooth part (the far rule)
+    import torch
+    from twoldg import ParticleSupport, project_source
+    D, roots, eps, grades, tol = 2, 4, 0.1, range(-10, 5), 1e-12
+    P = 3
+    p = _problem(D, P, roots)
+    he = 1 / roots / 2
+    ell = 0.05 * he
+    z = np.array([0.5 + 0.3 * ell, 0.5 + 0.22 * he])
+    zt = torch.tensor(z, dtype=torch.float64, device="cuda")
+
+    def S(xs):
+        r2 = ((xs - zt[:, None]) ** 2).sum(0)
+        b = torch.where(r2 < ell * ell, (1 - r2 / ell ** 2) ** 4, torch.zeros_like(r2))
+        return torch.cos(xs[0]) + b / ell ** D + eps * he / (r2 + (eps * he) ** 2) ** 0.5
+
+    def Sn(X):
+        r2 = np.sum((X - z[None, :]) ** 2, axis=1)
+        return np.cos(X[:, 0]) + np.where(r2 < ell * ell, (1 - r2 / ell ** 2) ** 4, 0.0) / ell ** D + \
+            eps * he / (r2 + (eps * he) ** 2) ** 0.5
+
+    du = p.statevector()
+    project_source(du, p, S, [ParticleSupport(z, [0.0, 0.0], ell)], (z, 10.0), factor=1.0)
+    got = _host(du)
+    g = irregular(len(got))
+    lhs = _inner(p, got, g, 2)
+    mesh = _mesh(p)
+    t = T.Tables(P)
+    rhs = 0.0
+    for b in range(mesh.nblocks):
+        for J in np.ndindex(2, 2):
+            e = tuple(reversed(J))
+            lo, hi = mesh.element_box(b, e)
+            gv = g[mesh.node_index(b, e, 2)]
+            rhs += reference_integral(lambda X: Sn(X) * (t.element_basis(lo, hi, X) @ gv), lo, hi, z, ell, grades,
+                                      ell)
+    assert lhs == pytest.approx(rhs, rel=tol)
+
+
+def test_projection_does_not_jump_across_rnear_or_faces(native):
+    # test/transfer_tests.jl:281-293: a source that does not move, projected
+    # with a particle that does, stays put to 1e-12
+    import torch
+    from twoldg import ParticleSupport, project_source
+    p = _problem(3, 3, 1)
+    he = 0.5
+    ell = 1e-3
+
+    def S(xs):
+        return torch.cos(xs[0] - xs[1] / 2) * torch.exp(xs[2] / 2)
+
+    def project(z):
+        du = p.statevector()
+        project_source(du, p, S, [ParticleSupport(z, [0.0] * 3, ell)], ((0.5, 0.5, 0.5), 2.0), rnear=1.5,
+                       factor=1.0)
+        return _host(du)
+
+    base = project((5.0, 5.0, 5.0))
+    for z in ((0.5 + 1.5 * he + 1e-6, 0.3, 0.2), (0.5 + 1.5 * he - 1e-6, 0.3, 0.2), (0.5 - 0.3 * ell, 0.3, 0.2),
+              (0.5 + 0.3 * ell, 0.5 - 0.2 * ell, 0.2)):
+        assert np.abs(project(z) - base).max() < 1e-12 * np.abs(base).max()
+
+
+def test_points_are_the_rules_points(native):
+    from twoldg import ParticleSupport, TransferPlan
+    p = _problem(2, 3, 2)
+    z = np.array([0.52, 0.49])
+    plan = TransferPlan(p, [ParticleSupport(z, [0.0, 0.0], 0.01)], (z, 1.0))
+    xs = plan.points().double().cpu().numpy()
+    c = plan.counts
+    assert xs.shape == (2, c["points"])
+    assert c["points"] == c["far_points"] + c["graded_points"] + c["near_points"]
+    mesh = _mesh(p)
+    t = T.Tables(3)
+    far, graded, near = T.classify(mesh, t, [T.Support(z, np.zeros(2), 0.01)], (z, 1.0), 1.0, 0.25)
+    assert (len(far), sum(map(len, graded)), len(near)) == (c["far_elements"], c["graded_elements"],
+                                                           c["near_elements"])
+    # the first far element's Gauss points, dimension 0 fastest
+    if far:
+        b, e = far[0]
+        lo, hi = mesh.element_box(b, e)
+        x, _, _ = t.far
+        q = len(x)
+        for j in range(q * q):
+            j0, j1 = j % q, j // q
+            assert xs[0, j] == pytest.approx(lo[0] + (hi[0] - lo[0]) * (1 + x[j0]) / 2, abs=1e-15)
+            assert xs[1, j] == pytest.approx(lo[1] + (hi[1] - lo[1]) * (1 + x[j1]) / 2, abs=1e-15)
+    # the nested rule's points, element by element, as the oracle lists them
+    X = np.concatenate([T.nested_points(T.Support(z, np.zeros(2), 0.01), t, *mesh.element_box(b, e), 2)[0]
+                        for b, e, _ in near])
+    assert np.allclose(xs[:, c["far_points"] + c["graded_points"]:].T, X, rtol=0, atol=1e-15)
+
+
+def test_refusals(native):
+    import twoldg
+    from twoldg import ParticleSupport, TransferPlan
+    p = _problem(3, 3, 1)
+    s = ParticleSupport((0.5, 0.5, 0.5), (0, 0, 0), 1e-3)
+    with pytest.raises(ValueError, match="rnear"):
+        TransferPlan(p, [s], ((0.5,) * 3, 1.0), rnear=10.0)
+    a = ParticleSupport((0.26, 0.26, 0.26), (0, 0, 0), 0.02)
+    b = ParticleSupport((0.27, 0.27, 0.27), (0, 0, 0), 0.02)
+    with pytest.raises(ValueError, match="two particles"):
+        TransferPlan(p, [a, b], ((0.5,) * 3, 1.0))
+    with pytest.raises(ValueError, match="below 1"):
+        ParticleSupport((0.5,) * 3, (0.8, 0.7, 0.0), 1e-3)
+    # a ball that reaches a coarser block
+    f = twoldg.wave_forest(np.float64, 2, 3, 2, roots=2)
+    f.refine([f.leaves[0]])
+    q = twoldg.WaveProblem(f, twoldg.Element(np.float64, 3))
+    with pytest.raises(ValueError, match="finest level"):
+        TransferPlan(q, [], ((0.75, 0.75), 0.1))
+    TransferPlan(q, [], ((0.1, 0.1), 0.05)).close()

@@ -1,0 +1,190 @@
+"""The particle-grid transfer on the CPU: the library's tables against the
+512-bit fixture, the quadrature rules' own properties, and the oracle against
+the reference's assertions (test/transfer_tests.jl) where they are cheap."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import transfer as T
+from transfer_cases import exact_moment, irregular, poly, reference_integral
+
+
+def _lib_table(P, dtype, name, q=None):
+    from twoldg.transfer import transfer_table
+    return transfer_table(P, dtype, name, q)
+
+
+@pytest.mark.parametrize("kind", ["f64", "f32"])
+def test_tables_are_the_512_bit_ones_rounded_once(kind):
+    # test/transfer_tests.jl:78-106: every table is the BigFloat one rounded once
+    dt, it = (np.float64, np.uint64) if kind == "f64" else (np.float32, np.uint32)
+    for n in (1, 2, 5, 7, 8, 10, 12, 14, 16, 24, 48, 80):
+        for what in ("nodes", "weights"):
+            lib = _lib_table(1, dt, "gauss_" + what, n)
+            assert np.array_equal(lib.view(it), T.gauss_bits(n, what, kind)), (n, what)
+    for P in range(1, 7):
+        lib = _lib_table(P, dt, "bary")
+        assert np.array_equal(lib.view(it), T.fixture_table(P, "bary", kind).view(it))
+        for q in sorted({P + 3, 14, 10, 8, 7}):
+            for name in ("lagrange", "contract"):
+                lib = _lib_table(P, dt, name, q)
+                ref = T.fixture_table(P, "%s_%d" % (name, q), kind).reshape(lib.shape)
+                assert np.array_equal(lib.view(it), ref.view(it)), (P, q, name)
+
+
+def test_gauss_rules_are_exact_to_degree_2n_minus_1():
+    # test/transfer_tests.jl:82-90
+    for n in (1, 2, 5, 12):
+        x, w = T.gauss(n)
+        for k in range(2 * n):
+            assert abs(np.sum(w * x ** k) - (2 / (k + 1) if k % 2 == 0 else 0)) < 1e-14
+        assert np.sum(w * x ** (2 * n)) - 2 / (2 * n + 1) < -1e-10
+        assert np.array_equal(x, -x[::-1])
+
+
+def test_contraction_is_the_weighted_lagrange_table():
+    # test/transfer_tests.jl:100-105
+    P = 3
+    con = T.fixture_table(P, "contract_6").reshape(4, 6)
+    lag = T.fixture_table(P, "lagrange_6").reshape(6, 4)
+    gw = T.gauss(6)[1]
+    w = T.Tables(P).weights
+    for i in range(4):
+        for k in range(6):
+            assert con[i, k] == pytest.approx(gw[k] * lag[k, i] / w[i], rel=1e-15)
+
+
+def test_graded_rule_is_the_tensor_gauss_rule_contracted():
+    # test/transfer_tests.jl:330-346: contraction one dimension at a time
+    # against the tensor Gauss rule applied point by point with the basis
+    for D, P in ((1, 4), (2, 3), (3, 3)):
+        t = T.Tables(P)
+        g = t.graded[1]
+        lo = [0.1 * (d + 1) for d in range(D)]
+        hi = [x + 0.3 for x in lo]
+
+        def S(X):
+            out = np.exp(X[:, 0])
+            for d in range(D):
+                out = out * np.cos(3 * X[:, d] + d + 1)
+            return out
+
+        x, w, _ = g
+        grids = [lo[d] + 0.3 * (1 + x) / 2 for d in range(D)]
+        mesh = np.meshgrid(*grids, indexing="ij")
+        X = np.stack([m.reshape(-1) for m in mesh], axis=1)
+        W = np.ones(1)
+        for d in range(D):
+            W = (W[:, None] * (w * 0.15)[None, :]).reshape(-1)
+        ref = (W[:, None] * S(X)[:, None] * t.element_basis(lo, hi, X)).sum(axis=0) / t.element_weights(0.3, D)
+        got = T.tensor_rule(S, g, lo, hi, D)
+        assert np.allclose(got, ref, rtol=1e-14, atol=1e-14 * np.abs(ref).max())
+
+
+def _oracle_projection_error(D, P, roots):
+    mesh = T.brick_mesh(D, P, 2, roots)
+    t = T.Tables(P)
+
+    def S(X):
+        out = np.sin(2 * np.pi * X[:, 0])
+        for d in range(1, D):
+            out = out * np.cos(2 * np.pi * X[:, d])
+        return out + 0.3
+
+    du = np.zeros(mesh.nblocks * 2 * mesh.NN)
+    T.project_source(du, mesh, t, S, [], (np.full(D, 0.5), 2.0), factor=1.0)
+    ref = np.zeros_like(du)
+    nodes = t.nodes
+    for b in range(mesh.nblocks):
+        for J in np.ndindex(*([2] * D)):
+            e = tuple(reversed(J))
+            lo, hi = mesh.element_box(b, e)
+            grids = [lo[d] + (hi[d] - lo[d]) * (1 + nodes) / 2 for d in range(D)]
+            m = np.meshgrid(*grids, indexing="ij")
+            X = np.stack([a.reshape(-1) for a in m], axis=1)
+            vals = S(X).reshape((P + 1,) * D)
+            ref[mesh.node_index(b, e, 2)] = np.transpose(vals, tuple(range(D - 1, -1, -1))).reshape(-1)
+    err = du - ref
+    return math.sqrt(T.weighted_inner(mesh, t, err, err, 2) / T.weighted_inner(mesh, t, np.ones_like(du),
+                                                                               np.ones_like(du), 2))
+
+
+def test_oracle_projection_is_consistent_at_order_P():
+    # test/transfer_tests.jl:108-133: (P S)_n - S(x_n) falls at the scheme's order
+    for D, P in ((1, 2), (1, 3), (1, 4), (2, 2), (2, 3), (2, 4)):
+        errs = [_oracle_projection_error(D, P, r) for r in (2, 4, 8)]
+        rate = np.polyfit(np.log([1 / 2, 1 / 4, 1 / 8]), np.log(errs), 1)[0]
+        assert rate > P - 0.1, (D, P, errs)
+    e = [_oracle_projection_error(3, 2, r) for r in (2, 4)]
+    assert math.log2(e[0] / e[1]) > 2 - 0.2
+
+
+def test_oracle_near_rule_integrates_the_particle():
+    # test/transfer_tests.jl:172-214, one moving case: the nested rule split
+    # at the support gives Q / gamma and the polynomial moment to 1e-12
+    mesh = T.brick_mesh(3, 3, 2, 1)
+    t = T.Tables(3)
+    he = 0.5
+    ell = 1e-2 * he
+    Q = 1e-3
+    v = np.array([0.1, -0.15, 0.05])
+    z = np.array([0.5, 0.5, 0.5]) + ell * np.array([0.3, -0.2, 0.1])
+    s = T.Support(z, v, ell)
+    du = np.zeros(mesh.nblocks * 2 * mesh.NN)
+    T.project_source(du, mesh, t, lambda X: T.particle_density(X, z, v, ell, Q), [s], (z, 2 * ell),
+                     factor=1.0, var=1, he=he)
+    gamma = 1 / math.sqrt(1 - v @ v)
+    one = np.ones_like(du)
+    assert T.weighted_inner(mesh, t, du, one, 1) == pytest.approx(Q / gamma, rel=1e-12)
+    # g = poly at the nodes
+    g = np.zeros_like(du)
+    for b in range(mesh.nblocks):
+        for J in np.ndindex(2, 2, 2):
+            e = tuple(reversed(J))
+            lo, hi = mesh.element_box(b, e)
+            grids = [lo[d] + (hi[d] - lo[d]) * (1 + t.nodes) / 2 for d in range(3)]
+            m = np.meshgrid(*grids, indexing="ij")
+            X = np.stack([a.reshape(-1) for a in m], axis=1)
+            g[mesh.node_index(b, e, 1)] = np.transpose(poly(X).reshape(4, 4, 4), (2, 1, 0)).reshape(-1)
+    assert T.weighted_inner(mesh, t, du, g, 1) == pytest.approx(exact_moment(poly, Q, ell, z, v), rel=1e-12)
+    # the adjoint pairing over the support's elements, compact (src/transfer.jl:1779-1815)
+    acc = 0.0
+    for b in range(mesh.nblocks):
+        for J in np.ndindex(2, 2, 2):
+            e = tuple(reversed(J))
+            lo, hi = mesh.element_box(b, e)
+            gv = g[mesh.node_index(b, e, 1)]
+            acc += T.nested_rule(lambda X: T.particle_density(X, z, v, ell, Q) * (t.element_basis(lo, hi, X) @ gv),
+                                 s, t, lo, hi, 3, compact=True)
+    assert acc == pytest.approx(exact_moment(poly, Q, ell, z, v), rel=1e-12)
+
+
+def test_oracle_projection_is_adjoint_to_the_reconstruction_1d():
+    # test/transfer_tests.jl:135-170, D = 1: <P S, g>_w = int S g_h for a
+    # bump straddling a face, a Lorentzian peak and a smooth part
+    D, roots, eps, grades, tol = 1, 8, 0.1, range(-12, 7), 1e-13
+    P = 3
+    mesh = T.brick_mesh(D, P, 2, roots)
+    t = T.Tables(P)
+    he = 1 / roots / 2
+    ell = 0.05 * he
+    z = np.array([0.5 + 0.3 * ell])
+
+    def S(X):
+        r2 = np.sum((X - z[None, :]) ** 2, axis=1)
+        return np.cos(X[:, 0]) + np.where(r2 < ell * ell, (1 - r2 / ell ** 2) ** 4, 0.0) / ell ** D + \
+            eps * he / (r2 + (eps * he) ** 2) ** 0.5
+
+    du = np.zeros(mesh.nblocks * 2 * mesh.NN)
+    T.project_source(du, mesh, t, S, [T.Support(z, np.zeros(1), ell)], (z, 10.0), factor=1.0)
+    g = irregular(len(du))
+    lhs = T.weighted_inner(mesh, t, du, g, 2)
+    rhs = 0.0
+    for b in range(mesh.nblocks):
+        for e in ((0,), (1,)):
+            lo, hi = mesh.element_box(b, e)
+            gv = g[mesh.node_index(b, e, 2)]
+            rhs += reference_integral(lambda X: S(X) * (t.element_basis(lo, hi, X) @ gv), lo, hi, z, ell,
+                                      grades, ell)
+    assert lhs == pytest.approx(rhs, rel=tol)

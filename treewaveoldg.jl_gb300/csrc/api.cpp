@@ -737,6 +737,23 @@ struct twoldg_problem : twoldg_runner {
 
 struct twoldg_batch : twoldg_runner {};
 
+namespace twoldg {
+// A problem's shape, precision (0: float64 fields, 1: float32), block count and
+// stream, for the transfer's plans (transfer.cpp).
+bool problem_shape(twoldg_problem* p, int* D, int* P, int* E, int* prec, int64_t* nblocks, cudaStream_t* stream) {
+    if (!p) return false;
+    *D = p->D;
+    *P = p->P;
+    *E = p->E;
+    *prec = p->prec == TWOLDG_F64 ? 0 : 1;
+    int64_t NN = 1;
+    for (int d = 0; d < p->D; ++d) NN *= (int64_t)p->E * (p->P + 1);
+    *nblocks = p->total_words / (2 * NN);
+    *stream = p->stream;
+    return true;
+}
+}  // namespace twoldg
+
 extern "C" {
 
 const char* twoldg_last_error(void) { return g_err.c_str(); }

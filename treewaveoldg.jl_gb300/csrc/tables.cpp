@@ -156,4 +156,97 @@ bool build_tables(int P, ElementTables<double>& f64, ElementTables<float>& f32) 
     return true;
 }
 
+namespace {
+
+// Gauss-Legendre nodes (ascending) and weights of n points
+// (src/transfer.jl:44-62): Newton's iteration on L_n from the Chebyshev
+// points -cos(pi (4i - 1) / (4n + 2)), then symmetrised so that
+// x[i] == -x[n-1-i] holds after any rounding; w = 2 / ((1 - x^2) L_n'(x)^2).
+void gauss_legendre(int n, std::vector<dd>& x, std::vector<dd>& w) {
+    const double pi = 3.14159265358979323846;
+    x.assign(n, dd());
+    for (int i = 1; i <= n; ++i) x[i - 1] = dd(-std::cos(pi * (4.0 * i - 1) / (4.0 * n + 2)));
+    auto value_and_slope = [&](dd t, dd& L, dd& dL) {
+        std::vector<dd> all = legendre_all(n, t);
+        L = all[n];
+        dL = dd((double)n) * (t * all[n] - all[n - 1]) / (t * t - dd(1.0));
+    };
+    for (int it = 0; it < 200; ++it) {
+        double worst = 0;
+        std::vector<dd> delta(n);
+        for (int i = 0; i < n; ++i) {
+            dd L, dL;
+            value_and_slope(x[i], L, dL);
+            delta[i] = L / dL;
+            worst = std::fmax(worst, std::fabs(delta[i].hi));
+        }
+        for (int i = 0; i < n; ++i) x[i] = x[i] - delta[i];
+        if (worst <= 1e-31) break;
+    }
+    std::vector<dd> s(n);
+    for (int i = 0; i < n; ++i) s[i] = (x[i] - x[n - 1 - i]) / dd(2.0);
+    x = s;
+    w.assign(n, dd());
+    for (int i = 0; i < n; ++i) {
+        dd L, dL;
+        value_and_slope(x[i], L, dL);
+        w[i] = dd(2.0) / ((dd(1.0) - x[i] * x[i]) * dL * dL);
+    }
+}
+
+std::vector<dd> bary_dd(const std::vector<dd>& xi) {
+    const int P1 = (int)xi.size();
+    std::vector<dd> b(P1);
+    for (int i = 0; i < P1; ++i) {
+        dd p(1.0);
+        for (int j = 0; j < P1; ++j)
+            if (j != i) p = p * (xi[i] - xi[j]);
+        b[i] = dd(1.0) / p;
+    }
+    return b;
+}
+
+}  // namespace
+
+bool build_rule(int P, int q, RuleTables<double>& f64, RuleTables<float>& f32) {
+    if (P < 1 || P > kMaxP || q < 1 || q > kMaxRule) return false;
+    const int P1 = P + 1;
+    std::vector<dd> xi, wh, xg, wg;
+    gll(P, xi, wh);
+    gauss_legendre(q, xg, wg);
+    const std::vector<dd> bary = bary_dd(xi);
+    std::vector<dd> lag(q * P1), con(P1 * q);
+    for (int k = 0; k < q; ++k)
+        for (int i = 0; i < P1; ++i) {
+            dd phi = bary[i];
+            for (int j = 0; j < P1; ++j)
+                if (j != i) phi = phi * (xg[k] - xi[j]);
+            lag[k * P1 + i] = phi;
+            con[i * q + k] = wg[k] * phi / wh[i];
+        }
+    auto put = [&](auto& t, auto conv) {
+        t.nodes.clear(); t.weights.clear(); t.lagrange.clear(); t.contract.clear();
+        for (auto& v : xg) t.nodes.push_back(conv(v));
+        for (auto& v : wg) t.weights.push_back(conv(v));
+        for (auto& v : lag) t.lagrange.push_back(conv(v));
+        for (auto& v : con) t.contract.push_back(conv(v));
+    };
+    put(f64, [](dd v) { return to_double(v); });
+    put(f32, [](dd v) { return to_float(v); });
+    return true;
+}
+
+bool build_bary(int P, std::vector<double>& f64, std::vector<float>& f32) {
+    if (P < 1 || P > kMaxP) return false;
+    std::vector<dd> xi, wh;
+    gll(P, xi, wh);
+    f64.clear();
+    f32.clear();
+    for (auto& v : bary_dd(xi)) {
+        f64.push_back(to_double(v));
+        f32.push_back(to_float(v));
+    }
+    return true;
+}
+
 }  // namespace twoldg

@@ -1,0 +1,94 @@
+// The particle-grid transfer's device passes: what the host plan hands the
+// kernels, and the launchers (transfer_kernels.cu) the host plan calls.
+//
+// The projection (P S)_n = (1/w_n) int_{element(n)} S phi_n runs three
+// rules (src/transfer.jl:1-35): the far rule and the graded bands are tensor
+// Gauss rules, one CTA per element evaluating S at its q^D points into shared
+// memory and contracting them there one dimension at a time (the reference's
+// two passes, source_points / contract, fused, so the points never reach
+// HBM); the nested rule near a particle runs over the point list the host
+// made, in chunks of at most kNearChunk points per element, whose per-node
+// partial sums are then added in order.
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace twoldg {
+
+constexpr int kNearChunk = 256;
+constexpr int kMaxParticles = 8;
+
+// One particle of the built-in density source rho(x) = Q rho0(|L(v)(x - z)|^2,
+// ell) (src/particle.jl:117-127), with the boost's g = gamma^2 / (gamma + 1).
+struct TransferParticle {
+    double z[3], v[3], ell, charge, g;
+};
+
+// A tensor rule element (far or graded): its block, its element index per
+// dimension, its rule and where its points' values start.
+struct RuleElement {
+    int32_t block, e[3], rule, pad;
+    int64_t base;
+};
+
+// A near element: block, element, its chunks [c0, c1), its points from `base`.
+struct NearElement {
+    int32_t block, e[3], c0, c1;
+};
+
+// A chunk of near points [p0, p1) of near element `elem`.
+struct NearChunk {
+    int32_t p0, p1, elem, pad;
+};
+
+enum { SOURCE_VALUES = 0, SOURCE_DENSITY = 1 };
+
+// Everything the kernels read, device pointers in the field type T
+// (`prec` 0: double, 1: float).
+struct TransferLaunch {
+    int prec = 0, D = 3, P = 3, E = 2, N = 8;
+    int64_t NN = 0;             // N^D
+    const void* origins = nullptr;   // nblocks x D, T
+    const void* spacings = nullptr;  // nblocks, T
+    // tensor rules: per rule its q, the offset of its nodes (q) and of its
+    // contraction ((P+1) x q) in `tables`
+    int nrules = 0;
+    int rule_q[16] = {0};
+    int rule_nodes[16] = {0};
+    int rule_contract[16] = {0};
+    int max_q = 0;
+    const void* tables = nullptr;    // T
+    const RuleElement* rule_elems = nullptr;
+    int64_t n_rule_elems = 0;
+    // nested rule
+    const void* near_xs = nullptr;   // npoints x D, T
+    const void* near_ws = nullptr;   // npoints, T
+    const NearChunk* chunks = nullptr;
+    int64_t n_chunks = 0;
+    const NearElement* near_elems = nullptr;
+    int64_t n_near_elems = 0;
+    int64_t near_base = 0;           // index of the first near point among all points
+    const void* bary = nullptr;      // P+1, T
+    const void* gll = nullptr;       // P+1 Gauss-Lobatto nodes, T
+    const void* wn = nullptr;        // (P+1)^D node weights of a finest element, T
+    void* partials = nullptr;        // n_chunks x (P+1)^D, T
+    // the source
+    int source = SOURCE_VALUES;
+    const void* values = nullptr;    // all points' values, T (SOURCE_VALUES)
+    int nparticles = 0;
+    TransferParticle particles[kMaxParticles];
+    // the output: du[var] += factor * P S
+    void* du = nullptr;
+    int var = 1;
+    double factor = 1.0;
+};
+
+// The projection's kernels on `stream`; returns the launch error, if any.
+cudaError_t launch_projection(const TransferLaunch& a, cudaStream_t stream);
+
+// Every point of the plan's rules, tensor rules first (element by element,
+// dimension 0 fastest), then the near points, as (D, npoints) in T.
+cudaError_t launch_points(const TransferLaunch& a, void* xs, int64_t npoints, cudaStream_t stream);
+
+}  // namespace twoldg

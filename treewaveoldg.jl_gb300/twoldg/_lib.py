@@ -21,6 +21,8 @@ EXPORTS = [
     "twoldg_synchronize", "twoldg_batch_create", "twoldg_batch_destroy", "twoldg_batch_offsets",
     "twoldg_batch_rk4_step", "twoldg_batch_synchronize", "twoldg_profile_step", "twoldg_stream",
     "twoldg_rhs_static", "twoldg_autotune", "twoldg_batch_autotune", "twoldg_transfer", "twoldg_gather",
+    "twoldg_transfer_plan_create", "twoldg_transfer_plan_destroy", "twoldg_transfer_plan_counts",
+    "twoldg_transfer_points", "twoldg_project_values", "twoldg_project_density", "twoldg_transfer_table",
 ]
 
 
@@ -44,6 +46,25 @@ class Desc(ctypes.Structure):
         ("fac_rmodes", ctypes.POINTER(ctypes.c_double)), ("fac_rduals", ctypes.POINTER(ctypes.c_double)),
         ("fac_aslot", ctypes.POINTER(ctypes.c_int32)), ("fac_aw", ctypes.POINTER(ctypes.c_double)),
         ("fac_achol", ctypes.POINTER(ctypes.c_double)), ("fac_ntab", ctypes.c_int32),
+    ]
+
+
+class Particle(ctypes.Structure):
+    """twoldg_particle."""
+    _fields_ = [("z", ctypes.c_double * 3), ("v", ctypes.c_double * 3), ("ell", ctypes.c_double),
+                ("charge", ctypes.c_double)]
+
+
+class TransferDesc(ctypes.Structure):
+    """twoldg_transfer_desc."""
+    _fields_ = [
+        ("origins", ctypes.POINTER(ctypes.c_double)), ("spacings", ctypes.POINTER(ctypes.c_double)),
+        ("levels", ctypes.POINTER(ctypes.c_int32)), ("mask", ctypes.POINTER(ctypes.c_uint8)),
+        ("h_e", ctypes.c_double), ("ball_centre", ctypes.c_double * 3), ("ball_radius", ctypes.c_double),
+        ("particles", ctypes.POINTER(Particle)), ("nparticles", ctypes.c_int32), ("rnear", ctypes.c_double),
+        ("q", ctypes.c_int32), ("nsinh", ctypes.c_int32), ("nmid", ctypes.c_int32), ("ninner", ctypes.c_int32),
+        ("nbands", ctypes.c_int32), ("band_from", ctypes.POINTER(ctypes.c_double)),
+        ("band_points", ctypes.POINTER(ctypes.c_int32)), ("rfar", ctypes.c_double),
     ]
 
 
@@ -93,6 +114,13 @@ def lib():
             "twoldg_gather": (ctypes.c_int, [vp, vp, i32, i64, i32, vp, vp, vp]),
             "twoldg_batch_autotune": (ctypes.c_int, [vp, vp, ctypes.POINTER(d), ctypes.c_char_p, ctypes.c_char_p,
                                                      ctypes.c_size_t]),
+            "twoldg_transfer_plan_create": (ctypes.c_int, [vp, ctypes.POINTER(TransferDesc), ctypes.POINTER(vp)]),
+            "twoldg_transfer_plan_destroy": (ctypes.c_int, [vp]),
+            "twoldg_transfer_plan_counts": (ctypes.c_int, [vp, ctypes.POINTER(i64)]),
+            "twoldg_transfer_points": (ctypes.c_int, [vp, vp]),
+            "twoldg_project_values": (ctypes.c_int, [vp, vp, vp, d, i32]),
+            "twoldg_project_density": (ctypes.c_int, [vp, vp, d, i32]),
+            "twoldg_transfer_table": (ctypes.c_int, [i32, i32, ctypes.c_char_p, i32, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
