@@ -56,13 +56,15 @@ def parse():
                          "a smaller m' for profiling)")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner (untimed, before the warm-up) and run the default launch layouts")
-    ap.add_argument("--workload", default="box256", choices=["box256", "nested", "c1", "ball", "ball13"],
+    ap.add_argument("--workload", default="box256", choices=["box256", "nested", "c1", "ball", "ball13", "transfer"],
                     help="box256: the 256^3 periodic box (the headline); nested: the 3D reflecting box with "
                          "three nested refinement levels (P=3, E=2, roots=8) and a Gaussian pulse; c1: the 2D "
                          "periodic P=4, E=2, roots=8 box to a quarter period at CFL 0.25; ball: the seven-patch "
                          "ball, P=3, E=2, roots=(4,4), plane wave with Dirichlet sphere, to t=6; ball13: the "
                          "reference's benchmark ball, thirteen patches, roots (4,4,44), E=4, P=3, Lc=4, Rm=12, "
-                         "R1=100, radiative sphere (19.1M nodes)")
+                         "R1=100, radiative sphere (19.1M nodes); transfer: the projection of two particles' "
+                         "density onto the nodes over the first run's window (box of side 5, h_e = 1/8, P=3, E=4, "
+                         "ell = 1e-3, R2 = 2.5)")
     return ap.parse_args()
 
 
@@ -437,6 +439,130 @@ def ball_benchmark(args, twoldg, torch):
     print(json.dumps(line))
 
 
+def transfer_setup(twoldg, T=np.float64, hdiv=8):
+    """The first run's transfer (bin/projection.jl, CODE.md "Quadrature"): two
+    opposite charges Q = +-sqrt(0.005), ell = 1e-3, on a circle of diameter 1
+    at v = 0.2, moved off the element corners by (0.31, 0.17, 0.43) h_e, in a
+    periodic box of side 5 with h_e = 1/hdiv, P = 3, E = 4; the source's ball
+    is the window's, R2 = 2.5 about the centre."""
+    roots = 5 * hdiv // 4
+    forest = twoldg.wave_forest(T, 3, 3, 4, roots=roots, L=5.0)
+    p = twoldg.WaveProblem(forest, twoldg.Element(T, 3))
+    he = 1.0 / hdiv
+    c = np.array([2.5, 2.5, 2.5])
+    off = np.array([0.31, 0.17, 0.43]) * he
+    q = math.sqrt(0.005)
+    parts = [twoldg.ParticleSupport(c + np.array([0.5, 0, 0]) + off, (0.0, 0.2, 0.0), 1e-3, charge=q),
+             twoldg.ParticleSupport(c - np.array([0.5, 0, 0]) + off, (0.0, -0.2, 0.0), 1e-3, charge=-q)]
+    return p, parts, (c, 2.5)
+
+
+def transfer_benchmark(args, twoldg, torch, record=True):
+    """Projections of the first run's two particles: the library's plan (host),
+    then K projections of their density (evaluated in the kernels) and of a
+    caller's values at the plan's points, each timed alone with CUDA events on
+    the library's stream and L2 flushed in between; the far rule's oracle on a
+    sample of elements for the CPU baseline."""
+    lib = twoldg._lib.lib()
+    p, parts, ball = transfer_setup(twoldg)
+    t0 = time.perf_counter()
+    plan = twoldg.TransferPlan(p, parts, ball)
+    plan_s = time.perf_counter() - t0
+    # the plan for moved particles, as an inspiral's right-hand side redoes it
+    # at every stage: the pair turned about the centre by 1e-3 rad per update
+    upd = []
+    for k in range(1, 8):
+        ang = 1e-3 * k
+        rot = np.array([[math.cos(ang), -math.sin(ang), 0], [math.sin(ang), math.cos(ang), 0], [0, 0, 1]])
+        moved = [twoldg.ParticleSupport(ball[0] + rot @ (np.array(s.z) - ball[0]), rot @ np.array(s.v), s.ell,
+                                        charge=s.charge) for s in parts]
+        t0 = time.perf_counter()
+        plan.update(moved)
+        upd.append(time.perf_counter() - t0)
+    plan.update(parts)
+    c = plan.counts
+    stream = torch.cuda.ExternalStream(lib.twoldg_stream(p.handle))
+    du = p.statevector()
+    xs = plan.points()
+    r = ((xs - 2.5) ** 2).sum(0).sqrt()
+    values = (torch.cos(3 * r) * torch.exp(-r)).contiguous()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    times = {"density": [], "values": []}
+    for kind in ("density", "values"):
+        for it in range(args.warmup + args.steps):
+            flush.fill_(float(it))
+            torch.cuda.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            if kind == "density":
+                twoldg._lib.check(lib.twoldg_project_density(plan._h, ctypes.c_void_p(du.data_ptr()), -1.0, 2))
+            else:
+                twoldg._lib.check(lib.twoldg_project_values(plan._h, ctypes.c_void_p(values.data_ptr()),
+                                                            ctypes.c_void_p(du.data_ptr()), -1.0, 2))
+            ev1.record(stream)
+            ev1.synchronize()
+            if it >= args.warmup:
+                times[kind].append(ev0.elapsed_time(ev1))
+    ms = {k: float(np.median(v)) for k, v in times.items()}
+    # algorithmic bytes of the values path: each point's value read once, the
+    # touched elements' nodes read and written, the nested rule's points and
+    # weights read
+    M = 64
+    elems = c["far_elements"] + c["graded_elements"] + c["near_elements"]
+    alg = 8 * c["points"] + 2 * 8 * M * elems + 4 * 8 * c["near_points"]
+    hbm, peak_kind = peaks()
+    out = {"workload": "first-run window: 2 particles (Q = +-sqrt(0.005), ell = 1e-3, v = 0.2, off the corners), "
+                       "box of side 5, h_e = 1/8, P=3, E=4 (%d blocks of 16^3), ball R2 = 2.5" % p.nblocks,
+           "counts": c, "plan_ms": plan_s * 1e3, "plan_update_ms": float(np.median(upd)) * 1e3,
+           "host_threads": os.cpu_count(), "projection_ms": ms,
+           "points_per_s": {k: c["points"] / (v / 1e3) for k, v in ms.items()},
+           "values_roofline": {"bound": "hbm", "achieved": alg / (ms["values"] / 1e3) / 1e9, "peak": hbm,
+                               "unit": "GB/s", "frac": alg / (ms["values"] / 1e3) / 1e9 / hbm,
+                               "algorithmic_bytes": alg, "peak_kind": peak_kind},
+           "gpu_launches_per_projection": 3}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = transfer_cpu_sample(p, parts, ball, plan)
+    plan.close()
+    return out
+
+
+def transfer_cpu_sample(p, parts, ball, plan):
+    """The oracle's projection of the same density on a sample (200 far-rule
+    elements and one nested-rule element, the particle's own), scaled by the
+    plan's element counts to one projection; one host thread."""
+    from oracle import transfer as OT
+    f = p.forest
+    mesh = OT.Mesh([[f.block_extent(k)[d][0] for d in range(3)] for k in f.leaves],
+                   [f.spacing(k) for k in f.leaves], 3, 4)
+    t = OT.Tables(3)
+
+    def S(X):
+        return sum(OT.particle_density(X, s.z, s.v, s.ell, s.charge) for s in parts)
+
+    blocks = list(range(mesh.nblocks))[::97][:8]
+    elems = [(b, e) for b in blocks for e in [(0, 0, 0), (1, 2, 3), (3, 3, 3), (2, 1, 0)]]
+    elems = (elems * 8)[:200]
+    t0 = time.perf_counter()
+    for b, e in elems:
+        lo, hi = mesh.element_box(b, e)
+        OT.tensor_rule(S, t.far, lo, hi, 3)
+    far_s = (time.perf_counter() - t0) / len(elems)
+    s0 = parts[0]
+    he = 0.125
+    lo = [math.floor(s0.z[d] / he) * he for d in range(3)]
+    hi = [x + he for x in lo]
+    sup = OT.Support(s0.z, s0.v, s0.ell)
+    t0 = time.perf_counter()
+    OT.nested_rule(lambda X: S(X)[:, None] * t.element_basis(lo, hi, X), sup, t, lo, hi, 3)
+    near_s = time.perf_counter() - t0
+    c = plan.counts
+    total = far_s * (c["far_elements"] + c["graded_elements"]) + near_s * c["near_elements"]
+    return {"value": 1.0 / total, "unit": "projections/s", "cores": 1, "kind": "port",
+            "sample": "the oracle's far rule on 200 elements and its nested rule on the particle's own element, "
+                      "scaled by the plan's counts (far and graded elements at the far rule's cost, near elements "
+                      "at the particle's element's)", "seconds_per_projection": total}
+
+
 # --- multi-rank plumbing (replicas) -------------------------------------------
 _dist = None
 
@@ -549,6 +675,20 @@ def main():
         return
     if WORKLOAD == "ball13":
         ball_benchmark(args, twoldg, torch)
+        return
+    if WORKLOAD == "transfer":
+        tr = transfer_benchmark(args, twoldg, torch)
+        ms = tr["projection_ms"]["values"]
+        line = {"metric": "projections/s (a caller's source at every point of the first run's window: 10.95M "
+                          "points, far, graded and nested rules)",
+                "value": 1e3 / ms, "unit": "projections/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": tr["workload"], "l2_flush": "64 MB written between "
+                                                "projections"},
+                "transfer": tr, "roofline": tr["values_roofline"], "gpu_launches": 3 * args.steps}
+        if "cpu_baseline" in tr:
+            line["cpu_baseline"] = tr["cpu_baseline"]
+        print(json.dumps(line))
         return
     arms = {}
     wanted = args.arms.split(",")

@@ -318,6 +318,13 @@ typedef struct twoldg_transfer_plan twoldg_transfer_plan;
  * element, the ball or a support on a level below the finest), classifies the
  * elements and lists the nested rule's points. Synchronous. */
 int twoldg_transfer_plan_create(twoldg_problem* p, const twoldg_transfer_desc* desc, twoldg_transfer_plan** out);
+/* The same plan for new particle positions (and count, at most 8): the
+ * ball, the frame and the quadrature are kept, as the reference's SourceBall
+ * keeps them (src/transfer.jl:946-982), and only what the positions decide
+ * -- the elements by rule and the nested rule's points -- is redone, into the
+ * plan's device buffers. Waits for the plan's earlier projections first.
+ * Synchronous. */
+int twoldg_transfer_plan_update(twoldg_transfer_plan* plan, const twoldg_particle* particles, int32_t nparticles);
 int twoldg_transfer_plan_destroy(twoldg_transfer_plan* plan);
 /* counts[8]: far elements, far points, graded elements, graded points,
  * near elements, near points, near chunks, all points. */

@@ -291,3 +291,48 @@ def test_refusals(native):
     with pytest.raises(ValueError, match="finest level"):
         TransferPlan(q, [], ((0.75, 0.75), 0.1))
     TransferPlan(q, [], ((0.1, 0.1), 0.05)).close()
+
+
+def test_first_run_plan_counts_match_the_oracle(native):
+    # the library's classification of the first run's window: the oracle's
+    # counts, which hold the reference's 31 102 far elements (CODE.md
+    # "Quadrature")
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from bench import transfer_setup
+    import twoldg
+    p, parts, ball = transfer_setup(twoldg)
+    plan = twoldg.TransferPlan(p, parts, ball)
+    c = plan.counts
+    assert c["far_elements"] == 31102 and c["graded_elements"] == 134 + 266 + 438 + 5240
+    assert c["near_elements"] == 44
+    assert c["far_points"] == 31102 * 216
+    assert c["graded_points"] == 134 * 14 ** 3 + 266 * 10 ** 3 + 438 * 8 ** 3 + 5240 * 7 ** 3
+    plan.close()
+
+
+def test_updated_plan_projects_as_a_fresh_one(native):
+    # the reference holds a projection through a kept SourceBall to a fresh
+    # one's bit for bit (CODE.md "What the projection reads of the forest is
+    # built once"): an updated plan, likewise, for the density and for values
+    import torch
+    from twoldg import ParticleSupport, TransferPlan
+    p = _problem(3, 3, 2)
+    ball = ((0.5, 0.5, 0.5), 0.6)
+    a = [ParticleSupport((0.41, 0.52, 0.47), (0.1, 0.0, 0.0), 0.02, charge=0.5),
+         ParticleSupport((0.7, 0.33, 0.61), (0.0, -0.2, 0.05), 0.015, charge=-0.5)]
+    b = [ParticleSupport((0.43, 0.51, 0.49), (0.1, 0.02, 0.0), 0.02, charge=0.5),
+         ParticleSupport((0.69, 0.35, 0.6), (0.0, -0.2, 0.05), 0.015, charge=-0.5)]
+
+    def S(xs):
+        return torch.cos(3 * xs[0]) * torch.exp(xs[1] - xs[2])
+
+    plan = TransferPlan(p, a, ball)
+    plan.update(b)
+    fresh = TransferPlan(p, b, ball)
+    assert plan.counts == fresh.counts
+    for src in ("density", S):
+        d1, d2 = p.statevector(), p.statevector()
+        plan.project(d1, src)
+        fresh.project(d2, src)
+        assert torch.equal(d1, d2)

@@ -188,3 +188,28 @@ def test_oracle_projection_is_adjoint_to_the_reconstruction_1d():
             rhs += reference_integral(lambda X: S(X) * (t.element_basis(lo, hi, X) @ gv), lo, hi, z, ell,
                                       grades, ell)
     assert lhs == pytest.approx(rhs, rel=tol)
+
+
+def first_run_window(he=0.125):
+    """The first run's particles and window at h_e = 1/8 (bin/projection.jl):
+    opposite charges on a circle of diameter 1 at v = 0.2, off the element
+    corners by (0.31, 0.17, 0.43) h_e, ell = 1e-3, in a box of side 5 (origin at a
+    corner), P = 3, E = 4, the window's ball R2 = 2.5 about the centre."""
+    c = np.array([2.5] * 3)
+    off = np.array([0.31, 0.17, 0.43]) * he
+    parts = [T.Support(c + np.array([0.5, 0, 0]) + off, [0, 0.2, 0], 1e-3),
+             T.Support(c - np.array([0.5, 0, 0]) + off, [0, -0.2, 0], 1e-3)]
+    n = int(round(5 / (4 * he)))
+    w = 5.0 / n
+    origins = [[c_[d] * w for d in range(3)] for c_ in [tuple(reversed(J)) for J in np.ndindex(n, n, n)]]
+    return T.Mesh(origins, [w / 16] * len(origins), 3, 4), parts, (c, 2.5)
+
+
+def test_first_run_window_has_the_reference_far_count():
+    # CODE.md "Quadrature": "of the first run's 31 102 [far elements] at
+    # h_e = d/8, off the grid" -- the classification by r_far = 9 h_e,
+    # r_near = h_e and the window's ball
+    mesh, parts, ball = first_run_window()
+    far, graded, near = T.classify(mesh, T.Tables(3), parts, ball, 1.0, 0.125)
+    assert len(far) == 31102
+    assert [len(g) for g in graded] == [134, 266, 438, 5240] and len(near) == 44

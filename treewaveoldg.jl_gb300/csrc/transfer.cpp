@@ -2,18 +2,25 @@
 // 1151-1285, 1380-1415): the refusals, the classification of the elements
 // of the blocks the source's ball meets into the far rule, the graded bands
 // and the nested rule, the nested rule's points (split at each particle's
-// support, Gauss inside, Johnston and Elliott's sinh rule outside), and the
-// C ABI over the kernels of transfer_kernels.cu. Positions, boxes and the
-// nested rule's points are formed in double and rounded once to the field
-// type when they are uploaded.
+// support, Gauss inside, Johnston and Elliott's sinh rule outside) in
+// innermost lines, and the C ABI over the kernels of transfer_kernels.cu.
+// A plan keeps what does not move with the particles (the frame's geometry,
+// the ball's blocks, the tables, on the host and the device) and redoes only
+// what the particles' positions decide when they move, into device buffers
+// it reuses. Positions, boxes and the nested rule's points are formed in
+// double and rounded once to the field type when they are uploaded.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/twoldg.h"
@@ -50,13 +57,6 @@ struct Rule1D {
 struct NestedTables {
     Rule1D sinh, mid, inner;
 };
-
-Rule1D gauss_rule(int n) {
-    RuleTables<double> r64;
-    RuleTables<float> r32;
-    build_rule(1, n, r64, r32);
-    return Rule1D{r64.nodes, r64.weights};
-}
 
 // The squared distance from x to the box [lo, hi] over dimensions [d0, d1)
 // (src/transfer.jl:292-300).
@@ -147,8 +147,10 @@ void sinh_points(const Rule1D& r, double a, double b, double c, double beta, std
     const double lo = std::asinh((1 + xc) / eps), hi = std::asinh((1 - xc) / eps);
     const double mu = (hi + lo) / 2, eta = (lo - hi) / 2;
     for (size_t k = 0; k < r.x.size(); ++k) {
-        xs.push_back(mid + half * (xc + eps * std::sinh(mu * r.x[k] - eta)));
-        ws.push_back(r.w[k] * eps * mu * std::cosh(mu * r.x[k] - eta) * half);
+        // sinh and cosh from one exponential
+        const double ex = std::exp(mu * r.x[k] - eta), ix = 1 / ex;
+        xs.push_back(mid + half * (xc + eps * ((ex - ix) / 2)));
+        ws.push_back(r.w[k] * eps * mu * ((ex + ix) / 2) * half);
     }
 }
 
@@ -178,7 +180,7 @@ void line_fold(const Support& s, const NestedTables& t, const double* lo, const 
             ws.clear();
             if (has_extent && extent[0] < mid && mid < extent[1]) {
                 inner_points(t.inner, a, b, innermost, xs, ws);
-                seg(xs, ws);
+                seg(xs, ws, true);
             } else if (!compact) {
                 const double c = std::min(std::max(s.z[d], a), b);
                 const double beta = std::max(std::sqrt(off2 + (s.z[d] - c) * (s.z[d] - c)),
@@ -187,27 +189,50 @@ void line_fold(const Support& s, const NestedTables& t, const double* lo, const 
                     sinh_points(t.mid, a, b, c, beta, xs, ws);
                 else
                     sinh_points(t.sinh, a, b, c, beta, xs, ws);
-                seg(xs, ws);
+                seg(xs, ws, false);
             }
         }
         a = b;
     }
 }
 
-// Every point of the nested rule's remaining n dimensions through `prefix`,
-// each with w times its lines' weights (collect_points!, src/transfer.jl:
-// 1302-1328).
-void collect_points(const Support& s, const NestedTables& t, const double* lo, const double* hi,
-                    std::vector<double>& prefix, double w, int n, std::vector<double>& xs, std::vector<double>& ws) {
-    if (n == 0) {
-        xs.insert(xs.end(), prefix.begin(), prefix.end());
-        ws.push_back(w);
+// The nested rule's points through `prefix` in innermost lines
+// (collect_points!, src/transfer.jl:1302-1328): with n dimensions remaining,
+// each point of this line recurses; with one remaining, the line itself is
+// emitted, its fixed coordinates (padded to two), the product w of the outer
+// lines' weights, and its segments' points and weights in order.
+struct NearLines {
+    std::vector<double> lx, lw, vals;   // per point; per line: prefix[2], w
+    std::vector<int32_t> range;         // per line: p0, p1
+    std::vector<int32_t> inner;         // per line: the points inside the support's section
+};
+
+void collect_lines(const Support& s, const NestedTables& t, const double* lo, const double* hi,
+                   std::vector<double>& prefix, double w, int n, NearLines& out) {
+    if (n == 1) {
+        const int32_t p0 = (int32_t)out.lw.size();
+        int32_t i0 = -1, i1 = -1;
+        line_fold(s, t, lo, hi, prefix, true, false,
+                  [&](const std::vector<double>& lx, const std::vector<double>& lw, bool inside) {
+                      // the inside segments are consecutive: the section is an interval
+                      if (inside && i0 < 0) i0 = (int32_t)out.lw.size();
+                      out.lx.insert(out.lx.end(), lx.begin(), lx.end());
+                      out.lw.insert(out.lw.end(), lw.begin(), lw.end());
+                      if (inside) i1 = (int32_t)out.lw.size();
+                  });
+        out.range.push_back(p0);
+        out.range.push_back((int32_t)out.lw.size());
+        out.inner.push_back(i0 < 0 ? 0 : i0);
+        out.inner.push_back(i0 < 0 ? 0 : i1);
+        out.vals.push_back(prefix.size() > 0 ? prefix[0] : 0.0);
+        out.vals.push_back(prefix.size() > 1 ? prefix[1] : 0.0);
+        out.vals.push_back(w);
         return;
     }
-    line_fold(s, t, lo, hi, prefix, n == 1, false, [&](const std::vector<double>& lx, const std::vector<double>& lw) {
+    line_fold(s, t, lo, hi, prefix, false, false, [&](const std::vector<double>& lx, const std::vector<double>& lw, bool) {
         for (size_t k = 0; k < lx.size(); ++k) {
             prefix.push_back(lx[k]);
-            collect_points(s, t, lo, hi, prefix, w * lw[k], n - 1, xs, ws);
+            collect_lines(s, t, lo, hi, prefix, w * lw[k], n - 1, out);
             prefix.pop_back();
         }
     });
@@ -217,67 +242,490 @@ struct HostElem {
     int block, e[3], particle;
 };
 
+// The tables a plan reads, built once per process in double-double and kept
+// (the 1D Gauss rules of the nested rule, each tensor rule of an order, the
+// element's nodes and weights).
+struct TableStore {
+    std::mutex m;
+    std::map<std::pair<int, int>, RuleTables<double>> rules;
+    std::map<int, ElementTables<double>> elements;
+    std::map<int, std::vector<double>> bary;
+
+    const RuleTables<double>& rule(int P, int q) {
+        std::lock_guard<std::mutex> g(m);
+        auto it = rules.find({P, q});
+        if (it == rules.end()) {
+            RuleTables<double> r64;
+            RuleTables<float> r32;
+            build_rule(P, q, r64, r32);
+            it = rules.emplace(std::make_pair(P, q), std::move(r64)).first;
+        }
+        return it->second;
+    }
+    const ElementTables<double>& element(int P) {
+        std::lock_guard<std::mutex> g(m);
+        auto it = elements.find(P);
+        if (it == elements.end()) {
+            ElementTables<double> t64;
+            ElementTables<float> t32;
+            build_tables(P, t64, t32);
+            it = elements.emplace(P, std::move(t64)).first;
+        }
+        return it->second;
+    }
+    const std::vector<double>& barycentric(int P) {
+        std::lock_guard<std::mutex> g(m);
+        auto it = bary.find(P);
+        if (it == bary.end()) {
+            std::vector<double> b64;
+            std::vector<float> b32;
+            build_bary(P, b64, b32);
+            it = bary.emplace(P, std::move(b64)).first;
+        }
+        return it->second;
+    }
+};
+
+TableStore& store() {
+    static TableStore s;
+    return s;
+}
+
+Rule1D gauss_line(int n) {
+    const RuleTables<double>& r = store().rule(1, n);
+    return Rule1D{r.nodes, r.weights};
+}
+
+// A device buffer that grows and is never shrunk, so that a plan's updates
+// reuse it.
+struct DevVec {
+    void* p = nullptr;
+    size_t cap = 0;
+    DevVec() = default;
+    DevVec(const DevVec&) = delete;
+    DevVec& operator=(const DevVec&) = delete;
+    ~DevVec() {
+        if (p) cudaFree(p);
+    }
+    cudaError_t reserve(size_t bytes) {
+        bytes = std::max<size_t>(bytes, 16);
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        return e;
+    }
+    template <typename V>
+    cudaError_t put(const std::vector<V>& v) {
+        cudaError_t e = reserve(v.size() * sizeof(V));
+        if (e != cudaSuccess || v.empty()) return e;
+        return cudaMemcpy(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice);
+    }
+    // v rounded to the field type (prec 0: double, 1: float)
+    cudaError_t put_field(const std::vector<double>& v, int prec) {
+        if (prec == 0) return put(v);
+        return put(std::vector<float>(v.begin(), v.end()));
+    }
+};
+
 }  // namespace
 
 struct twoldg_transfer_plan {
-    TransferLaunch L;
+    // what does not move with the particles (SourceBall, src/transfer.jl:946-982)
+    int D = 3, P = 3, E = 2, N = 8, P1 = 4, prec = 0;
+    int64_t nb = 0;
     cudaStream_t stream = nullptr;
+    std::vector<double> origins, spacings;
+    std::vector<int32_t> levels;
+    std::vector<uint8_t> mask;
+    int top = 0;
+    double he = 0, centre[3] = {0, 0, 0}, R = 0, rnear = 1, rfar = 9;
+    std::vector<double> band_from;
+    std::vector<int> rule_q;
+    NestedTables nt;
+    std::vector<int64_t> ball_blocks;   // the frame's blocks that meet the ball
+    DevVec d_origins, d_spacings, d_tables, d_bary, d_gll, d_wn;
+    // what the particles decide
+    DevVec d_relems, d_lx, d_lw, d_vals, d_lines, d_chunks, d_nelems, d_partials;
+    DevVec d_drelems, d_dvals, d_dlines, d_dchunks, d_delems, d_dpartials;
+    // L: every element and point; Ld: the built-in density's, which vanishes
+    // outside the particles' supports -- the elements that meet a support and,
+    // on the near elements, the lines' points inside it
+    TransferLaunch L, Ld;
     int64_t counts[8] = {0};
     int64_t npoints = 0;
     bool density_ok = false;
-    std::vector<void*> bufs;
+
     ~twoldg_transfer_plan() {
         if (stream) cudaStreamSynchronize(stream);
-        for (void* b : bufs) cudaFree(b);
     }
-    template <typename V>
-    cudaError_t upload(const std::vector<V>& v, const void** out) {
-        void* p = nullptr;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(v.size() * sizeof(V), 16));
-        if (e != cudaSuccess) return e;
-        bufs.push_back(p);
-        if (!v.empty()) e = cudaMemcpy(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice);
-        *out = p;
-        return e;
-    }
+    int set_particles(const twoldg_particle* tp, int n);
 };
 
 namespace {
 
-template <typename T>
-std::vector<T> rounded(const std::vector<double>& v) {
-    return std::vector<T>(v.begin(), v.end());
-}
-
-template <typename T>
-int upload_all(twoldg_transfer_plan* pl, const std::vector<double>& origins, const std::vector<double>& spacings,
-               const std::vector<double>& tabs, const std::vector<double>& nxs, const std::vector<double>& nws,
-               const std::vector<double>& bary, const std::vector<double>& gll, const std::vector<double>& wn) {
-    TransferLaunch& L = pl->L;
-    cudaError_t e;
-#define UP(vec, field)                                                                     \
-    e = pl->upload(rounded<T>(vec), &L.field);                                             \
-    if (e != cudaSuccess) return fail(TWOLDG_ECUDA, std::string("transfer upload: ") + cudaGetErrorString(e));
-    UP(origins, origins)
-    UP(spacings, spacings)
-    UP(tabs, tables)
-    UP(nxs, near_xs)
-    UP(nws, near_ws)
-    UP(bary, bary)
-    UP(gll, gll)
-    UP(wn, wn)
-#undef UP
-    int M = 1;
-    for (int d = 0; d < L.D; ++d) M *= L.P + 1;
-    void* part = nullptr;
-    e = cudaMalloc(&part, std::max<size_t>((size_t)L.n_chunks * M * sizeof(T), 16));
-    if (e != cudaSuccess) return fail(TWOLDG_ENOMEM, std::string("transfer partials: ") + cudaGetErrorString(e));
-    pl->bufs.push_back(part);
-    L.partials = part;
-    return TWOLDG_OK;
-}
+#define TRY_CUDA(call, what)                                                                        \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return fail(TWOLDG_ECUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
 
 }  // namespace
+
+// The particle-dependent plan (projection_plan, src/transfer.jl:984-1022):
+// the supports' finest-level check, the elements of the ball's blocks by rule
+// (host_elements, :1380-1415), the nested rule's lines (threaded over the near
+// elements, each element's lines in the serial order), the density's subsets,
+// and their upload into the plan's reused device buffers.
+int twoldg_transfer_plan::set_particles(const twoldg_particle* tps, int np) {
+    if (np < 0 || np > kMaxParticles)
+        return fail(TWOLDG_EUNSUP, "at most " + std::to_string(kMaxParticles) + " particles, got " + std::to_string(np));
+    if (np > 0 && !tps) return fail(TWOLDG_EINVAL, "particles must not be NULL");
+    std::vector<Support> parts(np);
+    for (int k = 0; k < np; ++k) {
+        Support& s = parts[k];
+        s.D = D;
+        double vv = 0;
+        for (int j = 0; j < 3; ++j) {
+            s.z[j] = j < D ? tps[k].z[j] : 0;
+            s.v[j] = j < D ? tps[k].v[j] : 0;
+            vv += s.v[j] * s.v[j];
+        }
+        s.ell = tps[k].ell;
+        if (!(tps[k].ell > 0)) return fail(TWOLDG_EINVAL, "particle " + std::to_string(k) + ": ell must be positive");
+        if (!(vv < 1)) return fail(TWOLDG_EINVAL, "particle " + std::to_string(k) + ": |v| must be below 1");
+    }
+    auto in_frame = [&](int64_t b) { return mask.empty() || mask[b]; };
+    auto block_box = [&](int64_t b, double* lo, double* hi) {
+        for (int k = 0; k < D; ++k) {
+            lo[k] = origins[b * D + k];
+            hi[k] = lo[k] + spacings[b] * N;
+        }
+    };
+    auto elem_box = [&](int64_t b, const int* e, double* lo, double* hi) {
+        for (int k = 0; k < D; ++k) {
+            lo[k] = origins[b * D + k] + spacings[b] * (e[k] * P1);
+            hi[k] = origins[b * D + k] + spacings[b] * ((e[k] + 1) * P1);
+        }
+    };
+    // every support on the finest level (check_finest, src/transfer.jl:847-870)
+    if (!levels.empty()) {
+        for (const Support& s : parts) {
+            for (int corner = 0; corner < (1 << D); ++corner) {
+                double x[3];
+                for (int k = 0; k < D; ++k) x[k] = s.z[k] + ((corner >> k) & 1 ? s.ell : -s.ell);
+                for (int64_t b = 0; b < nb; ++b) {
+                    if (!in_frame(b)) continue;
+                    double lo[3], hi[3];
+                    block_box(b, lo, hi);
+                    bool inside = true;
+                    for (int k = 0; k < D; ++k) inside = inside && lo[k] <= x[k] && x[k] < hi[k];
+                    if (!inside) continue;
+                    if (levels[b] != top)
+                        return fail(TWOLDG_EINVAL, "project_source! needs the finest level, " + std::to_string(top) +
+                                                       ", under every particle's support, and the support of radius " +
+                                                       fmt(s.ell) + " reaches a block of level " +
+                                                       std::to_string(levels[b]));
+                    break;
+                }
+            }
+        }
+    }
+    // the elements by rule
+    const double rn = rnear * he, rf = rfar * he;
+    std::vector<std::vector<HostElem>> lists(rule_q.size());
+    std::vector<HostElem> near;
+    int Ed[3] = {1, 1, 1};
+    for (int k = 0; k < D; ++k) Ed[k] = E;
+    std::vector<double> dist2(parts.size());
+    for (int64_t b : ball_blocks) {
+        for (int e2 = 0; e2 < Ed[2]; ++e2)
+            for (int e1 = 0; e1 < Ed[1]; ++e1)
+                for (int e0 = 0; e0 < Ed[0]; ++e0) {
+                    const int e[3] = {e0, e1, e2};
+                    double lo[3], hi[3];
+                    elem_box(b, e, lo, hi);
+                    if (box_distance2(centre, lo, hi, 0, D) >= R * R) continue;
+                    bool host = false;
+                    for (size_t k = 0; k < parts.size(); ++k) {
+                        dist2[k] = box_distance2(parts[k].z, lo, hi, 0, D);
+                        host = host || dist2[k] < rf * rf;
+                    }
+                    HostElem h{(int)b, {e0, e1, e2}, 0};
+                    if (!host) {
+                        lists[0].push_back(h);
+                        continue;
+                    }
+                    size_t amin = 0;
+                    for (size_t k = 1; k < parts.size(); ++k)
+                        if (dist2[k] < dist2[amin]) amin = k;
+                    if (dist2[amin] >= rn * rn) {
+                        const double delta = std::sqrt(dist2[amin]) / he;
+                        int band = 0;
+                        for (size_t i = 0; i < band_from.size(); ++i)
+                            if (band_from[i] <= delta) band = (int)i;
+                        lists[1 + band].push_back(h);
+                        continue;
+                    }
+                    int inside = 0;
+                    for (size_t k = 0; k < parts.size(); ++k) inside += dist2[k] < parts[k].ell * parts[k].ell;
+                    if (inside > 1) {
+                        std::string at;
+                        for (int k = 0; k < D; ++k) at += (k ? ", " : "") + fmt(lo[k]);
+                        return fail(TWOLDG_EINVAL, "the supports of two particles meet the element at (" + at +
+                                                       "), and the near rule splits at one: the particles are closer "
+                                                       "than an element");
+                    }
+                    h.particle = (int)amin;
+                    near.push_back(h);
+                }
+    }
+    // The nested rule's lines on up to 16 host threads, threaded as the
+    // reference threads its near pass (src/transfer.jl:1160-1213): over the
+    // points of each near element's outermost line (the element's own line in
+    // one dimension), each item the lines through one point, kept in the
+    // serial order. The particle's own element holds the most points, and
+    // threading over elements left it on one thread.
+    struct Item {
+        int elem;
+        double x, w;
+    };
+    std::vector<Item> items;
+    for (size_t i = 0; i < near.size(); ++i) {
+        if (D == 1) {
+            items.push_back(Item{(int)i, 0.0, 1.0});
+            continue;
+        }
+        double lo[3], hi[3];
+        elem_box(near[i].block, near[i].e, lo, hi);
+        line_fold(parts[near[i].particle], nt, lo, hi, std::vector<double>(), false, false,
+                  [&](const std::vector<double>& lx, const std::vector<double>& lw, bool) {
+                      for (size_t k = 0; k < lx.size(); ++k) items.push_back(Item{(int)i, lx[k], lw[k]});
+                  });
+    }
+    std::vector<NearLines> per(items.size());
+    {
+        std::atomic<size_t> next(0);
+        auto work = [&]() {
+            for (size_t n = next++; n < items.size(); n = next++) {
+                const Item& it = items[n];
+                double lo[3], hi[3];
+                elem_box(near[it.elem].block, near[it.elem].e, lo, hi);
+                std::vector<double> prefix;
+                if (D == 1) {
+                    collect_lines(parts[near[it.elem].particle], nt, lo, hi, prefix, 1.0, 1, per[n]);
+                } else {
+                    prefix.push_back(it.x);
+                    collect_lines(parts[near[it.elem].particle], nt, lo, hi, prefix, it.w, D - 1, per[n]);
+                }
+            }
+        };
+        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        const unsigned nt_ = (unsigned)std::min<size_t>(hw, items.size());
+        std::vector<std::thread> pool;
+        for (unsigned k = 1; k < nt_; ++k) pool.emplace_back(work);
+        work();
+        for (auto& t : pool) t.join();
+    }
+    NearLines nl;
+    std::vector<int64_t> first(near.size() + 1, 0);   // per near element its first line
+    size_t nlx = 0, nlines = 0;
+    for (const NearLines& x : per) {
+        nlx += x.lw.size();
+        nlines += x.range.size() / 2;
+    }
+    nl.lx.reserve(nlx);
+    nl.lw.reserve(nlx);
+    nl.vals.reserve(3 * nlines);
+    nl.range.reserve(2 * nlines);
+    nl.inner.reserve(2 * nlines);
+    for (size_t n = 0; n < per.size(); ++n) {
+        NearLines& x = per[n];
+        const int32_t off = (int32_t)nl.lw.size();
+        if (nl.lw.size() + x.lw.size() > (size_t)std::numeric_limits<int32_t>::max() / 2)
+            return fail(TWOLDG_EUNSUP, "the nested rule's points exceed 2^30");
+        nl.lx.insert(nl.lx.end(), x.lx.begin(), x.lx.end());
+        nl.lw.insert(nl.lw.end(), x.lw.begin(), x.lw.end());
+        nl.vals.insert(nl.vals.end(), x.vals.begin(), x.vals.end());
+        for (int32_t v : x.range) nl.range.push_back(v + off);
+        for (size_t k = 0; k < x.inner.size(); k += 2) {
+            const bool any = x.inner[k + 1] > x.inner[k];
+            nl.inner.push_back(any ? x.inner[k] + off : 0);
+            nl.inner.push_back(any ? x.inner[k + 1] + off : 0);
+        }
+        first[items[n].elem + 1] = (int64_t)nl.range.size() / 2;
+        x = NearLines();
+    }
+    for (size_t i = 0; i < near.size(); ++i) first[i + 1] = std::max(first[i + 1], first[i]);
+    // tensor rule elements and the values' offsets
+    std::vector<RuleElement> relems;
+    int64_t base = 0;
+    std::fill(counts, counts + 8, 0);
+    for (size_t r = 0; r < lists.size(); ++r) {
+        int64_t per_el = 1;
+        for (int k = 0; k < D; ++k) per_el *= rule_q[r];
+        for (const HostElem& h : lists[r]) {
+            RuleElement re{};
+            re.block = h.block;
+            for (int k = 0; k < 3; ++k) re.e[k] = h.e[k];
+            re.rule = (int)r;
+            re.base = base;
+            base += per_el;
+            relems.push_back(re);
+        }
+        if (r == 0) {
+            counts[0] = (int64_t)lists[0].size();
+            counts[1] = base;
+        } else {
+            counts[2] += (int64_t)lists[r].size();
+        }
+    }
+    counts[3] = base - counts[1];
+    // Near elements and their chunks of lines: at most kNearLines lines a
+    // chunk, fewer when the lines are few, so that a small set (the density's
+    // lines inside the supports) still spreads over the GPU's SMs.
+    auto chunk_lines = [](int64_t nlines) {
+        return (int64_t)std::max<int64_t>(4, std::min<int64_t>(kNearLines, (nlines + 607) / 608));
+    };
+    const int64_t cl = chunk_lines(first.back());
+    std::vector<NearElement> nelems;
+    std::vector<NearChunk> chunks;
+    for (size_t i = 0; i < near.size(); ++i) {
+        NearElement ne{};
+        ne.block = near[i].block;
+        for (int k = 0; k < 3; ++k) ne.e[k] = near[i].e[k];
+        ne.c0 = (int32_t)chunks.size();
+        for (int64_t a = first[i]; a < first[i + 1]; a += cl)
+            chunks.push_back(NearChunk{(int32_t)a, (int32_t)std::min<int64_t>(a + cl, first[i + 1]), (int32_t)i, 0});
+        ne.c1 = (int32_t)chunks.size();
+        nelems.push_back(ne);
+    }
+    std::vector<NearLine> lines(nl.range.size() / 2);
+    for (size_t l = 0; l < lines.size(); ++l) lines[l] = NearLine{nl.range[2 * l], nl.range[2 * l + 1]};
+    counts[4] = (int64_t)near.size();
+    counts[5] = (int64_t)nl.lw.size();
+    counts[6] = (int64_t)chunks.size();
+    npoints = base + (int64_t)nl.lw.size();
+    counts[7] = npoints;
+    // The density's elements and lines. Its support |L(v)(x - z)| <= ell lies
+    // within |x - z| <= ell; a box farther than that (with a margin of 1e-3
+    // for the field type's rounding) from every particle holds no point where
+    // it is nonzero, and on a near element that meets no other particle's
+    // support, a line's points outside its particle's section are outside too.
+    auto meets = [&](int block, const int32_t* e, int k) {
+        const int ee[3] = {e[0], e[1], e[2]};
+        double lo[3], hi[3];
+        elem_box(block, ee, lo, hi);
+        return box_distance2(parts[k].z, lo, hi, 0, D) <= parts[k].ell * parts[k].ell * (1 + 1e-3);
+    };
+    std::vector<RuleElement> drelems;
+    for (const RuleElement& re : relems)
+        for (size_t k = 0; k < parts.size(); ++k)
+            if (meets(re.block, re.e, (int)k)) {
+                drelems.push_back(re);
+                break;
+            }
+    // each list's elements by rule (both keep the rules' order)
+    auto starts = [&](const std::vector<RuleElement>& v, int64_t* st) {
+        for (size_t r = 0; r <= rule_q.size(); ++r) st[r] = 0;
+        for (const RuleElement& re : v) ++st[re.rule + 1];
+        for (size_t r = 0; r < rule_q.size(); ++r) st[r + 1] += st[r];
+    };
+    std::vector<NearLine> dlines;
+    std::vector<double> dvals;
+    std::vector<NearChunk> dchunks;
+    std::vector<NearElement> delems;
+    std::vector<std::pair<int64_t, int64_t>> dranges(near.size(), {0, 0});
+    for (size_t i = 0; i < near.size(); ++i) {
+        bool others = false;
+        for (size_t k = 0; k < parts.size(); ++k)
+            if ((int)k != near[i].particle && meets(near[i].block, nelems[i].e, (int)k)) others = true;
+        const int64_t l0 = (int64_t)dlines.size();
+        for (int64_t l = first[i]; l < first[i + 1]; ++l) {
+            if (others)
+                dlines.push_back(lines[l]);
+            else if (nl.inner[2 * l + 1] > nl.inner[2 * l])
+                dlines.push_back(NearLine{nl.inner[2 * l], nl.inner[2 * l + 1]});
+            else
+                continue;
+            dvals.insert(dvals.end(), nl.vals.begin() + 3 * l, nl.vals.begin() + 3 * l + 3);
+        }
+        dranges[i] = {l0, (int64_t)dlines.size()};
+    }
+    const int64_t dcl = chunk_lines((int64_t)dlines.size());
+    for (size_t i = 0; i < near.size(); ++i) {
+        const int64_t l0 = dranges[i].first, l1 = dranges[i].second;
+        if (l1 == l0) continue;
+        NearElement ne = nelems[i];
+        ne.c0 = (int32_t)dchunks.size();
+        for (int64_t a = l0; a < l1; a += dcl)
+            dchunks.push_back(NearChunk{(int32_t)a, (int32_t)std::min<int64_t>(a + dcl, l1), (int32_t)delems.size(), 0});
+        ne.c1 = (int32_t)dchunks.size();
+        delems.push_back(ne);
+    }
+    // upload: the previous projection may still read the buffers
+    TRY_CUDA(cudaStreamSynchronize(stream), "transfer plan");
+    int M = 1;
+    for (int k = 0; k < D; ++k) M *= P1;
+    const size_t wsz = prec == 0 ? 8 : 4;
+    TRY_CUDA(d_relems.put(relems), "transfer upload");
+    TRY_CUDA(d_lx.put_field(nl.lx, prec), "transfer upload");
+    TRY_CUDA(d_lw.put_field(nl.lw, prec), "transfer upload");
+    TRY_CUDA(d_vals.put_field(nl.vals, prec), "transfer upload");
+    TRY_CUDA(d_lines.put(lines), "transfer upload");
+    TRY_CUDA(d_chunks.put(chunks), "transfer upload");
+    TRY_CUDA(d_nelems.put(nelems), "transfer upload");
+    TRY_CUDA(d_partials.reserve(chunks.size() * M * wsz), "transfer partials");
+    TRY_CUDA(d_drelems.put(drelems), "transfer upload");
+    TRY_CUDA(d_dvals.put_field(dvals, prec), "transfer upload");
+    TRY_CUDA(d_dlines.put(dlines), "transfer upload");
+    TRY_CUDA(d_dchunks.put(dchunks), "transfer upload");
+    TRY_CUDA(d_delems.put(delems), "transfer upload");
+    TRY_CUDA(d_dpartials.reserve(dchunks.size() * M * wsz), "transfer partials");
+    L.rule_elems = static_cast<const RuleElement*>(d_relems.p);
+    L.n_rule_elems = (int64_t)relems.size();
+    starts(relems, L.rule_start);
+    L.near_lx = d_lx.p;
+    L.near_lw = d_lw.p;
+    L.line_vals = d_vals.p;
+    L.lines = static_cast<const NearLine*>(d_lines.p);
+    L.n_lines = (int64_t)lines.size();
+    L.chunks = static_cast<const NearChunk*>(d_chunks.p);
+    L.n_chunks = (int64_t)chunks.size();
+    L.near_elems = static_cast<const NearElement*>(d_nelems.p);
+    L.n_near_elems = (int64_t)nelems.size();
+    L.near_base = base;
+    L.partials = d_partials.p;
+    L.nparticles = np;
+    for (int k = 0; k < np; ++k) {
+        TransferParticle& q_ = L.particles[k];
+        double vv = 0;
+        for (int j = 0; j < 3; ++j) {
+            q_.z[j] = tps[k].z[j];
+            q_.v[j] = tps[k].v[j];
+            vv += tps[k].v[j] * tps[k].v[j];
+        }
+        const double gamma = 1 / std::sqrt(1 - vv);
+        q_.g = gamma * gamma / (gamma + 1);
+        q_.ell = tps[k].ell;
+        q_.charge = tps[k].charge;
+    }
+    Ld = L;
+    Ld.rule_elems = static_cast<const RuleElement*>(d_drelems.p);
+    Ld.n_rule_elems = (int64_t)drelems.size();
+    starts(drelems, Ld.rule_start);
+    Ld.line_vals = d_dvals.p;
+    Ld.lines = static_cast<const NearLine*>(d_dlines.p);
+    Ld.n_lines = (int64_t)dlines.size();
+    Ld.chunks = static_cast<const NearChunk*>(d_dchunks.p);
+    Ld.n_chunks = (int64_t)dchunks.size();
+    Ld.near_elems = static_cast<const NearElement*>(d_delems.p);
+    Ld.n_near_elems = (int64_t)delems.size();
+    Ld.partials = d_dpartials.p;
+    return TWOLDG_OK;
+}
 
 extern "C" {
 
@@ -314,44 +762,50 @@ int twoldg_transfer_table(int32_t order, int32_t precision, const char* name, in
 int twoldg_transfer_plan_create(twoldg_problem* p, const twoldg_transfer_desc* d, twoldg_transfer_plan** out) {
     if (!p || !d || !out) return fail(TWOLDG_EINVAL, "problem, descriptor and out must not be NULL");
     *out = nullptr;
+    std::unique_ptr<twoldg_transfer_plan> pl(new twoldg_transfer_plan());
+    twoldg_transfer_plan& T = *pl;
     int D, P, E, prec;
     int64_t nb;
     cudaStream_t stream;
     if (!problem_shape(p, &D, &P, &E, &prec, &nb, &stream)) return fail(TWOLDG_EINVAL, "bad problem");
     if (D < 1 || D > 3) return fail(TWOLDG_EUNSUP, "the transfer runs in 1 to 3 dimensions");
     if (!d->origins || !d->spacings) return fail(TWOLDG_EINVAL, "origins and spacings must not be NULL");
-    if (d->nparticles < 0 || d->nparticles > kMaxParticles)
-        return fail(TWOLDG_EUNSUP, "at most " + std::to_string(kMaxParticles) + " particles, got " +
-                                       std::to_string(d->nparticles));
-    if (d->nparticles > 0 && !d->particles) return fail(TWOLDG_EINVAL, "particles must not be NULL");
     if (!(d->h_e > 0)) return fail(TWOLDG_EINVAL, "h_e must be positive");
-    const int P1 = P + 1, N = E * P1;
+    T.D = D;
+    T.P = P;
+    T.E = E;
+    T.P1 = P + 1;
+    T.N = E * (P + 1);
+    T.prec = prec;
+    T.nb = nb;
+    T.stream = stream;
     // the quadrature, with the reference's defaults (src/transfer.jl:139-170)
     const int q = d->q > 0 ? d->q : P + 3;
     const int nsinh = d->nsinh > 0 ? d->nsinh : 48, nmid = d->nmid > 0 ? d->nmid : 16;
     const int ninner = d->ninner > 0 ? d->ninner : 24;
-    const double rfar = d->rfar > 0 ? d->rfar : 9.0;
-    std::vector<double> band_from = {1, 2, 3, 4};
+    T.rfar = d->rfar > 0 ? d->rfar : 9.0;
+    T.band_from = {1, 2, 3, 4};
     std::vector<int> band_points = {14, 10, 8, 7};
     if (d->nbands > 0) {
         if (!d->band_from || !d->band_points) return fail(TWOLDG_EINVAL, "band_from and band_points must not be NULL");
         if (d->nbands > 15) return fail(TWOLDG_EUNSUP, "at most 15 graded bands");
-        band_from.assign(d->band_from, d->band_from + d->nbands);
+        T.band_from.assign(d->band_from, d->band_from + d->nbands);
         band_points.assign(d->band_points, d->band_points + d->nbands);
     }
-    for (size_t i = 0; i < band_from.size(); ++i) {
-        if ((i > 0 && !(band_from[i - 1] < band_from[i])) || !(0 <= band_from[i] && band_from[i] < rfar))
+    for (size_t i = 0; i < T.band_from.size(); ++i) {
+        if ((i > 0 && !(T.band_from[i - 1] < T.band_from[i])) || !(0 <= T.band_from[i] && T.band_from[i] < T.rfar))
             return fail(TWOLDG_EINVAL, "the graded rule's distances must increase from 0 and stay below rfar = " +
-                                           fmt(rfar));
+                                           fmt(T.rfar));
     }
-    if (!(0 <= d->rnear && d->rnear <= rfar))
+    if (!(0 <= d->rnear && d->rnear <= T.rfar))
         return fail(TWOLDG_EINVAL, "rnear = " + fmt(d->rnear) + " must lie between 0 and the far rule's distance rfar = " +
-                                       fmt(rfar));
-    std::vector<int> rule_q = {q};
-    for (int b : band_points) rule_q.push_back(b);
+                                       fmt(T.rfar));
+    T.rnear = d->rnear;
+    T.rule_q = {q};
+    for (int b : band_points) T.rule_q.push_back(b);
     int max_q = 0;
-    for (int r : rule_q) {
-        if (r < 1) return fail(TWOLDG_EINVAL, "a rule needs at least one point");
+    for (int r : T.rule_q) {
+        if (r < 1 || r > kMaxRule) return fail(TWOLDG_EINVAL, "a rule needs 1.." + std::to_string(kMaxRule) + " points");
         max_q = std::max(max_q, r);
     }
     int64_t cap = 1;
@@ -360,267 +814,91 @@ int twoldg_transfer_plan_create(twoldg_problem* p, const twoldg_transfer_desc* d
                                                   " points exceeds the device's 4096 per element");
     if (nsinh > kMaxRule || nmid > kMaxRule || ninner > kMaxRule)
         return fail(TWOLDG_EINVAL, "the nested rule's lines take at most " + std::to_string(kMaxRule) + " points");
-
-    const double he = d->h_e, rn = d->rnear * he, rf = rfar * he;
-    std::vector<Support> parts(d->nparticles);
-    for (int k = 0; k < d->nparticles; ++k) {
-        const twoldg_particle& tp = d->particles[k];
-        Support& s = parts[k];
-        s.D = D;
-        double vv = 0;
-        for (int j = 0; j < 3; ++j) {
-            s.z[j] = j < D ? tp.z[j] : 0;
-            s.v[j] = j < D ? tp.v[j] : 0;
-            vv += s.v[j] * s.v[j];
-        }
-        s.ell = tp.ell;
-        if (!(tp.ell > 0)) return fail(TWOLDG_EINVAL, "particle " + std::to_string(k) + ": ell must be positive");
-        if (!(vv < 1)) return fail(TWOLDG_EINVAL, "particle " + std::to_string(k) + ": |v| must be below 1");
-    }
-    const double* c = d->ball_centre;
-    const double R = d->ball_radius;
-    auto block_box = [&](int64_t b, double* lo, double* hi) {
-        for (int k = 0; k < D; ++k) {
-            lo[k] = d->origins[b * D + k];
-            hi[k] = lo[k] + d->spacings[b] * N;
-        }
-    };
-    auto in_frame = [&](int64_t b) { return !d->mask || d->mask[b]; };
-    // the finest-level checks (check_finest, src/transfer.jl:823-870)
-    if (d->levels) {
-        int top = 0;
-        for (int64_t b = 0; b < nb; ++b) top = std::max(top, (int)d->levels[b]);
-        for (int64_t b = 0; b < nb; ++b) {
-            if (d->levels[b] == top || !in_frame(b)) continue;
-            double lo[3], hi[3];
-            block_box(b, lo, hi);
-            const double r2 = box_distance2(c, lo, hi, 0, D);
-            if (r2 < R * R)
-                return fail(TWOLDG_EINVAL,
-                            "project_source! needs the finest level, " + std::to_string(top) +
-                                ", under the source's ball of radius " + fmt(R) + ", and a block of level " +
-                                std::to_string(d->levels[b]) + " reaches to " + fmt(std::sqrt(r2)) +
-                                " from the ball's centre: the transfer measures its distances in the finest element "
-                                "width h_e, and would integrate a coarser element with a rule chosen for a finer one");
-        }
-        for (const Support& s : parts) {
-            for (int corner = 0; corner < (1 << D); ++corner) {
-                double x[3];
-                for (int k = 0; k < D; ++k) x[k] = s.z[k] + ((corner >> k) & 1 ? s.ell : -s.ell);
-                for (int64_t b = 0; b < nb; ++b) {
-                    if (!in_frame(b)) continue;
-                    double lo[3], hi[3];
-                    block_box(b, lo, hi);
-                    bool inside = true;
-                    for (int k = 0; k < D; ++k) inside = inside && lo[k] <= x[k] && x[k] < hi[k];
-                    if (!inside) continue;
-                    if (d->levels[b] != top)
-                        return fail(TWOLDG_EINVAL, "project_source! needs the finest level, " + std::to_string(top) +
-                                                       ", under every particle's support, and the support of radius " +
-                                                       fmt(s.ell) + " reaches a block of level " +
-                                                       std::to_string(d->levels[b]));
-                    break;
-                }
-            }
-        }
-    }
-    // the elements by rule (host_elements, element_class, src/transfer.jl:
-    // 493-503, 1380-1415)
-    std::vector<std::vector<HostElem>> lists(rule_q.size());
-    std::vector<HostElem> near;
-    int Ed[3] = {1, 1, 1};
-    for (int k = 0; k < D; ++k) Ed[k] = E;
+    T.nt = NestedTables{gauss_line(nsinh), gauss_line(nmid), gauss_line(ninner)};
+    T.he = d->h_e;
+    for (int k = 0; k < 3; ++k) T.centre[k] = k < D ? d->ball_centre[k] : 0;
+    T.R = d->ball_radius;
+    T.origins.assign(d->origins, d->origins + nb * D);
+    T.spacings.assign(d->spacings, d->spacings + nb);
+    if (d->levels) T.levels.assign(d->levels, d->levels + nb);
+    if (d->mask) T.mask.assign(d->mask, d->mask + nb);
+    // the ball's blocks and the ball's finest-level check (SourceBall,
+    // check_finest, src/transfer.jl:823-845, 958-982)
+    for (int64_t b = 0; b < nb; ++b)
+        if (!T.levels.empty()) T.top = std::max(T.top, (int)T.levels[b]);
     for (int64_t b = 0; b < nb; ++b) {
-        if (!in_frame(b)) continue;
-        double blo[3], bhi[3];
-        block_box(b, blo, bhi);
-        if (!(box_distance2(c, blo, bhi, 0, D) < R * R)) continue;
-        for (int e2 = 0; e2 < Ed[2]; ++e2)
-            for (int e1 = 0; e1 < Ed[1]; ++e1)
-                for (int e0 = 0; e0 < Ed[0]; ++e0) {
-                    const int e[3] = {e0, e1, e2};
-                    double lo[3], hi[3];
-                    for (int k = 0; k < D; ++k) {
-                        lo[k] = d->origins[b * D + k] + d->spacings[b] * (e[k] * P1);
-                        hi[k] = d->origins[b * D + k] + d->spacings[b] * ((e[k] + 1) * P1);
-                    }
-                    if (box_distance2(c, lo, hi, 0, D) >= R * R) continue;
-                    std::vector<double> dist2(parts.size());
-                    bool host = false;
-                    for (size_t k = 0; k < parts.size(); ++k) {
-                        dist2[k] = box_distance2(parts[k].z, lo, hi, 0, D);
-                        host = host || dist2[k] < rf * rf;
-                    }
-                    HostElem he_{(int)b, {e0, e1, e2}, 0};
-                    if (!host) {
-                        lists[0].push_back(he_);
-                        continue;
-                    }
-                    size_t amin = 0;
-                    for (size_t k = 1; k < parts.size(); ++k)
-                        if (dist2[k] < dist2[amin]) amin = k;
-                    if (dist2[amin] >= rn * rn) {
-                        const double delta = std::sqrt(dist2[amin]) / he;
-                        int band = 0;
-                        for (size_t i = 0; i < band_from.size(); ++i)
-                            if (band_from[i] <= delta) band = (int)i;
-                        lists[1 + band].push_back(he_);
-                        continue;
-                    }
-                    int inside = 0;
-                    for (size_t k = 0; k < parts.size(); ++k) inside += dist2[k] < parts[k].ell * parts[k].ell;
-                    if (inside > 1) {
-                        std::string at;
-                        for (int k = 0; k < D; ++k) at += (k ? ", " : "") + fmt(lo[k]);
-                        return fail(TWOLDG_EINVAL, "the supports of two particles meet the element at (" + at +
-                                                       "), and the near rule splits at one: the particles are closer "
-                                                       "than an element");
-                    }
-                    he_.particle = (int)amin;
-                    near.push_back(he_);
-                }
-    }
-    // the nested rule's points, element by element (nested_points,
-    // src/transfer.jl:1257-1285)
-    NestedTables nt{gauss_rule(nsinh), gauss_rule(nmid), gauss_rule(ninner)};
-    std::vector<double> nxs, nws;
-    std::vector<int64_t> first = {0};
-    for (const HostElem& h : near) {
+        if (!T.mask.empty() && !T.mask[b]) continue;
         double lo[3], hi[3];
         for (int k = 0; k < D; ++k) {
-            lo[k] = d->origins[(int64_t)h.block * D + k] + d->spacings[h.block] * (h.e[k] * P1);
-            hi[k] = d->origins[(int64_t)h.block * D + k] + d->spacings[h.block] * ((h.e[k] + 1) * P1);
+            lo[k] = T.origins[b * D + k];
+            hi[k] = lo[k] + T.spacings[b] * T.N;
         }
-        std::vector<double> prefix;
-        collect_points(parts[h.particle], nt, lo, hi, prefix, 1.0, D, nxs, nws);
-        first.push_back((int64_t)nws.size());
-        if (nws.size() > (size_t)std::numeric_limits<int32_t>::max())
-            return fail(TWOLDG_EUNSUP, "the nested rule's points exceed 2^31");
+        const double r2 = box_distance2(T.centre, lo, hi, 0, D);
+        if (!(r2 < T.R * T.R)) continue;
+        if (!T.levels.empty() && T.levels[b] != T.top)
+            return fail(TWOLDG_EINVAL,
+                        "project_source! needs the finest level, " + std::to_string(T.top) +
+                            ", under the source's ball of radius " + fmt(T.R) + ", and a block of level " +
+                            std::to_string(T.levels[b]) + " reaches to " + fmt(std::sqrt(r2)) +
+                            " from the ball's centre: the transfer measures its distances in the finest element "
+                            "width h_e, and would integrate a coarser element with a rule chosen for a finer one");
+        T.ball_blocks.push_back(b);
     }
-
-    std::unique_ptr<twoldg_transfer_plan> pl(new twoldg_transfer_plan());
-    pl->stream = stream;
-    TransferLaunch& L = pl->L;
+    // tables and geometry on the device, once
+    std::vector<double> tabs;
+    TransferLaunch& L = T.L;
     L.prec = prec;
     L.D = D;
     L.P = P;
     L.E = E;
-    L.N = N;
+    L.N = T.N;
     L.NN = 1;
-    for (int k = 0; k < D; ++k) L.NN *= N;
-    // tensor rules: tables, elements, value offsets
-    std::vector<double> tabs;
-    L.nrules = (int)rule_q.size();
+    for (int k = 0; k < D; ++k) L.NN *= T.N;
+    L.nrules = (int)T.rule_q.size();
     L.max_q = max_q;
-    for (size_t r = 0; r < rule_q.size(); ++r) {
-        RuleTables<double> r64;
-        RuleTables<float> r32;
-        if (!build_rule(P, rule_q[r], r64, r32)) return fail(TWOLDG_EINVAL, "bad rule");
-        L.rule_q[r] = rule_q[r];
+    for (size_t r = 0; r < T.rule_q.size(); ++r) {
+        const RuleTables<double>& rt = store().rule(P, T.rule_q[r]);
+        L.rule_q[r] = T.rule_q[r];
         L.rule_nodes[r] = (int)tabs.size();
-        tabs.insert(tabs.end(), r64.nodes.begin(), r64.nodes.end());
+        tabs.insert(tabs.end(), rt.nodes.begin(), rt.nodes.end());
         L.rule_contract[r] = (int)tabs.size();
-        tabs.insert(tabs.end(), r64.contract.begin(), r64.contract.end());
+        tabs.insert(tabs.end(), rt.contract.begin(), rt.contract.end());
     }
-    std::vector<RuleElement> relems;
-    int64_t base = 0;
-    for (size_t r = 0; r < lists.size(); ++r) {
-        int64_t per = 1;
-        for (int k = 0; k < D; ++k) per *= rule_q[r];
-        for (const HostElem& h : lists[r]) {
-            RuleElement re{};
-            re.block = h.block;
-            for (int k = 0; k < 3; ++k) re.e[k] = h.e[k];
-            re.rule = (int)r;
-            re.base = base;
-            base += per;
-            relems.push_back(re);
+    const ElementTables<double>& et = store().element(P);
+    int M = 1;
+    for (int k = 0; k < D; ++k) M *= T.P1;
+    std::vector<double> wn(M);
+    for (int m = 0; m < M; ++m) {
+        double w = 1;
+        int r = m;
+        for (int k = 0; k < D; ++k) {
+            w = et.weights[r % T.P1] * (T.he / 2) * w;
+            r /= T.P1;
         }
-        if (r == 0) {
-            pl->counts[0] = (int64_t)lists[0].size();
-            pl->counts[1] = base;
-        } else {
-            pl->counts[2] += (int64_t)lists[r].size();
-        }
+        wn[m] = w;
     }
-    pl->counts[3] = base - pl->counts[1];
-    L.near_base = base;
-    // near elements and their chunks
-    std::vector<NearElement> nelems;
-    std::vector<NearChunk> chunks;
-    for (size_t i = 0; i < near.size(); ++i) {
-        NearElement ne{};
-        ne.block = near[i].block;
-        for (int k = 0; k < 3; ++k) ne.e[k] = near[i].e[k];
-        ne.c0 = (int32_t)chunks.size();
-        for (int64_t a = first[i]; a < first[i + 1]; a += kNearChunk)
-            chunks.push_back(NearChunk{(int32_t)a, (int32_t)std::min<int64_t>(a + kNearChunk, first[i + 1]), (int32_t)i, 0});
-        ne.c1 = (int32_t)chunks.size();
-        nelems.push_back(ne);
-    }
-    pl->counts[4] = (int64_t)near.size();
-    pl->counts[5] = (int64_t)nws.size();
-    pl->counts[6] = (int64_t)chunks.size();
-    pl->npoints = base + (int64_t)nws.size();
-    pl->counts[7] = pl->npoints;
-    L.n_rule_elems = (int64_t)relems.size();
-    L.n_chunks = (int64_t)chunks.size();
-    L.n_near_elems = (int64_t)nelems.size();
-    // element tables and the finest element's node weights
-    std::vector<double> bary64, gll64;
-    {
-        std::vector<float> b32;
-        build_bary(P, bary64, b32);
-        ElementTables<double> t64;
-        ElementTables<float> t32;
-        build_tables(P, t64, t32);
-        gll64 = t64.nodes;
-        int M = 1;
-        for (int k = 0; k < D; ++k) M *= P1;
-        std::vector<double> wn(M);
-        for (int m = 0; m < M; ++m) {
-            double w = 1;
-            int r = m;
-            for (int k = 0; k < D; ++k) {
-                w = t64.weights[r % P1] * (he / 2) * w;
-                r /= P1;
-            }
-            wn[m] = w;
-        }
-        std::vector<double> origins(d->origins, d->origins + nb * D), spacings(d->spacings, d->spacings + nb);
-        int rc = prec == 0 ? upload_all<double>(pl.get(), origins, spacings, tabs, nxs, nws, bary64, gll64, wn)
-                           : upload_all<float>(pl.get(), origins, spacings, tabs, nxs, nws, bary64, gll64, wn);
-        if (rc) return rc;
-    }
-    const void* dp = nullptr;
-    cudaError_t e = pl->upload(relems, &dp);
-    if (e != cudaSuccess) return fail(TWOLDG_ECUDA, std::string("transfer upload: ") + cudaGetErrorString(e));
-    L.rule_elems = static_cast<const RuleElement*>(dp);
-    e = pl->upload(chunks, &dp);
-    if (e != cudaSuccess) return fail(TWOLDG_ECUDA, std::string("transfer upload: ") + cudaGetErrorString(e));
-    L.chunks = static_cast<const NearChunk*>(dp);
-    e = pl->upload(nelems, &dp);
-    if (e != cudaSuccess) return fail(TWOLDG_ECUDA, std::string("transfer upload: ") + cudaGetErrorString(e));
-    L.near_elems = static_cast<const NearElement*>(dp);
-    // the density source's particles
-    L.nparticles = d->nparticles;
-    for (int k = 0; k < d->nparticles; ++k) {
-        const twoldg_particle& tp = d->particles[k];
-        TransferParticle& q_ = L.particles[k];
-        double vv = 0;
-        for (int j = 0; j < 3; ++j) {
-            q_.z[j] = tp.z[j];
-            q_.v[j] = tp.v[j];
-            vv += tp.v[j] * tp.v[j];
-        }
-        const double gamma = 1 / std::sqrt(1 - vv);
-        q_.g = gamma * gamma / (gamma + 1);
-        q_.ell = tp.ell;
-        q_.charge = tp.charge;
-    }
-    pl->density_ok = D == 3;
+    TRY_CUDA(T.d_origins.put_field(T.origins, prec), "transfer upload");
+    TRY_CUDA(T.d_spacings.put_field(T.spacings, prec), "transfer upload");
+    TRY_CUDA(T.d_tables.put_field(tabs, prec), "transfer upload");
+    TRY_CUDA(T.d_bary.put_field(store().barycentric(P), prec), "transfer upload");
+    TRY_CUDA(T.d_gll.put_field(et.nodes, prec), "transfer upload");
+    TRY_CUDA(T.d_wn.put_field(wn, prec), "transfer upload");
+    L.origins = T.d_origins.p;
+    L.spacings = T.d_spacings.p;
+    L.tables = T.d_tables.p;
+    L.bary = T.d_bary.p;
+    L.gll = T.d_gll.p;
+    L.wn = T.d_wn.p;
+    T.density_ok = D == 3;
+    int rc = T.set_particles(d->particles, d->nparticles);
+    if (rc) return rc;
     *out = pl.release();
     return TWOLDG_OK;
+}
+
+int twoldg_transfer_plan_update(twoldg_transfer_plan* plan, const twoldg_particle* particles, int32_t nparticles) {
+    if (!plan) return fail(TWOLDG_EINVAL, "plan must not be NULL");
+    return plan->set_particles(particles, nparticles);
 }
 
 int twoldg_transfer_plan_destroy(twoldg_transfer_plan* plan) {
@@ -644,7 +922,7 @@ int twoldg_transfer_points(twoldg_transfer_plan* plan, void* xs) {
 static int project(twoldg_transfer_plan* plan, int source, const void* values, void* du, double factor, int32_t var) {
     if (!plan || !du) return fail(TWOLDG_EINVAL, "plan and du must not be NULL");
     if (var != 1 && var != 2) return fail(TWOLDG_EINVAL, "var is 1 (u) or 2 (v)");
-    TransferLaunch L = plan->L;
+    TransferLaunch L = source == SOURCE_DENSITY ? plan->Ld : plan->L;
     L.source = source;
     L.values = values;
     L.du = du;

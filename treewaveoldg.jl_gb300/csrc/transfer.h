@@ -6,9 +6,15 @@
 // Gauss rules, one CTA per element evaluating S at its q^D points into shared
 // memory and contracting them there one dimension at a time (the reference's
 // two passes, source_points / contract, fused, so the points never reach
-// HBM); the nested rule near a particle runs over the point list the host
-// made, in chunks of at most kNearChunk points per element, whose per-node
-// partial sums are then added in order.
+// HBM); the nested rule near a particle runs over the host's point list,
+// which comes in innermost lines (the points that share all coordinates but
+// the last): a line's points are summed against the last dimension's Lagrange
+// polynomials into P+1 numbers, and one outer product with the other
+// dimensions' polynomials at the line's fixed coordinates adds them to the
+// element's nodes, so that the per-point work is one Lagrange evaluation and
+// P+1 multiply-adds instead of D evaluations and (P+1)^D (the reference's
+// near_partials_kernel!). Lines are taken in chunks of one element's lines,
+// whose per-node sums are added in order by a second kernel.
 #pragma once
 #include <cstdint>
 
@@ -16,7 +22,7 @@
 
 namespace twoldg {
 
-constexpr int kNearChunk = 256;
+constexpr int kNearLines = 64;    // lines per chunk, at most
 constexpr int kMaxParticles = 8;
 
 // One particle of the built-in density source rho(x) = Q rho0(|L(v)(x - z)|^2,
@@ -32,14 +38,20 @@ struct RuleElement {
     int64_t base;
 };
 
-// A near element: block, element, its chunks [c0, c1), its points from `base`.
+// A near element: block, element, its chunks [c0, c1).
 struct NearElement {
     int32_t block, e[3], c0, c1;
 };
 
-// A chunk of near points [p0, p1) of near element `elem`.
+// An innermost line of the nested rule: its points [p0, p1); its fixed
+// coordinates and the product of the outer lines' weights sit in line_vals.
+struct NearLine {
+    int32_t p0, p1;
+};
+
+// A chunk of lines [l0, l1) of near element `elem`.
 struct NearChunk {
-    int32_t p0, p1, elem, pad;
+    int32_t l0, l1, elem, pad;
 };
 
 enum { SOURCE_VALUES = 0, SOURCE_DENSITY = 1 };
@@ -59,11 +71,15 @@ struct TransferLaunch {
     int rule_contract[16] = {0};
     int max_q = 0;
     const void* tables = nullptr;    // T
-    const RuleElement* rule_elems = nullptr;
+    const RuleElement* rule_elems = nullptr;   // grouped by rule
     int64_t n_rule_elems = 0;
+    int64_t rule_start[17] = {0};              // rule r's elements: [rule_start[r], rule_start[r+1])
     // nested rule
-    const void* near_xs = nullptr;   // npoints x D, T
-    const void* near_ws = nullptr;   // npoints, T
+    const void* near_lx = nullptr;   // per point its last coordinate, T
+    const void* near_lw = nullptr;   // per point its last line's weight, T
+    const NearLine* lines = nullptr;
+    const void* line_vals = nullptr; // per line: its fixed coordinates (2) and outer weight, T
+    int64_t n_lines = 0;
     const NearChunk* chunks = nullptr;
     int64_t n_chunks = 0;
     const NearElement* near_elems = nullptr;

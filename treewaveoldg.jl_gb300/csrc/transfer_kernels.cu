@@ -1,9 +1,14 @@
 // The particle-grid transfer's device passes (src/transfer.jl:520-680,
 // 1215-1378): the tensor rules (far and graded) fused into one kernel that
 // evaluates the source at an element's q^D Gauss points into shared memory
-// and contracts them there, and the nested rule's two kernels over the
-// host's point list (per-chunk partial sums per node, then each element's
-// chunks added in order).
+// and contracts them there, and the nested rule over the host's innermost
+// lines (per line a reduction against the last dimension's Lagrange
+// polynomials and one outer product; per chunk of lines the per-node sums;
+// per element the chunks added in order).
+//
+// On GB300 these passes are bound by the FP64 pipe, not by HBM: the kernels
+// are shaped to spend as few double-precision operations per point as the
+// rules allow.
 #include "transfer.h"
 
 namespace twoldg {
@@ -11,7 +16,9 @@ namespace twoldg {
 namespace {
 
 constexpr int kRuleThreads = 128;
-constexpr int kNearThreads = 256;
+constexpr int kLineThreads = 128;   // 16 groups of kGroup lanes
+constexpr int kGroup = 8;           // lanes per line
+constexpr int kFinishThreads = 256;
 
 template <typename T, int D>
 __device__ __forceinline__ void element_box(const TransferLaunch& a, int b, const int32_t* e, T (&lo)[D], T (&hi)[D]) {
@@ -27,36 +34,23 @@ __device__ __forceinline__ void element_box(const TransferLaunch& a, int b, cons
     }
 }
 
-// S at x: the caller's value of point `idx`, or the particles' density
-// sum_k Q_k rho0(|L(v_k)(x - z_k)|^2, ell_k), rho0(q, l) = l^-3 (3465/512)
-// (1 - q/l^2)^4 / pi inside the support (src/particle.jl:117-127;
-// src/particle_forms.jl:29-37).
-template <typename T, int D>
-__device__ __forceinline__ T source_at(const TransferLaunch& a, const T (&x)[D], int64_t idx) {
-    if (a.source == SOURCE_VALUES) return static_cast<const T*>(a.values)[idx];
+// The particles' density at x: sum_k Q_k rho0(|L(v_k)(x - z_k)|^2, ell_k),
+// rho0(q, l) = l^-3 (3465/512) (1 - q/l^2)^4 / pi inside the support and 0
+// outside (src/particle.jl:117-127; src/particle_forms.jl:29-37).
+template <typename T>
+__device__ __forceinline__ T density(const TransferLaunch& a, T x0, T x1, T x2) {
     T s = T(0);
-    if constexpr (D == 3) {
-        for (int k = 0; k < a.nparticles; ++k) {
-            const TransferParticle& p = a.particles[k];
-            T r[3], vr = T(0);
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                r[d] = x[d] - T(p.z[d]);
-                vr += T(p.v[d]) * r[d];
-            }
-            const T f = T(p.g) * vr;
-            T q = T(0);
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                const T y = r[d] + f * T(p.v[d]);
-                q += y * y;
-            }
-            const T l = T(p.ell);
-            if (q < l * l) {
-                const T u = T(1) - q / (l * l);
-                const T poly = (((T(3465) / T(512)) * u) * u * u) * u;
-                s += T(p.charge) * (poly / (l * l * l) / T(3.141592653589793238462643383279502884));
-            }
+    for (int k = 0; k < a.nparticles; ++k) {
+        const TransferParticle& p = a.particles[k];
+        const T r0 = x0 - T(p.z[0]), r1 = x1 - T(p.z[1]), r2 = x2 - T(p.z[2]);
+        const T f = T(p.g) * (T(p.v[0]) * r0 + T(p.v[1]) * r1 + T(p.v[2]) * r2);
+        const T y0 = r0 + f * T(p.v[0]), y1 = r1 + f * T(p.v[1]), y2 = r2 + f * T(p.v[2]);
+        const T q = y0 * y0 + y1 * y1 + y2 * y2;
+        const T l = T(p.ell);
+        if (q < l * l) {
+            const T u = T(1) - q / (l * l);
+            const T poly = (((T(3465) / T(512)) * u) * u * u) * u;
+            s += T(p.charge) * (poly / (l * l * l) / T(3.141592653589793238462643383279502884));
         }
     }
     return s;
@@ -66,7 +60,7 @@ __device__ __forceinline__ T source_at(const TransferLaunch& a, const T (&x)[D],
 // contraction with contract[i][k] = w_k phi_i(x_k) / w^_i one dimension at a
 // time (the sum over k in order, src/transfer.jl:592-621), and factor times
 // the element's P S added to variable `var` of du.
-template <typename T, int D>
+template <typename T, int D, int SRC>
 __global__ void __launch_bounds__(kRuleThreads) tensor_rule_kernel(const TransferLaunch a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x;
@@ -79,28 +73,41 @@ __global__ void __launch_bounds__(kRuleThreads) tensor_rule_kernel(const Transfe
     for (int d = 0; d < D; ++d) cap *= cq;
     T* buf0 = reinterpret_cast<T*>(smem_raw);
     T* buf1 = buf0 + cap;
-    T* nodes = buf1 + cap;
-    T* con = nodes + a.max_q;
+    T* xg = buf1 + cap;             // D x max_q point coordinates
+    T* con = xg + D * a.max_q;
     const T* tables = static_cast<const T*>(a.tables);
-    for (int k = tid; k < q; k += blockDim.x) nodes[k] = tables[a.rule_nodes[el.rule] + k];
     for (int k = tid; k < P1 * q; k += blockDim.x) con[k] = tables[a.rule_contract[el.rule] + k];
-    __syncthreads();
-    T lo[D], hi[D];
-    element_box<T, D>(a, el.block, el.e, lo, hi);
     int npts = 1;
     for (int d = 0; d < D; ++d) npts *= q;
-    for (int j = tid; j < npts; j += blockDim.x) {
-        T x[D];
-        int r = j;
+    if (SRC == SOURCE_VALUES) {
+        const T* vals = static_cast<const T*>(a.values) + el.base;
+        for (int j = tid; j < npts; j += blockDim.x) buf0[j] = vals[j];
+        __syncthreads();
+    } else {
+        // the density's elements are those that meet a support (the host's
+        // list), so every one is evaluated
+        T lo[D], hi[D];
+        element_box<T, D>(a, el.block, el.e, lo, hi);
+        for (int k = tid; k < D * q; k += blockDim.x) {
+            const int d = k / q, j = k % q;
+            T l = lo[0], h = hi[0];
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            const int jd = r % q;
-            r /= q;
-            x[d] = lo[d] + (hi[d] - lo[d]) * (T(1) + nodes[jd]) / T(2);
+            for (int dd = 1; dd < D; ++dd)
+                if (d == dd) {
+                    l = lo[dd];
+                    h = hi[dd];
+                }
+            xg[d * a.max_q + j] = l + (h - l) * (T(1) + tables[a.rule_nodes[el.rule] + j]) / T(2);
         }
-        buf0[j] = source_at<T, D>(a, x, el.base + j);
+        __syncthreads();
+        if constexpr (D == 3) {
+            for (int j = tid; j < npts; j += blockDim.x) {
+                const int j0 = j % q, j1 = (j / q) % q, j2 = j / (q * q);
+                buf0[j] = density<T>(a, xg[j0], xg[a.max_q + j1], xg[2 * a.max_q + j2]);
+            }
+        }
+        __syncthreads();
     }
-    __syncthreads();
     T* in = buf0;
     T* out = buf1;
 #pragma unroll
@@ -144,97 +151,213 @@ __global__ void __launch_bounds__(kRuleThreads) tensor_rule_kernel(const Transfe
     }
 }
 
-// The nested rule, pass 1: chunk c's points summed for every node m of their
-// element, sum_p w_p (S(x_p) phi_m(x_p)), with phi_m the product of the
-// dimensions' Lagrange polynomials in their product form (src/transfer.jl:
-// 171-182, 1330-1352).
-template <typename T, int D>
-__global__ void __launch_bounds__(kNearThreads) near_partials_kernel(const TransferLaunch a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int tid = threadIdx.x;
-    const int P1 = a.P + 1;
-    const NearChunk ch = a.chunks[blockIdx.x];
-    const NearElement ne = a.near_elems[ch.elem];
-    const int n = ch.p1 - ch.p0;
-    T* sv = reinterpret_cast<T*>(smem_raw);   // S at the points
-    T* sw = sv + kNearChunk;                  // their weights
-    T* lag = sw + kNearChunk;                 // [p][d][i]
-    T lo[D], hi[D];
-    element_box<T, D>(a, ne.block, ne.e, lo, hi);
-    const T* xs = static_cast<const T*>(a.near_xs);
-    const T* bary = static_cast<const T*>(a.bary);
-    const T* gll = static_cast<const T*>(a.gll);
-    for (int p = tid; p < n; p += blockDim.x) {
-        const int64_t g = ch.p0 + p;
-        T x[D];
+// phi_i(xi) for every node i, bary_i prod_{j != i} (xi - x^_j), by prefix and
+// suffix products of the differences.
+template <typename T, int P1>
+__device__ __forceinline__ void lagrange_all(const T (&nodes)[P1], const T (&bary)[P1], T xi, T (&phi)[P1]) {
+    T diff[P1], pre[P1];
 #pragma unroll
-        for (int d = 0; d < D; ++d) x[d] = xs[g * D + d];
-        sv[p] = source_at<T, D>(a, x, a.near_base + g);
-        sw[p] = static_cast<const T*>(a.near_ws)[g];
+    for (int j = 0; j < P1; ++j) diff[j] = xi - nodes[j];
+    pre[0] = T(1);
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            const T xi = (T(2) * x[d] - lo[d] - hi[d]) / (hi[d] - lo[d]);
-            for (int i = 0; i < P1; ++i) {
-                T acc = bary[i];
-                for (int j = 0; j < P1; ++j)
-                    if (j != i) acc *= xi - gll[j];
-                lag[(p * D + d) * P1 + i] = acc;
-            }
-        }
-    }
-    __syncthreads();
-    int M = 1;
-    for (int d = 0; d < D; ++d) M *= P1;
-    T* partials = static_cast<T*>(a.partials) + (int64_t)blockIdx.x * M;
-    for (int m = tid; m < M; m += blockDim.x) {
-        int K[D];
-        int r = m;
+    for (int j = 1; j < P1; ++j) pre[j] = pre[j - 1] * diff[j - 1];
+    T suf = T(1);
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            K[d] = r % P1;
-            r /= P1;
-        }
-        T acc = T(0);
-        for (int p = 0; p < n; ++p) {
-            T phi = T(1);
-#pragma unroll
-            for (int d = 0; d < D; ++d) phi = lag[(p * D + d) * P1 + K[d]] * phi;
-            acc += sw[p] * (sv[p] * phi);
-        }
-        partials[m] = acc;
+    for (int i = P1 - 1; i >= 0; --i) {
+        phi[i] = bary[i] * (pre[i] * suf);
+        suf *= diff[i];
     }
 }
 
-// The nested rule, pass 2: element i's chunks added in order for node m, and
-// factor times that over w_m added to its node (src/transfer.jl:1354-1369).
+template <typename T, int P1>
+__device__ __forceinline__ T lagrange_one(const T (&nodes)[P1], const T (&bary)[P1], T xi, int i) {
+    T acc = T(0);
+#pragma unroll
+    for (int k = 0; k < P1; ++k) {
+        if (k != i) continue;
+        acc = bary[k];
+#pragma unroll
+        for (int j = 0; j < P1; ++j)
+            if (j != k) acc *= xi - nodes[j];
+    }
+    return acc;
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl8(unsigned mask, T v, int src) {
+    return __shfl_sync(mask, v, src, kGroup);
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl8_xor(unsigned mask, T v, int off) {
+    return __shfl_xor_sync(mask, v, off, kGroup);
+}
+
+// The nested rule, one CTA per chunk of an element's innermost lines, a group
+// of kGroup lanes per line: the line's points summed against the last
+// dimension's Lagrange polynomials, r_i = sum_p w_p S(x_p) phi_i(x_p,last);
+// then node (K_0 .. K_D-1) gets w_line prod_{d<D-1} phi_{K_d}(x_d) r_{K_D-1},
+// the product of the point's line weights and Lagrange values regrouped
+// (src/transfer.jl:1330-1352). The chunk's per-node sums go to partials.
+template <typename T, int D, int P1, int SRC>
+__global__ void __launch_bounds__(kLineThreads) near_lines_kernel(const TransferLaunch a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int M = D == 1 ? P1 : (D == 2 ? P1 * P1 : P1 * P1 * P1);
+    constexpr int MO = M / P1;                       // nodes of the outer dimensions
+    constexpr int NPL = (M + kGroup - 1) / kGroup;   // nodes per lane
+    constexpr int NOUT = (D - 1) * P1;               // outer Lagrange values per line
+    const int tid = threadIdx.x;
+    const int group = tid / kGroup, lane = tid % kGroup, ngroups = blockDim.x / kGroup;
+    const unsigned mask = 0xffu << ((tid % 32) / kGroup * kGroup);
+    const NearChunk ch = a.chunks[blockIdx.x];
+    const NearElement ne = a.near_elems[ch.elem];
+    T lo[D], hi[D];
+    element_box<T, D>(a, ne.block, ne.e, lo, hi);
+    T sum[D], inv[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        sum[d] = lo[d] + hi[d];
+        inv[d] = T(1) / (hi[d] - lo[d]);
+    }
+    T nodes[P1], bary[P1];
+#pragma unroll
+    for (int i = 0; i < P1; ++i) {
+        nodes[i] = static_cast<const T*>(a.gll)[i];
+        bary[i] = static_cast<const T*>(a.bary)[i];
+    }
+    const T* lx = static_cast<const T*>(a.near_lx);
+    const T* lw = static_cast<const T*>(a.near_lw);
+    const T* lv = static_cast<const T*>(a.line_vals);
+    const T* vals = static_cast<const T*>(a.values);
+    T acc[NPL];
+#pragma unroll
+    for (int k = 0; k < NPL; ++k) acc[k] = T(0);
+    for (int l = ch.l0 + group; l < ch.l1; l += ngroups) {
+        const NearLine L = a.lines[l];
+        const T pre0 = lv[3 * (int64_t)l], pre1 = lv[3 * (int64_t)l + 1], wl = lv[3 * (int64_t)l + 2];
+        T r[P1];
+#pragma unroll
+        for (int i = 0; i < P1; ++i) r[i] = T(0);
+        for (int p = L.p0 + lane; p < L.p1; p += kGroup) {
+            const T x = lx[p];
+            T phi[P1];
+            lagrange_all<T, P1>(nodes, bary, (T(2) * x - sum[D - 1]) * inv[D - 1], phi);
+            T S;
+            if (SRC == SOURCE_VALUES) {
+                S = vals[a.near_base + p];
+            } else {
+                S = D == 3 ? density<T>(a, pre0, pre1, x) : T(0);
+            }
+            const T c = lw[p] * S;
+#pragma unroll
+            for (int i = 0; i < P1; ++i) r[i] += c * phi[i];
+        }
+#pragma unroll
+        for (int off = kGroup / 2; off > 0; off /= 2)
+#pragma unroll
+            for (int i = 0; i < P1; ++i) r[i] += shfl8_xor(mask, r[i], off);
+        // the outer dimensions' Lagrange values at the line's fixed
+        // coordinates, value j = d (P+1) + i on lane j % kGroup
+        T ov[(NOUT + kGroup - 1) / kGroup + 1];
+#pragma unroll
+        for (int s = 0; s * kGroup < NOUT; ++s) {
+            const int j = s * kGroup + lane;
+            T v = T(0);
+            if (j < NOUT) {
+                const int d = j / P1, i = j % P1;
+                // select, not an index: the arrays stay in registers
+                const T xc = d == 0 ? pre0 : pre1;
+                const T sd = d == 0 ? sum[0] : sum[D > 1 ? 1 : 0];
+                const T id = d == 0 ? inv[0] : inv[D > 1 ? 1 : 0];
+                v = lagrange_one<T, P1>(nodes, bary, (T(2) * xc - sd) * id, i);
+            }
+            ov[s] = v;
+        }
+#pragma unroll
+        for (int k = 0; k < NPL; ++k) {
+            const int m = lane + kGroup * k;
+            const int mm = m < M ? m : 0;
+            const int Klast = mm / MO;
+            int o = mm % MO;
+            T outer = wl;
+#pragma unroll
+            for (int d = 0; d < D - 1; ++d) {
+                const int j = d * P1 + o % P1;
+                o /= P1;
+                T got = T(0);
+#pragma unroll
+                for (int s = 0; s * kGroup < NOUT; ++s) {
+                    const T t = shfl8(mask, ov[s], j % kGroup);
+                    if (j / kGroup == s) got = t;
+                }
+                outer *= got;
+            }
+            T rk = T(0);
+#pragma unroll
+            for (int i = 0; i < P1; ++i)
+                if (i == Klast) rk = r[i];
+            if (m < M) acc[k] += outer * rk;
+        }
+    }
+    // the groups' sums, added in group order
+    T* red = reinterpret_cast<T*>(smem_raw);   // ngroups x M
+#pragma unroll
+    for (int k = 0; k < NPL; ++k) {
+        const int m = lane + kGroup * k;
+        if (m < M) red[group * M + m] = acc[k];
+    }
+    __syncthreads();
+    T* partials = static_cast<T*>(a.partials) + (int64_t)blockIdx.x * M;
+    for (int m = tid; m < M; m += blockDim.x) {
+        T s = T(0);
+        for (int g = 0; g < ngroups; ++g) s += red[g * M + m];
+        partials[m] = s;
+    }
+}
+
+// The nested rule's last pass: element i's chunks added in order for node m,
+// split over the CTA's threads and added back in thread order, and factor
+// times that over w_m added to its node (src/transfer.jl:1354-1369).
 template <typename T, int D>
-__global__ void near_finish_kernel(const TransferLaunch a) {
+__global__ void __launch_bounds__(kFinishThreads) near_finish_kernel(const TransferLaunch a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* red = reinterpret_cast<T*>(smem_raw);
     const NearElement ne = a.near_elems[blockIdx.x];
     const int P1 = a.P + 1;
     int M = 1;
     for (int d = 0; d < D; ++d) M *= P1;
+    const int split = M >= kFinishThreads ? 1 : kFinishThreads / M;
     const T* partials = static_cast<const T*>(a.partials);
     const T* wn = static_cast<const T*>(a.wn);
     T* du = static_cast<T*>(a.du) + (int64_t)ne.block * 2 * a.NN + (int64_t)(a.var - 1) * a.NN;
     const T factor = T(a.factor);
-    for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    for (int m0 = 0; m0 < M; m0 += kFinishThreads / split) {
+        const int m = m0 + threadIdx.x / split, g = threadIdx.x % split;
         T acc = T(0);
-        for (int c = ne.c0; c < ne.c1; ++c) acc += partials[(int64_t)c * M + m];
-        int r = m;
-        int64_t idx = 0, stride = 1;
+        if (m < M)
+            for (int c = ne.c0 + g; c < ne.c1; c += split) acc += partials[(int64_t)c * M + m];
+        red[threadIdx.x] = acc;
+        __syncthreads();
+        if (m < M && g == 0) {
+            T s = T(0);
+            for (int k = 0; k < split; ++k) s += red[threadIdx.x + k];
+            int r = m;
+            int64_t idx = 0, stride = 1;
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            const int K = r % P1;
-            r /= P1;
-            idx += (int64_t)(ne.e[d] * P1 + K) * stride;
-            stride *= a.N;
+            for (int d = 0; d < D; ++d) {
+                const int K = r % P1;
+                r /= P1;
+                idx += (int64_t)(ne.e[d] * P1 + K) * stride;
+                stride *= a.N;
+            }
+            du[idx] += factor * s / wn[m];
         }
-        du[idx] += factor * acc / wn[m];
+        __syncthreads();
     }
 }
 
 // Every point of the plan: the tensor rules' (one CTA per element), then the
-// near points, as (D, npoints).
+// near points (a warp per line), as (D, npoints).
 template <typename T, int D>
 __global__ void rule_points_kernel(const TransferLaunch a, T* xs, int64_t npoints) {
     const RuleElement el = a.rule_elems[blockIdx.x];
@@ -256,12 +379,18 @@ __global__ void rule_points_kernel(const TransferLaunch a, T* xs, int64_t npoint
 }
 
 template <typename T, int D>
-__global__ void near_points_kernel(const TransferLaunch a, T* xs, int64_t npoints, int64_t nnear) {
-    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nnear) return;
-    const T* src = static_cast<const T*>(a.near_xs);
+__global__ void near_points_kernel(const TransferLaunch a, T* xs, int64_t npoints) {
+    const int64_t l = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    if (l >= a.n_lines) return;
+    const NearLine L = a.lines[l];
+    const T* lv = static_cast<const T*>(a.line_vals);
+    const T* lx = static_cast<const T*>(a.near_lx);
+    for (int p = L.p0 + threadIdx.x % 32; p < L.p1; p += 32) {
+        const int64_t at = a.near_base + p;
 #pragma unroll
-    for (int d = 0; d < D; ++d) xs[(int64_t)d * npoints + a.near_base + p] = src[p * D + d];
+        for (int d = 0; d < D - 1; ++d) xs[(int64_t)d * npoints + at] = lv[3 * l + d];
+        xs[(int64_t)(D - 1) * npoints + at] = lx[p];
+    }
 }
 
 template <typename T, int D>
@@ -269,34 +398,66 @@ size_t rule_smem(const TransferLaunch& a) {
     const size_t cq = (size_t)(a.max_q > a.P + 1 ? a.max_q : a.P + 1);
     size_t cap = 1;
     for (int d = 0; d < D; ++d) cap *= cq;
-    return (2 * cap + (size_t)a.max_q * (a.P + 2)) * sizeof(T);
+    return (2 * cap + (size_t)a.max_q * (D + a.P + 1)) * sizeof(T);
 }
 
-template <typename T, int D>
-size_t near_smem(const TransferLaunch& a) {
-    return ((size_t)2 * kNearChunk + (size_t)kNearChunk * D * (a.P + 1)) * sizeof(T);
+// One launch per rule, its shared memory sized for that rule's q: the far
+// rule's q = P + 3 needs a fraction of the largest graded band's.
+template <typename T, int D, int SRC>
+cudaError_t run_rules(const TransferLaunch& a, cudaStream_t stream) {
+    cudaError_t e = cudaFuncSetAttribute(tensor_rule_kernel<T, D, SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)rule_smem<T, D>(a));
+    if (e != cudaSuccess) return e;
+    for (int r = 0; r < a.nrules; ++r) {
+        const int64_t n = a.rule_start[r + 1] - a.rule_start[r];
+        if (n <= 0) continue;
+        TransferLaunch b = a;
+        b.rule_elems = a.rule_elems + a.rule_start[r];
+        b.max_q = a.rule_q[r];
+        tensor_rule_kernel<T, D, SRC><<<(unsigned)n, kRuleThreads, rule_smem<T, D>(b), stream>>>(b);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+template <typename T, int D, int P1, int SRC>
+cudaError_t run_lines(const TransferLaunch& a, cudaStream_t stream) {
+    constexpr int M = D == 1 ? P1 : (D == 2 ? P1 * P1 : P1 * P1 * P1);
+    const size_t smem = (size_t)(kLineThreads / kGroup) * M * sizeof(T);
+    cudaError_t e = cudaFuncSetAttribute(near_lines_kernel<T, D, P1, SRC>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    near_lines_kernel<T, D, P1, SRC><<<(unsigned)a.n_chunks, kLineThreads, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T, int D, int SRC>
+cudaError_t run_lines_p(const TransferLaunch& a, cudaStream_t stream) {
+    switch (a.P + 1) {
+        case 2: return run_lines<T, D, 2, SRC>(a, stream);
+        case 3: return run_lines<T, D, 3, SRC>(a, stream);
+        case 4: return run_lines<T, D, 4, SRC>(a, stream);
+        case 5: return run_lines<T, D, 5, SRC>(a, stream);
+        case 6: return run_lines<T, D, 6, SRC>(a, stream);
+        case 7: return run_lines<T, D, 7, SRC>(a, stream);
+    }
+    return cudaErrorInvalidValue;
 }
 
 template <typename T, int D>
 cudaError_t projection(const TransferLaunch& a, cudaStream_t stream) {
+    cudaError_t e;
     if (a.n_rule_elems > 0) {
-        const size_t smem = rule_smem<T, D>(a);
-        cudaError_t e = cudaFuncSetAttribute(tensor_rule_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        tensor_rule_kernel<T, D><<<(unsigned)a.n_rule_elems, kRuleThreads, smem, stream>>>(a);
-        e = cudaGetLastError();
+        e = a.source == SOURCE_VALUES ? run_rules<T, D, SOURCE_VALUES>(a, stream)
+                                      : run_rules<T, D, SOURCE_DENSITY>(a, stream);
         if (e != cudaSuccess) return e;
     }
     if (a.n_chunks > 0) {
-        const size_t smem = near_smem<T, D>(a);
-        cudaError_t e = cudaFuncSetAttribute(near_partials_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
+        e = a.source == SOURCE_VALUES ? run_lines_p<T, D, SOURCE_VALUES>(a, stream)
+                                      : run_lines_p<T, D, SOURCE_DENSITY>(a, stream);
         if (e != cudaSuccess) return e;
-        near_partials_kernel<T, D><<<(unsigned)a.n_chunks, kNearThreads, smem, stream>>>(a);
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-        near_finish_kernel<T, D><<<(unsigned)a.n_near_elems, 128, 0, stream>>>(a);
+        near_finish_kernel<T, D><<<(unsigned)a.n_near_elems, kFinishThreads, kFinishThreads * sizeof(T), stream>>>(a);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -310,10 +471,8 @@ cudaError_t points(const TransferLaunch& a, void* xs, int64_t npoints, cudaStrea
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    const int64_t nnear = npoints - a.near_base;
-    if (nnear > 0) {
-        near_points_kernel<T, D><<<(unsigned)((nnear + 255) / 256), 256, 0, stream>>>(a, static_cast<T*>(xs), npoints,
-                                                                                     nnear);
+    if (a.n_lines > 0) {
+        near_points_kernel<T, D><<<(unsigned)((a.n_lines + 7) / 8), 256, 0, stream>>>(a, static_cast<T*>(xs), npoints);
         return cudaGetLastError();
     }
     return cudaSuccess;

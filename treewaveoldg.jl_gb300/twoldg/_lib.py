@@ -21,7 +21,8 @@ EXPORTS = [
     "twoldg_synchronize", "twoldg_batch_create", "twoldg_batch_destroy", "twoldg_batch_offsets",
     "twoldg_batch_rk4_step", "twoldg_batch_synchronize", "twoldg_profile_step", "twoldg_stream",
     "twoldg_rhs_static", "twoldg_autotune", "twoldg_batch_autotune", "twoldg_transfer", "twoldg_gather",
-    "twoldg_transfer_plan_create", "twoldg_transfer_plan_destroy", "twoldg_transfer_plan_counts",
+    "twoldg_transfer_plan_create", "twoldg_transfer_plan_update", "twoldg_transfer_plan_destroy",
+    "twoldg_transfer_plan_counts",
     "twoldg_transfer_points", "twoldg_project_values", "twoldg_project_density", "twoldg_transfer_table",
 ]
 
@@ -115,6 +116,7 @@ def lib():
             "twoldg_batch_autotune": (ctypes.c_int, [vp, vp, ctypes.POINTER(d), ctypes.c_char_p, ctypes.c_char_p,
                                                      ctypes.c_size_t]),
             "twoldg_transfer_plan_create": (ctypes.c_int, [vp, ctypes.POINTER(TransferDesc), ctypes.POINTER(vp)]),
+            "twoldg_transfer_plan_update": (ctypes.c_int, [vp, ctypes.POINTER(Particle), i32]),
             "twoldg_transfer_plan_destroy": (ctypes.c_int, [vp]),
             "twoldg_transfer_plan_counts": (ctypes.c_int, [vp, ctypes.POINTER(i64)]),
             "twoldg_transfer_points": (ctypes.c_int, [vp, vp]),

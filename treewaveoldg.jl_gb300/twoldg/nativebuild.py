@@ -61,7 +61,7 @@ def _compile(src, nvcc, verbose):
             cmd.insert(1, "-Xptxas=-v")
     else:
         cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "include")
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-pthread",
                "-I" + cuda_inc, "-c", path, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -88,7 +88,7 @@ def build(force=False, verbose=False):
             if log.strip():
                 print(o, "\n", log, file=sys.stderr)
     tmp = lib_path() + ".tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "static"]
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "static", "-Xcompiler", "-pthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))

@@ -121,15 +121,10 @@ class TransferPlan:
         if len(centre) != D:
             raise ValueError("the ball's centre has %d coordinates in %d dimensions" % (len(centre), D))
         from .ball import BallForest
-        if isinstance(p.forest, BallForest):
-            # the transfer works in the cube alone (check_in_patch, src/transfer.jl:802-812)
-            for what, lo, hi in [("the source's ball of radius %r about %r" % (R, centre),
-                                  [c - R for c in centre], [c + R for c in centre])] + \
-                    [("the support of radius %r about z = %r" % (s.ell, s.z), [z - s.ell for z in s.z],
-                      [z + s.ell for z in s.z]) for s in self.particles]:
-                if not all(dom[d][0] <= lo[d] and hi[d] <= dom[d][1] for d in range(D)):
-                    raise ValueError("the transfer needs %s inside the ball's cube patch, %r, where the particles "
-                                     "run" % (what, dom))
+        self.frame_domain = dom if isinstance(p.forest, BallForest) else None
+        if self.frame_domain is not None:
+            self._check_in_patch([("the source's ball of radius %r about %r" % (R, centre),
+                                   [c - R for c in centre], [c + R for c in centre])])
         self._arrays = [np.ascontiguousarray(origins.reshape(-1), dtype=np.float64),
                         np.ascontiguousarray(spacings, dtype=np.float64), np.ascontiguousarray(levels),
                         np.ascontiguousarray(mask)]
@@ -163,11 +158,38 @@ class TransferPlan:
         h = ctypes.c_void_p()
         _lib.check(_lib.lib().twoldg_transfer_plan_create(p.handle, ctypes.byref(d), ctypes.byref(h)))
         self._h = h
+        self._read_counts()
+
+    def _read_counts(self):
         c = (ctypes.c_int64 * 8)()
-        _lib.check(_lib.lib().twoldg_transfer_plan_counts(h, c))
+        _lib.check(_lib.lib().twoldg_transfer_plan_counts(self._h, c))
         keys = ("far_elements", "far_points", "graded_elements", "graded_points", "near_elements", "near_points",
                 "near_chunks", "points")
         self.counts = dict(zip(keys, [int(x) for x in c]))
+
+    def update(self, particles):
+        """The plan for the particles at new positions: the ball, the frame
+        and the quadrature stay (the reference's SourceBall), the elements by
+        rule and the nested rule's points are redone."""
+        self.particles = tuple(particles)
+        if self.frame_domain is not None:
+            self._check_in_patch([])
+        parts = (_lib.Particle * max(1, len(self.particles)))(*[s._c() for s in self.particles])
+        _lib.check(_lib.lib().twoldg_transfer_plan_update(self._h, ctypes.cast(parts, ctypes.POINTER(_lib.Particle)),
+                                                          len(self.particles)))
+        self._parts = parts
+        self._read_counts()
+        return self
+
+    def _check_in_patch(self, extra):
+        """The transfer works in the cube alone (check_in_patch, src/transfer.jl:802-812)."""
+        dom = self.frame_domain
+        D = self.p.D
+        for what, lo, hi in extra + [("the support of radius %r about z = %r" % (s.ell, s.z),
+                                      [z - s.ell for z in s.z], [z + s.ell for z in s.z]) for s in self.particles]:
+            if not all(dom[d][0] <= lo[d] and hi[d] <= dom[d][1] for d in range(D)):
+                raise ValueError("the transfer needs %s inside the ball's cube patch, %r, where the particles run"
+                                 % (what, dom))
 
     def close(self):
         if getattr(self, "_h", None):
