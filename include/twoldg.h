@@ -340,6 +340,15 @@ int twoldg_project_values(twoldg_transfer_plan* plan, const void* values, void* 
 /* The same with S the particles' density sum_k Q_k rho0(|L(v_k)(x - z_k)|),
  * evaluated on the device (dim 3). Asynchronous. */
 int twoldg_project_density(twoldg_transfer_plan* plan, void* du, double factor, int32_t var);
+/* average_shared!(ua, sn, var) -- src/transfer.jl:1616-1714, SharedNodes
+ * :1520-1614: variable var (1 or 2) of the state u, in the blocks the plan's
+ * ball meets, with every node that elements share replaced by the mean over
+ * them (two on a face, four on an edge, eight at a corner in 3D), one
+ * dimension at a time, each pair of coincident nodes across a face taking
+ * their mean, the lower one's value first. A face to a block outside the
+ * ball's, on another level or past the domain (no periodic images) is left
+ * alone. Asynchronous on the problem's stream. */
+int twoldg_average_shared(twoldg_transfer_plan* plan, void* u, int32_t var);
 /* A transfer table of order P in float64 (precision 0) or float32 (1):
  * "bary" (P+1), and of the q-point Gauss-Legendre rule "gauss_nodes" (q),
  * "gauss_weights" (q), "lagrange" (q x (P+1)), "contract" ((P+1) x q); built

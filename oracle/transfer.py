@@ -437,3 +437,50 @@ def weighted_inner(mesh, t, a, b, var):
             idx = mesh.node_index(blk, e, var)
             acc += float(np.sum(wn * a[idx] * b[idx]))
     return acc
+
+
+def average_shared(u, mesh, ball, var):
+    """average_shared!(ua, sn, var) (src/transfer.jl:1616-1714) on the flat
+    state vector u (numpy, in place): in the frame's blocks that the ball
+    meets, D passes; in pass d every pair of coincident nodes across a face
+    along d -- between a block's elements, and across its upper face to the
+    ball's block there on the same level -- takes their mean, the lower
+    node's value first. No periodic images."""
+    D, N, P1, E = mesh.D, mesh.N, mesh.P + 1, mesh.E
+    c, R = np.asarray(ball[0], dtype=np.float64), float(ball[1])
+    lo = mesh.origins
+    hi = mesh.origins + mesh.spacings[:, None] * N
+    blocks = [b for b in range(mesh.nblocks)
+              if mesh.mask[b] and box_distance2(c, lo[b], hi[b], range(D)) < R * R]
+    member = set(blocks)
+
+    def across(b, d):
+        h = mesh.spacings[b]
+        x = [lo[b, k] + h * N / 2 if k != d else lo[b, k] + h * (N + 0.5) for k in range(D)]
+        for g in range(mesh.nblocks):
+            if mesh.mask[g] and all(lo[g, k] <= x[k] < hi[g, k] for k in range(D)):
+                return g if g in member and mesh.spacings[g] == h else None
+        return None
+
+    U = u.reshape(mesh.nblocks, 2, mesh.NN)
+    for d in range(D):
+        ax = D - 1 - d              # dimension d is axis D-1-d of a block's (N,)*D view
+        for b in blocks:
+            a = U[b, var - 1].reshape((N,) * D)
+            for k in range(1, E):
+                i1 = [slice(None)] * D
+                i2 = [slice(None)] * D
+                i1[ax], i2[ax] = k * P1 - 1, k * P1
+                m = (a[tuple(i1)] + a[tuple(i2)]) / 2
+                a[tuple(i1)] = m
+                a[tuple(i2)] = m
+            bn = across(b, d)
+            if bn is not None:
+                an = U[bn, var - 1].reshape((N,) * D)
+                i1 = [slice(None)] * D
+                i2 = [slice(None)] * D
+                i1[ax], i2[ax] = N - 1, 0
+                m = (a[tuple(i1)] + an[tuple(i2)]) / 2
+                a[tuple(i1)] = m
+                an[tuple(i2)] = m
+    return u

@@ -336,3 +336,71 @@ def test_updated_plan_projects_as_a_fresh_one(native):
         plan.project(d1, src)
         fresh.project(d2, src)
         assert torch.equal(d1, d2)
+
+
+@pytest.mark.parametrize("D,roots,ball", [(2, 3, ((0.4, 0.55), 0.5)), (3, 2, ((0.5, 0.5, 0.5), 2.0))])
+def test_averaging_matches_the_oracle_bit_for_bit(native, D, roots, ball):
+    # average_shared! (src/transfer.jl:1616-1714): each pair of coincident
+    # nodes takes (lower + upper) / 2, in the ball's blocks
+    import torch
+    from twoldg import TransferPlan
+    p = _problem(D, 3, roots)
+    rng = np.random.default_rng(11)
+    host = rng.standard_normal(p.state_words)
+    u = torch.from_numpy(host.copy()).cuda()
+    plan = TransferPlan(p, [], ball)
+    plan.average_shared(u, var=2)
+    ref = T.average_shared(host.copy(), _mesh(p), ball, 2)
+    assert np.array_equal(_host(u), ref)
+    plan.average_shared(u, var=1)
+    assert np.array_equal(_host(u), T.average_shared(ref.copy(), _mesh(p), ball, 1))
+
+
+def test_source_rhs_is_the_wave_rhs_less_the_averaged_projection(native):
+    # inspiral_rhs!'s field part (src/inspiral.jl): wave_rhs!, the projected
+    # source subtracted from v's rate, the averaging over shared nodes
+    import torch
+    import twoldg
+    from oracle.oracle import Oracle
+    from cases import smooth_data, state_from
+    p = _problem(3, 3, 2)
+    o = Oracle(p.forest, 3)
+    u0 = o.truncate(state_from(p.forest, 3, smooth_data(3)))
+    z = np.array([0.52, 0.46, 0.49])
+    v = np.array([0.05, 0.1, -0.02])
+    s = twoldg.ParticleSupport(z, v, 0.03, charge=0.4)
+    ball = ((0.5, 0.5, 0.5), 0.7)
+    plan = twoldg.TransferPlan(p, [s], ball)
+    du = p.statevector()
+    twoldg.source_rhs(du, torch.from_numpy(u0).cuda(), p, plan, "density")
+    ref = o.rhs(u0)
+    T.project_source(ref, _mesh(p), T.Tables(3), lambda X: T.particle_density(X, z, v, 0.03, 0.4),
+                     [T.Support(z, v, 0.03)], ball, factor=-1.0, var=2, he=0.25)
+    T.average_shared(ref, _mesh(p), ball, 2)
+    assert np.abs(_host(du) - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_projection_in_the_ball_cube_keeps_the_charge(native):
+    # the particles' frame on the seven-patch ball is its affine cube
+    # (ParticleFrame, src/transfer.jl:705-766): a particle there projects
+    # its charge Q / gamma onto the cube's nodes
+    import twoldg
+    forest, geo = twoldg.sevenpatch_forest(np.float64, 3, 2, roots=(4, 4), Lc=1.0, R1=3.0)
+    p = twoldg.WaveProblem(forest, twoldg.Element(np.float64, 3), truncate=True, geometry=geo,
+                           boundary=twoldg.RadiativeBoundary())
+    v = np.array([0.1, 0.05, -0.2])
+    z = np.array([0.013, -0.021, 0.008])
+    Q, ell = 0.2, 0.01
+    du = p.statevector()
+    twoldg.project_source(du, p, "density", [twoldg.ParticleSupport(z, v, ell, charge=Q)], (z, 3 * ell),
+                          factor=1.0, var=1)
+    got = _host(du).reshape(p.nblocks, 2, p.NN)
+    scale = 2 * geo.Lc / 4
+    w1 = np.tile(T.Tables(3).weights, 2) * (scale / p.N * 4 / 2)
+    w = (w1[:, None, None] * w1[None, :, None] * w1[None, None, :]).reshape(-1)
+    total = sum(float(np.sum(w * got[b, 0])) for b, (patch, _) in enumerate(forest.blocks) if patch == 0)
+    assert np.abs(got[[b for b, (q, _) in enumerate(forest.blocks) if q != 0], 0]).max() == 0
+    gamma = 1 / math.sqrt(1 - v @ v)
+    assert total == pytest.approx(Q / gamma, rel=1e-12)
+    with pytest.raises(ValueError, match="cube"):
+        twoldg.TransferPlan(p, [twoldg.ParticleSupport((0.99, 0.0, 0.0), (0, 0, 0), 0.05)], ((0.5, 0, 0), 0.2))

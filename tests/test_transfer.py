@@ -213,3 +213,38 @@ def test_first_run_window_has_the_reference_far_count():
     far, graded, near = T.classify(mesh, T.Tables(3), parts, ball, 1.0, 0.125)
     assert len(far) == 31102
     assert [len(g) for g in graded] == [134, 266, 438, 5240] and len(near) == 44
+
+
+def test_oracle_averaging_is_the_projection_onto_continuous_fields():
+    # average_shared! (src/transfer.jl:1616-1714): shared nodes end equal,
+    # a second averaging changes nothing, sum w u is kept, and a continuous
+    # field (a polynomial at the nodes) is left as it is
+    for D in (2, 3):
+        mesh = T.brick_mesh(D, 3, 2, 2)
+        t = T.Tables(3)
+        rng = np.random.default_rng(5)
+        u = rng.standard_normal(mesh.nblocks * 2 * mesh.NN)
+        w0 = T.weighted_inner(mesh, t, u, np.ones_like(u), 2)
+        ball = (np.full(D, 0.5), 10.0)
+        a = T.average_shared(u.copy(), mesh, ball, 2)
+        assert np.array_equal(T.average_shared(a.copy(), mesh, ball, 2), a)
+        assert T.weighted_inner(mesh, t, a, np.ones_like(a), 2) == pytest.approx(w0, rel=1e-13)
+        # coincident nodes across the face between blocks 0 and its upper
+        # neighbour along dimension 0 (blocks listed with dimension 0 fastest)
+        N = mesh.N
+        A = a.reshape(mesh.nblocks, 2, mesh.NN)[:, 1]
+        f0 = A[0].reshape((N,) * D)[..., N - 1]
+        f1 = A[1].reshape((N,) * D)[..., 0]
+        assert np.array_equal(f0, f1)
+        # a continuous field
+        g = np.zeros_like(u)
+        for b in range(mesh.nblocks):
+            for J in np.ndindex(*([2] * D)):
+                e = tuple(reversed(J))
+                lo, hi = mesh.element_box(b, e)
+                grids = [lo[d] + (hi[d] - lo[d]) * (1 + t.nodes) / 2 for d in range(D)]
+                m = np.meshgrid(*grids, indexing="ij")
+                X = np.stack([x.reshape(-1) for x in m], axis=1)
+                vals = (1 + X[:, 0] * X[:, -1]).reshape((4,) * D)
+                g[mesh.node_index(b, e, 2)] = np.transpose(vals, tuple(range(D - 1, -1, -1))).reshape(-1)
+        assert np.allclose(T.average_shared(g.copy(), mesh, ball, 2), g, rtol=0, atol=1e-15)

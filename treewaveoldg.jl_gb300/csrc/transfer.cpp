@@ -21,6 +21,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "../../include/twoldg.h"
@@ -347,6 +348,9 @@ struct twoldg_transfer_plan {
     NestedTables nt;
     std::vector<int64_t> ball_blocks;   // the frame's blocks that meet the ball
     DevVec d_origins, d_spacings, d_tables, d_bary, d_gll, d_wn;
+    // the averaging's blocks and upper neighbours (SharedNodes)
+    DevVec d_avg_blocks, d_avg_upper;
+    AverageLaunch A;
     // what the particles decide
     DevVec d_relems, d_lx, d_lw, d_vals, d_lines, d_chunks, d_nelems, d_partials;
     DevVec d_drelems, d_dvals, d_dlines, d_dchunks, d_delems, d_dpartials;
@@ -844,6 +848,54 @@ int twoldg_transfer_plan_create(twoldg_problem* p, const twoldg_transfer_desc* d
                             "width h_e, and would integrate a coarser element with a rule chosen for a finer one");
         T.ball_blocks.push_back(b);
     }
+    // The averaging's pairs (SharedNodes, src/transfer.jl:1520-1614): per ball
+    // block and dimension the ball block across its upper face on the same
+    // level, found by its integer position among the blocks of its spacing
+    // (counted from the first such block, in block widths); no periodic images.
+    {
+        std::map<uint64_t, int64_t> first_of;   // spacing bits -> its first ball block
+        std::map<std::tuple<uint64_t, int64_t, int64_t, int64_t>, int32_t> at;
+        auto bits = [](double x) {
+            uint64_t u;
+            std::memcpy(&u, &x, sizeof u);
+            return u;
+        };
+        auto key = [&](int64_t b, int dd) {
+            const uint64_t sb = bits(T.spacings[b]);
+            const int64_t r = first_of[sb];
+            const double w = T.spacings[b] * T.N;
+            int64_t c[3] = {0, 0, 0};
+            for (int k = 0; k < D; ++k)
+                c[k] = std::llround((T.origins[b * D + k] - T.origins[r * D + k]) / w) + (k == dd ? 1 : 0);
+            return std::make_tuple(sb, c[0], c[1], c[2]);
+        };
+        for (int64_t b : T.ball_blocks) first_of.emplace(bits(T.spacings[b]), b);
+        for (size_t i = 0; i < T.ball_blocks.size(); ++i) at[key(T.ball_blocks[i], -1)] = (int32_t)T.ball_blocks[i];
+        std::vector<int32_t> blocks, upper;
+        for (int64_t b : T.ball_blocks) {
+            blocks.push_back((int32_t)b);
+            for (int k = 0; k < 3; ++k) {
+                int32_t u = -1;
+                if (k < D) {
+                    auto it = at.find(key(b, k));
+                    if (it != at.end()) u = it->second;
+                }
+                upper.push_back(u);
+            }
+        }
+        TRY_CUDA(T.d_avg_blocks.put(blocks), "transfer upload");
+        TRY_CUDA(T.d_avg_upper.put(upper), "transfer upload");
+        T.A.prec = prec;
+        T.A.D = D;
+        T.A.P = P;
+        T.A.E = E;
+        T.A.N = T.N;
+        T.A.NN = 1;
+        for (int k = 0; k < D; ++k) T.A.NN *= T.N;
+        T.A.blocks = static_cast<const int32_t*>(T.d_avg_blocks.p);
+        T.A.upper = static_cast<const int32_t*>(T.d_avg_upper.p);
+        T.A.nball = (int64_t)blocks.size();
+    }
     // tables and geometry on the device, once
     std::vector<double> tabs;
     TransferLaunch& L = T.L;
@@ -936,6 +988,17 @@ static int project(twoldg_transfer_plan* plan, int source, const void* values, v
 int twoldg_project_values(twoldg_transfer_plan* plan, const void* values, void* du, double factor, int32_t var) {
     if (plan && plan->npoints > 0 && !values) return fail(TWOLDG_EINVAL, "values must not be NULL");
     return project(plan, SOURCE_VALUES, values, du, factor, var);
+}
+
+int twoldg_average_shared(twoldg_transfer_plan* plan, void* u, int32_t var) {
+    if (!plan || !u) return fail(TWOLDG_EINVAL, "plan and u must not be NULL");
+    if (var != 1 && var != 2) return fail(TWOLDG_EINVAL, "var is 1 (u) or 2 (v)");
+    AverageLaunch A = plan->A;
+    A.u = u;
+    A.var = var;
+    cudaError_t e = launch_average(A, plan->stream);
+    if (e != cudaSuccess) return fail(TWOLDG_ECUDA, std::string("average_shared: ") + cudaGetErrorString(e));
+    return TWOLDG_OK;
 }
 
 int twoldg_project_density(twoldg_transfer_plan* plan, void* du, double factor, int32_t var) {

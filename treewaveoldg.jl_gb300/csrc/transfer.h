@@ -100,6 +100,22 @@ struct TransferLaunch {
     double factor = 1.0;
 };
 
+// The averaging over shared nodes (average_shared!, src/transfer.jl:1616-1714):
+// the ball's blocks and, per block and dimension, the block across its upper
+// face (-1 for none: outside the ball's blocks, on another level, or past
+// the domain).
+struct AverageLaunch {
+    int prec = 0, D = 3, P = 3, E = 2, N = 8;
+    int64_t NN = 0;
+    const int32_t* blocks = nullptr;
+    const int32_t* upper = nullptr;   // nblocks_ball x 3
+    int64_t nball = 0;
+    void* u = nullptr;
+    int var = 2;
+};
+
+cudaError_t launch_average(const AverageLaunch& a, cudaStream_t stream);
+
 // The projection's kernels on `stream`; returns the launch error, if any.
 cudaError_t launch_projection(const TransferLaunch& a, cudaStream_t stream);
 

@@ -9,6 +9,8 @@
 // On GB300 these passes are bound by the FP64 pipe, not by HBM: the kernels
 // are shaped to spend as few double-precision operations per point as the
 // rules allow.
+#include <algorithm>
+
 #include "transfer.h"
 
 namespace twoldg {
@@ -478,6 +480,70 @@ cudaError_t points(const TransferLaunch& a, void* xs, int64_t npoints, cudaStrea
     return cudaSuccess;
 }
 
+// One pass of the averaging along dimension d: item (J, k, i) takes, in
+// the i-th ball block, the nodes k(P+1) - 1 and k(P+1) along d for k < E (the
+// faces between its elements), or for k = E its node N - 1 and node 0 of the
+// block across its upper face; J runs over the other dimensions. Both nodes
+// get their mean, the lower one's value first. No two items write one node.
+template <typename T, int D>
+__global__ void average_kernel(const AverageLaunch a, int d) {
+    int64_t per = 1;
+    for (int m = 0; m < D - 1; ++m) per *= a.N;
+    const int64_t total = per * a.E * a.nball;
+    const int P1 = a.P + 1;
+    for (int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; item < total;
+         item += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t J = item % per;
+        const int k = (int)((item / per) % a.E) + 1;
+        const int64_t i = item / (per * a.E);
+        // the other dimensions' indices, in order, with d's left out
+        int64_t off = 0, stride = 1, rest = J, strd = 1;
+        for (int m = 0; m < D; ++m) {
+            if (m == d) {
+                strd = stride;
+            } else {
+                off += (rest % a.N) * stride;
+                rest /= a.N;
+            }
+            stride *= a.N;
+        }
+        T* u = static_cast<T*>(a.u);
+        const int64_t b = a.blocks[i];
+        const int64_t vb = (int64_t)(a.var - 1) * a.NN;
+        if (k < a.E) {
+            T* p1 = u + b * 2 * a.NN + vb + off + (int64_t)(k * P1 - 1) * strd;
+            T* p2 = u + b * 2 * a.NN + vb + off + (int64_t)(k * P1) * strd;
+            const T mean = (*p1 + *p2) / T(2);
+            *p1 = mean;
+            *p2 = mean;
+        } else {
+            const int64_t bn = a.upper[i * 3 + d];
+            if (bn >= 0) {
+                T* p1 = u + b * 2 * a.NN + vb + off + (int64_t)(a.N - 1) * strd;
+                T* p2 = u + bn * 2 * a.NN + vb + off;
+                const T mean = (*p1 + *p2) / T(2);
+                *p1 = mean;
+                *p2 = mean;
+            }
+        }
+    }
+}
+
+template <typename T, int D>
+cudaError_t average(const AverageLaunch& a, cudaStream_t s) {
+    int64_t per = 1;
+    for (int m = 0; m < D - 1; ++m) per *= a.N;
+    const int64_t total = per * a.E * a.nball;
+    if (total == 0) return cudaSuccess;
+    const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, 152 * 16);
+    for (int d = 0; d < D; ++d) {
+        average_kernel<T, D><<<grid, 256, 0, s>>>(a, d);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 template <typename T>
 cudaError_t projection_d(const TransferLaunch& a, cudaStream_t s) {
     switch (a.D) {
@@ -506,6 +572,23 @@ cudaError_t launch_projection(const TransferLaunch& a, cudaStream_t stream) {
 
 cudaError_t launch_points(const TransferLaunch& a, void* xs, int64_t npoints, cudaStream_t stream) {
     return a.prec == 0 ? points_d<double>(a, xs, npoints, stream) : points_d<float>(a, xs, npoints, stream);
+}
+
+cudaError_t launch_average(const AverageLaunch& a, cudaStream_t stream) {
+    if (a.prec == 0) {
+        switch (a.D) {
+            case 1: return average<double, 1>(a, stream);
+            case 2: return average<double, 2>(a, stream);
+            case 3: return average<double, 3>(a, stream);
+        }
+    } else {
+        switch (a.D) {
+            case 1: return average<float, 1>(a, stream);
+            case 2: return average<float, 2>(a, stream);
+            case 3: return average<float, 3>(a, stream);
+        }
+    }
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace twoldg

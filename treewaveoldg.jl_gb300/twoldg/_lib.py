@@ -24,6 +24,7 @@ EXPORTS = [
     "twoldg_transfer_plan_create", "twoldg_transfer_plan_update", "twoldg_transfer_plan_destroy",
     "twoldg_transfer_plan_counts",
     "twoldg_transfer_points", "twoldg_project_values", "twoldg_project_density", "twoldg_transfer_table",
+    "twoldg_average_shared",
 ]
 
 
@@ -122,6 +123,7 @@ def lib():
             "twoldg_transfer_points": (ctypes.c_int, [vp, vp]),
             "twoldg_project_values": (ctypes.c_int, [vp, vp, vp, d, i32]),
             "twoldg_project_density": (ctypes.c_int, [vp, vp, d, i32]),
+            "twoldg_average_shared": (ctypes.c_int, [vp, vp, i32]),
             "twoldg_transfer_table": (ctypes.c_int, [i32, i32, ctypes.c_char_p, i32, vp]),
         }
         for name, (res, args) in sig.items():

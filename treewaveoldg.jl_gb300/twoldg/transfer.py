@@ -234,6 +234,31 @@ class TransferPlan:
         return du
 
 
+    def average_shared(self, u, var=2):
+        """average_shared!(ua, sn, var) (src/transfer.jl:1616-1714): variable
+        var of u, in the blocks the plan's ball meets, with every node that
+        elements share replaced by the mean over them. Returns u."""
+        _check_state(self.p, u)
+        _sync_torch()
+        _lib.check(_lib.lib().twoldg_average_shared(self._h, _dptr(u), int(var)))
+        self.p.synchronize()
+        return u
+
+
+def source_rhs(du, u, p, plan, S, t=0.0, factor=-1.0, average=True):
+    """The field part of the reference's inspiral_rhs! (src/inspiral.jl):
+    wave_rhs! of u, then factor times the projection of S onto v's rate, then
+    (average=True) the averaging over shared nodes of that rate, as the
+    reference writes the source. `plan` is the TransferPlan of the particles'
+    current positions. Returns du."""
+    from .problem import wave_rhs
+    wave_rhs(du, u, p, t)
+    plan.project(du, S, factor=factor, var=2)
+    if average:
+        plan.average_shared(du, var=2)
+    return du
+
+
 def _torch():
     import torch
     return torch
