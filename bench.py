@@ -704,7 +704,9 @@ def main():
     acc64, u64 = (None, None) if args.accuracy_steps == 0 else accuracy(twoldg, torch, arms["f64"], args.accuracy_steps)
     acc32 = None if args.accuracy_steps == 0 else accuracy(twoldg, torch, arms["f32c"], args.accuracy_steps,
                                                            ref64=u64)[0]
-    ee = None if args.no_e2e else e2e(twoldg, torch, arms["f32c"], max(3, args.steps // 4))
+    # at least 20 pipelined steps: with fewer, filling and draining the
+    # two-buffer pipeline is a visible share of the timed region
+    ee = None if args.no_e2e else e2e(twoldg, torch, arms["f32c"], max(20, args.steps))
     bat = None if args.no_batched else batched(twoldg, torch, max(10, args.steps // 4), args.warmup,
                                                args.accuracy_steps)
     hbm, peak_kind = peaks()
