@@ -737,7 +737,9 @@ def main():
         "fp64": {"value": v64, "ms_per_step": arms["f64"]["ms"] / args.steps,
                  "stage_ms": [float(x) for x in arms["f64"]["stage_ms"]],
                  "roofline_frac": bytes_ns["f64"] * nodes / 4 / (float(np.mean(arms["f64"]["stage_ms"])) / 1e3)
-                 / 1e9 / hbm, "layout": arms["f64"]["layout"]},
+                 / 1e9 / hbm, "layout": arms["f64"]["layout"],
+                 "bound": "the FP64 pipe, not HBM (ncu: 84% FP64-pipe activity per stage, "
+                          "profiles/stage3r_f64_256cube.md); roofline_frac is the HBM fraction"},
         "speedup_vs_fp64": value / v64,
         "accuracy": {"fp64": acc64, "f32c": acc32},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
