@@ -144,12 +144,13 @@ public:
         int n = 0;
         if constexpr (D == 3) {
             if (kernel == 1) {
+                // the stages between the first and the last
                 if (E == 2)
-                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage3r_kernel<T, P, 2, COMP>, threads,
-                                                                  Stage3R<T, P, 2, COMP>::words * sizeof(T));
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage3r_kernel<T, P, 2, false, false, 2>,
+                                                                  threads, Stage3R<T, P, 2, false>::words * sizeof(T));
                 else
-                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage3r_kernel<T, P, 4, COMP>, threads,
-                                                                  Stage3R<T, P, 4, COMP>::words * sizeof(T));
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage3r_kernel<T, P, 4, false, false, 2>,
+                                                                  threads, Stage3R<T, P, 4, false>::words * sizeof(T));
                 return n;
             }
         }
@@ -279,25 +280,33 @@ public:
     // The register-line kernel: stage 4 of the compensated path with the
     // compensation array, stage 1 in the lean variant where that fits one more
     // CTA per SM, every other stage without the compensation array.
+    // One instantiation per stage (its data flow compiled in, no other's).
     template <int E>
     cudaError_t launch3r(const StageArgs<T>& a, int grid, int mode, cudaStream_t s) const {
         if constexpr (D == 3) {
             using SL = Stage3R<T, P, E, false, true>;
             using S0 = Stage3R<T, P, E, false>;
             using SC = Stage3R<T, P, E, true>;
+            const size_t m0 = S0::words * sizeof(T);
             if constexpr (COMP) {
                 if (mode == MODE_STAGE4) {
-                    stage3r_kernel<T, P, E, true><<<grid, SC::NT, SC::words * sizeof(T), s>>>(a, tb_);
+                    stage3r_kernel<T, P, E, true, false, 4><<<grid, SC::NT, SC::words * sizeof(T), s>>>(a, tb_);
                     return cudaGetLastError();
                 }
             }
-            if constexpr (SL::MINB > S0::MINB) {
-                if (mode == MODE_STAGE1)
-                    stage3r_kernel<T, P, E, false, true><<<grid, SL::NT, SL::words * sizeof(T), s>>>(a, tb_);
+            if (mode == MODE_STAGE1) {
+                if constexpr (SL::MINB > S0::MINB)
+                    stage3r_kernel<T, P, E, false, true, 1><<<grid, SL::NT, SL::words * sizeof(T), s>>>(a, tb_);
                 else
-                    stage3r_kernel<T, P, E, false><<<grid, S0::NT, S0::words * sizeof(T), s>>>(a, tb_);
+                    stage3r_kernel<T, P, E, false, false, 1><<<grid, S0::NT, m0, s>>>(a, tb_);
+            } else if (mode == 2) {
+                stage3r_kernel<T, P, E, false, false, 2><<<grid, S0::NT, m0, s>>>(a, tb_);
+            } else if (mode == 3) {
+                stage3r_kernel<T, P, E, false, false, 3><<<grid, S0::NT, m0, s>>>(a, tb_);
+            } else if (mode == MODE_STAGE4) {
+                stage3r_kernel<T, P, E, false, false, 4><<<grid, S0::NT, m0, s>>>(a, tb_);
             } else {
-                stage3r_kernel<T, P, E, false><<<grid, S0::NT, S0::words * sizeof(T), s>>>(a, tb_);
+                stage3r_kernel<T, P, E, false><<<grid, S0::NT, m0, s>>>(a, tb_);
             }
         }
         return cudaGetLastError();
@@ -305,10 +314,15 @@ public:
     template <int E>
     void set_attrs3r() {
         if constexpr (D == 3) {
-            if constexpr (COMP) set_attrs(stage3r_kernel<T, P, E, true>);
+            if constexpr (COMP) set_attrs(stage3r_kernel<T, P, E, true, false, 4>);
             set_attrs(stage3r_kernel<T, P, E, false>);
+            set_attrs(stage3r_kernel<T, P, E, false, false, 2>);
+            set_attrs(stage3r_kernel<T, P, E, false, false, 3>);
+            if constexpr (!COMP) set_attrs(stage3r_kernel<T, P, E, false, false, 4>);
             if constexpr (Stage3R<T, P, E, false, true>::MINB > Stage3R<T, P, E, false>::MINB)
-                set_attrs(stage3r_kernel<T, P, E, false, true>);
+                set_attrs(stage3r_kernel<T, P, E, false, true, 1>);
+            else
+                set_attrs(stage3r_kernel<T, P, E, false, false, 1>);
         }
     }
 

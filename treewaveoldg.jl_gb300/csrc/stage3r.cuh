@@ -44,6 +44,29 @@ constexpr int half_bank_stride(int lo) {
         if (x % VW == 0 && (x * sizeof(T)) % 128 == 64) return x;
 }
 
+// The L2 prefetch of a block's stage operands (and of the column source of
+// the CTA's next block), as the register-line kernel reads them: u^n in
+// stages 1 and 2, k1_v in stage 2, the stage input, u^n and the increments in
+// stages 3 and 4, the compensation in stage 4.
+template <typename T>
+__device__ __forceinline__ void prefetch_stage3r(const StageArgs<T>& a, int item, int64_t NN) {
+    const int mode = a.mode;
+    const int64_t off = a.items[item].off;
+    const size_t w = (size_t)NN * sizeof(T);
+    prefetch_l2(a.u + off, 2 * w);
+    if (mode == 2) prefetch_l2(a.y + off + NN, w);
+    if (mode == 3 || mode == MODE_STAGE4) {
+        prefetch_l2(a.y + off, 2 * w);
+        prefetch_l2(a.acc + off, 2 * w);
+        if (mode == MODE_STAGE4 && a.comp) prefetch_l2(a.comp + off, 2 * w);
+    }
+    const int nxt = item + gridDim.x;
+    if (nxt < a.nitems) {
+        const T* src = (mode == 3 || mode == MODE_STAGE4) ? a.y : a.u;
+        prefetch_l2(src + a.items[nxt].off, 2 * w);
+    }
+}
+
 template <typename T, int P, int E, bool COMP, bool LEAN = false>
 struct Stage3R {
     static constexpr int P1 = P + 1;
@@ -171,7 +194,10 @@ __device__ __forceinline__ void truncate_lines(const Tab<T, P>& tb, T* sl, T* sc
     }
 }
 
-template <typename T, int P, int E, bool COMP, bool LEAN = false>
+// FM: the stage the instantiation runs (1-4), so that each stage's code holds
+// only its own data flow, or 0 for the mode in the arguments (the right-hand
+// side).
+template <typename T, int P, int E, bool COMP, bool LEAN = false, int FM = 0>
 __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P, E, COMP, LEAN>::MINB)
     stage3r_kernel(StageArgs<T> a, Tab<T, P> tb) {
     using S = Stage3R<T, P, E, COMP, LEAN>;
@@ -191,8 +217,17 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
     const int l0 = LX * ca + LXY * cb;
     const int l1 = ca + LXY * cb;
     const int l2 = ca + LX * cb;
-    const int mode = a.mode;
-    const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
+    const int mode = FM ? FM : a.mode;
+    // The stage's data flow. Stage 1 stores only the stage derivative's v
+    // part k1_v, truncated, in the v half of `y` (its u part is u^n's own v):
+    // stage 2 forms Y2 = u^n + dt/2 k1 and the first increment dt/6 k1 from
+    // u^n, which it reads anyway, and k1_v, so neither Y2 nor the increment
+    // goes through HBM (8 words a node instead of 14 over the two stages in
+    // FP32). The truncation acts on k1_v instead of on Y2's v, the same by
+    // linearity since u^n's v is truncated. Stages 3 and 4 read Y3, Y4 and
+    // the increments as stored.
+    const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1 || mode == 2) ? a.u : a.y;
+    const T* vsrc = mode == 2 ? a.y : ysrc;
 
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         const BlockItem& it = a.items[item];
@@ -203,12 +238,19 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
         for (int f = 0; f < 6; ++f) nb[f] = it.nb[f];
         const T inv_h = T(1) / T(it.h);
         const T* yu = ysrc + it.off;
-        if (tid == 0) prefetch_stage<T>(a, item, 2 * (int64_t)NN);
+        if (tid == 0) prefetch_stage3r<T>(a, item, NN);
         // every global load of the block's prologue at once: the column, the u
         // ghosts and the neighbours' gradient parts at this face point
         T line[N + 2];
+        if (mode == 2) {
+            // Y2's u, dt/2 k1_u = dt/2 v^n added to u^n
+            const T cn1 = a.rk[4 * it.problem + 2];
 #pragma unroll
-        for (int j = 0; j < N; ++j) line[1 + j] = yu[tid + F * j];
+            for (int j = 0; j < N; ++j) line[1 + j] = yu[tid + F * j] + cn1 * yu[NN + tid + F * j];
+        } else {
+#pragma unroll
+            for (int j = 0; j < N; ++j) line[1 + j] = yu[tid + F * j];
+        }
         T ug[6], gp[6];
 #pragma unroll
         for (int f = 0; f < 6; ++f) {
@@ -288,7 +330,7 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
             }
             __syncthreads();
         }
-        const T* yv = ysrc + it.off + NN;
+        const T* yv = vsrc + it.off + NN;
         if (mode == MODE_RHS) {
             T* du = a.du + it.off;
 #pragma unroll
@@ -302,6 +344,7 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
         // ---- the RK combination along the column, element by element, with the
         // truncation along z in registers
         const RkCoef<T> rc(mode, a.rk + 4 * it.problem);
+        const RkCoef<T> rc1(1, a.rk + 4 * it.problem);   // dt/6 and dt/2
         const T* __restrict__ un = a.u + it.off;
         T* __restrict__ acc = a.acc + it.off;
         T* __restrict__ comp = COMP ? a.comp + it.off : nullptr;
@@ -310,7 +353,7 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
         // store it from registers as each element is done; stage 4, which
         // writes u^n in place, stores it with v at the end (measured faster)
         T* out = (mode == MODE_STAGE4 ? a.u : a.y) + it.off;
-        const bool early_u = mode != MODE_STAGE4;
+        const bool early_u = mode == 2 || mode == 3;
 #pragma unroll
         for (int ez = 0; ez < E; ++ez) {
             T y[P1], uu[P1], uv[P1], au[P1], av[P1], cu[P1], cvi[P1];
@@ -327,7 +370,13 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
                     uu[q] = un[n];
                     uv[q] = un[NN + n];
                 }
-                if (mode != 1) {
+                if (mode == 2) {
+                    // y[q] holds k1_v: Y2's v and the first increment
+                    const T k1v = y[q];
+                    y[q] = uv[q] + rc1.cn * k1v;
+                    au[q] = rc1.ca * uv[q];
+                    av[q] = rc1.ca * k1v;
+                } else if (mode != 1) {
                     au[q] = acc[n];
                     av[q] = acc[NN + n];
                 }
@@ -344,7 +393,16 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
                 T o_u[1], o_v[1], o_c[1];
                 T yq[1] = {y[q]}, uuq[1] = {uu[q]}, uvq[1] = {uv[q]}, auq[1] = {au[q]}, avq[1] = {av[q]},
                   cuq[1] = {cu[q]}, cviq[1] = {cvi[q]};
-                stage_points<T, COMP, 1>(mode, rc, yq, uuq, uvq, auq, avq, cuq, cviq, lap, inv_h, o_u, o_v, o_c);
+                if (mode == MODE_STAGE1) {
+                    // Y2's u for the face export; the stage derivative's v,
+                    // truncated below and stored
+                    o_u[0] = uuq[0] + rc.cn * yq[0];
+                    o_v[0] = lap[0] * inv_h;
+                    o_c[0] = T(0);
+                } else {
+                    stage_points<T, COMP, 1>(mode, rc, yq, uuq, uvq, auq, avq, cuq, cviq, lap, inv_h, o_u, o_v,
+                                             o_c);
+                }
                 au[q] = auq[0];
                 av[q] = avq[0];
                 cu[q] = cuq[0];
@@ -377,7 +435,7 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
             for (int q = 0; q < P1; ++q) {
                 const int j = ez * P1 + q;
                 const int n = tid + F * j;
-                if (mode != MODE_STAGE4) {
+                if (mode == 2 || mode == 3) {
                     acc[n] = au[q];
                     acc[NN + n] = av[q];
                 }
@@ -420,7 +478,7 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
         // ---- the new v of the column (and in stage 4 its u)
 #pragma unroll
         for (int j = 0; j < N; ++j) {
-            if (!early_u) out[tid + F * j] = su[s2 + SXY * j];
+            if (mode == MODE_STAGE4) out[tid + F * j] = su[s2 + SXY * j];
             out[NN + tid + F * j] = sl[l2 + LXY * j];
             if (final_comp) comp[NN + tid + F * j] = sc[l2 + LXY * j];
         }
