@@ -78,32 +78,44 @@ def peaks():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling during the timed region: the sampler is started
+    and seen to report before the region begins, samples every 10 ms, and,
+    for a region shorter than that, keeps the first sample after it."""
 
     def __init__(self, index):
         self.index = index
-        self.samples = []
+        self.samples = []            # (time, fields)
         self._p = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         cmd = ["nvidia-smi", "-i", str(self.index),
                "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
                "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-               "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"]
+               "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "10"]
         try:
             self._p = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
+            deadline = time.time() + 5
+            while not self.samples and time.time() < deadline and self._p.poll() is None:
+                time.sleep(0.005)
         except OSError:
             self._p = None
+        self.t0 = time.time()
         return self
 
     def _read(self):
         for line in self._p.stdout:
-            self.samples.append([x.strip() for x in line.split(",")])
+            self.samples.append((time.time(), [x.strip() for x in line.split(",")]))
 
     def __exit__(self, *a):
+        self.t1 = time.time()
         if self._p is not None:
+            deadline = self.t1 + 1
+            while not any(t >= self.t1 for t, _ in self.samples) and time.time() < deadline \
+                    and self._p.poll() is None:
+                time.sleep(0.005)
             self._p.terminate()
             try:
                 self._p.wait(timeout=5)
@@ -111,12 +123,19 @@ class Clocks:
                 self._p.kill()
 
     def summary(self):
-        sm = [float(s[0]) for s in self.samples if len(s) >= 7 and s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if len(s) >= 7 and s[1].replace(".", "").isdigit()]
+        inside = [f for t, f in self.samples if self.t0 <= t <= self.t1]
+        trailing = 0
+        if not inside:
+            after = [f for t, f in self.samples if t > self.t1][:1]
+            inside, trailing = after, len(after)
+        ok = [s for s in inside if len(s) >= 7]
+        sm = [float(s[0]) for s in ok if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in ok if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples if len(s) >= 7 for i in range(4) if s[3 + i] == "Active"})
+        reasons = sorted({names[i] for s in ok for i in range(4) if s[3 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(ok) - trailing, "trailing_samples": trailing,
+                "interval_ms": 10}
 
 
 WORKLOAD = "box256"
