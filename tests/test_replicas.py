@@ -1,0 +1,54 @@
+"""The N > 1 path of the bench, which runs independent replicas (the field
+step has no collective; the survey's multi-GPU row plans replicas only): two
+gloo ranks on the CPU take the barrier and the maximum of their times, and
+the reference arm runs on rank 0 alone."""
+import multiprocessing as mp
+import os
+import socket
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(r, port, q):
+    os.environ.update({"RANK": str(r), "LOCAL_RANK": str(r), "WORLD_SIZE": "2", "MASTER_ADDR": "127.0.0.1",
+                       "MASTER_PORT": str(port)})
+    sys.path.insert(0, ROOT)
+    import torch
+    import bench
+    bench.init_dist(torch)
+    bench.barrier()
+    # each replica's time; the job's time is the slowest replica's
+    got = bench.max_over_ranks(1.5 + r)
+    q.put((r, bench.world(), bench.rank(), got))
+    bench._dist.destroy_process_group()
+
+
+def test_two_gloo_replicas_take_the_slowest_time():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    out = sorted(q.get(timeout=10) for _ in range(2))
+    assert out == [(0, 2, 0, 2.5), (1, 2, 1, 2.5)]
+
+
+def test_reference_arm_runs_on_rank_zero_alone():
+    env = dict(os.environ, RANK="1", LOCAL_RANK="1", WORLD_SIZE="2", MASTER_ADDR="127.0.0.1",
+               MASTER_PORT=str(_free_port()))
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
+                        "--steps", "1", "--warmup", "0"], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0
+    assert r.stdout.strip() == ""
