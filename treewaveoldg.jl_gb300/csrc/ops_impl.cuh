@@ -7,6 +7,7 @@
 #include "kernels.cuh"
 #include "ops.h"
 #include "stage3r.cuh"
+#include "stage2r.cuh"
 #include "fullmetric.cuh"
 
 namespace twoldg {
@@ -46,6 +47,10 @@ public:
         set_attrs(stage_kernel<T, D, P, COMP>);
         set_attrs(stage_kernel_c<T, D, P, 2, COMP>);
         set_attrs(stage_kernel_c<T, D, P, 4, COMP>);
+        if constexpr (D == 2) {
+            set_attrs2r<2>();
+            set_attrs2r<4>();
+        }
         if constexpr (D == 3) {
             set_attrs3r<2>();
             set_attrs3r<4>();
@@ -128,6 +133,10 @@ public:
             line = flat && aligned && ((E == 2 && Stage3R<T, P, 2, COMP>::usable) ||
                                        (E == 4 && Stage3R<T, P, 4, COMP>::usable));
         }
+        if constexpr (D == 2) {
+            line = flat && aligned && ((E == 2 && Stage2R<T, P, 2, COMP>::usable) ||
+                                       (E == 4 && Stage2R<T, P, 4, COMP>::usable));
+        }
         const bool fixed = aligned && (E == 2 || E == 4);
         if (kernel == 1 && line) return 1;
         if (kernel == 2 && fixed) return 2;
@@ -135,6 +144,7 @@ public:
         return line ? 1 : fixed ? 2 : 3;
     }
     int run_threads(int kernel, int E) const {
+        if (kernel == 1 && D == 2) return E == 2 ? Stage2R<T, P, 2, false>::NT : Stage2R<T, P, 4, false>::NT;
         if (kernel == 1) return E * (P + 1) * E * (P + 1);
         if (kernel == 2) return E == 2 ? StageLaunch<T, D, P, 2>::NT : StageLaunch<T, D, P, 4>::NT;
         return std::min(launch_.threads ? launch_.threads : default_threads(E), 256);
@@ -151,6 +161,17 @@ public:
                 else
                     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage3r_kernel<T, P, 4, false, false, 2>,
                                                                   threads, Stage3R<T, P, 4, false>::words * sizeof(T));
+                return n;
+            }
+        }
+        if constexpr (D == 2) {
+            if (kernel == 1) {
+                if (E == 2)
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage2r_kernel<T, P, 2, false>, threads,
+                                                                  Stage2R<T, P, 2, false>::words * sizeof(T));
+                else
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage2r_kernel<T, P, 4, false>, threads,
+                                                                  Stage2R<T, P, 4, false>::words * sizeof(T));
                 return n;
             }
         }
@@ -267,6 +288,10 @@ public:
             if (k == 1 && E == 2) return launch3r<2>(a, grid, mode, s);
             if (k == 1 && E == 4) return launch3r<4>(a, grid, mode, s);
         }
+        if constexpr (D == 2) {
+            if (k == 1 && E == 2) return launch2r<2>(a, grid, mode, s);
+            if (k == 1 && E == 4) return launch2r<4>(a, grid, mode, s);
+        }
         if (k == 2 && E == 2) {
             stage_kernel_c<T, D, P, 2, COMP><<<grid, StageLaunch<T, D, P, 2>::NT, smem, s>>>(a, tb_);
         } else if (k == 2 && E == 4) {
@@ -310,6 +335,32 @@ public:
             }
         }
         return cudaGetLastError();
+    }
+    // The 2D register-line kernel: K blocks a CTA, so the grid is the items
+    // over K (capped by the persistent layout's CTAs); stage 4 of the
+    // compensated path with the compensation array.
+    template <int E>
+    cudaError_t launch2r(const StageArgs<T>& a, int grid, int mode, cudaStream_t s) const {
+        if constexpr (D == 2) {
+            using S0 = Stage2R<T, P, E, false>;
+            using SC = Stage2R<T, P, E, true>;
+            const int g = std::max(1, std::min(grid, (a.nitems + S0::K - 1) / S0::K));
+            if constexpr (COMP) {
+                if (mode == MODE_STAGE4) {
+                    stage2r_kernel<T, P, E, true><<<g, SC::NT, SC::words * sizeof(T), s>>>(a, tb_);
+                    return cudaGetLastError();
+                }
+            }
+            stage2r_kernel<T, P, E, false><<<g, S0::NT, S0::words * sizeof(T), s>>>(a, tb_);
+        }
+        return cudaGetLastError();
+    }
+    template <int E>
+    void set_attrs2r() {
+        if constexpr (D == 2) {
+            if constexpr (COMP) set_attrs(stage2r_kernel<T, P, E, true>);
+            set_attrs(stage2r_kernel<T, P, E, false>);
+        }
     }
     template <int E>
     void set_attrs3r() {
