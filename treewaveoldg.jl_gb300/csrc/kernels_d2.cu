@@ -1,11 +1,27 @@
-// Kernel instantiations for D = 2 (one translation unit per dimension so
-// that the build compiles them in parallel).
+// Kernel dispatch for D = 2. The instantiations for each order P live in
+// their own translation unit (kernels_d2_p<P>.cu) so that the build
+// compiles them in parallel.
 #include "ops_impl.cuh"
 
 namespace twoldg {
 
+Ops* make_ops_d2_p1(int prec, const ElementTables<double>& t64, const ElementTables<float>& t32);
+Ops* make_ops_d2_p2(int prec, const ElementTables<double>& t64, const ElementTables<float>& t32);
+Ops* make_ops_d2_p3(int prec, const ElementTables<double>& t64, const ElementTables<float>& t32);
+Ops* make_ops_d2_p4(int prec, const ElementTables<double>& t64, const ElementTables<float>& t32);
+Ops* make_ops_d2_p5(int prec, const ElementTables<double>& t64, const ElementTables<float>& t32);
+Ops* make_ops_d2_p6(int prec, const ElementTables<double>& t64, const ElementTables<float>& t32);
+
 Ops* make_ops_d2(int prec, int P, const ElementTables<double>& t64, const ElementTables<float>& t32) {
-    return make_ops_dim<2>(prec, P, t64, t32);
+    switch (P) {
+        case 1: return make_ops_d2_p1(prec, t64, t32);
+        case 2: return make_ops_d2_p2(prec, t64, t32);
+        case 3: return make_ops_d2_p3(prec, t64, t32);
+        case 4: return make_ops_d2_p4(prec, t64, t32);
+        case 5: return make_ops_d2_p5(prec, t64, t32);
+        case 6: return make_ops_d2_p6(prec, t64, t32);
+        default: return nullptr;
+    }
 }
 
 }  // namespace twoldg

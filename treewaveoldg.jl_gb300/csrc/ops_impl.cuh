@@ -167,10 +167,10 @@ public:
         if constexpr (D == 2) {
             if (kernel == 1) {
                 if (E == 2)
-                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage2r_kernel<T, P, 2, false>, threads,
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage2r_kernel<T, P, 2, false, 2>, threads,
                                                                   Stage2R<T, P, 2, false>::words * sizeof(T));
                 else
-                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage2r_kernel<T, P, 4, false>, threads,
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage2r_kernel<T, P, 4, false, 2>, threads,
                                                                   Stage2R<T, P, 4, false>::words * sizeof(T));
                 return n;
             }
@@ -345,21 +345,35 @@ public:
             using S0 = Stage2R<T, P, E, false>;
             using SC = Stage2R<T, P, E, true>;
             const int g = std::max(1, std::min(grid, (a.nitems + S0::K - 1) / S0::K));
+            const size_t m0 = S0::words * sizeof(T);
             if constexpr (COMP) {
                 if (mode == MODE_STAGE4) {
-                    stage2r_kernel<T, P, E, true><<<g, SC::NT, SC::words * sizeof(T), s>>>(a, tb_);
+                    stage2r_kernel<T, P, E, true, 4><<<g, SC::NT, SC::words * sizeof(T), s>>>(a, tb_);
                     return cudaGetLastError();
                 }
             }
-            stage2r_kernel<T, P, E, false><<<g, S0::NT, S0::words * sizeof(T), s>>>(a, tb_);
+            if (mode == MODE_STAGE1)
+                stage2r_kernel<T, P, E, false, 1><<<g, S0::NT, m0, s>>>(a, tb_);
+            else if (mode == 2)
+                stage2r_kernel<T, P, E, false, 2><<<g, S0::NT, m0, s>>>(a, tb_);
+            else if (mode == 3)
+                stage2r_kernel<T, P, E, false, 3><<<g, S0::NT, m0, s>>>(a, tb_);
+            else if (mode == MODE_STAGE4)
+                stage2r_kernel<T, P, E, false, 4><<<g, S0::NT, m0, s>>>(a, tb_);
+            else
+                stage2r_kernel<T, P, E, false><<<g, S0::NT, m0, s>>>(a, tb_);
         }
         return cudaGetLastError();
     }
     template <int E>
     void set_attrs2r() {
         if constexpr (D == 2) {
-            if constexpr (COMP) set_attrs(stage2r_kernel<T, P, E, true>);
+            if constexpr (COMP) set_attrs(stage2r_kernel<T, P, E, true, 4>);
             set_attrs(stage2r_kernel<T, P, E, false>);
+            set_attrs(stage2r_kernel<T, P, E, false, 1>);
+            set_attrs(stage2r_kernel<T, P, E, false, 2>);
+            set_attrs(stage2r_kernel<T, P, E, false, 3>);
+            if constexpr (!COMP) set_attrs(stage2r_kernel<T, P, E, false, 4>);
         }
     }
     template <int E>

@@ -31,7 +31,9 @@ struct Stage2R {
     static constexpr bool usable = N <= 32;
 };
 
-template <typename T, int P, int E, bool COMP>
+// FM: the stage the instantiation runs (1-4), so that each stage's code holds
+// only its own data flow, or 0 for the mode in the arguments.
+template <typename T, int P, int E, bool COMP, int FM = 0>
 __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
     stage2r_kernel(StageArgs<T> a, Tab<T, P> tb) {
     using S = Stage2R<T, P, E, COMP>;
@@ -41,7 +43,7 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
     T* su = reinterpret_cast<T*>(smem_raw) + bs * S::PER;
     T* sl = su + S::SS;
     T* sc = sl + S::LS;   // compensated only
-    const int mode = a.mode;
+    const int mode = FM ? FM : a.mode;
     const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
     const bool final_comp = COMP && mode == MODE_STAGE4;
 
