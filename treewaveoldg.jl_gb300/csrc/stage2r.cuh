@@ -44,7 +44,11 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
     T* sl = su + S::SS;
     T* sc = sl + S::LS;   // compensated only
     const int mode = FM ? FM : a.mode;
-    const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
+    // the stages' data flow is the 3D kernel's: stage 1 stores only the
+    // truncated v-rate k1_v in the v half of `y`, stage 2 forms Y2 and the
+    // first increment from u^n and k1_v
+    const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1 || mode == 2) ? a.u : a.y;
+    const T* vsrc = mode == 2 ? a.y : ysrc;
     const bool final_comp = COMP && mode == MODE_STAGE4;
 
     for (int base = blockIdx.x * K; base < a.nitems; base += gridDim.x * K) {
@@ -65,8 +69,14 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
             inv_h = T(1) / T(it->h);
             const T* yu = ysrc + it->off;
             T line[N + 2];
+            if (mode == 2) {
+                const T cn1 = a.rk[4 * it->problem + 2];
 #pragma unroll
-            for (int j = 0; j < N; ++j) line[1 + j] = yu[c + N * j];
+                for (int j = 0; j < N; ++j) line[1 + j] = yu[c + N * j] + cn1 * yu[NN + c + N * j];
+            } else {
+#pragma unroll
+                for (int j = 0; j < N; ++j) line[1 + j] = yu[c + N * j];
+            }
             // face f's ghosts at this thread's tangential point: x faces at
             // row x1 = c, y faces at column x0 = c
 #pragma unroll
@@ -128,8 +138,9 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
         // ---- the RK combination down the column, element by element, with
         // the truncation along y in registers
         if (live) {
-            const T* yv = ysrc + it->off + NN;
+            const T* yv = vsrc + it->off + NN;
             const RkCoef<T> rc(mode, a.rk + 4 * it->problem);
+            const RkCoef<T> rc1(1, a.rk + 4 * it->problem);   // dt/6 and dt/2
             const T* __restrict__ un = a.u + it->off;
             T* __restrict__ acc = a.acc + it->off;
             T* __restrict__ comp = COMP ? a.comp + it->off : nullptr;
@@ -148,7 +159,13 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
                         uu[q] = un[n];
                         uv[q] = un[NN + n];
                     }
-                    if (mode != MODE_STAGE1) {
+                    if (mode == 2) {
+                        // y[q] holds k1_v: Y2's v and the first increment
+                        const T k1v = y[q];
+                        y[q] = uv[q] + rc1.cn * k1v;
+                        au[q] = rc1.ca * uv[q];
+                        av[q] = rc1.ca * k1v;
+                    } else if (mode != MODE_STAGE1) {
                         au[q] = acc[n];
                         av[q] = acc[NN + n];
                     }
@@ -165,8 +182,15 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
                     T o_u[1], o_v[1], o_c[1];
                     T yq[1] = {y[q]}, uuq[1] = {uu[q]}, uvq[1] = {uv[q]}, auq[1] = {au[q]}, avq[1] = {av[q]},
                       cuq[1] = {cu[q]}, cviq[1] = {cvi[q]};
-                    stage_points<T, COMP, 1>(mode, rc, yq, uuq, uvq, auq, avq, cuq, cviq, lap, inv_h, o_u, o_v,
-                                             o_c);
+                    if (mode == MODE_STAGE1) {
+                        // Y2's u for the face export; the v-rate, truncated below and stored
+                        o_u[0] = uuq[0] + rc.cn * yq[0];
+                        o_v[0] = lap[0] * inv_h;
+                        o_c[0] = T(0);
+                    } else {
+                        stage_points<T, COMP, 1>(mode, rc, yq, uuq, uvq, auq, avq, cuq, cviq, lap, inv_h, o_u,
+                                                 o_v, o_c);
+                    }
                     au[q] = auq[0];
                     av[q] = avq[0];
                     cu[q] = cuq[0];
@@ -199,7 +223,7 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
                 for (int q = 0; q < P1; ++q) {
                     const int j = ey * P1 + q;
                     const int n = c + N * j;
-                    if (mode != MODE_STAGE4) {
+                    if (mode == 2 || mode == 3) {
                         acc[n] = au[q];
                         acc[NN + n] = av[q];
                         out[n] = nu[q];
