@@ -325,7 +325,10 @@ public:
                 else
                     stage3r_kernel<T, P, E, false, false, 1><<<grid, S0::NT, m0, s>>>(a, tb_);
             } else if (mode == 2) {
-                stage3r_kernel<T, P, E, false, false, 2><<<grid, S0::NT, m0, s>>>(a, tb_);
+                if constexpr (SL::MINB > S0::MINB)
+                    stage3r_kernel<T, P, E, false, true, 2><<<grid, SL::NT, SL::words * sizeof(T), s>>>(a, tb_);
+                else
+                    stage3r_kernel<T, P, E, false, false, 2><<<grid, S0::NT, m0, s>>>(a, tb_);
             } else if (mode == 3) {
                 stage3r_kernel<T, P, E, false, false, 3><<<grid, S0::NT, m0, s>>>(a, tb_);
             } else if (mode == MODE_STAGE4) {
@@ -382,6 +385,8 @@ public:
             if constexpr (COMP) set_attrs(stage3r_kernel<T, P, E, true, false, 4>);
             set_attrs(stage3r_kernel<T, P, E, false>);
             set_attrs(stage3r_kernel<T, P, E, false, false, 2>);
+            if constexpr (Stage3R<T, P, E, false, true>::MINB > Stage3R<T, P, E, false>::MINB)
+                set_attrs(stage3r_kernel<T, P, E, false, true, 2>);
             set_attrs(stage3r_kernel<T, P, E, false, false, 3>);
             if constexpr (!COMP) set_attrs(stage3r_kernel<T, P, E, false, false, 4>);
             if constexpr (Stage3R<T, P, E, false, true>::MINB > Stage3R<T, P, E, false>::MINB)
