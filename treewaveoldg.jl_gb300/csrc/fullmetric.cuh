@@ -401,7 +401,9 @@ __device__ __forceinline__ void stage_legendre(const FmTab<T, P>& ft, T* L) {
     __syncthreads();
 }
 
-template <typename T, int P, bool COMP>
+// FM: the stage the instantiation runs (1-4), so that each stage's code holds
+// only its own data flow, or 0 for the mode in the arguments.
+template <typename T, int P, bool COMP, int FM = 0>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 4) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb, FmTab<T, P> ft) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using G = ShapeR<3, P>;
@@ -413,7 +415,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 4) fm_stage_kernel(F
     T* cbuf = sc + g.LS;                      // truncation coefficients
     __shared__ T sLeg[P * (P + 1)];
     stage_legendre<T, P>(ft, sLeg);
-    const int mode = a.mode;
+    const int mode = FM ? FM : a.mode;
     const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1) ? a.u : a.y;
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         const BlockItem& it = a.items[item];

@@ -56,6 +56,10 @@ public:
             set_attrs3r<4>();
             set_attrs(fm_gradient_kernel<T, P>);
             set_attrs(fm_stage_kernel<T, P, COMP>);
+            set_attrs(fm_stage_kernel<T, P, COMP, 1>);
+            set_attrs(fm_stage_kernel<T, P, COMP, 2>);
+            set_attrs(fm_stage_kernel<T, P, COMP, 3>);
+            set_attrs(fm_stage_kernel<T, P, COMP, 4>);
             set_attrs(fm_truncate_kernel<T, P>);
             // Legendre L_q, q < P, at the Gauss-Lobatto nodes, for the full metric's truncation
             for (int i = 0; i <= P; ++i) {
@@ -497,8 +501,14 @@ public:
         else {
             size_t smem = fm_stage_smem(E);
             if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
-            fm_stage_kernel<T, P, COMP><<<std::min(nitems, kMaxGrid), 256, smem, s>>>(
-                fm_args(items, nitems, E, mode, truncate, p), tb_, ft_);
+            const int g = std::min(nitems, kMaxGrid);
+            const FmArgs<T> fa = fm_args(items, nitems, E, mode, truncate, p);
+            // one instantiation per stage
+            if (mode == MODE_STAGE1) fm_stage_kernel<T, P, COMP, 1><<<g, 256, smem, s>>>(fa, tb_, ft_);
+            else if (mode == 2) fm_stage_kernel<T, P, COMP, 2><<<g, 256, smem, s>>>(fa, tb_, ft_);
+            else if (mode == 3) fm_stage_kernel<T, P, COMP, 3><<<g, 256, smem, s>>>(fa, tb_, ft_);
+            else if (mode == MODE_STAGE4) fm_stage_kernel<T, P, COMP, 4><<<g, 256, smem, s>>>(fa, tb_, ft_);
+            else fm_stage_kernel<T, P, COMP><<<g, 256, smem, s>>>(fa, tb_, ft_);
             return cudaGetLastError();
         }
     }
