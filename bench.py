@@ -41,7 +41,7 @@ METRIC = "node-steps/s on 1 GB300: mixed-precision batched vs plain FP64, at equ
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--roots", type=int, default=16)
