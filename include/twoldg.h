@@ -349,6 +349,27 @@ int twoldg_project_density(twoldg_transfer_plan* plan, void* du, double factor, 
  * ball's, on another level or past the domain (no periodic images) is left
  * alone. Asynchronous on the problem's stream. */
 int twoldg_average_shared(twoldg_transfer_plan* plan, void* u, int32_t var);
+/* pairing(p, t, u, K, s; var, continuous) -- src/transfer.jl:1779-1797 --
+ * for each of the plan's particles k with its density kernel
+ * K = (grad rho_k, rho_k) (density_kernel, src/dynamic.jl:124-135; the two
+ * pairings of particle_forces, src/inspiral.jl:491-504): out[4k + c] =
+ * int (d rho_k / dx_c) g_h for c < 3 and int rho_k g_h for c = 3, g_h the
+ * polynomial of variable var (1 or 2) of the device state u on the elements
+ * that meet the support (support_elements, :1726-1758), each integrated by the
+ * nested rule kept to the support. With continuous nonzero, g_h is first made
+ * continuous by the mean over the elements that share each node
+ * (continuous_values, :1449-1500), refused where a support element is on the
+ * domain's face or next to another level. The kernel's moments int K phi_n
+ * are formed in FP64 on the device at the first pairing after the particles
+ * move; each pairing then gathers and sums on the device. Refused unless
+ * 2 ell < h_e and the support's box lies inside the domain (no periodic
+ * images); dim 3 only. Synchronous: out is host memory. */
+int twoldg_pairing(twoldg_transfer_plan* plan, const void* u, int32_t var, int32_t continuous, double* out);
+/* support_elements(p, s) -- src/transfer.jl:1726-1758: the elements that
+ * hold a corner of particle k's support box [z - ell, z + ell], in the
+ * corners' order (the first dimension fastest, the lower side first), as rows
+ * (block, e0, e1, e2) of out (at most 8 rows); *n gets their number. */
+int twoldg_support_elements(twoldg_transfer_plan* plan, int32_t k, int32_t* out, int32_t* n);
 /* A transfer table of order P in float64 (precision 0) or float32 (1):
  * "bary" (P+1), and of the q-point Gauss-Legendre rule "gauss_nodes" (q),
  * "gauss_weights" (q), "lagrange" (q x (P+1)), "contract" ((P+1) x q); built

@@ -484,3 +484,136 @@ def average_shared(u, mesh, ball, var):
                 a[tuple(i1)] = m
                 an[tuple(i2)] = m
     return u
+
+
+def density_kernel(X, z, v, ell, charge):
+    """(grad rho, rho) of one particle at the points X (npts, 3), as (npts, 4):
+    particle_density and its gradient (src/particle.jl:117-127; density_kernel,
+    src/dynamic.jl:124-135): y = L(v)(x - z), rho = Q rho0(y.y),
+    grad rho = L(v)(2 Q rho0'(y.y) y), L symmetric."""
+    X = np.atleast_2d(np.asarray(X, dtype=np.float64))
+    z = np.asarray(z, dtype=np.float64)
+    v = np.asarray(v, dtype=np.float64)
+    gamma = 1 / math.sqrt(1 - float(np.dot(v, v)))
+    g = gamma ** 2 / (gamma + 1)
+    r = X - z[None, :]
+    y = r + (g * (r @ v))[:, None] * v[None, :]
+    q = np.sum(y * y, axis=1)
+    inside = q < ell ** 2
+    u = np.where(inside, 1 - q / ell ** 2, 0.0)
+    c = (3465 / 512) / ell ** 3 / math.pi
+    rho = charge * c * u ** 4
+    drho = -4 * charge * c * u ** 3 / ell ** 2
+    w = 2 * drho[:, None] * y
+    grad = w + (g * (w @ v))[:, None] * v[None, :]
+    return np.concatenate([grad, rho[:, None]], axis=1)
+
+
+def frame_domain(mesh):
+    """The frame's box: the hull of its blocks."""
+    lo = mesh.origins[mesh.mask].min(axis=0)
+    hi = (mesh.origins[mesh.mask] + mesh.spacings[mesh.mask][:, None] * mesh.N).max(axis=0)
+    return lo, hi
+
+
+def locate_element(mesh, x):
+    """locate_element (src/transfer.jl:1417-1431): the frame's block that holds
+    x, and the element there, clamped to the block."""
+    P1 = mesh.P + 1
+    for b in range(mesh.nblocks):
+        if not mesh.mask[b]:
+            continue
+        lo = mesh.origins[b]
+        hi = lo + mesh.spacings[b] * mesh.N
+        if all(lo[d] <= x[d] < hi[d] for d in range(mesh.D)):
+            e = tuple(min(max(int(math.floor((x[d] - lo[d]) / (mesh.spacings[b] * P1))), 0), mesh.E - 1)
+                      for d in range(mesh.D))
+            return b, e
+    raise ValueError("the point %r is outside the domain" % (tuple(x),))
+
+
+def support_elements(mesh, s, he):
+    """support_elements (src/transfer.jl:1726-1758): the elements that hold a
+    corner of the box [z - ell, z + ell], in the corners' order (dimension 0
+    fastest, the lower side first)."""
+    D = mesh.D
+    if not 2 * s.ell < he:
+        raise ValueError("the particle's support, 2l = %r across, is not smaller than an element, h_e = %r"
+                         % (2 * s.ell, he))
+    dlo, dhi = frame_domain(mesh)
+    if not all(dlo[d] <= s.z[d] - s.ell and s.z[d] + s.ell < dhi[d] for d in range(D)):
+        raise ValueError("the particle's support around z = %r reaches past the domain's faces; the transfer "
+                         "does not look for periodic images" % (tuple(s.z),))
+    out = []
+    for corner in range(1 << D):
+        x = [s.z[d] + (s.ell if (corner >> d) & 1 else -s.ell) for d in range(D)]
+        be = locate_element(mesh, x)
+        if be not in out:
+            out.append(be)
+    return out
+
+
+def continuous_values(u, mesh, b, e, var):
+    """continuous_values (src/transfer.jl:1449-1500): the element's nodal
+    values of var with every node on its boundary replaced by the mean over
+    the elements that share it (the element's own value first, then its
+    neighbours with dimension 0 varying fastest); the neighbours on the same
+    level, no periodic images."""
+    D, E, P, P1 = mesh.D, mesh.E, mesh.P, mesh.P + 1
+    lo, hi = mesh.element_box(b, e)
+    dlo, dhi = frame_domain(mesh)
+
+    def neighbour(s):
+        en = tuple(e[d] + s[d] for d in range(D))
+        if all(0 <= en[d] < E for d in range(D)):
+            return b, en
+        x = [(lo[d] + hi[d]) / 2 + s[d] * (hi[d] - lo[d]) for d in range(D)]
+        if not all(dlo[d] < x[d] < dhi[d] for d in range(D)):
+            raise ValueError("the element at %r is on the domain's face; the continuous reconstruction, like the "
+                             "transfer, does not look for periodic images" % (tuple(lo),))
+        bn, en = locate_element(mesh, x)
+        if mesh.spacings[bn] != mesh.spacings[b]:
+            raise ValueError("the element at %r has a neighbour on another level; the continuous reconstruction "
+                             "needs the same level across every face" % (tuple(lo),))
+        return bn, en
+
+    U = u.reshape(mesh.nblocks, 2, mesh.NN)
+    N = mesh.N
+
+    def read(bn, en, K):
+        return U[bn, var - 1, sum((en[d] * P1 + K[d]) * N ** d for d in range(D))]
+
+    out = []
+    for J in np.ndindex(*([P1] * D)):
+        K = tuple(reversed(J))                   # dimension 0 fastest
+        dirs = [-1 if K[d] == 0 else (1 if K[d] == P else 0) for d in range(D)]
+        acc, count = read(b, e, K), 1
+        free = [d for d in range(D) if dirs[d] != 0]
+        for code in range(1, 1 << len(free)):
+            s = [0] * D
+            for i, d in enumerate(free):
+                if (code >> i) & 1:
+                    s[d] = dirs[d]
+            bn, en = neighbour(s)
+            Kn = tuple(K[d] if s[d] == 0 else (P if s[d] < 0 else 0) for d in range(D))
+            acc += read(bn, en, Kn)
+            count += 1
+        out.append(acc / count)
+    return np.array(out)
+
+
+def pairing(u, mesh, t, K, s, var=1, continuous=False, he=None):
+    """pairing(p, t, u, K, s; var, continuous) (src/transfer.jl:1779-1797):
+    int K g_h over the support's elements, each by the nested rule kept to the
+    support (compact), g_h the element's polynomial of var (made continuous
+    first with continuous=True). K maps points (npts, D) to (npts, C)."""
+    D = mesh.D
+    if he is None:
+        he = float(np.min(mesh.spacings[mesh.mask])) * (mesh.P + 1)
+    acc = 0.0
+    for b, e in support_elements(mesh, s, he):
+        lo, hi = mesh.element_box(b, e)
+        g = continuous_values(u, mesh, b, e, var) if continuous else u[mesh.node_index(b, e, var)]
+        acc = acc + nested_rule(lambda X: np.asarray(K(X)) * (t.element_basis(lo, hi, X) @ g)[:, None],
+                                s, t, lo, hi, D, compact=True)
+    return acc

@@ -404,3 +404,203 @@ def test_projection_in_the_ball_cube_keeps_the_charge(native):
     assert total == pytest.approx(Q / gamma, rel=1e-12)
     with pytest.raises(ValueError, match="cube"):
         twoldg.TransferPlan(p, [twoldg.ParticleSupport((0.99, 0.0, 0.0), (0, 0, 0), 0.05)], ((0.5, 0, 0), 0.2))
+
+
+# The pairing (src/transfer.jl:1779-1797) of each particle's density kernel
+# (grad rho, rho) with a field, on the device against the oracle's nested
+# rule. The gradient's integrand is of size Q/ell, the density's of size Q:
+# each component is held to 1e-12 of its own scale times max |g|.
+def _pair_scale(s, Q):
+    return np.array([Q / s.ell] * 3 + [Q])
+
+
+def _oracle_pairs(p, g, parts, Q, var, continuous):
+    mesh, t = _mesh(p), T.Tables(p.P)
+    he = min(p.forest.spacing(k) for k in p.forest.leaves) * (p.P + 1)
+    return np.array([T.pairing(g, mesh, t, lambda X, s=s: T.density_kernel(X, s.z, s.v, s.ell, Q),
+                               T.Support(s.z, s.v, s.ell), var=var, continuous=continuous, he=he) for s in parts])
+
+
+@pytest.mark.parametrize("moving", [False, True])
+def test_pairing_matches_the_oracle(native, moving):
+    import torch
+    from twoldg import ParticleSupport, TransferPlan
+    p = _problem(3, 3, 4)
+    he, Q = 0.125, 0.07
+    ell = 0.05 * he
+    v = np.array([0.2, -0.1, 0.05]) if moving else np.zeros(3)
+    # one support on the corner of eight blocks, one across an element face
+    parts = [ParticleSupport((0.5 + 0.3 * ell, 0.5 - 0.2 * ell, 0.5 + 0.1 * ell), v, ell, charge=Q),
+             ParticleSupport((0.3, 0.375 - 0.4 * ell, 0.7), -v, ell, charge=Q)]
+    plan = TransferPlan(p, parts, ((0.5, 0.5, 0.5), 0.6))
+    assert [len(plan.support_elements(k)) for k in range(2)] == [8, 2]
+    mesh = _mesh(p)
+    for k, s in enumerate(parts):
+        assert plan.support_elements(k) == T.support_elements(mesh, T.Support(s.z, s.v, s.ell), he)
+    g = irregular(p.state_words)
+    u = torch.from_numpy(g.copy()).cuda()
+    for var in (1, 2):
+        for continuous in (False, True):
+            got = plan.pairing(u, var=var, continuous=continuous)
+            ref = _oracle_pairs(p, g, parts, Q, var, continuous)
+            for k, s in enumerate(parts):
+                assert np.all(np.abs(got[k] - ref[k]) <= 1e-12 * _pair_scale(s, Q)), (var, continuous, k)
+
+
+@pytest.mark.parametrize("ratio", [1e-1, 1e-2, 1e-3, 1e-4])
+@pytest.mark.parametrize("moving", [False, True])
+def test_pairing_integrates_the_particle_at_any_size(native, ratio, moving):
+    # test/transfer_tests.jl:172-214 through the device: the pairing with a
+    # polynomial is its exact moment (the ball rule in the rest frame), and
+    # the gradient's is minus the moment of the polynomial's gradient
+    import torch
+    from twoldg import ParticleSupport, TransferPlan
+    from transfer_cases import grad_poly
+    p = _problem(3, 3, 1)
+    he, Q = 0.5, 1e-3
+    ell = ratio * he
+    v = np.array([0.1, -0.15, 0.05]) if moving else np.zeros(3)
+    z = np.array([0.5, 0.5, 0.5]) + ell * np.array([0.3, -0.2, 0.1])
+    plan = TransferPlan(p, [ParticleSupport(z, v, ell, charge=Q)], (z, 2 * ell))
+    assert len(plan.support_elements(0)) == 8
+    g = p.fill_at_nodes(lambda x, var: poly(np.stack([x[0].reshape(-1), x[1].reshape(-1), x[2].reshape(-1)],
+                                                     axis=1)).reshape(x[0].shape)).reshape(-1)
+    got = plan.pairing(torch.from_numpy(g.copy()).cuda(), var=1)[0]
+    assert got[3] == pytest.approx(exact_moment(poly, Q, ell, z, v), rel=1e-12)
+    for d in range(3):
+        assert abs(got[d] + exact_moment(lambda X: grad_poly(X)[:, d], Q, ell, z, v)) <= 1e-12 * Q / ell
+
+
+def test_pairing_is_the_density_projection_folded(native):
+    # test/transfer_tests.jl:398-425: <P rho, g>_w, the projection of the
+    # density over the mesh folded with g, is the pairing of rho with g
+    import torch
+    from twoldg import ParticleSupport, TransferPlan
+    p = _problem(3, 3, 2)
+    he, Q = 0.25, 0.07
+    ell = 0.01 * he
+    g = irregular(p.state_words)
+    for v in (np.zeros(3), np.array([0.2, 0.1, 0.0])):
+        z = np.array([0.5, 0.5 + 0.004 * he, 0.3])
+        plan = TransferPlan(p, [ParticleSupport(z, v, ell, charge=Q)], (z, 2 * ell))
+        du = p.statevector()
+        plan.project(du, "density", factor=1.0, var=1)
+        fold = _inner(p, _host(du), g, 1)
+        got = plan.pairing(torch.from_numpy(g.copy()).cuda(), var=1)[0]
+        assert got[3] == pytest.approx(fold, rel=1e-13)
+
+
+def test_continuous_pairing_reads_a_continuous_field_as_it_is(native):
+    # test/transfer_tests.jl:427-472 through the device
+    import torch
+    from twoldg import ParticleSupport, TransferPlan
+    p = _problem(3, 3, 4)
+    he, Q = 0.125, 0.07
+    ell = 0.01 * he
+
+    def smooth(x, var):
+        return var * (np.sin(np.pi * (2 * x[0] + 0.3)) * np.cos(np.pi * (3 * x[1] - 0.1)) + x[2] ** 2)
+
+    g = p.fill_at_nodes(smooth).reshape(-1)
+    u = torch.from_numpy(g.copy()).cuda()
+    for z in ((0.5 + 0.3 * ell, 0.375 - 0.4 * ell, 0.6), (0.5 - 0.2 * ell, 0.5 + 0.3 * ell, 0.625 + 0.1 * ell)):
+        plan = TransferPlan(p, [ParticleSupport(z, (0, 0, 0), ell, charge=Q)], (z, 2 * ell))
+        for var in (1, 2):
+            a = plan.pairing(u, var=var, continuous=True)[0]
+            b = plan.pairing(u, var=var)[0]
+            assert np.all(np.abs(a - b) <= 1e-12 * np.abs(b).max()), var
+        b0, e0 = plan.support_elements(0)[0]
+        g2 = g.copy().reshape(p.nblocks, 2, -1)
+        P1, N = p.P + 1, p.N
+        for K in np.ndindex(P1, P1, P1):
+            i = sum((e0[d] * P1 + K[d]) * N ** d for d in range(3))
+            g2[b0, 0, i] += 1
+        u2 = torch.from_numpy(g2.reshape(-1).copy()).cuda()
+
+        def jump(continuous):
+            return np.linalg.norm((plan.pairing(u2, 1, continuous) - plan.pairing(u, 1, continuous))[0, :3])
+
+        assert jump(False) > 0.1 * Q / ell
+        assert jump(True) < 0.15 * jump(False) and jump(True) < 10 * Q / he
+    plan = TransferPlan(p, [ParticleSupport((0.5, 0.125 - 0.4 * ell, 0.6), (0, 0, 0), ell)], ((0.5, 0.5, 0.5), 0.6))
+    plan.pairing(u, 1)
+    with pytest.raises(ValueError, match="does not look for periodic images"):
+        plan.pairing(u, 1, continuous=True)
+
+
+def test_pairing_refusals(native):
+    import torch
+    from twoldg import ParticleSupport, TransferPlan
+    p = _problem(3, 3, 1)
+    u = torch.zeros(p.state_words, dtype=torch.float64, device="cuda")
+    plan = TransferPlan(p, [ParticleSupport((0.3, 0.3, 0.3), (0, 0, 0), 0.3)], ((0.3, 0.3, 0.3), 0.5))
+    with pytest.raises(ValueError, match="not smaller than an element"):
+        plan.pairing(u)
+    plan.update([ParticleSupport((0.01, 0.3, 0.3), (0, 0, 0), 0.02)])
+    with pytest.raises(ValueError, match="periodic images"):
+        plan.pairing(u)
+    # the projection still runs on the refused plan
+    plan.project(p.statevector(), "density")
+
+
+def test_float32_pairing_matches_the_oracle_of_its_values(native):
+    # the moments are FP64 whatever the field type: the pairing of an FP32
+    # state is the oracle's pairing of the same (rounded) values
+    import torch
+    from twoldg import ParticleSupport, TransferPlan
+    p = _problem(3, 3, 2, dtype=np.float32)
+    he, Q = 0.25, 0.07
+    ell = 0.05 * he
+    s = ParticleSupport((0.5 + 0.3 * ell, 0.5 - 0.2 * ell, 0.4), (0.1, 0.2, 0.0), ell, charge=Q)
+    plan = TransferPlan(p, [s], ((0.5, 0.5, 0.5), 0.6))
+    g = irregular(p.state_words).astype(np.float32)
+    u = torch.from_numpy(g.copy()).cuda()
+    ref = _oracle_pairs(p, g.astype(np.float64), [s], Q, 2, True)
+    got = plan.pairing(u, var=2, continuous=True)
+    assert np.all(np.abs(got[0] - ref[0]) <= 1e-12 * _pair_scale(s, Q))
+
+
+def test_pairing_repeats_and_follows_the_particles(native):
+    # a pairing is the same to the bit on every call, and an updated plan's is
+    # a fresh plan's; particle_forces is grad rho paired with u less v times
+    # rho paired with v
+    import torch
+    import twoldg
+    from twoldg import ParticleSupport, TransferPlan
+    p = _problem(3, 3, 2)
+    ball = ((0.5, 0.5, 0.5), 0.6)
+    a = [ParticleSupport((0.41, 0.52, 0.47), (0.1, 0.0, 0.0), 0.02, charge=0.5),
+         ParticleSupport((0.7, 0.33, 0.61), (0.0, -0.2, 0.05), 0.015, charge=-0.5)]
+    b = [ParticleSupport((0.5, 0.51, 0.49), (0.1, 0.02, 0.0), 0.02, charge=0.5),
+         ParticleSupport((0.69, 0.375, 0.6), (0.0, -0.2, 0.05), 0.015, charge=-0.5)]
+    u = torch.from_numpy(irregular(p.state_words)).cuda()
+    plan = TransferPlan(p, a, ball)
+    first = plan.pairing(u, 1, True)
+    assert np.array_equal(first, plan.pairing(u, 1, True))
+    plan.update(b)
+    fresh = TransferPlan(p, b, ball)
+    for var in (1, 2):
+        assert np.array_equal(plan.pairing(u, var, True), fresh.pairing(u, var, True))
+    F = twoldg.particle_forces(plan, u)
+    phi, pi = plan.pairing(u, 1, True), plan.pairing(u, 2, True)
+    v = np.array([s.v for s in b])
+    assert np.array_equal(F, phi[:, :3] - v * pi[:, 3:4])
+
+
+def test_pairing_in_the_ball_cube(native):
+    # in the seven-patch ball's cube a constant field pairs to Q / gamma with
+    # rho and to zero with grad rho
+    import torch
+    import twoldg
+    forest, geo = twoldg.sevenpatch_forest(np.float64, 3, 2, roots=(4, 4), Lc=1.0, R1=3.0)
+    p = twoldg.WaveProblem(forest, twoldg.Element(np.float64, 3), truncate=True, geometry=geo,
+                           boundary=twoldg.RadiativeBoundary())
+    v = np.array([0.1, 0.05, -0.2])
+    z = np.array([0.013, -0.021, 0.008])
+    Q, ell = 0.2, 0.01
+    plan = twoldg.TransferPlan(p, [twoldg.ParticleSupport(z, v, ell, charge=Q)], (z, 3 * ell))
+    u = torch.ones(p.state_words, dtype=torch.float64, device="cuda")
+    got = plan.pairing(u, var=1, continuous=True)[0]
+    gamma = 1 / math.sqrt(1 - v @ v)
+    assert got[3] == pytest.approx(Q / gamma, rel=1e-12)
+    assert np.abs(got[:3]).max() <= 1e-12 * Q / ell

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from oracle import transfer as T
-from transfer_cases import exact_moment, irregular, poly, reference_integral
+from transfer_cases import brick_values, exact_moment, grad_poly, irregular, poly, reference_integral
 
 
 def _lib_table(P, dtype, name, q=None):
@@ -248,3 +248,87 @@ def test_oracle_averaging_is_the_projection_onto_continuous_fields():
                 vals = (1 + X[:, 0] * X[:, -1]).reshape((4,) * D)
                 g[mesh.node_index(b, e, 2)] = np.transpose(vals, tuple(range(D - 1, -1, -1))).reshape(-1)
         assert np.allclose(T.average_shared(g.copy(), mesh, ball, 2), g, rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("ratio", [1e-1, 1e-3])
+@pytest.mark.parametrize("moving", [False, True])
+def test_oracle_pairing_integrates_the_particle(ratio, moving):
+    # test/transfer_tests.jl:172-214: the pairing of the particle's density
+    # with a polynomial is exact to 1e-12 at any size; the gradient's, whose
+    # integrand is of size Q/ell and cancels to Q |grad g|, to 1e-12 Q/ell
+    P = 3
+    mesh = T.brick_mesh(3, P, 2, 1)
+    t = T.Tables(P)
+    he = 0.5
+    ell, Q = ratio * he, 1e-3
+    v = np.array([0.1, -0.15, 0.05]) if moving else np.zeros(3)
+    z = np.array([0.5, 0.5, 0.5]) + ell * np.array([0.3, -0.2, 0.1])
+    s = T.Support(z, v, ell)
+    g = brick_values(mesh, t, poly)
+    got = T.pairing(g, mesh, t, lambda X: T.density_kernel(X, z, v, ell, Q), s, var=1)
+    assert got[3] == pytest.approx(exact_moment(poly, Q, ell, z, v), rel=1e-12)
+    for d in range(3):
+        exact = -exact_moment(lambda X: grad_poly(X)[:, d], Q, ell, z, v)
+        assert abs(got[d] - exact) <= 1e-12 * Q / ell
+    assert len(T.support_elements(mesh, s, he)) == 8
+
+
+def test_oracle_pairing_is_the_projection_folded():
+    # test/transfer_tests.jl:398-425: the pairing over the support equals the
+    # projection of the kernel over the mesh folded with the grid function
+    P = 3
+    mesh = T.brick_mesh(3, P, 2, 1)
+    t = T.Tables(P)
+    he = 0.5
+    ell, Q = 0.01 * he, 0.07
+    g = irregular(mesh.nblocks * 2 * mesh.NN)
+    z = np.array([0.5, 0.5 + 0.004 * he, 0.3])
+    for v, comps in ((np.zeros(3), (3,)), (np.array([0.2, 0.1, 0.0]), (0, 1, 2, 3))):
+        s = T.Support(z, v, ell)
+        got = T.pairing(g, mesh, t, lambda X: T.density_kernel(X, z, v, ell, Q), s, var=1)
+        for c in comps:
+            du = T.project_source(np.zeros_like(g), mesh, t, lambda X: T.density_kernel(X, z, v, ell, Q)[:, c], [s],
+                                  (z, 2 * ell), factor=1.0, var=1, he=he)
+            fold = T.weighted_inner(mesh, t, du, g, 1)
+            assert got[c] == pytest.approx(fold, rel=1e-13 if c == 3 else 1e-12)
+
+
+def test_oracle_continuous_pairing():
+    # test/transfer_tests.jl:427-472: the continuous pairing reads a field
+    # filled at the nodes as it is, takes away most of a face jump, and
+    # refuses to look across the domain's faces
+    P = 3
+    mesh = T.brick_mesh(3, P, 2, 2)
+    t = T.Tables(P)
+    he = 0.25
+    ell, Q = 0.01 * he, 0.07
+
+    def smooth(X):
+        return np.sin(np.pi * (2 * X[:, 0] + 0.3)) * np.cos(np.pi * (3 * X[:, 1] - 0.1)) + X[:, 2] ** 2
+
+    g = brick_values(mesh, t, smooth)
+    g.reshape(mesh.nblocks, 2, mesh.NN)[:, 1] *= 2
+    z = np.array([0.5 - 0.2 * ell, 0.5 + 0.3 * ell, 0.625 + 0.1 * ell])
+    s = T.Support(z, np.zeros(3), ell)
+
+    def K(X):
+        return T.density_kernel(X, z, np.zeros(3), ell, Q)
+
+    for var in (1, 2):
+        a = T.pairing(g, mesh, t, K, s, var=var, continuous=True)
+        b = T.pairing(g, mesh, t, K, s, var=var)
+        assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
+    b0, e0 = T.support_elements(mesh, s, he)[0]
+    g2 = g.copy()
+    g2[mesh.node_index(b0, e0, 1)] += 1
+
+    def jump(continuous):
+        return (T.pairing(g2, mesh, t, K, s, var=1, continuous=continuous) -
+                T.pairing(g, mesh, t, K, s, var=1, continuous=continuous))[:3]
+
+    plain, cont = np.linalg.norm(jump(False)), np.linalg.norm(jump(True))
+    assert plain > 0.1 * Q / ell
+    assert cont < 0.15 * plain and cont < 10 * Q / he
+    s = T.Support(np.array([0.5, 0.125 - 0.4 * ell, 0.6]), np.zeros(3), ell)
+    with pytest.raises(ValueError, match="does not look for periodic images"):
+        T.pairing(g, mesh, t, lambda X: np.ones((len(X), 1)), s, continuous=True)

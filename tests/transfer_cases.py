@@ -77,3 +77,25 @@ def reference_integral(f, lo, hi, z, scale, grades, ell, prefix=()):
             return np.array([reference_integral(f, lo, hi, z, scale, grades, ell, prefix + (float(x),))
                              for x in xs])
     return _composite(g, lo[d], hi[d], breaks)
+
+
+def grad_poly(X):
+    """The gradient of poly, (npts, 3)."""
+    X = np.atleast_2d(X)
+    x, y, z = X[:, 0], X[:, 1], X[:, 2]
+    return np.stack([1 + 3 * x ** 2 * y ** 3 * z ** 3, -4 * y * z + 3 * x ** 3 * y ** 2 * z ** 3,
+                     -2 * y * y + 3 * x ** 3 * y ** 3 * z ** 2], axis=1)
+
+
+def brick_values(mesh, t, f):
+    """A state vector of the oracle's brick mesh with f at every node, in
+    both variables."""
+    u = np.zeros(mesh.nblocks * 2 * mesh.NN)
+    P1 = mesh.P + 1
+    for b, e in mesh.elements():
+        lo, hi = mesh.element_box(b, e)
+        xs = [lo[d] + (hi[d] - lo[d]) * (1 + t.nodes) / 2 for d in range(mesh.D)]
+        X = np.array([[xs[d][K[mesh.D - 1 - d]] for d in range(mesh.D)] for K in np.ndindex(*([P1] * mesh.D))])
+        for var in (1, 2):
+            u[mesh.node_index(b, e, var)] = f(X)
+    return u

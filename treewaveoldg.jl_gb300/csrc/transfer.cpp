@@ -3,7 +3,9 @@
 // of the blocks the source's ball meets into the far rule, the graded bands
 // and the nested rule, the nested rule's points (split at each particle's
 // support, Gauss inside, Johnston and Elliott's sinh rule outside) in
-// innermost lines, and the C ABI over the kernels of transfer_kernels.cu.
+// innermost lines, the pairing's support elements, compact lines and node
+// gathers (:1449-1500, 1726-1797), and the C ABI over the kernels of
+// transfer_kernels.cu.
 // A plan keeps what does not move with the particles (the frame's geometry,
 // the ball's blocks, the tables, on the host and the device) and redoes only
 // what the particles' positions decide when they move, into device buffers
@@ -208,12 +210,15 @@ struct NearLines {
     std::vector<int32_t> inner;         // per line: the points inside the support's section
 };
 
+// With `compact` (the pairing's rule, whose kernel vanishes outside the
+// support) every line keeps only its segments inside the support's section,
+// and a line left without points is not emitted.
 void collect_lines(const Support& s, const NestedTables& t, const double* lo, const double* hi,
-                   std::vector<double>& prefix, double w, int n, NearLines& out) {
+                   std::vector<double>& prefix, double w, int n, bool compact, NearLines& out) {
     if (n == 1) {
         const int32_t p0 = (int32_t)out.lw.size();
         int32_t i0 = -1, i1 = -1;
-        line_fold(s, t, lo, hi, prefix, true, false,
+        line_fold(s, t, lo, hi, prefix, true, compact,
                   [&](const std::vector<double>& lx, const std::vector<double>& lw, bool inside) {
                       // the inside segments are consecutive: the section is an interval
                       if (inside && i0 < 0) i0 = (int32_t)out.lw.size();
@@ -221,6 +226,7 @@ void collect_lines(const Support& s, const NestedTables& t, const double* lo, co
                       out.lw.insert(out.lw.end(), lw.begin(), lw.end());
                       if (inside) i1 = (int32_t)out.lw.size();
                   });
+        if (compact && (int32_t)out.lw.size() == p0) return;
         out.range.push_back(p0);
         out.range.push_back((int32_t)out.lw.size());
         out.inner.push_back(i0 < 0 ? 0 : i0);
@@ -230,18 +236,111 @@ void collect_lines(const Support& s, const NestedTables& t, const double* lo, co
         out.vals.push_back(w);
         return;
     }
-    line_fold(s, t, lo, hi, prefix, false, false, [&](const std::vector<double>& lx, const std::vector<double>& lw, bool) {
-        for (size_t k = 0; k < lx.size(); ++k) {
-            prefix.push_back(lx[k]);
-            collect_lines(s, t, lo, hi, prefix, w * lw[k], n - 1, out);
-            prefix.pop_back();
-        }
-    });
+    line_fold(s, t, lo, hi, prefix, false, compact,
+              [&](const std::vector<double>& lx, const std::vector<double>& lw, bool) {
+                  for (size_t k = 0; k < lx.size(); ++k) {
+                      prefix.push_back(lx[k]);
+                      collect_lines(s, t, lo, hi, prefix, w * lw[k], n - 1, compact, out);
+                      prefix.pop_back();
+                  }
+              });
 }
 
 struct HostElem {
     int block, e[3], particle;
 };
+
+// An element box and the particle whose support splits its nested rule.
+struct LineBox {
+    double lo[3], hi[3];
+    int particle;
+};
+
+// The nested rule's innermost lines over the boxes on up to 16 host threads,
+// threaded as the reference threads its near pass (src/transfer.jl:1160-1213):
+// over the points of each box's outermost line (the box's own line in one
+// dimension), each item the lines through one point, kept in the serial
+// order. The particle's own element holds the most points, and threading over
+// elements left it on one thread. first[i] is box i's first line, first[n]
+// the number of lines. False if the points exceed what an int32 indexes.
+bool nested_lines(const std::vector<Support>& parts, const NestedTables& nt, int D, const std::vector<LineBox>& boxes,
+                  bool compact, NearLines& nl, std::vector<int64_t>& first) {
+    struct Item {
+        int box;
+        double x, w;
+    };
+    std::vector<Item> items;
+    for (size_t i = 0; i < boxes.size(); ++i) {
+        if (D == 1) {
+            items.push_back(Item{(int)i, 0.0, 1.0});
+            continue;
+        }
+        line_fold(parts[boxes[i].particle], nt, boxes[i].lo, boxes[i].hi, std::vector<double>(), false, compact,
+                  [&](const std::vector<double>& lx, const std::vector<double>& lw, bool) {
+                      for (size_t k = 0; k < lx.size(); ++k) items.push_back(Item{(int)i, lx[k], lw[k]});
+                  });
+    }
+    std::vector<NearLines> per(items.size());
+    {
+        std::atomic<size_t> next(0);
+        auto work = [&]() {
+            for (size_t n = next++; n < items.size(); n = next++) {
+                const Item& it = items[n];
+                const LineBox& bx = boxes[it.box];
+                std::vector<double> prefix;
+                if (D == 1) {
+                    collect_lines(parts[bx.particle], nt, bx.lo, bx.hi, prefix, 1.0, 1, compact, per[n]);
+                } else {
+                    prefix.push_back(it.x);
+                    collect_lines(parts[bx.particle], nt, bx.lo, bx.hi, prefix, it.w, D - 1, compact, per[n]);
+                }
+            }
+        };
+        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        const unsigned nt_ = (unsigned)std::min<size_t>(hw, items.size());
+        std::vector<std::thread> pool;
+        for (unsigned k = 1; k < nt_; ++k) pool.emplace_back(work);
+        work();
+        for (auto& t : pool) t.join();
+    }
+    first.assign(boxes.size() + 1, 0);
+    size_t nlx = 0, nlines = 0;
+    for (const NearLines& x : per) {
+        nlx += x.lw.size();
+        nlines += x.range.size() / 2;
+    }
+    nl = NearLines();
+    nl.lx.reserve(nlx);
+    nl.lw.reserve(nlx);
+    nl.vals.reserve(3 * nlines);
+    nl.range.reserve(2 * nlines);
+    nl.inner.reserve(2 * nlines);
+    for (size_t n = 0; n < per.size(); ++n) {
+        NearLines& x = per[n];
+        const int32_t off = (int32_t)nl.lw.size();
+        if (nl.lw.size() + x.lw.size() > (size_t)std::numeric_limits<int32_t>::max() / 2) return false;
+        nl.lx.insert(nl.lx.end(), x.lx.begin(), x.lx.end());
+        nl.lw.insert(nl.lw.end(), x.lw.begin(), x.lw.end());
+        nl.vals.insert(nl.vals.end(), x.vals.begin(), x.vals.end());
+        for (int32_t v : x.range) nl.range.push_back(v + off);
+        for (size_t k = 0; k < x.inner.size(); k += 2) {
+            const bool any = x.inner[k + 1] > x.inner[k];
+            nl.inner.push_back(any ? x.inner[k] + off : 0);
+            nl.inner.push_back(any ? x.inner[k + 1] + off : 0);
+        }
+        first[items[n].box + 1] = (int64_t)nl.range.size() / 2;
+        x = NearLines();
+    }
+    for (size_t i = 0; i < boxes.size(); ++i) first[i + 1] = std::max(first[i + 1], first[i]);
+    return true;
+}
+
+// At most kNearLines lines a chunk, fewer when the lines are few, so that a
+// small set (the density's lines inside the supports) still spreads over the
+// GPU's SMs.
+int64_t chunk_lines(int64_t nlines) {
+    return (int64_t)std::max<int64_t>(4, std::min<int64_t>(kNearLines, (nlines + 607) / 608));
+}
 
 // The tables a plan reads, built once per process in double-double and kept
 // (the 1D Gauss rules of the nested rule, each tensor rule of an order, the
@@ -361,11 +460,28 @@ struct twoldg_transfer_plan {
     int64_t counts[8] = {0};
     int64_t npoints = 0;
     bool density_ok = false;
+    // the particles as set_particles last took them, and the frame's box
+    std::vector<Support> supports;
+    double dom_lo[3] = {0, 0, 0}, dom_hi[3] = {0, 0, 0};
+    // The pairing, built at the first pairing after the particles move: per
+    // particle its support elements, their compact lines and moments, and
+    // the gathers of their nodal values, plain and averaged over the elements
+    // that share a node (the latter refused, with its reason, where a
+    // support element is on the domain's face or next to a coarser block).
+    bool pair_ready = false;
+    std::string pair_cont_error;
+    std::vector<int32_t> pair_list;   // (block, e0, e1, e2) per support element
+    DevVec d_pelems, d_plx, d_plw, d_pvals, d_plines, d_pchunks, d_ppartials, d_pmoments;
+    DevVec d_pgather, d_pgather_c, d_pbary, d_pgll, d_pout;
+    PairingLaunch PL;
 
     ~twoldg_transfer_plan() {
         if (stream) cudaStreamSynchronize(stream);
     }
     int set_particles(const twoldg_particle* tp, int n);
+    int build_pairing();
+    // the frame's block that holds x (lo <= x < hi), or -1
+    int64_t locate(const double* x) const;
 };
 
 namespace {
@@ -384,6 +500,8 @@ namespace {
 // elements, each element's lines in the serial order), the density's subsets,
 // and their upload into the plan's reused device buffers.
 int twoldg_transfer_plan::set_particles(const twoldg_particle* tps, int np) {
+    // the pairing is rebuilt from the supports kept below, the last ones taken
+    pair_ready = false;
     if (np < 0 || np > kMaxParticles)
         return fail(TWOLDG_EUNSUP, "at most " + std::to_string(kMaxParticles) + " particles, got " + std::to_string(np));
     if (np > 0 && !tps) return fail(TWOLDG_EINVAL, "particles must not be NULL");
@@ -486,83 +604,16 @@ int twoldg_transfer_plan::set_particles(const twoldg_particle* tps, int np) {
                     near.push_back(h);
                 }
     }
-    // The nested rule's lines on up to 16 host threads, threaded as the
-    // reference threads its near pass (src/transfer.jl:1160-1213): over the
-    // points of each near element's outermost line (the element's own line in
-    // one dimension), each item the lines through one point, kept in the
-    // serial order. The particle's own element holds the most points, and
-    // threading over elements left it on one thread.
-    struct Item {
-        int elem;
-        double x, w;
-    };
-    std::vector<Item> items;
+    // the nested rule's lines, per near element its first line
+    std::vector<LineBox> boxes(near.size());
     for (size_t i = 0; i < near.size(); ++i) {
-        if (D == 1) {
-            items.push_back(Item{(int)i, 0.0, 1.0});
-            continue;
-        }
-        double lo[3], hi[3];
-        elem_box(near[i].block, near[i].e, lo, hi);
-        line_fold(parts[near[i].particle], nt, lo, hi, std::vector<double>(), false, false,
-                  [&](const std::vector<double>& lx, const std::vector<double>& lw, bool) {
-                      for (size_t k = 0; k < lx.size(); ++k) items.push_back(Item{(int)i, lx[k], lw[k]});
-                  });
-    }
-    std::vector<NearLines> per(items.size());
-    {
-        std::atomic<size_t> next(0);
-        auto work = [&]() {
-            for (size_t n = next++; n < items.size(); n = next++) {
-                const Item& it = items[n];
-                double lo[3], hi[3];
-                elem_box(near[it.elem].block, near[it.elem].e, lo, hi);
-                std::vector<double> prefix;
-                if (D == 1) {
-                    collect_lines(parts[near[it.elem].particle], nt, lo, hi, prefix, 1.0, 1, per[n]);
-                } else {
-                    prefix.push_back(it.x);
-                    collect_lines(parts[near[it.elem].particle], nt, lo, hi, prefix, it.w, D - 1, per[n]);
-                }
-            }
-        };
-        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-        const unsigned nt_ = (unsigned)std::min<size_t>(hw, items.size());
-        std::vector<std::thread> pool;
-        for (unsigned k = 1; k < nt_; ++k) pool.emplace_back(work);
-        work();
-        for (auto& t : pool) t.join();
+        elem_box(near[i].block, near[i].e, boxes[i].lo, boxes[i].hi);
+        boxes[i].particle = near[i].particle;
     }
     NearLines nl;
-    std::vector<int64_t> first(near.size() + 1, 0);   // per near element its first line
-    size_t nlx = 0, nlines = 0;
-    for (const NearLines& x : per) {
-        nlx += x.lw.size();
-        nlines += x.range.size() / 2;
-    }
-    nl.lx.reserve(nlx);
-    nl.lw.reserve(nlx);
-    nl.vals.reserve(3 * nlines);
-    nl.range.reserve(2 * nlines);
-    nl.inner.reserve(2 * nlines);
-    for (size_t n = 0; n < per.size(); ++n) {
-        NearLines& x = per[n];
-        const int32_t off = (int32_t)nl.lw.size();
-        if (nl.lw.size() + x.lw.size() > (size_t)std::numeric_limits<int32_t>::max() / 2)
-            return fail(TWOLDG_EUNSUP, "the nested rule's points exceed 2^30");
-        nl.lx.insert(nl.lx.end(), x.lx.begin(), x.lx.end());
-        nl.lw.insert(nl.lw.end(), x.lw.begin(), x.lw.end());
-        nl.vals.insert(nl.vals.end(), x.vals.begin(), x.vals.end());
-        for (int32_t v : x.range) nl.range.push_back(v + off);
-        for (size_t k = 0; k < x.inner.size(); k += 2) {
-            const bool any = x.inner[k + 1] > x.inner[k];
-            nl.inner.push_back(any ? x.inner[k] + off : 0);
-            nl.inner.push_back(any ? x.inner[k + 1] + off : 0);
-        }
-        first[items[n].elem + 1] = (int64_t)nl.range.size() / 2;
-        x = NearLines();
-    }
-    for (size_t i = 0; i < near.size(); ++i) first[i + 1] = std::max(first[i + 1], first[i]);
+    std::vector<int64_t> first;
+    if (!nested_lines(parts, nt, D, boxes, false, nl, first))
+        return fail(TWOLDG_EUNSUP, "the nested rule's points exceed 2^30");
     // tensor rule elements and the values' offsets
     std::vector<RuleElement> relems;
     int64_t base = 0;
@@ -587,12 +638,7 @@ int twoldg_transfer_plan::set_particles(const twoldg_particle* tps, int np) {
         }
     }
     counts[3] = base - counts[1];
-    // Near elements and their chunks of lines: at most kNearLines lines a
-    // chunk, fewer when the lines are few, so that a small set (the density's
-    // lines inside the supports) still spreads over the GPU's SMs.
-    auto chunk_lines = [](int64_t nlines) {
-        return (int64_t)std::max<int64_t>(4, std::min<int64_t>(kNearLines, (nlines + 607) / 608));
-    };
+    // near elements and their chunks of lines
     const int64_t cl = chunk_lines(first.back());
     std::vector<NearElement> nelems;
     std::vector<NearChunk> chunks;
@@ -728,6 +774,212 @@ int twoldg_transfer_plan::set_particles(const twoldg_particle* tps, int np) {
     Ld.near_elems = static_cast<const NearElement*>(d_delems.p);
     Ld.n_near_elems = (int64_t)delems.size();
     Ld.partials = d_dpartials.p;
+    supports = parts;
+    return TWOLDG_OK;
+}
+
+int64_t twoldg_transfer_plan::locate(const double* x) const {
+    for (int64_t b = 0; b < nb; ++b) {
+        if (!mask.empty() && !mask[b]) continue;
+        bool in = true;
+        for (int k = 0; k < D; ++k) {
+            const double lo = origins[b * D + k];
+            in = in && lo <= x[k] && x[k] < lo + spacings[b] * N;
+        }
+        if (in) return b;
+    }
+    return -1;
+}
+
+// The pairing's fixed part for the current particles (support_elements,
+// src/transfer.jl:1726-1758; continuous_values, :1449-1500): the elements
+// that hold a corner of each support's box, in the corners' order; their
+// lines of the nested rule kept to the support and the moments of the
+// kernel over them, launched on the plan's stream; and the two gathers.
+int twoldg_transfer_plan::build_pairing() {
+    if (D != 3) return fail(TWOLDG_EUNSUP, "the particles' density kernel is three-dimensional");
+    const int np = (int)supports.size();
+    const int M = P1 * P1 * P1;
+    const int64_t NNv = (int64_t)N * N * N;
+    auto elem_box = [&](int64_t b, const int* e, double* lo, double* hi) {
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = origins[b * 3 + k] + spacings[b] * (e[k] * P1);
+            hi[k] = origins[b * 3 + k] + spacings[b] * ((e[k] + 1) * P1);
+        }
+    };
+    auto element_of = [&](int64_t b, const double* x, int* e) {
+        for (int k = 0; k < 3; ++k) {
+            const int64_t i = (int64_t)std::floor((x[k] - origins[b * 3 + k]) / (spacings[b] * P1));
+            e[k] = (int)std::min<int64_t>(std::max<int64_t>(i, 0), E - 1);
+        }
+    };
+    std::vector<int32_t> list;
+    std::vector<LineBox> boxes;
+    int32_t firsts[kMaxParticles + 1] = {0};
+    for (int k = 0; k < np; ++k) {
+        const Support& s = supports[k];
+        if (!(2 * s.ell < he))
+            return fail(TWOLDG_EINVAL, "the particle's support, 2l = " + fmt(2 * s.ell) +
+                                           " across, is not smaller than an element, h_e = " + fmt(he));
+        bool inside = true;
+        for (int d = 0; d < 3; ++d) inside = inside && dom_lo[d] <= s.z[d] - s.ell && s.z[d] + s.ell < dom_hi[d];
+        if (!inside)
+            return fail(TWOLDG_EINVAL, "the particle's support around z = (" + fmt(s.z[0]) + ", " + fmt(s.z[1]) + ", " +
+                                           fmt(s.z[2]) + ") reaches past the domain's faces; the transfer does not "
+                                           "look for periodic images");
+        const size_t start = list.size() / 4;
+        for (int corner = 0; corner < 8; ++corner) {
+            double x[3];
+            for (int d = 0; d < 3; ++d) x[d] = s.z[d] + ((corner >> d) & 1 ? s.ell : -s.ell);
+            const int64_t b = locate(x);
+            if (b < 0) return fail(TWOLDG_EINVAL, "a corner of particle " + std::to_string(k) + "'s support box is "
+                                                  "outside the frame's blocks");
+            int e[3];
+            element_of(b, x, e);
+            bool seen = false;
+            for (size_t i = start; i < list.size() / 4; ++i)
+                seen = seen || (list[4 * i] == b && list[4 * i + 1] == e[0] && list[4 * i + 2] == e[1] &&
+                                list[4 * i + 3] == e[2]);
+            if (seen) continue;
+            list.insert(list.end(), {(int32_t)b, e[0], e[1], e[2]});
+            LineBox bx{};
+            elem_box(b, e, bx.lo, bx.hi);
+            bx.particle = k;
+            boxes.push_back(bx);
+        }
+        firsts[k + 1] = (int32_t)(list.size() / 4);
+    }
+    const int64_t ne = (int64_t)boxes.size();
+    NearLines nl;
+    std::vector<int64_t> first;
+    if (!nested_lines(supports, nt, D, boxes, true, nl, first))
+        return fail(TWOLDG_EUNSUP, "the pairing's points exceed 2^30");
+    std::vector<NearLine> lines(nl.range.size() / 2);
+    for (size_t l = 0; l < lines.size(); ++l) lines[l] = NearLine{nl.range[2 * l], nl.range[2 * l + 1]};
+    const int64_t cl = chunk_lines((int64_t)lines.size());
+    std::vector<PairElement> pel(ne);
+    std::vector<NearChunk> chunks;
+    for (int64_t i = 0; i < ne; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            pel[i].lo[k] = boxes[i].lo[k];
+            pel[i].hi[k] = boxes[i].hi[k];
+        }
+        pel[i].particle = boxes[i].particle;
+        pel[i].c0 = (int32_t)chunks.size();
+        for (int64_t a = first[i]; a < first[i + 1]; a += cl)
+            chunks.push_back(NearChunk{(int32_t)a, (int32_t)std::min<int64_t>(a + cl, first[i + 1]), (int32_t)i, 0});
+        pel[i].c1 = (int32_t)chunks.size();
+    }
+    // the gathers: per element and node (dimension 0 fastest) the state
+    // offsets of variable 1; for the continuous one the element's own value
+    // first, then the elements across each face, edge and corner the node is
+    // on, in the reference's order (the first dimension fastest)
+    auto offset = [&](int64_t b, const int* e, const int* K) {
+        int64_t o = b * 2 * NNv, st = 1;
+        for (int d = 0; d < 3; ++d) {
+            o += (int64_t)(e[d] * P1 + K[d]) * st;
+            st *= N;
+        }
+        return o;
+    };
+    std::vector<int64_t> gplain((size_t)ne * M * kGather, -1), gcont((size_t)ne * M * kGather, -1);
+    pair_cont_error.clear();
+    for (int64_t i = 0; i < ne && pair_cont_error.empty(); ++i) {
+        const int64_t b = list[4 * i];
+        const int e[3] = {list[4 * i + 1], list[4 * i + 2], list[4 * i + 3]};
+        const double* lo = boxes[i].lo;
+        const double* hi = boxes[i].hi;
+        for (int m = 0; m < M && pair_cont_error.empty(); ++m) {
+            const int K[3] = {m % P1, (m / P1) % P1, m / (P1 * P1)};
+            int64_t* gc = &gcont[((size_t)i * M + m) * kGather];
+            gplain[((size_t)i * M + m) * kGather] = offset(b, e, K);
+            int n = 0;
+            gc[n++] = offset(b, e, K);
+            int dirs[3], freed[3], nfree = 0;
+            for (int d = 0; d < 3; ++d) {
+                dirs[d] = K[d] == 0 ? -1 : (K[d] == P ? 1 : 0);
+                if (dirs[d] != 0) freed[nfree++] = d;
+            }
+            for (int code = 1; code < (1 << nfree); ++code) {
+                int s[3] = {0, 0, 0};
+                for (int j = 0; j < nfree; ++j)
+                    if ((code >> j) & 1) s[freed[j]] = dirs[freed[j]];
+                int en[3];
+                int64_t bn = b;
+                bool within = true;
+                for (int d = 0; d < 3; ++d) {
+                    en[d] = e[d] + s[d];
+                    within = within && 0 <= en[d] && en[d] < E;
+                }
+                if (!within) {
+                    double x[3];
+                    bool in_dom = true;
+                    for (int d = 0; d < 3; ++d) {
+                        x[d] = (lo[d] + hi[d]) / 2 + s[d] * (hi[d] - lo[d]);
+                        in_dom = in_dom && dom_lo[d] < x[d] && x[d] < dom_hi[d];
+                    }
+                    std::string at = "(" + fmt(lo[0]) + ", " + fmt(lo[1]) + ", " + fmt(lo[2]) + ")";
+                    bn = in_dom ? locate(x) : -1;
+                    if (bn < 0) {
+                        pair_cont_error = "the element at " + at + " is on the domain's face; the continuous "
+                                          "reconstruction, like the transfer, does not look for periodic images";
+                        break;
+                    }
+                    if (spacings[bn] != spacings[b]) {
+                        pair_cont_error = "the element at " + at + " has a neighbour on another level; the "
+                                          "continuous reconstruction needs the same level across every face";
+                        break;
+                    }
+                    element_of(bn, x, en);
+                }
+                int Kn[3];
+                for (int d = 0; d < 3; ++d) Kn[d] = s[d] == 0 ? K[d] : (s[d] < 0 ? P : 0);
+                gc[n++] = offset(bn, en, Kn);
+            }
+        }
+    }
+    // upload (an earlier pairing may still read the buffers), then the moments
+    TRY_CUDA(cudaStreamSynchronize(stream), "pairing plan");
+    const ElementTables<double>& et = store().element(P);
+    TRY_CUDA(d_pbary.put(store().barycentric(P)), "pairing upload");
+    TRY_CUDA(d_pgll.put(et.nodes), "pairing upload");
+    TRY_CUDA(d_pelems.put(pel), "pairing upload");
+    TRY_CUDA(d_plx.put(nl.lx), "pairing upload");
+    TRY_CUDA(d_plw.put(nl.lw), "pairing upload");
+    TRY_CUDA(d_pvals.put(nl.vals), "pairing upload");
+    TRY_CUDA(d_plines.put(lines), "pairing upload");
+    TRY_CUDA(d_pchunks.put(chunks), "pairing upload");
+    TRY_CUDA(d_pgather.put(gplain), "pairing upload");
+    if (pair_cont_error.empty()) TRY_CUDA(d_pgather_c.put(gcont), "pairing upload");
+    TRY_CUDA(d_ppartials.reserve(chunks.size() * kPairComponents * M * sizeof(double)), "pairing partials");
+    TRY_CUDA(d_pmoments.reserve((size_t)ne * kPairComponents * M * sizeof(double)), "pairing moments");
+    TRY_CUDA(d_pout.reserve((size_t)std::max(np, 1) * kPairComponents * sizeof(double)), "pairing output");
+    PairingLaunch& a = PL;
+    a = PairingLaunch();
+    a.prec = prec;
+    a.P = P;
+    a.N = N;
+    a.NN = NNv;
+    a.nparticles = np;
+    for (int k = 0; k < np; ++k) a.particles[k] = L.particles[k];
+    for (int k = 0; k <= np; ++k) a.first[k] = firsts[k];
+    a.elems = static_cast<const PairElement*>(d_pelems.p);
+    a.n_elems = ne;
+    a.lines = static_cast<const NearLine*>(d_plines.p);
+    a.lx = static_cast<const double*>(d_plx.p);
+    a.lw = static_cast<const double*>(d_plw.p);
+    a.line_vals = static_cast<const double*>(d_pvals.p);
+    a.chunks = static_cast<const NearChunk*>(d_pchunks.p);
+    a.n_chunks = (int64_t)chunks.size();
+    a.bary = static_cast<const double*>(d_pbary.p);
+    a.gll = static_cast<const double*>(d_pgll.p);
+    a.partials = static_cast<double*>(d_ppartials.p);
+    a.moments = static_cast<double*>(d_pmoments.p);
+    a.out = static_cast<double*>(d_pout.p);
+    cudaError_t e = launch_pairing_moments(a, stream);
+    if (e != cudaSuccess) return fail(TWOLDG_ECUDA, std::string("pairing moments: ") + cudaGetErrorString(e));
+    pair_list = list;
+    pair_ready = true;
     return TWOLDG_OK;
 }
 
@@ -826,6 +1078,17 @@ int twoldg_transfer_plan_create(twoldg_problem* p, const twoldg_transfer_desc* d
     T.spacings.assign(d->spacings, d->spacings + nb);
     if (d->levels) T.levels.assign(d->levels, d->levels + nb);
     if (d->mask) T.mask.assign(d->mask, d->mask + nb);
+    // the frame's box: the hull of its blocks
+    bool any = false;
+    for (int64_t b = 0; b < nb; ++b) {
+        if (!T.mask.empty() && !T.mask[b]) continue;
+        for (int k = 0; k < D; ++k) {
+            const double lo = T.origins[b * D + k], hi = lo + T.spacings[b] * T.N;
+            T.dom_lo[k] = any ? std::min(T.dom_lo[k], lo) : lo;
+            T.dom_hi[k] = any ? std::max(T.dom_hi[k], hi) : hi;
+        }
+        any = true;
+    }
     // the ball's blocks and the ball's finest-level check (SourceBall,
     // check_finest, src/transfer.jl:823-845, 958-982)
     for (int64_t b = 0; b < nb; ++b)
@@ -998,6 +1261,44 @@ int twoldg_average_shared(twoldg_transfer_plan* plan, void* u, int32_t var) {
     A.var = var;
     cudaError_t e = launch_average(A, plan->stream);
     if (e != cudaSuccess) return fail(TWOLDG_ECUDA, std::string("average_shared: ") + cudaGetErrorString(e));
+    return TWOLDG_OK;
+}
+
+int twoldg_pairing(twoldg_transfer_plan* plan, const void* u, int32_t var, int32_t continuous, double* out) {
+    if (!plan || !u || !out) return fail(TWOLDG_EINVAL, "plan, u and out must not be NULL");
+    if (var != 1 && var != 2) return fail(TWOLDG_EINVAL, "var is 1 (u) or 2 (v)");
+    if (!plan->pair_ready) {
+        const int rc = plan->build_pairing();
+        if (rc) return rc;
+    }
+    if (continuous && !plan->pair_cont_error.empty()) return fail(TWOLDG_EINVAL, plan->pair_cont_error);
+    const int np = plan->PL.nparticles;
+    if (np == 0) return TWOLDG_OK;
+    PairingLaunch a = plan->PL;
+    a.u = u;
+    a.var = var;
+    a.gather = static_cast<const int64_t*>(continuous ? plan->d_pgather_c.p : plan->d_pgather.p);
+    cudaError_t e = launch_pairing_dot(a, plan->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, a.out, (size_t)np * kPairComponents * sizeof(double), cudaMemcpyDeviceToHost,
+                            plan->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(plan->stream);
+    if (e != cudaSuccess) return fail(TWOLDG_ECUDA, std::string("pairing: ") + cudaGetErrorString(e));
+    return TWOLDG_OK;
+}
+
+int twoldg_support_elements(twoldg_transfer_plan* plan, int32_t k, int32_t* out, int32_t* n) {
+    if (!plan || !out || !n) return fail(TWOLDG_EINVAL, "plan, out and n must not be NULL");
+    if (k < 0 || k >= (int32_t)plan->supports.size())
+        return fail(TWOLDG_EINVAL, "particle " + std::to_string(k) + " is not among the plan's " +
+                                       std::to_string(plan->supports.size()));
+    if (!plan->pair_ready) {
+        const int rc = plan->build_pairing();
+        if (rc) return rc;
+    }
+    const int32_t e0 = plan->PL.first[k], e1 = plan->PL.first[k + 1];
+    std::memcpy(out, plan->pair_list.data() + 4 * (size_t)e0, 4 * (size_t)(e1 - e0) * sizeof(int32_t));
+    *n = e1 - e0;
     return TWOLDG_OK;
 }
 

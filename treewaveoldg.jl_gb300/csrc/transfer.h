@@ -116,6 +116,55 @@ struct AverageLaunch {
 
 cudaError_t launch_average(const AverageLaunch& a, cudaStream_t stream);
 
+// The pairing (pairing, src/transfer.jl:1779-1797) of each particle's kernel
+// K = (grad rho, rho) (density_kernel, src/dynamic.jl:124-135) with a field:
+// int K g_h = sum_m g_m mu_m over the elements that meet the support, where
+// mu_m = int K phi_m are the kernel's moments, fixed while the particles do
+// not move. They are computed once per set of positions, in FP64 whatever the
+// field type, from the nested rule kept to the support (compact), in innermost
+// lines as the projection's; each pairing after that is one gather of the
+// elements' nodal values (averaged over the elements that share a node, for
+// the continuous pairing) and one dot product per particle.
+constexpr int kPairComponents = 4;   // d rho / dx_d for d < 3, then rho
+
+// A support element: its box, its particle and its chunks of lines.
+struct PairElement {
+    double lo[3], hi[3];
+    int32_t particle, c0, c1, pad;
+};
+
+struct PairingLaunch {
+    int prec = 0, P = 3, N = 8;
+    int64_t NN = 0;
+    int nparticles = 0;
+    TransferParticle particles[kMaxParticles];
+    int32_t first[kMaxParticles + 1] = {0};   // particle k's elements: [first[k], first[k+1])
+    const PairElement* elems = nullptr;
+    int64_t n_elems = 0;
+    const NearLine* lines = nullptr;
+    const double* lx = nullptr;         // per point its last coordinate
+    const double* lw = nullptr;         // per point its last line's weight
+    const double* line_vals = nullptr;  // per line: fixed coordinates (2), outer weight
+    const NearChunk* chunks = nullptr;  // chunk.elem indexes elems
+    int64_t n_chunks = 0;
+    const double* bary = nullptr;       // P+1
+    const double* gll = nullptr;        // P+1
+    double* partials = nullptr;         // n_chunks x 4 x (P+1)^3
+    double* moments = nullptr;          // n_elems x 4 x (P+1)^3
+    // per element and node the state offsets (of variable 1) of the values
+    // averaged there, kGather of them, -1 past the last
+    const int64_t* gather = nullptr;
+    const void* u = nullptr;
+    int var = 1;
+    double* out = nullptr;              // nparticles x 4
+};
+constexpr int kGather = 8;
+
+// The moments of every support element, on `stream`.
+cudaError_t launch_pairing_moments(const PairingLaunch& a, cudaStream_t stream);
+// The pairings with a.u through a.gather into a.out, on `stream`.
+cudaError_t launch_pairing_dot(const PairingLaunch& a, cudaStream_t stream);
+
 // The projection's kernels on `stream`; returns the launch error, if any.
 cudaError_t launch_projection(const TransferLaunch& a, cudaStream_t stream);
 

@@ -564,7 +564,247 @@ cudaError_t points_d(const TransferLaunch& a, void* xs, int64_t n, cudaStream_t 
     return cudaErrorInvalidValue;
 }
 
+// Component c of one particle's kernel at x: d rho / dx_c for c < 3, rho for
+// c = 3 (density_kernel, src/dynamic.jl:124-135): y = L(v)(x - z), q = y.y,
+// rho = Q rho0(q) and grad rho = L(v)(2 Q rho0'(q) y), L being symmetric, with
+// rho0(q) = l^-3 (3465/512) (1 - q/l^2)^4 / pi inside the support.
+__device__ __forceinline__ double kernel_component(const TransferParticle& p, double x0, double x1, double x2, int c) {
+    const double r0 = x0 - p.z[0], r1 = x1 - p.z[1], r2 = x2 - p.z[2];
+    const double f = p.g * (p.v[0] * r0 + p.v[1] * r1 + p.v[2] * r2);
+    const double y0 = r0 + f * p.v[0], y1 = r1 + f * p.v[1], y2 = r2 + f * p.v[2];
+    const double q = y0 * y0 + y1 * y1 + y2 * y2;
+    const double l2 = p.ell * p.ell;
+    if (!(q < l2)) return 0.0;
+    const double u = 1.0 - q / l2;
+    const double c0 = p.charge * (3465.0 / 512.0) / (l2 * p.ell) / 3.141592653589793238462643383279502884;
+    const double u3 = (u * u) * u;
+    if (c == 3) return c0 * (u3 * u);
+    const double s = -8.0 * c0 * u3 / l2;            // 2 rho0'(q)
+    const double w0 = s * y0, w1 = s * y1, w2 = s * y2;
+    const double h = p.g * (p.v[0] * w0 + p.v[1] * w1 + p.v[2] * w2);
+    // select, not an index: the values stay in registers
+    const double wc = c == 0 ? w0 : (c == 1 ? w1 : w2);
+    const double vc = c == 0 ? p.v[0] : (c == 1 ? p.v[1] : p.v[2]);
+    return wc + h * vc;
+}
+
+// The kernel's moments over one chunk of a support element's compact lines,
+// component blockIdx.y: per line r_i = sum_p w_p K_c(x_p) phi_i(x_p,last),
+// then node (K_0, K_1, K_2) gets w_line phi_K0(x_0) phi_K1(x_1) r_K2, as the
+// nested rule's projection kernel regroups them; the groups' sums in group
+// order go to partials[chunk][c].
+template <int P1>
+__global__ void __launch_bounds__(kLineThreads) pairing_lines_kernel(const PairingLaunch a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int M = P1 * P1 * P1;
+    constexpr int MO = P1 * P1;
+    constexpr int NPL = (M + kGroup - 1) / kGroup;
+    constexpr int NOUT = 2 * P1;
+    const int tid = threadIdx.x;
+    const int group = tid / kGroup, lane = tid % kGroup, ngroups = blockDim.x / kGroup;
+    const unsigned mask = 0xffu << ((tid % 32) / kGroup * kGroup);
+    const int comp = blockIdx.y;
+    const NearChunk ch = a.chunks[blockIdx.x];
+    const PairElement el = a.elems[ch.elem];
+    const TransferParticle pt = a.particles[el.particle];
+    const double sum0 = el.lo[0] + el.hi[0], sum1 = el.lo[1] + el.hi[1], sum2 = el.lo[2] + el.hi[2];
+    const double inv0 = 1.0 / (el.hi[0] - el.lo[0]), inv1 = 1.0 / (el.hi[1] - el.lo[1]);
+    const double inv2 = 1.0 / (el.hi[2] - el.lo[2]);
+    double nodes[P1], bary[P1];
+#pragma unroll
+    for (int i = 0; i < P1; ++i) {
+        nodes[i] = a.gll[i];
+        bary[i] = a.bary[i];
+    }
+    double acc[NPL];
+#pragma unroll
+    for (int k = 0; k < NPL; ++k) acc[k] = 0.0;
+    for (int l = ch.l0 + group; l < ch.l1; l += ngroups) {
+        const NearLine L = a.lines[l];
+        const double pre0 = a.line_vals[3 * (int64_t)l], pre1 = a.line_vals[3 * (int64_t)l + 1];
+        const double wl = a.line_vals[3 * (int64_t)l + 2];
+        double r[P1];
+#pragma unroll
+        for (int i = 0; i < P1; ++i) r[i] = 0.0;
+        for (int p = L.p0 + lane; p < L.p1; p += kGroup) {
+            const double x = a.lx[p];
+            double phi[P1];
+            lagrange_all<double, P1>(nodes, bary, (2.0 * x - sum2) * inv2, phi);
+            const double c = a.lw[p] * kernel_component(pt, pre0, pre1, x, comp);
+#pragma unroll
+            for (int i = 0; i < P1; ++i) r[i] += c * phi[i];
+        }
+#pragma unroll
+        for (int off = kGroup / 2; off > 0; off /= 2)
+#pragma unroll
+            for (int i = 0; i < P1; ++i) r[i] += shfl8_xor(mask, r[i], off);
+        // the two outer dimensions' Lagrange values, value j = d (P+1) + i on
+        // lane j % kGroup
+        double ov[(NOUT + kGroup - 1) / kGroup + 1];
+#pragma unroll
+        for (int s = 0; s * kGroup < NOUT; ++s) {
+            const int j = s * kGroup + lane;
+            double v = 0.0;
+            if (j < NOUT) {
+                const int d = j / P1, i = j % P1;
+                const double xi = d == 0 ? (2.0 * pre0 - sum0) * inv0 : (2.0 * pre1 - sum1) * inv1;
+                v = lagrange_one<double, P1>(nodes, bary, xi, i);
+            }
+            ov[s] = v;
+        }
+#pragma unroll
+        for (int k = 0; k < NPL; ++k) {
+            const int m = lane + kGroup * k;
+            const int mm = m < M ? m : 0;
+            const int Klast = mm / MO;
+            int o = mm % MO;
+            double outer = wl;
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                const int j = d * P1 + o % P1;
+                o /= P1;
+                double got = 0.0;
+#pragma unroll
+                for (int s = 0; s * kGroup < NOUT; ++s) {
+                    const double t = shfl8(mask, ov[s], j % kGroup);
+                    if (j / kGroup == s) got = t;
+                }
+                outer *= got;
+            }
+            double rk = 0.0;
+#pragma unroll
+            for (int i = 0; i < P1; ++i)
+                if (i == Klast) rk = r[i];
+            if (m < M) acc[k] += outer * rk;
+        }
+    }
+    double* red = reinterpret_cast<double*>(smem_raw);   // ngroups x M
+#pragma unroll
+    for (int k = 0; k < NPL; ++k) {
+        const int m = lane + kGroup * k;
+        if (m < M) red[group * M + m] = acc[k];
+    }
+    __syncthreads();
+    double* out = a.partials + ((int64_t)blockIdx.x * kPairComponents + comp) * M;
+    for (int m = tid; m < M; m += blockDim.x) {
+        double s = 0.0;
+        for (int g = 0; g < ngroups; ++g) s += red[g * M + m];
+        out[m] = s;
+    }
+}
+
+// Each support element's moments: its chunks' sums added in order.
+template <int P1>
+__global__ void pairing_moments_kernel(const PairingLaunch a) {
+    constexpr int CM = kPairComponents * P1 * P1 * P1;
+    const PairElement el = a.elems[blockIdx.x];
+    for (int j = threadIdx.x; j < CM; j += blockDim.x) {
+        double s = 0.0;
+        for (int c = el.c0; c < el.c1; ++c) s += a.partials[(int64_t)c * CM + j];
+        a.moments[(int64_t)blockIdx.x * CM + j] = s;
+    }
+}
+
+constexpr int kDotThreads = 256;
+
+// One CTA per particle: over its support elements' nodes, the node's value
+// (the mean over the values the gather lists, the element's own first) times
+// the node's moments, summed per thread and then over the threads in a fixed
+// tree, so that a pairing is the same to the bit on every call.
+template <typename T, int P1>
+__global__ void __launch_bounds__(kDotThreads) pairing_dot_kernel(const PairingLaunch a) {
+    constexpr int M = P1 * P1 * P1;
+    __shared__ double red[kPairComponents][kDotThreads];
+    const int k = blockIdx.x, tid = threadIdx.x;
+    const int64_t e0 = a.first[k], e1 = a.first[k + 1];
+    const T* u = static_cast<const T*>(a.u);
+    const int64_t vb = (int64_t)(a.var - 1) * a.NN;
+    double acc[kPairComponents] = {0.0, 0.0, 0.0, 0.0};
+    for (int64_t j = tid; j < (e1 - e0) * M; j += kDotThreads) {
+        const int64_t e = e0 + j / M;
+        const int m = (int)(j % M);
+        const int64_t* gi = a.gather + (e * M + m) * kGather;
+        double g = 0.0;
+        int n = 0;
+        for (int i = 0; i < kGather; ++i) {
+            const int64_t o = gi[i];
+            if (o < 0) break;
+            g += (double)u[o + vb];
+            ++n;
+        }
+        g /= (double)(n > 0 ? n : 1);
+        const double* mu = a.moments + e * kPairComponents * M + m;
+#pragma unroll
+        for (int c = 0; c < kPairComponents; ++c) acc[c] += g * mu[c * M];
+    }
+#pragma unroll
+    for (int c = 0; c < kPairComponents; ++c) red[c][tid] = acc[c];
+    __syncthreads();
+    for (int s = kDotThreads / 2; s > 0; s /= 2) {
+        if (tid < s)
+#pragma unroll
+            for (int c = 0; c < kPairComponents; ++c) red[c][tid] += red[c][tid + s];
+        __syncthreads();
+    }
+    if (tid < kPairComponents) a.out[k * kPairComponents + tid] = red[tid][0];
+}
+
+template <int P1>
+cudaError_t pairing_moments(const PairingLaunch& a, cudaStream_t s) {
+    constexpr int M = P1 * P1 * P1;
+    cudaError_t e;
+    if (a.n_chunks > 0) {
+        const size_t smem = (size_t)(kLineThreads / kGroup) * M * sizeof(double);
+        e = cudaFuncSetAttribute(pairing_lines_kernel<P1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        pairing_lines_kernel<P1><<<dim3((unsigned)a.n_chunks, kPairComponents), kLineThreads, smem, s>>>(a);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (a.n_elems > 0) {
+        pairing_moments_kernel<P1><<<(unsigned)a.n_elems, 256, 0, s>>>(a);
+        return cudaGetLastError();
+    }
+    return cudaSuccess;
+}
+
+template <typename T, int P1>
+cudaError_t pairing_dot(const PairingLaunch& a, cudaStream_t s) {
+    if (a.nparticles <= 0) return cudaSuccess;
+    pairing_dot_kernel<T, P1><<<(unsigned)a.nparticles, kDotThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t pairing_dot_p(const PairingLaunch& a, cudaStream_t s) {
+    switch (a.P + 1) {
+        case 2: return pairing_dot<T, 2>(a, s);
+        case 3: return pairing_dot<T, 3>(a, s);
+        case 4: return pairing_dot<T, 4>(a, s);
+        case 5: return pairing_dot<T, 5>(a, s);
+        case 6: return pairing_dot<T, 6>(a, s);
+        case 7: return pairing_dot<T, 7>(a, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
 }  // namespace
+
+cudaError_t launch_pairing_moments(const PairingLaunch& a, cudaStream_t stream) {
+    switch (a.P + 1) {
+        case 2: return pairing_moments<2>(a, stream);
+        case 3: return pairing_moments<3>(a, stream);
+        case 4: return pairing_moments<4>(a, stream);
+        case 5: return pairing_moments<5>(a, stream);
+        case 6: return pairing_moments<6>(a, stream);
+        case 7: return pairing_moments<7>(a, stream);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_pairing_dot(const PairingLaunch& a, cudaStream_t stream) {
+    return a.prec == 0 ? pairing_dot_p<double>(a, stream) : pairing_dot_p<float>(a, stream);
+}
 
 cudaError_t launch_projection(const TransferLaunch& a, cudaStream_t stream) {
     return a.prec == 0 ? projection_d<double>(a, stream) : projection_d<float>(a, stream);

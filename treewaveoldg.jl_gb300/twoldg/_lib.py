@@ -24,7 +24,7 @@ EXPORTS = [
     "twoldg_transfer_plan_create", "twoldg_transfer_plan_update", "twoldg_transfer_plan_destroy",
     "twoldg_transfer_plan_counts",
     "twoldg_transfer_points", "twoldg_project_values", "twoldg_project_density", "twoldg_transfer_table",
-    "twoldg_average_shared",
+    "twoldg_average_shared", "twoldg_pairing", "twoldg_support_elements",
 ]
 
 
@@ -124,6 +124,8 @@ def lib():
             "twoldg_project_values": (ctypes.c_int, [vp, vp, vp, d, i32]),
             "twoldg_project_density": (ctypes.c_int, [vp, vp, d, i32]),
             "twoldg_average_shared": (ctypes.c_int, [vp, vp, i32]),
+            "twoldg_pairing": (ctypes.c_int, [vp, vp, i32, i32, vp]),
+            "twoldg_support_elements": (ctypes.c_int, [vp, i32, vp, vp]),
             "twoldg_transfer_table": (ctypes.c_int, [i32, i32, ctypes.c_char_p, i32, vp]),
         }
         for name, (res, args) in sig.items():

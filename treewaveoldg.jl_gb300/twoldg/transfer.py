@@ -244,6 +244,43 @@ class TransferPlan:
         self.p.synchronize()
         return u
 
+    def pairing(self, u, var=1, continuous=False):
+        """pairing(p, t, u, K, s; var, continuous) (src/transfer.jl:1779-1797)
+        of every particle's density kernel K = (grad rho, rho) (density_kernel,
+        src/dynamic.jl:124-135) with variable var of the state u, as a
+        (nparticles, 4) float64 array: row k is int (grad rho_k) g_h, then
+        int rho_k g_h, over the elements that meet particle k's support. With
+        continuous=True g_h is first averaged over the elements that share each
+        node (continuous_values, :1449-1500)."""
+        _check_state(self.p, u)
+        out = np.zeros((len(self.particles), 4), dtype=np.float64)
+        _sync_torch()
+        _lib.check(_lib.lib().twoldg_pairing(self._h, _dptr(u), int(var), 1 if continuous else 0,
+                                             out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def support_elements(self, k=0):
+        """support_elements(p, s) (src/transfer.jl:1726-1758) of particle k:
+        the (block, (e0, e1, e2)) pairs that hold a corner of its support's box,
+        block and element indices from 0."""
+        out = np.zeros((8, 4), dtype=np.int32)
+        n = ctypes.c_int32()
+        _lib.check(_lib.lib().twoldg_support_elements(self._h, int(k), out.ctypes.data_as(ctypes.c_void_p),
+                                                      ctypes.byref(n)))
+        return [(int(r[0]), (int(r[1]), int(r[2]), int(r[3]))) for r in out[:n.value]]
+
+
+def particle_forces(plan, u, continuous=True):
+    """The grid's part of each particle's force, particle_forces
+    (src/inspiral.jl:474-504): F_k = int (grad rho_k) Phi - v_k int rho_k Pi,
+    Phi and Pi variables 1 and 2 of the field state u, read through the
+    pairing (continuous by default, as the averaging writes the source).
+    Returns (nparticles, 3) float64."""
+    phi = plan.pairing(u, var=1, continuous=continuous)
+    pi = plan.pairing(u, var=2, continuous=continuous)
+    v = np.array([s.v for s in plan.particles], dtype=np.float64).reshape(len(plan.particles), -1)
+    return phi[:, :3] - v[:, :3] * pi[:, 3:4]
+
 
 def source_rhs(du, u, p, plan, S, t=0.0, factor=-1.0, average=True):
     """The field part of the reference's inspiral_rhs! (src/inspiral.jl):
