@@ -475,9 +475,9 @@ struct twoldg_transfer_plan {
     DevVec d_pgather, d_pgather_c, d_pbary, d_pgll, d_pout;
     PairingLaunch PL;
 
-    ~twoldg_transfer_plan() {
-        if (stream) cudaStreamSynchronize(stream);
-    }
+    // The stream is the problem's, which may be destroyed first (a garbage
+    // collector finalises in any order): wait for the device instead.
+    ~twoldg_transfer_plan() { cudaDeviceSynchronize(); }
     int set_particles(const twoldg_particle* tp, int n);
     int build_pairing();
     // the frame's block that holds x (lo <= x < hi), or -1
@@ -883,6 +883,14 @@ int twoldg_transfer_plan::build_pairing() {
         return o;
     };
     std::vector<int64_t> gplain((size_t)ne * M * kGather, -1), gcont((size_t)ne * M * kGather, -1);
+    for (int64_t i = 0; i < ne; ++i) {
+        const int e[3] = {list[4 * i + 1], list[4 * i + 2], list[4 * i + 3]};
+        for (int m = 0; m < M; ++m) {
+            const int K[3] = {m % P1, (m / P1) % P1, m / (P1 * P1)};
+            gplain[((size_t)i * M + m) * kGather] = offset(list[4 * i], e, K);
+        }
+    }
+    // the continuous one stops at the first refusal, which it keeps
     pair_cont_error.clear();
     for (int64_t i = 0; i < ne && pair_cont_error.empty(); ++i) {
         const int64_t b = list[4 * i];
@@ -892,7 +900,6 @@ int twoldg_transfer_plan::build_pairing() {
         for (int m = 0; m < M && pair_cont_error.empty(); ++m) {
             const int K[3] = {m % P1, (m / P1) % P1, m / (P1 * P1)};
             int64_t* gc = &gcont[((size_t)i * M + m) * kGather];
-            gplain[((size_t)i * M + m) * kGather] = offset(b, e, K);
             int n = 0;
             gc[n++] = offset(b, e, K);
             int dirs[3], freed[3], nfree = 0;
