@@ -410,6 +410,14 @@ def test_projection_in_the_ball_cube_keeps_the_charge(native):
 # (grad rho, rho) with a field, on the device against the oracle's nested
 # rule. The gradient's integrand is of size Q/ell, the density's of size Q:
 # each component is held to 1e-12 of its own scale times max |g|.
+def _grad_tolerance(Q, ell, z):
+    # The gradient's integrand is of size Q/ell and cancels to Q |grad g|.
+    # Each point's position is rounded to eps |z| in absolute coordinates,
+    # eps |z| / ell of the support, which the integrand's slope Q/ell^2 turns
+    # into an error of that order: 1e-12 Q/ell, and ten times eps |z| Q/ell^2.
+    return 1e-12 * Q / ell + 10 * np.finfo(np.float64).eps * float(np.linalg.norm(z)) * Q / ell ** 2
+
+
 def _pair_scale(s, Q):
     return np.array([Q / s.ell] * 3 + [Q])
 
@@ -468,7 +476,7 @@ def test_pairing_integrates_the_particle_at_any_size(native, ratio, moving):
     got = plan.pairing(torch.from_numpy(g.copy()).cuda(), var=1)[0]
     assert got[3] == pytest.approx(exact_moment(poly, Q, ell, z, v), rel=1e-12)
     for d in range(3):
-        assert abs(got[d] + exact_moment(lambda X: grad_poly(X)[:, d], Q, ell, z, v)) <= 1e-12 * Q / ell
+        assert abs(got[d] + exact_moment(lambda X: grad_poly(X)[:, d], Q, ell, z, v)) <= _grad_tolerance(Q, ell, z)
 
 
 def test_pairing_is_the_density_projection_folded(native):
@@ -571,7 +579,7 @@ def test_pairing_repeats_and_follows_the_particles(native):
     ball = ((0.5, 0.5, 0.5), 0.6)
     a = [ParticleSupport((0.41, 0.52, 0.47), (0.1, 0.0, 0.0), 0.02, charge=0.5),
          ParticleSupport((0.7, 0.33, 0.61), (0.0, -0.2, 0.05), 0.015, charge=-0.5)]
-    b = [ParticleSupport((0.5, 0.51, 0.49), (0.1, 0.02, 0.0), 0.02, charge=0.5),
+    b = [ParticleSupport((0.5, 0.56, 0.44), (0.1, 0.02, 0.0), 0.02, charge=0.5),
          ParticleSupport((0.69, 0.375, 0.6), (0.0, -0.2, 0.05), 0.015, charge=-0.5)]
     u = torch.from_numpy(irregular(p.state_words)).cuda()
     plan = TransferPlan(p, a, ball)
