@@ -523,6 +523,18 @@ def transfer_benchmark(args, twoldg, torch, record=True):
             if it >= args.warmup:
                 times[kind].append(ev0.elapsed_time(ev1))
     ms = {k: float(np.median(v)) for k, v in times.items()}
+    # the pairing of each particle's (grad rho, rho) with a field (the
+    # inspiral's force), host-visible latency: the first after the particles
+    # move builds the supports' compact rule and the kernel's moments, every
+    # later one gathers, sums and copies 8 numbers back
+    t0 = time.perf_counter()
+    plan.pairing(du, 1, True)
+    pair_first = time.perf_counter() - t0
+    pair = []
+    for _ in range(20):
+        t0 = time.perf_counter()
+        plan.pairing(du, 1, True)
+        pair.append(time.perf_counter() - t0)
     # algorithmic bytes of the values path: each point's value read once, the
     # touched elements' nodes read and written, the nested rule's points and
     # weights read
@@ -538,7 +550,8 @@ def transfer_benchmark(args, twoldg, torch, record=True):
            "values_roofline": {"bound": "hbm", "achieved": alg / (ms["values"] / 1e3) / 1e9, "peak": hbm,
                                "unit": "GB/s", "frac": alg / (ms["values"] / 1e3) / 1e9 / hbm,
                                "algorithmic_bytes": alg, "peak_kind": peak_kind},
-           "gpu_launches_per_projection": 3}
+           "gpu_launches_per_projection": 3,
+           "pairing_ms": {"first_after_update": pair_first * 1e3, "steady": float(np.median(pair)) * 1e3}}
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = transfer_cpu_sample(p, parts, ball, plan)
     plan.close()

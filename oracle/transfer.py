@@ -6,8 +6,10 @@ A numpy restatement of the reference's projection of a source onto the nodes
 (src/transfer.jl): the far and graded tensor Gauss rules (:462-491, :520-680),
 the nested rule split at a particle's support with Gauss points inside and
 Johnston and Elliott's sinh rule outside (:233-455), the classification of
-elements (:493-503, :1380-1415), the reconstruction (:1990-2009) and the ball
-rule (:2032-2048). Tables come from tests/golden/transfer_tables.json and
+elements (:493-503, :1380-1415), the reconstruction (:1990-2009), the ball
+rule (:2032-2048), the averaging over shared nodes (:1616-1714), and the
+pairing with its support elements and continuous values (:1449-1500,
+:1726-1797) for the density kernel (src/dynamic.jl:124-135). Tables come from tests/golden/transfer_tables.json and
 element_tables.json (mpmath at 512 bits, rounded once), never from the library
 under test. Sums run over flattened point lists where the reference nests
 them, which moves results by rounding only.

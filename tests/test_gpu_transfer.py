@@ -593,6 +593,10 @@ def test_pairing_repeats_and_follows_the_particles(native):
     phi, pi = plan.pairing(u, 1, True), plan.pairing(u, 2, True)
     v = np.array([s.v for s in b])
     assert np.array_equal(F, phi[:, :3] - v * pi[:, 3:4])
+    # source_pairing: the pairing of the density's own projection, averaged
+    du = p.statevector()
+    plan.project(du, "density", factor=1.0, var=1)
+    assert np.array_equal(twoldg.source_pairing(plan, "density"), plan.pairing(du, 1, True))
 
 
 def test_pairing_in_the_ball_cube(native):

@@ -270,6 +270,18 @@ class TransferPlan:
         return [(int(r[0]), (int(r[1]), int(r[2]), int(r[3]))) for r in out[:n.value]]
 
 
+def source_pairing(plan, S, continuous=True):
+    """source_pairing(p, t, S, K, s; continuous) (src/transfer.jl:1799-1825)
+    for the plan's particles' kernels (grad rho, rho): <K, A P S> without a
+    field, as the pairing of S's projection (S as TransferPlan.project takes
+    it), averaged over shared nodes with continuous=True. The plan's ball must
+    hold the supports' elements and every element sharing a node with them,
+    where the reference projects. Returns (nparticles, 4) float64."""
+    du = plan.p.statevector()
+    plan.project(du, S, factor=1.0, var=1)
+    return plan.pairing(du, var=1, continuous=continuous)
+
+
 def particle_forces(plan, u, continuous=True):
     """The grid's part of each particle's force, particle_forces
     (src/inspiral.jl:474-504): F_k = int (grad rho_k) Phi - v_k int rho_k Pi,
