@@ -475,9 +475,23 @@ struct twoldg_transfer_plan {
     DevVec d_pgather, d_pgather_c, d_pbary, d_pgll, d_pout;
     PairingLaunch PL;
 
+    // The projection's three parts run at once: the far rule on the problem's
+    // stream, the graded bands on side[0], the nested rule on side[1] (of the
+    // highest priority: its chain is the longest), forked from and joined
+    // back into the problem's stream by events.
+    cudaStream_t side[2] = {nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
+
     // The stream is the problem's, which may be destroyed first (a garbage
     // collector finalises in any order): wait for the device instead.
-    ~twoldg_transfer_plan() { cudaDeviceSynchronize(); }
+    ~twoldg_transfer_plan() {
+        cudaDeviceSynchronize();
+        for (int k = 0; k < 2; ++k) {
+            if (side[k]) cudaStreamDestroy(side[k]);
+            if (join[k]) cudaEventDestroy(join[k]);
+        }
+        if (fork) cudaEventDestroy(fork);
+    }
     int set_particles(const twoldg_particle* tp, int n);
     int build_pairing();
     // the frame's block that holds x (lo <= x < hi), or -1
@@ -1042,6 +1056,14 @@ int twoldg_transfer_plan_create(twoldg_problem* p, const twoldg_transfer_desc* d
     T.prec = prec;
     T.nb = nb;
     T.stream = stream;
+    {
+        int least = 0, greatest = 0;
+        TRY_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest), "transfer streams");
+        TRY_CUDA(cudaStreamCreateWithPriority(&T.side[0], cudaStreamNonBlocking, least), "transfer streams");
+        TRY_CUDA(cudaStreamCreateWithPriority(&T.side[1], cudaStreamNonBlocking, greatest), "transfer streams");
+        TRY_CUDA(cudaEventCreateWithFlags(&T.fork, cudaEventDisableTiming), "transfer events");
+        for (int k = 0; k < 2; ++k) TRY_CUDA(cudaEventCreateWithFlags(&T.join[k], cudaEventDisableTiming), "transfer events");
+    }
     // the quadrature, with the reference's defaults (src/transfer.jl:139-170)
     const int q = d->q > 0 ? d->q : P + 3;
     const int nsinh = d->nsinh > 0 ? d->nsinh : 48, nmid = d->nmid > 0 ? d->nmid : 16;
@@ -1250,7 +1272,15 @@ static int project(twoldg_transfer_plan* plan, int source, const void* values, v
     L.du = du;
     L.var = var;
     L.factor = factor;
-    cudaError_t e = launch_projection(L, plan->stream);
+    TRY_CUDA(cudaEventRecord(plan->fork, plan->stream), "projection fork");
+    for (int k = 0; k < 2; ++k) TRY_CUDA(cudaStreamWaitEvent(plan->side[k], plan->fork, 0), "projection fork");
+    cudaError_t e = launch_projection(L, plan->stream, plan->side[0], plan->side[1]);
+    // the problem's stream waits for both sides, whatever the launches gave
+    for (int k = 0; k < 2; ++k) {
+        const cudaError_t r = cudaEventRecord(plan->join[k], plan->side[k]);
+        const cudaError_t w = r == cudaSuccess ? cudaStreamWaitEvent(plan->stream, plan->join[k], 0) : r;
+        if (e == cudaSuccess) e = w;
+    }
     if (e != cudaSuccess) return fail(TWOLDG_ECUDA, std::string("projection: ") + cudaGetErrorString(e));
     return TWOLDG_OK;
 }

@@ -165,8 +165,10 @@ cudaError_t launch_pairing_moments(const PairingLaunch& a, cudaStream_t stream);
 // The pairings with a.u through a.gather into a.out, on `stream`.
 cudaError_t launch_pairing_dot(const PairingLaunch& a, cudaStream_t stream);
 
-// The projection's kernels on `stream`; returns the launch error, if any.
-cudaError_t launch_projection(const TransferLaunch& a, cudaStream_t stream);
+// The projection's kernels: the far rule on `far`, the graded bands on
+// `bands`, the nested rule on `near` (they write disjoint elements, so the
+// three may run at once); returns the launch error, if any.
+cudaError_t launch_projection(const TransferLaunch& a, cudaStream_t far, cudaStream_t bands, cudaStream_t near);
 
 // Every point of the plan's rules, tensor rules first (element by element,
 // dimension 0 fastest), then the near points, as (D, npoints) in T.

@@ -403,14 +403,14 @@ size_t rule_smem(const TransferLaunch& a) {
     return (2 * cap + (size_t)a.max_q * (D + a.P + 1)) * sizeof(T);
 }
 
-// One launch per rule, its shared memory sized for that rule's q: the far
-// rule's q = P + 3 needs a fraction of the largest graded band's.
+// One launch per rule of [r0, r1), its shared memory sized for that rule's
+// q: the far rule's q = P + 3 needs a fraction of the largest graded band's.
 template <typename T, int D, int SRC>
-cudaError_t run_rules(const TransferLaunch& a, cudaStream_t stream) {
+cudaError_t run_rules(const TransferLaunch& a, int r0, int r1, cudaStream_t stream) {
     cudaError_t e = cudaFuncSetAttribute(tensor_rule_kernel<T, D, SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)rule_smem<T, D>(a));
     if (e != cudaSuccess) return e;
-    for (int r = 0; r < a.nrules; ++r) {
+    for (int r = r0; r < r1; ++r) {
         const int64_t n = a.rule_start[r + 1] - a.rule_start[r];
         if (n <= 0) continue;
         TransferLaunch b = a;
@@ -447,20 +447,26 @@ cudaError_t run_lines_p(const TransferLaunch& a, cudaStream_t stream) {
     return cudaErrorInvalidValue;
 }
 
+// The nested rule first, on its own stream: its chain (lines, then finish)
+// is the longest and its CTAs the fewest; then the graded bands and the far
+// rule. The three write disjoint elements' nodes.
 template <typename T, int D>
-cudaError_t projection(const TransferLaunch& a, cudaStream_t stream) {
+cudaError_t projection(const TransferLaunch& a, cudaStream_t far, cudaStream_t bands, cudaStream_t near) {
     cudaError_t e;
-    if (a.n_rule_elems > 0) {
-        e = a.source == SOURCE_VALUES ? run_rules<T, D, SOURCE_VALUES>(a, stream)
-                                      : run_rules<T, D, SOURCE_DENSITY>(a, stream);
+    if (a.n_chunks > 0) {
+        e = a.source == SOURCE_VALUES ? run_lines_p<T, D, SOURCE_VALUES>(a, near)
+                                      : run_lines_p<T, D, SOURCE_DENSITY>(a, near);
+        if (e != cudaSuccess) return e;
+        near_finish_kernel<T, D><<<(unsigned)a.n_near_elems, kFinishThreads, kFinishThreads * sizeof(T), near>>>(a);
+        e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    if (a.n_chunks > 0) {
-        e = a.source == SOURCE_VALUES ? run_lines_p<T, D, SOURCE_VALUES>(a, stream)
-                                      : run_lines_p<T, D, SOURCE_DENSITY>(a, stream);
+    if (a.n_rule_elems > 0) {
+        e = a.source == SOURCE_VALUES ? run_rules<T, D, SOURCE_VALUES>(a, 1, a.nrules, bands)
+                                      : run_rules<T, D, SOURCE_DENSITY>(a, 1, a.nrules, bands);
         if (e != cudaSuccess) return e;
-        near_finish_kernel<T, D><<<(unsigned)a.n_near_elems, kFinishThreads, kFinishThreads * sizeof(T), stream>>>(a);
-        e = cudaGetLastError();
+        e = a.source == SOURCE_VALUES ? run_rules<T, D, SOURCE_VALUES>(a, 0, 1, far)
+                                      : run_rules<T, D, SOURCE_DENSITY>(a, 0, 1, far);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -545,11 +551,11 @@ cudaError_t average(const AverageLaunch& a, cudaStream_t s) {
 }
 
 template <typename T>
-cudaError_t projection_d(const TransferLaunch& a, cudaStream_t s) {
+cudaError_t projection_d(const TransferLaunch& a, cudaStream_t far, cudaStream_t bands, cudaStream_t near) {
     switch (a.D) {
-        case 1: return projection<T, 1>(a, s);
-        case 2: return projection<T, 2>(a, s);
-        case 3: return projection<T, 3>(a, s);
+        case 1: return projection<T, 1>(a, far, bands, near);
+        case 2: return projection<T, 2>(a, far, bands, near);
+        case 3: return projection<T, 3>(a, far, bands, near);
     }
     return cudaErrorInvalidValue;
 }
@@ -806,8 +812,8 @@ cudaError_t launch_pairing_dot(const PairingLaunch& a, cudaStream_t stream) {
     return a.prec == 0 ? pairing_dot_p<double>(a, stream) : pairing_dot_p<float>(a, stream);
 }
 
-cudaError_t launch_projection(const TransferLaunch& a, cudaStream_t stream) {
-    return a.prec == 0 ? projection_d<double>(a, stream) : projection_d<float>(a, stream);
+cudaError_t launch_projection(const TransferLaunch& a, cudaStream_t far, cudaStream_t bands, cudaStream_t near) {
+    return a.prec == 0 ? projection_d<double>(a, far, bands, near) : projection_d<float>(a, far, bands, near);
 }
 
 cudaError_t launch_points(const TransferLaunch& a, void* xs, int64_t npoints, cudaStream_t stream) {
