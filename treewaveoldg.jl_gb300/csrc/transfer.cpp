@@ -24,6 +24,7 @@
 #include <string>
 #include <thread>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/twoldg.h"
@@ -167,14 +168,18 @@ template <typename Fn>
 void line_fold(const Support& s, const NestedTables& t, const double* lo, const double* hi,
                const std::vector<double>& prefix, bool innermost, bool compact, Fn&& seg) {
     const int D = s.D, F = (int)prefix.size(), d = F;
-    std::vector<double> breaks;
+    // scratch per thread and per level of the recursion (an outer line's
+    // points are still being visited while its inner lines are folded)
+    thread_local std::vector<double> scratch[3][3];
+    std::vector<double>& breaks = scratch[F][0];
+    std::vector<double>& xs = scratch[F][1];
+    std::vector<double>& ws = scratch[F][2];
     bool has_extent;
     double extent[2] = {0, 0};
     support_breaks(s, prefix.data(), F, lo, hi, breaks, has_extent, extent);
     double off2 = box_distance2(s.z, lo, hi, d + 1, D);
     for (int j = 0; j < F; ++j) off2 += (prefix[j] - s.z[j]) * (prefix[j] - s.z[j]);
     double a = lo[d];
-    std::vector<double> xs, ws;
     for (size_t k = 0; k <= breaks.size(); ++k) {
         const double b = k < breaks.size() ? breaks[k] : hi[d];
         if (b > a) {
@@ -205,7 +210,7 @@ void line_fold(const Support& s, const NestedTables& t, const double* lo, const 
 // emitted, its fixed coordinates (padded to two), the product w of the outer
 // lines' weights, and its segments' points and weights in order.
 struct NearLines {
-    std::vector<double> lx, lw, vals;   // per point; per line: prefix[2], w
+    std::vector<double> lx, lw, vals;   // per point (in a line's own, not once laid out); per line: prefix[2], w
     std::vector<int32_t> range;         // per line: p0, p1
     std::vector<int32_t> inner;         // per line: the points inside the support's section
 };
@@ -256,15 +261,34 @@ struct LineBox {
     int particle;
 };
 
-// The nested rule's innermost lines over the boxes on up to 16 host threads,
-// threaded as the reference threads its near pass (src/transfer.jl:1160-1213):
-// over the points of each box's outermost line (the box's own line in one
-// dimension), each item the lines through one point, kept in the serial
-// order. The particle's own element holds the most points, and threading over
-// elements left it on one thread. first[i] is box i's first line, first[n]
-// the number of lines. False if the points exceed what an int32 indexes.
-bool nested_lines(const std::vector<Support>& parts, const NestedTables& nt, int D, const std::vector<LineBox>& boxes,
-                  bool compact, NearLines& nl, std::vector<int64_t>& first) {
+// fn(i) for i in [0, n) on up to 16 host threads, taken in turn.
+template <typename Fn>
+void parallel_for(size_t n, Fn&& fn) {
+    std::atomic<size_t> next(0);
+    auto work = [&]() {
+        for (size_t i = next++; i < n; i = next++) fn(i);
+    };
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const unsigned nt = (unsigned)std::min<size_t>(hw, n);
+    std::vector<std::thread> pool;
+    for (unsigned k = 1; k < nt; ++k) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+}
+
+// The nested rule's innermost lines over the boxes, threaded as the reference
+// threads its near pass (src/transfer.jl:1160-1213): over the points of each
+// box's outermost line (the box's own line in one dimension), each item the
+// lines through one point, kept in the serial order. The particle's own
+// element holds the most points, and threading over elements left it on one
+// thread. Then the layout, threaded too: each item's points at its offset in
+// xs and ws (npoints each, of the field type T, which dst(npoints, xs, ws)
+// provides), its lines' per-line values, ranges and inner ranges in nl.
+// first[i] is box i's first line, first[n] the number of lines. Returns 0,
+// 1 if the points exceed what an int32 indexes, 2 if dst failed.
+template <typename T, typename Dst>
+int nested_lines(const std::vector<Support>& parts, const NestedTables& nt, int D, const std::vector<LineBox>& boxes,
+                 bool compact, NearLines& nl, std::vector<int64_t>& first, Dst&& dst) {
     struct Item {
         int box;
         double x, w;
@@ -281,59 +305,75 @@ bool nested_lines(const std::vector<Support>& parts, const NestedTables& nt, int
                   });
     }
     std::vector<NearLines> per(items.size());
-    {
-        std::atomic<size_t> next(0);
-        auto work = [&]() {
-            for (size_t n = next++; n < items.size(); n = next++) {
-                const Item& it = items[n];
-                const LineBox& bx = boxes[it.box];
-                std::vector<double> prefix;
-                if (D == 1) {
-                    collect_lines(parts[bx.particle], nt, bx.lo, bx.hi, prefix, 1.0, 1, compact, per[n]);
-                } else {
-                    prefix.push_back(it.x);
-                    collect_lines(parts[bx.particle], nt, bx.lo, bx.hi, prefix, it.w, D - 1, compact, per[n]);
-                }
-            }
-        };
-        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-        const unsigned nt_ = (unsigned)std::min<size_t>(hw, items.size());
-        std::vector<std::thread> pool;
-        for (unsigned k = 1; k < nt_; ++k) pool.emplace_back(work);
-        work();
-        for (auto& t : pool) t.join();
-    }
-    first.assign(boxes.size() + 1, 0);
-    size_t nlx = 0, nlines = 0;
-    for (const NearLines& x : per) {
-        nlx += x.lw.size();
-        nlines += x.range.size() / 2;
-    }
-    nl = NearLines();
-    nl.lx.reserve(nlx);
-    nl.lw.reserve(nlx);
-    nl.vals.reserve(3 * nlines);
-    nl.range.reserve(2 * nlines);
-    nl.inner.reserve(2 * nlines);
+    parallel_for(items.size(), [&](size_t n) {
+        const Item& it = items[n];
+        const LineBox& bx = boxes[it.box];
+        std::vector<double> prefix;
+        if (D == 1) {
+            collect_lines(parts[bx.particle], nt, bx.lo, bx.hi, prefix, 1.0, 1, compact, per[n]);
+        } else {
+            prefix.push_back(it.x);
+            collect_lines(parts[bx.particle], nt, bx.lo, bx.hi, prefix, it.w, D - 1, compact, per[n]);
+        }
+    });
+    std::vector<int64_t> poff(per.size() + 1, 0), loff(per.size() + 1, 0);
     for (size_t n = 0; n < per.size(); ++n) {
+        poff[n + 1] = poff[n] + (int64_t)per[n].lw.size();
+        loff[n + 1] = loff[n] + (int64_t)per[n].range.size() / 2;
+    }
+    if (poff.back() > std::numeric_limits<int32_t>::max() / 2) return 1;
+    first.assign(boxes.size() + 1, 0);
+    for (size_t n = 0; n < per.size(); ++n) first[items[n].box + 1] = loff[n + 1];
+    for (size_t i = 0; i < boxes.size(); ++i) first[i + 1] = std::max(first[i + 1], first[i]);
+    T* xs = nullptr;
+    T* ws = nullptr;
+    if (!dst(poff.back(), xs, ws)) return 2;
+    const int64_t nlines = loff.back();
+    nl.vals.resize(3 * nlines);
+    nl.range.resize(2 * nlines);
+    nl.inner.resize(2 * nlines);
+    parallel_for(per.size(), [&](size_t n) {
         NearLines& x = per[n];
-        const int32_t off = (int32_t)nl.lw.size();
-        if (nl.lw.size() + x.lw.size() > (size_t)std::numeric_limits<int32_t>::max() / 2) return false;
-        nl.lx.insert(nl.lx.end(), x.lx.begin(), x.lx.end());
-        nl.lw.insert(nl.lw.end(), x.lw.begin(), x.lw.end());
-        nl.vals.insert(nl.vals.end(), x.vals.begin(), x.vals.end());
-        for (int32_t v : x.range) nl.range.push_back(v + off);
+        const int64_t p0 = poff[n], l0 = loff[n];
+        const int32_t off = (int32_t)p0;
+        for (size_t k = 0; k < x.lw.size(); ++k) {
+            xs[p0 + k] = (T)x.lx[k];
+            ws[p0 + k] = (T)x.lw[k];
+        }
+        std::copy(x.vals.begin(), x.vals.end(), nl.vals.begin() + 3 * l0);
+        for (size_t k = 0; k < x.range.size(); ++k) nl.range[2 * l0 + k] = x.range[k] + off;
         for (size_t k = 0; k < x.inner.size(); k += 2) {
             const bool any = x.inner[k + 1] > x.inner[k];
-            nl.inner.push_back(any ? x.inner[k] + off : 0);
-            nl.inner.push_back(any ? x.inner[k + 1] + off : 0);
+            nl.inner[2 * l0 + k] = any ? x.inner[k] + off : 0;
+            nl.inner[2 * l0 + k + 1] = any ? x.inner[k + 1] + off : 0;
         }
-        first[items[n].box + 1] = (int64_t)nl.range.size() / 2;
         x = NearLines();
-    }
-    for (size_t i = 0; i < boxes.size(); ++i) first[i + 1] = std::max(first[i + 1], first[i]);
-    return true;
+    });
+    return 0;
 }
+
+// A page-locked host buffer that grows and is never shrunk: the plan's
+// points go there and to the device by an asynchronous copy.
+struct PinnedBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    cudaError_t reserve(size_t bytes) {
+        bytes = std::max<size_t>(bytes, 16);
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaHostAlloc(&p, bytes, cudaHostAllocDefault);
+        if (e == cudaSuccess) cap = bytes;
+        return e;
+    }
+};
 
 // At most kNearLines lines a chunk, fewer when the lines are few, so that a
 // small set (the density's lines inside the supports) still spreads over the
@@ -481,6 +521,12 @@ struct twoldg_transfer_plan {
     // back into the problem's stream by events.
     cudaStream_t side[2] = {nullptr, nullptr};
     cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
+    // the nested rule's points staged for the device, two stages in turn,
+    // each with the event after its last copy; the per-line values
+    PinnedBuf stage[2];
+    cudaEvent_t staged[2] = {nullptr, nullptr};
+    int stage_next = 0;
+    NearLines host_lines;
 
     // The stream is the problem's, which may be destroyed first (a garbage
     // collector finalises in any order): wait for the device instead.
@@ -489,6 +535,7 @@ struct twoldg_transfer_plan {
         for (int k = 0; k < 2; ++k) {
             if (side[k]) cudaStreamDestroy(side[k]);
             if (join[k]) cudaEventDestroy(join[k]);
+            if (staged[k]) cudaEventDestroy(staged[k]);
         }
         if (fork) cudaEventDestroy(fork);
     }
@@ -624,10 +671,30 @@ int twoldg_transfer_plan::set_particles(const twoldg_particle* tps, int np) {
         elem_box(near[i].block, near[i].e, boxes[i].lo, boxes[i].hi);
         boxes[i].particle = near[i].particle;
     }
-    NearLines nl;
+    // The points go straight into a page-locked stage in the field type, two
+    // stages taken in turn: the other may still be copying to the device. The
+    // per-line values stay on the host, in buffers the plan keeps.
+    NearLines& nl = host_lines;
     std::vector<int64_t> first;
-    if (!nested_lines(parts, nt, D, boxes, false, nl, first))
-        return fail(TWOLDG_EUNSUP, "the nested rule's points exceed 2^30");
+    const int sb = stage_next;
+    const size_t wsz = prec == 0 ? 8 : 4;
+    int64_t npts = 0;
+    cudaError_t stage_err = cudaSuccess;
+    auto to_stage = [&](int64_t n, auto*& xs, auto*& ws) {
+        stage_err = cudaEventSynchronize(staged[sb]);
+        if (stage_err == cudaSuccess) stage_err = stage[sb].reserve(2 * (size_t)n * wsz);
+        if (stage_err != cudaSuccess) return false;
+        using V = std::remove_pointer_t<std::remove_reference_t<decltype(xs)>>;
+        xs = static_cast<V*>(stage[sb].p);
+        ws = xs + n;
+        npts = n;
+        return true;
+    };
+    const int lrc = prec == 0 ? nested_lines<double>(parts, nt, D, boxes, false, nl, first, to_stage)
+                              : nested_lines<float>(parts, nt, D, boxes, false, nl, first, to_stage);
+    if (lrc == 1) return fail(TWOLDG_EUNSUP, "the nested rule's points exceed 2^30");
+    if (lrc == 2) return fail(TWOLDG_ECUDA, std::string("transfer stage: ") + cudaGetErrorString(stage_err));
+    stage_next ^= 1;
     // tensor rule elements and the values' offsets
     std::vector<RuleElement> relems;
     int64_t base = 0;
@@ -669,9 +736,9 @@ int twoldg_transfer_plan::set_particles(const twoldg_particle* tps, int np) {
     std::vector<NearLine> lines(nl.range.size() / 2);
     for (size_t l = 0; l < lines.size(); ++l) lines[l] = NearLine{nl.range[2 * l], nl.range[2 * l + 1]};
     counts[4] = (int64_t)near.size();
-    counts[5] = (int64_t)nl.lw.size();
+    counts[5] = npts;
     counts[6] = (int64_t)chunks.size();
-    npoints = base + (int64_t)nl.lw.size();
+    npoints = base + npts;
     counts[7] = npoints;
     // The density's elements and lines. Its support |L(v)(x - z)| <= ell lies
     // within |x - z| <= ell; a box farther than that (with a margin of 1e-3
@@ -733,10 +800,16 @@ int twoldg_transfer_plan::set_particles(const twoldg_particle* tps, int np) {
     TRY_CUDA(cudaStreamSynchronize(stream), "transfer plan");
     int M = 1;
     for (int k = 0; k < D; ++k) M *= P1;
-    const size_t wsz = prec == 0 ? 8 : 4;
     TRY_CUDA(d_relems.put(relems), "transfer upload");
-    TRY_CUDA(d_lx.put_field(nl.lx, prec), "transfer upload");
-    TRY_CUDA(d_lw.put_field(nl.lw, prec), "transfer upload");
+    TRY_CUDA(d_lx.reserve((size_t)npts * wsz), "transfer upload");
+    TRY_CUDA(d_lw.reserve((size_t)npts * wsz), "transfer upload");
+    if (npts > 0) {
+        const char* st = static_cast<const char*>(stage[sb].p);
+        TRY_CUDA(cudaMemcpyAsync(d_lx.p, st, (size_t)npts * wsz, cudaMemcpyHostToDevice, stream), "transfer upload");
+        TRY_CUDA(cudaMemcpyAsync(d_lw.p, st + (size_t)npts * wsz, (size_t)npts * wsz, cudaMemcpyHostToDevice, stream),
+                 "transfer upload");
+        TRY_CUDA(cudaEventRecord(staged[sb], stream), "transfer upload");
+    }
     TRY_CUDA(d_vals.put_field(nl.vals, prec), "transfer upload");
     TRY_CUDA(d_lines.put(lines), "transfer upload");
     TRY_CUDA(d_chunks.put(chunks), "transfer upload");
@@ -866,7 +939,14 @@ int twoldg_transfer_plan::build_pairing() {
     const int64_t ne = (int64_t)boxes.size();
     NearLines nl;
     std::vector<int64_t> first;
-    if (!nested_lines(supports, nt, D, boxes, true, nl, first))
+    auto to_vectors = [&](int64_t n, double*& xs, double*& ws) {
+        nl.lx.resize(n);
+        nl.lw.resize(n);
+        xs = nl.lx.data();
+        ws = nl.lw.data();
+        return true;
+    };
+    if (nested_lines<double>(supports, nt, D, boxes, true, nl, first, to_vectors) != 0)
         return fail(TWOLDG_EUNSUP, "the pairing's points exceed 2^30");
     std::vector<NearLine> lines(nl.range.size() / 2);
     for (size_t l = 0; l < lines.size(); ++l) lines[l] = NearLine{nl.range[2 * l], nl.range[2 * l + 1]};
@@ -1062,7 +1142,10 @@ int twoldg_transfer_plan_create(twoldg_problem* p, const twoldg_transfer_desc* d
         TRY_CUDA(cudaStreamCreateWithPriority(&T.side[0], cudaStreamNonBlocking, least), "transfer streams");
         TRY_CUDA(cudaStreamCreateWithPriority(&T.side[1], cudaStreamNonBlocking, greatest), "transfer streams");
         TRY_CUDA(cudaEventCreateWithFlags(&T.fork, cudaEventDisableTiming), "transfer events");
-        for (int k = 0; k < 2; ++k) TRY_CUDA(cudaEventCreateWithFlags(&T.join[k], cudaEventDisableTiming), "transfer events");
+        for (int k = 0; k < 2; ++k) {
+            TRY_CUDA(cudaEventCreateWithFlags(&T.join[k], cudaEventDisableTiming), "transfer events");
+            TRY_CUDA(cudaEventCreateWithFlags(&T.staged[k], cudaEventDisableTiming), "transfer events");
+        }
     }
     // the quadrature, with the reference's defaults (src/transfer.jl:139-170)
     const int q = d->q > 0 ? d->q : P + 3;
