@@ -334,3 +334,22 @@ def test_oracle_continuous_pairing():
     s = T.Support(np.array([0.5, 0.125 - 0.4 * ell, 0.6]), np.zeros(3), ell)
     with pytest.raises(ValueError, match="does not look for periodic images"):
         T.pairing(g, mesh, t, lambda X: np.ones((len(X), 1)), s, continuous=True)
+
+
+def test_transfer_entry_points_refuse_bad_arguments_on_the_host():
+    # the C ABI's argument checks run before any device work
+    import ctypes
+    from twoldg import _lib
+    lib = _lib.lib()
+    out = (ctypes.c_double * 8)()
+    n = ctypes.c_int32()
+    h = ctypes.c_void_p()
+    assert lib.twoldg_pairing(None, None, 1, 0, out) == _lib.TWOLDG_EINVAL
+    assert b"must not be NULL" in lib.twoldg_last_error()
+    assert lib.twoldg_support_elements(None, 0, out, ctypes.byref(n)) == _lib.TWOLDG_EINVAL
+    assert lib.twoldg_transfer_plan_create(None, None, ctypes.byref(h)) == _lib.TWOLDG_EINVAL
+    assert lib.twoldg_project_density(None, None, 1.0, 1) == _lib.TWOLDG_EINVAL
+    assert lib.twoldg_average_shared(None, None, 2) == _lib.TWOLDG_EINVAL
+    assert lib.twoldg_transfer_table(3, 0, b"nodes", 6, out) == _lib.TWOLDG_EINVAL
+    assert b"unknown transfer table" in lib.twoldg_last_error()
+    assert lib.twoldg_transfer_table(0, 0, b"bary", 6, out) == _lib.TWOLDG_EINVAL
