@@ -12,6 +12,12 @@ closure the reference's launch_points! hook runs (ext/TreeWaveOLDGCUDAExt.jl:
 23-30). The transfer runs in the particles' frame (ParticleFrame, src/
 transfer.jl:705-766): a brick's own coordinates, or the affine cube patch of
 the seven- and thirteen-patch balls.
+
+The other direction, from the field to the particles: TransferPlan.pairing
+is pairing(p, t, u, K, s; var, continuous) (src/transfer.jl:1779-1797) for
+each particle's density kernel K = (grad rho, rho), particle_forces the grid's
+part of the force (src/inspiral.jl:474-504), and source_pairing the pairing of
+a source's own projection (src/transfer.jl:1799-1825).
 """
 import ctypes
 import math
