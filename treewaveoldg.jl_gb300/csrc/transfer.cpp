@@ -991,6 +991,11 @@ int twoldg_transfer_plan::build_pairing() {
         const int e[3] = {list[4 * i + 1], list[4 * i + 2], list[4 * i + 3]};
         const double* lo = boxes[i].lo;
         const double* hi = boxes[i].hi;
+        // the element's neighbour in each of the 26 directions, found at its
+        // first use (in node order, so that a refusal is the first node's)
+        bool nb_found[27] = {false};
+        int64_t nb_block[27];
+        int nb_e[27][3];
         for (int m = 0; m < M && pair_cont_error.empty(); ++m) {
             const int K[3] = {m % P1, (m / P1) % P1, m / (P1 * P1)};
             int64_t* gc = &gcont[((size_t)i * M + m) * kGather];
@@ -1013,25 +1018,32 @@ int twoldg_transfer_plan::build_pairing() {
                     within = within && 0 <= en[d] && en[d] < E;
                 }
                 if (!within) {
-                    double x[3];
-                    bool in_dom = true;
-                    for (int d = 0; d < 3; ++d) {
-                        x[d] = (lo[d] + hi[d]) / 2 + s[d] * (hi[d] - lo[d]);
-                        in_dom = in_dom && dom_lo[d] < x[d] && x[d] < dom_hi[d];
+                    const int si = (s[0] + 1) + 3 * (s[1] + 1) + 9 * (s[2] + 1);
+                    if (!nb_found[si]) {
+                        double x[3];
+                        bool in_dom = true;
+                        for (int d = 0; d < 3; ++d) {
+                            x[d] = (lo[d] + hi[d]) / 2 + s[d] * (hi[d] - lo[d]);
+                            in_dom = in_dom && dom_lo[d] < x[d] && x[d] < dom_hi[d];
+                        }
+                        const int64_t found = in_dom ? locate(x) : -1;
+                        const char* why = found < 0 ? " is on the domain's face; the continuous reconstruction, like "
+                                                      "the transfer, does not look for periodic images"
+                                          : spacings[found] != spacings[b]
+                                              ? " has a neighbour on another level; the continuous reconstruction "
+                                                "needs the same level across every face"
+                                              : nullptr;
+                        if (why) {
+                            pair_cont_error = "the element at (" + fmt(lo[0]) + ", " + fmt(lo[1]) + ", " +
+                                              fmt(lo[2]) + ")" + why;
+                            break;
+                        }
+                        nb_block[si] = found;
+                        element_of(found, x, nb_e[si]);
+                        nb_found[si] = true;
                     }
-                    std::string at = "(" + fmt(lo[0]) + ", " + fmt(lo[1]) + ", " + fmt(lo[2]) + ")";
-                    bn = in_dom ? locate(x) : -1;
-                    if (bn < 0) {
-                        pair_cont_error = "the element at " + at + " is on the domain's face; the continuous "
-                                          "reconstruction, like the transfer, does not look for periodic images";
-                        break;
-                    }
-                    if (spacings[bn] != spacings[b]) {
-                        pair_cont_error = "the element at " + at + " has a neighbour on another level; the "
-                                          "continuous reconstruction needs the same level across every face";
-                        break;
-                    }
-                    element_of(bn, x, en);
+                    bn = nb_block[si];
+                    for (int d = 0; d < 3; ++d) en[d] = nb_e[si][d];
                 }
                 int Kn[3];
                 for (int d = 0; d < 3; ++d) Kn[d] = s[d] == 0 ? K[d] : (s[d] < 0 ? P : 0);
