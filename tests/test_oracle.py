@@ -9,7 +9,7 @@ import pytest
 from cases import refined_forest, scrambled, state_from, smooth_data
 from dense import along, from_global, global_array, global_operators
 from oracle.oracle import Oracle, golden_tables
-from oracle_drivers import oracle_errors
+from oracle_drivers import exact, oracle_errors
 from twoldg.forest import wave_forest
 
 
@@ -195,3 +195,94 @@ def test_energy_lost_at_rk4_rate():
             losses.append((E0 - E1) / E0)
         assert 0 < losses[1] < losses[0]
         assert losses[0] / losses[1] > 2 ** 5
+
+
+def test_reflecting_energy_is_kept_but_for_rk4():
+    # test/reflect_tests.jl:33-49: on the reflecting box the discrete energy,
+    # with the gradient carrying the wall's parity, is an invariant of the
+    # semi-discrete system; 50 steps at cfl 1/2 lose RK4's own share, never gain
+    for D, P in ((1, 2), (2, 2)):
+        forest = wave_forest(np.float64, D, P, 2, roots=2, reflecting=True)
+        o = Oracle(forest, P)
+        f0, _ = exact(D, 1.0, 1, 0.0, True)
+        u0 = o.truncate(state_from(forest, P, f0))
+        dt = 0.5 * forest.minimum_spacing() / (P + 1)
+        u = o.rk4(u0, dt, 50)
+        E0, E1 = o.energy(u0), o.energy(u)
+        assert E1 <= E0
+        assert E1 == pytest.approx(E0, rel=1e-6)
+
+
+def test_reflecting_forest_declares_walls():
+    # test/reflect_tests.jl:51-64: periodic stays the default, and a
+    # reflecting forest has walls on every face and no periodic direction
+    periodic = wave_forest(np.float64, 2, 2, 2, roots=2)
+    assert all(periodic.periodic) and not any(periodic.reflecting)
+    walls = wave_forest(np.float64, 2, 2, 2, roots=2, reflecting=True)
+    assert not any(walls.periodic) and all(walls.reflecting)
+
+
+def _rates(D, P, truncate=True, reflecting=False, roots=(2, 4, 8)):
+    from twoldg.drivers import convergence_rate
+    rs = [oracle_errors(D, P, 2, r, truncate=truncate, reflecting=reflecting) for r in roots]
+    hs = [r["h"] for r in rs]
+    return (convergence_rate(hs, [r["l2"] for r in rs]), convergence_rate(hs, [r["linf"] for r in rs]),
+            [r["l2"] for r in rs])
+
+
+@pytest.mark.parametrize("D", [1, 2])
+@pytest.mark.parametrize("P", [2, 3, 4])
+def test_truncated_error_converges_at_order_P(D, P):
+    # test/sinewave_tests.jl:16-26, the paper's bound O(h_e^P)
+    l2, linf, _ = _rates(D, P)
+    assert P - 0.25 < l2 < P + 0.2
+    assert P - 0.8 < linf < P + 0.4
+
+
+@pytest.mark.parametrize("P", [3, 4])
+def test_untruncated_u_is_more_accurate_but_irregular(P):
+    # test/sinewave_tests.jl:28-39
+    plain, _, errs = _rates(1, P, truncate=False)
+    _, _, terrs = _rates(1, P)
+    assert plain > P - 1
+    assert errs[-1] < terrs[-1]
+
+
+def test_first_order_at_P_1():
+    # test/sinewave_tests.jl:41-47
+    l2, _, _ = _rates(1, 1)
+    assert 0.8 < l2 < 1.1
+
+
+@pytest.mark.parametrize("D,P", [(1, 2), (1, 3), (2, 2), (2, 3)])
+def test_reflecting_mode_converges_at_order_P(D, P):
+    # test/reflect_tests.jl:21-31
+    l2, linf, _ = _rates(D, P, reflecting=True)
+    assert P - 0.35 < l2 < P + 0.4
+    assert P - 1.0 < linf < P + 0.6
+
+
+@pytest.mark.parametrize("D,P", [(1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4)])
+def test_rk4_is_stable_to_cfl_5_over_root_D(D, P):
+    # test/evolution_tests.jl:196-222: the largest eigenvalue of the
+    # truncated semi-discrete Laplacian, by power iteration through the
+    # right-hand side and the truncation, puts RK4's limit |lambda dt| <= 2
+    # sqrt 2 at the same cfl for every P, which pins oldg_timestep's
+    # h_min / (P + 1) = h_e / (P + 1)^2
+    import types
+    from twoldg.problem import oldg_timestep
+    forest = wave_forest(np.float64, D, P, 2, roots=2)
+    o = Oracle(forest, P)
+    x = o.truncate(state_from(forest, P, lambda y, var: np.sin(np.pi * (37 * sum(y) + 0.1)) if var == 1
+                              else 0 * y[0]))
+    nb = len(forest.leaves)
+    X = x.reshape(nb, 2, -1)
+    lam = 0.0
+    for _ in range(300):
+        Y = o.truncate(o.rhs(X.reshape(-1))).reshape(nb, 2, -1)
+        lap = Y[:, 1]
+        lam = np.linalg.norm(lap) / np.linalg.norm(X[:, 0])
+        X[:, 0] = lap / np.linalg.norm(lap)
+    p = types.SimpleNamespace(dtype=np.dtype(np.float64), forest=forest, hspeed=None, P=P)
+    cflmax = 2 * math.sqrt(2) / math.sqrt(lam) / oldg_timestep(p, 1.0)
+    assert 4.8 < cflmax * math.sqrt(D) < 5.8
