@@ -286,3 +286,186 @@ def test_rk4_is_stable_to_cfl_5_over_root_D(D, P):
     p = types.SimpleNamespace(dtype=np.dtype(np.float64), forest=forest, hspeed=None, P=P)
     cflmax = 2 * math.sqrt(2) / math.sqrt(lam) / oldg_timestep(p, 1.0)
     assert 4.8 < cflmax * math.sqrt(D) < 5.8
+
+
+def _standing(D, P, roots, refined=False, reflecting=False):
+    """standing_errors (test/refined_tests.jl:311-331) on the oracle: the
+    standing mode to a quarter period, its quadrature L2 error over the box,
+    over the ball of radius 1/4 about the refined region's centre (nodes
+    strictly inside), its largest error there, and the energy lost."""
+    from cases import node_positions
+    r = oracle_errors(D, P, 2, roots, refined=refined, reflecting=reflecting)
+    forest = r["forest"]
+    nb, NN = len(forest.leaves), forest.N ** D
+    f1, _ = exact(D, 1.0, 1, r["dt"] * r["nsteps"], reflecting)
+    x = node_positions(forest, P)
+    xs = tuple(x[:, k, :] for k in range(D))
+    err = r["state"].reshape(nb, 2, NN) - np.stack([f1(xs, 1), f1(xs, 2)], axis=1)
+    wh = golden_tables(P)["weights"].astype(np.float64)
+    grids = np.indices([forest.N] * D).reshape(D, -1)[::-1]
+    w = np.empty((nb, NN))
+    for b, key in enumerate(forest.leaves):
+        ww = np.ones(NN)
+        for d in range(D):
+            ww = ww * (forest.spacing(key) * (P + 1) / 2 * wh[grids[d] % (P + 1)])
+        w[b] = ww
+    centre = np.full(D, 0.25 if reflecting else 0.5)
+    inside = np.sum((x - centre[None, :, None]) ** 2, axis=1) < 0.25 ** 2
+    W = np.stack([w, w], axis=1)
+    B = np.stack([inside, inside], axis=1)
+    e2 = err ** 2
+    return dict(l2=math.sqrt(np.sum(W * e2) / np.sum(W)), ball_l2=math.sqrt(np.sum((W * e2)[B]) / np.sum(W[B])),
+                ball_linf=float(np.abs(err)[B].max()), loss=(r["energy0"] - r["energy"]) / r["energy0"])
+
+
+@pytest.mark.parametrize("D", [1, 2])
+@pytest.mark.parametrize("P", [2, 3, 4])
+def test_standing_mode_converges_at_order_P_on_two_levels(D, P):
+    # test/refined_tests.jl:333-354: doubling every level, the box's error
+    # falls at order P, and inside the refined middle it lies between the
+    # uniform coarse and fine runs' (its largest error too, in 1D)
+    c, f = _standing(D, P, 4), _standing(D, P, 8)
+    m4, m8 = _standing(D, P, 4, refined=True), _standing(D, P, 8, refined=True)
+    assert P - 0.25 < math.log2(m4["l2"] / m8["l2"]) < P + 0.2
+    assert f["l2"] < m4["l2"] < c["l2"]
+    assert f["ball_l2"] < m4["ball_l2"] < c["ball_l2"]
+    if D == 1:
+        assert f["ball_linf"] < m4["ball_linf"] < c["ball_linf"]
+
+
+@pytest.mark.parametrize("D,P,truncate,reflecting", [(1, 3, True, False), (2, 2, True, False), (2, 3, False, False),
+                                                     (2, 3, True, True)])
+def test_energy_on_two_levels_is_lost_only_to_rk4(D, P, truncate, reflecting):
+    # test/refined_tests.jl:356-376
+    forest = refined_forest(D, P, reflecting=reflecting)
+    o = Oracle(forest, P, truncate=truncate)
+
+    def f(x, var):
+        return sum(np.sin(np.pi * (2 * (d + 1) * x[d] + var / 3)) * np.cos(2 * np.pi * x[(d + 1) % D])
+                   for d in range(D))
+
+    u0 = o.truncate(state_from(forest, P, f)) if truncate else state_from(forest, P, f)
+    E0 = o.energy(u0)
+    losses = []
+    for cfl in (1.0, 0.5):
+        dt = cfl * forest.minimum_spacing() / (P + 1)
+        losses.append((E0 - o.energy(o.rk4(u0, dt, 200))) / E0)
+    assert 0 < losses[1] < losses[0]
+    assert losses[0] / losses[1] > 2 ** 5
+
+
+def _cflmax(forest, P):
+    import types
+    from twoldg.problem import oldg_timestep
+    D = forest.D
+    o = Oracle(forest, P)
+    x = o.truncate(state_from(forest, P, lambda y, var: np.sin(np.pi * (37 * sum(y) + 0.1)) if var == 1
+                              else 0 * y[0]))
+    nb = len(forest.leaves)
+    X = x.reshape(nb, 2, -1)
+    lam = 0.0
+    for _ in range(300):
+        lap = o.truncate(o.rhs(X.reshape(-1))).reshape(nb, 2, -1)[:, 1]
+        lam = np.linalg.norm(lap) / np.linalg.norm(X[:, 0])
+        X[:, 0] = lap / np.linalg.norm(lap)
+    p = types.SimpleNamespace(dtype=np.dtype(np.float64), forest=forest, hspeed=None, P=P)
+    return 2 * math.sqrt(2) / math.sqrt(lam) / oldg_timestep(p, 1.0)
+
+
+@pytest.mark.parametrize("D,P", [(1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4), (3, 1)])
+def test_rk4_limit_on_two_levels_is_the_uniform_one(D, P):
+    # test/refined_tests.jl:378-409: the coarse-fine faces add no mode
+    # stiffer than a uniform forest at the finest spacing has
+    uniform = _cflmax(wave_forest(np.float64, D, P, 2, roots=3 if D == 3 else 4), P)
+    twolevel = _cflmax(refined_forest(D, P), P)
+    assert 0.99 < twolevel / uniform < 1.1
+    assert 4.8 < twolevel * math.sqrt(D) < 6.2
+
+
+@pytest.mark.parametrize("D", [1, 2])
+@pytest.mark.parametrize("P", [2, 3])
+def test_reflecting_box_refined_at_its_walls(D, P):
+    # test/refined_tests.jl:411-431
+    corner = tuple((0.0, 0.5) for _ in range(D))
+    c, f = _standing(D, P, 4, reflecting=True), _standing(D, P, 8, reflecting=True)
+    m4 = _standing(D, P, 4, refined=corner, reflecting=True)
+    m8 = _standing(D, P, 8, refined=corner, reflecting=True)
+    assert P - 0.25 < math.log2(m4["l2"] / m8["l2"]) < P + 0.2
+    assert f["l2"] < m4["l2"] < c["l2"]
+    assert f["ball_l2"] < m4["ball_l2"] < c["ball_l2"]
+    assert 0 <= m4["loss"] < 1e-8
+
+
+def test_coarse_ghost_degree_loss_in_2d():
+    # test/refined_tests.jl:433-447 records, as a broken test, that in 2D at
+    # P = 3 the refined middle's largest error falls by about 2^1.77 from
+    # roots 8 to 16, not 2^(P - 1/2): the coarse ghost, the adjoint
+    # restriction, is exact only to degree P - 1 tangentially. The shortfall
+    # shows here too, which pins that ghost; the box's L2 keeps order P.
+    P = 3
+    m8, m16 = _standing(2, P, 8, refined=True), _standing(2, P, 16, refined=True)
+    assert math.log2(m8["ball_linf"] / m16["ball_linf"]) < P - 0.5
+    assert P - 0.25 < math.log2(m8["l2"] / m16["l2"]) < P + 0.2
+
+
+# The reference's measured errors inside the refined region (1/4, 3/4)^D
+# (CODE.md:4646-4662): D, P, roots, then L2 and L-infinity of the uniform
+# coarse run (roots), the two-level forest (roots, the middle refined) and
+# the uniform fine run (2 roots), the standing mode at a quarter period.
+REFINED_REGION = [
+    (1, 2, 8, (3.93e-02, 1.25e-02, 1.13e-02), (8.21e-02, 5.03e-02, 2.75e-02)),
+    (1, 2, 16, (1.13e-02, 2.51e-03, 2.23e-03), (2.75e-02, 8.64e-03, 5.01e-03)),
+    (1, 3, 8, (9.36e-04, 2.10e-04, 1.16e-04), (3.04e-03, 1.14e-03, 3.93e-04)),
+    (1, 3, 16, (1.16e-04, 1.96e-05, 1.45e-05), (3.93e-04, 1.28e-04, 4.96e-05)),
+    (1, 4, 8, (3.52e-05, 4.68e-06, 2.35e-06), (8.43e-05, 1.53e-05, 8.15e-06)),
+    (1, 4, 16, (2.35e-06, 2.12e-07, 1.19e-07), (8.15e-06, 8.94e-07, 2.93e-07)),
+    (2, 2, 8, (5.21e-02, 1.51e-02, 1.19e-02), (2.05e-01, 1.38e-01, 4.62e-02)),
+    (2, 2, 16, (1.19e-02, 4.24e-03, 3.25e-03), (4.62e-02, 4.00e-02, 1.31e-02)),
+    (2, 3, 8, (1.33e-03, 3.69e-04, 1.63e-04), (5.02e-03, 3.42e-03, 5.84e-04)),
+    (2, 3, 16, (1.63e-04, 6.67e-05, 2.04e-05), (5.84e-04, 9.65e-04, 7.18e-05)),
+    (2, 4, 8, (4.53e-05, 1.39e-05, 2.91e-06), (2.14e-04, 1.98e-04, 1.30e-05)),
+    (2, 4, 16, (2.91e-06, 1.15e-06, 1.77e-07), (1.30e-05, 1.42e-05, 8.65e-07)),
+]
+
+
+def _region_errors(D, P, roots, refined):
+    """L2 and L-infinity of the error at the nodes strictly inside (1/4, 3/4)^D,
+    both variables, weighted by each node's quadrature weight."""
+    from cases import node_positions
+    r = oracle_errors(D, P, 2, roots, refined=refined)
+    forest = r["forest"]
+    nb, NN = len(forest.leaves), forest.N ** D
+    f1, _ = exact(D, 1.0, 1, r["dt"] * r["nsteps"], False)
+    x = node_positions(forest, P)
+    xs = tuple(x[:, k, :] for k in range(D))
+    err = r["state"].reshape(nb, 2, NN) - np.stack([f1(xs, 1), f1(xs, 2)], axis=1)
+    wh = golden_tables(P)["weights"].astype(np.float64)
+    grids = np.indices([forest.N] * D).reshape(D, -1)[::-1]
+    w = np.empty((nb, NN))
+    for b, key in enumerate(forest.leaves):
+        ww = np.ones(NN)
+        for d in range(D):
+            ww = ww * (forest.spacing(key) * (P + 1) / 2 * wh[grids[d] % (P + 1)])
+        w[b] = ww
+    inside = np.all((x > 0.25) & (x < 0.75), axis=1)
+    W, S = np.stack([w, w], axis=1), np.stack([inside, inside], axis=1)
+    return math.sqrt(np.sum((W * err * err)[S]) / np.sum(W[S])), float(np.abs(err)[S].max())
+
+
+def _printed(value, printed):
+    """value rounds to the three significant digits printed."""
+    e = math.floor(math.log10(abs(printed)))
+    return abs(value - printed) <= 0.5001 * 10.0 ** (e - 2)
+
+
+@pytest.mark.parametrize("row", REFINED_REGION, ids=["D%d-P%d-roots%d" % r[:3] for r in REFINED_REGION])
+def test_refined_region_table(row):
+    # the two-level forest's coupling (coarse-fine ghosts by injection in
+    # 1D, by I and R tangentially in 2D) pinned by the reference's own
+    # measurements, every printed digit
+    D, P, roots, l2, linf = row
+    runs = [_region_errors(D, P, roots, False), _region_errors(D, P, roots, True),
+            _region_errors(D, P, 2 * roots, False)]
+    for k, (a, b) in enumerate(runs):
+        assert _printed(a, l2[k]), ("L2", k, a, l2[k])
+        assert _printed(b, linf[k]), ("Linf", k, b, linf[k])
