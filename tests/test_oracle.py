@@ -9,7 +9,12 @@ import pytest
 from cases import refined_forest, scrambled, state_from, smooth_data
 from dense import along, from_global, global_array, global_operators
 from oracle.oracle import Oracle, golden_tables
-from oracle_drivers import exact, oracle_errors
+from oracle_drivers import exact
+from oracle_drivers import oracle_errors as _oracle_errors
+import functools
+
+# runs that several tests read are made once (the results are only read)
+oracle_errors = functools.lru_cache(maxsize=None)(_oracle_errors)
 from twoldg.forest import wave_forest
 
 
@@ -469,3 +474,34 @@ def test_refined_region_table(row):
     for k, (a, b) in enumerate(runs):
         assert _printed(a, l2[k]), ("L2", k, a, l2[k])
         assert _printed(b, linf[k]), ("Linf", k, b, linf[k])
+
+
+# The reference's two-level convergence tables (CODE.md:4616-4636): D, P,
+# the L2 and the L-infinity errors over the box of the two-level forest (the
+# middle half refined) and of the uniform forest, at roots 4, 8, 16, 32.
+REFINED_BOX = [
+    (1, 2, (1.12e-01, 3.26e-02, 9.12e-03, 1.95e-03), (1.34e-01, 3.88e-02, 1.13e-02, 2.22e-03),
+     (3.10e-01, 8.52e-02, 2.64e-02, 6.07e-03), (2.75e-01, 8.21e-02, 2.75e-02, 5.01e-03)),
+    (1, 3, (5.66e-03, 6.75e-04, 8.32e-05, 1.04e-05), (8.20e-03, 9.27e-04, 1.16e-04, 1.45e-05),
+     (2.83e-02, 3.06e-03, 3.93e-04, 4.98e-05), (2.94e-02, 3.04e-03, 3.93e-04, 4.96e-05)),
+    (1, 4, (3.70e-04, 2.37e-05, 1.64e-06, 8.38e-08), (5.70e-04, 3.50e-05, 2.34e-06, 1.19e-07),
+     (2.31e-03, 7.52e-05, 8.22e-06, 2.90e-07), (2.23e-03, 8.43e-05, 8.15e-06, 2.93e-07)),
+    (2, 2, (1.67e-01, 4.70e-02, 1.09e-02, 2.97e-03), (1.83e-01, 5.21e-02, 1.19e-02, 3.26e-03),
+     (6.81e-01, 1.97e-01, 4.73e-02, 1.32e-02), (6.59e-01, 2.05e-01, 4.62e-02, 1.31e-02)),
+    (2, 3, (9.63e-03, 1.17e-03, 1.45e-04, 1.86e-05), (1.11e-02, 1.33e-03, 1.63e-04, 2.04e-05),
+     (4.83e-02, 4.94e-03, 9.65e-04, 1.90e-04), (4.28e-02, 5.02e-03, 5.84e-04, 7.18e-05)),
+    (2, 4, (5.68e-04, 3.97e-05, 2.58e-06, 1.60e-07), (6.62e-04, 4.54e-05, 2.91e-06, 1.77e-07),
+     (3.58e-03, 4.40e-04, 3.15e-05, 2.77e-06), (2.31e-03, 2.14e-04, 1.30e-05, 8.65e-07)),
+]
+
+
+@pytest.mark.parametrize("row", REFINED_BOX, ids=["D%d-P%d" % r[:2] for r in REFINED_BOX])
+def test_refined_box_tables(row):
+    # the standing mode on two-level and uniform forests at roots 4 to 32,
+    # RK4 at cfl 1/2 at the finest spacing, truncated: every printed digit
+    D, P, two_l2, uni_l2, two_linf, uni_linf = row
+    for i, roots in enumerate((4, 8, 16, 32)):
+        two, uni = oracle_errors(D, P, 2, roots, refined=True), oracle_errors(D, P, 2, roots)
+        assert _printed(two["l2"], two_l2[i]) and _printed(uni["l2"], uni_l2[i]), (roots, two["l2"], uni["l2"])
+        assert _printed(two["linf"], two_linf[i]) and _printed(uni["linf"], uni_linf[i]), (roots, two["linf"],
+                                                                                          uni["linf"])
