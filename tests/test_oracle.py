@@ -457,10 +457,10 @@ def _region_errors(D, P, roots, refined):
     return math.sqrt(np.sum((W * err * err)[S]) / np.sum(W[S])), float(np.abs(err)[S].max())
 
 
-def _printed(value, printed):
-    """value rounds to the three significant digits printed."""
+def _printed(value, printed, digits=3):
+    """value rounds to the significant digits printed."""
     e = math.floor(math.log10(abs(printed)))
-    return abs(value - printed) <= 0.5001 * 10.0 ** (e - 2)
+    return abs(value - printed) <= 0.5001 * 10.0 ** (e - digits + 1)
 
 
 @pytest.mark.parametrize("row", REFINED_REGION, ids=["D%d-P%d-roots%d" % r[:3] for r in REFINED_REGION])
@@ -602,3 +602,67 @@ def test_full_period_on_two_levels():
     for i, roots in enumerate((4, 8, 16)):
         assert _printed(oracle_errors(2, 3, 2, roots, periods=1.0)["l2"], uniform[i])
         assert _printed(oracle_errors(2, 3, 2, roots, periods=1.0, refined=True)["l2"], twolevel[i])
+
+
+def _bloch_blocks(P, truncate, M=6):
+    """The semi-discrete operator (the right-hand side, then the truncation)
+    on a periodic line of M elements of width 1, cut into the blocks by
+    which an element hears its neighbours: A_k couples element g to g + k,
+    u then v in each. Also the largest coupling beyond the neighbours."""
+    E = 2
+    forest = wave_forest(np.float64, 1, P, E, roots=M // E, L=float(M))
+    o = Oracle(forest, P, truncate=truncate)
+    nb, N, P1 = len(forest.leaves), forest.N, P + 1
+    n = 2 * nb * N
+    A = np.empty((n, n))
+    for j in range(n):
+        X = np.zeros(n)
+        X[j] = 1.0
+        Y = o.rhs(X)
+        A[:, j] = o.truncate(Y) if truncate else Y
+
+    def idx(g):
+        b, e = divmod(g % M, E)
+        base = b * 2 * N + e * P1
+        return np.concatenate([base + np.arange(P1), base + N + np.arange(P1)])
+
+    blocks = {k: A[np.ix_(idx(2), idx(2 + k))] for k in (-1, 0, 1)}
+    beyond = max(np.abs(A[np.ix_(idx(2), idx(2 + k))]).max() for k in range(2, M - 1))
+    return blocks, beyond
+
+
+def _bloch(blocks, theta):
+    """The eigenvalues of A(theta) = sum_k A_k e^{i k theta}."""
+    return np.linalg.eigvals(sum(b * np.exp(1j * k * theta) for k, b in blocks.items()))
+
+
+def test_dispersion_relation():
+    # CODE.md:4766-4801 ("Why the error outruns light"), P = 3, h_e = 1: the
+    # Bloch eigenvalues are +-i omega (energy kept mode by mode); with the
+    # truncation two branches are frozen, the physical one has a gap at
+    # k h = pi from 3.113 to 3.464, the branches meet at 7.746 at 2 pi, and the
+    # spectral radius is 8.641; without it a spurious branch leaves 0 at
+    # three times the speed of light, and the spectral radius is 9.105
+    def rho(blocks):
+        grid = np.linspace(0, 2 * np.pi, 721)
+        best = max(grid, key=lambda t: np.abs(_bloch(blocks, t)).max())
+        from scipy.optimize import minimize_scalar
+        r = minimize_scalar(lambda t: -np.abs(_bloch(blocks, t)).max(), bounds=(best - 0.01, best + 0.01),
+                            method="bounded", options={"xatol": 1e-10})
+        return -r.fun
+
+    for truncate in (True, False):
+        blocks, beyond = _bloch_blocks(3, truncate)
+        assert beyond == 0
+        for t in np.linspace(0, 2 * np.pi, 37):
+            assert np.abs(_bloch(blocks, t).real).max() < 2e-7
+        w_pi = np.sort(np.abs(_bloch(blocks, np.pi)))
+        w_0 = np.sort(np.abs(_bloch(blocks, 0.0)))
+        slow = np.sort(np.abs(_bloch(blocks, 0.01)))
+        if truncate:
+            assert np.all(w_pi[:2] < 1e-7) and _printed(w_pi[2], 3.113, 4) and _printed(w_pi[4], 3.464, 4)
+            assert _printed(w_0[-1], 7.746, 4) and _printed(rho(blocks), 8.641, 4)
+            assert not np.any(np.abs(slow / 0.01 - 3) < 0.05)
+        else:
+            assert _printed(w_0[-1], 7.746, 4) and _printed(rho(blocks), 9.105, 4)
+            assert np.any(np.abs(slow / 0.01 - 3) < 0.05)
