@@ -163,26 +163,53 @@ def test_reflecting_wall_mirrors_with_parity():
     del mirror
 
 
-@pytest.mark.parametrize("D,P,row", [
-    (1, 3, (1.48e-2, 1.70e-3, 2.08e-4, 9.37e-2, 1.15e-2, 1.29e-3)),
-    (2, 3, (1.47e-2, 1.71e-3, 2.08e-4, 1.43e-1, 1.55e-2, 1.87e-3)),
-    (2, 4, (1.46e-3, 1.02e-4, 6.61e-6, 1.20e-2, 9.31e-4, 6.38e-5)),
-])
-def test_convergence_table(D, P, row):
-    # reference CODE.md:4124-4145 (truncated, E = 2, roots 2/4/8, cfl 1/2,
-    # quarter period): the published L2 errors of u and v, to the 3 digits printed
+# reference CODE.md:4124-4145: the standing sine mode to a quarter period,
+# E = 2, roots 2, 4, 8, cfl 1/2: D, P, truncate, the L2 errors of u and of v
+CONVERGENCE = [
+    (1, 1, True, (5.06e-1, 2.72e-1, 1.38e-1), (3.16, 1.70, 8.67e-1)),
+    (1, 1, False, (1.10e-1, 2.83e-2, 7.12e-3), (4.92e-1, 1.17e-1, 2.87e-2)),
+    (1, 2, True, (1.00e-1, 2.69e-2, 6.65e-3), (7.76e-1, 1.88e-1, 5.45e-2)),
+    (1, 2, False, (8.08e-2, 3.46e-3, 4.38e-4), (6.93e-1, 1.13e-1, 2.48e-2)),
+    (1, 3, True, (1.48e-2, 1.70e-3, 2.08e-4), (9.37e-2, 1.15e-2, 1.29e-3)),
+    (1, 3, False, (2.77e-3, 8.41e-5, 2.59e-6), (4.38e-2, 1.01e-2, 1.29e-3)),
+    (1, 4, True, (1.42e-3, 1.02e-4, 6.63e-6), (1.12e-2, 7.99e-4, 4.90e-5)),
+    (1, 4, False, (2.32e-4, 6.90e-6, 1.44e-7), (1.00e-2, 1.08e-4, 2.49e-5)),
+    (1, 5, True, (1.12e-4, 3.23e-6, 9.85e-8), (7.21e-4, 1.98e-5, 6.26e-7)),
+    (1, 5, False, (1.36e-5, 1.44e-7, 1.10e-9), (2.56e-4, 1.20e-5, 4.08e-7)),
+    (2, 1, True, (4.35e-1, 2.61e-1, 1.37e-1), (3.86, 2.32, 1.21)),
+    (2, 1, False, (7.80e-2, 2.00e-2, 5.04e-3), (4.92e-1, 1.17e-1, 2.87e-2)),
+    (2, 2, True, (1.04e-1, 2.56e-2, 6.54e-3), (8.95e-1, 2.58e-1, 7.34e-2)),
+    (2, 2, False, (6.73e-2, 4.68e-3, 3.67e-4), (2.59e-1, 8.05e-2, 2.66e-2)),
+    (2, 3, True, (1.47e-2, 1.71e-3, 2.08e-4), (1.43e-1, 1.55e-2, 1.87e-3)),
+    (2, 3, False, (2.89e-3, 3.99e-4, 4.85e-5), (5.23e-2, 5.70e-3, 8.05e-4)),
+    (2, 4, True, (1.46e-3, 1.02e-4, 6.61e-6), (1.20e-2, 9.31e-4, 6.38e-5)),
+    (2, 4, False, (2.87e-4, 5.15e-6, 1.05e-7), (1.01e-2, 4.11e-4, 2.69e-5)),
+    (2, 5, True, (1.12e-4, 3.23e-6, 9.86e-8), (1.03e-3, 2.90e-5, 8.78e-7)),
+    (2, 5, False, (5.42e-6, 3.55e-7, 1.28e-8), (5.99e-4, 1.66e-5, 4.65e-7)),
+]
+
+
+@pytest.mark.parametrize("row", CONVERGENCE, ids=["D%d-P%d-%s" % (r[0], r[1], "trunc" if r[2] else "plain")
+                                                  for r in CONVERGENCE])
+def test_convergence_table(row):
+    # every printed digit
+    D, P, truncate, us, vs = row
     for i, roots in enumerate((2, 4, 8)):
-        r = oracle_errors(D, P, 2, roots)
-        assert r["eu"] == pytest.approx(row[i], rel=0.006), (roots, r["eu"])
-        assert r["ev"] == pytest.approx(row[3 + i], rel=0.006), (roots, r["ev"])
+        r = oracle_errors(D, P, 2, roots, truncate=truncate)
+        assert _printed(r["eu"], us[i]), ("u", roots, r["eu"])
+        assert _printed(r["ev"], vs[i]), ("v", roots, r["ev"])
 
 
 def test_reflecting_convergence_table():
-    # reference CODE.md:4160-4169: D = 1, P = 3 reflecting, l2 4.23e-3 4.81e-4 6.0e-5
-    for roots, ref in zip((2, 4, 8), (4.23e-3, 4.81e-4, 6.0e-5)):
-        r = oracle_errors(1, 3, 2, roots, reflecting=True)
-        assert r["l2"] == pytest.approx(ref, rel=0.01)
-        assert r["energy"] <= r["energy0"]
+    # reference CODE.md:4165-4169: the Neumann mode on the reflecting box, l2
+    # errors at roots 2, 4, 8, every printed digit (two or three)
+    rows = [(1, 2, ((6.9e-2, 2), (1.98e-2, 3), (5.72e-3, 3))), (1, 3, ((4.23e-3, 3), (4.81e-4, 3), (6.0e-5, 2))),
+            (2, 2, ((9.31e-2, 3), (2.64e-2, 3), (6.05e-3, 3)))]
+    for D, P, refs in rows:
+        for roots, (ref, digits) in zip((2, 4, 8), refs):
+            r = oracle_errors(D, P, 2, roots, reflecting=True)
+            assert _printed(r["l2"], ref, digits), (D, P, roots, r["l2"])
+            assert r["energy"] <= r["energy0"]
 
 
 def test_energy_lost_at_rk4_rate():
