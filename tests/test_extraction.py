@@ -134,3 +134,51 @@ def test_extraction_refuses_what_it_cannot_read():
     g, geo = annulus_forest(np.float64, 2, 2)
     with pytest.raises(ValueError, match="brick or the seven-patch ball"):
         element_stencils(g, 2, [np.array([0.5, 0.5])], geometry=geo)
+
+
+@pytest.mark.parametrize("D,P", [(2, 3), (3, 2), (3, 4)])
+def test_gradient_stencils_are_the_basis_derivatives(D, P):
+    # reconstruct_gradient (src/transfer.jl:2011-2030) reads the element's
+    # polynomial through derivative weights: they are the oracle's basis
+    # derivatives at the point, and a polynomial of degree P per dimension
+    # filled at the nodes gives its exact gradient
+    from oracle import transfer as OT
+    from twoldg.extraction import element_stencils
+    from twoldg.forest import wave_forest
+    forest = wave_forest(np.float64, D, P, 2, roots=2)
+    t = OT.Tables(P)
+    rng = np.random.default_rng(7)
+    pts = rng.uniform(0.02, 0.98, size=(6, D))
+    P1, N = P + 1, forest.N
+    coef = rng.standard_normal(D)
+
+    def g(X):
+        return sum(coef[d] * X[..., d] ** P for d in range(D)) + np.prod(X, axis=-1)
+
+    def grad(X):
+        out = np.stack([coef[d] * P * X[..., d] ** (P - 1) for d in range(D)], axis=-1)
+        for d in range(D):
+            out[..., d] += np.prod(np.delete(X, d, axis=-1), axis=-1)
+        return out
+
+    from cases import node_positions
+    x = node_positions(forest, P)
+    nb = len(forest.leaves)
+    u = np.zeros((nb, 2, N ** D))
+    u[:, 0] = g(np.moveaxis(x, 1, 2))
+    u = u.reshape(-1)
+    for d in range(D):
+        index, weights = element_stencils(forest, P, pts, deriv=d)
+        for j, X in enumerate(pts):
+            b = int(index[j, 0] // (2 * N ** D))
+            pos = index[j, 0] - b * 2 * N ** D
+            e = [(pos // N ** k) % N // P1 for k in range(D)]
+            lo = [forest.block_extent(forest.leaves[b])[k][0] + forest.spacing(forest.leaves[b]) * e[k] * P1
+                  for k in range(D)]
+            hi = [lo[k] + forest.spacing(forest.leaves[b]) * P1 for k in range(D)]
+            ref = t.element_basis(lo, hi, X[None, :], deriv=d)[0]
+            assert np.abs(weights[j] - ref).max() <= 1e-12 * np.abs(ref).max()
+        got = np.sum(weights * u[index], axis=1)
+        assert np.abs(got - grad(pts)[:, d]).max() <= 1e-11 * np.abs(grad(pts)).max()
+    with pytest.raises(ValueError, match="brick"):
+        element_stencils(forest, P, pts, deriv=D)

@@ -616,3 +616,19 @@ def test_pairing_in_the_ball_cube(native):
     gamma = 1 / math.sqrt(1 - v @ v)
     assert got[3] == pytest.approx(Q / gamma, rel=1e-12)
     assert np.abs(got[:3]).max() <= 1e-12 * Q / ell
+
+
+def test_reconstruct_gradient_is_the_polynomial_gradient(native):
+    # reconstruct_gradient (src/transfer.jl:2011-2030) through the device
+    # gather: a polynomial of degree P per dimension filled at the nodes gives
+    # its exact gradient, inside an element and on its faces
+    import torch
+    import twoldg
+    p = _problem(3, 3, 2)
+    g = p.fill_at_nodes(lambda x, var: var * (x[0] ** 3 + x[0] * x[1] * x[2] - 2 * x[1] ** 2)).reshape(-1)
+    u = torch.from_numpy(g.copy()).cuda()
+    for X in ((0.31, 0.52, 0.77), (0.5, 0.25, 0.9)):
+        exact = np.array([3 * X[0] ** 2 + X[1] * X[2], X[0] * X[2] - 4 * X[1], X[0] * X[1]])
+        for var in (1, 2):
+            got = twoldg.reconstruct_gradient(p, u, X, var=var)
+            assert np.abs(got - var * exact).max() <= 1e-12 * np.abs(exact).max()

@@ -26,6 +26,6 @@ from .blast import adaptive_blast, blast_exact, blast_initial, blast_reference, 
 from .extraction import (PlaneExtraction, SphereExtraction, ball_patch_point, harmonic_modes, plane_values,
                          sphere_modes, sphere_rule, sphere_values, spherical_harmonics)
 from .transfer import (ParticleSupport, TransferPlan, particle_forces, particle_frame, project_source, reconstruct,
-                       self_inertia, source_pairing, source_rhs, transfer_table)
+                       reconstruct_gradient, self_inertia, source_pairing, source_rhs, transfer_table)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -113,6 +113,23 @@ def _lagrange(nodes, z):
     return w
 
 
+def _lagrange_derivative(nodes, z):
+    """d/dz of every Lagrange polynomial through the nodes, at z (the
+    product rule over the factors)."""
+    n = len(nodes)
+    out = np.zeros(n)
+    for j in range(n):
+        for k in range(n):
+            if k == j:
+                continue
+            term = 1.0 / (nodes[j] - nodes[k])
+            for q in range(n):
+                if q != j and q != k:
+                    term *= (z - nodes[q]) / (nodes[j] - nodes[q])
+            out[j] += term
+    return out
+
+
 def _locate_brick(forest, x):
     """The leaf containing the physical point x of a brick and the point's
     position in it scaled to [0, 1]^D."""
@@ -135,12 +152,14 @@ def _locate_brick(forest, x):
     return forest._index[key], out
 
 
-def element_stencils(forest, P, points, geometry=None):
+def element_stencils(forest, P, points, geometry=None, deriv=None):
     """Each point's element and its weights, the element's own degree-P
     polynomial through its Gauss-Lobatto nodes (src/extraction.jl:172-214):
     state-vector positions of the (P+1)^D nodes for variable 1 and the
-    products of the 1D Lagrange weights, one row per point. `geometry` is a
-    brick's diagonal-metric map, which the extraction cannot invert."""
+    products of the 1D Lagrange weights, one row per point. With deriv = d
+    (a brick only) the weights give the polynomial's derivative along
+    dimension d instead (src/transfer.jl:2011-2030). `geometry` is a brick's
+    diagonal-metric map, which the extraction cannot invert."""
     from .ball import BallForest
     from .element import Element
     D, N = forest.D, forest.N
@@ -150,6 +169,8 @@ def element_stencils(forest, P, points, geometry=None):
     if ball and not isinstance(forest.geo, SevenPatchBall):
         raise ValueError("the extraction maps physical points to the forest on a brick or the seven-patch "
                          "ball only, not on a %s" % type(forest.geo).__name__)
+    if deriv is not None and (ball or not 0 <= deriv < D):
+        raise ValueError("the gradient's stencils are a brick's, along a dimension 0..%d" % (D - 1))
     if geometry is not None and not ball:
         raise ValueError("the extraction maps physical points to the forest on a brick or the seven-patch "
                          "ball only, not on a %s" % type(geometry).__name__)
@@ -167,6 +188,10 @@ def element_stencils(forest, P, points, geometry=None):
             b, local = _locate_brick(forest, x)
         e = [min(int(math.floor(local[d] * E)), E - 1) for d in range(D)]
         W = [_lagrange(nodes, 2 * (local[d] * E - e[d]) - 1) for d in range(D)]
+        if deriv is not None:
+            # d xi / d x = 2 E over the block's width along deriv
+            lo, hi = forest.block_extent(forest.leaves[b])[deriv]
+            W[deriv] = _lagrange_derivative(nodes, 2 * (local[deriv] * E - e[deriv]) - 1) * (2 * E / (hi - lo))
         q = 0
         for I in np.ndindex(*([P1] * D)):
             J = I[::-1]                      # first dimension fastest

@@ -17,7 +17,9 @@ The other direction, from the field to the particles: TransferPlan.pairing
 is pairing(p, t, u, K, s; var, continuous) (src/transfer.jl:1779-1797) for
 each particle's density kernel K = (grad rho, rho), particle_forces the grid's
 part of the force (src/inspiral.jl:474-504), and source_pairing the pairing of
-a source's own projection (src/transfer.jl:1799-1825).
+a source's own projection (src/transfer.jl:1799-1825). reconstruct and
+reconstruct_gradient read a state's element polynomial and its gradient at a
+point.
 """
 import ctypes
 import math
@@ -348,6 +350,27 @@ def reconstruct(p, u, x, var=1):
                                         dptr(out)))
     p.synchronize()
     return float(out.item())
+
+
+def reconstruct_gradient(p, u, x, var=1):
+    """reconstruct_gradient(p, t, u, x; var) (src/transfer.jl:2011-2030): the
+    gradient of reconstruct's polynomial at the point x of a brick, as a (D,)
+    array: one gather of D rows of derivative weights."""
+    from .extraction import element_stencils
+    from .problem import _dptr as dptr
+    torch = _torch()
+    rows = [element_stencils(p.forest, p.P, np.asarray([x], dtype=np.float64), deriv=d) for d in range(p.D)]
+    index = np.concatenate([r[0] for r in rows])
+    weights = np.concatenate([r[1] for r in rows])
+    idx = torch.as_tensor(index, device=p.device)
+    w = torch.as_tensor(weights, dtype=p.torch_dtype(), device=p.device)
+    out = torch.empty(p.D, dtype=p.torch_dtype(), device=p.device)
+    _check_state(p, u)
+    _sync_torch()
+    _lib.check(_lib.lib().twoldg_gather(p.handle, dptr(u), int(var), p.D, index.shape[1], dptr(idx), dptr(w),
+                                        dptr(out)))
+    p.synchronize()
+    return out.double().cpu().numpy()
 
 
 def self_inertia(Q, ell):
