@@ -71,3 +71,16 @@ def test_annulus_rhs_is_self_adjoint_and_rotation_free():
     w = _weights(o, forest, 3) * coef[:, 0]
     la, lb = lap(a), lap(b)
     assert abs(np.sum(w * b * la) - np.sum(w * lb * a)) < 1e-12 * np.sum(np.abs(w * b * la))
+
+
+def test_annulus_energy_changes_by_rk4_loss_alone():
+    # test/annulus_tests.jl:165-185: P = 3, roots (2, 1), the rotating mode to
+    # t = pi/k at cfl 1/2 and 1/4: never a gain, a loss below 1e-8, falling by
+    # more than 16 as the step halves
+    losses = []
+    for cfl in (0.5, 0.25):
+        r = oracle_annulus_errors(3, 2, (2, 1), cfl=cfl)
+        assert r["energy"] <= r["energy0"]
+        losses.append((r["energy0"] - r["energy"]) / r["energy0"])
+    assert losses[0] < 1e-8
+    assert losses[0] / losses[1] > 16
