@@ -7,10 +7,11 @@ from oracle.oracle import BallOracle
 from twoldg.ball import PlaneWave, ball_forest, ball_tables, node_logical, sevenpatch_forest
 
 
-def ball_setup(P, E, roots, truncate=True, k=(1.1, -0.7, 0.5), phi=0.3, Rm=None, radiative=None, Lc=1.0, R1=3.0):
+def ball_setup(P, E, roots, truncate=True, k=(1.1, -0.7, 0.5), phi=0.3, Rm=None, radiative=None, Lc=1.0, R1=3.0,
+               grading=0.0):
     """A ball (the thirteen-patch one with Rm), its tables and its oracle;
     radiative = (kappa, inverse_r) replaces the Dirichlet wave."""
-    forest, geo = ball_forest(np.float64, P, E, roots, Lc, R1, Rm=Rm)
+    forest, geo = ball_forest(np.float64, P, E, roots, Lc, R1, Rm=Rm, grading=grading)
     wave = PlaneWave(k, phi)
     tables = ball_tables(forest, P, wave)
     rad = None

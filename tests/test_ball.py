@@ -88,11 +88,16 @@ def test_sevenpatch_published_table(row):
         assert _printed(1 - r["energy"] / r["energy0"], des[i], digits=2), (s, r["energy"] / r["energy0"])
 
 
-def test_ball_laplacian_is_self_adjoint_away_from_the_sphere():
+@pytest.mark.parametrize("P", [2, 3])
+@pytest.mark.parametrize("grading", [0.0, 1.5])
+def test_ball_laplacian_is_self_adjoint_away_from_the_sphere(P, grading):
     # with homogeneous data (a field vanishing on the sphere's ghosts), the
     # full-metric Laplacian is self-adjoint in sqrt(g)-weighted quadrature over
-    # the cube and its glued shells: checked on fields supported inside |x| < 1.5
-    forest, geo, wave, tables, o = ball_setup(2, 2, (2, 2), truncate=False, k=(0.0, 0.0, 0.0), phi=0.0)
+    # the cube and its glued shells, graded or not, to the 1e-13 of
+    # test/sevenpatch_tests.jl:182-226: checked on fields supported inside
+    # |x| < 1.5
+    forest, geo, wave, tables, o = ball_setup(P, 2, (2, 2), truncate=False, k=(0.0, 0.0, 0.0), phi=0.0,
+                                              grading=grading)
     from ball_cases import physical_nodes
     X = physical_nodes(forest, tables)
     r = np.linalg.norm(X, axis=1)
@@ -103,12 +108,12 @@ def test_ball_laplacian_is_self_adjoint_away_from_the_sphere():
         s = np.zeros((nb, 2, NN))
         s[:, 0] = a
         return o.rhs(s.reshape(-1)).reshape(nb, 2, NN)[:, 1]
-    P1 = 3
+    P1 = P + 1
     N = forest.N
-    wq = Element(np.float64, 2).weights
+    wq = Element(np.float64, P).weights
     w1 = (1.0 / N) * P1 / 2 * wq[np.arange(N) % P1]
     w = np.kron(np.kron(w1, w1), w1)[None, :] * tables["coef"].reshape(nb, 10, NN)[:, 0]
     a, b = bump(0), bump(1)
     la, lb = lap(a), lap(b)
     lhs, rhs = np.sum(w * b * la), np.sum(w * lb * a)
-    assert abs(lhs - rhs) < 1e-10 * np.sum(np.abs(w * b * la))
+    assert abs(lhs - rhs) < 1e-13 * np.sum(np.abs(w * b * la))
