@@ -353,3 +353,85 @@ def test_transfer_entry_points_refuse_bad_arguments_on_the_host():
     assert lib.twoldg_transfer_table(3, 0, b"nodes", 6, out) == _lib.TWOLDG_EINVAL
     assert b"unknown transfer table" in lib.twoldg_last_error()
     assert lib.twoldg_transfer_table(0, 0, b"bary", 6, out) == _lib.TWOLDG_EINVAL
+
+
+def test_ball_rule_is_exact_on_what_it_should_be():
+    # test/transfer_tests.jl:585-600: the volume and moments of the unit
+    # ball, and the particle profile's unit charge
+    ys, ws = T.ball_rule(8, 8)
+    assert np.sum(ws) == pytest.approx(4 * math.pi / 3, rel=1e-14)
+    assert np.sum(ws * ys[:, 0] ** 2) == pytest.approx(4 * math.pi / 15, rel=1e-14)
+    assert np.sum(ws * ys[:, 0] ** 2 * ys[:, 1] ** 2 * ys[:, 2] ** 2) == pytest.approx(4 * math.pi / 945, rel=1e-13)
+    assert abs(np.sum(ws * ys[:, 0] ** 3 * ys[:, 1])) < 1e-15
+    ell = 1e-3
+    rho = T.particle_density(ys * ell, np.zeros(3), np.zeros(3), ell, 1.0)
+    assert np.sum(ws * rho * ell ** 3) == pytest.approx(1.0, rel=1e-14)
+
+
+@pytest.mark.parametrize("D,P", [(1, 4), (2, 3), (3, 2)])
+def test_reconstruction_is_the_element_polynomial(D, P):
+    # test/transfer_tests.jl:554-583 through the host stencils the device
+    # gather reads: exact on a polynomial of degree P per dimension, with its
+    # gradient, and the stored value at a node (a face node reconstructs the
+    # upper element, so those are left out)
+    from cases import node_positions
+    from twoldg.extraction import element_stencils
+    from twoldg.forest import wave_forest
+    forest = wave_forest(np.float64, D, P, 2, roots=2)
+    N, nb = forest.N, len(forest.leaves)
+    x = np.moveaxis(node_positions(forest, P), 1, 2)            # (nb, N^D, D)
+
+    def poly(X):
+        return np.prod([1 + (d + 1) * X[..., d] - X[..., d] ** P for d in range(D)], axis=0)
+
+    def grad(X):
+        out = []
+        for d in range(D):
+            g = (d + 1) - P * X[..., d] ** (P - 1)
+            for k in range(D):
+                if k != d:
+                    g = g * (1 + (k + 1) * X[..., k] - X[..., k] ** P)
+            out.append(g)
+        return np.stack(out, axis=-1)
+
+    u = np.zeros((nb, 2, N ** D))
+    u[:, 0] = poly(x)
+    u = u.reshape(-1)
+    pts = np.array([[(0.3 + 0.618 * k * (d + 1)) % 1.0 for d in range(D)] for k in range(1, 21)])
+    index, weights = element_stencils(forest, P, pts)
+    assert np.allclose(np.sum(weights * u[index], axis=1), poly(pts), rtol=1e-13, atol=0)
+    for d in range(D):
+        index, weights = element_stencils(forest, P, pts, deriv=d)
+        assert np.abs(np.sum(weights * u[index], axis=1) - grad(pts)[:, d]).max() <= 1e-12 * np.abs(grad(pts)).max()
+    w = irregular(nb * 2 * N ** D).reshape(nb, 2, N ** D)
+    grids = np.indices([N] * D).reshape(D, -1)[::-1]
+    interior = np.all(grids % (P + 1) != P, axis=0)
+    for b in (0, nb - 1):
+        X = x[b][interior]
+        index, weights = element_stencils(forest, P, X)
+        got = np.sum(weights * w.reshape(-1)[index + N ** D], axis=1)
+        assert np.abs(got - w[b, 1][interior]).max() <= 1e-14
+
+
+@pytest.mark.parametrize("ratio", [1e-1, 1e-2, 1e-3, 1e-4])
+def test_sinh_points_grow_like_log_of_he_over_ell(ratio):
+    # test/transfer_tests.jl:216-240: for the field of a particle of size ell
+    # just outside a face of the unit element, a sinh rule of
+    # 16 + 8 log10(h_e/ell) points per line reaches 1e-12 of an 80-point one
+    P = 3
+    lo, hi = [0.0, 0.0, 0.0], [1.0, 1.0, 1.0]
+    ell = ratio
+    z = np.array([1 + 1.01 * ell, 0.3, 0.6])
+    s = T.Support(z, np.zeros(3), ell)
+
+    def field(t):
+        def g(X):
+            r2 = np.sum((X - z) ** 2, axis=1)
+            val = np.where(r2 < ell ** 2, (3 - r2 / ell ** 2) / (2 * ell), 1 / np.sqrt(r2))
+            return val[:, None] * t.element_basis(lo, hi, X)
+        return g
+
+    tref = T.Tables(P, nsinh=80)
+    ref = T.nested_rule(field(tref), s, tref, lo, hi, 3)
+    t = T.Tables(P, nsinh=16 + 8 * round(math.log10(1 / ratio)))
+    assert np.abs(T.nested_rule(field(t), s, t, lo, hi, 3) - ref).max() < 1e-12 * np.abs(ref).max()
