@@ -693,3 +693,19 @@ def test_dispersion_relation():
         else:
             assert _printed(w_0[-1], 7.746, 4) and _printed(rho(blocks), 9.105, 4)
             assert np.any(np.abs(slow / 0.01 - 3) < 0.05)
+
+
+@pytest.mark.parametrize("D,P", [(1, 3), (2, 2), (2, 3)])
+def test_quadrature_norm_integrates_what_the_element_represents(D, P):
+    # test/layout_tests.jl:41-60: a constant has norm one (p = 2 and 1), the
+    # mean of |prod x^k|^2 over the unit box is exact while its degree 2k is
+    # within the element's quadrature, and the largest value is 1
+    forest = wave_forest(np.float64, D, P, 2, roots=2)
+    o = Oracle(forest, P)
+    one = state_from(forest, P, lambda x, var: 1.0 + 0 * x[0])
+    assert o.norm(one, 2, 1) == pytest.approx(1.0, abs=1e-14)
+    assert o.norm(one, 1, 1) == pytest.approx(1.0, abs=1e-14)
+    k = P - 1
+    mono = state_from(forest, P, lambda x, var: np.prod(x, axis=0) ** k)
+    assert o.norm(mono, 2, 1) == pytest.approx(math.sqrt(1 / (2 * k + 1)) ** D, abs=1e-13)
+    assert o.norm(mono, 0, 1) == pytest.approx(1.0, abs=1e-14)
