@@ -1,5 +1,7 @@
 """The annulus (a diagonal metric): the oracle against the reference's
 published convergence table, and the metric's projector properties. No GPU."""
+import math
+
 import numpy as np
 import pytest
 
@@ -84,3 +86,61 @@ def test_annulus_energy_changes_by_rk4_loss_alone():
         losses.append((r["energy0"] - r["energy"]) / r["energy0"])
     assert losses[0] < 1e-8
     assert losses[0] / losses[1] > 16
+
+
+def _host_truncation(forest, P, modes, duals, s):
+    """The truncation the kernels apply from the host's per-line tables: on
+    v, along dimension 0 then 1, each element line's v -= mode (dual . v)."""
+    nb, N, P1 = len(forest.leaves), forest.N, P + 1
+    E = N // P1
+    modes = modes.reshape(2, nb, E, P1)
+    duals = duals.reshape(2, nb, E, P1)
+    out = s.reshape(nb, 2, N, N).copy()              # [b, var, i1, i0]
+    for b in range(nb):
+        v = out[b, 1]
+        for e in range(E):
+            sl = slice(e * P1, (e + 1) * P1)
+            v[:, sl] -= np.outer(v[:, sl] @ duals[0, b, e], modes[0, b, e])
+        for e in range(E):
+            sl = slice(e * P1, (e + 1) * P1)
+            v[sl, :] -= np.outer(modes[1, b, e], duals[1, b, e] @ v[sl, :])
+    return out.reshape(-1)
+
+
+@pytest.mark.parametrize("P", [2, 3, 4])
+def test_annulus_truncation_is_the_sqrtg_orthogonal_projection(P):
+    # test/annulus_tests.jl:95-131, for the library's host tables (which the
+    # kernels read) and for the oracle's own projector (long double from the
+    # sqrt(g) factors): self-adjoint in the sqrt(g) weights, a projection onto
+    # Q_{P-1} (the flat projector leaves its result), u left alone, the
+    # kinetic energy not raised; along the angle the tables are the element's
+    from annulus_cases import line_weights
+    from oracle.oracle import Oracle
+    from test_oracle import _weights
+    el = Element(np.float64, P)
+    forest, geo = annulus_forest(np.float64, P, 2, roots=(2, 2), r0=0.25, r1=2.0)
+    coef, modes, duals, _ = metric_tables(forest, el, geo)
+    o = Oracle(forest, P, coef=coef, line_weights=line_weights(forest, geo, P))
+    flat = Oracle(forest, P)
+    nb, NN = len(forest.leaves), forest.N ** 2
+    wg = (_weights(o, forest, P) * coef.reshape(nb, 3, NN)[:, 0]).reshape(-1)
+    rng = np.random.default_rng(5)
+    a, b = rng.standard_normal(nb * 2 * NN), rng.standard_normal(nb * 2 * NN)
+
+    def v(x):
+        return x.reshape(nb, 2, NN)[:, 1].reshape(-1)
+
+    def inner(x, y):
+        return float(np.sum(wg * x * y))
+
+    for trunc in (lambda s: _host_truncation(forest, P, modes, duals, s), o.truncate):
+        ta, tb = trunc(a), trunc(b)
+        scale = math.sqrt(inner(v(a), v(a)) * inner(v(b), v(b)))
+        assert abs(inner(v(ta), v(b)) - inner(v(a), v(tb))) < 1e-14 * scale
+        assert np.allclose(trunc(ta), ta, rtol=0, atol=1e-13 * np.abs(ta).max())
+        assert np.allclose(flat.truncate(ta), ta, rtol=0, atol=1e-12 * np.abs(ta).max())
+        assert np.array_equal(ta.reshape(nb, 2, NN)[:, 0], a.reshape(nb, 2, NN)[:, 0])
+        assert inner(v(ta), v(ta)) <= inner(v(a), v(a))
+    assert np.allclose(_host_truncation(forest, P, modes, duals, a), o.truncate(a), rtol=0, atol=1e-13 * np.abs(a).max())
+    m = modes.reshape(2, nb, 2, P + 1)[0]
+    assert np.allclose(m, np.broadcast_to(el.topmode.astype(np.float64), m.shape), rtol=1e-13, atol=1e-14)
