@@ -144,3 +144,28 @@ def test_annulus_truncation_is_the_sqrtg_orthogonal_projection(P):
     assert np.allclose(_host_truncation(forest, P, modes, duals, a), o.truncate(a), rtol=0, atol=1e-13 * np.abs(a).max())
     m = modes.reshape(2, nb, 2, P + 1)[0]
     assert np.allclose(m, np.broadcast_to(el.topmode.astype(np.float64), m.shape), rtol=1e-13, atol=1e-14)
+
+
+def test_bessel_mode_is_the_annulus_neumann_mode():
+    # test/annulus_tests.jl:200-216: the exact solution has d_r u = 0 on both
+    # walls and R(k r0) = 1 by its scaling; the roots are ordered
+    from scipy.special import jv, yv
+    from twoldg.geometry import _dbesselj, _dbessely, annulus_wavenumber
+    r0, r1 = 0.5, 2.0
+    for m, n in ((0, 1), (1, 1), (2, 1), (3, 2)):
+        k = annulus_wavenumber(m, n, r0, r1)
+        assert k > 0
+        jr0, yr0 = _dbesselj(m, k * r0), _dbessely(m, k * r0)
+        scale = math.pi * k * r0 / 2
+        for r in (r0, r1):
+            assert abs(scale * (_dbesselj(m, k * r) * yr0 - _dbessely(m, k * r) * jr0)) < 1e-12
+        assert scale * (jv(m, k * r0) * yr0 - yv(m, k * r0) * jr0) == pytest.approx(1.0, rel=1e-12)
+    assert annulus_wavenumber(1, 1, 1, 2) < annulus_wavenumber(1, 2, 1, 2)
+
+
+def test_annulus_forest_refuses_what_it_does_not_map():
+    # test/annulus_tests.jl:218-230, the forest's own refusals
+    with pytest.raises(ValueError, match="odd"):
+        annulus_forest(np.float64, 2, 3)
+    with pytest.raises(ValueError, match="0 < r0 < r1"):
+        annulus_forest(np.float64, 2, 2, r0=2, r1=1)
