@@ -1,6 +1,8 @@
 """The seven-patch ball (full metric, quarter-turn glue, Dirichlet sphere):
 the host geometry and glue, and the oracle against the reference's published
 table. No GPU."""
+import math
+
 import numpy as np
 import pytest
 
@@ -117,3 +119,52 @@ def test_ball_laplacian_is_self_adjoint_away_from_the_sphere(P, grading):
     la, lb = lap(a), lap(b)
     lhs, rhs = np.sum(w * b * la), np.sum(w * lb * a)
     assert abs(lhs - rhs) < 1e-13 * np.sum(np.abs(w * b * la))
+
+
+
+def _flat_truncate(s, nb, N, el):
+    """The element's own tensor projector on v, line by line along each
+    dimension in order: the identity on Q_{P-1} and on nothing else."""
+    P1 = el.P + 1
+    mode, dual = el.topmode.astype(np.float64), el.topdual.astype(np.float64)
+    out = s.reshape(nb, 2, N, N, N).copy()                      # [b, var, i2, i1, i0]
+    v = out[:, 1]
+    for d in range(3):
+        w = np.moveaxis(v, 3 - d, -1)                          # a view, dimension d last
+        for e in range(N // P1):
+            line = w[..., e * P1:(e + 1) * P1]
+            line -= (line @ dual)[..., None] * mode
+    return out.reshape(-1)
+
+
+@pytest.mark.parametrize("P", [2, 3])
+def test_ball_truncation_is_the_sqrtg_orthogonal_projection(P):
+    # test/sevenpatch_tests.jl:128-158 on the oracle's projector (each
+    # element's solved directly from sqrt(g)): self-adjoint in the sqrt(g)
+    # weights, a projection, onto Q_{P-1} (the element's own projector leaves
+    # its result and not the data's), u left alone, the kinetic energy not
+    # raised
+    forest, geo, wave, tables, o = ball_setup(P, 2, (2, 2), truncate=True, k=(0.0, 0.0, 0.0), phi=0.0)
+    el = Element(np.float64, P)
+    nb, N = forest.nleaves(), forest.N
+    NN = N ** 3
+    P1 = P + 1
+    w1 = (1.0 / N) * P1 / 2 * el.weights.astype(np.float64)[np.arange(N) % P1]
+    wg = (np.kron(np.kron(w1, w1), w1)[None, :] * tables["coef"].reshape(nb, 10, NN)[:, 0]).reshape(-1)
+    rng = np.random.default_rng(3)
+    a, b = rng.standard_normal(nb * 2 * NN), rng.standard_normal(nb * 2 * NN)
+
+    def v(x):
+        return x.reshape(nb, 2, NN)[:, 1].reshape(-1)
+
+    def inner(x, y):
+        return float(np.sum(wg * x * y))
+
+    ta, tb = o.truncate(a), o.truncate(b)
+    scale = math.sqrt(inner(v(a), v(a)) * inner(v(b), v(b)))
+    assert abs(inner(v(ta), v(b)) - inner(v(a), v(tb))) < 1e-14 * scale
+    assert np.allclose(o.truncate(ta), ta, rtol=0, atol=1e-13 * np.abs(ta).max())
+    assert np.allclose(_flat_truncate(ta, nb, N, el), ta, rtol=0, atol=1e-12 * np.abs(ta).max())
+    assert not np.allclose(_flat_truncate(a, nb, N, el), a)
+    assert np.array_equal(ta.reshape(nb, 2, NN)[:, 0], a.reshape(nb, 2, NN)[:, 0])
+    assert inner(v(ta), v(ta)) <= inner(v(a), v(a))
