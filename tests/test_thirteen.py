@@ -257,3 +257,21 @@ def test_radiative_published_table(kappa, inverse_r, left, l2):
     else:
         assert ratio == pytest.approx(left, rel=0.03)
     assert r["l2"] == pytest.approx(l2, rel=0.02)
+
+
+def test_outer_shells_sqrtg_is_the_product_of_the_declared_factors():
+    # test/thirteenpatch_tests.jl:116-138: the factored truncation is
+    # sqrt(g)-orthogonal only if the radial factor r^2 r' and the angular one
+    # (2/n)^2 (1 + c_a^2 + c_b^2)^(-3/2) multiply to the frame's sqrt(g), with
+    # one angular function shared by the six shells; the cube and the inner
+    # shells do not factorize
+    from twoldg.ball import thirteenpatch_forest
+    forest, geo = thirteenpatch_forest(np.float64, 2, 2, roots=(3, 1, 2), Lc=1.0, Rm=2.0, R1=3.5)
+    assert all(geo.factored_dim(q) == -1 for q in range(7))
+    for xi in ((0.3, 0.7, 0.9), (2.9, 0.1, 1.2), (1.5, 1.5, 1.5)):
+        for q in range(7, 13):
+            k = geo.factored_dim(q)
+            assert k == (q - 7) // 2
+            xa, xb = (xi[j] for j in range(3) if j != k)
+            J = float(geo.frame(xi, q)[0])
+            assert geo.radial_volume(xi[k], q) * geo.angular_volume(xa, xb) == pytest.approx(J, rel=1e-14)
