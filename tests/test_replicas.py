@@ -1,7 +1,8 @@
-"""The N > 1 path of the bench, which runs independent replicas (the field
-step has no collective; the survey's multi-GPU row plans replicas only): two
-gloo ranks on the CPU take the barrier and the maximum of their times, and
-the reference arm runs on rank 0 alone."""
+"""The bench on the CPU: its N > 1 path, which runs independent replicas (the
+field step has no collective; the survey's multi-GPU row plans replicas only),
+where two gloo ranks take the barrier and the maximum of their times and the
+reference arm runs on rank 0 alone; the reference arm's JSON line; and the
+clock summary of the timed region."""
 import multiprocessing as mp
 import os
 import socket
@@ -74,3 +75,29 @@ def test_reference_arm_line_keeps_the_contract():
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert "workload" in d["config"]
+
+
+def test_clock_summary_reads_the_timed_region():
+    # the bench's nvidia-smi summary: the median SM clock and the largest max
+    # clock of the samples inside the timed region, the throttle reasons any
+    # of them had active, malformed lines left out; with no sample inside, the
+    # first one after the region, counted as trailing
+    sys.path.insert(0, ROOT)
+    import bench
+    c = bench.Clocks(0)
+    na, on = "Not Active", "Active"
+    c.samples = [(0.5, ["1400", "2070", "300", na, na, na, na]),
+                 (1.1, ["2070", "2070", "900", na, na, na, on]),
+                 (1.2, ["2050", "2070", "950", na, na, na, na]),
+                 (1.3, ["[N/A]", "2070", "950", na, na, na, na]),
+                 (1.35, ["2070", "2070"]),
+                 (1.4, ["2070", "2070", "990", na, na, na, na]),
+                 (2.5, ["2070", "2070", "100", on, na, na, na])]
+    c.t0, c.t1 = 1.0, 2.0
+    s = c.summary()
+    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
+    assert s["samples"] == 4 and s["trailing_samples"] == 0
+    c.t0, c.t1 = 2.0, 2.2
+    s = c.summary()
+    assert s["samples"] == 0 and s["trailing_samples"] == 1 and s["reasons"] == ["hw_slowdown"]
