@@ -112,3 +112,39 @@ def test_sine_ensemble_is_seeded():
     b = twoldg.sine_ensemble(8, seed=0)
     assert [(f.N, P, len(f.leaves)) for f, P, _ in a] == [(f.N, P, len(f.leaves)) for f, P, _ in b]
     assert all(2 <= P <= 5 for _, P, _ in a)
+
+
+def test_flat_kernels_refuse_a_face_table_or_a_bare_metric_kind():
+    """The flat and diagonal kernels read a neighbour's face plane as it lies:
+    a descriptor with an explicit face table (glued patches, boundary faces)
+    but no full metric, or a metric kind without its coefficients, is refused
+    before any device work, by the problem and by the static right-hand side."""
+    f = wave_forest(np.float64, 3, 3, 4, roots=1)
+    d, keep = twoldg.problem.make_desc(f, twoldg.Element(np.float64, 3), True, _lib.F64)
+    nb = np.full(6, -1, dtype=np.int32)
+    code = np.zeros(6, dtype=np.int32)
+    d.face_nb = nb.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    d.face_code = code.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    assert _create(d) == _lib.TWOLDG_EUNSUP
+    assert b"face table" in _lib.lib().twoldg_last_error()
+    buf = (ctypes.c_double * 16)()
+    du, u = ctypes.cast(buf, ctypes.c_void_p), ctypes.c_void_p(ctypes.addressof(buf) + 64)
+    assert _lib.lib().twoldg_rhs_static(ctypes.byref(d), du, u, 0.0, None) == _lib.TWOLDG_EUNSUP
+    assert b"face table" in _lib.lib().twoldg_last_error()
+    d.face_nb = None
+    d.face_code = None
+    d.metric = 1
+    assert _create(d) == _lib.TWOLDG_EINVAL
+    assert b"needs coef" in _lib.lib().twoldg_last_error()
+    assert _lib.lib().twoldg_rhs_static(ctypes.byref(d), du, u, 0.0, None) == _lib.TWOLDG_EUNSUP
+    d.metric = 5
+    assert _create(d) == _lib.TWOLDG_EINVAL
+    d.metric = 0
+    # a forest past the static array's 16 MiB is refused on the host too:
+    # 1000 blocks of 16^3 in FP64 need two face arrays of 1000 * 6 * 16^2
+    # words, 23.4 MiB
+    g = wave_forest(np.float64, 3, 3, 4, roots=10)
+    d2, keep2 = twoldg.problem.make_desc(g, twoldg.Element(np.float64, 3), True, _lib.F64)
+    assert _lib.lib().twoldg_rhs_static(ctypes.byref(d2), du, u, 0.0, None) == _lib.TWOLDG_EINVAL
+    assert b"16 MiB" in _lib.lib().twoldg_last_error()
+    del keep, keep2

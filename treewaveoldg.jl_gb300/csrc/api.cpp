@@ -165,6 +165,16 @@ struct twoldg_runner {
                 return fail(TWOLDG_EUNSUP, "element order P = " + std::to_string(m.P) + " is not built (1..6)");
             const bool metric = d.coef != nullptr;
             const int full = d.metric == 2 ? 1 : 0;
+            if (d.metric < 0 || d.metric > 2)
+                return fail(TWOLDG_EINVAL, "metric must be 0 (flat), 1 (diagonal) or 2 (full), not " +
+                                               std::to_string(d.metric));
+            if (d.metric == 1 && !d.coef) return fail(TWOLDG_EINVAL, "a diagonal metric (metric = 1) needs coef");
+            // The flat and diagonal kernels read a neighbour's face plane as it
+            // lies (no orientation, no boundary face): an explicit face table
+            // (glued patches, boundary faces) needs the full metric's kernels.
+            if (d.face_nb && !full)
+                return fail(TWOLDG_EUNSUP, "an explicit face table (face_nb) is served by the full metric "
+                                           "(metric = 2) only: a flat or diagonal forest is a brick of roots");
             if (full) {
                 if (m.D != 3) return fail(TWOLDG_EINVAL, "the full metric is three-dimensional");
                 if (!d.coef || !d.elem_slot || !d.bnd_x)

@@ -12,12 +12,16 @@
 //
 // Set-up: the first call on a device (with that device current) looks up
 // the array's device address with cudaGetSymbolAddress and caches it per
-// device, so that first call should come before any stream capture. Every
+// device, so that first call should come before any stream capture. The
+// cached address belongs to the device's primary context: after a
+// cudaDeviceReset the array moves and the cache is stale, so a process that
+// resets a device must not call this entry point on it again. Every
 // call shares the one array per device and overwrites it; nothing in it has
 // to start at zero (each call writes every word it later reads), but calls
 // whose work overlaps on the GPU race on it, so a caller serialises them.
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -51,23 +55,14 @@ extern "C" int twoldg_rhs_static(const twoldg_desc* desc, void* du, const void* 
     (void)t;
     if (!desc || !du || !u) return static_rhs_fail(TWOLDG_EINVAL, "desc, du and u must not be NULL");
     if (du == u) return static_rhs_fail(TWOLDG_EINVAL, "du and u must not alias: the right-hand side never writes u");
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return static_rhs_fail(TWOLDG_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return static_rhs_fail(TWOLDG_EUNSUP, "device ordinal beyond 64");
-    void* base = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_scratch_ptr[dev]) {
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_static_scratch);
-            if (e != cudaSuccess)
-                return static_rhs_fail(TWOLDG_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            g_scratch_ptr[dev] = p;
-        }
-        base = g_scratch_ptr[dev];
-    }
-    if (desc->coef) return static_rhs_fail(TWOLDG_EUNSUP, "twoldg_rhs_static serves flat problems (coef = NULL)");
+    // Only the flat brick: the flat kernels read a neighbour's face plane as it
+    // lies, so a metric or an explicit face table (oriented glues, boundary
+    // faces) would be read wrongly. Checked before any CUDA call.
+    if (desc->coef || desc->metric != 0)
+        return static_rhs_fail(TWOLDG_EUNSUP, "twoldg_rhs_static serves flat problems (coef = NULL, metric = 0)");
+    if (desc->face_nb || desc->face_code)
+        return static_rhs_fail(TWOLDG_EUNSUP, "twoldg_rhs_static serves a brick of roots, not an explicit face "
+                                              "table (face_nb = NULL)");
     Mesh m;
     std::string err;
     if (!build_mesh(*desc, m, err)) return static_rhs_fail(TWOLDG_EINVAL, err);
@@ -100,6 +95,23 @@ extern "C" int twoldg_rhs_static(const twoldg_desc* desc, void* du, const void* 
     if (ops->stage_smem(m.E) > 227 * 1024) {
         delete ops;
         return static_rhs_fail(TWOLDG_EUNSUP, "block too large for one CTA's shared memory");
+    }
+    std::unique_ptr<Ops> own(ops);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return static_rhs_fail(TWOLDG_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return static_rhs_fail(TWOLDG_EUNSUP, "device ordinal beyond 64");
+    void* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (!g_scratch_ptr[dev]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_static_scratch);
+            if (e != cudaSuccess)
+                return static_rhs_fail(TWOLDG_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            g_scratch_ptr[dev] = p;
+        }
+        base = g_scratch_ptr[dev];
     }
     cudaStream_t s = (cudaStream_t)stream;
     unsigned char* p = (unsigned char*)base;
@@ -137,7 +149,6 @@ extern "C" int twoldg_rhs_static(const twoldg_desc* desc, void* du, const void* 
     }
     // The host tables the copies read are staged before cudaMemcpyAsync returns
     // (pageable source), and the kernels took their tables by value, so both
-    // may go now; the work itself stays queued on `stream`.
-    delete ops;
+    // may go now (with `own`); the work itself stays queued on `stream`.
     return rc;
 }
