@@ -73,6 +73,7 @@ def test_reference_arm_line_keeps_the_contract():
     assert d["value"] > 0 and d["unit"] == "node-steps/s" and d["higher_is_better"] is True
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
     assert d["cpu_baseline"]["value"] == d["value"]
+    assert d["cpu_baseline"]["same_config"] is True
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert "workload" in d["config"]
 
