@@ -3,20 +3,27 @@
 Workload (default): the 3D periodic uniform forest, P = 3, E = 4, roots = 16
 (4096 blocks of 16^3, 256^3 = 16.8M nodes), the standing sine mode with
 wavenumbers (1, 2, 3), dt = 0.5 h/(P+1), h = 1/256. A step is one RK4 step
-of the whole forest (4 fused stage launches replayed from a CUDA graph).
+of the whole forest (4 fused stage launches replayed from a CUDA graph);
+the value is the median of --repeats timed regions of exactly --steps steps.
 
 Arms: the plain FP64 path (the drop-in) and the FP32-field path with FP64
 energy/time and compensated (two-sum) RK accumulation, the headline
 `value`. Both run 100 steps from the same initial data outside the timed
 region to state the L2 / Linf error against the exact solution and against
-the FP64 run, and the energy drift.
+the FP64 run, and the energy drift. Beside them the line carries the other
+configurations as sub-objects: the 512-problem 2D ensemble (`batched`), the
+nested reflecting box (`nested`), the thirteen-patch benchmark ball
+(`ball13`), the 2D quarter-period box (`c1`) and the seven-patch ball
+(`ball7`, and at the reference's own plane wave `ball7_reference_wave`),
+each with both precisions, and the kernels around the stage kernel with
+their achieved bandwidth (`aux_kernels`).
 
---impl reference times the reference's CPU algorithm (the C oracle port,
-all host threads) on a bounded sample of the same workload; the reference
-itself is Julia and is not installed on this machine.
+--impl reference times the reference's CPU data flow (oracle/refcpu.c, a C
+restatement held to the oracle; all host threads) on the same 256^3 box;
+the reference itself is Julia and is not installed on this machine.
 
 Under torchrun (N > 1) every rank runs an independent replica (the path
-does not shard on one box: replicas only), a barrier brackets the timed
+does not shard on one box: replicas only), a barrier brackets each timed
 region, and the time is the max over ranks.
 """
 import argparse
@@ -51,6 +58,10 @@ def parse():
                     help="comma list of the precisions to run; the headline needs f32c (profiling runs one)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="leave out the nested box, the benchmark ball and the small configurations")
+    ap.add_argument("--repeats", type=int, default=10,
+                    help="timed regions of exactly --steps steps each; the median is the value")
     ap.add_argument("--ball-roots", default="4,4,44",
                     help="ball13: the roots (n, m, m') of the thirteen-patch ball (the benchmark ball's 4,4,44; "
                          "a smaller m' for profiling)")
@@ -141,11 +152,14 @@ class Clocks:
 WORKLOAD = "box256"
 TUNE = True
 KERNEL_NAMES = {1: "stage3r_kernel", 2: "stage_kernel_c", 3: "stage_kernel"}
+# algorithmic bytes per node-step: 34 words (+4 compensation words for f32c)
+BYTES_NS = {"f64": 272.0, "f32c": 152.0}
 
 
-def c2_problem(twoldg, roots, precision):
+def box_problem(twoldg, workload, roots, precision):
+    """The 256^3 periodic box (P = 3, E = 4) or the nested reflecting box."""
     dtype = np.float64 if precision == "f64" else np.float32
-    if WORKLOAD == "nested":
+    if workload == "nested":
         forest = twoldg.wave_forest(dtype, 3, 3, 2, roots=8, reflecting=True,
                                     refined=twoldg.nested_cubes(3, 1 / 8, 3))
     else:
@@ -154,8 +168,8 @@ def c2_problem(twoldg, roots, precision):
     return forest, p
 
 
-def c2_initial(x, var, T):
-    if WORKLOAD == "nested":
+def box_initial(workload, x, var, T):
+    if workload == "nested":
         r2 = sum((x[d] - T(0.5)) ** 2 for d in range(3))
         u = np.exp(-r2 / T(0.05) ** 2).astype(T)
         return u if var == 1 else np.zeros_like(u)
@@ -164,51 +178,71 @@ def c2_initial(x, var, T):
     return u if var == 1 else np.zeros_like(u)
 
 
-def c2_exact(x, var, t, T):
-    if WORKLOAD == "nested":
+def c2_initial(x, var, T):
+    return box_initial("box256", x, var, T)
+
+
+def box_exact(workload, x, var, t, T):
+    if workload == "nested":
         return None  # no closed form: errors are stated against the FP64 run
     om = 2 * math.pi * math.sqrt(14.0)
     s = np.sin(2 * math.pi * x[0]) * np.sin(4 * math.pi * x[1]) * np.sin(6 * math.pi * x[2])
     return (math.cos(om * t) * s if var == 1 else -om * math.sin(om * t) * s).astype(T)
 
 
-def run_arm(twoldg, torch, precision, roots, steps, warmup, clocks_index):
+def timed_regions(twoldg, torch, p, u, dt, steps, repeats, clocks_index, t0=0.0):
+    """`repeats` timed regions of exactly `steps` RK4 steps each, every one
+    bracketed by a barrier and a device synchronisation and timed with CUDA
+    events on the library's own stream (max over ranks), the clock sampler
+    running through all of them. Returns (per-region ms, clock summary)."""
+    lib = twoldg._lib.lib()
+    ptr = ctypes.c_void_p(u.data_ptr())
+    stream = torch.cuda.ExternalStream(lib.twoldg_stream(p.handle))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times = []
+    with Clocks(clocks_index) as clk:
+        for r in range(repeats):
+            barrier()
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ptr, t0 + r * steps * dt, dt, steps))
+            ev1.record(stream)
+            ev1.synchronize()
+            torch.cuda.synchronize()
+            times.append(max_over_ranks(ev0.elapsed_time(ev1)))
+    return times, clk.summary()
+
+
+def run_arm(twoldg, torch, precision, roots, steps, warmup, clocks_index, workload=None, repeats=10):
+    workload = workload or WORKLOAD
     T = np.float64 if precision == "f64" else np.float32
-    forest, p = c2_problem(twoldg, roots, precision)
-    u0 = twoldg.initial_state(p, lambda x, var: c2_initial(x, var, T))
+    forest, p = box_problem(twoldg, workload, roots, precision)
+    u0 = twoldg.initial_state(p, lambda x, var: box_initial(workload, x, var, T))
     dt = 0.5 * forest.minimum_spacing() / 4
     lib = twoldg._lib.lib()
     u = u0.clone()
     ptr = ctypes.c_void_p(u.data_ptr())
-    stream = torch.cuda.ExternalStream(lib.twoldg_stream(p.handle))
     torch.cuda.synchronize()
     layout = p.autotune(u, dt) if TUNE else {}
     twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ptr, 0.0, dt, warmup))
     p.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    torch.cuda.synchronize()
-    with Clocks(clocks_index) as clk:
-        ev0.record(stream)
-        twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ptr, 0.0, dt, steps))
-        ev1.record(stream)
-        ev1.synchronize()
-    torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1)
-    ms = max_over_ranks(ms)
-    # per-stage launch durations (events between the stage launches)
+    times, clocks = timed_regions(twoldg, torch, p, u, dt, steps, repeats, clocks_index)
+    ms = float(np.median(times))
+    # per-stage launch durations (the four stages launched one by one with
+    # events between them, outside the step's graph)
     st = (ctypes.c_float * 4)()
     prof = []
     for _ in range(5):
         twoldg._lib.check(lib.twoldg_profile_step(p.handle, ptr, dt, st))
         prof.append(list(st))
     stage_ms = np.min(np.array(prof), axis=0)
-    return dict(forest=forest, p=p, u0=u0, dt=dt, ms=ms, stage_ms=stage_ms, clocks=clk.summary(),
-                nodes=p.state_words // 2, layout=layout)
+    return dict(forest=forest, p=p, u0=u0, dt=dt, ms=ms, region_ms=times, stage_ms=stage_ms, clocks=clocks,
+                nodes=p.state_words // 2, layout=layout, workload=workload, u=u)
 
 
 def accuracy(twoldg, torch, arm, nsteps, ref64=None):
     p, T = arm["p"], arm["p"].dtype.type
+    workload = arm["workload"]
     u = arm["u0"].clone()
     if p.precision == "f32c":
         twoldg._lib.check(twoldg._lib.lib().twoldg_reset_compensation(p.handle))
@@ -219,14 +253,77 @@ def accuracy(twoldg, torch, arm, nsteps, ref64=None):
     e1 = twoldg.wave_energy(p, u)
     t = nsteps * arm["dt"]
     out = dict(energy_drift=abs(e1 - e0) / e0, steps=nsteps)
-    if WORKLOAD != "nested":
-        ue = p.to_device(p.fill_at_nodes(lambda x, var: c2_exact(x, var, t, T)))
+    if workload != "nested":
+        ue = p.to_device(p.fill_at_nodes(lambda x, var: box_exact(workload, x, var, t, T)))
         out.update(l2=twoldg.quadrature_norm(p, u, 2, ref=ue), linf=twoldg.quadrature_norm(p, u, math.inf, ref=ue))
     if ref64 is not None:
         r = ref64.to(u.dtype)
         out["l2_vs_fp64"] = twoldg.quadrature_norm(p, u, 2, ref=r)
         out["linf_vs_fp64"] = twoldg.quadrature_norm(p, u, math.inf, ref=r)
     return out, u
+
+
+def aux_kernels(twoldg, arm, hbm, reps=5):
+    """Achieved HBM bandwidth of the kernels around the stage kernel, one
+    launch each, timed with CUDA events on the library's stream
+    (twoldg_profile_kernels; least of `reps`), against their algorithmic
+    bytes: the face export reads P+1 planes per face and writes two
+    (u's face node and the own element's part of its wide derivative), the
+    energy reads u and v (2 words a node), the norm of u - ref reads both
+    states (4), the indicator's peak reads u (1), the modal indicator reads u
+    (1) and writes one word per element, the truncation reads and writes v
+    (2). Coarse-fine ghosts (nested forests only) are reported as time."""
+    lib = twoldg._lib.lib()
+    p, u = arm["p"], arm["u"]
+    W = 8 if p.precision == "f64" else 4
+    forest = arm["forest"]
+    N, D, P = forest.N, forest.D, 3
+    nb, nodes = len(forest.leaves), arm["nodes"]
+    F = N ** (D - 1)
+    ms = (ctypes.c_float * 7)()
+    best = [math.inf] * 7
+    for _ in range(reps):
+        twoldg._lib.check(lib.twoldg_profile_kernels(p.handle, ctypes.c_void_p(u.data_ptr()), ms, 7))
+        best = [min(a, b) for a, b in zip(best, ms)]
+    E = N // (P + 1)
+    alg = {"export_faces_kernel": W * nb * 2 * D * F * (P + 1 + 2),
+           "energy_kernel": W * nodes * 2, "norm_kernel": W * nodes * 4, "maxabs_kernel": W * nodes,
+           "mode_kernel": W * (nodes + nb * E ** D), "truncate_kernel": W * nodes * 2}
+    names = ["export_faces_kernel", "cf_ghost_u/g_kernel", "energy_kernel", "norm_kernel", "maxabs_kernel",
+             "mode_kernel", "truncate_kernel"]
+    out = {}
+    for k, name in enumerate(names):
+        t = best[k]
+        if name in alg:
+            gbs = alg[name] / (t / 1e3) / 1e9
+            out[name] = {"us": t * 1e3, "algorithmic_bytes": alg[name], "achieved_gbs": gbs, "frac": gbs / hbm}
+        elif t > 0:
+            out[name] = {"us": t * 1e3, "bound": "latency (coarse-fine face planes only)"}
+    return out
+
+
+def box_object(twoldg, torch, workload, roots, steps, warmup, accuracy_steps, repeats, clocks_index, hbm):
+    """Both arms of a box workload, as a sub-object of the bench line: value
+    (FP32 + compensated), FP64 beside it, the roofline, accuracy against the
+    FP64 run and the energy drift, and the auxiliary kernels' bandwidth."""
+    arms = {prec: run_arm(twoldg, torch, prec, roots, steps, warmup, clocks_index, workload, repeats)
+            for prec in ("f64", "f32c")}
+    acc64, u64 = accuracy(twoldg, torch, arms["f64"], accuracy_steps)
+    acc32 = accuracy(twoldg, torch, arms["f32c"], accuracy_steps, ref64=u64)[0]
+    out = {}
+    for prec, a in arms.items():
+        mps = a["ms"] / steps
+        ach = BYTES_NS[prec] * a["nodes"] / (mps / 1e3) / 1e9
+        out[prec] = {"value": a["nodes"] * steps / (a["ms"] / 1e3), "ms_per_step": mps,
+                     "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm},
+                     "stage_ms": [float(x) for x in a["stage_ms"]], "clocks": a["clocks"],
+                     "aux_kernels": aux_kernels(twoldg, a, hbm)}
+    out["f64"]["accuracy"], out["f32c"]["accuracy"] = acc64, acc32
+    out["nodes"] = arms["f32c"]["nodes"]
+    out["blocks"] = len(arms["f32c"]["forest"].leaves)
+    out["steps"], out["repeats"] = steps, repeats
+    out["speedup_f32c_vs_f64"] = out["f32c"]["value"] / out["f64"]["value"]
+    return out
 
 
 def e2e(twoldg, torch, arm, steps):
@@ -304,7 +401,9 @@ def batched(twoldg, torch, steps, warmup, accuracy_steps, n=512):
         b.rk4_step(u, dts, steps)
         b.synchronize()
         sec = time.perf_counter() - t0
-        out[prec] = {"value": b.nodes * steps / sec, "ms_per_step": sec * 1e3 / steps}
+        ach = BYTES_NS[prec] * b.nodes * steps / sec / 1e9
+        out[prec] = {"value": b.nodes * steps / sec, "ms_per_step": sec * 1e3 / steps,
+                     "achieved_gbs": ach}
         if accuracy_steps:
             v = u0.clone()
             b.rk4_step(v, dts, accuracy_steps)
@@ -322,10 +421,13 @@ def batched(twoldg, torch, steps, warmup, accuracy_steps, n=512):
 
 
 # --- the small configurations: whole runs to t_end, FP64 against FP32 + compensated ---------
-def small_problem(twoldg, prec):
-    """(problem, u0, dt, nsteps, t_end, exact(t) -> device state) of the c1 or ball workload."""
+def small_problem(twoldg, prec, workload=None):
+    """(problem, u0, dt, nsteps, t_end, exact(t) -> device state) of the c1 or
+    ball workload; ball_ref is the seven-patch ball at the reference's own
+    plane wave, k = (1.1, -0.7, 0.5), to t = 1 (src/sevenpatch.jl:84-117)."""
+    workload = workload or WORKLOAD
     T = np.float64 if prec == "f64" else np.float32
-    if WORKLOAD == "c1":
+    if workload == "c1":
         forest = twoldg.wave_forest(T, 2, 4, 2, roots=8)
         p = twoldg.WaveProblem(forest, twoldg.Element(T, 4), precision=prec)
         u0 = twoldg.initial_state(p, twoldg.wave_exact(2, 1.0, 1, 0.0, T))
@@ -336,10 +438,14 @@ def small_problem(twoldg, prec):
     else:
         forest, geo = twoldg.sevenpatch_forest(T, 3, 2, roots=(4, 4), Lc=1.0, R1=3.0)
         k = np.array([1.1, -0.7, 0.5])
-        wave = twoldg.PlaneWave(2 * math.pi * k / np.linalg.norm(k), 0.3)
+        if workload == "ball_ref":
+            wave = twoldg.PlaneWave(k, 0.3)
+            t_end, cfl = 1.0, 0.5
+        else:
+            wave = twoldg.PlaneWave(2 * math.pi * k / np.linalg.norm(k), 0.3)
+            t_end, cfl = 6.0, 0.5
         p = twoldg.WaveProblem(forest, twoldg.Element(T, 3), geometry=geo, boundary=wave, precision=prec)
         u0 = twoldg.initial_state(p, twoldg.sevenpatch_exact(geo, wave, 0.0))
-        t_end, cfl = 6.0, 0.5
 
         def exact(t):
             return p.to_device(p.fill_at_nodes(twoldg.sevenpatch_exact(geo, wave, t)))
@@ -348,20 +454,29 @@ def small_problem(twoldg, prec):
     return p, u0, dt, nsteps, float(T(t_end)), exact
 
 
-def small_config(args, twoldg, torch):
+SMALL_NAMES = {
+    "c1": "2D periodic box, P=4, E=2, roots=8 (6400 nodes), sin(2 pi x) sin(2 pi y) to a quarter period at CFL 0.25",
+    "ball": "seven-patch ball, P=3, E=2, roots=(4,4), Lc=1, R1=3 (%d nodes), plane wave |k|=2 pi along "
+            "(1.1,-0.7,0.5), phi=0.3, Dirichlet sphere, to t=6 at CFL 0.5",
+    "ball_ref": "seven-patch ball, P=3, E=2, roots=(4,4), Lc=1, R1=3 (%d nodes), the reference's plane wave "
+                "k=(1.1,-0.7,0.5), phi=0.3, Dirichlet sphere, to t=1 at CFL 0.5",
+}
+
+
+def small_run(twoldg, torch, workload, reps):
     """Both arms of a small configuration: node-steps/s of the whole run to
-    t_end (CUDA events on the library's stream, after a warm-up run), the L2
-    and Linf errors against the exact solution and against the FP64 run, and
-    the energy drift."""
+    t_end (CUDA events on the library's stream, least of `reps` runs after a
+    warm-up run), the L2 and Linf errors against the exact solution and
+    against the FP64 run, and the energy drift."""
     lib = twoldg._lib.lib()
     arms, final = {}, {}
     for prec in ("f64", "f32c"):
-        p, u0, dt, nsteps, t_end, exact = small_problem(twoldg, prec)
+        p, u0, dt, nsteps, t_end, exact = small_problem(twoldg, prec, workload)
         u = u0.clone()
         layout = p.autotune(u, dt) if TUNE else {}
         stream = torch.cuda.ExternalStream(lib.twoldg_stream(p.handle))
         best = math.inf
-        for rep in range(1 + max(1, args.steps // 50)):
+        for rep in range(1 + reps):
             u = u0.clone()
             if prec == "f32c":
                 twoldg._lib.check(lib.twoldg_reset_compensation(p.handle))
@@ -379,6 +494,8 @@ def small_config(args, twoldg, torch):
         arms[prec] = {"value": nodes * nsteps / (best / 1e3), "ms_per_step": best / nsteps, "nsteps": nsteps,
                       "nodes": nodes, "layout": layout,
                       "l2": twoldg.quadrature_norm(p, u, 2, ref=ue),
+                      "l2u": twoldg.quadrature_norm(p, u, 2, vars=(1,), ref=ue),
+                      "l2v": twoldg.quadrature_norm(p, u, 2, vars=(2,), ref=ue),
                       "linf": twoldg.quadrature_norm(p, u, math.inf, ref=ue),
                       "energy_drift": abs(e1 - e0) / abs(e0)}
         final[prec] = (p, u)
@@ -386,31 +503,37 @@ def small_config(args, twoldg, torch):
     r = final["f64"][1].to(u32.dtype)
     arms["f32c"]["l2_vs_fp64"] = twoldg.quadrature_norm(p32, u32, 2, ref=r)
     arms["f32c"]["linf_vs_fp64"] = twoldg.quadrature_norm(p32, u32, math.inf, ref=r)
-    head = arms["f32c"]
-    name = ("2D periodic box, P=4, E=2, roots=8 (6400 nodes), sin(2 pi x) sin(2 pi y) to a quarter period at "
-            "CFL 0.25" if WORKLOAD == "c1" else
-            "seven-patch ball, P=3, E=2, roots=(4,4), Lc=1, R1=3 (%d nodes), plane wave |k|=2 pi, phi=0.3, "
-            "Dirichlet sphere, to t=6 at CFL 0.5" % head["nodes"])
+    name = SMALL_NAMES[workload]
+    if "%d" in name:
+        name = name % arms["f32c"]["nodes"]
+    return {"workload": name, "fp64": arms["f64"], "f32c": arms["f32c"],
+            "speedup_f32c_vs_f64": arms["f32c"]["value"] / arms["f64"]["value"],
+            "l2_flush": "none: the state fits in L2 (a whole run to t_end is timed)"}
+
+
+def small_config(args, twoldg, torch):
+    res = small_run(twoldg, torch, WORKLOAD, max(1, args.steps // 50))
+    head = res["f32c"]
     line = {"metric": METRIC, "value": head["value"], "unit": "node-steps/s", "n_gpus": 1,
             "steps": head["nsteps"], "warmup": 1, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": name, "precision": "f32c",
-                       "l2_flush": "none: the state fits in L2 (a whole run to t_end is timed)"},
-            "fp64": arms["f64"], "f32c": arms["f32c"], "speedup_vs_fp64": head["value"] / arms["f64"]["value"],
+            "config": {"workload": res["workload"], "precision": "f32c", "l2_flush": res["l2_flush"]},
+            "fp64": res["fp64"], "f32c": res["f32c"], "speedup_vs_fp64": res["speedup_f32c_vs_f64"],
             "roofline": None, "gpu_launches": None}
     print(json.dumps(line))
 
 
-def ball_benchmark(args, twoldg, torch):
+def ball13_run(twoldg, torch, roots, steps, warmup, repeats=3):
     """The reference's benchmark ball (bin/ball_benchmark.jl): the
     thirteen-patch ball of 4672 blocks of 16^3 (roots (4, 4, 44), Lc = 4,
     Rm = 12, R1 = 100), P = 3, Sommerfeld's radiative sphere, truncation on,
-    the state sin(1), sin(2), ... truncated; K RK4 steps at cfl 1/2 timed with
-    CUDA events on the library's stream, FP64 and FP32 + compensated, and the
-    FP32 run's L2 distance from the FP64 one after the warm-up and timed steps."""
+    the state sin(1), sin(2), ... truncated; `repeats` timed regions of
+    `steps` RK4 steps at cfl 1/2 with CUDA events on the library's stream,
+    FP64 and FP32 + compensated, and the FP32 run's L2 distance from the FP64
+    one and the two energies after the warm-up and timed steps."""
     lib = twoldg._lib.lib()
-    roots = tuple(int(x) for x in args.ball_roots.split(","))
     forest, geo = twoldg.thirteenpatch_forest(np.float64, 3, 4, roots=roots, Lc=4.0, Rm=12.0, R1=100.0)
+    hbm, _ = peaks()
     arms, final = {}, {}
     for prec in ("f64", "f32c"):
         T = np.float64 if prec == "f64" else np.float32
@@ -418,43 +541,53 @@ def ball_benchmark(args, twoldg, torch):
                                precision=prec)
         u = torch.from_numpy(np.sin(np.arange(1, p.state_words + 1, dtype=np.float64)).astype(T)).cuda()
         twoldg.truncate_state(u, p)
+        e0 = twoldg.wave_energy(p, u, t=0.0)
         dt = float(twoldg.oldg_timestep(p, 0.5))
         ptr = ctypes.c_void_p(u.data_ptr())
-        stream = torch.cuda.ExternalStream(lib.twoldg_stream(p.handle))
         torch.cuda.synchronize()
-        twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ptr, 0.0, dt, args.warmup))
+        twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ptr, 0.0, dt, warmup))
         p.synchronize()
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with Clocks(0) as clk:
-            ev0.record(stream)
-            twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ptr, args.warmup * dt, dt, args.steps))
-            ev1.record(stream)
-            ev1.synchronize()
-        ms = ev0.elapsed_time(ev1)
+        times, clocks = timed_regions(twoldg, torch, p, u, dt, steps, repeats, 0, t0=warmup * dt)
+        ms = float(np.median(times))
         nodes = p.state_words // 2
         st = (ctypes.c_float * 4)()
         v = u.clone()
         twoldg._lib.check(lib.twoldg_profile_step(p.handle, ctypes.c_void_p(v.data_ptr()), dt, st))
-        arms[prec] = {"value": nodes * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
-                      "ns_per_node_step": ms * 1e6 / args.steps / nodes, "stage_ms": [float(x) for x in st],
-                      "nodes": nodes, "dt": dt, "clocks": clk.summary()}
+        t1 = (warmup + repeats * steps) * dt
+        mps = ms / steps
+        ach = BYTES_NS[prec] * nodes / (mps / 1e3) / 1e9
+        arms[prec] = {"value": nodes * steps / (ms / 1e3), "ms_per_step": mps,
+                      "ns_per_node_step": mps * 1e6 / nodes, "stage_ms": [float(x) for x in st],
+                      "nodes": nodes, "dt": dt, "clocks": clocks,
+                      "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                                   "note": "the survey's algorithmic bytes of the flat step; the full metric reads "
+                                           "fluxes and sqrt(g) besides"},
+                      "energy0": e0, "energy": twoldg.wave_energy(p, u, t=t1)}
         final[prec] = (p, u)
-        if prec == "f32c":
-            p32, u32 = p, u
+    p32, u32 = final["f32c"]
     r = final["f64"][1].to(torch.float32)
     arms["f32c"]["l2_vs_fp64"] = float(twoldg.quadrature_norm(p32, u32, 2, ref=r))
-    head = arms["f32c"]
+    arms["f32c"]["energy_vs_fp64"] = abs(arms["f32c"]["energy"] - arms["f64"]["energy"]) / arms["f64"]["energy"]
+    return {"workload": "the benchmark ball: thirteen-patch, roots %s, E=4, P=3, Lc=4, Rm=12, R1=100 (%d blocks "
+                        "of 16^3, %d nodes), Sommerfeld radiative sphere, truncation on, state sin(1..n) truncated, "
+                        "cfl 1/2" % (roots, forest.nleaves(), arms["f32c"]["nodes"]),
+            "fp64": arms["f64"], "f32c": arms["f32c"], "steps": steps, "repeats": repeats,
+            "speedup_f32c_vs_f64": arms["f32c"]["value"] / arms["f64"]["value"],
+            "reference_h200_ns_per_node_step": {"f64": 2.84, "f32": 1.92, "source": "CODE.md:5108-5122"},
+            "gpu_launches_per_step": 9}
+
+
+def ball_benchmark(args, twoldg, torch):
+    roots = tuple(int(x) for x in args.ball_roots.split(","))
+    res = ball13_run(twoldg, torch, roots, args.steps, args.warmup, repeats=1)
+    head = res["f32c"]
     line = {"metric": METRIC, "value": head["value"], "unit": "node-steps/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "the benchmark ball: thirteen-patch, roots %s, E=4, P=3, Lc=4, Rm=12, "
-                                   "R1=100 (%d blocks of 16^3, %d nodes), Sommerfeld radiative sphere, "
-                                   "truncation on, state sin(1..n) truncated, cfl 1/2"
-                                   % (roots, forest.nleaves(), head["nodes"]),
-                       "precision": "f32c", "l2_flush": "inputs larger than L2"},
-            "fp64": arms["f64"], "f32c": arms["f32c"], "speedup_vs_fp64": head["value"] / arms["f64"]["value"],
-            "reference_h200_ns_per_node_step": {"f64": 2.84, "f32": 1.92, "source": "CODE.md:5108-5122"},
-            "clocks": head["clocks"], "roofline": None, "gpu_launches": 1 + 9 * args.steps}
+            "config": {"workload": res["workload"], "precision": "f32c", "l2_flush": "inputs larger than L2"},
+            "fp64": res["fp64"], "f32c": res["f32c"], "speedup_vs_fp64": res["speedup_f32c_vs_f64"],
+            "reference_h200_ns_per_node_step": res["reference_h200_ns_per_node_step"],
+            "clocks": head["clocks"], "roofline": head["roofline"], "gpu_launches": 1 + 9 * args.steps}
     print(json.dumps(line))
 
 
@@ -769,11 +902,28 @@ def main():
             line["cpu_baseline"] = tr["cpu_baseline"]
         print(json.dumps(line))
         return
+    if WORKLOAD == "nested":
+        hbm, _ = peaks()
+        obj = box_object(twoldg, torch, "nested", 8, args.steps, args.warmup, args.accuracy_steps, args.repeats,
+                         local, hbm)
+        head = obj["f32c"]
+        line = {"metric": METRIC, "value": head["value"], "unit": "node-steps/s", "n_gpus": 1, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "3D reflecting box, nested cubes 1/8, 1/4, 1/2 (3 levels), P=3, E=2, roots=8 "
+                                       "(%d blocks, %d nodes), Gaussian pulse, FP32 fields + compensated RK4"
+                                       % (obj["blocks"], obj["nodes"]), "precision": "f32c",
+                           "l2_flush": "none: the state fits in L2"},
+                "nested": obj, "roofline": head["roofline"], "clocks": head["clocks"],
+                "gpu_launches": None}
+        print(json.dumps(line))
+        return
     arms = {}
     wanted = args.arms.split(",")
     for prec in ("f64", "f32c"):
         if prec in wanted:
-            arms[prec] = run_arm(twoldg, torch, prec, args.roots, args.steps, args.warmup, local)
+            arms[prec] = run_arm(twoldg, torch, prec, args.roots, args.steps, args.warmup, local,
+                                 repeats=args.repeats)
     if set(wanted) != {"f64", "f32c"}:
         # a partial run (profiling): report the arms' times only
         if rank() == 0:
@@ -791,45 +941,63 @@ def main():
     hbm, peak_kind = peaks()
     head = arms["f32c"]
     nodes = head["nodes"]
-    value = nodes * args.steps / (head["ms"] / 1e3) * world()
-    v64 = nodes * args.steps / (arms["f64"]["ms"] / 1e3) * world()
-    # algorithmic bytes per node-step: 34 words (+4 compensation words for f32c)
-    bytes_ns = {"f64": 272.0, "f32c": 152.0}
+    mps = head["ms"] / args.steps
+    value = nodes / (mps / 1e3) * world()
+    v64 = nodes / (arms["f64"]["ms"] / args.steps / 1e3) * world()
+    # the stage kernel's average launch over the timed region: a step is its
+    # four launches back to back in the step's graph (and one face export per
+    # rk4_step call), so a launch averages a quarter of a step
+    achieved = BYTES_NS["f32c"] * nodes / (mps / 1e3) / 1e9
+    ach64 = BYTES_NS["f64"] * nodes / (arms["f64"]["ms"] / args.steps / 1e3) / 1e9
     stage = head["stage_ms"]
-    achieved = bytes_ns["f32c"] * nodes / 4 / (float(np.mean(stage)) / 1e3) / 1e9
     traffic = traffic_from_profiles("f32c")
     chosen = next(iter(head["layout"].values()), {"kernel": 1})
-    kname = "%s (3D, P=3, E=%d, float, compensated)" % (KERNEL_NAMES.get(chosen["kernel"], "stage3r_kernel"),
-                                                         2 if WORKLOAD == "nested" else 4)
+    kname = "%s (3D, P=3, E=4, float, compensated)" % KERNEL_NAMES.get(chosen["kernel"], "stage3r_kernel")
     line = {
         "metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world(), "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": head["ms"] / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": mps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": ("3D periodic uniform forest, P=3, E=4, roots=%d (%d blocks of 16^3, %d nodes), "
-                                "standing sine mode (1,2,3), dt=0.5h/(P+1), FP32 fields + compensated RK4"
-                                % (args.roots, len(head["forest"].leaves), nodes)) if WORKLOAD != "nested" else
-                               ("3D reflecting box, nested cubes 1/8, 1/4, 1/2 (3 levels), P=3, E=2, roots=8 (%d blocks "
-                                "of 8^3, %d nodes), Gaussian pulse exp(-r^2/0.05^2), dt=0.5h_min/(P+1), FP32 fields + "
-                                "compensated RK4" % (len(head["forest"].leaves), nodes)),
+        "config": {"workload": "3D periodic uniform forest, P=3, E=4, roots=%d (%d blocks of 16^3, %d nodes), "
+                               "standing sine mode (1,2,3), dt=0.5h/(P+1), FP32 fields + compensated RK4"
+                               % (args.roots, len(head["forest"].leaves), nodes),
                    "precision": "f32c", "parallelism": "replicas" if world() > 1 else "single",
-                   "l2_flush": "inputs larger than L2 (state %.0f MB + stage scratch)" % (nodes * 8 / 1e6)},
-        "fp64": {"value": v64, "ms_per_step": arms["f64"]["ms"] / args.steps,
+                   "l2_flush": "inputs larger than L2 (state %.0f MB + stage scratch)" % (nodes * 8 / 1e6),
+                   "timing": "median of %d timed regions of exactly %d RK4 steps each (CUDA events on the "
+                             "library's stream, barrier and synchronisation around each)" % (args.repeats, args.steps)},
+        "region_ms": head["region_ms"],
+        "fp64": {"value": v64, "ms_per_step": arms["f64"]["ms"] / args.steps, "region_ms": arms["f64"]["region_ms"],
                  "stage_ms": [float(x) for x in arms["f64"]["stage_ms"]],
-                 "roofline_frac": bytes_ns["f64"] * nodes / 4 / (float(np.mean(arms["f64"]["stage_ms"])) / 1e3)
-                 / 1e9 / hbm, "layout": arms["f64"]["layout"],
+                 "roofline_frac": ach64 / hbm, "layout": arms["f64"]["layout"],
+                 "aux_kernels": aux_kernels(twoldg, arms["f64"], hbm),
                  "bound": "the FP64 pipe, not HBM (ncu: 84% FP64-pipe activity per stage, "
                           "profiles/stage3r_f64_256cube.md); roofline_frac is the HBM fraction"},
         "speedup_vs_fp64": value / v64,
         "accuracy": {"fp64": acc64, "f32c": acc32},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_kind": peak_kind, "kernel": kname, "layout": head["layout"],
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per stage launch, profiles/stage3r_f32c_256cube.md",
-                     "stage_ms": [float(x) for x in stage]},
+                     "achieved_from": "the timed region: 152 B/node-step x nodes / ms_per_step, i.e. the survey's "
+                                      "algorithmic bytes per stage launch over the average launch (a quarter step)",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per stage launch, "
+                                       "profiles/stage3r_f32c_256cube.md",
+                     "stage_ms": [float(x) for x in stage],
+                     "stage_ms_source": "twoldg_profile_step: the four stages launched one by one outside the "
+                                        "step's graph with events between them; their sum exceeds the graph's step "
+                                        "by the launch gaps the graph removes"},
+        "aux_kernels": aux_kernels(twoldg, head, hbm),
         "clocks": head["clocks"],
         "e2e": ee,
         "batched": bat,
-        "gpu_launches": 1 + 4 * args.steps,
+        "gpu_launches": args.repeats * (1 + 4 * args.steps),
     }
+    if not args.no_extra:
+        line["nested"] = box_object(twoldg, torch, "nested", 8, 100, args.warmup, args.accuracy_steps, 5, local, hbm)
+        line["nested"]["workload"] = ("3D reflecting box, nested cubes 1/8, 1/4, 1/2 (3 levels), P=3, E=2, roots=8 "
+                                      "(8^3 blocks), Gaussian pulse exp(-r^2/0.05^2), dt=0.5h_min/(P+1); the state "
+                                      "fits in L2, so the roofline bounds it from above only")
+        line["ball13"] = ball13_run(twoldg, torch, (4, 4, 44), 20, args.warmup, repeats=3)
+        line["c1"] = small_run(twoldg, torch, "c1", 2)
+        line["ball7"] = small_run(twoldg, torch, "ball", 2)
+        line["ball7_reference_wave"] = small_run(twoldg, torch, "ball_ref", 1)
     if rank() == 0 and world() == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(5)
     if rank() == 0:

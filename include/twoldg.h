@@ -205,6 +205,17 @@ int twoldg_mode_amplitude(twoldg_problem* p, const void* u, int32_t var, int32_t
  * without the graph, with CUDA events between the four stages, and returns
  * each stage's duration in milliseconds (stage_ms[4]). Synchronous. */
 int twoldg_profile_step(twoldg_problem* p, void* u, double dt, float* stage_ms);
+/* Diagnostics (no reference counterpart): times, with CUDA events on the
+ * problem's stream, one launch each of the kernels around the stage kernel,
+ * on the state u (not changed): ms[0] the face export (export_faces_kernel),
+ * ms[1] the coarse-fine ghosts (cf_ghost_u/g_kernel; 0 without coarse-fine
+ * faces), ms[2] the energy's reduction (energy_kernel, after that export),
+ * ms[3] the norm of u - u (norm_kernel, p = 2, both variables), ms[4] the
+ * indicator's peak (maxabs_kernel, u), ms[5] the modal indicator up to mode
+ * max(P - 1, 1) (mode_kernel, u), ms[6] the truncation of a copy of u
+ * (truncate_kernel). n must be at least 7. Flat and diagonal problems only.
+ * Synchronous. */
+int twoldg_profile_kernels(twoldg_problem* p, const void* u, float* ms, int32_t n);
 /* The extraction's gather (sphere_values / plane_values, src/extraction.jl:
  * 216-245): out[j] = sum_q weights[q + nper j] * u[index[q + nper j] + (var-1)
  * N^D] for j < npoints, the element polynomials of variable var (1: u, 2: v)

@@ -1010,6 +1010,55 @@ int twoldg_profile_step(twoldg_problem* p, void* u, double dt, float* stage_ms) 
 
 void* twoldg_stream(twoldg_problem* p) { return p ? (void*)p->stream : nullptr; }
 
+int twoldg_profile_kernels(twoldg_problem* p, const void* u, float* ms, int32_t n) {
+    if (!p || !u || !ms) return fail(TWOLDG_EINVAL, "NULL argument");
+    if (n < 7) return fail(TWOLDG_EINVAL, "ms must hold 7 durations");
+    Group& g = *p->groups[0];
+    if (g.full) return fail(TWOLDG_EUNSUP, "the kernels timed here are the flat and diagonal ones");
+    const BlockItem* items = (const BlockItem*)g.d_items.p;
+    const int nitems = (int)g.items.size();
+    // the truncation acts on a copy in the stage buffer, so u is not changed
+    CK(cudaMemcpyAsync(p->y.p, u, (size_t)p->total_words * p->wsize, cudaMemcpyDeviceToDevice, p->stream));
+    const int mode = p->P > 1 ? p->P - 1 : 1;
+    std::vector<int> modes(mode);
+    std::vector<double> w(mode), pw(mode);
+    for (int m = 1; m <= mode; ++m) {
+        modes[m - 1] = m;
+        w[m - 1] = doublefactorial(m);
+        pw[m - 1] = (double)mode / m;
+    }
+    cudaEvent_t ev[8];
+    for (int i = 0; i < 8; ++i) CK(cudaEventCreate(&ev[i]));
+    int r = TWOLDG_OK;
+    auto step = [&](int i, cudaError_t e) {
+        if (e != cudaSuccess && r == TWOLDG_OK) r = cuda_fail(e, "profile_kernels");
+        cudaEventRecord(ev[i], p->stream);
+    };
+    cudaEventRecord(ev[0], p->stream);
+    r = p->export_all(u);
+    cudaEventRecord(ev[1], p->stream);
+    if (!r) r = p->cf_all(g, 0);
+    cudaEventRecord(ev[2], p->stream);
+    StagePtrs sp = p->ptrs(g, const_cast<void*>(u), 0);
+    step(3, g.ops->energy(items, nitems, g.E, sp, p->stream));
+    step(4, g.ops->norm(items, nitems, g.E, u, p->y.p, 2, 3, (double*)g.d_part.p, (double*)g.d_part2.p,
+                        g.metric ? g.d_coef.p : nullptr, 1 + g.D, p->stream));
+    step(5, g.ops->maxabs(items, nitems, g.E, u, 0, (double*)g.d_part.p, p->stream));
+    // the indicator's tau goes to the second accumulator half of the stage buffer
+    step(6, g.ops->modes(items, nitems, g.E, u, 0, mode, modes.data(), w.data(), pw.data(),
+                         1.0 / doublefactorial(mode), p->acc.p, p->stream));
+    step(7, g.ops->truncate(items, nitems, g.E, p->y.p, g.metric ? g.d_trm.p : nullptr,
+                            g.metric ? g.d_trd.p : nullptr, p->stream));
+    cudaError_t e = cudaEventSynchronize(ev[7]);
+    if (e != cudaSuccess && r == TWOLDG_OK) r = cuda_fail(e, "cudaEventSynchronize");
+    for (int i = 0; i < 7 && r == TWOLDG_OK; ++i) {
+        e = cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
+        if (e != cudaSuccess) r = cuda_fail(e, "cudaEventElapsedTime");
+    }
+    for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
+    return r;
+}
+
 int twoldg_synchronize(twoldg_problem* p) {
     if (!p) return fail(TWOLDG_EINVAL, "NULL problem");
     CK(cudaStreamSynchronize(p->stream));

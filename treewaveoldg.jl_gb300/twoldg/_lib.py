@@ -19,7 +19,8 @@ EXPORTS = [
     "twoldg_rhs", "twoldg_truncate", "twoldg_rk4_step", "twoldg_reset_compensation",
     "twoldg_energy", "twoldg_norm", "twoldg_modal_indicator", "twoldg_mode_amplitude",
     "twoldg_synchronize", "twoldg_batch_create", "twoldg_batch_destroy", "twoldg_batch_offsets",
-    "twoldg_batch_rk4_step", "twoldg_batch_synchronize", "twoldg_profile_step", "twoldg_stream",
+    "twoldg_batch_rk4_step", "twoldg_batch_synchronize", "twoldg_profile_step", "twoldg_profile_kernels",
+    "twoldg_stream",
     "twoldg_rhs_static", "twoldg_autotune", "twoldg_batch_autotune", "twoldg_transfer", "twoldg_gather",
     "twoldg_transfer_plan_create", "twoldg_transfer_plan_update", "twoldg_transfer_plan_destroy",
     "twoldg_transfer_plan_counts",
@@ -109,6 +110,7 @@ def lib():
             "twoldg_batch_rk4_step": (ctypes.c_int, [vp, vp, ctypes.POINTER(d), i32]),
             "twoldg_batch_synchronize": (ctypes.c_int, [vp]),
             "twoldg_profile_step": (ctypes.c_int, [vp, vp, d, ctypes.POINTER(ctypes.c_float)]),
+            "twoldg_profile_kernels": (ctypes.c_int, [vp, vp, ctypes.POINTER(ctypes.c_float), i32]),
             "twoldg_stream": (vp, [vp]),
             "twoldg_rhs_static": (ctypes.c_int, [ctypes.POINTER(Desc), vp, vp, d, vp]),
             "twoldg_autotune": (ctypes.c_int, [vp, vp, d, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]),
