@@ -114,7 +114,9 @@ typedef struct twoldg_desc {
      * the face F* = -sigma |S[d]| (kappa v + inv_r u), sigma = -1 on a low
      * face and +1 on a high one. kappa >= 0; inv_r = 1/R, or 0 without the u/R
      * term. The energy then carries the boundary's own term,
-     * 1/2 inv_r sum w |S[d]| u^2 over the boundary faces' nodes. */
+     * 1/2 inv_r sum w |S[d]| u^2 over the boundary faces' nodes; 2 Dirichlet
+     * data of any form, whose values the caller supplies at the stage times
+     * (twoldg_set_boundary_values). */
     int32_t boundary;
     double kappa;
     double inv_r;
@@ -205,6 +207,28 @@ int twoldg_mode_amplitude(twoldg_problem* p, const void* u, int32_t var, int32_t
  * without the graph, with CUDA events between the four stages, and returns
  * each stage's duration in milliseconds (stage_ms[4]). Synchronous. */
 int twoldg_profile_step(twoldg_problem* p, void* u, double dt, float* stage_ms);
+/* Dirichlet data of any form, data(x, t) -> (u, grad u), on the boundary
+ * faces of a full-metric problem with boundary = 2: the reference's
+ * DirichletValues{:u} and {:grad} through boundary_by_coordinates
+ * (src/evolution.jl:1110-1127, 1303-1314), which evaluate a Julia function at
+ * every ghost; here the caller evaluates it (with a kernel of its own, as the
+ * reference's launch_points! runs a closure) into a device table the library
+ * reads. twoldg_boundary_faces lists the boundary faces' slots b*6 + f in the
+ * order the table uses (slots NULL: only *n, their number); their nodes'
+ * positions are the descriptor's bnd_x of those slots.
+ * twoldg_set_boundary_values hands the table over: `values` (device, FP64)
+ * holds nlevels time levels t0 + k dt/2, each level nbf faces, each face u at
+ * its N^2 face nodes and then the three Cartesian components of grad u, N^2
+ * each: values[((k * nbf + j) * 4 + c) * N^2 + t]. The library keeps the
+ * pointer: the table must stay on the device, unchanged, until the work that
+ * reads it is done. A call at time t reads level (t - t0) / (dt/2); rk4_step
+ * from t of nsteps steps of size dt reads the 2 nsteps + 1 levels from t on,
+ * and needs the table's dt; twoldg_rhs and twoldg_energy at t read t's level.
+ * Each such call is refused (TWOLDG_EINVAL) when the table does not hold its
+ * times. Asynchronous on the problem's stream. */
+int twoldg_boundary_faces(twoldg_problem* p, int32_t* slots, int32_t* n);
+int twoldg_set_boundary_values(twoldg_problem* p, const double* values, int32_t nlevels, double t0, double dt);
+
 /* Diagnostics (no reference counterpart): times, with CUDA events on the
  * problem's stream, one launch each of the kernels around the stage kernel,
  * on the state u (not changed): ms[0] the face export (export_faces_kernel),

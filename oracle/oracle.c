@@ -70,7 +70,8 @@ typedef struct {
     double t;
     /* the boundary faces' condition: 0 the Dirichlet plane wave, 1 radiative
      * (src/evolution.jl:1129-1260): u's ghost is the face node's u, and the
-     * face's flux is F* = -sigma |S[d]| (kappa v + inv_r u) */
+     * face's flux is F* = -sigma |S[d]| (kappa v + inv_r u); 2 the Dirichlet
+     * spherical standing wave j0(k r) cos(k t), k = wave_k[0] */
     int boundary;
     double kappa, inv_r;
     /* the per-element projections' LU factors with partial pivoting, built by
@@ -613,6 +614,26 @@ static void face_node(int N, int f, int t, int xd, int* x) {
     for (int k = 0; k < 3; ++k) x[k] = k == d ? xd : tt[k2++];
 }
 
+/* The spherical standing wave u = j0(k r) cos(k t), j0(x) = sin(x)/x, an
+ * exact solution of the wave equation regular at the origin, and its
+ * Cartesian gradient k j0'(k r) cos(k t) x / r, j0'(x) = (x cos x - sin x)/x^2:
+ * the Dirichlet data of boundary kind 2 (k = wave_k[0]), the stand-in for any
+ * data(x, t) of the reference's DirichletValues (src/evolution.jl:1110-1127). */
+static double standing_u(const oracle_mesh* m, const double* X, int F, int t, double time, double* grad) {
+    const double k = m->wave_k[0];
+    const double x = X[t], y = X[F + t], z = X[2 * F + t];
+    const double r = sqrt(x * x + y * y + z * z), kr = k * r, c = cos(k * time);
+    const double j0 = kr > 1e-6 ? sin(kr) / kr : 1 - kr * kr / 6;
+    const double dj0 = kr > 1e-6 ? (kr * cos(kr) - sin(kr)) / (kr * kr) : -kr / 3;
+    if (grad) {
+        const double g = r > 0 ? k * dj0 * c / r : 0.0;
+        grad[0] = g * x;
+        grad[1] = g * y;
+        grad[2] = g * z;
+    }
+    return j0 * c;
+}
+
 static double wave_phase(const oracle_mesh* m, const double* X, int F, int t, double time) {
     double om = sqrt(m->wave_k[0] * m->wave_k[0] + m->wave_k[1] * m->wave_k[1] + m->wave_k[2] * m->wave_k[2]);
     return m->wave_k[0] * X[t] + m->wave_k[1] * X[F + t] + m->wave_k[2] * X[2 * F + t] - om * time + m->wave_phi;
@@ -663,6 +684,9 @@ static void full_gradient(const oracle_mesh* m, const double* u, double* V) {
                             int y[3] = {x[0], x[1], x[2]};
                             y[e] = pos < 0 ? 0 : N - 1;
                             val = u[(int64_t)b * 2 * NN + y[0] + N * (y[1] + N * y[2])];
+                        } else if (isnan(val) && m->boundary == 2) {
+                            const double* X = m->bnd_x + ((int64_t)b * 6 + face) * 3 * F;
+                            val = standing_u(m, X, (int)F, t, m->t, NULL);
                         } else if (isnan(val)) {
                             const double* X = m->bnd_x + ((int64_t)b * 6 + face) * 3 * F;
                             val = sin(wave_phase(m, X, (int)F, t, m->t));
@@ -728,7 +752,10 @@ int oracle_rhs_full(const oracle_mesh* m, const double* u, double* du) {
                             acc += coefk * (2 * Fstar - Fo);
                             continue;
                         }
-                        if (m->face_nb[b * 6 + face] < 0) {
+                        if (m->face_nb[b * 6 + face] < 0 && m->boundary == 2) {
+                            const double* X = m->bnd_x + ((int64_t)b * 6 + face) * 3 * F;
+                            standing_u(m, X, (int)F, t, m->t, Vw);
+                        } else if (m->face_nb[b * 6 + face] < 0) {
                             const double* X = m->bnd_x + ((int64_t)b * 6 + face) * 3 * F;
                             double c = cos(wave_phase(m, X, (int)F, t, m->t));
                             for (int ci = 0; ci < 3; ++ci) Vw[ci] = m->wave_k[ci] * c;

@@ -191,9 +191,10 @@ class BallOracle(Oracle):
     element (every block off the affine cube, the factored ones included:
     the oracle solves each element's projection from sqrt(g) itself, so the
     factored tables are checked against it); `radiative` is (kappa, inv_r)
-    or None."""
+    or None; `standing` is k of the spherical standing wave j0(k r) cos(k t)
+    as the Dirichlet data (evaluated here, from the formula), or None."""
 
-    def __init__(self, forest, P, tables, wave, truncate=True, radiative=None):
+    def __init__(self, forest, P, tables, wave, truncate=True, radiative=None, standing=None):
         self.forest = forest
         self.P = P
         self.D = 3
@@ -224,6 +225,9 @@ class BallOracle(Oracle):
         m.metric = 2
         if radiative is not None:
             m.boundary, m.kappa, m.inv_r = 1, float(radiative[0]), float(radiative[1])
+        if standing is not None:
+            # the spherical standing wave j0(k r) cos(k t) as the Dirichlet data
+            m.boundary, m.wave_k[0] = 2, float(standing)
         dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int32)
         m.level = a["level"].ctypes.data_as(ip)
         m.corner = a["corner"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64))

@@ -168,3 +168,30 @@ def test_ball_truncation_is_the_sqrtg_orthogonal_projection(P):
     assert not np.allclose(_flat_truncate(a, nb, N, el), a)
     assert np.array_equal(ta.reshape(nb, 2, NN)[:, 0], a.reshape(nb, 2, NN)[:, 0])
     assert inner(v(ta), v(ta)) <= inner(v(a), v(a))
+
+
+def test_dirichlet_data_of_any_form_converge_at_order_P():
+    """Dirichlet data other than the plane wave (the reference's
+    DirichletValues takes any data(x, t), src/evolution.jl:1110-1127): the
+    spherical standing wave j0(k r) cos(k t), k = 2, as the data on the
+    seven-patch ball's sphere, P = 3 truncated, to t = 1/2 at cfl 1/2. The
+    oracle's run converges at order P between roots (2, 2) and (3, 3)."""
+    import math
+    from twoldg.ball import SphericalStandingWave, ball_forest, ball_tables
+    from oracle.oracle import BallOracle
+    from ball_cases import ball_state
+    w = SphericalStandingWave(2.0)
+    errs, hs = [], []
+    for roots in ((2, 2), (3, 3)):
+        forest, geo = ball_forest(np.float64, 3, 2, roots, 1.0, 3.0)
+        tables = ball_tables(forest, 3, w)
+        o = BallOracle(forest, 3, tables, None, truncate=True, standing=2.0)
+        u0 = o.truncate(ball_state(forest, tables, lambda x, v: w.state(x, 0.0, v)))
+        n = int(math.ceil(0.5 / (0.5 * tables["hspeed"] / 4)))
+        u = o.rk4(u0, 0.5 / n, n, 0.0)
+        ue = ball_state(forest, tables, lambda x, v: w.state(x, 0.5, v))
+        errs.append(o.norm(u, 2, 3, ue))
+        hs.append(1.0 / roots[0])
+    assert errs[0] < 1.2e-3
+    rate = math.log(errs[0] / errs[1]) / math.log(hs[0] / hs[1])
+    assert rate > 2.7, (errs, rate)

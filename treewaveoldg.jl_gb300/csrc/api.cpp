@@ -95,6 +95,15 @@ struct Group {
     // the factored truncation: per block slot, per factored block its radial
     // dimension, pair and angular table index, the angular tables
     DevBuf d_fslot, d_fradial, d_frm, d_frd, d_faslot, d_faw, d_fachol;
+    // boundary kind 2: per face slot the boundary face's index (-1 inside),
+    // the number of boundary faces, and the caller's table as last set (on the
+    // host, and on the device where the captured kernels read it)
+    std::vector<int> bidx;
+    int nbf = 0;
+    DevBuf d_bidx, d_btab;
+    BoundaryTable h_btab{};
+    double btab_dt = 0;
+    bool btab_set = false;
     std::vector<int> fslot, fradial, faslot;
     std::vector<double> frm, frd, faw, fachol;
     int nslots() const { return (int)items.size() * 2 * D; }
@@ -180,8 +189,9 @@ struct twoldg_runner {
                 if (!d.coef || !d.elem_slot || !d.bnd_x)
                     return fail(TWOLDG_EINVAL, "a full metric needs coef, elem_slot and bnd_x");
                 if (n != 1) return fail(TWOLDG_EUNSUP, "a full-metric problem is stepped alone, not in a batch");
-                if (d.boundary != 0 && d.boundary != 1)
-                    return fail(TWOLDG_EINVAL, "boundary must be 0 (Dirichlet plane wave) or 1 (radiative)");
+                if (d.boundary != 0 && d.boundary != 1 && d.boundary != 2)
+                    return fail(TWOLDG_EINVAL, "boundary must be 0 (Dirichlet plane wave), 1 (radiative) or 2 "
+                                               "(Dirichlet values the caller supplies)");
                 if (d.boundary == 1 && !(d.kappa >= 0))
                     return fail(TWOLDG_EINVAL, "kappa = " + std::to_string(d.kappa) +
                                                    " is negative, and a radiative boundary with kappa < 0 feeds "
@@ -247,6 +257,9 @@ struct twoldg_runner {
                 for (int q = 0; q < 3; ++q) g->wave_k[q] = d.wave_k[q];
                 g->wave_phi = d.wave_phi;
                 g->boundary = d.boundary;
+                g->bidx.assign((size_t)m.nblocks * 2 * m.D, -1);
+                for (size_t q = 0; q < g->bidx.size(); ++q)
+                    if (d.face_nb[q] < 0) g->bidx[q] = g->nbf++;
                 g->kappa = d.kappa;
                 g->inv_r = d.inv_r;
                 g->fslot.assign(m.nblocks, 0);
@@ -356,6 +369,10 @@ struct twoldg_runner {
                 CK(cudaMemset(g.d_fv.p, 0, (size_t)g.nslots() * 3 * g.F * wsize));
                 CK(g.d_bndx.alloc(g.bndx.size() * sizeof(double)));
                 CK(cudaMemcpy(g.d_bndx.p, g.bndx.data(), g.bndx.size() * sizeof(double), cudaMemcpyHostToDevice));
+                CK(g.d_bidx.alloc(g.bidx.size() * sizeof(int)));
+                CK(cudaMemcpy(g.d_bidx.p, g.bidx.data(), g.bidx.size() * sizeof(int), cudaMemcpyHostToDevice));
+                CK(g.d_btab.alloc(sizeof(BoundaryTable)));
+                CK(cudaMemset(g.d_btab.p, 0, sizeof(BoundaryTable)));
                 CK(g.d_eslot.alloc(g.eslot.size() * sizeof(int)));
                 CK(cudaMemcpy(g.d_eslot.p, g.eslot.data(), g.eslot.size() * sizeof(int), cudaMemcpyHostToDevice));
                 CK(g.d_fslot.alloc(g.fslot.size() * sizeof(int)));
@@ -475,6 +492,8 @@ struct twoldg_runner {
         p.faslot = (const int*)g.d_faslot.p;
         p.faw = g.d_faw.p;
         p.fachol = g.d_fachol.p;
+        p.bidx = (const int*)g.d_bidx.p;
+        p.btab = (const BoundaryTable*)g.d_btab.p;
         p.ew = g.d_ew.p;
         p.echol = g.d_echol.p;
         p.partial = (double*)g.d_part.p;
@@ -489,6 +508,31 @@ struct twoldg_runner {
         }
         CK(cudaMemcpyAsync(d_tinfo.p, h_tinfo.data(), h_tinfo.size() * sizeof(double), cudaMemcpyHostToDevice,
                            stream));
+        return TWOLDG_OK;
+    }
+
+    // Boundary kind 2: the caller's table must hold every stage time that a
+    // call from t of nsteps steps of size dt reaches (t + j dt/2, j = 0 ..
+    // 2 nsteps), as levels of its own spacing; nsteps = 0 asks for t alone.
+    int boundary_window(double t, double dt, int nsteps) {
+        for (auto& gp : groups) {
+            Group& g = *gp;
+            if (!g.full || g.boundary != 2) continue;
+            if (!g.btab_set)
+                return fail(TWOLDG_EINVAL, "the problem's Dirichlet data are the caller's (boundary 2) and none "
+                                           "were given: call twoldg_set_boundary_values first");
+            const double half = 0.5 * g.btab_dt;
+            const double kf = (t - g.h_btab.t0) / half;
+            const double k0 = std::nearbyint(kf);
+            if (!(std::fabs(kf - k0) <= 1e-6))
+                return fail(TWOLDG_EINVAL, "t = " + std::to_string(t) + " is not a level of the boundary values "
+                                           "(t0 + k dt/2)");
+            if (nsteps > 0 && !(std::fabs(dt - g.btab_dt) <= 1e-12 * g.btab_dt))
+                return fail(TWOLDG_EINVAL, "the step dt differs from the boundary values' dt");
+            if (k0 < 0 || k0 + 2.0 * nsteps > g.h_btab.nlevels - 1)
+                return fail(TWOLDG_EINVAL, "the boundary values' " + std::to_string(g.h_btab.nlevels) +
+                                               " levels do not cover the call's stage times");
+        }
         return TWOLDG_OK;
     }
 
@@ -699,7 +743,8 @@ struct twoldg_runner {
             comp_u = u;
         }
         if (any_full()) {
-            int rr = set_time(t0, dts);
+            int rr = nsteps > 0 ? boundary_window(t0, dts[0], nsteps) : TWOLDG_OK;
+            if (!rr) rr = set_time(t0, dts);
             if (rr) return rr;
         }
         if (nsteps == 0) return TWOLDG_OK;
@@ -837,7 +882,8 @@ int twoldg_rhs(twoldg_problem* p, void* du, const void* u, double t) {
     if (r) return r;
     Group& g = *p->groups[0];
     if (g.full) {
-        r = p->set_time(t, nullptr);
+        r = p->boundary_window(t, 0.0, 0);
+        if (!r) r = p->set_time(t, nullptr);
         if (r) return r;
         FmPtrs fp = p->fptrs(g, const_cast<void*>(u), 0);
         fp.du = du;
@@ -884,7 +930,8 @@ int twoldg_energy(twoldg_problem* p, const void* u, double t, double* energy) {
     if (r) return r;
     Group& g = *p->groups[0];
     if (g.full) {
-        r = p->set_time(t, nullptr);
+        r = p->boundary_window(t, 0.0, 0);
+        if (!r) r = p->set_time(t, nullptr);
         if (r) return r;
         FmPtrs fp = p->fptrs(g, const_cast<void*>(u), 0);
         CK(g.ops->fm_gradient((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, 5, fp, p->stream));
@@ -984,7 +1031,8 @@ int twoldg_profile_step(twoldg_problem* p, void* u, double dt, float* stage_ms) 
     if (!p || !u || !stage_ms) return fail(TWOLDG_EINVAL, "NULL argument");
     double dts = dt;
     // make sure dt is on the device (rk4 with zero steps uploads it)
-    int r = p->rk4(u, &dts, 0);
+    int r = p->any_full() ? p->boundary_window(0.0, dt, 1) : TWOLDG_OK;
+    if (!r) r = p->rk4(u, &dts, 0);
     if (r) return r;
     r = p->export_all(u);
     if (r) return r;
@@ -1057,6 +1105,38 @@ int twoldg_profile_kernels(twoldg_problem* p, const void* u, float* ms, int32_t 
     }
     for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
     return r;
+}
+
+int twoldg_boundary_faces(twoldg_problem* p, int32_t* slots, int32_t* n) {
+    if (!p || !n) return fail(TWOLDG_EINVAL, "NULL argument");
+    Group& g = *p->groups[0];
+    if (!g.full || g.boundary != 2)
+        return fail(TWOLDG_EINVAL, "the problem does not take the caller's Dirichlet values (boundary 2)");
+    if (slots)
+        for (size_t q = 0; q < g.bidx.size(); ++q)
+            if (g.bidx[q] >= 0) slots[g.bidx[q]] = (int32_t)q;
+    *n = g.nbf;
+    return TWOLDG_OK;
+}
+
+int twoldg_set_boundary_values(twoldg_problem* p, const double* values, int32_t nlevels, double t0, double dt) {
+    if (!p || !values) return fail(TWOLDG_EINVAL, "NULL argument");
+    Group& g = *p->groups[0];
+    if (!g.full || g.boundary != 2)
+        return fail(TWOLDG_EINVAL, "the problem does not take the caller's Dirichlet values (boundary 2)");
+    if (nlevels < 1) return fail(TWOLDG_EINVAL, "nlevels must be at least 1");
+    if (!(dt > 0) || !std::isfinite(dt) || !std::isfinite(t0))
+        return fail(TWOLDG_EINVAL, "t0 must be finite and dt positive and finite");
+    g.h_btab.values = values;
+    g.h_btab.nlevels = nlevels;
+    g.h_btab.nbf = g.nbf;
+    g.h_btab.t0 = t0;
+    g.h_btab.inv_half = 2.0 / dt;
+    g.btab_dt = dt;
+    g.btab_set = true;
+    // ordered before every later launch on the problem's stream
+    CK(cudaMemcpyAsync(g.d_btab.p, &g.h_btab, sizeof(BoundaryTable), cudaMemcpyHostToDevice, p->stream));
+    return TWOLDG_OK;
 }
 
 int twoldg_synchronize(twoldg_problem* p) {

@@ -71,6 +71,10 @@ struct FmArgs {
     const int* faslot;
     const T* faw;
     const T* fachol;
+    // boundary kind 2: the caller's Dirichlet values (device table and the
+    // boundary face index of every face slot)
+    const int* bidx;
+    const BoundaryTable* btab;
 };
 
 template <typename T, int P>
@@ -81,6 +85,18 @@ struct FmTab {
 __device__ __forceinline__ double stage_time(const double* tinfo, int problem, int mode) {
     const double c = mode == 1 || mode == 0 ? 0.0 : mode == 4 ? 1.0 : 0.5;
     return tinfo[2 * problem] + c * tinfo[2 * problem + 1];
+}
+
+// The caller's Dirichlet values of boundary face slot `slot` at time t: u,
+// then the gradient's three Cartesian components, F values each. The level is
+// the nearest to t; the host has checked that every stage time a call reaches
+// is a level of the table, and the clamp only keeps the index in bounds.
+template <typename T>
+__device__ __forceinline__ const double* boundary_values(const FmArgs<T>& a, int slot, double t, int F) {
+    const BoundaryTable bt = *a.btab;
+    long long k = llrint((t - bt.t0) * bt.inv_half);
+    k = k < 0 ? 0 : (k >= bt.nlevels ? bt.nlevels - 1 : k);
+    return bt.values + ((k * bt.nbf + a.bidx[slot]) * 4) * (int64_t)F;
 }
 
 // The neighbour's tangential index of this face's point t = a + N b.
@@ -135,6 +151,9 @@ __global__ void __launch_bounds__(256) fm_gradient_kernel(FmArgs<T> a, Tab<T, P>
                 int xo[3];
                 plane_coords<3>(g, d, tt, side == 0 ? 0 : g.N - 1, xo);
                 v = yu[oidx<3>(g, xo)];
+            } else if (it.nb[f] < 0 && a.boundary == 2) {
+                // Dirichlet: the caller's value at the boundary face node
+                v = (T)boundary_values(a, it.slot + f, t, g.F)[tt];
             } else if (it.nb[f] < 0) {
                 // Dirichlet: the data at the boundary face node's position
                 const double* X = a.bnd_x + (int64_t)(it.slot + f) * 3 * g.F;
@@ -477,7 +496,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 4) fm_stage_kernel(F
                     continue;
                 }
                 T Vg[3];
-                if (it.nb[f] < 0) {
+                if (it.nb[f] < 0 && a.boundary == 2) {
+                    const double* bv = boundary_values(a, it.slot + f, t, g.F);
+#pragma unroll
+                    for (int ci = 0; ci < 3; ++ci) Vg[ci] = (T)bv[(1 + ci) * g.F + tt];
+                } else if (it.nb[f] < 0) {
                     const double* X = a.bnd_x + (int64_t)(it.slot + f) * 3 * g.F;
                     const double th = a.wave.k[0] * X[tt] + a.wave.k[1] * X[g.F + tt] +
                                       a.wave.k[2] * X[2 * g.F + tt] - a.wave.omega * t + a.wave.phi;

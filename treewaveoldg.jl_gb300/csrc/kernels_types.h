@@ -25,6 +25,19 @@ struct CfFace {
     double h;           // spacing of the block owning `slot`
 };
 
+// Dirichlet data a caller supplies for the boundary faces of a full-metric
+// problem (boundary kind 2): level k holds, for every boundary face j (the
+// faces with no neighbour, in slot order) and its tangential node t, u and
+// then the three Cartesian components of its gradient at time t0 + k / inv_half,
+// values[((k * nbf + j) * 4 + c) * F + t].
+struct BoundaryTable {
+    const double* values;
+    int32_t nlevels;
+    int32_t nbf;
+    double t0;
+    double inv_half;    // 2 / dt: two levels per step (t_n + dt/2 and t_n + dt)
+};
+
 // One block of a regrid transfer: the new block at dst (words), from the old
 // leaf src[0] (copy), from its parent src[0] as child `sub` (bit d: the
 // upper half along d; refine), or from its 2^D children src[bits] (coarsen).

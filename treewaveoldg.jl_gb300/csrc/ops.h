@@ -53,7 +53,7 @@ struct FmPtrs {
     const void* ew;
     const void* echol;
     double* partial;
-    int boundary;       // 0 Dirichlet plane wave, 1 radiative
+    int boundary;       // 0 Dirichlet plane wave, 1 radiative, 2 the caller's Dirichlet values
     double kappa;
     double inv_r;
     const int* fslot;   // factored truncation (fullmetric.cuh)
@@ -63,6 +63,8 @@ struct FmPtrs {
     const int* faslot;
     const void* faw;
     const void* fachol;
+    const int* bidx;    // boundary kind 2: per face slot its boundary face index (-1 inside)
+    const BoundaryTable* btab;
 };
 
 // A launch layout of the stage kernel. kernel: 0 the shape's default, 1 the

@@ -478,6 +478,8 @@ public:
         a.faslot = p.faslot;
         a.faw = (const T*)p.faw;
         a.fachol = (const T*)p.fachol;
+        a.bidx = p.bidx;
+        a.btab = p.btab;
         return a;
     }
     static size_t fm_grad_smem(int E) { return (padded_words(E) + 3 * plain_words(E)) * sizeof(T); }

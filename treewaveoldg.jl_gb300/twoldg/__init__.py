@@ -17,8 +17,9 @@ from .indicator import modal_indicator, mode_amplitude
 from .batch import Batch, fill_batch, sine_ensemble
 from .geometry import (PolarAnnulus, annulus_errors, annulus_exact, annulus_forest, annulus_wavenumber,
                        metric_tables, projector_mode)
-from .ball import (BallForest, OutgoingPulse, PlaneWave, RadiativeBoundary, SevenPatchBall, ThirteenPatchBall,
-                   radiative_errors, sevenpatch_errors, sevenpatch_exact, sevenpatch_forest, thirteenpatch_forest)
+from .ball import (BallForest, DirichletData, OutgoingPulse, PlaneWave, RadiativeBoundary, SevenPatchBall,
+                   SphericalStandingWave, ThirteenPatchBall, radiative_errors, sevenpatch_errors, sevenpatch_exact,
+                   sevenpatch_forest, thirteenpatch_forest)
 
 from .regrid import COARSEN, KEEP, REFINE, refine_flags, refine_mark, regrid, transfer_state
 from .blast import adaptive_blast, blast_exact, blast_initial, blast_reference, refinement_buffer, uniform_blast

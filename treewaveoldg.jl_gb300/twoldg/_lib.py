@@ -20,7 +20,7 @@ EXPORTS = [
     "twoldg_energy", "twoldg_norm", "twoldg_modal_indicator", "twoldg_mode_amplitude",
     "twoldg_synchronize", "twoldg_batch_create", "twoldg_batch_destroy", "twoldg_batch_offsets",
     "twoldg_batch_rk4_step", "twoldg_batch_synchronize", "twoldg_profile_step", "twoldg_profile_kernels",
-    "twoldg_stream",
+    "twoldg_stream", "twoldg_boundary_faces", "twoldg_set_boundary_values",
     "twoldg_rhs_static", "twoldg_autotune", "twoldg_batch_autotune", "twoldg_transfer", "twoldg_gather",
     "twoldg_transfer_plan_create", "twoldg_transfer_plan_update", "twoldg_transfer_plan_destroy",
     "twoldg_transfer_plan_counts",
@@ -112,6 +112,8 @@ def lib():
             "twoldg_profile_step": (ctypes.c_int, [vp, vp, d, ctypes.POINTER(ctypes.c_float)]),
             "twoldg_profile_kernels": (ctypes.c_int, [vp, vp, ctypes.POINTER(ctypes.c_float), i32]),
             "twoldg_stream": (vp, [vp]),
+            "twoldg_boundary_faces": (ctypes.c_int, [vp, vp, ctypes.POINTER(i32)]),
+            "twoldg_set_boundary_values": (ctypes.c_int, [vp, vp, i32, d, d]),
             "twoldg_rhs_static": (ctypes.c_int, [ctypes.POINTER(Desc), vp, vp, d, vp]),
             "twoldg_autotune": (ctypes.c_int, [vp, vp, d, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]),
             "twoldg_transfer": (ctypes.c_int, [ctypes.POINTER(Desc), vp, ctypes.POINTER(Desc), vp, vp]),

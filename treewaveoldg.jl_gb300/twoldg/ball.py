@@ -442,6 +442,49 @@ class RadiativeBoundary:
         self.inverse_r = bool(inverse_r)
 
 
+class DirichletData:
+    """Dirichlet data of any form on a ball's outer sphere: the reference's
+    DirichletValues{:u} and {:grad} through boundary_by_coordinates
+    (src/evolution.jl:1110-1127, 1303-1314), with `data(X, t)` returning u at
+    the physical positions X (a (3, n) array) and the Cartesian gradient of u
+    there ((3, n)). The problem evaluates it at the boundary face nodes for
+    every stage time of a call and hands the library the table
+    (twoldg_set_boundary_values)."""
+
+    def __init__(self, data):
+        self.data = data
+
+
+class SphericalStandingWave(DirichletData):
+    """u = j0(k r) cos(k t) with j0(x) = sin(x)/x, an exact solution of the
+    wave equation regular at the origin, v = du/dt = -k j0(k r) sin(k t), and
+    grad u = k j0'(k r) cos(k t) x/r with j0'(x) = (x cos x - sin x)/x^2; as
+    Dirichlet data on the sphere it is a stand-in for any data(x, t)."""
+
+    def __init__(self, k):
+        self.k = float(k)
+        super().__init__(self._data)
+
+    def _radial(self, X):
+        X = [np.asarray(x, dtype=np.float64) for x in X]
+        r = np.sqrt(X[0] ** 2 + X[1] ** 2 + X[2] ** 2)
+        kr = self.k * r
+        small = kr < 1e-6
+        krs = np.where(small, 1.0, kr)
+        j0 = np.where(small, 1 - kr * kr / 6, np.sin(krs) / krs)
+        dj0 = np.where(small, -kr / 3, (krs * np.cos(krs) - np.sin(krs)) / krs ** 2)
+        return X, r, j0, dj0
+
+    def state(self, X, t, var):
+        _, _, j0, _ = self._radial(X)
+        return j0 * math.cos(self.k * t) if var == 1 else -self.k * j0 * math.sin(self.k * t)
+
+    def _data(self, X, t):
+        X, r, j0, dj0 = self._radial(X)
+        g = np.where(r > 0, self.k * dj0 * math.cos(self.k * t) / np.where(r > 0, r, 1.0), 0.0)
+        return j0 * math.cos(self.k * t), np.stack([g * X[0], g * X[1], g * X[2]])
+
+
 class OutgoingPulse:
     """u = (f(t - r) - f(t + r)) / r with f(s) = exp(-s^2/w^2), a solution of the
     wave equation regular at the origin, and v = du/dt (src/sevenpatch.jl:130-177);
@@ -630,7 +673,8 @@ def factored_tables(forest, P, el):
 
 def ball_desc(forest, P, truncate, precision, tables, wave):
     """The twoldg_desc of a ball problem (an explicit face table and the full
-    metric); `wave` is the Dirichlet PlaneWave or a RadiativeBoundary."""
+    metric); `wave` is the Dirichlet PlaneWave, Dirichlet data of any form
+    (DirichletData) or a RadiativeBoundary."""
     import ctypes
     from . import _lib
     nb = forest.nleaves()
@@ -662,6 +706,8 @@ def ball_desc(forest, P, truncate, precision, tables, wave):
         d.boundary = 1
         d.kappa = wave.kappa
         d.inv_r = 1.0 / forest.geo.outer_radius() if wave.inverse_r else 0.0
+    elif isinstance(wave, DirichletData):
+        d.boundary = 2
     else:
         for k in range(3):
             d.wave_k[k] = wave.k[k]

@@ -133,6 +133,41 @@ class WaveProblem:
         w = ctypes.c_int64()
         _lib.check(_lib.lib().twoldg_state_words(h, ctypes.byref(w)))
         self.state_words = w.value
+        self._bnd = None
+        from .ball import DirichletData
+        if self.full and isinstance(boundary, DirichletData):
+            n = ctypes.c_int32()
+            _lib.check(_lib.lib().twoldg_boundary_faces(h, None, ctypes.byref(n)))
+            slots = np.zeros(max(1, n.value), dtype=np.int32)
+            _lib.check(_lib.lib().twoldg_boundary_faces(h, slots.ctypes.data_as(ctypes.c_void_p), ctypes.byref(n)))
+            F = self.N ** 2
+            X = np.asarray(self.metric["bnd_x"]).reshape(-1, 3, F)[slots[:n.value]]
+            # the boundary face nodes' positions, (3, nbf F): face by face
+            self._bnd = np.ascontiguousarray(X.transpose(1, 0, 2).reshape(3, -1))
+            self._bnd_table = None
+
+    # the most levels one table holds: a longer run is stepped in chunks
+    BOUNDARY_CHUNK_STEPS = 256
+
+    def boundary_window(self, t0, dt, nlevels):
+        """Boundary kind 2: the caller's Dirichlet data at the boundary face
+        nodes for the times t0 + k dt/2, k < nlevels, as the device table the
+        library reads (u and the three gradient components per face)."""
+        torch = _torch()
+        if self._bnd is None:
+            return
+        F = self.N ** 2
+        nbf = self._bnd.shape[1] // F
+        table = np.empty((nlevels, 4, nbf, F))
+        for k in range(nlevels):
+            u, g = self.boundary.data(self._bnd, t0 + k * (0.5 * dt))
+            table[k, 0] = np.asarray(u).reshape(nbf, F)
+            table[k, 1:] = np.asarray(g).reshape(3, nbf, F)
+        dev = torch.from_numpy(np.ascontiguousarray(table.transpose(0, 2, 1, 3))).to(self.device)
+        self.synchronize()            # the table it replaces is read no more
+        self._bnd_table = dev
+        _lib.check(_lib.lib().twoldg_set_boundary_values(self.handle, _dptr(dev), int(nlevels), float(t0),
+                                                         float(dt)))
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -241,6 +276,8 @@ def wave_rhs(du, u, p, t=0.0):
     """wave_rhs!(du, u, p, t) (src/evolution.jl:1367-1371)."""
     _check_state(p, u)
     _check_state(p, du)
+    if p._bnd is not None:
+        p.boundary_window(float(t), 1.0, 1)
     _sync_torch()
     _lib.check(_lib.lib().twoldg_rhs(p.handle, _dptr(du), _dptr(u), float(t)))
     p.synchronize()
@@ -264,6 +301,8 @@ def truncate_stage(u, integrator, p, t):
 def wave_energy(p, u, t=None):
     """wave_energy(p, u) (src/evolution.jl:1472-1489), accumulated in FP64."""
     _check_state(p, u)
+    if p._bnd is not None:
+        p.boundary_window(0.0 if t is None else float(t), 1.0, 1)
     _sync_torch()
     e = ctypes.c_double()
     _lib.check(_lib.lib().twoldg_energy(p.handle, _dptr(u), 0.0 if t is None else float(t), ctypes.byref(e)))
@@ -344,6 +383,17 @@ class WaveIntegrator:
     def _advance(self, n):
         if n <= 0:
             return
+        if self.p._bnd is not None:
+            # the caller's Dirichlet data, chunk by chunk of steps
+            while n > 0:
+                m = min(n, self.p.BOUNDARY_CHUNK_STEPS)
+                self.p.boundary_window(self.t, self.dt, 2 * m + 1)
+                self._steps(m)
+                n -= m
+            return
+        self._steps(n)
+
+    def _steps(self, n):
         _sync_torch()
         _lib.check(_lib.lib().twoldg_rk4_step(self.p.handle, _dptr(self.u), self.t, self.dt, int(n)))
         self.p.synchronize()
