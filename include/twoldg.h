@@ -48,6 +48,8 @@ extern "C" {
  * ghosts. Blocks are numbered in the caller's order, which is the state
  * layout's block order.
  */
+#define TWOLDG_FACE_BRICK (-2)  /* face_nb: a face between two blocks of a refined brick patch */
+
 typedef struct twoldg_desc {
     int32_t dim;             /* D = 1, 2 or 3 */
     int32_t order;           /* P >= 1 */
@@ -88,7 +90,14 @@ typedef struct twoldg_desc {
      * b, or -1 for a face on the domain's boundary, which takes the Dirichlet
      * data below; face_code[b*2D + f] = (the neighbour's face) | (o << 4),
      * where o maps this face's tangential point (a, b) to the neighbour's:
-     * bit 0 swaps a and b, bit 1 then reverses the first, bit 2 the second. */
+     * bit 0 swaps a and b, bit 1 then reverses the first, bit 2 the second.
+     * One patch may be a refined brick (the ball's affine cube, refined as
+     * src/geometry.jl:494-553 refines it): the faces between its blocks are
+     * TWOLDG_FACE_BRICK, and those blocks give their level and their corner
+     * (in blocks of that level) in a brick of roots[d] root blocks, whose
+     * faces the library resolves by level and corner, coarse-fine faces
+     * included (the element-local I and R of the flat problem). Explicit
+     * faces join blocks of one level. */
     const int32_t* face_nb;
     const int32_t* face_code;
     /* The full metric's truncation (ElementTruncation, src/evolution.jl:723-899):

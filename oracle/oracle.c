@@ -77,6 +77,10 @@ typedef struct {
     /* the per-element projections' LU factors with partial pivoting, built by
      * oracle_full_prepare (NULL: each projection factors its own Gram matrix) */
     void* cache;
+    /* a refined brick patch (the ball's affine cube, face_nb -2 between its
+     * blocks): built by oracle_full_prepare from the blocks' level and corner
+     * in a brick of roots[k] root blocks */
+    void* brick;
 } oracle_mesh;
 
 typedef struct {
@@ -655,14 +659,94 @@ static double full_ghost(const oracle_mesh* m, int N, int64_t NN, const double* 
     return f[nb * bstride + comp * cs + x[0] + N * (x[1] + N * x[2])];
 }
 
+/* A refined brick patch inside the ball (its affine cube): its blocks as a
+ * forest of their own, whose ghosts across the faces between them are the
+ * flat problem's (ghost_value: injection, or the coarse element's polynomial
+ * at a fine node, or the restriction R = M_c^-1 I^T M_f), located in its own
+ * finest-cell map; `f` holds one field over the brick's blocks. */
+typedef struct {
+    oracle_mesh sub;
+    ctx_t ctx;
+    int nb;
+    int* local;        /* global block -> brick block, or -1 */
+    int* global;       /* brick block -> global block */
+    int32_t* level;
+    int64_t* corner;
+    double* f;         /* one field over the brick's blocks, N^3 each */
+} brick_t;
+
+static void brick_free(brick_t* br) {
+    if (!br) return;
+    free(br->local); free(br->global); free(br->level); free(br->corner); free(br->f); free(br->ctx.owner);
+    free(br);
+}
+
+static brick_t* brick_build(const oracle_mesh* m) {
+    const int N = m->E * (m->P + 1);
+    const int64_t NN = (int64_t)N * N * N;
+    int nb = 0;
+    for (int b = 0; b < m->nblocks; ++b)
+        for (int f = 0; f < 6; ++f)
+            if (m->face_nb[b * 6 + f] == -2) { ++nb; break; }
+    if (nb == 0) return NULL;
+    brick_t* br = (brick_t*)calloc(1, sizeof(brick_t));
+    br->local = (int*)malloc(sizeof(int) * m->nblocks);
+    br->global = (int*)malloc(sizeof(int) * nb);
+    br->level = (int32_t*)malloc(sizeof(int32_t) * nb);
+    br->corner = (int64_t*)malloc(sizeof(int64_t) * 3 * nb);
+    br->f = (double*)malloc(sizeof(double) * NN * nb);
+    br->nb = nb;
+    int k = 0;
+    for (int b = 0; b < m->nblocks; ++b) {
+        br->local[b] = -1;
+        for (int f = 0; f < 6; ++f)
+            if (m->face_nb[b * 6 + f] == -2) {
+                br->local[b] = k;
+                br->global[k] = b;
+                br->level[k] = m->level[b];
+                for (int q = 0; q < 3; ++q) br->corner[3 * k + q] = m->corner[(int64_t)b * 3 + q];
+                ++k;
+                break;
+            }
+    }
+    br->sub = *m;
+    br->sub.nblocks = nb;
+    br->sub.level = br->level;
+    br->sub.corner = br->corner;
+    for (int q = 0; q < 3; ++q) {
+        br->sub.periodic[q] = 0;
+        br->sub.reflecting[q] = 1;
+        br->sub.lo[q] = 0.0;
+        br->sub.hi[q] = (double)m->roots[q];
+    }
+    br->sub.cache = NULL;
+    br->sub.brick = NULL;
+    if (ctx_init(&br->ctx, &br->sub)) { brick_free(br); return NULL; }
+    return br;
+}
+
+/* Copy component `comp` of a field (bstride words per block, component
+ * stride cs) of the brick's blocks into br->f. */
+static void brick_gather(brick_t* br, const double* fld, int64_t NN, int64_t bstride, int comp, int64_t cs) {
+    for (int l = 0; l < br->nb; ++l)
+        memcpy(br->f + (int64_t)l * NN, fld + (int64_t)br->global[l] * bstride + comp * cs, sizeof(double) * NN);
+}
+
+/* The logical node spacing of block b: a root block spans 1, a level-L block 2^-L. */
+static double full_spacing(const oracle_mesh* m, int b, int N) {
+    return 1.0 / N / (double)((int64_t)1 << m->level[b]);
+}
+
 /* V = grad u at every node of every block, (3, N^3) per block. */
 static void full_gradient(const oracle_mesh* m, const double* u, double* V) {
     const int P = m->P, P1 = P + 1, PW = P + 3, N = m->E * P1;
     const int64_t NN = (int64_t)N * N * N, F = (int64_t)N * N;
-    const double h = 1.0 / N;
+    brick_t* br = (brick_t*)m->brick;
+    if (br) brick_gather(br, u, NN, 2 * NN, 0, 0);
 #pragma omp parallel for schedule(dynamic)
     for (int b = 0; b < m->nblocks; ++b) {
         const double* cf = m->coef + (int64_t)b * 10 * NN;
+        const double h = full_spacing(m, b, N);
         for (int64_t n = 0; n < NN; ++n) {
             int x[3] = {(int)(n % N), (int)((n / N) % N), (int)(n / F)};
             double De[3];
@@ -679,6 +763,11 @@ static void full_gradient(const oracle_mesh* m, const double* u, double* V) {
                         int tt[2];
                         for (int q = 0; q < 3; ++q) if (q != e) tt[k2++] = x[q];
                         t = tt[0] + N * tt[1];
+                        if (m->face_nb[b * 6 + face] == -2) {
+                            val = ghost_value(&br->ctx, br->local[b], e, pos >= N, x, br->f, 1.0);
+                            acc += coefk * val;
+                            continue;
+                        }
                         val = full_ghost(m, N, NN, u, 2 * NN, 0, 0, b, face, t);
                         if (isnan(val) && m->boundary == 1) {
                             int y[3] = {x[0], x[1], x[2]};
@@ -712,13 +801,24 @@ static void full_gradient(const oracle_mesh* m, const double* u, double* V) {
 int oracle_rhs_full(const oracle_mesh* m, const double* u, double* du) {
     const int P = m->P, P1 = P + 1, PW = P + 3, N = m->E * P1;
     const int64_t NN = (int64_t)N * N * N, F = (int64_t)N * N;
-    const double h = 1.0 / N;
     double* V = (double*)malloc(sizeof(double) * 3 * NN * m->nblocks);
     if (!V) return -1;
     full_gradient(m, u, V);
+    /* the brick's V components, each a field of its own for ghost_value */
+    brick_t* br = (brick_t*)m->brick;
+    double* Vb[3] = {NULL, NULL, NULL};
+    if (br) {
+        for (int ci = 0; ci < 3; ++ci) {
+            Vb[ci] = (double*)malloc(sizeof(double) * NN * br->nb);
+            if (!Vb[ci]) { for (int q = 0; q < 3; ++q) free(Vb[q]); free(V); return -1; }
+            for (int l = 0; l < br->nb; ++l)
+                memcpy(Vb[ci] + (int64_t)l * NN, V + (int64_t)br->global[l] * 3 * NN + ci * NN, sizeof(double) * NN);
+        }
+    }
 #pragma omp parallel for schedule(dynamic)
     for (int b = 0; b < m->nblocks; ++b) {
         const double* cf = m->coef + (int64_t)b * 10 * NN;
+        const double h = full_spacing(m, b, N);
         for (int64_t n = 0; n < NN; ++n) {
             int x[3] = {(int)(n % N), (int)((n / N) % N), (int)(n / F)};
             double lap = 0;
@@ -738,6 +838,14 @@ int oracle_rhs_full(const oracle_mesh* m, const double* u, double* du) {
                         int t = tt[0] + N * tt[1];
                         y[d] = pos < 0 ? 0 : N - 1;
                         sn = y[0] + N * (y[1] + N * y[2]);
+                        if (m->face_nb[b * 6 + face] == -2) {
+                            for (int ci = 0; ci < 3; ++ci)
+                                Vw[ci] = ghost_value(&br->ctx, br->local[b], d, pos >= N, x, Vb[ci], 1.0);
+                            double Fd = 0;
+                            for (int ci = 0; ci < 3; ++ci) Fd += cf[(1 + 3 * d + ci) * NN + sn] * Vw[ci];
+                            acc += coefk * Fd;
+                            continue;
+                        }
                         if (m->face_nb[b * 6 + face] < 0 && m->boundary == 1) {
                             /* the ghost's flux 2 F* - F: the central flux is F* */
                             double Fo = 0, S2 = 0;
@@ -779,6 +887,7 @@ int oracle_rhs_full(const oracle_mesh* m, const double* u, double* du) {
         }
     }
     free(V);
+    for (int ci = 0; ci < 3; ++ci) free(Vb[ci]);
     return 0;
 }
 
@@ -938,10 +1047,13 @@ int oracle_full_prepare(oracle_mesh* m) {
         }
     }
     m->cache = c;
+    m->brick = brick_build(m);
     return 0;
 }
 
 void oracle_full_release(oracle_mesh* m) {
+    brick_free((brick_t*)m->brick);
+    m->brick = NULL;
     proj_cache_t* c = (proj_cache_t*)m->cache;
     if (!c) return;
     free(c->first); free(c->lu); free(c->piv); free(c->w); free(c->idx); free(c);
@@ -1035,10 +1147,10 @@ int oracle_energy_full(const oracle_mesh* m, const double* u, double* out) {
     double* V = (double*)malloc(sizeof(double) * 3 * NN * m->nblocks);
     if (!V) return -1;
     full_gradient(m, u, V);
-    const double h = 1.0 / N;
     double e = 0;
     for (int b = 0; b < m->nblocks; ++b) {
         const double* cf = m->coef + (int64_t)b * 10 * NN;
+        const double h = full_spacing(m, b, N);
         double s = 0;
         for (int64_t n = 0; n < NN; ++n) {
             double w = 1;
@@ -1052,7 +1164,7 @@ int oracle_energy_full(const oracle_mesh* m, const double* u, double* out) {
         /* a radiative boundary's own energy: inv_r sum w |S[d]| u^2 over its faces' nodes */
         if (m->boundary == 1 && m->inv_r != 0) {
             for (int face = 0; face < 6; ++face) {
-                if (m->face_nb[b * 6 + face] >= 0) continue;
+                if (m->face_nb[b * 6 + face] != -1) continue;
                 int d = face / 2;
                 for (int t = 0; t < N * N; ++t) {
                     int x[3];
@@ -1077,10 +1189,10 @@ int oracle_energy_full(const oracle_mesh* m, const double* u, double* out) {
 int oracle_norm_full(const oracle_mesh* m, const double* u, const double* ref, int p, int vars_mask, double* out) {
     const int P1 = m->P + 1, N = m->E * P1;
     const int64_t NN = (int64_t)N * N * N;
-    const double h = 1.0 / N;
     double num = 0, vol = 0;
     for (int b = 0; b < m->nblocks; ++b)
         for (int var = 0; var < 2; ++var) {
+            const double h = full_spacing(m, b, N);
             if (!(vars_mask & (1 << var))) continue;
             for (int64_t n = 0; n < NN; ++n) {
                 int64_t o = (int64_t)b * 2 * NN + var * NN + n;

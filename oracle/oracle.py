@@ -30,7 +30,7 @@ class OracleMesh(ctypes.Structure):
         ("elem_slot", ctypes.POINTER(ctypes.c_int32)), ("bnd_x", ctypes.POINTER(ctypes.c_double)),
         ("wave_k", ctypes.c_double * 3), ("wave_phi", ctypes.c_double), ("t", ctypes.c_double),
         ("boundary", ctypes.c_int), ("kappa", ctypes.c_double), ("inv_r", ctypes.c_double),
-        ("cache", ctypes.c_void_p),
+        ("cache", ctypes.c_void_p), ("brick", ctypes.c_void_p),
     ]
 
 
@@ -207,8 +207,8 @@ class BallOracle(Oracle):
                  stencil=np.ascontiguousarray(t["stencil"]).reshape(-1),
                  projector=np.ascontiguousarray(t["truncate"]).reshape(-1),
                  duals=np.ascontiguousarray(t["duals"]).reshape(-1),
-                 level=np.zeros(self.nblocks, dtype=np.int32),
-                 corner=np.zeros(3 * self.nblocks, dtype=np.int64),
+                 level=np.array(getattr(forest, "levels", [0] * self.nblocks), dtype=np.int32),
+                 corner=np.array([c if p == 0 else (0, 0, 0) for p, c in forest.blocks], dtype=np.int64).reshape(-1),
                  coef=np.ascontiguousarray(tables["coef"], dtype=np.float64),
                  face_nb=np.ascontiguousarray(forest.face_nb, dtype=np.int32),
                  face_code=np.ascontiguousarray(forest.face_code, dtype=np.int32),
@@ -218,8 +218,10 @@ class BallOracle(Oracle):
         self._arrays = a
         m = OracleMesh()
         m.D, m.P, m.E, m.nblocks, m.truncate = 3, P, self.E, self.nblocks, 1 if truncate else 0
+        n = forest.geo.patch_roots(0)[0]
         for k in range(3):
-            m.roots[k], m.periodic[k], m.reflecting[k], m.lo[k], m.hi[k] = 1, 0, 0, 0.0, 1.0
+            # a root block spans 1: the cube's n roots, a brick for a refined cube
+            m.roots[k], m.periodic[k], m.reflecting[k], m.lo[k], m.hi[k] = n, 0, 0, 0.0, float(n)
             m.wave_k[k] = wave.k[k] if wave is not None else 0.0
         m.wave_phi = wave.phi if wave is not None else 0.0
         m.metric = 2

@@ -8,10 +8,11 @@ from twoldg.ball import PlaneWave, ball_forest, ball_tables, node_logical, seven
 
 
 def ball_setup(P, E, roots, truncate=True, k=(1.1, -0.7, 0.5), phi=0.3, Rm=None, radiative=None, Lc=1.0, R1=3.0,
-               grading=0.0):
-    """A ball (the thirteen-patch one with Rm), its tables and its oracle;
-    radiative = (kappa, inverse_r) replaces the Dirichlet wave."""
-    forest, geo = ball_forest(np.float64, P, E, roots, Lc, R1, Rm=Rm, grading=grading)
+               grading=0.0, refined=False):
+    """A ball (the thirteen-patch one with Rm, its cube refined by `refined`),
+    its tables and its oracle; radiative = (kappa, inverse_r) replaces the
+    Dirichlet wave."""
+    forest, geo = ball_forest(np.float64, P, E, roots, Lc, R1, Rm=Rm, grading=grading, refined=refined)
     wave = PlaneWave(k, phi)
     tables = ball_tables(forest, P, wave)
     rad = None

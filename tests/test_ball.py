@@ -195,3 +195,119 @@ def test_dirichlet_data_of_any_form_converge_at_order_P():
     assert errs[0] < 1.2e-3
     rate = math.log(errs[0] / errs[1]) / math.log(hs[0] / hs[1])
     assert rate > 2.7, (errs, rate)
+
+
+# --- the refined cube (src/geometry.jl:494-553, test/sevenpatch_tests.jl:421-535) ---
+
+def _refined(P, roots=(4, 1), refined=True, Rm=None, k=(0.0, 0.0, 0.0), phi=0.0, truncate=False):
+    from twoldg.ball import ball_forest, ball_tables, PlaneWave
+    from oracle.oracle import BallOracle
+    forest, geo = ball_forest(np.float64, P, 2, roots, 1.0, 3.0, Rm=Rm, refined=refined)
+    wave = PlaneWave(k, phi)
+    tables = ball_tables(forest, P, wave)
+    return forest, geo, wave, tables, BallOracle(forest, P, tables, wave, truncate=truncate)
+
+
+def test_refined_ball_forest_and_its_refusals():
+    # refined=True refines the cube's middle half to level 1 and nothing else;
+    # a region reaching the cube's faces would refine a shell across the glue,
+    # and a region with no block centre in it refines nothing: both refused
+    from twoldg.ball import CUBE_FACE, sevenpatch_forest
+    f, geo = sevenpatch_forest(np.float64, 2, 2, roots=(4, 1), refined=True)
+    assert max(f.levels) == 1
+    assert all(p == 0 or lv == 0 for (p, _), lv in zip(f.blocks, f.levels))
+    assert f.nleaves() == 64 - 8 + 64 + 6 * 16
+    assert f.minimum_spacing() == pytest.approx(0.5 / f.N)
+    # the cube's inner faces are resolved by the library; the glue and the sphere as before
+    assert np.sum(f.face_nb == CUBE_FACE) > 0 and np.sum(f.face_nb == -1) == 6 * 16
+    with pytest.raises(ValueError, match="reaches the cube's faces"):
+        sevenpatch_forest(np.float64, 2, 2, roots=(4, 1), refined=((0.0, 2.0), (1.0, 3.0), (1.0, 3.0)))
+    with pytest.raises(ValueError, match="no block centre"):
+        sevenpatch_forest(np.float64, 2, 2, roots=(2, 1), refined=True)
+    # the inspiral's nested cubes inside the ball: two levels about the centre
+    from twoldg.forest import nested_cubes
+    g, _ = sevenpatch_forest(np.float64, 2, 2, roots=(8, 1), refined=nested_cubes(3, 1.0, 3))
+    assert max(g.levels) == 2
+
+
+@pytest.mark.parametrize("P", [2, 3])
+@pytest.mark.parametrize("truncate", [False, True])
+def test_refined_ball_energy_is_invariant(P, truncate):
+    # test/sevenpatch_tests.jl:421-444 on the oracle: with homogeneous data the
+    # Laplacian of the refined ball is self-adjoint in the sqrt(g)-weighted
+    # quadrature across the cube's coarse-fine faces and the glues (the coarse
+    # ghost of the Cartesian gradient the adjoint of the fine one), and with
+    # the truncation so is the projected operator, to 1e-13 of the terms
+    from ball_cases import physical_nodes
+    forest, geo, wave, tables, o = _refined(P, truncate=truncate)
+    X = physical_nodes(forest, tables)
+    r = np.linalg.norm(X, axis=1)
+    nb, N = forest.nleaves(), forest.N
+    NN = N ** 3
+    bump = lambda c: np.where(r < 1.5, np.cos(np.pi * r / 3.0) ** 4, 0.0) * (1 + 0.3 * X[:, c])
+
+    def op(a):
+        s = np.zeros((nb, 2, NN))
+        s[:, 1] = a
+        s = o.truncate(s.reshape(-1)) if truncate else s.reshape(-1)
+        s = s.reshape(nb, 2, NN)
+        s[:, 0], s[:, 1] = s[:, 1].copy(), 0.0
+        out = o.rhs(s.reshape(-1)).reshape(nb, 2, NN)
+        t = np.zeros((nb, 2, NN))
+        t[:, 1] = out[:, 1]
+        return (o.truncate(t.reshape(-1)) if truncate else t.reshape(-1)).reshape(nb, 2, NN)[:, 1]
+    P1 = P + 1
+    wq = Element(np.float64, P).weights
+    hs = np.array([forest.block_scale(b) / N for b in range(nb)])
+    w1 = hs[:, None] * P1 / 2 * wq[np.arange(N) % P1][None, :]
+    w = np.einsum("bi,bj,bk->bkji", w1, w1, w1).reshape(nb, NN) * tables["coef"].reshape(nb, 10, NN)[:, 0]
+    a, b = bump(0), bump(1)
+    la, lb = op(a), op(b)
+    lhs, rhs = np.sum(w * b * la), np.sum(w * lb * a)
+    scale = np.sum(np.abs(w * b * la))
+    assert scale > 1
+    assert abs(lhs - rhs) < 1e-13 * scale
+
+
+def test_refined_ball_time_step_is_the_binding_blocks():
+    # test/sevenpatch_tests.jl:480-497: the step is the smaller of each block's
+    # own spacing over its own speed, here the cube's finest blocks',
+    # h/(n/2Lc), and above the finest spacing over the fastest speed
+    P = 2
+    forest, geo, wave, tables, o = _refined(P)
+    h = forest.minimum_spacing()
+    assert tables["hspeed"] == pytest.approx(h / (4 / 2), rel=1e-14)
+    from twoldg.ball import ball_forest, ball_tables
+    uniform, _ = ball_forest(np.float64, P, 2, (4, 1), 1.0, 3.0)
+    t0 = ball_tables(uniform, P, wave)
+    speed = uniform.minimum_spacing() / t0["hspeed"]      # the fastest logical speed, uniform ball
+    assert tables["hspeed"] > 1.5 * h / speed
+
+
+def test_refined_ball_cube_takes_the_element_projector():
+    # test/sevenpatch_tests.jl:446-470: the cube's blocks hold no tables
+    # (slot 0, the element's tensor projector), the shells' theirs
+    forest, geo, wave, tables, o = _refined(3, truncate=True)
+    cube = np.array([p == 0 for p, _ in forest.blocks])
+    slot = np.asarray(tables["elem_slot"])
+    assert np.all((slot == 0) == cube)
+    assert sorted(slot[~cube]) == list(range(1, int(np.sum(~cube)) + 1))
+
+
+def test_refined_ball_plane_wave_as_accurate_as_uniform():
+    # test/sevenpatch_tests.jl:499-535 on the oracle: refining the cube adds
+    # resolution there and nothing else, so the error cannot grow
+    from ball_cases import ball_state
+    for P in (2, 3):
+        res = {}
+        for refined in (False, True):
+            forest, geo, wave, tables, o = _refined(P, refined=refined, k=(1.1, -0.7, 0.5), phi=0.3,
+                                                    truncate=True)
+            u0 = o.truncate(ball_state(forest, tables, lambda x, v: wave.state(x, 0.0, v)))
+            n = int(math.ceil(0.25 / (0.5 * tables["hspeed"] / (P + 1))))
+            u = o.rk4(u0, 0.25 / n, n, 0.0)
+            ue = ball_state(forest, tables, lambda x, v: wave.state(x, 0.25, v))
+            res[refined] = (o.norm(u, 2, 3, ue), forest.nleaves(), forest.minimum_spacing())
+        assert res[True][1] > res[False][1]
+        assert res[True][0] <= 1.01 * res[False][0]
+        assert res[True][2] == res[False][2] / 2

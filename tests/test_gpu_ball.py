@@ -152,3 +152,59 @@ def test_dirichlet_data_of_any_form_refusals(native):
     assert L.twoldg_rk4_step(p.handle, up, 0.01, dt, 1) == _lib.TWOLDG_OK
     p.synchronize()
     torch.cuda.synchronize()
+
+
+# --- the refined cube (src/geometry.jl:494-553): coarse-fine faces under the full metric ---
+
+@pytest.mark.parametrize("P,truncate,Rm,radiative", [(2, True, None, None), (3, False, None, None),
+                                                     (3, True, None, None), (3, True, 2.0, (1.0, True))],
+                         ids=["P2-trunc", "P3", "P3-trunc", "P3-thirteen-radiative"])
+def test_refined_ball_parity_f64(native, P, truncate, Rm, radiative):
+    """The ball with its cube refined (the middle half to level 1) through the
+    library against the oracle: right-hand side, truncation, four RK4 steps,
+    energy and norm to 1e-12; the seven-patch ball with the plane wave, and
+    the thirteen-patch one (roots (4, 1, 1)) under Sommerfeld's condition."""
+    import torch
+    import twoldg
+    from twoldg.ball import RadiativeBoundary
+    roots = (4, 1) if Rm is None else (4, 1, 1)
+    forest, geo, wave, tables, o = ball_setup(P, 2, roots, truncate, Rm=Rm, radiative=radiative, refined=True)
+    assert max(forest.levels) == 1
+    bnd = wave if radiative is None else RadiativeBoundary(*radiative)
+    p = twoldg.WaveProblem(forest, twoldg.Element(np.float64, P), truncate=truncate, geometry=forest.geo,
+                           boundary=bnd)
+    f = lambda x, v: np.sin(0.4 * x[0] + v) * np.cos(0.3 * x[1] - 0.2 * x[2]) + 0.1 * x[2] * v
+    u = ball_state(forest, tables, f)
+    ud = torch.from_numpy(u).cuda()
+    du = p.statevector()
+    twoldg.wave_rhs(du, ud, p, 0.25)
+    assert rel(du.cpu().numpy(), o.rhs(u, 0.25)) < 1e-12
+    if truncate:
+        w = ud.clone()
+        twoldg.truncate_state(w, p)
+        assert rel(w.cpu().numpy(), o.truncate(u)) < 1e-12
+    u0 = o.truncate(u) if truncate else u
+    dt = 0.5 * tables["hspeed"] / (P + 1)
+    integ = twoldg.wave_integrator(p, torch.from_numpy(u0).cuda(), 0.1, 0.1 + 4 * dt, dt)
+    integ.nsteps = 4
+    integ.solve()
+    ref = o.rk4(u0, dt, 4, 0.1)
+    assert rel(integ.u.cpu().numpy(), ref) < 1e-12
+    t1 = 0.1 + 4 * dt
+    assert twoldg.wave_energy(p, integ.u, t=t1) == pytest.approx(o.energy(ref, t1), rel=1e-12)
+    r = torch.from_numpy(u).cuda()
+    assert twoldg.quadrature_norm(p, integ.u, 2, ref=r) == pytest.approx(o.norm(ref, 2, 3, u), rel=1e-12)
+
+
+def test_refined_ball_plane_wave_accuracy(native):
+    # test/sevenpatch_tests.jl:499-535 through the library: refining the cube
+    # does not raise the plane wave's error, and halves the finest spacing
+    import twoldg
+    for P in (2, 3):
+        r0 = twoldg.sevenpatch_errors(np.float64, P=P, E=2, roots=(4, 1), tend=0.25)
+        r1 = twoldg.sevenpatch_errors(np.float64, P=P, E=2, roots=(4, 1), tend=0.25, refined=True)
+        assert r1["nblocks"] > r0["nblocks"]
+        assert r1["l2"] <= 1.01 * r0["l2"]
+        assert r1["h"] == r0["h"] / 2
+    r32 = twoldg.sevenpatch_errors(np.float32, P=3, E=2, roots=(4, 1), tend=0.25, refined=True, precision="f32c")
+    assert r32["l2"] == pytest.approx(r1["l2"], rel=1e-3)

@@ -201,7 +201,7 @@ struct twoldg_runner {
             }
             if (metric && !full && (!d.trunc_modes || !d.trunc_duals))
                 return fail(TWOLDG_EINVAL, "a metric (coef) needs its truncation pairs (trunc_modes, trunc_duals)");
-            if (metric && !m.cf.empty())
+            if (metric && !full && !m.cf.empty())
                 return fail(TWOLDG_EINVAL, "a geometry takes refinement only in an affine patch, which a diagonal "
                                            "metric's coefficients do not describe: no coarse-fine faces with coef");
             auto key = std::make_tuple(m.D, m.P, m.E, (d.truncate ? 1 : 0) + (metric ? 2 : 0) + (full ? 4 : 0));
@@ -259,7 +259,7 @@ struct twoldg_runner {
                 g->boundary = d.boundary;
                 g->bidx.assign((size_t)m.nblocks * 2 * m.D, -1);
                 for (size_t q = 0; q < g->bidx.size(); ++q)
-                    if (d.face_nb[q] < 0) g->bidx[q] = g->nbf++;
+                    if (d.face_nb[q] == -1) g->bidx[q] = g->nbf++;
                 g->kappa = d.kappa;
                 g->inv_r = d.inv_r;
                 g->fslot.assign(m.nblocks, 0);
@@ -311,6 +311,14 @@ struct twoldg_runner {
                 return fail(TWOLDG_EUNSUP, "block of N = " + std::to_string(g.E * (g.P + 1)) + " nodes per dim in " +
                                                std::to_string(g.D) + "D does not fit one CTA's shared memory");
         }
+        // The smallest shape groups first: their stage launches are few CTAs
+        // and bound by latency, so launched first they are all resident at once
+        // and the large groups' CTAs fill the GPU around them, where a large
+        // launch first would hold every SM until its last wave is dispatched.
+        std::stable_sort(groups.begin(), groups.end(), [](const std::unique_ptr<Group>& a,
+                                                          const std::unique_ptr<Group>& b) {
+            return (int64_t)a->items.size() * a->NN < (int64_t)b->items.size() * b->NN;
+        });
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         if (groups.size() > 1) {
             CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
@@ -340,7 +348,8 @@ struct twoldg_runner {
             size_t dbytes = g.cf.empty() ? 16 : fbytes;
             CK(g.ugd.alloc(dbytes));
             CK(g.gfd.alloc(dbytes));
-            CK(g.ggd.alloc(dbytes));
+            // the full metric's dense gradient ghosts are the three Cartesian components
+            CK(g.ggd.alloc(g.full && !g.cf.empty() ? 3 * dbytes : dbytes));
             CK(g.d_part.alloc(g.items.size() * sizeof(double)));
             CK(g.d_part2.alloc(g.items.size() * sizeof(double)));
             if (g.full) {
@@ -494,6 +503,8 @@ struct twoldg_runner {
         p.fachol = g.d_fachol.p;
         p.bidx = (const int*)g.d_bidx.p;
         p.btab = (const BoundaryTable*)g.d_btab.p;
+        p.ugd = g.cf.empty() ? nullptr : g.ugd.p;
+        p.vgd = g.cf.empty() ? nullptr : g.ggd.p;
         p.ew = g.d_ew.p;
         p.echol = g.d_echol.p;
         p.partial = (double*)g.d_part.p;
@@ -559,10 +570,25 @@ struct twoldg_runner {
     }
 
     // Stage s of group g (reading the face planes `in`), enqueued on st.
+    // The full metric's coarse-fine ghosts (a refined brick patch): u's from
+    // the face exports before the gradient pass (vars 1), V's from its face
+    // planes before the stage pass (vars 3).
+    int fm_dense(Group& g, const FmPtrs& fp, int vars, cudaStream_t st) {
+        if (g.cf.empty()) return TWOLDG_OK;
+        const void* src = vars == 1 ? fp.fu_in : (const void*)fp.fv;
+        void* dst = vars == 1 ? g.ugd.p : g.ggd.p;
+        CK(g.ops->cf_planes((const CfFace*)g.d_cf.p, (int)g.cf.size(), g.E, src, dst, vars, st));
+        return TWOLDG_OK;
+    }
+
     int enqueue_stage(Group& g, void* u, int s, int in, cudaStream_t st) {
         if (g.full) {
             FmPtrs fp = fptrs(g, u, in);
+            int r = fm_dense(g, fp, 1, st);
+            if (r) return r;
             CK(g.ops->fm_gradient((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, fp, st));
+            r = fm_dense(g, fp, 3, st);
+            if (r) return r;
             CK(g.ops->fm_stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, fp, st));
             return TWOLDG_OK;
         }
@@ -887,7 +913,11 @@ int twoldg_rhs(twoldg_problem* p, void* du, const void* u, double t) {
         if (r) return r;
         FmPtrs fp = p->fptrs(g, const_cast<void*>(u), 0);
         fp.du = du;
+        r = p->fm_dense(g, fp, 1, p->stream);
+        if (r) return r;
         CK(g.ops->fm_gradient((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, 0, fp, p->stream));
+        r = p->fm_dense(g, fp, 3, p->stream);
+        if (r) return r;
         CK(g.ops->fm_stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, 0, 0, fp, p->stream));
         return TWOLDG_OK;
     }
@@ -934,6 +964,8 @@ int twoldg_energy(twoldg_problem* p, const void* u, double t, double* energy) {
         if (!r) r = p->set_time(t, nullptr);
         if (r) return r;
         FmPtrs fp = p->fptrs(g, const_cast<void*>(u), 0);
+        r = p->fm_dense(g, fp, 1, p->stream);
+        if (r) return r;
         CK(g.ops->fm_gradient((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, 5, fp, p->stream));
         CK(g.ops->fm_energy((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, fp, p->stream));
     } else {

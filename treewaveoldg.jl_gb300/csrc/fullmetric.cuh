@@ -75,6 +75,10 @@ struct FmArgs {
     // boundary face index of every face slot)
     const int* bidx;
     const BoundaryTable* btab;
+    // coarse-fine faces of a refined brick patch (flags bit f of an item):
+    // u's ghosts (N^2 per slot) and V's ((3, N^2) per slot)
+    const T* ugd;
+    const T* vgd;
 };
 
 template <typename T, int P>
@@ -145,7 +149,10 @@ __global__ void __launch_bounds__(256) fm_gradient_kernel(FmArgs<T> a, Tab<T, P>
             const int f = i / g.F, tt = i % g.F;
             const int d = f >> 1, side = f & 1;
             T v;
-            if (it.nb[f] < 0 && a.boundary == 1) {
+            if (it.flags & (1u << f)) {
+                // a coarse-fine face: the neighbour's u through I or R
+                v = a.ugd[(int64_t)(it.slot + f) * g.F + tt];
+            } else if (it.nb[f] < 0 && a.boundary == 1) {
                 // radiative: the face node's own u, so that the wide derivative's
                 // face correction vanishes there (src/evolution.jl:1213-1221)
                 int xo[3];
@@ -478,7 +485,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 4) fm_stage_kernel(F
                 plane_coords<3>(g, d, tt, side == 0 ? 0 : g.N - 1, xo);
                 plane_coords<3>(g, d, tt, side == 0 ? -1 : g.N, xg);
                 const int o = oidx<3>(g, xo);
-                if (it.nb[f] < 0 && a.boundary == 1) {
+                if (it.nb[f] < 0 && !(it.flags & (1u << f)) && a.boundary == 1) {
                     // radiative: the ghost's flux 2 F* - F, so that the central
                     // flux through the face is F* = -sigma |S[d]| (kappa v + u / R)
                     // (src/evolution.jl:1232-1260)
@@ -496,7 +503,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 4) fm_stage_kernel(F
                     continue;
                 }
                 T Vg[3];
-                if (it.nb[f] < 0 && a.boundary == 2) {
+                if (it.flags & (1u << f)) {
+                    const T* src = a.vgd + (int64_t)(it.slot + f) * 3 * g.F;
+#pragma unroll
+                    for (int ci = 0; ci < 3; ++ci) Vg[ci] = src[ci * g.F + tt];
+                } else if (it.nb[f] < 0 && a.boundary == 2) {
                     const double* bv = boundary_values(a, it.slot + f, t, g.F);
 #pragma unroll
                     for (int ci = 0; ci < 3; ++ci) Vg[ci] = (T)bv[(1 + ci) * g.F + tt];
@@ -650,7 +661,7 @@ __global__ void __launch_bounds__(256) fm_energy_kernel(FmArgs<T> a, Tab<T, P> t
             const T* uu = a.u + it.off;
             for (int i = threadIdx.x; i < 6 * g.F; i += blockDim.x) {
                 const int f = i / g.F, tt = i % g.F;
-                if (it.nb[f] >= 0) continue;
+                if (it.nb[f] >= 0 || (it.flags & (1u << f))) continue;
                 const int d = f >> 1, side = f & 1;
                 int x[3];
                 plane_coords<3>(g, d, tt, side == 0 ? 0 : g.N - 1, x);

@@ -231,11 +231,12 @@ __global__ void export_faces_kernel(const BlockItem* items, int nitems, int E, c
 // them fastest. One thread per (cf face, t).
 template <typename T, int D, int P>
 __device__ __forceinline__ T cf_apply(const CfFace& c, int t, int N, int E, int F, const T* src,
-                                      const CfTab<T, P>& ct) {
+                                      const CfTab<T, P>& ct, int64_t sstride = -1) {
+    if (sstride < 0) sstride = F;   // words per face slot of src
     constexpr int P1 = P + 1;
     constexpr int DT = D - 1;
     if constexpr (DT == 0) {
-        return src[(int64_t)c.src[0] * F];
+        return src[(int64_t)c.src[0] * sstride];
     } else {
         int n[DT];
         {
@@ -252,7 +253,7 @@ __device__ __forceinline__ T cf_apply(const CfFace& c, int t, int N, int E, int 
                 row[k] = (e & 1) * P1 + i;
                 cb[k] = (q * halfE + e / 2) * P1;
             }
-            const T* s = src + (int64_t)c.src[0] * F;
+            const T* s = src + (int64_t)c.src[0] * sstride;
             T acc = T(0);
             if constexpr (DT == 1) {
 #pragma unroll
@@ -277,7 +278,7 @@ __device__ __forceinline__ T cf_apply(const CfFace& c, int t, int N, int E, int 
                 bits |= q << k;
                 fb[k] = 2 * (ec % halfE) * P1;
             }
-            const T* s = src + (int64_t)c.src[bits] * F;
+            const T* s = src + (int64_t)c.src[bits] * sstride;
             T acc = T(0);
             if constexpr (DT == 1) {
 #pragma unroll
@@ -310,6 +311,26 @@ __global__ void cf_ghost_u_kernel(const CfFace* cf, int ncf, int E, const T* fu,
         int64_t o = (int64_t)face.slot * F + t;
         ugd[o] = ug;
         gfd[o] = (fog[o] + ghost_coef<T, P>(tb, face.side) * ug) / T(face.h);
+    }
+}
+
+// The coarse-fine image of `vars` planes per face slot ((vars, F) per slot):
+// the full metric's u ghosts (vars 1, from the face exports) and Cartesian
+// gradient ghosts (vars 3, from the V face planes) of a refined brick patch,
+// where the map is affine and the flat problem's I and R apply to each.
+template <typename T, int D, int P>
+__global__ void cf_plane_kernel(const CfFace* cf, int ncf, int E, int vars, const T* src, T* dst, CfTab<T, P> ct) {
+    int N = E * (P + 1);
+    int F = ipow(N, D - 1);
+    int64_t total = (int64_t)ncf * vars * F;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int t = (int)(i % F);
+        const int comp = (int)((i / F) % vars);
+        const int c = (int)(i / ((int64_t)F * vars));
+        CfFace face = cf[c];
+        dst[((int64_t)face.slot * vars + comp) * F + t] =
+            cf_apply<T, D, P>(face, t, N, E, F, src + (int64_t)comp * F, ct, (int64_t)vars * F);
     }
 }
 

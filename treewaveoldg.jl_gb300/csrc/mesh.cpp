@@ -35,8 +35,108 @@ struct Key {
 
 }  // namespace
 
+// The faces of a refined brick patch inside an explicit face table (the
+// ball's affine cube): the blocks whose faces are marked TWOLDG_FACE_BRICK
+// are leaves of a brick of roots[d] root blocks, at their level and corner,
+// and each such face is resolved as build_mesh resolves a brick's faces: a
+// same-level neighbour by injection, a coarser one as the fine side of a
+// coarse-fine face (I), 2^(D-1) finer ones as its coarse side (R).
+static bool brick_faces(const twoldg_desc& d, Mesh& m, std::string& err) {
+    std::ostringstream es;
+    const int D = d.dim;
+    std::map<Key, int> leaves;
+    for (int b = 0; b < d.nblocks; ++b) {
+        bool in = false;
+        for (int f = 0; f < 2 * D; ++f) in = in || d.face_nb[b * 2 * D + f] == TWOLDG_FACE_BRICK;
+        if (!in && d.level[b] == 0) continue;
+        Key key{d.level[b], {0, 0, 0}};
+        if (key.level < 0 || key.level > 20) { es << "block " << b << " has level " << key.level; err = es.str(); return false; }
+        for (int k = 0; k < D; ++k) {
+            key.c[k] = d.corner[(int64_t)b * D + k];
+            const int64_t ext = (int64_t)d.roots[k] << key.level;
+            if (key.c[k] < 0 || key.c[k] >= ext) {
+                es << "block " << b << " corner[" << k << "] = " << key.c[k] << " is outside the brick [0, " << ext
+                   << ")";
+                err = es.str();
+                return false;
+            }
+        }
+        if (!leaves.emplace(key, b).second) { es << "block " << b << " duplicates another leaf"; err = es.str(); return false; }
+    }
+    auto slot = [&](int b, int f) { return b * 2 * D + f; };
+    for (const auto& kv : leaves) {
+        const int b = kv.second, lv = kv.first.level;
+        const int64_t* c = kv.first.c;
+        BlockItem& it = m.items[b];
+        for (int f = 0; f < 2 * D; ++f) {
+            if (d.face_nb[b * 2 * D + f] != TWOLDG_FACE_BRICK) continue;
+            const int dd = f / 2, side = f % 2;
+            Key n{lv, {c[0], c[1], c[2]}};
+            n.c[dd] += side ? 1 : -1;
+            if (n.c[dd] < 0 || n.c[dd] >= ((int64_t)d.roots[dd] << lv)) {
+                es << "block " << b << " face " << f << " is marked a brick face and leaves the brick";
+                err = es.str();
+                return false;
+            }
+            auto same = leaves.find(n);
+            if (same != leaves.end()) {
+                it.nb[f] = slot(same->second, f ^ 1);
+                m.nsame++;
+                continue;
+            }
+            if (lv > 0) {
+                Key p{lv - 1, {0, 0, 0}};
+                for (int k = 0; k < D; ++k) p.c[k] = n.c[k] >> 1;
+                auto coarse = leaves.find(p);
+                if (coarse != leaves.end()) {
+                    CfFace cf{};
+                    cf.slot = slot(b, f);
+                    cf.kind = 0;
+                    cf.src[0] = slot(coarse->second, f ^ 1);
+                    int bit = 0;
+                    for (int k = 0; k < D; ++k) {
+                        if (k == dd) continue;
+                        cf.sub |= (int)(c[k] & 1) << bit;
+                        ++bit;
+                    }
+                    cf.side = side;
+                    cf.h = m.h[b];
+                    m.cf.push_back(cf);
+                    it.flags |= 1u << f;
+                    continue;
+                }
+            }
+            CfFace cf{};
+            cf.slot = slot(b, f);
+            cf.kind = 1;
+            cf.side = side;
+            cf.h = m.h[b];
+            for (int q = 0; q < (1 << (D - 1)); ++q) {
+                Key ch{lv + 1, {0, 0, 0}};
+                int bit = 0;
+                for (int k = 0; k < D; ++k) {
+                    if (k == dd) ch.c[k] = 2 * n.c[k] + (side ? 0 : 1);
+                    else { ch.c[k] = 2 * n.c[k] + ((q >> bit) & 1); ++bit; }
+                }
+                auto fine = leaves.find(ch);
+                if (fine == leaves.end()) {
+                    es << "block " << b << " face " << f << " has no neighbour one level apart at most: the brick "
+                       << "must be 2:1 balanced across faces and tile its patch";
+                    err = es.str();
+                    return false;
+                }
+                cf.src[q] = slot(fine->second, f ^ 1);
+            }
+            m.cf.push_back(cf);
+            it.flags |= 1u << f;
+        }
+    }
+    return true;
+}
+
 // An explicit face table (a forest of glued patches): neighbours, faces and
-// orientations as given; a face with no neighbour is a boundary face.
+// orientations as given; a face with no neighbour is a boundary face, and the
+// faces marked TWOLDG_FACE_BRICK are those of a refined brick patch.
 static bool build_explicit(const twoldg_desc& d, Mesh& m, std::string& err) {
     std::ostringstream es;
     const int D = d.dim;
@@ -44,9 +144,14 @@ static bool build_explicit(const twoldg_desc& d, Mesh& m, std::string& err) {
     m.items.assign(d.nblocks, BlockItem{});
     m.hmin = INFINITY;
     const double cell = (d.hi[0] - d.lo[0]) / d.roots[0];
+    bool brick = false;
     for (int b = 0; b < d.nblocks; ++b) {
-        if (d.level[b] != 0) { err = "a forest with an explicit face table takes level-0 blocks only"; return false; }
-        m.h[b] = cell / m.N;
+        if (d.level[b] < 0 || d.level[b] > 20) {
+            es << "block " << b << " has level " << d.level[b];
+            err = es.str();
+            return false;
+        }
+        m.h[b] = cell / std::ldexp(1.0, d.level[b]) / m.N;
         m.hmin = std::fmin(m.hmin, m.h[b]);
         BlockItem& it = m.items[b];
         it.off = (int64_t)b * 2 * m.NN;
@@ -56,6 +161,7 @@ static bool build_explicit(const twoldg_desc& d, Mesh& m, std::string& err) {
         for (int f = 0; f < 2 * D; ++f) {
             const int nb = d.face_nb[b * 2 * D + f];
             const int code = d.face_code[b * 2 * D + f];
+            if (nb == TWOLDG_FACE_BRICK) { brick = true; continue; }
             if (nb < 0) { m.nwall++; continue; }
             const int nf = code & 15, o = (code >> 4) & 7;
             if (nb >= d.nblocks || nf >= 2 * D) {
@@ -69,12 +175,18 @@ static bool build_explicit(const twoldg_desc& d, Mesh& m, std::string& err) {
                 err = es.str();
                 return false;
             }
+            if (d.level[nb] != d.level[b]) {
+                es << "blocks " << b << " and " << nb << " meet across an explicit face at levels " << d.level[b]
+                   << " and " << d.level[nb] << ": only a brick patch's faces join blocks of two levels";
+                err = es.str();
+                return false;
+            }
             it.nb[f] = nb * 2 * D + nf;
             it.orient |= (uint32_t)o << (3 * f);
             m.nsame++;
         }
     }
-    return true;
+    return !brick || brick_faces(d, m, err);
 }
 
 bool build_mesh(const twoldg_desc& d, Mesh& m, std::string& err) {

@@ -65,6 +65,8 @@ struct FmPtrs {
     const void* fachol;
     const int* bidx;    // boundary kind 2: per face slot its boundary face index (-1 inside)
     const BoundaryTable* btab;
+    const void* ugd;    // coarse-fine faces (a refined brick patch): u's ghosts per slot (N^2)
+    const void* vgd;    // and V's, (3, N^2) per slot
 };
 
 // A launch layout of the stage kernel. kernel: 0 the shape's default, 1 the
@@ -99,6 +101,9 @@ public:
                                  cudaStream_t s) const = 0;
     virtual cudaError_t cf_ghosts(const CfFace* cf, int ncf, int E, const void* fu, const void* fog, void* ugd,
                                   void* gfd, void* ggd, cudaStream_t s) const = 0;
+    // the coarse-fine image (I or R) of `vars` face planes per slot (vars, N^(D-1)) into dst
+    virtual cudaError_t cf_planes(const CfFace* cf, int ncf, int E, const void* src, void* dst, int vars,
+                                  cudaStream_t s) const = 0;
     virtual cudaError_t stage(const BlockItem* items, int nitems, int E, int mode, int truncate,
                               const StagePtrs& p, int grid, cudaStream_t s) const = 0;
     virtual cudaError_t energy(const BlockItem* items, int nitems, int E, const StagePtrs& p,

@@ -257,6 +257,16 @@ public:
         return cudaGetLastError();
     }
 
+    cudaError_t cf_planes(const CfFace* cf, int ncf, int E, const void* src, void* dst, int vars,
+                          cudaStream_t s) const override {
+        if (ncf == 0) return cudaSuccess;
+        int64_t F = 1;
+        for (int k = 0; k < D - 1; ++k) F *= (int64_t)E * (P + 1);
+        int g = grid_for((int64_t)ncf * vars * F, 256);
+        cf_plane_kernel<T, D, P><<<g, 256, 0, s>>>(cf, ncf, E, vars, (const T*)src, (T*)dst, ct_);
+        return cudaGetLastError();
+    }
+
     cudaError_t stage(const BlockItem* items, int nitems, int E, int mode, int truncate, const StagePtrs& p,
                       int grid, cudaStream_t s) const override {
         StageArgs<T> a;
@@ -480,6 +490,8 @@ public:
         a.fachol = (const T*)p.fachol;
         a.bidx = p.bidx;
         a.btab = p.btab;
+        a.ugd = (const T*)p.ugd;
+        a.vgd = (const T*)p.vgd;
         return a;
     }
     static size_t fm_grad_smem(int E) { return (padded_words(E) + 3 * plain_words(E)) * sizeof(T); }

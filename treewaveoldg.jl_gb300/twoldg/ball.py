@@ -240,9 +240,13 @@ class ThirteenPatchBall:
         return (2.0 / n) ** 2 / (q * np.sqrt(q))
 
 class BallForest:
-    """The forest of a ball: its patches' root blocks (level 0) and
-    the explicit face table. Blocks are ordered patch by patch, and within a
-    patch by corner with the first dimension fastest."""
+    """The forest of a ball: its patches' blocks and the explicit face table.
+    Blocks are ordered patch by patch, and within a patch by corner with the
+    first dimension fastest; a refined cube (patch 0) holds its leaves in the
+    Morton order of a refined box. Every root block has logical extent 1, a
+    block of level L 2^-L, and `levels` holds each block's level (only the
+    affine cube refines); `leaves` pairs it with the corner, counted in
+    blocks of that level."""
 
     def __init__(self, geo, N):
         self.geo = geo
@@ -255,7 +259,9 @@ class BallForest:
                 for c1 in range(r[1]):
                     for c0 in range(r[0]):
                         self.blocks.append((p, (c0, c1, c2)))
-        self.leaves = [(0, c) for _, c in self.blocks]   # level 0, for layout helpers
+        self.levels = [0] * len(self.blocks)
+        self.leaves = [(0, c) for _, c in self.blocks]
+        self.refined = False
         self.face_nb = None
         self.face_code = None
 
@@ -263,15 +269,46 @@ class BallForest:
         return len(self.blocks)
 
     def spacing(self, key=None):
-        return 1.0 / self.N                 # every root block has logical extent 1
+        return (1.0 if key is None else 2.0 ** -key[0]) / self.N
 
     def minimum_spacing(self):
-        return 1.0 / self.N
+        return 2.0 ** -max(self.levels) / self.N
+
+    def block_scale(self, b):
+        """The logical extent of block b: 2^-level."""
+        return 2.0 ** -self.levels[b]
 
 
-def face_plane_logical(corner, N, offs, f):
+def refine_cube(forest, refined):
+    """The ball's cube (patch 0, n roots per side) refined as wave_forest
+    refines a box (src/geometry.jl:540-553): `refined` is True (the middle
+    half, (n/4, 3n/4)^3), a tuple of three intervals (one region), or a list
+    of such tuples (one region per level), in the cube's logical coordinates
+    [0, n]^3, each level balanced 2:1 across faces, edges and corners. The
+    glue keeps the leaves across a glued face at one level, so a refinement
+    that reaches the cube's faces would refine a shell, whose map is not
+    affine, and is refused."""
+    from .forest import Forest, refine_regions, refinement_regions
+    n = forest.geo.patch_roots(0)[0]
+    cube = Forest([n] * 3, forest.N, [0.0] * 3, [float(n)] * 3, [False] * 3, [True] * 3)
+    refine_regions(cube, refinement_regions(refined, 3, float(n)), n)
+    for lv, c in cube.leaves:
+        if lv > 0 and any(c[k] == 0 or c[k] == (n << lv) - 1 for k in range(3)):
+            raise ValueError("the refinement %r reaches the cube's faces, and the glue keeps the leaves across a "
+                             "glued face at one level, so it would refine a shell, whose map is not affine: keep "
+                             "the regions at least one root inside the cube [0, %d]^3" % (refined, n))
+    shells = [(p, c) for p, c in forest.blocks if p != 0]
+    forest.blocks = [(0, c) for _, c in cube.leaves] + shells
+    forest.levels = [lv for lv, _ in cube.leaves] + [0] * len(shells)
+    forest.leaves = [(lv, c) for lv, (_, c) in zip(forest.levels, forest.blocks)]
+    forest.refined = max(forest.levels) > 0
+    return forest
+
+
+def face_plane_logical(corner, N, offs, f, scale=1.0):
     """Logical coordinates (3 arrays of N^2) of the face-node plane of face f of
-    a block at integer corner; tangential dims in increasing order, first fastest."""
+    a block at integer corner and of extent `scale` (2^-level); tangential
+    dims in increasing order, first fastest."""
     P1 = len(offs)
     n = np.arange(N)
     x1d = (n // P1) * P1 + offs[n % P1]
@@ -279,9 +316,9 @@ def face_plane_logical(corner, N, offs, f):
     tang = [k for k in range(3) if k != d]
     a, b = np.meshgrid(x1d, x1d, indexing="xy")   # a varies fastest along columns
     coords = [None] * 3
-    coords[tang[0]] = corner[tang[0]] + a.reshape(-1) / N
-    coords[tang[1]] = corner[tang[1]] + b.reshape(-1) / N
-    coords[d] = np.full(N * N, float(corner[d] + (1 if side else 0)))
+    coords[tang[0]] = (corner[tang[0]] + a.reshape(-1) / N) * scale
+    coords[tang[1]] = (corner[tang[1]] + b.reshape(-1) / N) * scale
+    coords[d] = np.full(N * N, float(corner[d] + (1 if side else 0)) * scale)
     return coords
 
 
@@ -297,8 +334,15 @@ def orient(a, b, code, N):
     return a, b
 
 
+# face_nb of a face between two blocks of a refined cube: the library finds
+# the neighbour, or the coarse-fine partners, by level and corner
+CUBE_FACE = -2
+
+
 def build_ball_faces(forest, offsets):
-    """The face table of a ball forest by matching face-node positions."""
+    """The face table of a ball forest by matching face-node positions. In a
+    refined cube every face between two cube blocks is CUBE_FACE, which the
+    library's mesh compiler resolves by the blocks' levels and corners."""
     geo, N = forest.geo, forest.N
     nb = forest.nleaves()
     face_nb = np.full(nb * 6, -1, dtype=np.int32)
@@ -308,22 +352,26 @@ def build_ball_faces(forest, offsets):
     centre = {}
     for bi, (p, c) in enumerate(forest.blocks):
         for f in range(6):
-            x = geo.position(face_plane_logical(c, N, offsets, f), p)
+            x = geo.position(face_plane_logical(c, N, offsets, f, forest.block_scale(bi)), p)
             X = np.stack([np.asarray(v) for v in x], axis=-1)
             pos[(bi, f)] = X
             centre[(bi, f)] = X.mean(axis=0)
     # same-patch neighbours first
     for bi, (p, c) in enumerate(forest.blocks):
         r = geo.patch_roots(p)
+        lv = forest.levels[bi]
         for f in range(6):
             d, side = f // 2, f % 2
             cn = list(c)
             cn[d] += 1 if side else -1
-            if 0 <= cn[d] < r[d]:
-                face_nb[bi * 6 + f] = index[(p, tuple(cn))]
-                face_code[bi * 6 + f] = (f ^ 1)
+            if 0 <= cn[d] < (r[d] << lv):
+                if forest.refined and p == 0:
+                    face_nb[bi * 6 + f] = CUBE_FACE
+                else:
+                    face_nb[bi * 6 + f] = index[(p, tuple(cn))]
+                    face_code[bi * 6 + f] = (f ^ 1)
     # glued faces: the unmatched faces whose face-node centres coincide
-    open_faces = [(bi, f) for bi in range(nb) for f in range(6) if face_nb[bi * 6 + f] < 0]
+    open_faces = [(bi, f) for bi in range(nb) for f in range(6) if face_nb[bi * 6 + f] == -1]
     keys = {}
     scale = geo.R1
     for bf in open_faces:
@@ -363,21 +411,24 @@ def build_ball_faces(forest, offsets):
     return face_nb, face_code
 
 
-def sevenpatch_forest(T, P, E, roots=(2, 2), Lc=1.0, R1=3.0, grading=0.0):
-    """The ball forest and its map (src/geometry.jl:525-538)."""
+def sevenpatch_forest(T, P, E, roots=(2, 2), Lc=1.0, R1=3.0, grading=0.0, refined=False):
+    """The ball forest and its map (src/geometry.jl:494-538); `refined`
+    refines the affine cube (refine_cube)."""
     from .element import Element
     if E % 2:
         raise ValueError("E = %d elements of order P = %d per block is odd, and E must be even" % (E, P))
     geo = SevenPatchBall(Lc, R1, roots, grading)
     forest = BallForest(geo, E * (P + 1))
+    if refined is not False:
+        refine_cube(forest, refined)
     build_ball_faces(forest, Element(np.float64, P).offsets.astype(np.float64))
     return forest, geo
 
 
-def thirteenpatch_forest(T, P, E, roots=(2, 1, 1), Lc=1.0, Rm=2.0, R1=3.0):
+def thirteenpatch_forest(T, P, E, roots=(2, 1, 1), Lc=1.0, Rm=2.0, R1=3.0, refined=False):
     """The thirteen-patch ball's forest and its map (src/geometry.jl:719-751):
     roots = (n, m, m'), the cube's per side and the inner and outer shells'
-    radial ones."""
+    radial ones; `refined` refines the affine cube (refine_cube)."""
     from .element import Element
     if E % 2:
         raise ValueError("E = %d elements of order P = %d per block is odd, and E must be even" % (E, P))
@@ -386,18 +437,20 @@ def thirteenpatch_forest(T, P, E, roots=(2, 1, 1), Lc=1.0, Rm=2.0, R1=3.0):
                          "and outer shells' radial ones, got %r" % (tuple(roots),))
     geo = ThirteenPatchBall(Lc, Rm, R1, roots)
     forest = BallForest(geo, E * (P + 1))
+    if refined is not False:
+        refine_cube(forest, refined)
     build_ball_faces(forest, Element(np.float64, P).offsets.astype(np.float64))
     return forest, geo
 
 
-def ball_forest(T, P, E, roots, Lc, R1, Rm=None, grading=0.0):
+def ball_forest(T, P, E, roots, Lc, R1, Rm=None, grading=0.0, refined=False):
     """The seven-patch ball, or with a middle radius Rm the thirteen-patch one
     (src/sevenpatch.jl:119-128)."""
     if Rm is None:
-        return sevenpatch_forest(T, P, E, roots=roots, Lc=Lc, R1=R1, grading=grading)
+        return sevenpatch_forest(T, P, E, roots=roots, Lc=Lc, R1=R1, grading=grading, refined=refined)
     if grading != 0:
         raise ValueError("the thirteen-patch ball's inner shells are ungraded: grading must be 0 with Rm")
-    return thirteenpatch_forest(T, P, E, roots=roots, Lc=Lc, Rm=Rm, R1=R1)
+    return thirteenpatch_forest(T, P, E, roots=roots, Lc=Lc, Rm=Rm, R1=R1, refined=refined)
 
 
 def node_logical(forest, P, offsets):
@@ -409,8 +462,9 @@ def node_logical(forest, P, offsets):
     grids = np.indices([N] * 3).reshape(3, -1)[::-1]
     out = np.empty((forest.nleaves(), 3, N ** 3))
     for b, (p, c) in enumerate(forest.blocks):
+        s = forest.block_scale(b)
         for k in range(3):
-            out[b, k] = c[k] + x1d[grids[k]] / N
+            out[b, k] = (c[k] + x1d[grids[k]] / N) * s
     return out
 
 
@@ -544,8 +598,10 @@ def ball_tables(forest, P, wave=None):
     NN = N ** 3
     coef = np.empty((nb, 10, NN))
     hspeed = math.inf
-    h = 1.0 / N
     for b, (p, c) in enumerate(forest.blocks):
+        # the time step is the CFL limit of the block that binds: its own
+        # spacing over its own largest logical speed
+        h = forest.block_scale(b) / N
         J, S = geo.frame(tuple(xl[b, k] for k in range(3)), p)
         coef[b, 0] = J
         for d in range(3):
@@ -591,7 +647,7 @@ def ball_tables(forest, P, wave=None):
     for b, (p, c) in enumerate(forest.blocks):
         for f in range(6):
             if forest.face_nb[b * 6 + f] < 0:
-                x = geo.position(face_plane_logical(c, N, offs, f), p)
+                x = geo.position(face_plane_logical(c, N, offs, f, forest.block_scale(b)), p)
                 bnd[b * 6 + f] = np.stack([np.asarray(v) for v in x])
     out = dict(coef=np.ascontiguousarray(coef.reshape(-1)), elem_slot=slot, elem_w=ew, elem_chol=echol,
                ntab=len(ws), bnd_x=np.ascontiguousarray(bnd.reshape(-1)), hspeed=hspeed, xl=xl)
@@ -683,14 +739,18 @@ def ball_desc(forest, P, truncate, precision, tables, wave):
     d.precision = precision
     d.truncate = 1 if truncate else 0
     d.nblocks = nb
+    # a root block has logical extent 1: the cube's n roots per side span [0, n]
+    n = forest.geo.patch_roots(0)[0]
     for k in range(3):
-        d.roots[k] = 1
+        d.roots[k] = n
         d.periodic[k] = 0
         d.reflecting[k] = 0
         d.lo[k] = 0.0
-        d.hi[k] = 1.0
-    levels = np.zeros(nb, dtype=np.int32)
-    corners = np.zeros(nb * 3, dtype=np.int64)
+        d.hi[k] = float(n)
+    # the blocks' levels, and the cube's corners (in blocks of their level),
+    # by which the library resolves the refined cube's faces
+    levels = np.array(forest.levels, dtype=np.int32)
+    corners = np.array([c if p == 0 else (0, 0, 0) for p, c in forest.blocks], dtype=np.int64).reshape(-1)
     ip, dp = ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)
     d.level = levels.ctypes.data_as(ip)
     d.corner = corners.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
@@ -735,15 +795,15 @@ def sevenpatch_exact(geo, wave, t, forest=None):
 
 
 def sevenpatch_errors(T=np.float64, P=3, E=2, roots=(2, 2), Lc=1.0, R1=3.0, k=(1.1, -0.7, 0.5), phi=0.3, cfl=0.5,
-                      tend=1.0, truncate=True, precision=None, Rm=None):
+                      tend=1.0, truncate=True, precision=None, Rm=None, refined=False):
     """sevenpatch_errors (src/sevenpatch.jl:61-117): the plane wave on the ball
-    to tend with itself as the Dirichlet data on the sphere; sqrt(g)-weighted L2
-    errors of u and v together and apart, Linf, the cube's physical spacing,
-    the step count and the energies."""
+    (its cube refined by `refined`) to tend with itself as the Dirichlet data
+    on the sphere; sqrt(g)-weighted L2 errors of u and v together and apart,
+    Linf, the cube's physical spacing, the step count and the energies."""
     from .element import Element
     from .problem import WaveProblem, initial_state, oldg_timestep, quadrature_norm, wave_energy, wave_integrator
     T = np.dtype(T)
-    forest, geo = ball_forest(T, P, E, roots, Lc, R1, Rm=Rm)
+    forest, geo = ball_forest(T, P, E, roots, Lc, R1, Rm=Rm, refined=refined)
     wave = PlaneWave(k, phi)
     problem = WaveProblem(forest, Element(T, P), truncate=truncate, geometry=geo, boundary=wave,
                           precision=precision)
@@ -764,7 +824,7 @@ def sevenpatch_errors(T=np.float64, P=3, E=2, roots=(2, 2), Lc=1.0, R1=3.0, k=(1
 
 
 def radiative_errors(T=np.float64, P=3, E=2, roots=(2, 2), Lc=1.0, R1=3.0, w=0.5, kappa=1.0, inverse_r=True,
-                     cfl=0.5, tend=2.0, truncate=True, precision=None, Rm=None):
+                     cfl=0.5, tend=2.0, truncate=True, precision=None, Rm=None, refined=False):
     """radiative_errors (src/sevenpatch.jl:186-237): the outgoing pulse of width
     w from the origin to tend under a radiative boundary of kappa (and u/R) on
     the outer sphere; sqrt(g)-weighted L2 errors of u and v together and apart,
@@ -773,7 +833,7 @@ def radiative_errors(T=np.float64, P=3, E=2, roots=(2, 2), Lc=1.0, R1=3.0, w=0.5
     from .element import Element
     from .problem import WaveProblem, initial_state, oldg_timestep, quadrature_norm, wave_energy, wave_integrator
     T = np.dtype(T)
-    forest, geo = ball_forest(T, P, E, roots, Lc, R1, Rm=Rm)
+    forest, geo = ball_forest(T, P, E, roots, Lc, R1, Rm=Rm, refined=refined)
     pulse = OutgoingPulse(w)
     problem = WaveProblem(forest, Element(T, P), truncate=truncate, geometry=geo,
                           boundary=RadiativeBoundary(kappa, inverse_r), precision=precision)

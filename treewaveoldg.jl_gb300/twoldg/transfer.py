@@ -93,11 +93,12 @@ def particle_frame(p):
             raise ValueError("the particles run in the ball's affine cube patch")
         n = geo.patch_roots(0)[0]
         scale = 2 * geo.Lc / n
-        origins = np.array([[-geo.Lc + scale * c[d] for d in range(3)] for _, c in forest.blocks])
-        spacings = np.full(forest.nleaves(), scale / N)
+        bs = np.array([forest.block_scale(b) for b in range(forest.nleaves())])
+        origins = np.array([[-geo.Lc + scale * s * c[d] for d in range(3)] for s, (_, c) in zip(bs, forest.blocks)])
+        spacings = scale * bs / N
         mask = np.array([1 if patch == 0 else 0 for patch, _ in forest.blocks], dtype=np.uint8)
-        levels = np.zeros(forest.nleaves(), dtype=np.int32)
-        he = scale / N * P1
+        levels = np.array(forest.levels, dtype=np.int32)
+        he = scale * bs.min() / N * P1
         dom = tuple((-geo.Lc, geo.Lc) for _ in range(3))
         return origins, spacings, mask, levels, he, dom
     if getattr(p, "geometry", None) is not None or getattr(p, "metric", None) is not None:
