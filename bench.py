@@ -289,7 +289,7 @@ def aux_kernels(twoldg, arm, hbm, reps=5):
     alg = {"export_faces_kernel": W * nb * 2 * D * F * (P + 1 + 2),
            "energy_kernel": W * nodes * 2, "norm_kernel": W * nodes * 4, "maxabs_kernel": W * nodes,
            "mode_kernel": W * (nodes + nb * E ** D), "truncate_kernel": W * nodes * 2}
-    names = ["export_faces_kernel", "cf_ghost_u/g_kernel", "energy_kernel", "norm_kernel", "maxabs_kernel",
+    names = ["export_faces_kernel", "cf_ghost_kernel", "energy_kernel", "norm_kernel", "maxabs_kernel",
              "mode_kernel", "truncate_kernel"]
     out = {}
     for k, name in enumerate(names):
@@ -319,6 +319,7 @@ def box_object(twoldg, torch, workload, roots, steps, warmup, accuracy_steps, re
                      "stage_ms": [float(x) for x in a["stage_ms"]], "clocks": a["clocks"],
                      "aux_kernels": aux_kernels(twoldg, a, hbm)}
     out["f64"]["accuracy"], out["f32c"]["accuracy"] = acc64, acc32
+    out["f64"]["layout"], out["f32c"]["layout"] = arms["f64"]["layout"], arms["f32c"]["layout"]
     out["nodes"] = arms["f32c"]["nodes"]
     out["blocks"] = len(arms["f32c"]["forest"].leaves)
     out["steps"], out["repeats"] = steps, repeats

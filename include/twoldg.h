@@ -241,7 +241,7 @@ int twoldg_set_boundary_values(twoldg_problem* p, const double* values, int32_t 
 /* Diagnostics (no reference counterpart): times, with CUDA events on the
  * problem's stream, one launch each of the kernels around the stage kernel,
  * on the state u (not changed): ms[0] the face export (export_faces_kernel),
- * ms[1] the coarse-fine ghosts (cf_ghost_u/g_kernel; 0 without coarse-fine
+ * ms[1] the coarse-fine ghosts (cf_ghost_kernel; 0 without coarse-fine
  * faces), ms[2] the energy's reduction (energy_kernel, after that export),
  * ms[3] the norm of u - u (norm_kernel, p = 2, both variables), ms[4] the
  * indicator's peak (maxabs_kernel, u), ms[5] the modal indicator up to mode

@@ -16,8 +16,8 @@
 //     (fog_nb + Wg * (the neighbour's own u ghost)) / h_nb,
 // and for a same-level or wall face that u ghost is this block's own face
 // node, so a stage needs only the previous stage's face exports and no
-// separate exchange pass. Coarse-fine faces are "dense": two small kernels
-// (cf_ghost_u, cf_ghost_g) fill their ghosts through the element-local
+// separate exchange pass. Coarse-fine faces are "dense": one small kernel
+// (cf_ghost_kernel) fills both their ghost planes through the element-local
 // prolongation I and restriction R before the stage kernel runs.
 #pragma once
 #include <cuda_runtime.h>
@@ -228,122 +228,181 @@ __global__ void export_faces_kernel(const BlockItem* items, int nitems, int E, c
 // ---------------------------------------------------------------------------
 // Coarse-fine ghosts. Tangential dims of a face normal to d are the other
 // dims in increasing order; a face's tangential index t has the first of
-// them fastest. One thread per (cf face, t).
-template <typename T, int D, int P>
-__device__ __forceinline__ T cf_apply(const CfFace& c, int t, int N, int E, int F, const T* src,
-                                      const CfTab<T, P>& ct, int64_t sstride = -1) {
-    if (sstride < 0) sstride = F;   // words per face slot of src
+// them fastest.
+// The restriction R = M_c^-1 I^T M_f at a coarse face node n (tangential
+// coordinates in the coarse face) from the fine face plane `fine` (row
+// stride N) that covers it: its coarse element's 2(P+1) fine nodes along
+// each tangential dimension.
+template <typename T, int DT, int P>
+__device__ __forceinline__ T restrict_at(const CfTab<T, P>& ct, const int* n, int N, int halfE, const T* fine) {
     constexpr int P1 = P + 1;
-    constexpr int DT = D - 1;
     if constexpr (DT == 0) {
-        return src[(int64_t)c.src[0] * sstride];
+        return fine[0];
+    } else if constexpr (DT == 1) {
+        const int ec = n[0] / P1, j = n[0] % P1, fb = 2 * (ec % halfE) * P1;
+        T acc = T(0);
+#pragma unroll
+        for (int r = 0; r < 2 * P1; ++r) acc += ct.R[j][r] * fine[fb + r];
+        return acc;
     } else {
-        int n[DT];
-        {
-            int tt = t;
-            for (int k = 0; k < DT; ++k) { n[k] = tt % N; tt /= N; }
+        const int ec0 = n[0] / P1, j0 = n[0] % P1, fb0 = 2 * (ec0 % halfE) * P1;
+        const int ec1 = n[1] / P1, j1 = n[1] % P1, fb1 = 2 * (ec1 % halfE) * P1;
+        T acc = T(0);
+#pragma unroll
+        for (int r1 = 0; r1 < 2 * P1; ++r1) {
+            T a = T(0);
+#pragma unroll
+            for (int r0 = 0; r0 < 2 * P1; ++r0) a += ct.R[j0][r0] * fine[(fb0 + r0) + N * (fb1 + r1)];
+            acc += ct.R[j1][r1] * a;
         }
-        const int halfE = E / 2;
-        if (c.kind == 0) {
-            // fine ghost from the coarse face: sum_j I[row][j] * coarse values
-            int row[DT], cb[DT];
-            for (int k = 0; k < DT; ++k) {
-                int e = n[k] / P1, i = n[k] % P1;
-                int q = (c.sub >> k) & 1;
-                row[k] = (e & 1) * P1 + i;
-                cb[k] = (q * halfE + e / 2) * P1;
-            }
-            const T* s = src + (int64_t)c.src[0] * sstride;
-            T acc = T(0);
-            if constexpr (DT == 1) {
-#pragma unroll
-                for (int j = 0; j < P1; ++j) acc += ct.I[row[0]][j] * s[cb[0] + j];
-            } else {
-#pragma unroll
-                for (int j2 = 0; j2 < P1; ++j2) {
-                    T a = T(0);
-#pragma unroll
-                    for (int j1 = 0; j1 < P1; ++j1) a += ct.I[row[0]][j1] * s[(cb[0] + j1) + N * (cb[1] + j2)];
-                    acc += ct.I[row[1]][j2] * a;
-                }
-            }
-            return acc;
-        } else {
-            // coarse ghost from the fine faces: sum_r R[j][r] * fine values
-            int j[DT], fb[DT], bits = 0;
-            for (int k = 0; k < DT; ++k) {
-                int ec = n[k] / P1;
-                j[k] = n[k] % P1;
-                int q = ec / halfE;
-                bits |= q << k;
-                fb[k] = 2 * (ec % halfE) * P1;
-            }
-            const T* s = src + (int64_t)c.src[bits] * sstride;
-            T acc = T(0);
-            if constexpr (DT == 1) {
-#pragma unroll
-                for (int r = 0; r < 2 * P1; ++r) acc += ct.R[j[0]][r] * s[fb[0] + r];
-            } else {
-#pragma unroll
-                for (int r2 = 0; r2 < 2 * P1; ++r2) {
-                    T a = T(0);
-#pragma unroll
-                    for (int r1 = 0; r1 < 2 * P1; ++r1) a += ct.R[j[0]][r1] * s[(fb[0] + r1) + N * (fb[1] + r2)];
-                    acc += ct.R[j[1]][r2] * a;
-                }
-            }
-            return acc;
-        }
+        return acc;
     }
 }
 
+// The prolongation I at a fine face node n (tangential coordinates in the
+// fine face) from the coarse face plane `coarse` (row stride N): the degree-P
+// polynomial of the coarse element over it; q's bit k says which half of the
+// coarse face the fine face covers along tangential dimension k, in units of
+// halfE coarse elements.
+template <typename T, int DT, int P>
+__device__ __forceinline__ T prolong_at(const CfTab<T, P>& ct, const int* n, int q, int N, int halfE,
+                                        const T* coarse) {
+    constexpr int P1 = P + 1;
+    if constexpr (DT == 0) {
+        return coarse[0];
+    } else if constexpr (DT == 1) {
+        const int e = n[0] / P1, row = (e & 1) * P1 + n[0] % P1, cb = ((q & 1) * halfE + e / 2) * P1;
+        T acc = T(0);
+#pragma unroll
+        for (int j = 0; j < P1; ++j) acc += ct.I[row][j] * coarse[cb + j];
+        return acc;
+    } else {
+        const int e0 = n[0] / P1, row0 = (e0 & 1) * P1 + n[0] % P1, cb0 = ((q & 1) * halfE + e0 / 2) * P1;
+        const int e1 = n[1] / P1, row1 = (e1 & 1) * P1 + n[1] % P1, cb1 = (((q >> 1) & 1) * halfE + e1 / 2) * P1;
+        T acc = T(0);
+#pragma unroll
+        for (int j1 = 0; j1 < P1; ++j1) {
+            T a = T(0);
+#pragma unroll
+            for (int j0 = 0; j0 < P1; ++j0) a += ct.I[row0][j0] * coarse[(cb0 + j0) + N * (cb1 + j1)];
+            acc += ct.I[row1][j1] * a;
+        }
+        return acc;
+    }
+}
+
+// Coarse-fine ghosts, one face per CTA, both planes in one launch. u's ghost
+// is the I or R image of the other side's face nodes. The gradient's ghost is
+// the image of the other side's face gradient, its own part plus its ghost
+// coefficient times its u ghost over its spacing, and that u ghost is in turn
+// the image of this side's face nodes, so the two images compose and no
+// exchange of the other side's gradient is needed: the other side's face
+// gradient over the part of the face that meets this one is formed first, in
+// shared memory (a quarter of a coarse face, or the four fine faces across
+// it), with the I and R tables, which the threads index by their own node.
 template <typename T, int D, int P>
-__global__ void cf_ghost_u_kernel(const CfFace* cf, int ncf, int E, const T* fu, const T* fog, T* ugd,
-                                  T* gfd, Tab<T, P> tb, CfTab<T, P> ct) {
-    int N = E * (P + 1);
-    int F = ipow(N, D - 1);
-    int64_t total = (int64_t)ncf * F;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        int c = (int)(i / F), t = (int)(i % F);
-        CfFace face = cf[c];
-        T ug = cf_apply<T, D, P>(face, t, N, E, F, fu, ct);
-        int64_t o = (int64_t)face.slot * F + t;
-        ugd[o] = ug;
-        gfd[o] = (fog[o] + ghost_coef<T, P>(tb, face.side) * ug) / T(face.h);
+__global__ void __launch_bounds__(128) cf_ghost_kernel(const CfFace* cf, int ncf, int E, const T* fu, const T* fog,
+                                                       T* ugd, T* ggd, Tab<T, P> tb, CfTab<T, P> ct) {
+    constexpr int P1 = P + 1, DT = D - 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ CfTab<T, P> sct;
+    T* G = reinterpret_cast<T*>(smem_raw);
+    const int N = E * P1, H = N / 2, halfE = E / 2;
+    const int F = ipow(N, DT);
+    {
+        const T* src = reinterpret_cast<const T*>(&ct);
+        T* dst = reinterpret_cast<T*>(&sct);
+        for (int i = threadIdx.x; i < (int)(sizeof(CfTab<T, P>) / sizeof(T)); i += blockDim.x) dst[i] = src[i];
+    }
+    for (int c = blockIdx.x; c < ncf; c += gridDim.x) {
+        const CfFace face = cf[c];
+        __syncthreads();  // the tables are in place; G is free
+        const T gco = ghost_coef<T, P>(tb, 1 - face.side);
+        const T* own = fu + (int64_t)face.slot * F;
+        if (face.kind == 0) {
+            // this block is the fine side: the coarse side's face gradient at
+            // the coarse nodes of this block's quarter, its u ghost the R image
+            // of this face's nodes
+            const T inv_hc = T(1) / T(2.0 * face.h);
+            const int nq = ipow(H, DT);
+            for (int m = threadIdx.x; m < nq; m += blockDim.x) {
+                int n[2] = {0, 0}, mm = m;
+                for (int k = 0; k < DT; ++k) { n[k] = ((face.sub >> k) & 1) * H + mm % H; mm /= H; }
+                const T ug = restrict_at<T, DT, P>(sct, n, N, halfE, own);
+                const int ci = DT == 2 ? n[0] + N * n[1] : n[0];
+                G[m] = (fog[(int64_t)face.src[0] * F + ci] + gco * ug) * inv_hc;
+            }
+        } else {
+            // the coarse side: each fine side's face gradient at its nodes, its
+            // u ghost the I image of this face's nodes
+            const T inv_hf = T(1) / T(0.5 * face.h);
+            const int nsub = 1 << DT;
+            for (int i = threadIdx.x; i < nsub * F; i += blockDim.x) {
+                const int q = i / F, tt = i % F;
+                int n[2] = {0, 0};
+                if (DT >= 1) n[0] = tt % N;
+                if (DT == 2) n[1] = tt / N;
+                const T ug = prolong_at<T, DT, P>(sct, n, q, N, halfE, own);
+                G[i] = (fog[(int64_t)face.src[q] * F + tt] + gco * ug) * inv_hf;
+            }
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < F; t += blockDim.x) {
+            int n[2] = {0, 0};
+            if (DT >= 1) n[0] = t % N;
+            if (DT == 2) n[1] = t / N;
+            T ug, gg;
+            if (face.kind == 0) {
+                ug = prolong_at<T, DT, P>(sct, n, face.sub, N, halfE, fu + (int64_t)face.src[0] * F);
+                gg = prolong_at<T, DT, P>(sct, n, 0, H, halfE, G);
+            } else {
+                int bits = 0;
+                for (int k = 0; k < DT; ++k) bits |= ((n[k] / P1) / halfE) << k;
+                ug = restrict_at<T, DT, P>(sct, n, N, halfE, fu + (int64_t)face.src[bits] * F);
+                gg = restrict_at<T, DT, P>(sct, n, N, halfE, G + (int64_t)bits * F);
+            }
+            ugd[(int64_t)face.slot * F + t] = ug;
+            ggd[(int64_t)face.slot * F + t] = gg;
+        }
     }
 }
 
 // The coarse-fine image of `vars` planes per face slot ((vars, F) per slot):
 // the full metric's u ghosts (vars 1, from the face exports) and Cartesian
 // gradient ghosts (vars 3, from the V face planes) of a refined brick patch,
-// where the map is affine and the flat problem's I and R apply to each.
+// where the map is affine and the flat problem's I and R apply to each. The
+// tables are staged in shared memory, which the threads index by their node.
 template <typename T, int D, int P>
-__global__ void cf_plane_kernel(const CfFace* cf, int ncf, int E, int vars, const T* src, T* dst, CfTab<T, P> ct) {
-    int N = E * (P + 1);
-    int F = ipow(N, D - 1);
-    int64_t total = (int64_t)ncf * vars * F;
+__global__ void __launch_bounds__(256) cf_plane_kernel(const CfFace* cf, int ncf, int E, int vars, const T* src, T* dst,
+                                                       CfTab<T, P> ct) {
+    constexpr int P1 = P + 1, DT = D - 1;
+    __shared__ CfTab<T, P> sct;
+    {
+        const T* s = reinterpret_cast<const T*>(&ct);
+        T* d = reinterpret_cast<T*>(&sct);
+        for (int i = threadIdx.x; i < (int)(sizeof(CfTab<T, P>) / sizeof(T)); i += blockDim.x) d[i] = s[i];
+    }
+    __syncthreads();
+    const int N = E * P1, halfE = E / 2;
+    const int F = ipow(N, DT);
+    const int64_t total = (int64_t)ncf * vars * F;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int t = (int)(i % F);
         const int comp = (int)((i / F) % vars);
-        const int c = (int)(i / ((int64_t)F * vars));
-        CfFace face = cf[c];
-        dst[((int64_t)face.slot * vars + comp) * F + t] =
-            cf_apply<T, D, P>(face, t, N, E, F, src + (int64_t)comp * F, ct, (int64_t)vars * F);
-    }
-}
-
-template <typename T, int D, int P>
-__global__ void cf_ghost_g_kernel(const CfFace* cf, int ncf, int E, const T* gfd, T* ggd, CfTab<T, P> ct) {
-    int N = E * (P + 1);
-    int F = ipow(N, D - 1);
-    int64_t total = (int64_t)ncf * F;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        int c = (int)(i / F), t = (int)(i % F);
-        CfFace face = cf[c];
-        ggd[(int64_t)face.slot * F + t] = cf_apply<T, D, P>(face, t, N, E, F, gfd, ct);
+        const CfFace face = cf[i / ((int64_t)F * vars)];
+        int n[2] = {0, 0};
+        if (DT >= 1) n[0] = t % N;
+        if (DT == 2) n[1] = t / N;
+        T v;
+        if (face.kind == 0) {
+            v = prolong_at<T, DT, P>(sct, n, face.sub, N, halfE, src + ((int64_t)face.src[0] * vars + comp) * F);
+        } else {
+            int bits = 0;
+            for (int k = 0; k < DT; ++k) bits |= ((n[k] / P1) / halfE) << k;
+            v = restrict_at<T, DT, P>(sct, n, N, halfE, src + ((int64_t)face.src[bits] * vars + comp) * F);
+        }
+        dst[((int64_t)face.slot * vars + comp) * F + t] = v;
     }
 }
 

@@ -250,10 +250,10 @@ public:
         if (ncf == 0) return cudaSuccess;
         int64_t F = 1;
         for (int k = 0; k < D - 1; ++k) F *= (int64_t)E * (P + 1);
-        int g = grid_for((int64_t)ncf * F, 256);
-        cf_ghost_u_kernel<T, D, P><<<g, 256, 0, s>>>(cf, ncf, E, (const T*)fu, (const T*)fog, (T*)ugd, (T*)gfd,
-                                                    tb_, ct_);
-        cf_ghost_g_kernel<T, D, P><<<g, 256, 0, s>>>(cf, ncf, E, (const T*)gfd, (T*)ggd, ct_);
+        (void)gfd;  // the composite images need no intermediate plane
+        const size_t smem = (size_t)(1 << (D - 1)) * F * sizeof(T);
+        cf_ghost_kernel<T, D, P><<<std::min(ncf, kMaxGrid), 128, smem, s>>>(cf, ncf, E, (const T*)fu, (const T*)fog,
+                                                                           (T*)ugd, (T*)ggd, tb_, ct_);
         return cudaGetLastError();
     }
 
