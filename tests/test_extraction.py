@@ -108,15 +108,21 @@ def test_brick_stencils_are_the_oracle_polynomials_and_converge():
     assert math.log2(errs[0] / errs[1]) > P + 0.5
 
 
-def test_ball_stencils_converge_across_the_patches():
-    # the seven-patch ball: spheres in the cube, across the cube-shell faces
-    # and in the shells converge at order P + 1 (test/extraction_tests.jl:95-131,
-    # without the refined cube)
+@pytest.mark.parametrize("refined", [False, True])
+def test_ball_stencils_converge_across_the_patches(refined):
+    # the seven-patch ball: spheres inside the cube's refined region, across
+    # its coarse-fine faces, across the cube-shell faces and in the shells
+    # converge at order P + 1 (test/extraction_tests.jl:95-131); refined, the
+    # cube's (s, 3s)^3 is one level finer, and a point read from the wrong
+    # level's leaf stops the error from falling
     P = 3
     table, dirs = sphere_rule(4, 10)
     errs = []
     for s in (1, 2):
-        f, geo = sevenpatch_forest(np.float64, P, 2, roots=(4 * s, 2 * s))
+        f, geo = sevenpatch_forest(np.float64, P, 2, roots=(4 * s, 2 * s),
+                                   refined=((s, 3 * s),) * 3 if refined else False)
+        if refined:
+            assert max(f.levels) == 1
         tables = ball_tables(f, P)
         u = ball_state(f, tables, fill)
         pts = np.concatenate([r * dirs for r in (0.3, 0.7, 1.3, 2.2)])

@@ -41,15 +41,16 @@ def test_brick_sphere_values_and_modes(native):
     assert np.abs(m).max() <= math.sqrt(4 * math.pi) * err
 
 
-@pytest.mark.parametrize("precision", ["f64", "f32c"])
-def test_ball_sphere_and_plane(native, precision):
+@pytest.mark.parametrize("precision,refined", [("f64", False), ("f32c", False), ("f64", True)])
+def test_ball_sphere_and_plane(native, precision, refined):
     import torch
     import twoldg
     from twoldg.ball import ball_tables
     from twoldg.extraction import PlaneExtraction, SphereExtraction, plane_values, sphere_modes, sphere_values
     P = 3
     T = np.float64 if precision == "f64" else np.float32
-    f, geo = twoldg.sevenpatch_forest(T, P, 2, roots=(4, 2))
+    # refined: the cube's (1, 3)^3 one level finer (test/extraction_tests.jl:95-200)
+    f, geo = twoldg.sevenpatch_forest(T, P, 2, roots=(4, 2), refined=((1.0, 3.0),) * 3 if refined else False)
     p = twoldg.WaveProblem(f, twoldg.Element(T, P), geometry=geo, boundary=twoldg.RadiativeBoundary(),
                            precision=precision)
     u = ball_state(f, ball_tables(f, P), fill)

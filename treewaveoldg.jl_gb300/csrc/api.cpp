@@ -76,9 +76,10 @@ struct Group {
     int64_t NN = 0, F = 1;
     std::vector<BlockItem> items;
     std::vector<CfFace> cf;
+    std::vector<int> cfidx;               // per face slot its index in cf (-1: none)
     std::vector<double> h;
     std::unique_ptr<Ops> ops;
-    DevBuf d_items, d_cf, fu[2], fog[2], ugd, gfd, ggd, d_part, d_part2;
+    DevBuf d_items, d_cf, d_cfidx, fu[2], fog[2], ugd, gfd, ggd, d_part, d_part2;
     bool metric = false;
     int full = 0;                         // 1: the full metric's two-pass stage
     std::vector<double> coef;             // per item (1 + D) N^D (or 1 + D^2: full), then the field type
@@ -339,6 +340,12 @@ struct twoldg_runner {
             CK(g.d_cf.alloc(g.cf.size() * sizeof(CfFace)));
             if (!g.cf.empty())
                 CK(cudaMemcpy(g.d_cf.p, g.cf.data(), g.cf.size() * sizeof(CfFace), cudaMemcpyHostToDevice));
+            if (!g.cf.empty() && !g.full) {
+                g.cfidx.assign(g.nslots(), -1);
+                for (size_t i = 0; i < g.cf.size(); ++i) g.cfidx[g.cf[i].slot] = (int)i;
+                CK(g.d_cfidx.alloc(g.cfidx.size() * sizeof(int)));
+                CK(cudaMemcpy(g.d_cfidx.p, g.cfidx.data(), g.cfidx.size() * sizeof(int), cudaMemcpyHostToDevice));
+            }
             for (int i = 0; i < 2; ++i) {
                 CK(g.fu[i].alloc(fbytes));
                 CK(g.fog[i].alloc(fbytes));
@@ -473,6 +480,18 @@ struct twoldg_runner {
         return p;
     }
 
+    // A stage's pointers: the stage forms its coarse-fine ghosts itself, from
+    // the face planes `in` (the other passes read the planes cf_all fills).
+    StagePtrs stage_ptrs(Group& g, void* u, int in) {
+        StagePtrs p = ptrs(g, u, in);
+        if (!g.cf.empty()) {
+            p.cf = (const CfFace*)g.d_cf.p;
+            p.cfidx = (const int*)g.d_cfidx.p;
+            p.ncf = (int)g.cf.size();
+        }
+        return p;
+    }
+
     FmPtrs fptrs(Group& g, void* u, int in) {
         FmPtrs p{};
         p.u = u;
@@ -592,10 +611,7 @@ struct twoldg_runner {
             CK(g.ops->fm_stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, fp, st));
             return TWOLDG_OK;
         }
-        if (!g.cf.empty())
-            CK(g.ops->cf_ghosts((const CfFace*)g.d_cf.p, (int)g.cf.size(), g.E, g.fu[in].p, g.fog[in].p, g.ugd.p,
-                                g.gfd.p, g.ggd.p, st));
-        StagePtrs p = ptrs(g, u, in);
+        StagePtrs p = stage_ptrs(g, u, in);
         CK(g.ops->stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, s, g.truncate, p, 0, st));
         return TWOLDG_OK;
     }
@@ -696,7 +712,7 @@ struct twoldg_runner {
             auto run3 = [&]() -> cudaError_t {
                 int in = 0;
                 for (int s = 1; s <= 3; ++s) {
-                    StagePtrs sp = ptrs(g, u, in);
+                    StagePtrs sp = stage_ptrs(g, u, in);
                     cudaError_t e = g.ops->stage((const BlockItem*)g.d_items.p, nit, g.E, s, g.truncate, sp, 0, stream);
                     if (e != cudaSuccess) return e;
                     in = 1 - in;
@@ -921,9 +937,7 @@ int twoldg_rhs(twoldg_problem* p, void* du, const void* u, double t) {
         CK(g.ops->fm_stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, 0, 0, fp, p->stream));
         return TWOLDG_OK;
     }
-    r = p->cf_all(g, 0);
-    if (r) return r;
-    StagePtrs s = p->ptrs(g, const_cast<void*>(u), 0);
+    StagePtrs s = p->stage_ptrs(g, const_cast<void*>(u), 0);
     s.du = du;
     CK(g.ops->stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, 0, 0, s, 0, p->stream));
     return TWOLDG_OK;

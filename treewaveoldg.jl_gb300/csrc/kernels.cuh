@@ -70,6 +70,11 @@ struct StageArgs {
     const T* coef;
     const T* trm;
     const T* trd;
+    // coarse-fine faces formed in the stage kernel's prologue (the 3D
+    // register-line kernel): the faces and, per face slot, the face's index
+    // among them; NULL where the planes ugd and ggd were filled before
+    const CfFace* cf;
+    const int* cfidx;
 };
 
 __host__ __device__ constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1); }
@@ -291,76 +296,103 @@ __device__ __forceinline__ T prolong_at(const CfTab<T, P>& ct, const int* n, int
     }
 }
 
-// Coarse-fine ghosts, one face per CTA, both planes in one launch. u's ghost
-// is the I or R image of the other side's face nodes. The gradient's ghost is
-// the image of the other side's face gradient, its own part plus its ghost
-// coefficient times its u ghost over its spacing, and that u ghost is in turn
-// the image of this side's face nodes, so the two images compose and no
-// exchange of the other side's gradient is needed: the other side's face
-// gradient over the part of the face that meets this one is formed first, in
-// shared memory (a quarter of a coarse face, or the four fine faces across
-// it), with the I and R tables, which the threads index by their own node.
+// Coarse-fine ghosts of one face, both planes. u's ghost is the I or R image
+// of the other side's face nodes. The gradient's ghost is the image of the
+// other side's face gradient, its own part plus its ghost coefficient times
+// its u ghost over its spacing, and that u ghost is in turn the image of this
+// side's face nodes, so the two images compose and no exchange of the other
+// side's gradient is needed. dense_fill forms the other side's face gradient
+// over the part of the face that meets this one, in the scratch G (a quarter
+// of a coarse face, H^(D-1) words, or the 2^(D-1) fine faces across it,
+// 2^(D-1) F words), with the CTA's threads tid = 0 .. nt-1; after a barrier
+// dense_point reads this face's two ghosts at its node t. The I and R tables
+// `ct` sit in shared memory, which the threads index by their own node.
+template <typename T, int DT, int P>
+__device__ __forceinline__ void dense_fill(const CfFace& face, int E, const T* fu, const T* fog, const Tab<T, P>& tb,
+                                           const CfTab<T, P>& ct, T* G, int tid, int nt) {
+    constexpr int P1 = P + 1;
+    const int N = E * P1, H = N / 2, halfE = E / 2;
+    const int F = DT == 0 ? 1 : DT == 1 ? N : N * N;
+    const T gco = ghost_coef<T, P>(tb, 1 - face.side);
+    const T* own = fu + (int64_t)face.slot * F;
+    if (face.kind == 0) {
+        // this block is the fine side: the coarse side's face gradient at the
+        // coarse nodes of this block's quarter, its u ghost the R image of
+        // this face's nodes
+        const T inv_hc = T(1) / T(2.0 * face.h);
+        const int nq = DT == 0 ? 1 : DT == 1 ? H : H * H;
+        for (int m = tid; m < nq; m += nt) {
+            int n[2] = {0, 0}, mm = m;
+            for (int k = 0; k < DT; ++k) { n[k] = ((face.sub >> k) & 1) * H + mm % H; mm /= H; }
+            const T ug = restrict_at<T, DT, P>(ct, n, N, halfE, own);
+            const int ci = DT == 2 ? n[0] + N * n[1] : n[0];
+            G[m] = (fog[(int64_t)face.src[0] * F + ci] + gco * ug) * inv_hc;
+        }
+    } else {
+        // the coarse side: each fine side's face gradient at its nodes, its u
+        // ghost the I image of this face's nodes
+        const T inv_hf = T(1) / T(0.5 * face.h);
+        const int nsub = 1 << DT;
+        for (int i = tid; i < nsub * F; i += nt) {
+            const int q = i / F, tt = i % F;
+            int n[2] = {0, 0};
+            if (DT >= 1) n[0] = tt % N;
+            if (DT == 2) n[1] = tt / N;
+            const T ug = prolong_at<T, DT, P>(ct, n, q, N, halfE, own);
+            G[i] = (fog[(int64_t)face.src[q] * F + tt] + gco * ug) * inv_hf;
+        }
+    }
+}
+
+template <typename T, int DT, int P>
+__device__ __forceinline__ void dense_point(const CfFace& face, int t, int E, const T* fu, const CfTab<T, P>& ct,
+                                            const T* G, T& ug, T& gg) {
+    constexpr int P1 = P + 1;
+    const int N = E * P1, H = N / 2, halfE = E / 2;
+    const int F = DT == 0 ? 1 : DT == 1 ? N : N * N;
+    int n[2] = {0, 0};
+    if (DT >= 1) n[0] = t % N;
+    if (DT == 2) n[1] = t / N;
+    if (face.kind == 0) {
+        ug = prolong_at<T, DT, P>(ct, n, face.sub, N, halfE, fu + (int64_t)face.src[0] * F);
+        gg = prolong_at<T, DT, P>(ct, n, 0, H, halfE, G);
+    } else {
+        int bits = 0;
+        for (int k = 0; k < DT; ++k) bits |= ((n[k] / P1) / halfE) << k;
+        ug = restrict_at<T, DT, P>(ct, n, N, halfE, fu + (int64_t)face.src[bits] * F);
+        gg = restrict_at<T, DT, P>(ct, n, N, halfE, G + (int64_t)bits * F);
+    }
+}
+
+// The I and R tables into shared memory by the CTA's threads (a barrier
+// follows before they are read).
+template <typename T, int P>
+__device__ __forceinline__ void stage_cftab(const CfTab<T, P>& ct, CfTab<T, P>* dst, int tid, int nt) {
+    const T* s = reinterpret_cast<const T*>(&ct);
+    T* d = reinterpret_cast<T*>(dst);
+    for (int i = tid; i < (int)(sizeof(CfTab<T, P>) / sizeof(T)); i += nt) d[i] = s[i];
+}
+
+// Coarse-fine ghosts in their own launch, one face per CTA, both planes (for
+// the kernels that do not form them in their prologue).
 template <typename T, int D, int P>
 __global__ void __launch_bounds__(128) cf_ghost_kernel(const CfFace* cf, int ncf, int E, const T* fu, const T* fog,
                                                        T* ugd, T* ggd, Tab<T, P> tb, CfTab<T, P> ct) {
-    constexpr int P1 = P + 1, DT = D - 1;
+    constexpr int DT = D - 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ CfTab<T, P> sct;
     T* G = reinterpret_cast<T*>(smem_raw);
-    const int N = E * P1, H = N / 2, halfE = E / 2;
+    const int N = E * (P + 1);
     const int F = ipow(N, DT);
-    {
-        const T* src = reinterpret_cast<const T*>(&ct);
-        T* dst = reinterpret_cast<T*>(&sct);
-        for (int i = threadIdx.x; i < (int)(sizeof(CfTab<T, P>) / sizeof(T)); i += blockDim.x) dst[i] = src[i];
-    }
+    stage_cftab<T, P>(ct, &sct, threadIdx.x, blockDim.x);
     for (int c = blockIdx.x; c < ncf; c += gridDim.x) {
-        const CfFace face = cf[c];
+        const CfFace& face = cf[c];
         __syncthreads();  // the tables are in place; G is free
-        const T gco = ghost_coef<T, P>(tb, 1 - face.side);
-        const T* own = fu + (int64_t)face.slot * F;
-        if (face.kind == 0) {
-            // this block is the fine side: the coarse side's face gradient at
-            // the coarse nodes of this block's quarter, its u ghost the R image
-            // of this face's nodes
-            const T inv_hc = T(1) / T(2.0 * face.h);
-            const int nq = ipow(H, DT);
-            for (int m = threadIdx.x; m < nq; m += blockDim.x) {
-                int n[2] = {0, 0}, mm = m;
-                for (int k = 0; k < DT; ++k) { n[k] = ((face.sub >> k) & 1) * H + mm % H; mm /= H; }
-                const T ug = restrict_at<T, DT, P>(sct, n, N, halfE, own);
-                const int ci = DT == 2 ? n[0] + N * n[1] : n[0];
-                G[m] = (fog[(int64_t)face.src[0] * F + ci] + gco * ug) * inv_hc;
-            }
-        } else {
-            // the coarse side: each fine side's face gradient at its nodes, its
-            // u ghost the I image of this face's nodes
-            const T inv_hf = T(1) / T(0.5 * face.h);
-            const int nsub = 1 << DT;
-            for (int i = threadIdx.x; i < nsub * F; i += blockDim.x) {
-                const int q = i / F, tt = i % F;
-                int n[2] = {0, 0};
-                if (DT >= 1) n[0] = tt % N;
-                if (DT == 2) n[1] = tt / N;
-                const T ug = prolong_at<T, DT, P>(sct, n, q, N, halfE, own);
-                G[i] = (fog[(int64_t)face.src[q] * F + tt] + gco * ug) * inv_hf;
-            }
-        }
+        dense_fill<T, DT, P>(face, E, fu, fog, tb, sct, G, threadIdx.x, blockDim.x);
         __syncthreads();
         for (int t = threadIdx.x; t < F; t += blockDim.x) {
-            int n[2] = {0, 0};
-            if (DT >= 1) n[0] = t % N;
-            if (DT == 2) n[1] = t / N;
             T ug, gg;
-            if (face.kind == 0) {
-                ug = prolong_at<T, DT, P>(sct, n, face.sub, N, halfE, fu + (int64_t)face.src[0] * F);
-                gg = prolong_at<T, DT, P>(sct, n, 0, H, halfE, G);
-            } else {
-                int bits = 0;
-                for (int k = 0; k < DT; ++k) bits |= ((n[k] / P1) / halfE) << k;
-                ug = restrict_at<T, DT, P>(sct, n, N, halfE, fu + (int64_t)face.src[bits] * F);
-                gg = restrict_at<T, DT, P>(sct, n, N, halfE, G + (int64_t)bits * F);
-            }
+            dense_point<T, DT, P>(face, t, E, fu, sct, G, ug, gg);
             ugd[(int64_t)face.slot * F + t] = ug;
             ggd[(int64_t)face.slot * F + t] = gg;
         }

@@ -1,0 +1,8 @@
+// The register-line stage with its coarse-fine prologue for D = 3, P = 2.
+#include "stage3r_cf.cuh"
+
+namespace twoldg {
+
+TWOLDG_STAGE3R_CF(2)
+
+}  // namespace twoldg

@@ -1,0 +1,8 @@
+// The register-line stage with its coarse-fine prologue for D = 3, P = 6.
+#include "stage3r_cf.cuh"
+
+namespace twoldg {
+
+TWOLDG_STAGE3R_CF(6)
+
+}  // namespace twoldg

@@ -29,6 +29,13 @@ struct StagePtrs {
     const void* coef;  // diagonal metric node values (NULL: flat)
     const void* trm;   // per-line truncation pairs (NULL: the element's)
     const void* trd;
+    // coarse-fine faces (NULL: none, or their ghost planes ugd and ggd are
+    // filled by the caller): the stage forms their ghosts itself, in the
+    // register-line kernel's prologue or by a launch of its own before the
+    // stage kernel; cfidx gives per face slot the face's index in cf (-1: none)
+    const CfFace* cf;
+    const int* cfidx;
+    int ncf;
 };
 
 // Buffers and data of the full-metric passes (fullmetric.cuh).

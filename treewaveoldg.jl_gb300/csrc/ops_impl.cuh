@@ -54,6 +54,7 @@ public:
         if constexpr (D == 3) {
             set_attrs3r<2>();
             set_attrs3r<4>();
+            stage3r_cf_attrs<T, P, COMP>(max_smem_);
             set_attrs(fm_gradient_kernel<T, P>);
             set_attrs(fm_stage_kernel<T, P, COMP>);
             set_attrs(fm_stage_kernel<T, P, COMP, 1>);
@@ -291,6 +292,8 @@ public:
         a.coef = (const T*)p.coef;
         a.trm = (const T*)p.trm;
         a.trd = (const T*)p.trd;
+        a.cf = nullptr;
+        a.cfidx = nullptr;
         size_t smem = stage_smem(E);
         if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
         if (grid <= 0) grid = std::min(nitems, grid_cap_ > 0 ? grid_cap_ : kMaxGrid);
@@ -298,6 +301,21 @@ public:
         uintptr_t al = (uintptr_t)p.u | (uintptr_t)p.y | (uintptr_t)p.acc | (uintptr_t)p.comp | (uintptr_t)p.du;
         const bool aligned = (al & 15) == 0;
         const int k = resolve(launch_.kernel, E, !p.coef, aligned);
+        if (p.cf && p.ncf > 0) {
+            // the 3D register-line kernel forms the coarse-fine ghosts in its
+            // prologue; the others read the planes a launch of their own fills
+            if constexpr (D == 3) {
+                if (k == 1 && (E == 2 || E == 4)) {
+                    a.cf = p.cf;
+                    a.cfidx = p.cfidx;
+                    if (E == 2) return stage3r_cf_launch<T, P, 2, COMP>(a, tb_, ct_, grid, mode, s);
+                    return stage3r_cf_launch<T, P, 4, COMP>(a, tb_, ct_, grid, mode, s);
+                }
+            }
+            cudaError_t e = cf_ghosts(p.cf, p.ncf, E, p.fu_in, p.fog_in, const_cast<void*>(p.ugd), nullptr,
+                                      const_cast<void*>(p.ggd), s);
+            if (e != cudaSuccess) return e;
+        }
         if constexpr (D == 3) {
             if (k == 1 && E == 2) return launch3r<2>(a, grid, mode, s);
             if (k == 1 && E == 4) return launch3r<4>(a, grid, mode, s);
@@ -329,26 +347,26 @@ public:
             const size_t m0 = S0::words * sizeof(T);
             if constexpr (COMP) {
                 if (mode == MODE_STAGE4) {
-                    stage3r_kernel<T, P, E, true, false, 4><<<grid, SC::NT, SC::words * sizeof(T), s>>>(a, tb_);
+                    stage3r_kernel<T, P, E, true, false, 4><<<grid, SC::NT, SC::words * sizeof(T), s>>>(a, tb_, ct_);
                     return cudaGetLastError();
                 }
             }
             if (mode == MODE_STAGE1) {
                 if constexpr (SL::MINB > S0::MINB)
-                    stage3r_kernel<T, P, E, false, true, 1><<<grid, SL::NT, SL::words * sizeof(T), s>>>(a, tb_);
+                    stage3r_kernel<T, P, E, false, true, 1><<<grid, SL::NT, SL::words * sizeof(T), s>>>(a, tb_, ct_);
                 else
-                    stage3r_kernel<T, P, E, false, false, 1><<<grid, S0::NT, m0, s>>>(a, tb_);
+                    stage3r_kernel<T, P, E, false, false, 1><<<grid, S0::NT, m0, s>>>(a, tb_, ct_);
             } else if (mode == 2) {
                 if constexpr (SL::MINB > S0::MINB)
-                    stage3r_kernel<T, P, E, false, true, 2><<<grid, SL::NT, SL::words * sizeof(T), s>>>(a, tb_);
+                    stage3r_kernel<T, P, E, false, true, 2><<<grid, SL::NT, SL::words * sizeof(T), s>>>(a, tb_, ct_);
                 else
-                    stage3r_kernel<T, P, E, false, false, 2><<<grid, S0::NT, m0, s>>>(a, tb_);
+                    stage3r_kernel<T, P, E, false, false, 2><<<grid, S0::NT, m0, s>>>(a, tb_, ct_);
             } else if (mode == 3) {
-                stage3r_kernel<T, P, E, false, false, 3><<<grid, S0::NT, m0, s>>>(a, tb_);
+                stage3r_kernel<T, P, E, false, false, 3><<<grid, S0::NT, m0, s>>>(a, tb_, ct_);
             } else if (mode == MODE_STAGE4) {
-                stage3r_kernel<T, P, E, false, false, 4><<<grid, S0::NT, m0, s>>>(a, tb_);
+                stage3r_kernel<T, P, E, false, false, 4><<<grid, S0::NT, m0, s>>>(a, tb_, ct_);
             } else {
-                stage3r_kernel<T, P, E, false><<<grid, S0::NT, m0, s>>>(a, tb_);
+                stage3r_kernel<T, P, E, false><<<grid, S0::NT, m0, s>>>(a, tb_, ct_);
             }
         }
         return cudaGetLastError();

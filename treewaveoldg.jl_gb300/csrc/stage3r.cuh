@@ -196,12 +196,19 @@ __device__ __forceinline__ void truncate_lines(const Tab<T, P>& tb, T* sl, T* sc
 
 // FM: the stage the instantiation runs (1-4), so that each stage's code holds
 // only its own data flow, or 0 for the mode in the arguments (the right-hand
-// side).
-template <typename T, int P, int E, bool COMP, bool LEAN = false, int FM = 0>
+// side). CFP: the kernel forms the ghosts of its coarse-fine faces itself, in
+// its prologue, from the previous stage's face exports (a.cf, a.cfidx; the
+// forests with refinement); without it they are read from the planes a.ugd
+// and a.ggd, which a uniform forest never reads.
+template <typename T, int P, int E, bool COMP, bool LEAN = false, int FM = 0, bool CFP = false>
 __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P, E, COMP, LEAN>::MINB)
-    stage3r_kernel(StageArgs<T> a, Tab<T, P> tb) {
+    stage3r_kernel(StageArgs<T> a, Tab<T, P> tb, CfTab<T, P> ct) {
     using S = Stage3R<T, P, E, COMP, LEAN>;
     constexpr int P1 = S::P1, N = S::N, F = S::F, NN = S::NN, VW = S::VW;
+    // the prologue's coarse-fine scratch (tables and the other side's face
+    // gradient) lives in the accumulator, which the z pass writes first
+    constexpr int kTabWords = (int)(sizeof(CfTab<T, P>) / sizeof(T));
+    static_assert(!CFP || S::LS >= kTabWords + 4 * F, "the accumulator holds the coarse-fine scratch");
     constexpr int SX = S::SX, SXY = S::SXY, LX = S::LX, LXY = S::LXY;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* su = reinterpret_cast<T*>(smem_raw);
@@ -255,11 +262,33 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
 #pragma unroll
         for (int f = 0; f < 6; ++f) {
             if (flags & (1u << f)) {
-                ug[f] = a.ugd[(int64_t)(slot + f) * F + tid];
-                gp[f] = a.ggd[(int64_t)(slot + f) * F + tid];
+                ug[f] = CFP ? T(0) : a.ugd[(int64_t)(slot + f) * F + tid];
+                gp[f] = CFP ? T(0) : a.ggd[(int64_t)(slot + f) * F + tid];
             } else {
                 ug[f] = a.fu_in[(int64_t)nb[f] * F + tid];
                 gp[f] = a.fog_in[(int64_t)nb[f] * F + tid];
+            }
+        }
+        if constexpr (CFP) {
+            if (flags & 0x3fu) {
+                // coarse-fine faces: both ghost planes from the previous
+                // stage's face exports, in place of a launch of their own
+                // (dense_fill, dense_point); the branch and the face loop are
+                // uniform in the CTA
+                CfTab<T, P>* sct = reinterpret_cast<CfTab<T, P>*>(sl);
+                T* G = sl + kTabWords;
+                stage_cftab<T, P>(ct, sct, tid, S::NT);
+#pragma unroll
+                for (int f = 0; f < 6; ++f) {
+                    if (flags & (1u << f)) {
+                        const CfFace& face = a.cf[a.cfidx[slot + f]];
+                        __syncthreads();
+                        dense_fill<T, 2, P>(face, E, a.fu_in, a.fog_in, tb, *sct, G, tid, S::NT);
+                        __syncthreads();
+                        dense_point<T, 2, P>(face, tid, E, a.fu_in, *sct, G, ug[f], gp[f]);
+                    }
+                }
+                __syncthreads();
             }
         }
         // ---- z: the column in registers
@@ -485,5 +514,14 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
         __syncthreads();
     }
 }
+
+// The register-line stage with its coarse-fine prologue (CFP), instantiated
+// per order in a translation unit of its own (kernels_d3_p<P>_cf.cu): its
+// shared-memory attributes, set once per device, and a launch of `mode`.
+template <typename T, int P, bool COMP>
+void stage3r_cf_attrs(int max_smem);
+template <typename T, int P, int E, bool COMP>
+cudaError_t stage3r_cf_launch(const StageArgs<T>& a, const Tab<T, P>& tb, const CfTab<T, P>& ct, int grid,
+                              int mode, cudaStream_t s);
 
 }  // namespace twoldg

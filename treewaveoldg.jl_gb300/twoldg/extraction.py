@@ -176,14 +176,22 @@ def element_stencils(forest, P, points, geometry=None, deriv=None):
                          "ball only, not on a %s" % type(geometry).__name__)
     index = np.empty((len(points), P1 ** D), dtype=np.int64)
     weights = np.empty((len(points), P1 ** D))
-    bindex = {blk: i for i, blk in enumerate(forest.blocks)} if ball else None
+    # a ball's leaves by (patch, level, corner): the refined cube's finest
+    # leaf holding a point is found from the finest level down
+    bindex = ({(p, lv, c): i for i, ((p, c), lv) in enumerate(zip(forest.blocks, forest.levels))}
+              if ball else None)
+    top = max(forest.levels) if ball else 0
     for j, x in enumerate(points):
         if ball:
             patch, xi = ball_patch_point(forest.geo, x)
             r = forest.geo.patch_roots(patch)
-            corner = tuple(min(int(math.floor(xi[d])), r[d] - 1) for d in range(3))
-            b = bindex[(patch, corner)]
-            local = [xi[d] - corner[d] for d in range(3)]
+            for lv in range(top, -1, -1):
+                s = 1 << lv
+                corner = tuple(min(int(math.floor(xi[d] * s)), r[d] * s - 1) for d in range(3))
+                b = bindex.get((patch, lv, corner))
+                if b is not None:
+                    break
+            local = [xi[d] * s - corner[d] for d in range(3)]
         else:
             b, local = _locate_brick(forest, x)
         e = [min(int(math.floor(local[d] * E)), E - 1) for d in range(D)]

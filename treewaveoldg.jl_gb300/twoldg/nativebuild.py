@@ -51,6 +51,14 @@ def up_to_date():
     return all(os.path.getmtime(d) <= t for d in _deps())
 
 
+def _cost(src):
+    import re
+    m = re.match(r"kernels_d(\d)(?:_p(\d))?", src)
+    if m:
+        return 100 * int(m.group(1)) + (int(m.group(2)) if m.group(2) else 0) * 10 + ("_cf" not in src)
+    return 50 if src.endswith(".cu") else 0
+
+
 def _compile(src, nvcc, verbose):
     path = os.path.join(CSRC, src)
     obj = os.path.join(OBJDIR, src + ".o")
@@ -78,7 +86,9 @@ def build(force=False, verbose=False):
         raise RuntimeError("nvcc not found: set CUDA_HOME")
     os.makedirs(OBJDIR, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
-    srcs = _sources()
+    # the longest compiles first (the 3D kernels, the higher orders first),
+    # so that the build's wall time is close to its longest unit's
+    srcs = sorted(_sources(), key=_cost, reverse=True)
     workers = min(len(srcs), os.cpu_count() or 4)
     with concurrent.futures.ThreadPoolExecutor(workers) as ex:
         results = list(ex.map(lambda s: _compile(s, nvcc, verbose), srcs))
