@@ -67,9 +67,11 @@ def parse():
                          "a smaller m' for profiling)")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner (untimed, before the warm-up) and run the default launch layouts")
-    ap.add_argument("--workload", default="box256", choices=["box256", "nested", "c1", "ball", "ball13", "transfer"],
+    ap.add_argument("--workload", default="box256", choices=["box256", "nested", "batched", "c1", "ball", "ball13",
+                                                             "transfer"],
                     help="box256: the 256^3 periodic box (the headline); nested: the 3D reflecting box with "
-                         "three nested refinement levels (P=3, E=2, roots=8) and a Gaussian pulse; c1: the 2D "
+                         "three nested refinement levels (P=3, E=2, roots=8) and a Gaussian pulse; batched: the "
+                         "512-problem 2D ensemble alone; c1: the 2D "
                          "periodic P=4, E=2, roots=8 box to a quarter period at CFL 0.25; ball: the seven-patch "
                          "ball, P=3, E=2, roots=(4,4), plane wave with Dirichlet sphere, to t=6; ball13: the "
                          "reference's benchmark ball, thirteen patches, roots (4,4,44), E=4, P=3, Lc=4, Rm=12, "
@@ -330,26 +332,30 @@ def box_object(twoldg, torch, workload, roots, steps, warmup, accuracy_steps, re
 def e2e(twoldg, torch, arm, steps):
     """The same metric through the public API with host buffers: every step
     copies its input state from pinned host memory to the device, takes one
-    RK4 step there and copies the result back to pinned host memory. Two
-    device buffers let the next step's upload overlap the previous step's
-    download (separate copy streams, ordered by events against the library's
-    stream); the last result read back is checked against a plain step."""
+    RK4 step there and copies the result back to pinned host memory. A ring
+    of NB device buffers lets a step's upload, the previous step's RK4 step
+    and the download before it run at once (separate copy streams, ordered by
+    events against the library's stream): with two, a buffer's upload, step
+    and download form a chain that the next use of it waits on, and with
+    three the host link (both directions at once) bounds the step; the last
+    result read back is checked against a plain step."""
+    NB = 3
     p = arm["p"]
     lib = twoldg._lib.lib()
     host_in = arm["u0"].cpu().pin_memory()
-    host_out = [torch.empty_like(host_in).pin_memory() for _ in range(2)]
-    dev = [torch.empty_like(arm["u0"]) for _ in range(2)]
+    host_out = [torch.empty_like(host_in).pin_memory() for _ in range(NB)]
+    dev = [torch.empty_like(arm["u0"]) for _ in range(NB)]
     dt = arm["dt"]
     compute = torch.cuda.ExternalStream(lib.twoldg_stream(p.handle))
     cin, cout = torch.cuda.Stream(), torch.cuda.Stream()
-    ev_in = [torch.cuda.Event() for _ in range(2)]
-    ev_done = [torch.cuda.Event() for _ in range(2)]
-    ev_out = [torch.cuda.Event() for _ in range(2)]
+    ev_in = [torch.cuda.Event() for _ in range(NB)]
+    ev_done = [torch.cuda.Event() for _ in range(NB)]
+    ev_out = [torch.cuda.Event() for _ in range(NB)]
 
     def step(k):
-        b = k % 2
+        b = k % NB
         with torch.cuda.stream(cin):
-            if k >= 2:
+            if k >= NB:
                 cin.wait_event(ev_out[b])        # that buffer's last download is done
             dev[b].copy_(host_in, non_blocking=True)
             ev_in[b].record(cin)
@@ -361,7 +367,7 @@ def e2e(twoldg, torch, arm, steps):
             host_out[b].copy_(dev[b], non_blocking=True)
             ev_out[b].record(cout)
 
-    for k in range(2):                           # capture both buffers' step graphs
+    for k in range(NB):                          # capture every buffer's step graph
         step(k)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -372,14 +378,14 @@ def e2e(twoldg, torch, arm, steps):
     check = arm["u0"].clone()
     twoldg._lib.check(lib.twoldg_rk4_step(p.handle, ctypes.c_void_p(check.data_ptr()), 0.0, dt, 1))
     p.synchronize()
-    if not torch.equal(check.cpu(), host_out[(steps - 1) % 2]):
+    if not torch.equal(check.cpu(), host_out[(steps - 1) % NB]):
         raise RuntimeError("the pipelined end-to-end step differs from a plain step")
     nbytes = dev[0].numel() * dev[0].element_size()
     return dict(value=arm["nodes"] * steps / sec * world(), unit="node-steps/s",
-                h2d_bytes_per_step=nbytes, d2h_bytes_per_step=nbytes, pipelined="double-buffered")
+                h2d_bytes_per_step=nbytes, d2h_bytes_per_step=nbytes, pipelined="%d device buffers" % NB)
 
 
-def batched(twoldg, torch, steps, warmup, accuracy_steps, n=512):
+def batched(twoldg, torch, steps, warmup, accuracy_steps, n=512, repeats=5):
     """The batched ensemble: n 2D periodic problems of uneven P, E and roots
     (seeded), all stepped by one graph launch per RK4 step; FP64 and FP32 +
     compensated node-steps/s, and the L2 difference of the two after
@@ -395,16 +401,29 @@ def batched(twoldg, torch, steps, warmup, accuracy_steps, n=512):
         u = u0.clone()
         if TUNE:
             out.setdefault("layout", {}).update(b.autotune(u, dts))
+        # warm-up, then one untimed call of the timed region's length, which
+        # captures its step graphs (a batch takes up to 16 steps a graph)
         b.rk4_step(u, dts, warmup)
-        b.synchronize()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
         b.rk4_step(u, dts, steps)
         b.synchronize()
-        sec = time.perf_counter() - t0
+        stream = b.stream()
+        arr = (ctypes.c_double * len(dts))(*[float(x) for x in dts])
+        regions = []
+        for _ in range(repeats):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            twoldg._lib.check(twoldg._lib.lib().twoldg_batch_rk4_step(b._h, ctypes.c_void_p(u.data_ptr()), arr,
+                                                                      steps))
+            e1.record(stream)
+            e1.synchronize()
+            regions.append(e0.elapsed_time(e1))
+        sec = float(np.median(regions)) / 1e3
         ach = BYTES_NS[prec] * b.nodes * steps / sec / 1e9
         out[prec] = {"value": b.nodes * steps / sec, "ms_per_step": sec * 1e3 / steps,
-                     "achieved_gbs": ach}
+                     "achieved_gbs": ach, "region_ms": regions,
+                     "timing": "median of %d timed regions of %d RK4 steps (CUDA events on the batch's stream)"
+                               % (repeats, steps)}
         if accuracy_steps:
             v = u0.clone()
             b.rk4_step(v, dts, accuracy_steps)
@@ -901,6 +920,23 @@ def main():
                 "transfer": tr, "roofline": tr["values_roofline"], "gpu_launches": 3 * args.steps}
         if "cpu_baseline" in tr:
             line["cpu_baseline"] = tr["cpu_baseline"]
+        print(json.dumps(line))
+        return
+    if WORKLOAD == "batched":
+        hbm, _ = peaks()
+        bat = batched(twoldg, torch, args.steps, args.warmup, args.accuracy_steps)
+        head = bat["f32c"]
+        line = {"metric": METRIC, "value": head["value"], "unit": "node-steps/s", "n_gpus": 1, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "the batched ensemble: %d 2D periodic problems, P 2-5, E 2/4, roots 4-16 "
+                                       "(seeded), %d nodes in %d shapes, FP32 fields + compensated RK4"
+                                       % (bat["members"], bat["nodes"], bat["shapes"]), "precision": "f32c",
+                           "l2_flush": "inputs larger than L2 (state %.0f MB + stage scratch)" % (bat["nodes"] * 8 / 1e6)},
+                "batched": bat,
+                "roofline": {"bound": "hbm", "achieved": head["achieved_gbs"], "peak": hbm, "unit": "GB/s",
+                             "frac": head["achieved_gbs"] / hbm},
+                "gpu_launches": None}
         print(json.dumps(line))
         return
     if WORKLOAD == "nested":

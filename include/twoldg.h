@@ -435,6 +435,9 @@ int twoldg_batch_rk4_step(twoldg_batch* b, void* u, const double* dt, int32_t ns
 int twoldg_batch_autotune(twoldg_batch* b, void* u, const double* dt, const char* cache, char* report,
                           size_t report_len);
 int twoldg_batch_synchronize(twoldg_batch* b);
+/* The batch's CUDA stream (a cudaStream_t), as twoldg_stream gives a
+ * problem's. */
+void* twoldg_batch_stream(twoldg_batch* b);
 
 #ifdef __cplusplus
 }

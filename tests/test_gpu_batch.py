@@ -13,6 +13,7 @@ from oracle.oracle import Oracle
 from twoldg.forest import wave_forest
 
 pytestmark = pytest.mark.gpu
+NSTEPS = 19
 
 
 def ensemble(n, seed, dtype=np.float64):
@@ -68,18 +69,20 @@ def test_batch_equals_members_alone(native, prec):
             big[offs[k]:offs[k] + u.numel()] = u
         torch.cuda.synchronize()
         dtarr = (ctypes.c_double * len(dts))(*dts)
-        _lib.check(_lib.lib().twoldg_batch_rk4_step(h, ctypes.c_void_p(big.data_ptr()), dtarr, 7))
+        # 19 steps: one launch of the batch's 16-step graph, whose groups run
+        # their chains through the 16 steps unjoined, and one of a 3-step one
+        _lib.check(_lib.lib().twoldg_batch_rk4_step(h, ctypes.c_void_p(big.data_ptr()), dtarr, NSTEPS))
         _lib.check(_lib.lib().twoldg_batch_synchronize(h))
         for k, (p, u0) in enumerate(zip(probs, states)):
-            integ = twoldg.wave_integrator(p, u0, 0.0, 7 * dts[k], dts[k])
-            integ.nsteps = 7
+            integ = twoldg.wave_integrator(p, u0, 0.0, NSTEPS * dts[k], dts[k])
+            integ.nsteps = NSTEPS
             integ.solve()
             got = big[offs[k]:offs[k] + u0.numel()].cpu().numpy()
             assert np.array_equal(got, integ.u.cpu().numpy()), k
             if prec == "f64" and k < 4:
                 forest, P, f = members[k]
                 o = Oracle(forest, P)
-                ref = o.rk4(u0.cpu().numpy(), dts[k], 7)
+                ref = o.rk4(u0.cpu().numpy(), dts[k], NSTEPS)
                 assert np.abs(got - ref).max() < 1e-12 * np.abs(ref).max()
     finally:
         _lib.lib().twoldg_batch_destroy(h)

@@ -137,10 +137,21 @@ struct twoldg_runner {
     std::vector<double> h_dts;                 // the dt each problem's coefficients were made for
     std::vector<unsigned char> h_rk;           // per problem dt/6, dt/3, dt/2, dt in the field type
     // the captured step graphs, keyed by the state pointer they were captured
-    // for (a caller that alternates a few state buffers keeps them all),
-    // most recently used first
-    static constexpr int kGraphs = 4;
-    std::vector<std::pair<void*, cudaGraphExec_t>> graphs;
+    // for (a caller that alternates a few state buffers keeps them all) and
+    // the steps one launch takes, most recently used first
+    static constexpr int kGraphs = 6;
+    struct StepGraph {
+        void* u;
+        int steps;
+        cudaGraphExec_t exec;
+    };
+    std::vector<StepGraph> graphs;
+    // A batch of several shape groups takes up to kChunk steps a graph
+    // launch (a call's remainder in a graph of its own): each group's chain of
+    // stages runs through them without waiting for the other groups at every
+    // step, so that a group that finishes a step early starts its next one
+    // instead of idling until the slowest group is done.
+    static constexpr int kChunk = 16;
     void* comp_u = nullptr;
     // Shape groups of a batch never exchange data, so each group's four
     // stages are one independent branch of the step's graph: side[i] carries
@@ -625,16 +636,21 @@ struct twoldg_runner {
         return TWOLDG_OK;
     }
 
-    // One RK4 step, enqueued on `stream` (captured into the graph): group 0
-    // on `stream`, every other group on its side stream between a fork and
-    // a join, so that the graph runs the groups' chains side by side.
-    int enqueue_step(void* u) {
+    // `steps` RK4 steps, enqueued on `stream` (captured into the graph):
+    // group 0 on `stream`, every other group on its side stream between a
+    // fork and a join, so that the graph runs the groups' chains side by
+    // side; groups never exchange data, so each chain takes all its steps
+    // before the join. The full metric's time advance follows the join, so
+    // its problems take one step a graph.
+    int enqueue_step(void* u, int steps = 1) {
         if (groups.size() > 1) CK(cudaEventRecord(fork, stream));
         for (size_t i = 0; i < groups.size(); ++i) {
             cudaStream_t st = i == 0 ? stream : side[i - 1];
             if (i > 0) CK(cudaStreamWaitEvent(st, fork, 0));
-            int r = enqueue_group(*groups[i], u, st);
-            if (r) return r;
+            for (int k = 0; k < steps; ++k) {
+                int r = enqueue_group(*groups[i], u, st);
+                if (r) return r;
+            }
             if (i > 0) CK(cudaEventRecord(join[i - 1], st));
         }
         for (size_t i = 1; i < groups.size(); ++i) CK(cudaStreamWaitEvent(stream, join[i - 1], 0));
@@ -648,7 +664,7 @@ struct twoldg_runner {
     void fm_advance_time(cudaStream_t s);
 
     void drop_graphs() {
-        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
         graphs.clear();
     }
 
@@ -792,31 +808,44 @@ struct twoldg_runner {
         if (nsteps == 0) return TWOLDG_OK;
         int r = export_all(u);
         if (r) return r;
+        const int chunk = (groups.size() > 1 && !any_full()) ? std::min(nsteps, kChunk) : 1;
         cudaGraphExec_t gexec = nullptr;
-        for (size_t i = 0; i < graphs.size(); ++i)
-            if (graphs[i].first == u) {
-                gexec = graphs[i].second;
-                std::rotate(graphs.begin(), graphs.begin() + i, graphs.begin() + i + 1);
-                break;
-            }
-        if (!gexec) {
-            cudaGraph_t graph;
-            CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-            r = enqueue_step(u);
-            cudaError_t e = cudaStreamEndCapture(stream, &graph);
-            if (r) { if (e == cudaSuccess) cudaGraphDestroy(graph); return r; }
-            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-            e = cudaGraphInstantiate(&gexec, graph, 0);
-            cudaGraphDestroy(graph);
-            if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
-            if ((int)graphs.size() == kGraphs) {
-                cudaGraphExecDestroy(graphs.back().second);
-                graphs.pop_back();
-            }
-            graphs.insert(graphs.begin(), {u, gexec});
+        r = step_graph(u, chunk, &gexec);
+        if (r) return r;
+        for (int i = 0; i + chunk <= nsteps; i += chunk) CK(cudaGraphLaunch(gexec, stream));
+        if (nsteps % chunk) {
+            r = step_graph(u, nsteps % chunk, &gexec);
+            if (r) return r;
+            CK(cudaGraphLaunch(gexec, stream));
         }
-        for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(gexec, stream));
         CK(cudaGetLastError());
+        return TWOLDG_OK;
+    }
+
+    // The graph of `steps` steps on state u, captured at its first use.
+    int step_graph(void* u, int steps, cudaGraphExec_t* out) {
+        for (size_t i = 0; i < graphs.size(); ++i)
+            if (graphs[i].u == u && graphs[i].steps == steps) {
+                *out = graphs[i].exec;
+                std::rotate(graphs.begin(), graphs.begin() + i, graphs.begin() + i + 1);
+                return TWOLDG_OK;
+            }
+        cudaGraph_t graph;
+        cudaGraphExec_t gexec = nullptr;
+        CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        int r = enqueue_step(u, steps);
+        cudaError_t e = cudaStreamEndCapture(stream, &graph);
+        if (r) { if (e == cudaSuccess) cudaGraphDestroy(graph); return r; }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+        if ((int)graphs.size() == kGraphs) {
+            cudaGraphExecDestroy(graphs.back().exec);
+            graphs.pop_back();
+        }
+        graphs.insert(graphs.begin(), StepGraph{u, steps, gexec});
+        *out = gexec;
         return TWOLDG_OK;
     }
 };
@@ -1340,6 +1369,8 @@ int twoldg_batch_autotune(twoldg_batch* b, void* u, const double* dt, const char
     if (r) return r;
     return tune_report(rep, report, report_len);
 }
+
+void* twoldg_batch_stream(twoldg_batch* b) { return b ? (void*)b->stream : nullptr; }
 
 int twoldg_batch_synchronize(twoldg_batch* b) {
     if (!b) return fail(TWOLDG_EINVAL, "NULL batch");

@@ -307,26 +307,30 @@ __device__ __forceinline__ T prolong_at(const CfTab<T, P>& ct, const int* n, int
 // 2^(D-1) F words), with the CTA's threads tid = 0 .. nt-1; after a barrier
 // dense_point reads this face's two ghosts at its node t. The I and R tables
 // `ct` sit in shared memory, which the threads index by their own node.
-template <typename T, int DT, int P>
-__device__ __forceinline__ void dense_fill(const CfFace& face, int E, const T* fu, const T* fog, const Tab<T, P>& tb,
-                                           const CfTab<T, P>& ct, T* G, int tid, int nt) {
+// The planes are read through accessors, so that they may sit in global
+// memory (the face exports) or staged in shared memory: own() is this face's
+// u plane, fog(q) and u(q) the other side's q-th face gradient part and u
+// plane (q = 0 on a fine side, the fine faces by child bits on a coarse one).
+template <typename T, int DT, int P, class Own, class Fog>
+__device__ __forceinline__ void dense_fill_at(const CfFace& face, int E, Own own, Fog fog, const Tab<T, P>& tb,
+                                              const CfTab<T, P>& ct, T* G, int tid, int nt) {
     constexpr int P1 = P + 1;
     const int N = E * P1, H = N / 2, halfE = E / 2;
     const int F = DT == 0 ? 1 : DT == 1 ? N : N * N;
     const T gco = ghost_coef<T, P>(tb, 1 - face.side);
-    const T* own = fu + (int64_t)face.slot * F;
     if (face.kind == 0) {
         // this block is the fine side: the coarse side's face gradient at the
         // coarse nodes of this block's quarter, its u ghost the R image of
         // this face's nodes
         const T inv_hc = T(1) / T(2.0 * face.h);
         const int nq = DT == 0 ? 1 : DT == 1 ? H : H * H;
+        const T* fc = fog(0);
         for (int m = tid; m < nq; m += nt) {
             int n[2] = {0, 0}, mm = m;
             for (int k = 0; k < DT; ++k) { n[k] = ((face.sub >> k) & 1) * H + mm % H; mm /= H; }
-            const T ug = restrict_at<T, DT, P>(ct, n, N, halfE, own);
+            const T ug = restrict_at<T, DT, P>(ct, n, N, halfE, own());
             const int ci = DT == 2 ? n[0] + N * n[1] : n[0];
-            G[m] = (fog[(int64_t)face.src[0] * F + ci] + gco * ug) * inv_hc;
+            G[m] = (fc[ci] + gco * ug) * inv_hc;
         }
     } else {
         // the coarse side: each fine side's face gradient at its nodes, its u
@@ -338,15 +342,15 @@ __device__ __forceinline__ void dense_fill(const CfFace& face, int E, const T* f
             int n[2] = {0, 0};
             if (DT >= 1) n[0] = tt % N;
             if (DT == 2) n[1] = tt / N;
-            const T ug = prolong_at<T, DT, P>(ct, n, q, N, halfE, own);
-            G[i] = (fog[(int64_t)face.src[q] * F + tt] + gco * ug) * inv_hf;
+            const T ug = prolong_at<T, DT, P>(ct, n, q, N, halfE, own());
+            G[i] = (fog(q)[tt] + gco * ug) * inv_hf;
         }
     }
 }
 
-template <typename T, int DT, int P>
-__device__ __forceinline__ void dense_point(const CfFace& face, int t, int E, const T* fu, const CfTab<T, P>& ct,
-                                            const T* G, T& ug, T& gg) {
+template <typename T, int DT, int P, class U>
+__device__ __forceinline__ void dense_point_at(const CfFace& face, int t, int E, U u, const CfTab<T, P>& ct,
+                                               const T* G, T& ug, T& gg) {
     constexpr int P1 = P + 1;
     const int N = E * P1, H = N / 2, halfE = E / 2;
     const int F = DT == 0 ? 1 : DT == 1 ? N : N * N;
@@ -354,14 +358,55 @@ __device__ __forceinline__ void dense_point(const CfFace& face, int t, int E, co
     if (DT >= 1) n[0] = t % N;
     if (DT == 2) n[1] = t / N;
     if (face.kind == 0) {
-        ug = prolong_at<T, DT, P>(ct, n, face.sub, N, halfE, fu + (int64_t)face.src[0] * F);
+        ug = prolong_at<T, DT, P>(ct, n, face.sub, N, halfE, u(0));
         gg = prolong_at<T, DT, P>(ct, n, 0, H, halfE, G);
     } else {
         int bits = 0;
         for (int k = 0; k < DT; ++k) bits |= ((n[k] / P1) / halfE) << k;
-        ug = restrict_at<T, DT, P>(ct, n, N, halfE, fu + (int64_t)face.src[bits] * F);
+        ug = restrict_at<T, DT, P>(ct, n, N, halfE, u(bits));
         gg = restrict_at<T, DT, P>(ct, n, N, halfE, G + (int64_t)bits * F);
     }
+}
+
+// The two with the planes read from the face exports in global memory.
+template <typename T, int DT, int P>
+__device__ __forceinline__ void dense_fill(const CfFace& face, int E, const T* fu, const T* fog, const Tab<T, P>& tb,
+                                           const CfTab<T, P>& ct, T* G, int tid, int nt) {
+    const int N = E * (P + 1);
+    const int F = DT == 0 ? 1 : DT == 1 ? N : N * N;
+    dense_fill_at<T, DT, P>(
+        face, E, [&]() { return fu + (int64_t)face.slot * F; },
+        [&](int q) { return fog + (int64_t)face.src[q] * F; }, tb, ct, G, tid, nt);
+}
+
+template <typename T, int DT, int P>
+__device__ __forceinline__ void dense_point(const CfFace& face, int t, int E, const T* fu, const CfTab<T, P>& ct,
+                                            const T* G, T& ug, T& gg) {
+    const int N = E * (P + 1);
+    const int F = DT == 0 ? 1 : DT == 1 ? N : N * N;
+    dense_point_at<T, DT, P>(face, t, E, [&](int q) { return fu + (int64_t)face.src[q] * F; }, ct, G, ug, gg);
+}
+
+// A face's planes staged in shared memory for dense_fill_at and
+// dense_point_at, in one region of staged_words(kind, F) words: on a coarse
+// side the four fine u planes, the four fine face gradient planes (which G
+// then overwrites in place) and its own u plane; on a fine side the coarse u
+// plane, the coarse face gradient plane, its own u plane and G's quarter.
+__host__ __device__ constexpr int staged_words(int kind, int F) { return kind ? 9 * F : 3 * F + (F + 3) / 4; }
+
+template <typename T, int DT, int P>
+__device__ __forceinline__ void stage_face_planes(const CfFace& face, int E, const T* fu, const T* fog, T* W, int tid,
+                                                  int nt) {
+    const int N = E * (P + 1);
+    const int F = DT == 0 ? 1 : DT == 1 ? N : N * N;
+    const int ns = face.kind ? 1 << DT : 1;
+    for (int i = tid; i < ns * F; i += nt) {
+        const int q = i / F, tt = i % F;
+        const int64_t o = (int64_t)face.src[q] * F + tt;
+        W[i] = fu[o];
+        W[ns * F + i] = fog[o];
+    }
+    for (int i = tid; i < F; i += nt) W[2 * ns * F + i] = fu[(int64_t)face.slot * F + i];
 }
 
 // The I and R tables into shared memory by the CTA's threads (a barrier

@@ -22,14 +22,90 @@ struct Stage2R {
     static constexpr int NN = N * N;
     static constexpr int K = 128 / N > 0 ? 128 / N : 1;   // blocks per CTA
     static constexpr int NT = K * N;
-    // u rows with the two x ghosts, and the accumulator / new v rows: odd
-    // pitches (N is even), so the rows a warp walks fall in distinct banks
-    static constexpr int SX = N + 3, LX = N + 1;
+    // u rows with the two x ghosts, and the accumulator / new v rows, each
+    // thread's row read and written as whole 16-byte words: NU and NL words
+    // a row, at pitches of an odd number of 16-byte words, so that the rows
+    // a quarter-warp walks fall in distinct banks
+    static constexpr int VW = 16 / sizeof(T);
+    static constexpr int NU = (N + 2 + VW - 1) / VW, NL = (N + VW - 1) / VW;
+    static constexpr int SX = vec_pitch<T>(N + 3), LX = vec_pitch<T>(N);
+    static_assert(SX >= NU * VW && LX >= NL * VW, "a row's last 16-byte word stays in its pitch");
     static constexpr int SS = SX * N, LS = LX * N;
     static constexpr int PER = SS + LS + (COMP ? LS : 0);   // words of one block
     static constexpr size_t words = (size_t)K * PER;
     static constexpr bool usable = N <= 32;
 };
+
+// A thread's row of NV 16-byte words at p (16-byte aligned) to and from
+// registers.
+template <typename T, int NV>
+__device__ __forceinline__ void row_load(const T* p, T (&r)[NV * (16 / sizeof(T))]) {
+    using V = typename V16<T>::type;
+    constexpr int VW = 16 / sizeof(T);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const V t = reinterpret_cast<const V*>(p)[k];
+        const T* e = reinterpret_cast<const T*>(&t);
+#pragma unroll
+        for (int q = 0; q < VW; ++q) r[k * VW + q] = e[q];
+    }
+}
+
+template <typename T, int NV>
+__device__ __forceinline__ void row_store(T* p, const T (&r)[NV * (16 / sizeof(T))]) {
+    using V = typename V16<T>::type;
+    constexpr int VW = 16 / sizeof(T);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        V t;
+        T* e = reinterpret_cast<T*>(&t);
+#pragma unroll
+        for (int q = 0; q < VW; ++q) e[q] = r[k * VW + q];
+        reinterpret_cast<V*>(p)[k] = t;
+    }
+}
+
+// The truncation of the E element lines of a thread's contiguous row (the
+// accumulator row sl and, in stage 4, the compensation row sc), each read
+// and written as whole 16-byte words; the arithmetic of truncate_lines.
+template <typename T, int P, int E, int NV>
+__device__ __forceinline__ void truncate_row(const Tab<T, P>& tb, T* sl, T* sc, bool final_comp) {
+    constexpr int P1 = P + 1, VW = 16 / sizeof(T);
+    T v[NV * VW];
+    row_load<T, NV>(sl, v);
+    if (final_comp) {
+        T w[NV * VW];
+        row_load<T, NV>(sc, w);
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            T c = T(0);
+#pragma unroll
+            for (int q = 0; q < P1; ++q) c += tb.td[q] * v[e * P1 + q];
+            T cc = T(0);
+#pragma unroll
+            for (int q = 0; q < P1; ++q) cc += tb.td[q] * w[e * P1 + q];
+            c += cc;
+#pragma unroll
+            for (int q = 0; q < P1; ++q) {
+                T s, err;
+                two_sum(v[e * P1 + q], -(tb.tm[q] * c), s, err);
+                v[e * P1 + q] = s;
+                w[e * P1 + q] += err;
+            }
+        }
+        row_store<T, NV>(sc, w);
+    } else {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            T c = T(0);
+#pragma unroll
+            for (int q = 0; q < P1; ++q) c += tb.td[q] * v[e * P1 + q];
+#pragma unroll
+            for (int q = 0; q < P1; ++q) v[e * P1 + q] = v[e * P1 + q] - tb.tm[q] * c;
+        }
+    }
+    row_store<T, NV>(sl, v);
+}
 
 // FM: the stage the instantiation runs (1-4), so that each stage's code holds
 // only its own data flow, or 0 for the mode in the arguments.
@@ -37,7 +113,8 @@ template <typename T, int P, int E, bool COMP, int FM = 0>
 __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
     stage2r_kernel(StageArgs<T> a, Tab<T, P> tb) {
     using S = Stage2R<T, P, E, COMP>;
-    constexpr int P1 = S::P1, N = S::N, NN = S::NN, SX = S::SX, LX = S::LX, K = S::K;
+    constexpr int P1 = S::P1, N = S::N, NN = S::NN, SX = S::SX, LX = S::LX, K = S::K, VW = S::VW;
+    constexpr int NU = S::NU, NL = S::NL;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int bs = threadIdx.x / N, c = threadIdx.x % N;   // block slot of the CTA, column
     T* su = reinterpret_cast<T*>(smem_raw) + bs * S::PER;
@@ -62,6 +139,9 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
         int slot = 0, nb[4] = {0, 0, 0, 0};
         T ug[4], gp[4];
         if (live) {
+            // the block's stage operands (and the next block this slot takes)
+            // into L2 while the CTA computes
+            if (c == 0) prefetch_stage3r<T>(a, item, NN, (int)gridDim.x * K);
             flags = it->flags;
             slot = it->slot;
 #pragma unroll
@@ -109,17 +189,21 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
         __syncthreads();
         // ---- x: row c from the shared copy of u
         if (live) {
-            T line[N + 2], g[N + 2], gi[N], lap[N];
+            T row[NU * VW], line[N + 2], g[N + 2], gi[N], lap[N];
+            row_load<T, NU>(su + c * SX, row);
 #pragma unroll
-            for (int k = 0; k < N + 2; ++k) line[k] = su[c * SX + k];
+            for (int k = 0; k < N + 2; ++k) line[k] = row[k];
             line_full<T, P, E>(tb, line, gi, inv_h);
 #pragma unroll
             for (int j = 0; j < N; ++j) g[1 + j] = gi[j];
             g[0] = grad_ghost<T, P>(tb, flags, nb[0], 0, gp[0], line[1], inv_h);
             g[N + 1] = grad_ghost<T, P>(tb, flags, nb[1], 1, gp[1], line[N], inv_h);
             line_full<T, P, E>(tb, g, lap, T(1));
+            T acc_row[NL * VW];
+            row_load<T, NL>(sl + c * LX, acc_row);
 #pragma unroll
-            for (int i = 0; i < N; ++i) sl[c * LX + i] += lap[i];
+            for (int i = 0; i < N; ++i) acc_row[i] += lap[i];
+            row_store<T, NL>(sl + c * LX, acc_row);
         }
         __syncthreads();
         if (mode == MODE_RHS) {
@@ -245,16 +329,18 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
         __syncthreads();
         // ---- the x faces of the new u (row c), and the truncation along x
         if (live) {
+            T row[NU * VW];
+            row_load<T, NU>(su + c * SX, row);
 #pragma unroll
             for (int side = 0; side < 2; ++side) {
                 T e[P1];
 #pragma unroll
-                for (int k = 0; k < P1; ++k) e[k] = su[c * SX + 1 + (side ? N - P1 : 0) + k];
+                for (int k = 0; k < P1; ++k) e[k] = row[1 + (side ? N - P1 : 0) + k];
                 const int64_t o = (int64_t)(slot + side) * N + c;
                 a.fu_out[o] = side == 0 ? e[0] : e[P];
                 a.fog_out[o] = own_face_part<T, P>(tb, side, e);
             }
-            if (a.truncate) truncate_lines<T, P, E, false>(tb, sl, sc, c * LX, 1, final_comp);
+            if (a.truncate) truncate_row<T, P, E, NL>(tb, sl + c * LX, sc + c * LX, final_comp);
         }
         __syncthreads();
         // ---- the new v of the column (and in stage 4 its u)

@@ -49,7 +49,7 @@ constexpr int half_bank_stride(int lo) {
 // stages 1 and 2, k1_v in stage 2, the stage input, u^n and the increments in
 // stages 3 and 4, the compensation in stage 4.
 template <typename T>
-__device__ __forceinline__ void prefetch_stage3r(const StageArgs<T>& a, int item, int64_t NN) {
+__device__ __forceinline__ void prefetch_stage3r(const StageArgs<T>& a, int item, int64_t NN, int stride = 0) {
     const int mode = a.mode;
     const int64_t off = a.items[item].off;
     const size_t w = (size_t)NN * sizeof(T);
@@ -60,7 +60,7 @@ __device__ __forceinline__ void prefetch_stage3r(const StageArgs<T>& a, int item
         prefetch_l2(a.acc + off, 2 * w);
         if (mode == MODE_STAGE4 && a.comp) prefetch_l2(a.comp + off, 2 * w);
     }
-    const int nxt = item + gridDim.x;
+    const int nxt = item + (stride ? stride : (int)gridDim.x);
     if (nxt < a.nitems) {
         const T* src = (mode == 3 || mode == MODE_STAGE4) ? a.y : a.u;
         prefetch_l2(src + a.items[nxt].off, 2 * w);
@@ -205,10 +205,12 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
     stage3r_kernel(StageArgs<T> a, Tab<T, P> tb, CfTab<T, P> ct) {
     using S = Stage3R<T, P, E, COMP, LEAN>;
     constexpr int P1 = S::P1, N = S::N, F = S::F, NN = S::NN, VW = S::VW;
-    // the prologue's coarse-fine scratch (tables and the other side's face
-    // gradient) lives in the accumulator, which the z pass writes first
+    // the prologue's coarse-fine scratch (the tables and the other side's
+    // face gradient of each of up to six faces, 4 F words at most a face)
+    // lives in the shared copy of u and the accumulator, which the z pass
+    // writes first
     constexpr int kTabWords = (int)(sizeof(CfTab<T, P>) / sizeof(T));
-    static_assert(!CFP || S::LS >= kTabWords + 4 * F, "the accumulator holds the coarse-fine scratch");
+    static_assert(!CFP || S::SS + S::LS >= kTabWords + 24 * F, "u and the accumulator hold the coarse-fine scratch");
     constexpr int SX = S::SX, SXY = S::SXY, LX = S::LX, LXY = S::LXY;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* su = reinterpret_cast<T*>(smem_raw);
@@ -272,20 +274,79 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
         if constexpr (CFP) {
             if (flags & 0x3fu) {
                 // coarse-fine faces: both ghost planes from the previous
-                // stage's face exports, in place of a launch of their own
-                // (dense_fill, dense_point); the branch and the face loop are
-                // uniform in the CTA
-                CfTab<T, P>* sct = reinterpret_cast<CfTab<T, P>*>(sl);
-                T* G = sl + kTabWords;
-                stage_cftab<T, P>(ct, sct, tid, S::NT);
+                // stage's face exports, in place of a launch of their own.
+                // Every face at once, so that their loads are in flight
+                // together; the branches and the face loops are uniform in
+                // the CTA. Where the faces' planes fit in the shared copy of u
+                // and the accumulator (which the z pass writes first), they
+                // are staged there with coalesced loads and the images read
+                // them from shared memory; otherwise the images read them
+                // from global memory. Three barriers after the tables.
+                CfTab<T, P>* sct = reinterpret_cast<CfTab<T, P>*>(su);
+                T* W = su + kTabWords;
+                int need = 0;
 #pragma unroll
-                for (int f = 0; f < 6; ++f) {
-                    if (flags & (1u << f)) {
-                        const CfFace& face = a.cf[a.cfidx[slot + f]];
-                        __syncthreads();
-                        dense_fill<T, 2, P>(face, E, a.fu_in, a.fog_in, tb, *sct, G, tid, S::NT);
-                        __syncthreads();
-                        dense_point<T, 2, P>(face, tid, E, a.fu_in, *sct, G, ug[f], gp[f]);
+                for (int f = 0; f < 6; ++f)
+                    if (flags & (1u << f)) need += staged_words(a.cf[a.cfidx[slot + f]].kind, F);
+                stage_cftab<T, P>(ct, sct, tid, S::NT);
+                if (need <= S::SS + S::LS - kTabWords) {
+                    int off = 0;
+#pragma unroll
+                    for (int f = 0; f < 6; ++f) {
+                        if (flags & (1u << f)) {
+                            const CfFace& face = a.cf[a.cfidx[slot + f]];
+                            stage_face_planes<T, 2, P>(face, E, a.fu_in, a.fog_in, W + off, tid, S::NT);
+                            off += staged_words(face.kind, F);
+                        }
+                    }
+                    __syncthreads();
+                    off = 0;
+#pragma unroll
+                    for (int f = 0; f < 6; ++f) {
+                        if (flags & (1u << f)) {
+                            const CfFace& face = a.cf[a.cfidx[slot + f]];
+                            T* w = W + off;
+                            const int ns = face.kind ? 4 : 1;
+                            dense_fill_at<T, 2, P>(
+                                face, E, [&]() { return (const T*)(w + 2 * ns * F); },
+                                [&](int q) { return (const T*)(w + ns * F + q * F); }, tb, *sct,
+                                w + (face.kind ? ns * F : 3 * F), tid, S::NT);
+                            off += staged_words(face.kind, F);
+                        }
+                    }
+                    __syncthreads();
+                    off = 0;
+#pragma unroll
+                    for (int f = 0; f < 6; ++f) {
+                        if (flags & (1u << f)) {
+                            const CfFace& face = a.cf[a.cfidx[slot + f]];
+                            const T* w = W + off;
+                            const int ns = face.kind ? 4 : 1;
+                            dense_point_at<T, 2, P>(face, tid, E, [&](int q) { return w + q * F; }, *sct,
+                                                    w + (face.kind ? ns * F : 3 * F), ug[f], gp[f]);
+                            off += staged_words(face.kind, F);
+                        }
+                    }
+                } else {
+                    __syncthreads();
+                    int off = 0;
+#pragma unroll
+                    for (int f = 0; f < 6; ++f) {
+                        if (flags & (1u << f)) {
+                            const CfFace& face = a.cf[a.cfidx[slot + f]];
+                            dense_fill<T, 2, P>(face, E, a.fu_in, a.fog_in, tb, *sct, W + off, tid, S::NT);
+                            off += face.kind == 0 ? (N / 2) * (N / 2) : 4 * F;
+                        }
+                    }
+                    __syncthreads();
+                    off = 0;
+#pragma unroll
+                    for (int f = 0; f < 6; ++f) {
+                        if (flags & (1u << f)) {
+                            const CfFace& face = a.cf[a.cfidx[slot + f]];
+                            dense_point<T, 2, P>(face, tid, E, a.fu_in, *sct, W + off, ug[f], gp[f]);
+                            off += face.kind == 0 ? (N / 2) * (N / 2) : 4 * F;
+                        }
                     }
                 }
                 __syncthreads();

@@ -19,7 +19,8 @@ EXPORTS = [
     "twoldg_rhs", "twoldg_truncate", "twoldg_rk4_step", "twoldg_reset_compensation",
     "twoldg_energy", "twoldg_norm", "twoldg_modal_indicator", "twoldg_mode_amplitude",
     "twoldg_synchronize", "twoldg_batch_create", "twoldg_batch_destroy", "twoldg_batch_offsets",
-    "twoldg_batch_rk4_step", "twoldg_batch_synchronize", "twoldg_profile_step", "twoldg_profile_kernels",
+    "twoldg_batch_rk4_step", "twoldg_batch_synchronize", "twoldg_batch_stream", "twoldg_profile_step",
+    "twoldg_profile_kernels",
     "twoldg_stream", "twoldg_boundary_faces", "twoldg_set_boundary_values",
     "twoldg_rhs_static", "twoldg_autotune", "twoldg_batch_autotune", "twoldg_transfer", "twoldg_gather",
     "twoldg_transfer_plan_create", "twoldg_transfer_plan_update", "twoldg_transfer_plan_destroy",
@@ -109,6 +110,7 @@ def lib():
             "twoldg_batch_offsets": (ctypes.c_int, [vp, ctypes.POINTER(i64), ctypes.POINTER(i64)]),
             "twoldg_batch_rk4_step": (ctypes.c_int, [vp, vp, ctypes.POINTER(d), i32]),
             "twoldg_batch_synchronize": (ctypes.c_int, [vp]),
+            "twoldg_batch_stream": (vp, [vp]),
             "twoldg_profile_step": (ctypes.c_int, [vp, vp, d, ctypes.POINTER(ctypes.c_float)]),
             "twoldg_profile_kernels": (ctypes.c_int, [vp, vp, ctypes.POINTER(ctypes.c_float), i32]),
             "twoldg_stream": (vp, [vp]),

@@ -60,6 +60,11 @@ class Batch:
     def synchronize(self):
         _lib.check(_lib.lib().twoldg_batch_synchronize(self._h))
 
+    def stream(self):
+        """The batch's CUDA stream as a torch ExternalStream (for events)."""
+        import torch
+        return torch.cuda.ExternalStream(_lib.lib().twoldg_batch_stream(self._h))
+
     def autotune(self, u, dts, cache=None):
         """Time the stage kernel's launch layouts of every shape group on u
         (unchanged) with steps dts and keep the fastest; cache: a JSON file of
