@@ -52,7 +52,7 @@ extern "C" {
 
 typedef struct twoldg_desc {
     int32_t dim;             /* D = 1, 2 or 3 */
-    int32_t order;           /* P >= 1 */
+    int32_t order;           /* P, 1 to 8 (TWOLDG_EUNSUP beyond) */
     int32_t elems;           /* E, even */
     int32_t precision;       /* TWOLDG_F64 / TWOLDG_F32 / TWOLDG_F32C */
     int32_t truncate;        /* 1: v held at degree P-1 (the paper's scheme) */

@@ -29,6 +29,15 @@ CASES = [
     (1, 3, 2, 4, False, True),
     (2, 2, 6, 2, False, False),     # E = 6: the run-time-shape kernel
     (3, 1, 6, 1, True, False),
+    # orders above 6: the run-time-shape kernel (Element(T, P) is any P >= 1,
+    # src/element.jl:129-170; the library builds P <= 8)
+    (1, 7, 2, 3, False, False),
+    (1, 8, 4, 2, True, False),
+    (2, 7, 2, 2, False, False),
+    (2, 8, 2, 2, True, False),
+    (2, 7, 2, 4, False, True),
+    (3, 7, 2, 1, False, False),
+    (3, 8, 2, 1, True, False),
 ]
 
 

@@ -183,7 +183,7 @@ struct twoldg_runner {
             std::string err;
             if (!build_mesh(d, m, err)) return fail(TWOLDG_EINVAL, err);
             if (!tables().get(m.P))
-                return fail(TWOLDG_EUNSUP, "element order P = " + std::to_string(m.P) + " is not built (1..6)");
+                return fail(TWOLDG_EUNSUP, "element order P = " + std::to_string(m.P) + " is not built (1..8)");
             const bool metric = d.coef != nullptr;
             const int full = d.metric == 2 ? 1 : 0;
             if (d.metric < 0 || d.metric > 2)

@@ -11,6 +11,8 @@ Ops* make_ops_d2_p3(int prec, const ElementTables<double>& t64, const ElementTab
 Ops* make_ops_d2_p4(int prec, const ElementTables<double>& t64, const ElementTables<float>& t32);
 Ops* make_ops_d2_p5(int prec, const ElementTables<double>& t64, const ElementTables<float>& t32);
 Ops* make_ops_d2_p6(int prec, const ElementTables<double>& t64, const ElementTables<float>& t32);
+Ops* make_ops_d2_p7(int prec, const ElementTables<double>& t64, const ElementTables<float>& t32);
+Ops* make_ops_d2_p8(int prec, const ElementTables<double>& t64, const ElementTables<float>& t32);
 
 Ops* make_ops_d2(int prec, int P, const ElementTables<double>& t64, const ElementTables<float>& t32) {
     switch (P) {
@@ -20,6 +22,8 @@ Ops* make_ops_d2(int prec, int P, const ElementTables<double>& t64, const Elemen
         case 4: return make_ops_d2_p4(prec, t64, t32);
         case 5: return make_ops_d2_p5(prec, t64, t32);
         case 6: return make_ops_d2_p6(prec, t64, t32);
+        case 7: return make_ops_d2_p7(prec, t64, t32);
+        case 8: return make_ops_d2_p8(prec, t64, t32);
         default: return nullptr;
     }
 }

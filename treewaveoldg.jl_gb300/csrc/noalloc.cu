@@ -86,7 +86,7 @@ extern "C" int twoldg_rhs_static(const twoldg_desc* desc, void* du, const void* 
     const ElementTables<double>* t64;
     const ElementTables<float>* t32;
     if (!static_rhs_tables(m.P, &t64, &t32))
-        return static_rhs_fail(TWOLDG_EUNSUP, "element order P = " + std::to_string(m.P) + " is not built (1..6)");
+        return static_rhs_fail(TWOLDG_EUNSUP, "element order P = " + std::to_string(m.P) + " is not built (1..8)");
     Ops* ops = nullptr;
     if (m.D == 1) ops = make_ops_d1(prec, m.P, *t64, *t32);
     if (m.D == 2) ops = make_ops_d2(prec, m.P, *t64, *t32);

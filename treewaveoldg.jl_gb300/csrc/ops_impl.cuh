@@ -32,6 +32,9 @@ inline int grid_for(int64_t work, int threads) {
 
 template <typename T, int D, int P, bool COMP>
 class OpsImpl : public Ops {
+    // the register-line and fixed-shape stage kernels are built for P <= 6;
+    // higher orders run the run-time-shape kernel
+    static constexpr bool kShaped = P <= 6;
     Tab<T, P> tb_;
     CfTab<T, P> ct_;
     ElementTables<T> et_;
@@ -45,16 +48,20 @@ public:
         cudaDeviceGetAttribute(&max_smem_, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev);
         set_attrs(stage_kernel<T, D, P, COMP>);
-        set_attrs(stage_kernel_c<T, D, P, 2, COMP>);
-        set_attrs(stage_kernel_c<T, D, P, 4, COMP>);
-        if constexpr (D == 2) {
+        if constexpr (kShaped) {
+            set_attrs(stage_kernel_c<T, D, P, 2, COMP>);
+            set_attrs(stage_kernel_c<T, D, P, 4, COMP>);
+        }
+        if constexpr (D == 2 && kShaped) {
             set_attrs2r<2>();
             set_attrs2r<4>();
         }
-        if constexpr (D == 3) {
+        if constexpr (D == 3 && kShaped) {
             set_attrs3r<2>();
             set_attrs3r<4>();
             stage3r_cf_attrs<T, P, COMP>(max_smem_);
+        }
+        if constexpr (D == 3) {
             set_attrs(fm_gradient_kernel<T, P>);
             set_attrs(fm_stage_kernel<T, P, COMP>);
             set_attrs(fm_stage_kernel<T, P, COMP, 1>);
@@ -134,15 +141,15 @@ public:
     // 0 or a kernel the shape cannot take means the first that it can
     int resolve(int kernel, int E, bool flat, bool aligned) const {
         bool line = false;
-        if constexpr (D == 3) {
+        if constexpr (D == 3 && kShaped) {
             line = flat && aligned && ((E == 2 && Stage3R<T, P, 2, COMP>::usable) ||
                                        (E == 4 && Stage3R<T, P, 4, COMP>::usable));
         }
-        if constexpr (D == 2) {
+        if constexpr (D == 2 && kShaped) {
             line = flat && aligned && ((E == 2 && Stage2R<T, P, 2, COMP>::usable) ||
                                        (E == 4 && Stage2R<T, P, 4, COMP>::usable));
         }
-        const bool fixed = aligned && (E == 2 || E == 4);
+        const bool fixed = kShaped && aligned && (E == 2 || E == 4);
         if (kernel == 1 && line) return 1;
         if (kernel == 2 && fixed) return 2;
         if (kernel == 3) return 3;
@@ -157,7 +164,7 @@ public:
     // CTAs of the resolved kernel one SM holds at once
     int resident(int kernel, int threads, int E) const {
         int n = 0;
-        if constexpr (D == 3) {
+        if constexpr (D == 3 && kShaped) {
             if (kernel == 1) {
                 // the stages between the first and the last
                 if (E == 2)
@@ -169,7 +176,7 @@ public:
                 return n;
             }
         }
-        if constexpr (D == 2) {
+        if constexpr (D == 2 && kShaped) {
             if (kernel == 1) {
                 if (E == 2)
                     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage2r_kernel<T, P, 2, false, 2>, threads,
@@ -180,14 +187,16 @@ public:
                 return n;
             }
         }
-        if (kernel == 2) {
-            if (E == 2)
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage_kernel_c<T, D, P, 2, COMP>, threads,
-                                                              stage_smem(E));
-            else
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage_kernel_c<T, D, P, 4, COMP>, threads,
-                                                              stage_smem(E));
-            return n;
+        if constexpr (kShaped) {
+            if (kernel == 2) {
+                if (E == 2)
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage_kernel_c<T, D, P, 2, COMP>, threads,
+                                                                  stage_smem(E));
+                else
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage_kernel_c<T, D, P, 4, COMP>, threads,
+                                                                  stage_smem(E));
+                return n;
+            }
         }
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage_kernel<T, D, P, COMP>, threads, stage_smem(E));
         return n;
@@ -304,7 +313,7 @@ public:
         if (p.cf && p.ncf > 0) {
             // the 3D register-line kernel forms the coarse-fine ghosts in its
             // prologue; the others read the planes a launch of their own fills
-            if constexpr (D == 3) {
+            if constexpr (D == 3 && kShaped) {
                 if (k == 1 && (E == 2 || E == 4)) {
                     a.cf = p.cf;
                     a.cfidx = p.cfidx;
@@ -316,21 +325,25 @@ public:
                                       const_cast<void*>(p.ggd), s);
             if (e != cudaSuccess) return e;
         }
-        if constexpr (D == 3) {
+        if constexpr (D == 3 && kShaped) {
             if (k == 1 && E == 2) return launch3r<2>(a, grid, mode, s);
             if (k == 1 && E == 4) return launch3r<4>(a, grid, mode, s);
         }
-        if constexpr (D == 2) {
+        if constexpr (D == 2 && kShaped) {
             if (k == 1 && E == 2) return launch2r<2>(a, grid, mode, s);
             if (k == 1 && E == 4) return launch2r<4>(a, grid, mode, s);
         }
-        if (k == 2 && E == 2) {
-            stage_kernel_c<T, D, P, 2, COMP><<<grid, StageLaunch<T, D, P, 2>::NT, smem, s>>>(a, tb_);
-        } else if (k == 2 && E == 4) {
-            stage_kernel_c<T, D, P, 4, COMP><<<grid, StageLaunch<T, D, P, 4>::NT, smem, s>>>(a, tb_);
-        } else {
-            stage_kernel<T, D, P, COMP><<<grid, run_threads(3, E), smem, s>>>(a, tb_);
+        if constexpr (kShaped) {
+            if (k == 2 && E == 2) {
+                stage_kernel_c<T, D, P, 2, COMP><<<grid, StageLaunch<T, D, P, 2>::NT, smem, s>>>(a, tb_);
+                return cudaGetLastError();
+            }
+            if (k == 2 && E == 4) {
+                stage_kernel_c<T, D, P, 4, COMP><<<grid, StageLaunch<T, D, P, 4>::NT, smem, s>>>(a, tb_);
+                return cudaGetLastError();
+            }
         }
+        stage_kernel<T, D, P, COMP><<<grid, run_threads(3, E), smem, s>>>(a, tb_);
         return cudaGetLastError();
     }
 
@@ -611,6 +624,8 @@ Ops* make_ops_dim(int prec, int P, const ElementTables<double>& t64, const Eleme
         case 4: return make_ops_p<D, 4>(prec, t64, t32);
         case 5: return make_ops_p<D, 5>(prec, t64, t32);
         case 6: return make_ops_p<D, 6>(prec, t64, t32);
+        case 7: return make_ops_p<D, 7>(prec, t64, t32);
+        case 8: return make_ops_p<D, 8>(prec, t64, t32);
         default: return nullptr;
     }
 }
