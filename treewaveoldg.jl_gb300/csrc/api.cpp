@@ -79,6 +79,10 @@ struct Group {
     std::vector<int> cfidx;               // per face slot its index in cf (-1: none)
     std::vector<double> h;
     std::unique_ptr<Ops> ops;
+    // a flat forest's coarse-fine ghost planes as the 3D register-line
+    // kernel's epilogues write them, per stage parity: u's ghost, the other
+    // side's part of the gradient's ghost and this side's own part
+    DevBuf eu[2], eg[2], es[2];
     DevBuf d_items, d_cf, d_cfidx, fu[2], fog[2], ugd, gfd, ggd, d_part, d_part2;
     bool metric = false;
     int full = 0;                         // 1: the full metric's two-pass stage
@@ -356,6 +360,11 @@ struct twoldg_runner {
                 for (size_t i = 0; i < g.cf.size(); ++i) g.cfidx[g.cf[i].slot] = (int)i;
                 CK(g.d_cfidx.alloc(g.cfidx.size() * sizeof(int)));
                 CK(cudaMemcpy(g.d_cfidx.p, g.cfidx.data(), g.cfidx.size() * sizeof(int), cudaMemcpyHostToDevice));
+                for (int i = 0; i < 2; ++i) {
+                    CK(g.eu[i].alloc(fbytes));
+                    CK(g.eg[i].alloc(fbytes));
+                    CK(g.es[i].alloc(fbytes));
+                }
             }
             for (int i = 0; i < 2; ++i) {
                 CK(g.fu[i].alloc(fbytes));
@@ -491,16 +500,38 @@ struct twoldg_runner {
         return p;
     }
 
-    // A stage's pointers: the stage forms its coarse-fine ghosts itself, from
-    // the face planes `in` (the other passes read the planes cf_all fills).
+    // An RK stage's pointers: on a forest with refinement its coarse-fine
+    // ghost planes of parity `in` (which the previous stage's epilogues, or
+    // prime_cf, wrote) and the next stage's (the other passes read the planes
+    // cf_all fills).
     StagePtrs stage_ptrs(Group& g, void* u, int in) {
         StagePtrs p = ptrs(g, u, in);
         if (!g.cf.empty()) {
             p.cf = (const CfFace*)g.d_cf.p;
             p.cfidx = (const int*)g.d_cfidx.p;
             p.ncf = (int)g.cf.size();
+            p.ugd = g.eu[in].p;
+            p.ggd = g.eg[in].p;
+            p.gsd = g.es[in].p;
+            p.ugd_out = g.eu[1 - in].p;
+            p.ggd_out = g.eg[1 - in].p;
+            p.gsd_out = g.es[1 - in].p;
         }
         return p;
+    }
+
+    // The first stage's coarse-fine ghost planes of every flat group with
+    // refinement, from the face exports of u: u's and the whole gradient
+    // ghost, with no own part.
+    int prime_cf() {
+        for (auto& gp : groups) {
+            Group& g = *gp;
+            if (g.full || g.cf.empty()) continue;
+            CK(g.ops->cf_ghosts((const CfFace*)g.d_cf.p, (int)g.cf.size(), g.E, g.fu[0].p, g.fog[0].p, g.eu[0].p,
+                                nullptr, g.eg[0].p, stream));
+            CK(cudaMemsetAsync(g.es[0].p, 0, (size_t)g.nslots() * g.F * wsize, stream));
+        }
+        return TWOLDG_OK;
     }
 
     FmPtrs fptrs(Group& g, void* u, int in) {
@@ -679,6 +710,7 @@ struct twoldg_runner {
         int r = rk4(u, dts, 0);
         if (r) return r;
         r = export_all(u);
+        if (!r) r = prime_cf();
         if (r) return r;
         std::map<std::string, std::string> lines;  // key -> the entry's text
         std::map<std::string, Launch> known;
@@ -807,6 +839,7 @@ struct twoldg_runner {
         }
         if (nsteps == 0) return TWOLDG_OK;
         int r = export_all(u);
+        if (!r) r = prime_cf();
         if (r) return r;
         const int chunk = (groups.size() > 1 && !any_full()) ? std::min(nsteps, kChunk) : 1;
         cudaGraphExec_t gexec = nullptr;
@@ -966,7 +999,9 @@ int twoldg_rhs(twoldg_problem* p, void* du, const void* u, double t) {
         CK(g.ops->fm_stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, 0, 0, fp, p->stream));
         return TWOLDG_OK;
     }
-    StagePtrs s = p->stage_ptrs(g, const_cast<void*>(u), 0);
+    r = p->cf_all(g, 0);
+    if (r) return r;
+    StagePtrs s = p->ptrs(g, const_cast<void*>(u), 0);
     s.du = du;
     CK(g.ops->stage((const BlockItem*)g.d_items.p, (int)g.items.size(), g.E, 0, 0, s, 0, p->stream));
     return TWOLDG_OK;
@@ -1110,6 +1145,7 @@ int twoldg_profile_step(twoldg_problem* p, void* u, double dt, float* stage_ms) 
     if (!r) r = p->rk4(u, &dts, 0);
     if (r) return r;
     r = p->export_all(u);
+    if (!r) r = p->prime_cf();
     if (r) return r;
     cudaEvent_t ev[5];
     for (int i = 0; i < 5; ++i) CK(cudaEventCreate(&ev[i]));

@@ -70,11 +70,18 @@ struct StageArgs {
     const T* coef;
     const T* trm;
     const T* trd;
-    // coarse-fine faces formed in the stage kernel's prologue (the 3D
-    // register-line kernel): the faces and, per face slot, the face's index
-    // among them; NULL where the planes ugd and ggd were filled before
+    // coarse-fine faces whose ghost planes the 3D register-line kernel
+    // writes in its epilogue for the next stage (the faces and, per face
+    // slot, the face's index among them; NULL where ugd and ggd are filled
+    // by a launch of their own): gsd is this block's own part of the
+    // gradient ghost, which adds to ggd, the other side's; the *_out planes
+    // are the next stage's
     const CfFace* cf;
     const int* cfidx;
+    const T* gsd;
+    T* ugd_out;
+    T* ggd_out;
+    T* gsd_out;
 };
 
 __host__ __device__ constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1); }

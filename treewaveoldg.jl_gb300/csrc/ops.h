@@ -30,12 +30,18 @@ struct StagePtrs {
     const void* trm;   // per-line truncation pairs (NULL: the element's)
     const void* trd;
     // coarse-fine faces (NULL: none, or their ghost planes ugd and ggd are
-    // filled by the caller): the stage forms their ghosts itself, in the
-    // register-line kernel's prologue or by a launch of its own before the
-    // stage kernel; cfidx gives per face slot the face's index in cf (-1: none)
+    // filled by the caller); cfidx gives per face slot the face's index in cf
+    // (-1: none). The 3D register-line kernel reads ugd, ggd and its own part
+    // gsd as the previous stage's epilogues wrote them and writes the next
+    // stage's into the *_out planes; the other kernels have ugd and ggd
+    // filled by a launch of their own before the stage kernel.
     const CfFace* cf;
     const int* cfidx;
     int ncf;
+    const void* gsd;
+    void* ugd_out;
+    void* ggd_out;
+    void* gsd_out;
 };
 
 // Buffers and data of the full-metric passes (fullmetric.cuh).

@@ -59,7 +59,7 @@ public:
         if constexpr (D == 3 && kShaped) {
             set_attrs3r<2>();
             set_attrs3r<4>();
-            stage3r_cf_attrs<T, P, COMP>(max_smem_);
+            if constexpr (sizeof(T) == 4) stage3r_cf_attrs<T, P, COMP>(max_smem_);
         }
         if constexpr (D == 3) {
             set_attrs(fm_gradient_kernel<T, P>);
@@ -303,6 +303,10 @@ public:
         a.trd = (const T*)p.trd;
         a.cf = nullptr;
         a.cfidx = nullptr;
+        a.gsd = (const T*)p.gsd;
+        a.ugd_out = (T*)p.ugd_out;
+        a.ggd_out = (T*)p.ggd_out;
+        a.gsd_out = (T*)p.gsd_out;
         size_t smem = stage_smem(E);
         if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
         if (grid <= 0) grid = std::min(nitems, grid_cap_ > 0 ? grid_cap_ : kMaxGrid);
@@ -311,10 +315,13 @@ public:
         const bool aligned = (al & 15) == 0;
         const int k = resolve(launch_.kernel, E, !p.coef, aligned);
         if (p.cf && p.ncf > 0) {
-            // the 3D register-line kernel forms the coarse-fine ghosts in its
-            // prologue; the others read the planes a launch of their own fills
-            if constexpr (D == 3 && kShaped) {
-                if (k == 1 && (E == 2 || E == 4)) {
+            // the 3D register-line kernel's FP32 RK stages read the planes the
+            // previous stage's epilogues wrote and write the next stage's;
+            // the others (FP64 among them: bound by the FP64 pipe, they
+            // measured faster so) read complete planes a launch of their own
+            // fills
+            if constexpr (D == 3 && kShaped && sizeof(T) == 4) {
+                if (k == 1 && (E == 2 || E == 4) && mode != MODE_RHS && p.ugd_out) {
                     a.cf = p.cf;
                     a.cfidx = p.cfidx;
                     if (E == 2) return stage3r_cf_launch<T, P, 2, COMP>(a, tb_, ct_, grid, mode, s);

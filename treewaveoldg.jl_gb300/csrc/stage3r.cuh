@@ -194,23 +194,109 @@ __device__ __forceinline__ void truncate_lines(const Tab<T, P>& tb, T* sl, T* sc
     }
 }
 
+// The coarse-fine epilogue of a block's stage: for each of its coarse-fine
+// faces, the images of its new face values that the next stage's ghosts are
+// made of, written into the next stage's planes. The gradient ghost of the
+// flat problem's coupling is the image of the other side's face gradient, its
+// own part plus its ghost coefficient times its u ghost over its spacing,
+// and that u ghost is the image of this side's face nodes (dense_fill,
+// dense_point); by linearity it splits into the image of the other side's
+// own part, which that side writes, and the image of this side's u passed
+// there and back, which this side writes:
+// - a fine side writes into the coarse side's planes, over its quarter, the
+//   R images of its u and of its own gradient part over its spacing, and
+//   into its own gsd plane the I image of the R image of its u, times its
+//   ghost coefficient over the coarse spacing;
+// - a coarse side writes into each fine side's planes the I images of its u
+//   and of its own gradient part over its spacing, and into its own gsd
+//   plane the R image of the I images of its u, times its ghost coefficient
+//   over the fine spacing.
+// The block's new u sits in the padded shared copy `su`; the tables, the
+// face's planes and the images use the accumulator `sl` as scratch. Every
+// thread passes every barrier; the face loop is uniform in the CTA.
+template <typename T, int P, int E, class S>
+__device__ __forceinline__ void cf_epilogue(const StageArgs<T>& a, const Tab<T, P>& tb, const CfTab<T, P>& ct,
+                                            int slot, uint32_t flags, int tid, const T* su, T* sl, int s0, int s1,
+                                            int s2) {
+    constexpr int N = S::N, F = S::F, H = N / 2, halfE = E / 2, NT = S::NT;
+    constexpr int SX = S::SX, SXY = S::SXY;
+    constexpr int kTabWords = (int)(sizeof(CfTab<T, P>) / sizeof(T));
+    CfTab<T, P>* sct = reinterpret_cast<CfTab<T, P>*>(sl);
+    T* U = sl + kTabWords;   // the face's new u
+    T* G = U + F;            // its own gradient part
+    T* X = G + F;            // R(u) (H^2 words) or I(u) (4 F words)
+    stage_cftab<T, P>(ct, sct, tid, NT);
+    int n[2] = {tid % N, tid / N};   // this thread's node of a face plane
+#pragma unroll 1
+    for (int f = 0; f < 6; ++f) {
+        if (!(flags & (1u << f))) continue;
+        const CfFace& face = a.cf[a.cfidx[slot + f]];
+        const int d = f >> 1, side = f & 1;
+        const int sd = d == 0 ? 1 : d == 1 ? SX : SXY;
+        const int base = (d == 0 ? s0 : d == 1 ? s1 : s2) + (side ? N - 1 - P : 0) * sd;
+        T e[P + 1];
+#pragma unroll
+        for (int k = 0; k <= P; ++k) e[k] = su[base + k * sd];
+        U[tid] = side == 0 ? e[0] : e[P];
+        G[tid] = own_face_part<T, P>(tb, side, e);
+        __syncthreads();
+        const T gco = ghost_coef<T, P>(tb, 1 - face.side);
+        if (face.kind == 0) {
+            // this block is the fine side: the coarse nodes of its quarter
+            const T inv_h = T(1) / T(face.h);
+            for (int m = tid; m < H * H; m += NT) {
+                const int c[2] = {((face.sub & 1) ? H : 0) + m % H, ((face.sub & 2) ? H : 0) + m / H};
+                const T ru = restrict_at<T, 2, P>(*sct, c, N, halfE, U);
+                const T rg = restrict_at<T, 2, P>(*sct, c, N, halfE, G);
+                const int64_t o = (int64_t)face.src[0] * F + c[0] + N * c[1];
+                a.ugd_out[o] = ru;
+                a.ggd_out[o] = rg * inv_h;
+                X[m] = ru;
+            }
+            __syncthreads();
+            const T k = gco * (T(1) / T(2.0 * face.h));
+            a.gsd_out[(int64_t)(slot + f) * F + tid] = k * prolong_at<T, 2, P>(*sct, n, 0, H, halfE, X);
+        } else {
+            // the coarse side: every node of the four fine faces across it
+            const T inv_h = T(1) / T(face.h);
+            for (int i = tid; i < 4 * F; i += NT) {
+                const int q = i / F, tt = i % F;
+                const int c[2] = {tt % N, tt / N};
+                const T iu = prolong_at<T, 2, P>(*sct, c, q, N, halfE, U);
+                const T ig = prolong_at<T, 2, P>(*sct, c, q, N, halfE, G);
+                const int64_t o = (int64_t)face.src[q] * F + tt;
+                a.ugd_out[o] = iu;
+                a.ggd_out[o] = ig * inv_h;
+                X[i] = iu;
+            }
+            __syncthreads();
+            int bits = 0;
+            for (int kk = 0; kk < 2; ++kk) bits |= ((n[kk] / (P + 1)) / halfE) << kk;
+            const T k = gco * (T(1) / T(0.5 * face.h));
+            a.gsd_out[(int64_t)(slot + f) * F + tid] = k * restrict_at<T, 2, P>(*sct, n, N, halfE, X + bits * F);
+        }
+        __syncthreads();
+    }
+}
+
 // FM: the stage the instantiation runs (1-4), so that each stage's code holds
 // only its own data flow, or 0 for the mode in the arguments (the right-hand
-// side). CFP: the kernel forms the ghosts of its coarse-fine faces itself, in
-// its prologue, from the previous stage's face exports (a.cf, a.cfidx; the
-// forests with refinement); without it they are read from the planes a.ugd
-// and a.ggd, which a uniform forest never reads.
+// side). CFP (a stage of a forest with refinement): the ghosts of the block's
+// coarse-fine faces are read from planes that the previous stage's epilogues
+// wrote, u's from ugd and the gradient's as the other side's part ggd plus
+// this block's own part gsd, and the block's epilogue writes the next
+// stage's (cf_epilogue); without it ugd and ggd are complete, filled by a
+// launch of their own, and a uniform forest never reads them.
 template <typename T, int P, int E, bool COMP, bool LEAN = false, int FM = 0, bool CFP = false>
 __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P, E, COMP, LEAN>::MINB)
     stage3r_kernel(StageArgs<T> a, Tab<T, P> tb, CfTab<T, P> ct) {
     using S = Stage3R<T, P, E, COMP, LEAN>;
     constexpr int P1 = S::P1, N = S::N, F = S::F, NN = S::NN, VW = S::VW;
-    // the prologue's coarse-fine scratch (the tables and the other side's
-    // face gradient of each of up to six faces, 4 F words at most a face)
-    // lives in the shared copy of u and the accumulator, which the z pass
-    // writes first
+    // the epilogue's scratch (the tables, a face's new u and own gradient
+    // part, and its images, 4 F words at most) lives in the accumulator,
+    // free once the block's new v is stored
     constexpr int kTabWords = (int)(sizeof(CfTab<T, P>) / sizeof(T));
-    static_assert(!CFP || S::SS + S::LS >= kTabWords + 24 * F, "u and the accumulator hold the coarse-fine scratch");
+    static_assert(!CFP || S::LS >= kTabWords + 6 * F, "the accumulator holds the coarse-fine scratch");
     constexpr int SX = S::SX, SXY = S::SXY, LX = S::LX, LXY = S::LXY;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* su = reinterpret_cast<T*>(smem_raw);
@@ -264,92 +350,12 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
 #pragma unroll
         for (int f = 0; f < 6; ++f) {
             if (flags & (1u << f)) {
-                ug[f] = CFP ? T(0) : a.ugd[(int64_t)(slot + f) * F + tid];
-                gp[f] = CFP ? T(0) : a.ggd[(int64_t)(slot + f) * F + tid];
+                const int64_t o = (int64_t)(slot + f) * F + tid;
+                ug[f] = a.ugd[o];
+                gp[f] = CFP ? a.ggd[o] + a.gsd[o] : a.ggd[o];
             } else {
                 ug[f] = a.fu_in[(int64_t)nb[f] * F + tid];
                 gp[f] = a.fog_in[(int64_t)nb[f] * F + tid];
-            }
-        }
-        if constexpr (CFP) {
-            if (flags & 0x3fu) {
-                // coarse-fine faces: both ghost planes from the previous
-                // stage's face exports, in place of a launch of their own.
-                // Every face at once, so that their loads are in flight
-                // together; the branches and the face loops are uniform in
-                // the CTA. Where the faces' planes fit in the shared copy of u
-                // and the accumulator (which the z pass writes first), they
-                // are staged there with coalesced loads and the images read
-                // them from shared memory; otherwise the images read them
-                // from global memory. Three barriers after the tables.
-                CfTab<T, P>* sct = reinterpret_cast<CfTab<T, P>*>(su);
-                T* W = su + kTabWords;
-                int need = 0;
-#pragma unroll
-                for (int f = 0; f < 6; ++f)
-                    if (flags & (1u << f)) need += staged_words(a.cf[a.cfidx[slot + f]].kind, F);
-                stage_cftab<T, P>(ct, sct, tid, S::NT);
-                if (need <= S::SS + S::LS - kTabWords) {
-                    int off = 0;
-#pragma unroll
-                    for (int f = 0; f < 6; ++f) {
-                        if (flags & (1u << f)) {
-                            const CfFace& face = a.cf[a.cfidx[slot + f]];
-                            stage_face_planes<T, 2, P>(face, E, a.fu_in, a.fog_in, W + off, tid, S::NT);
-                            off += staged_words(face.kind, F);
-                        }
-                    }
-                    __syncthreads();
-                    off = 0;
-#pragma unroll
-                    for (int f = 0; f < 6; ++f) {
-                        if (flags & (1u << f)) {
-                            const CfFace& face = a.cf[a.cfidx[slot + f]];
-                            T* w = W + off;
-                            const int ns = face.kind ? 4 : 1;
-                            dense_fill_at<T, 2, P>(
-                                face, E, [&]() { return (const T*)(w + 2 * ns * F); },
-                                [&](int q) { return (const T*)(w + ns * F + q * F); }, tb, *sct,
-                                w + (face.kind ? ns * F : 3 * F), tid, S::NT);
-                            off += staged_words(face.kind, F);
-                        }
-                    }
-                    __syncthreads();
-                    off = 0;
-#pragma unroll
-                    for (int f = 0; f < 6; ++f) {
-                        if (flags & (1u << f)) {
-                            const CfFace& face = a.cf[a.cfidx[slot + f]];
-                            const T* w = W + off;
-                            const int ns = face.kind ? 4 : 1;
-                            dense_point_at<T, 2, P>(face, tid, E, [&](int q) { return w + q * F; }, *sct,
-                                                    w + (face.kind ? ns * F : 3 * F), ug[f], gp[f]);
-                            off += staged_words(face.kind, F);
-                        }
-                    }
-                } else {
-                    __syncthreads();
-                    int off = 0;
-#pragma unroll
-                    for (int f = 0; f < 6; ++f) {
-                        if (flags & (1u << f)) {
-                            const CfFace& face = a.cf[a.cfidx[slot + f]];
-                            dense_fill<T, 2, P>(face, E, a.fu_in, a.fog_in, tb, *sct, W + off, tid, S::NT);
-                            off += face.kind == 0 ? (N / 2) * (N / 2) : 4 * F;
-                        }
-                    }
-                    __syncthreads();
-                    off = 0;
-#pragma unroll
-                    for (int f = 0; f < 6; ++f) {
-                        if (flags & (1u << f)) {
-                            const CfFace& face = a.cf[a.cfidx[slot + f]];
-                            dense_point<T, 2, P>(face, tid, E, a.fu_in, *sct, W + off, ug[f], gp[f]);
-                            off += face.kind == 0 ? (N / 2) * (N / 2) : 4 * F;
-                        }
-                    }
-                }
-                __syncthreads();
             }
         }
         // ---- z: the column in registers
@@ -573,12 +579,16 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
             if (final_comp) comp[NN + tid + F * j] = sc[l2 + LXY * j];
         }
         __syncthreads();
+        if constexpr (CFP) {
+            if (flags & 0x3fu) cf_epilogue<T, P, E, S>(a, tb, ct, slot, flags, tid, su, sl, s0, s1, s2);
+        }
     }
 }
 
-// The register-line stage with its coarse-fine prologue (CFP), instantiated
+// The register-line stage of a forest with refinement (CFP), instantiated
 // per order in a translation unit of its own (kernels_d3_p<P>_cf.cu): its
-// shared-memory attributes, set once per device, and a launch of `mode`.
+// shared-memory attributes, set once per device, and a launch of RK stage
+// `mode` (1 to 4).
 template <typename T, int P, bool COMP>
 void stage3r_cf_attrs(int max_smem);
 template <typename T, int P, int E, bool COMP>

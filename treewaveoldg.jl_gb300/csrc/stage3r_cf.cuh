@@ -1,8 +1,10 @@
-// The register-line stage with its coarse-fine prologue: the launches of the
-// CFP instantiations of stage3r_kernel and their attributes. Only the forests
-// with refinement run them, so they live in translation units of their own
+// The register-line stage of a forest with refinement: the launches of the
+// CFP instantiations of stage3r_kernel (coarse-fine ghost planes read as the
+// previous stage's epilogues wrote them, the next stage's written in the
+// block's epilogue) and their attributes. Only the forests with refinement run
+// them, so they live in translation units of their own
 // (kernels_d3_p<P>_cf.cu), which the build compiles beside the uniform ones,
-// and the uniform kernels keep their code as it is without the prologue.
+// and the uniform kernels keep their code as it is.
 #pragma once
 #include "kernels.cuh"
 #include "stage3r.cuh"
@@ -21,7 +23,6 @@ template <typename T, int P, int E, bool COMP>
 inline void stage3r_cf_attrs_e(int max_smem) {
     if constexpr (Stage3R<T, P, E, false>::usable) {
         if constexpr (COMP) stage3r_cf_attr(stage3r_kernel<T, P, E, true, false, 4, true>, max_smem);
-        stage3r_cf_attr(stage3r_kernel<T, P, E, false, false, 0, true>, max_smem);
         stage3r_cf_attr(stage3r_kernel<T, P, E, false, false, 1, true>, max_smem);
         stage3r_cf_attr(stage3r_kernel<T, P, E, false, false, 2, true>, max_smem);
         stage3r_cf_attr(stage3r_kernel<T, P, E, false, false, 3, true>, max_smem);
@@ -35,9 +36,10 @@ void stage3r_cf_attrs(int max_smem) {
     stage3r_cf_attrs_e<T, P, 4, COMP>(max_smem);
 }
 
-// Every stage in the plain register budget (the lean stage 1 and 2 variants
-// of the uniform forests are left out here: a block with coarse-fine faces
-// holds more live values through its prologue).
+// Every RK stage in the plain register budget (the lean stage 1 and 2
+// variants of the uniform forests are left out here); the right-hand side of
+// a forest with refinement runs the plain kernel after a launch that fills
+// its ghost planes.
 template <typename T, int P, int E, bool COMP>
 cudaError_t stage3r_cf_launch(const StageArgs<T>& a, const Tab<T, P>& tb, const CfTab<T, P>& ct, int grid,
                               int mode, cudaStream_t s) {
@@ -62,21 +64,20 @@ cudaError_t stage3r_cf_launch(const StageArgs<T>& a, const Tab<T, P>& tb, const 
         else if (mode == MODE_STAGE4)
             stage3r_kernel<T, P, E, false, false, 4, true><<<grid, S0::NT, m0, s>>>(a, tb, ct);
         else
-            stage3r_kernel<T, P, E, false, false, 0, true><<<grid, S0::NT, m0, s>>>(a, tb, ct);
+            return cudaErrorInvalidValue;
         return cudaGetLastError();
     }
 }
 
-// The instantiations of one order: FP64, FP32 and FP32 compensated.
+// The instantiations of one order: FP32 and FP32 compensated (the FP64
+// stages, bound by the FP64 pipe, fill their planes in a launch of their own,
+// which measured faster there).
 #define TWOLDG_STAGE3R_CF_E(T, P, E, COMP)                                                                      \
     template cudaError_t stage3r_cf_launch<T, P, E, COMP>(const StageArgs<T>&, const Tab<T, P>&,              \
                                                            const CfTab<T, P>&, int, int, cudaStream_t);
 #define TWOLDG_STAGE3R_CF(P)                                \
-    template void stage3r_cf_attrs<double, P, false>(int); \
     template void stage3r_cf_attrs<float, P, false>(int);  \
     template void stage3r_cf_attrs<float, P, true>(int);   \
-    TWOLDG_STAGE3R_CF_E(double, P, 2, false)               \
-    TWOLDG_STAGE3R_CF_E(double, P, 4, false)               \
     TWOLDG_STAGE3R_CF_E(float, P, 2, false)                \
     TWOLDG_STAGE3R_CF_E(float, P, 4, false)                \
     TWOLDG_STAGE3R_CF_E(float, P, 2, true)                 \
