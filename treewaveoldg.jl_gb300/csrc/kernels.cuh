@@ -1192,18 +1192,27 @@ __global__ void __launch_bounds__(256) energy_kernel(StageArgs<T> a, Tab<T, P> t
         const T inv_h = T(1) / T(h);
         load_u_with_ghosts<T, D, 0>(g, it, a.u, a, su);
         __syncthreads();
+        // the quadrature weight of a node is wscale^D times the product of
+        // its reference weights: the sum runs over the products, and the
+        // block's factor wscale^D multiplies it once, so a node costs few
+        // FP64 operations (the accumulation stays FP64)
         double local = 0;
         const double wscale = h * P1 / 2.0;
+        double wsD = 1.0;
+        for (int k = 0; k < D; ++k) wsD *= wscale;
+        double wqd[P1];
+#pragma unroll
+        for (int i = 0; i < P1; ++i) wqd[i] = (double)tb.wq[i];
         const T* uv = a.u + it.off + g.NN;
         // on a geometry: 1/2 sum w (sqrt(g) v^2 + sum_d F_d^2 / A_d), F_d = A_d D_d u
         const T* cf = a.coef ? a.coef + (int64_t)item * (1 + D) * g.NN : nullptr;
         for (int n = threadIdx.x; n < g.NN; n += blockDim.x) {
             int x[3];
             owned_coords<D>(g, n, x);
-            double w = 1.0;
-            for (int k = 0; k < D; ++k) w *= wscale * (double)tb.wq[x[k] % P1];
-            double v = (double)uv[n];
-            local += (cf ? (double)cf[n] : 1.0) * w * v * v;
+            double w = wqd[x[0] % P1];
+            for (int k = 1; k < D; ++k) w *= wqd[x[k] % P1];
+            const double v = (double)uv[n];
+            local += (cf ? (double)cf[n] * w : w) * v * v;
         }
         for (int d = 0; d < D; ++d) {
             const int sd = g.sstride(d);
@@ -1214,23 +1223,25 @@ __global__ void __launch_bounds__(256) energy_kernel(StageArgs<T> a, Tab<T, P> t
                 int base = sidx<D>(g, x);
                 double wt = 1.0;
                 for (int k = 0; k < D; ++k)
-                    if (k != d) wt *= wscale * (double)tb.wq[x[k] % P1];
+                    if (k != d) wt *= wqd[x[k] % P1];
                 T w[P + 3], out[P + 1];
 #pragma unroll
                 for (int k = 0; k < P + 3; ++k) w[k] = su[base + (k - 1) * sd];
                 line_derivative<T, P>(tb, w, out);
                 const int ob = oidx<D>(g, x);
                 const int od = d == 0 ? 1 : d == 1 ? g.N : g.N * g.N;
+                double line = 0;
 #pragma unroll
                 for (int i = 0; i <= P; ++i) {
-                    double gv = (double)(out[i] * inv_h);
-                    double Ad = cf ? (double)cf[(1 + d) * g.NN + ob + i * od] : 1.0;
-                    local += Ad * wt * wscale * (double)tb.wq[i] * gv * gv;
+                    const double gv = (double)(out[i] * inv_h);
+                    const double wi = cf ? (double)cf[(1 + d) * g.NN + ob + i * od] * wqd[i] : wqd[i];
+                    line += wi * gv * gv;
                 }
+                local += wt * line;
             }
         }
         double s = block_reduce_sum<D>(local, red);
-        if (threadIdx.x == 0) a.partial[item] = 0.5 * s;
+        if (threadIdx.x == 0) a.partial[item] = 0.5 * wsD * s;
         __syncthreads();
     }
 }
@@ -1246,14 +1257,21 @@ __global__ void norm_kernel(const BlockItem* items, int nitems, int E, const T* 
     constexpr int P1 = P + 1;
     const int N = E * P1;
     const int NN = ipow(N, D);
+    double wqd[P1];
+#pragma unroll
+    for (int i = 0; i < P1; ++i) wqd[i] = (double)tb.wq[i];
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         const BlockItem it = items[item];
+        // the weights' block factor wscale^D multiplies the sums once
         const double wscale = it.h * P1 / 2.0;
+        double wsD = 1.0;
+        for (int k = 0; k < D; ++k) wsD *= wscale;
         double num = 0, vol = 0;
         for (int n = threadIdx.x; n < NN; n += blockDim.x) {
-            double w = 1.0;
             int m = n;
-            for (int k = 0; k < D; ++k) { w *= wscale * (double)tb.wq[(m % N) % P1]; m /= N; }
+            double w = wqd[(m % N) % P1];
+            m /= N;
+            for (int k = 1; k < D; ++k) { w *= wqd[(m % N) % P1]; m /= N; }
             // on a geometry the norm is weighted by sqrt(g): the physical volume
             if (coef) w *= (double)coef[(int64_t)item * ncoef * NN + n];
             for (int var = 0; var < 2; ++var) {
@@ -1282,7 +1300,10 @@ __global__ void norm_kernel(const BlockItem* items, int nitems, int E, const T* 
             s = block_reduce_sum<D>(num, red);
         }
         double v = block_reduce_sum<D>(vol, red);
-        if (threadIdx.x == 0) { part_num[item] = s; part_vol[item] = v; }
+        if (threadIdx.x == 0) {
+            part_num[item] = p == 0 ? s : wsD * s;
+            part_vol[item] = wsD * v;
+        }
         __syncthreads();
     }
 }
@@ -1344,14 +1365,99 @@ __global__ void mode_kernel(const BlockItem* items, int nitems, int E, const T* 
     }
 }
 
-// Largest |u| of one variable, per block (the indicator's global scale).
+// The modal indicator with the block staged in shared memory: one CTA a
+// block (grid-stride), the variable's N^D values read once with coalesced
+// loads, then one thread an (element, dimension) pair (the element index
+// fastest), which takes every line of the element along that dimension and
+// keeps each mode's largest |c_q| in registers; the weight and power are
+// applied once per element and mode: the power is monotone and the weight
+// non-negative, so the largest (w |c|)^p over the lines is (w max |c|)^p.
+// smem: N^D values and D E^D nq words.
+template <typename T, int D, int P>
+__global__ void __launch_bounds__(256) mode_staged_kernel(const BlockItem* items, int nitems, int E, const T* u,
+                                                         int var, ModeTab<T, P> mt, T* tau) {
+    constexpr int P1 = P + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int N = E * P1;
+    const int NN = ipow(N, D);
+    const int EE = ipow(E, D);
+    const int nl = ipow(P1, D - 1);
+    const int nq = mt.nq;
+    T* sv = reinterpret_cast<T*>(smem_raw);
+    T* best = sv + ((NN + 3) & ~3);
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const T* a = u + items[item].off + (int64_t)var * NN;
+        for (int n = threadIdx.x; n < NN; n += blockDim.x) sv[n] = a[n];
+        __syncthreads();
+        for (int li = threadIdx.x; li < D * EE; li += blockDim.x) {
+            const int e = li % EE, d = li / EE;
+            int base = 0, s = 1, m = e, sd = 1;
+            int st[2] = {0, 0}, nt = 0;   // the strides of the line's two other dimensions
+            for (int k = 0; k < D; ++k) {
+                base += (m % E) * P1 * s;
+                m /= E;
+                if (k == d) sd = s;
+                else st[nt++] = s;
+                s *= N;
+            }
+            T top[P1];
+#pragma unroll
+            for (int q = 0; q < P1; ++q) top[q] = T(0);
+            for (int l = 0; l < nl; ++l) {
+                const int off = base + (l % P1) * st[0] + (D == 3 ? (l / P1) * st[1] : 0);
+                T line[P1];
+#pragma unroll
+                for (int j = 0; j < P1; ++j) line[j] = sv[off + j * sd];
+#pragma unroll
+                for (int q = 0; q < P1; ++q) {
+                    if (q < nq) {
+                        T c = T(0);
+#pragma unroll
+                        for (int j = 0; j < P1; ++j) c += mt.dual[q][j] * line[j];
+                        c = c < T(0) ? -c : c;
+                        top[q] = c > top[q] ? c : top[q];
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < P1; ++q)
+                if (q < nq) best[(d * EE + e) * nq + q] = top[q];
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < EE; e += blockDim.x) {
+            T out = T(0);
+#pragma unroll
+            for (int q = 0; q < P1; ++q) {
+                if (q < nq) {
+                    T c = best[e * nq + q];
+                    for (int d = 1; d < D; ++d) {
+                        const T cd = best[(d * EE + e) * nq + q];
+                        c = cd > c ? cd : c;
+                    }
+                    const T x = mt.weight[q] * c;
+                    const T v = mt.pw[q] == T(1) ? x : (T)pow((double)x, (double)mt.pw[q]);
+                    out = v > out ? v : out;
+                }
+            }
+            tau[(int64_t)item * EE + e] = mt.post * out;
+        }
+        __syncthreads();
+    }
+}
+
+// The largest |x| is exact in the field's own type, so the comparisons run
+// in it and only the block's result is widened to FP64.
 template <typename T, int D>
 __global__ void maxabs_kernel(const BlockItem* items, int nitems, int NN, const T* u, int var, double* part) {
     __shared__ double red[32];
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         const T* a = u + items[item].off + (int64_t)var * NN;
-        double m = 0;
-        for (int n = threadIdx.x; n < NN; n += blockDim.x) m = fmax(m, fabs((double)a[n]));
+        T mt = T(0);
+        for (int n = threadIdx.x; n < NN; n += blockDim.x) {
+            const T x = a[n];
+            mt = fmax(mt, x < T(0) ? -x : x);
+        }
+        double m = (double)mt;
         for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
         int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         if (lane == 0) red[wid] = m;

@@ -86,6 +86,7 @@ public:
         // the energy and truncation kernels stage blocks in shared memory too
         set_attrs(energy_kernel<T, D, P>);
         set_attrs(truncate_kernel<T, D, P>);
+        set_attrs(mode_staged_kernel<T, D, P>);
         cudaGetLastError();
         const int P1 = P + 1, PW = P + 3;
         for (int i = 0; i < P1; ++i) {
@@ -604,10 +605,21 @@ public:
         }
         mt.nq = nq;
         mt.post = (T)post;
-        int64_t EE = 1;
-        for (int k = 0; k < D; ++k) EE *= E;
-        mode_kernel<T, D, P><<<grid_for((int64_t)nitems * EE, 128), 128, 0, s>>>(items, nitems, E, (const T*)u,
-                                                                                 var, mt, (T*)tau);
+        int64_t EE = 1, NN = 1;
+        for (int k = 0; k < D; ++k) {
+            EE *= E;
+            NN *= (int64_t)E * (P + 1);
+        }
+        // the block staged in shared memory where it fits, else one thread
+        // an element reading global memory
+        const size_t smem = ((size_t)((NN + 3) & ~3) + (size_t)D * EE * nq) * sizeof(T);
+        if (smem <= (size_t)max_smem_) {
+            mode_staged_kernel<T, D, P><<<std::min(nitems, kMaxGrid), 256, smem, s>>>(items, nitems, E,
+                                                                                      (const T*)u, var, mt, (T*)tau);
+        } else {
+            mode_kernel<T, D, P><<<grid_for((int64_t)nitems * EE, 128), 128, 0, s>>>(items, nitems, E, (const T*)u,
+                                                                                     var, mt, (T*)tau);
+        }
         return cudaGetLastError();
     }
 };
