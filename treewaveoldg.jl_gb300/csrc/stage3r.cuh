@@ -2,8 +2,9 @@
 // lines in registers. One thread per (a, b) position of the block's N x N
 // cross-section; in direction d a thread owns the complete line of N nodes
 // at its tangential position (all E elements), so it holds the line of u,
-// its gradient D_d u / h (with the two gradient ghosts) and the Laplacian
-// term D_d D_d u in registers: the gradient never goes through shared memory.
+// its gradient D_d u (with the two gradient ghosts, all without the factor
+// 1/h, which the Laplacian takes once as 1/h^2) and the Laplacian term
+// D_d D_d u in registers: the gradient never goes through shared memory.
 // The z direction is the thread's own column, loaded from global memory
 // straight into registers, so it touches shared memory only to add its
 // Laplacian term; x and y lines read u from the padded shared copy and add
@@ -124,6 +125,18 @@ __device__ __forceinline__ T grad_ghost(const Tab<T, P>& tb, uint32_t flags, int
                                         T inv_h) {
     if (flags & (1u << f)) return pre;
     const T gnb = (pre + ghost_coef<T, P>(tb, nslot & 1) * own) * inv_h;
+    return (flags & (1u << (8 + f))) ? -gnb : gnb;
+}
+
+// The same ghost times h: the register-line 3D kernel differentiates u and
+// then its gradient without the two 1/h factors, and scales the Laplacian by
+// 1/h^2 once; a coarse-fine ghost (a plane of gradient values) takes the
+// factor h itself.
+template <typename T, int P>
+__device__ __forceinline__ T grad_ghost_raw(const Tab<T, P>& tb, uint32_t flags, int nslot, int f, T pre, T own,
+                                            T h) {
+    if (flags & (1u << f)) return pre * h;
+    const T gnb = pre + ghost_coef<T, P>(tb, nslot & 1) * own;
     return (flags & (1u << (8 + f))) ? -gnb : gnb;
 }
 
@@ -331,7 +344,10 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
         int nb[6];
 #pragma unroll
         for (int f = 0; f < 6; ++f) nb[f] = it.nb[f];
-        const T inv_h = T(1) / T(it.h);
+        // the two passes differentiate without 1/h; the Laplacian takes 1/h^2
+        const T hb = T(it.h);
+        const T inv_h = T(1) / hb;
+        const T inv_h2 = inv_h * inv_h;
         const T* yu = ysrc + it.off;
         if (tid == 0) prefetch_stage3r<T>(a, item, NN);
         // every global load of the block's prologue at once: the column, the u
@@ -369,11 +385,11 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
             line[0] = ug[4];
             line[N + 1] = ug[5];
             T g[N + 2], gi[N], lap[N];
-            line_full<T, P, E>(tb, line, gi, inv_h);
+            line_full<T, P, E>(tb, line, gi, T(1));
 #pragma unroll
             for (int j = 0; j < N; ++j) g[1 + j] = gi[j];
-            g[0] = grad_ghost<T, P>(tb, flags, nb[4], 4, gp[4], line[1], inv_h);
-            g[N + 1] = grad_ghost<T, P>(tb, flags, nb[5], 5, gp[5], line[N], inv_h);
+            g[0] = grad_ghost_raw<T, P>(tb, flags, nb[4], 4, gp[4], line[1], hb);
+            g[N + 1] = grad_ghost_raw<T, P>(tb, flags, nb[5], 5, gp[5], line[N], hb);
             line_full<T, P, E>(tb, g, lap, T(1));
 #pragma unroll
             for (int j = 0; j < N; ++j) sl[l2 + LXY * j] = lap[j];
@@ -403,11 +419,11 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
 #pragma unroll
                 for (int k = 0; k < N + 2; ++k) line[k] = su[sb + (k - 1) * ss];
             }
-            line_full<T, P, E>(tb, line, gi, inv_h);
+            line_full<T, P, E>(tb, line, gi, T(1));
 #pragma unroll
             for (int j = 0; j < N; ++j) g[1 + j] = gi[j];
-            g[0] = grad_ghost<T, P>(tb, flags, nb[2 * d], 2 * d, gp[2 * d], line[1], inv_h);
-            g[N + 1] = grad_ghost<T, P>(tb, flags, nb[2 * d + 1], 2 * d + 1, gp[2 * d + 1], line[N], inv_h);
+            g[0] = grad_ghost_raw<T, P>(tb, flags, nb[2 * d], 2 * d, gp[2 * d], line[1], hb);
+            g[N + 1] = grad_ghost_raw<T, P>(tb, flags, nb[2 * d + 1], 2 * d + 1, gp[2 * d + 1], line[N], hb);
             line_full<T, P, E>(tb, g, lap, T(1));
             if (d == 0 && N % VW == 0) {
                 using V = typename V16<T>::type;
@@ -432,7 +448,7 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
 #pragma unroll
             for (int j = 0; j < N; ++j) {
                 du[tid + F * j] = yv[tid + F * j];
-                du[NN + tid + F * j] = sl[l2 + LXY * j] * inv_h;
+                du[NN + tid + F * j] = sl[l2 + LXY * j] * inv_h2;
             }
             __syncthreads();
             continue;
@@ -493,10 +509,10 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
                     // Y2's u for the face export; the stage derivative's v,
                     // truncated below and stored
                     o_u[0] = uuq[0] + rc.cn * yq[0];
-                    o_v[0] = lap[0] * inv_h;
+                    o_v[0] = lap[0] * inv_h2;
                     o_c[0] = T(0);
                 } else {
-                    stage_points<T, COMP, 1>(mode, rc, yq, uuq, uvq, auq, avq, cuq, cviq, lap, inv_h, o_u, o_v,
+                    stage_points<T, COMP, 1>(mode, rc, yq, uuq, uvq, auq, avq, cuq, cviq, lap, inv_h2, o_u, o_v,
                                              o_c);
                 }
                 au[q] = auq[0];
