@@ -19,6 +19,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "stage3r.cuh"
 
 namespace twoldg {
 
@@ -120,6 +121,27 @@ __device__ __forceinline__ int sym_index(int d, int e) {
 }
 
 // ---------------------------------------------------------------------------
+// u's ghost across face f at its face node tt: a coarse-fine face's plane
+// (the neighbour's u through I or R), the radiative face's own node (index
+// `own` in the block, so that the wide derivative's face correction vanishes
+// there, src/evolution.jl:1213-1221), the caller's Dirichlet value, the plane
+// wave's value at the boundary face node's position, or the neighbour's
+// exported face node, oriented across a glue.
+template <typename T>
+__device__ __forceinline__ T fm_u_ghost(const FmArgs<T>& a, const BlockItem& it, int f, int tt, int F, int N, double t,
+                                        const T* yu, int own) {
+    if (it.flags & (1u << f)) return a.ugd[(int64_t)(it.slot + f) * F + tt];
+    if (it.nb[f] < 0 && a.boundary == 1) return yu[own];
+    if (it.nb[f] < 0 && a.boundary == 2) return (T)boundary_values(a, it.slot + f, t, F)[tt];
+    if (it.nb[f] < 0) {
+        const double* X = a.bnd_x + (int64_t)(it.slot + f) * 3 * F;
+        const double th = a.wave.k[0] * X[tt] + a.wave.k[1] * X[F + tt] + a.wave.k[2] * X[2 * F + tt] -
+                          a.wave.omega * t + a.wave.phi;
+        return (T)sin(th);
+    }
+    return a.fu_in[(int64_t)it.nb[f] * F + oriented(tt, N, face_orient(it, f))];
+}
+
 template <typename T, int P>
 __global__ void __launch_bounds__(256) fm_gradient_kernel(FmArgs<T> a, Tab<T, P> tb) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -148,28 +170,9 @@ __global__ void __launch_bounds__(256) fm_gradient_kernel(FmArgs<T> a, Tab<T, P>
         for (int i = threadIdx.x; i < 6 * g.F; i += blockDim.x) {
             const int f = i / g.F, tt = i % g.F;
             const int d = f >> 1, side = f & 1;
-            T v;
-            if (it.flags & (1u << f)) {
-                // a coarse-fine face: the neighbour's u through I or R
-                v = a.ugd[(int64_t)(it.slot + f) * g.F + tt];
-            } else if (it.nb[f] < 0 && a.boundary == 1) {
-                // radiative: the face node's own u, so that the wide derivative's
-                // face correction vanishes there (src/evolution.jl:1213-1221)
-                int xo[3];
-                plane_coords<3>(g, d, tt, side == 0 ? 0 : g.N - 1, xo);
-                v = yu[oidx<3>(g, xo)];
-            } else if (it.nb[f] < 0 && a.boundary == 2) {
-                // Dirichlet: the caller's value at the boundary face node
-                v = (T)boundary_values(a, it.slot + f, t, g.F)[tt];
-            } else if (it.nb[f] < 0) {
-                // Dirichlet: the data at the boundary face node's position
-                const double* X = a.bnd_x + (int64_t)(it.slot + f) * 3 * g.F;
-                const double th = a.wave.k[0] * X[tt] + a.wave.k[1] * X[g.F + tt] + a.wave.k[2] * X[2 * g.F + tt] -
-                                  a.wave.omega * t + a.wave.phi;
-                v = (T)sin(th);
-            } else {
-                v = a.fu_in[(int64_t)it.nb[f] * g.F + oriented(tt, g.N, face_orient(it, f))];
-            }
+            int xo[3];
+            plane_coords<3>(g, d, tt, side == 0 ? 0 : g.N - 1, xo);
+            const T v = fm_u_ghost(a, it, f, tt, g.F, g.N, t, yu, oidx<3>(g, xo));
             int xg[3];
             plane_coords<3>(g, d, tt, side == 0 ? -1 : g.N, xg);
             su[sidx<3>(g, xg)] = v;
@@ -247,6 +250,176 @@ __global__ void __launch_bounds__(256) fm_gradient_kernel(FmArgs<T> a, Tab<T, P>
 #pragma unroll
                 for (int e = 0; e < 3; ++e) s += cf[(1 + 3 * e + ci) * g.NN + n] * De[e];
                 o[ci * g.F + tt] = s / J;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// The gradient pass with a compile-time block shape (E = 2 or 4): the
+// register-line layout of stage3r_kernel. One thread per (a, b) position of
+// the block's cross-section: its z column of u in registers, where it forms
+// D_z u with the column's two ghosts; x and y lines from the padded shared
+// copy of u, D_x into a ghost-free shared array and D_y kept in registers
+// until every line has read u, then written over it. Each thread then forms
+// the fluxes (or, in the energy pass, V) down its column, and the face planes
+// of V read D_z on the x and y faces from a small plane buffer. Shared
+// memory: u, D_x and the four planes, against u and three full arrays in the
+// run-time-shape kernel.
+template <typename T, int P, int E>
+struct FmGradR {
+    using S = Stage3R<T, P, E, false>;
+    static constexpr size_t words = (size_t)S::SS + (size_t)S::LS + 4 * (size_t)S::F;
+};
+
+template <typename T, int P, int E>
+__global__ void __launch_bounds__(Stage3R<T, P, E, false>::NT) fm_gradient_r_kernel(FmArgs<T> a, Tab<T, P> tb) {
+    using S = Stage3R<T, P, E, false>;
+    constexpr int N = S::N, F = S::F, NN = S::NN, VW = S::VW;
+    constexpr int SX = S::SX, SXY = S::SXY, LX = S::LX, LXY = S::LXY;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* su = reinterpret_cast<T*>(smem_raw);   // padded u, then D_y (ghost-free layout)
+    T* sx = su + S::SS;                      // D_x, ghost-free layout
+    T* sz = sx + S::LS;                      // D_z on the nodes of faces 0-3, F each
+    const int tid = threadIdx.x, ca = tid % N, cb = tid / N;
+    const int s0 = 1 + SX * (ca + 1) + SXY * cb;   // x-line (x1, x2) = (ca, cb)
+    const int s1 = (ca + 1) + SX + SXY * cb;       // y-line (x0, x2) = (ca, cb)
+    const int s2 = (ca + 1) + SX * (cb + 1);       // z column (x0, x1) = (ca, cb)
+    const int l0 = LX * ca + LXY * cb, l1 = ca + LXY * cb, l2 = ca + LX * cb;
+    const int mode = a.mode;
+    const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1 || mode == MODE_ENERGY) ? a.u : a.y;
+    for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+        const BlockItem& it = a.items[item];
+        const T inv_h = T(1) / T(it.h);
+        const double t = stage_time(a.tinfo, it.problem, mode == MODE_ENERGY ? 0 : mode);
+        const T* yu = ysrc + it.off;
+        if (tid == 0) {
+            prefetch_l2(a.M + (int64_t)item * 6 * NN, 6 * (size_t)NN * sizeof(T));
+            prefetch_l2(a.coef + (int64_t)item * 10 * NN, (size_t)NN * sizeof(T));
+        }
+        T line[N + 2];
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            line[1 + j] = yu[tid + F * j];
+            su[s2 + SXY * j] = line[1 + j];
+        }
+        // this thread's ghosts: faces 0, 1 at its x line, 2, 3 at its y line
+        // (tangential index tid on both), 4, 5 at its column
+        su[s0 - 1] = fm_u_ghost(a, it, 0, tid, F, N, t, yu, N * ca + F * cb);
+        su[s0 + N] = fm_u_ghost(a, it, 1, tid, F, N, t, yu, (N - 1) + N * ca + F * cb);
+        su[s1 - SX] = fm_u_ghost(a, it, 2, tid, F, N, t, yu, ca + F * cb);
+        su[s1 + N * SX] = fm_u_ghost(a, it, 3, tid, F, N, t, yu, ca + N * (N - 1) + F * cb);
+        line[0] = fm_u_ghost(a, it, 4, tid, F, N, t, yu, tid);
+        line[N + 1] = fm_u_ghost(a, it, 5, tid, F, N, t, yu, tid + F * (N - 1));
+        T dz[N];
+        line_full<T, P, E>(tb, line, dz, inv_h);
+        // D_z on the x faces' nodes (0 or N-1, cb, j) and the y faces' (ca, 0 or N-1, j)
+        if (ca == 0 || ca == N - 1) {
+            T* o = sz + (ca == 0 ? 0 : F) + cb;
+#pragma unroll
+            for (int j = 0; j < N; ++j) o[N * j] = dz[j];
+        }
+        if (cb == 0 || cb == N - 1) {
+            T* o = sz + (cb == 0 ? 2 * F : 3 * F) + ca;
+#pragma unroll
+            for (int j = 0; j < N; ++j) o[N * j] = dz[j];
+        }
+        __syncthreads();
+        {
+            // D_x along the x line, 16-byte loads of the contiguous padded row
+            using V = typename V16<T>::type;
+            T xl[N + 2], dx[N];
+#pragma unroll
+            for (int k = 0; k + VW <= N + 2; k += VW) {
+                const V v = *reinterpret_cast<const V*>(su + s0 - 1 + k);
+                const T* e = reinterpret_cast<const T*>(&v);
+#pragma unroll
+                for (int q = 0; q < VW; ++q) xl[k + q] = e[q];
+            }
+#pragma unroll
+            for (int k = (N + 2) / VW * VW; k < N + 2; ++k) xl[k] = su[s0 - 1 + k];
+            line_full<T, P, E>(tb, xl, dx, inv_h);
+            if constexpr (N % VW == 0) {
+#pragma unroll
+                for (int j = 0; j < N; j += VW) {
+                    V v;
+                    T* e = reinterpret_cast<T*>(&v);
+#pragma unroll
+                    for (int q = 0; q < VW; ++q) e[q] = dx[j + q];
+                    *reinterpret_cast<V*>(sx + l0 + j) = v;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < N; ++j) sx[l0 + j] = dx[j];
+            }
+        }
+        T dy[N];
+        {
+            T yl[N + 2];
+#pragma unroll
+            for (int k = 0; k < N + 2; ++k) yl[k] = su[s1 + (k - 1) * SX];
+            line_full<T, P, E>(tb, yl, dy, inv_h);
+        }
+        __syncthreads();   // every line has read u: D_y goes over it
+#pragma unroll
+        for (int j = 0; j < N; ++j) su[l1 + LX * j] = dy[j];
+        __syncthreads();
+        const T* cf = a.coef + (int64_t)item * 10 * NN;
+        T* Vg = a.V + (int64_t)item * 3 * NN;
+        if (mode == MODE_ENERGY) {
+            // V = sum_e S[e] D_e u / (h sqrt(g)) at every node, for the energy
+#pragma unroll 4
+            for (int j = 0; j < N; ++j) {
+                const int n = tid + F * j, l = l2 + LXY * j;
+                const T De[3] = {sx[l], su[l], dz[j]};
+                const T J = cf[n];
+#pragma unroll
+                for (int ci = 0; ci < 3; ++ci) {
+                    T s = T(0);
+#pragma unroll
+                    for (int e = 0; e < 3; ++e) s += cf[(1 + 3 * e + ci) * NN + n] * De[e];
+                    Vg[ci * NN + n] = s / J;
+                }
+            }
+        } else {
+            // the fluxes F^d = sum_e M^de D_e u / h at the column's nodes
+            const T* Mb = a.M + (int64_t)item * 6 * NN;
+#pragma unroll 4
+            for (int j = 0; j < N; ++j) {
+                const int n = tid + F * j, l = l2 + LXY * j;
+                const T De[3] = {sx[l], su[l], dz[j]};
+                T m[6];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) m[k] = Mb[k * NN + n];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    T s = T(0);
+#pragma unroll
+                    for (int e = 0; e < 3; ++e) s += m[sym_index(d, e)] * De[e];
+                    Vg[d * NN + n] = s;
+                }
+            }
+        }
+        // V on the face planes for the neighbours: the x and y faces' nodes at
+        // tangential index tid, and the column's own two z-face nodes
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+            const int side = f & 1;
+            int x0, x1, x2;
+            T dzf;
+            if (f < 2) { x0 = side ? N - 1 : 0; x1 = ca; x2 = cb; dzf = sz[f * F + tid]; }
+            else if (f < 4) { x0 = ca; x1 = side ? N - 1 : 0; x2 = cb; dzf = sz[f * F + tid]; }
+            else { x0 = ca; x1 = cb; x2 = side ? N - 1 : 0; dzf = side ? dz[N - 1] : dz[0]; }
+            const int l = x0 + LX * x1 + LXY * x2, n = x0 + N * x1 + F * x2;
+            const T De[3] = {sx[l], su[l], dzf};
+            const T J = cf[n];
+            T* o = a.fv + (int64_t)(it.slot + f) * 3 * F;
+#pragma unroll
+            for (int ci = 0; ci < 3; ++ci) {
+                T s = T(0);
+#pragma unroll
+                for (int e = 0; e < 3; ++e) s += cf[(1 + 3 * e + ci) * NN + n] * De[e];
+                o[ci * F + tid] = s / J;
             }
         }
         __syncthreads();

@@ -63,6 +63,10 @@ public:
         }
         if constexpr (D == 3) {
             set_attrs(fm_gradient_kernel<T, P>);
+            if constexpr (kShaped) {
+                if constexpr (Stage3R<T, P, 2, false>::usable) set_attrs(fm_gradient_r_kernel<T, P, 2>);
+                if constexpr (Stage3R<T, P, 4, false>::usable) set_attrs(fm_gradient_r_kernel<T, P, 4>);
+            }
             set_attrs(fm_stage_kernel<T, P, COMP>);
             set_attrs(fm_stage_kernel<T, P, COMP, 1>);
             set_attrs(fm_stage_kernel<T, P, COMP, 2>);
@@ -541,10 +545,26 @@ public:
                             cudaStream_t s) const override {
         if constexpr (D != 3) return cudaErrorNotSupported;
         else {
+            const int g = std::min(nitems, kMaxGrid);
+            if constexpr (kShaped) {
+                // the register-line pass for the compile-time shapes
+                if (E == 2 && Stage3R<T, P, 2, false>::usable) {
+                    fm_gradient_r_kernel<T, P, 2><<<g, Stage3R<T, P, 2, false>::NT,
+                                                    FmGradR<T, P, 2>::words * sizeof(T), s>>>(
+                        fm_args(items, nitems, E, mode, 0, p), tb_);
+                    return cudaGetLastError();
+                }
+                if (E == 4 && Stage3R<T, P, 4, false>::usable &&
+                    FmGradR<T, P, 4>::words * sizeof(T) <= (size_t)max_smem_) {
+                    fm_gradient_r_kernel<T, P, 4><<<g, Stage3R<T, P, 4, false>::NT,
+                                                    FmGradR<T, P, 4>::words * sizeof(T), s>>>(
+                        fm_args(items, nitems, E, mode, 0, p), tb_);
+                    return cudaGetLastError();
+                }
+            }
             size_t smem = fm_grad_smem(E);
             if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
-            fm_gradient_kernel<T, P><<<std::min(nitems, kMaxGrid), 256, smem, s>>>(
-                fm_args(items, nitems, E, mode, 0, p), tb_);
+            fm_gradient_kernel<T, P><<<g, 256, smem, s>>>(fm_args(items, nitems, E, mode, 0, p), tb_);
             return cudaGetLastError();
         }
     }
