@@ -134,7 +134,8 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
         // no block and touches no memory
         const bool live = item < a.nitems;
         const BlockItem* it = live ? &a.items[item] : nullptr;
-        T inv_h = T(0);
+        // the two passes differentiate without 1/h; the Laplacian takes 1/h^2
+        T hb = T(0), inv_h2 = T(0);
         uint32_t flags = 0;
         int slot = 0, nb[4] = {0, 0, 0, 0};
         T ug[4], gp[4];
@@ -146,7 +147,9 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
             slot = it->slot;
 #pragma unroll
             for (int f = 0; f < 4; ++f) nb[f] = it->nb[f];
-            inv_h = T(1) / T(it->h);
+            hb = T(it->h);
+            const T inv_h = T(1) / hb;
+            inv_h2 = inv_h * inv_h;
             const T* yu = ysrc + it->off;
             T line[N + 2];
             if (mode == 2) {
@@ -177,11 +180,11 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
             line[N + 1] = ug[3];
             // ---- y: the column in registers
             T g[N + 2], gi[N], lap[N];
-            line_full<T, P, E>(tb, line, gi, inv_h);
+            line_full<T, P, E>(tb, line, gi, T(1));
 #pragma unroll
             for (int j = 0; j < N; ++j) g[1 + j] = gi[j];
-            g[0] = grad_ghost<T, P>(tb, flags, nb[2], 2, gp[2], line[1], inv_h);
-            g[N + 1] = grad_ghost<T, P>(tb, flags, nb[3], 3, gp[3], line[N], inv_h);
+            g[0] = grad_ghost_raw<T, P>(tb, flags, nb[2], 2, gp[2], line[1], hb);
+            g[N + 1] = grad_ghost_raw<T, P>(tb, flags, nb[3], 3, gp[3], line[N], hb);
             line_full<T, P, E>(tb, g, lap, T(1));
 #pragma unroll
             for (int j = 0; j < N; ++j) sl[j * LX + c] = lap[j];
@@ -193,11 +196,11 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
             row_load<T, NU>(su + c * SX, row);
 #pragma unroll
             for (int k = 0; k < N + 2; ++k) line[k] = row[k];
-            line_full<T, P, E>(tb, line, gi, inv_h);
+            line_full<T, P, E>(tb, line, gi, T(1));
 #pragma unroll
             for (int j = 0; j < N; ++j) g[1 + j] = gi[j];
-            g[0] = grad_ghost<T, P>(tb, flags, nb[0], 0, gp[0], line[1], inv_h);
-            g[N + 1] = grad_ghost<T, P>(tb, flags, nb[1], 1, gp[1], line[N], inv_h);
+            g[0] = grad_ghost_raw<T, P>(tb, flags, nb[0], 0, gp[0], line[1], hb);
+            g[N + 1] = grad_ghost_raw<T, P>(tb, flags, nb[1], 1, gp[1], line[N], hb);
             line_full<T, P, E>(tb, g, lap, T(1));
             T acc_row[NL * VW];
             row_load<T, NL>(sl + c * LX, acc_row);
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
 #pragma unroll
                 for (int j = 0; j < N; ++j) {
                     du[c + N * j] = yv[c + N * j];
-                    du[NN + c + N * j] = sl[j * LX + c] * inv_h;
+                    du[NN + c + N * j] = sl[j * LX + c] * inv_h2;
                 }
             }
             __syncthreads();
@@ -269,10 +272,10 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
                     if (mode == MODE_STAGE1) {
                         // Y2's u for the face export; the v-rate, truncated below and stored
                         o_u[0] = uuq[0] + rc.cn * yq[0];
-                        o_v[0] = lap[0] * inv_h;
+                        o_v[0] = lap[0] * inv_h2;
                         o_c[0] = T(0);
                     } else {
-                        stage_points<T, COMP, 1>(mode, rc, yq, uuq, uvq, auq, avq, cuq, cviq, lap, inv_h, o_u,
+                        stage_points<T, COMP, 1>(mode, rc, yq, uuq, uvq, auq, avq, cuq, cviq, lap, inv_h2, o_u,
                                                  o_v, o_c);
                     }
                     au[q] = auq[0];

@@ -116,22 +116,12 @@ __device__ __forceinline__ void line_full(const Tab<T, P>& tb, const T (&in)[E *
     }
 }
 
-// The gradient ghost of face f at this thread's face point, from the value
-// prefetched for it: the dense coarse-fine plane's, or the neighbour's own
-// part `pre` plus its ghost coefficient times its u ghost, which is this
-// block's own face node `own`.
-template <typename T, int P>
-__device__ __forceinline__ T grad_ghost(const Tab<T, P>& tb, uint32_t flags, int nslot, int f, T pre, T own,
-                                        T inv_h) {
-    if (flags & (1u << f)) return pre;
-    const T gnb = (pre + ghost_coef<T, P>(tb, nslot & 1) * own) * inv_h;
-    return (flags & (1u << (8 + f))) ? -gnb : gnb;
-}
-
-// The same ghost times h: the register-line 3D kernel differentiates u and
-// then its gradient without the two 1/h factors, and scales the Laplacian by
-// 1/h^2 once; a coarse-fine ghost (a plane of gradient values) takes the
-// factor h itself.
+// The gradient ghost of face f at this thread's face point times h, from the
+// value prefetched for it: the neighbour's own part `pre` plus its ghost
+// coefficient times its u ghost, which is this block's own face node `own`
+// (negated across a wall), or a coarse-fine face's plane of gradient values
+// times h. The register-line kernels differentiate u and then its gradient
+// without the two 1/h factors and scale the Laplacian by 1/h^2 once.
 template <typename T, int P>
 __device__ __forceinline__ T grad_ghost_raw(const Tab<T, P>& tb, uint32_t flags, int nslot, int f, T pre, T own,
                                             T h) {
