@@ -602,6 +602,57 @@ __device__ __forceinline__ void stage_legendre(const FmTab<T, P>& ft, T* L) {
 
 // FM: the stage the instantiation runs (1-4), so that each stage's code holds
 // only its own data flow, or 0 for the mode in the arguments.
+// The flux F^d = S[d] . V beyond face f (normal d, side) at its face node tt,
+// with this face node's own S[d] (node `o` of the block): the neighbour's
+// exported V, oriented across a glue; a coarse-fine face's plane; the
+// caller's Dirichlet gradient; the plane wave's gradient at the boundary face
+// node; or on the radiative sphere 2 F* - F, so that the central flux through
+// the face is F* = -sigma |S[d]| (kappa v + u / R) (src/evolution.jl:1232-1260).
+template <typename T>
+__device__ __forceinline__ T fm_flux_ghost(const FmArgs<T>& a, const BlockItem& it, int f, int d, int side, int tt,
+                                           int o, int F, int N, int NN, double t, const T* cf, const T* Fb,
+                                           const T* ysrc) {
+    if (it.nb[f] < 0 && !(it.flags & (1u << f)) && a.boundary == 1) {
+        const T Fo = Fb[d * NN + o];
+        T S2 = T(0);
+#pragma unroll
+        for (int ci = 0; ci < 3; ++ci) {
+            const T Sc = cf[(1 + 3 * d + ci) * NN + o];
+            S2 += Sc * Sc;
+        }
+        const T* yo = ysrc + it.off;
+        const T sigma = side ? T(1) : T(-1);
+        const T Fstar = -sigma * sqrt(S2) * (a.kappa * yo[NN + o] + a.inv_r * yo[o]);
+        return T(2) * Fstar - Fo;
+    }
+    T Vg[3];
+    if (it.flags & (1u << f)) {
+        const T* src = a.vgd + (int64_t)(it.slot + f) * 3 * F;
+#pragma unroll
+        for (int ci = 0; ci < 3; ++ci) Vg[ci] = src[ci * F + tt];
+    } else if (it.nb[f] < 0 && a.boundary == 2) {
+        const double* bv = boundary_values(a, it.slot + f, t, F);
+#pragma unroll
+        for (int ci = 0; ci < 3; ++ci) Vg[ci] = (T)bv[(1 + ci) * F + tt];
+    } else if (it.nb[f] < 0) {
+        const double* X = a.bnd_x + (int64_t)(it.slot + f) * 3 * F;
+        const double th = a.wave.k[0] * X[tt] + a.wave.k[1] * X[F + tt] + a.wave.k[2] * X[2 * F + tt] -
+                          a.wave.omega * t + a.wave.phi;
+        const double c = cos(th);
+#pragma unroll
+        for (int ci = 0; ci < 3; ++ci) Vg[ci] = (T)(a.wave.k[ci] * c);
+    } else {
+        const T* src = a.fv + (int64_t)it.nb[f] * 3 * F;
+        const int t2 = oriented(tt, N, face_orient(it, f));
+#pragma unroll
+        for (int ci = 0; ci < 3; ++ci) Vg[ci] = src[ci * F + t2];
+    }
+    T Fg = T(0);
+#pragma unroll
+    for (int ci = 0; ci < 3; ++ci) Fg += cf[(1 + 3 * d + ci) * NN + o] * Vg[ci];
+    return Fg;
+}
+
 template <typename T, int P, bool COMP, int FM = 0>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 4) fm_stage_kernel(FmArgs<T> a, Tab<T, P> tb, FmTab<T, P> ft) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -658,49 +709,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 4) fm_stage_kernel(F
                 plane_coords<3>(g, d, tt, side == 0 ? 0 : g.N - 1, xo);
                 plane_coords<3>(g, d, tt, side == 0 ? -1 : g.N, xg);
                 const int o = oidx<3>(g, xo);
-                if (it.nb[f] < 0 && !(it.flags & (1u << f)) && a.boundary == 1) {
-                    // radiative: the ghost's flux 2 F* - F, so that the central
-                    // flux through the face is F* = -sigma |S[d]| (kappa v + u / R)
-                    // (src/evolution.jl:1232-1260)
-                    const T F = Fb[d * g.NN + o];
-                    T S2 = T(0);
-#pragma unroll
-                    for (int ci = 0; ci < 3; ++ci) {
-                        const T Sc = cf[(1 + 3 * d + ci) * g.NN + o];
-                        S2 += Sc * Sc;
-                    }
-                    const T* yo = ysrc + it.off;
-                    const T sigma = side ? T(1) : T(-1);
-                    const T Fstar = -sigma * sqrt(S2) * (a.kappa * yo[g.NN + o] + a.inv_r * yo[o]);
-                    sF[sidx<3>(g, xg)] = T(2) * Fstar - F;
-                    continue;
-                }
-                T Vg[3];
-                if (it.flags & (1u << f)) {
-                    const T* src = a.vgd + (int64_t)(it.slot + f) * 3 * g.F;
-#pragma unroll
-                    for (int ci = 0; ci < 3; ++ci) Vg[ci] = src[ci * g.F + tt];
-                } else if (it.nb[f] < 0 && a.boundary == 2) {
-                    const double* bv = boundary_values(a, it.slot + f, t, g.F);
-#pragma unroll
-                    for (int ci = 0; ci < 3; ++ci) Vg[ci] = (T)bv[(1 + ci) * g.F + tt];
-                } else if (it.nb[f] < 0) {
-                    const double* X = a.bnd_x + (int64_t)(it.slot + f) * 3 * g.F;
-                    const double th = a.wave.k[0] * X[tt] + a.wave.k[1] * X[g.F + tt] +
-                                      a.wave.k[2] * X[2 * g.F + tt] - a.wave.omega * t + a.wave.phi;
-                    const double c = cos(th);
-#pragma unroll
-                    for (int ci = 0; ci < 3; ++ci) Vg[ci] = (T)(a.wave.k[ci] * c);
-                } else {
-                    const T* src = a.fv + (int64_t)it.nb[f] * 3 * g.F;
-                    const int t2 = oriented(tt, g.N, face_orient(it, f));
-#pragma unroll
-                    for (int ci = 0; ci < 3; ++ci) Vg[ci] = src[ci * g.F + t2];
-                }
-                T F = T(0);
-#pragma unroll
-                for (int ci = 0; ci < 3; ++ci) F += cf[(1 + 3 * d + ci) * g.NN + o] * Vg[ci];
-                sF[sidx<3>(g, xg)] = F;
+                sF[sidx<3>(g, xg)] = fm_flux_ghost(a, it, f, d, side, tt, o, g.F, g.N, g.NN, t, cf, Fb, ysrc);
             }
             __syncthreads();
             for (int L = threadIdx.x; L < g.E * g.F; L += blockDim.x) {
@@ -775,6 +784,18 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 4) fm_stage_kernel(F
         __syncthreads();
     }
 }
+
+// The stage pass with a compile-time block shape (E = 2 or 4) in the
+// register-line layout (fmstage_r.cuh), instantiated per order in a
+// translation unit of its own (kernels_d3_p<P>_fm.cu): its shared-memory
+// attributes, its shared memory in bytes, and a launch of RK stage `mode`.
+template <typename T, int P, int E, bool COMP>
+void fm_stage_r_attrs(int max_smem);
+template <typename T, int P, int E, bool COMP>
+size_t fm_stage_r_smem();
+template <typename T, int P, int E, bool COMP>
+cudaError_t fm_stage_r_launch(const FmArgs<T>& a, const Tab<T, P>& tb, const FmTab<T, P>& ft, int grid, int mode,
+                              cudaStream_t s);
 
 // The standalone truncation of the full metric (twoldg_truncate).
 template <typename T, int P>

@@ -1,0 +1,8 @@
+// The full-metric stage pass with a compile-time block shape for D = 3, P = 1.
+#include "fmstage_r.cuh"
+
+namespace twoldg {
+
+TWOLDG_FMSTAGE_R(1)
+
+}  // namespace twoldg

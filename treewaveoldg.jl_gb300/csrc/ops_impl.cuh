@@ -66,6 +66,8 @@ public:
             if constexpr (kShaped) {
                 if constexpr (Stage3R<T, P, 2, false>::usable) set_attrs(fm_gradient_r_kernel<T, P, 2>);
                 if constexpr (Stage3R<T, P, 4, false>::usable) set_attrs(fm_gradient_r_kernel<T, P, 4>);
+                fm_stage_r_attrs<T, P, 2, COMP>(max_smem_);
+                fm_stage_r_attrs<T, P, 4, COMP>(max_smem_);
             }
             set_attrs(fm_stage_kernel<T, P, COMP>);
             set_attrs(fm_stage_kernel<T, P, COMP, 1>);
@@ -576,6 +578,17 @@ public:
             if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
             const int g = std::min(nitems, kMaxGrid);
             const FmArgs<T> fa = fm_args(items, nitems, E, mode, truncate, p);
+            if constexpr (kShaped) {
+                // the register-line pass for the compile-time shapes' RK stages
+                if (mode >= MODE_STAGE1 && mode <= MODE_STAGE4) {
+                    if (E == 2 && Stage3R<T, P, 2, false>::usable &&
+                        fm_stage_r_smem<T, P, 2, COMP>() <= (size_t)max_smem_)
+                        return fm_stage_r_launch<T, P, 2, COMP>(fa, tb_, ft_, g, mode, s);
+                    if (E == 4 && Stage3R<T, P, 4, false>::usable &&
+                        fm_stage_r_smem<T, P, 4, COMP>() <= (size_t)max_smem_)
+                        return fm_stage_r_launch<T, P, 4, COMP>(fa, tb_, ft_, g, mode, s);
+                }
+            }
             // one instantiation per stage
             if (mode == MODE_STAGE1) fm_stage_kernel<T, P, COMP, 1><<<g, 256, smem, s>>>(fa, tb_, ft_);
             else if (mode == 2) fm_stage_kernel<T, P, COMP, 2><<<g, 256, smem, s>>>(fa, tb_, ft_);
