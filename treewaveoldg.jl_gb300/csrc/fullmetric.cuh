@@ -449,18 +449,54 @@ __device__ __forceinline__ void fm_project_block(const G& g, const FmArgs<T>& a,
         cbuf[i] = c;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < EE; e += blockDim.x) {
+    if (EE <= (int)blockDim.x) {
+        // the triangular solves by every thread of the CTA: G threads an
+        // element, column by column, one barrier a column. At column q each
+        // of an element's threads forms the unknown from its settled
+        // right-hand side and subtracts its column from its own share of the
+        // rows still open; the unknown is stored one column later, when no
+        // thread reads that row any more.
+        const int G = blockDim.x / EE;
+        const int e = threadIdx.x % EE, gl = threadIdx.x / EE;
+        const bool act = gl < G;
         T* c = cbuf + e * m3;
         const T* Ue = U + (int64_t)e * m3 * m3;   // column-major: U[r][q] at r + m3 q
+        T prev = T(0);
         for (int q = 0; q < m3; ++q) {            // U^T y = c
-            T s = c[q];
-            for (int r = 0; r < q; ++r) s -= Ue[r + m3 * q] * c[r];
-            c[q] = s / Ue[q + m3 * q];
+            if (act) {
+                const T y = c[q] / Ue[q + m3 * q];
+                if (q > 0 && gl == (q - 1) % G) c[q - 1] = prev;
+                for (int r = q + 1 + gl; r < m3; r += G) c[r] -= Ue[q + m3 * r] * y;
+                prev = y;
+            }
+            __syncthreads();
         }
+        if (act && gl == (m3 - 1) % G) c[m3 - 1] = prev;
+        __syncthreads();
         for (int q = m3 - 1; q >= 0; --q) {       // U z = y
-            T s = c[q];
-            for (int r = q + 1; r < m3; ++r) s -= Ue[q + m3 * r] * c[r];
-            c[q] = s / Ue[q + m3 * q];
+            if (act) {
+                const T z = c[q] / Ue[q + m3 * q];
+                if (q < m3 - 1 && gl == (q + 1) % G) c[q + 1] = prev;
+                for (int r = gl; r < q; r += G) c[r] -= Ue[r + m3 * q] * z;
+                prev = z;
+            }
+            __syncthreads();
+        }
+        if (act && gl == 0) c[0] = prev;
+    } else {
+        for (int e = threadIdx.x; e < EE; e += blockDim.x) {
+            T* c = cbuf + e * m3;
+            const T* Ue = U + (int64_t)e * m3 * m3;   // column-major: U[r][q] at r + m3 q
+            for (int q = 0; q < m3; ++q) {            // U^T y = c
+                T s = c[q];
+                for (int r = 0; r < q; ++r) s -= Ue[r + m3 * q] * c[r];
+                c[q] = s / Ue[q + m3 * q];
+            }
+            for (int q = m3 - 1; q >= 0; --q) {       // U z = y
+                T s = c[q];
+                for (int r = q + 1; r < m3; ++r) s -= Ue[q + m3 * r] * c[r];
+                c[q] = s / Ue[q + m3 * q];
+            }
         }
     }
     __syncthreads();
