@@ -436,48 +436,87 @@ __device__ __forceinline__ void fm_project_block(const G& g, const FmArgs<T>& a,
     const int EE = g.E * g.E * g.E;
     const T* W = a.ew + (int64_t)slot * n3 * EE;
     const T* U = a.echol + (int64_t)slot * m3 * m3 * EE;
-    for (int i = threadIdx.x; i < EE * m3; i += blockDim.x) {
-        const int e = i / m3, q = i % m3;
-        const int q0 = q % P, q1 = (q / P) % P, q2 = q / (P * P);
-        const int e0 = e % g.E, e1 = (e / g.E) % g.E, e2 = e / (g.E * g.E);
-        T c = T(0);
-        for (int nn = 0; nn < n3; ++nn) {
-            const int n0 = nn % P1, n1 = (nn / P1) % P1, n2 = nn / (P1 * P1);
-            const int x[3] = {e0 * P1 + n0, e1 * P1 + n1, e2 * P1 + n2};
-            c += L[q0 * P1 + n0] * L[q1 * P1 + n1] * L[q2 * P1 + n2] * W[(int64_t)e * n3 + nn] * sv[lidx<3>(g, x)];
+    // The element's node at (n0, n1, n2) in the ghost-free layout.
+    auto at = [&](int e, int n0, int n1, int n2) {
+        const int x[3] = {(e % g.E) * P1 + n0, ((e / g.E) % g.E) * P1 + n1, (e / (g.E * g.E)) * P1 + n2};
+        return lidx<3>(g, x);
+    };
+    // c = Psi^T W v with Psi = L x L x L, one dimension at a time (sum
+    // factorisation): each pass's thread owns one element line, reads its
+    // P+1 values and writes its P results over the first P of them, so that
+    // the passes work in place in the element's nodes; the last pass writes c.
+    for (int i = threadIdx.x; i < EE * P1 * P1; i += blockDim.x) {     // along n0: (q0, n1, n2)
+        const int e = i / (P1 * P1), n1 = i % P1, n2 = (i / P1) % P1;
+        T t[P1];
+#pragma unroll
+        for (int n0 = 0; n0 < P1; ++n0)
+            t[n0] = W[(int64_t)e * n3 + n0 + P1 * (n1 + P1 * n2)] * sv[at(e, n0, n1, n2)];
+#pragma unroll
+        for (int q0 = 0; q0 < P; ++q0) {
+            T c = T(0);
+#pragma unroll
+            for (int n0 = 0; n0 < P1; ++n0) c += L[q0 * P1 + n0] * t[n0];
+            sv[at(e, q0, n1, n2)] = c;
         }
-        cbuf[i] = c;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < EE * P * P1; i += blockDim.x) {      // along n1: (q0, q1, n2)
+        const int e = i / (P * P1), q0 = i % P, n2 = (i / P) % P1;
+        T t[P1];
+#pragma unroll
+        for (int n1 = 0; n1 < P1; ++n1) t[n1] = sv[at(e, q0, n1, n2)];
+#pragma unroll
+        for (int q1 = 0; q1 < P; ++q1) {
+            T c = T(0);
+#pragma unroll
+            for (int n1 = 0; n1 < P1; ++n1) c += L[q1 * P1 + n1] * t[n1];
+            sv[at(e, q0, q1, n2)] = c;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < EE * P * P; i += blockDim.x) {       // along n2: (q0, q1, q2)
+        const int e = i / (P * P), q0 = i % P, q1 = (i / P) % P;
+        T t[P1];
+#pragma unroll
+        for (int n2 = 0; n2 < P1; ++n2) t[n2] = sv[at(e, q0, q1, n2)];
+#pragma unroll
+        for (int q2 = 0; q2 < P; ++q2) {
+            T c = T(0);
+#pragma unroll
+            for (int n2 = 0; n2 < P1; ++n2) c += L[q2 * P1 + n2] * t[n2];
+            cbuf[e * m3 + q0 + P * (q1 + P * q2)] = c;
+        }
     }
     __syncthreads();
     if (EE <= (int)blockDim.x) {
-        // the triangular solves by every thread of the CTA: G threads an
+        // the triangular solves by every thread of the CTA: NG threads an
         // element, column by column, one barrier a column. At column q each
         // of an element's threads forms the unknown from its settled
         // right-hand side and subtracts its column from its own share of the
         // rows still open; the unknown is stored one column later, when no
         // thread reads that row any more.
-        const int G = blockDim.x / EE;
+        const int NG = blockDim.x / EE;
         const int e = threadIdx.x % EE, gl = threadIdx.x / EE;
-        const bool act = gl < G;
+        const bool act = gl < NG;
         T* c = cbuf + e * m3;
         const T* Ue = U + (int64_t)e * m3 * m3;   // column-major: U[r][q] at r + m3 q
         T prev = T(0);
         for (int q = 0; q < m3; ++q) {            // U^T y = c
             if (act) {
                 const T y = c[q] / Ue[q + m3 * q];
-                if (q > 0 && gl == (q - 1) % G) c[q - 1] = prev;
-                for (int r = q + 1 + gl; r < m3; r += G) c[r] -= Ue[q + m3 * r] * y;
+                if (q > 0 && gl == (q - 1) % NG) c[q - 1] = prev;
+                for (int r = q + 1 + gl; r < m3; r += NG) c[r] -= Ue[q + m3 * r] * y;
                 prev = y;
             }
             __syncthreads();
         }
-        if (act && gl == (m3 - 1) % G) c[m3 - 1] = prev;
+        if (act && gl == (m3 - 1) % NG) c[m3 - 1] = prev;
         __syncthreads();
         for (int q = m3 - 1; q >= 0; --q) {       // U z = y
             if (act) {
                 const T z = c[q] / Ue[q + m3 * q];
-                if (q < m3 - 1 && gl == (q + 1) % G) c[q + 1] = prev;
-                for (int r = gl; r < q; r += G) c[r] -= Ue[r + m3 * q] * z;
+                if (q < m3 - 1 && gl == (q + 1) % NG) c[q + 1] = prev;
+                for (int r = gl; r < q; r += NG) c[r] -= Ue[r + m3 * q] * z;
                 prev = z;
             }
             __syncthreads();
@@ -500,18 +539,49 @@ __device__ __forceinline__ void fm_project_block(const G& g, const FmArgs<T>& a,
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < EE * n3; i += blockDim.x) {
-        const int e = i / n3, nn = i % n3;
-        const int n0 = nn % P1, n1 = (nn / P1) % P1, n2 = nn / (P1 * P1);
-        const int e0 = e % g.E, e1 = (e / g.E) % g.E, e2 = e / (g.E * g.E);
-        const T* c = cbuf + e * m3;
-        T z = T(0);
-        for (int q = 0; q < m3; ++q) {
-            const int q0 = q % P, q1 = (q / P) % P, q2 = q / (P * P);
-            z += L[q0 * P1 + n0] * L[q1 * P1 + n1] * L[q2 * P1 + n2] * c[q];
+    // v = Psi z, the same passes backwards: from c along q2 into the
+    // element's nodes (q0, q1, n2), then along q1 and q0, each line's thread
+    // reading its P values before it writes its P+1
+    for (int i = threadIdx.x; i < EE * P * P; i += blockDim.x) {       // along q2: (q0, q1, n2)
+        const int e = i / (P * P), q0 = i % P, q1 = (i / P) % P;
+        T t[P];
+#pragma unroll
+        for (int q2 = 0; q2 < P; ++q2) t[q2] = cbuf[e * m3 + q0 + P * (q1 + P * q2)];
+#pragma unroll
+        for (int n2 = 0; n2 < P1; ++n2) {
+            T z = T(0);
+#pragma unroll
+            for (int q2 = 0; q2 < P; ++q2) z += L[q2 * P1 + n2] * t[q2];
+            sv[at(e, q0, q1, n2)] = z;
         }
-        const int x[3] = {e0 * P1 + n0, e1 * P1 + n1, e2 * P1 + n2};
-        sv[lidx<3>(g, x)] = z;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < EE * P * P1; i += blockDim.x) {      // along q1: (q0, n1, n2)
+        const int e = i / (P * P1), q0 = i % P, n2 = (i / P) % P1;
+        T t[P];
+#pragma unroll
+        for (int q1 = 0; q1 < P; ++q1) t[q1] = sv[at(e, q0, q1, n2)];
+#pragma unroll
+        for (int n1 = 0; n1 < P1; ++n1) {
+            T z = T(0);
+#pragma unroll
+            for (int q1 = 0; q1 < P; ++q1) z += L[q1 * P1 + n1] * t[q1];
+            sv[at(e, q0, n1, n2)] = z;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < EE * P1 * P1; i += blockDim.x) {     // along q0: (n0, n1, n2)
+        const int e = i / (P1 * P1), n1 = i % P1, n2 = (i / P1) % P1;
+        T t[P];
+#pragma unroll
+        for (int q0 = 0; q0 < P; ++q0) t[q0] = sv[at(e, q0, n1, n2)];
+#pragma unroll
+        for (int n0 = 0; n0 < P1; ++n0) {
+            T z = T(0);
+#pragma unroll
+            for (int q0 = 0; q0 < P; ++q0) z += L[q0 * P1 + n0] * t[q0];
+            sv[at(e, n0, n1, n2)] = z;
+        }
     }
     __syncthreads();
 }
@@ -521,7 +591,6 @@ __device__ __forceinline__ void fm_project_block(const G& g, const FmArgs<T>& a,
 // an element's P+1 planes across k the 2D sqrt(g)-orthogonal projection with
 // the angular tables: c = Psi^T W v, U^T y = c, U z = y, v = Psi z. The two
 // act on different indices and their product is the projection onto Q_{P-1}.
-// cbuf holds (P+1) P^2 coefficients per element.
 // The node of an element with index jk along dimension k and (ja, jb) along
 // the two others in increasing order, as an index into the ghost-free
 // layout; selects only, so that nothing indexes a local array at run time.
@@ -560,51 +629,79 @@ __device__ __forceinline__ void fm_project_factored(const G& g, const FmArgs<T>&
         for (int j = 0; j < P1; ++j) sv[l0 + j * ls] = v[j] - rm[j] * c;
     }
     __syncthreads();
-    // across k, plane by plane: c = Psi^T W v
-    for (int i = threadIdx.x; i < EE * P1 * m2; i += blockDim.x) {
-        const int q = i % m2, j = (i / m2) % P1, e = i / (m2 * P1);
+    // across k, plane by plane, one thread a plane of an element: c = Psi^T W v
+    // with Psi = L x L summed one dimension at a time, the Cholesky solves
+    // U^T y = c, U z = y, and v = Psi z back the same way, all in registers;
+    // the planes are disjoint, so no barrier separates the steps
+    for (int u = threadIdx.x; u < EE * P1; u += blockDim.x) {
+        const int e = u / P1, j = u % P1;
         const int e0 = e % E, e1 = (e / E) % E, e2 = e / E2;
         const int ek = pick3(k, e0, e1, e2), ea = pick3(d0, e0, e1, e2), eb = pick3(d1, e0, e1, e2);
         const T* W = a.faw + ((int64_t)A * E2 + ea + E * eb) * n2;
-        const int q0 = q % P, q1 = q / P;
-        T c = T(0);
+        const T* U = a.fachol + ((int64_t)A * E2 + ea + E * eb) * m2 * m2;   // U[r][q] at r + m2 q
+        T t[P1][P1];
 #pragma unroll
         for (int nb = 0; nb < P1; ++nb)
 #pragma unroll
             for (int na = 0; na < P1; ++na)
-                c += L[q0 * P1 + na] * L[q1 * P1 + nb] * W[na + P1 * nb] *
-                     sv[node_across(g, k, ek * P1 + j, ea * P1 + na, eb * P1 + nb)];
-        cbuf[i] = c;
-    }
-    __syncthreads();
-    for (int u = threadIdx.x; u < EE * P1; u += blockDim.x) {
-        const int e = u / P1;
-        const int e0 = e % E, e1 = (e / E) % E, e2 = e / E2;
-        const int ea = pick3(d0, e0, e1, e2), eb = pick3(d1, e0, e1, e2);
-        T* c = cbuf + u * m2;
-        const T* U = a.fachol + ((int64_t)A * E2 + ea + E * eb) * m2 * m2;   // U[r][q] at r + m2 q
+                t[nb][na] = W[na + P1 * nb] * sv[node_across(g, k, ek * P1 + j, ea * P1 + na, eb * P1 + nb)];
+        T c[m2];
+        {
+            T A0[P1][P];   // A0[nb][q0] = sum_na L_q0(na) t[nb][na]
+#pragma unroll
+            for (int nb = 0; nb < P1; ++nb)
+#pragma unroll
+                for (int q0 = 0; q0 < P; ++q0) {
+                    T s = T(0);
+#pragma unroll
+                    for (int na = 0; na < P1; ++na) s += L[q0 * P1 + na] * t[nb][na];
+                    A0[nb][q0] = s;
+                }
+#pragma unroll
+            for (int q1 = 0; q1 < P; ++q1)
+#pragma unroll
+                for (int q0 = 0; q0 < P; ++q0) {
+                    T s = T(0);
+#pragma unroll
+                    for (int nb = 0; nb < P1; ++nb) s += L[q1 * P1 + nb] * A0[nb][q0];
+                    c[q0 + P * q1] = s;
+                }
+        }
+#pragma unroll
         for (int q = 0; q < m2; ++q) {            // U^T y = c
             T s = c[q];
+#pragma unroll
             for (int r = 0; r < q; ++r) s -= U[r + m2 * q] * c[r];
             c[q] = s / U[q + m2 * q];
         }
+#pragma unroll
         for (int q = m2 - 1; q >= 0; --q) {       // U z = y
             T s = c[q];
+#pragma unroll
             for (int r = q + 1; r < m2; ++r) s -= U[q + m2 * r] * c[r];
             c[q] = s / U[q + m2 * q];
         }
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < EE * P1 * n2; i += blockDim.x) {
-        const int nn = i % n2, j = (i / n2) % P1, e = i / (n2 * P1);
-        const int e0 = e % E, e1 = (e / E) % E, e2 = e / E2;
-        const int ek = pick3(k, e0, e1, e2), ea = pick3(d0, e0, e1, e2), eb = pick3(d1, e0, e1, e2);
-        const int na = nn % P1, nb = nn / P1;
-        const T* c = cbuf + (e * P1 + j) * m2;
-        T z = T(0);
+        {
+            T B0[P1][P];   // B0[nb][q0] = sum_q1 L_q1(nb) z[q0 + P q1]
 #pragma unroll
-        for (int q = 0; q < m2; ++q) z += L[(q % P) * P1 + na] * L[(q / P) * P1 + nb] * c[q];
-        sv[node_across(g, k, ek * P1 + j, ea * P1 + na, eb * P1 + nb)] = z;
+            for (int nb = 0; nb < P1; ++nb)
+#pragma unroll
+                for (int q0 = 0; q0 < P; ++q0) {
+                    T s = T(0);
+#pragma unroll
+                    for (int q1 = 0; q1 < P; ++q1) s += L[q1 * P1 + nb] * c[q0 + P * q1];
+                    B0[nb][q0] = s;
+                }
+#pragma unroll
+            for (int nb = 0; nb < P1; ++nb)
+#pragma unroll
+                for (int na = 0; na < P1; ++na) {
+                    T z = T(0);
+#pragma unroll
+                    for (int q0 = 0; q0 < P; ++q0) z += L[q0 * P1 + na] * B0[nb][q0];
+                    sv[node_across(g, k, ek * P1 + j, ea * P1 + na, eb * P1 + nb)] = z;
+                }
+        }
     }
     __syncthreads();
 }
