@@ -150,11 +150,12 @@ struct twoldg_runner {
         cudaGraphExec_t exec;
     };
     std::vector<StepGraph> graphs;
-    // A batch of several shape groups takes up to kChunk steps a graph
-    // launch (a call's remainder in a graph of its own): each group's chain of
-    // stages runs through them without waiting for the other groups at every
-    // step, so that a group that finishes a step early starts its next one
-    // instead of idling until the slowest group is done.
+    // A call takes up to kChunk steps a graph launch (its remainder in a
+    // graph of its own): the steps follow one another without a gap between
+    // graph launches, and in a batch of several shape groups each group's
+    // chain of stages runs through them without waiting for the other groups
+    // at every step, so that a group that finishes a step early starts its
+    // next one instead of idling until the slowest group is done.
     static constexpr int kChunk = 16;
     void* comp_u = nullptr;
     // Shape groups of a batch never exchange data, so each group's four
@@ -671,23 +672,28 @@ struct twoldg_runner {
     // group 0 on `stream`, every other group on its side stream between a
     // fork and a join, so that the graph runs the groups' chains side by
     // side; groups never exchange data, so each chain takes all its steps
-    // before the join. The full metric's time advance follows the join, so
-    // its problems take one step a graph.
+    // before the join. The full metric's boundary reads the problems' time,
+    // advanced on the device after every step: its steps each take a fork,
+    // the groups' four stages and a join before the advance.
     int enqueue_step(void* u, int steps = 1) {
-        if (groups.size() > 1) CK(cudaEventRecord(fork, stream));
-        for (size_t i = 0; i < groups.size(); ++i) {
-            cudaStream_t st = i == 0 ? stream : side[i - 1];
-            if (i > 0) CK(cudaStreamWaitEvent(st, fork, 0));
-            for (int k = 0; k < steps; ++k) {
-                int r = enqueue_group(*groups[i], u, st);
-                if (r) return r;
+        const bool full = any_full();
+        for (int k0 = 0; k0 < steps; k0 += full ? 1 : steps) {
+            const int n = full ? 1 : steps;
+            if (groups.size() > 1) CK(cudaEventRecord(fork, stream));
+            for (size_t i = 0; i < groups.size(); ++i) {
+                cudaStream_t st = i == 0 ? stream : side[i - 1];
+                if (i > 0) CK(cudaStreamWaitEvent(st, fork, 0));
+                for (int k = 0; k < n; ++k) {
+                    int r = enqueue_group(*groups[i], u, st);
+                    if (r) return r;
+                }
+                if (i > 0) CK(cudaEventRecord(join[i - 1], st));
             }
-            if (i > 0) CK(cudaEventRecord(join[i - 1], st));
-        }
-        for (size_t i = 1; i < groups.size(); ++i) CK(cudaStreamWaitEvent(stream, join[i - 1], 0));
-        if (any_full()) {
-            fm_advance_time(stream);
-            CK(cudaGetLastError());
+            for (size_t i = 1; i < groups.size(); ++i) CK(cudaStreamWaitEvent(stream, join[i - 1], 0));
+            if (full) {
+                fm_advance_time(stream);
+                CK(cudaGetLastError());
+            }
         }
         return TWOLDG_OK;
     }
@@ -841,7 +847,7 @@ struct twoldg_runner {
         int r = export_all(u);
         if (!r) r = prime_cf();
         if (r) return r;
-        const int chunk = (groups.size() > 1 && !any_full()) ? std::min(nsteps, kChunk) : 1;
+        const int chunk = std::min(nsteps, kChunk);
         cudaGraphExec_t gexec = nullptr;
         r = step_graph(u, chunk, &gexec);
         if (r) return r;
