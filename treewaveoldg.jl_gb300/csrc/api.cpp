@@ -507,6 +507,11 @@ struct twoldg_runner {
     // cf_all fills).
     StagePtrs stage_ptrs(Group& g, void* u, int in) {
         StagePtrs p = ptrs(g, u, in);
+        // one group's chain of stages: each stage kernel may become resident
+        // while the one before finishes. The groups of a batch run their
+        // chains side by side, where a stage waiting on its SMs would hold
+        // them from another group's running stage.
+        p.pdl = groups.size() == 1;
         if (!g.cf.empty()) {
             p.cf = (const CfFace*)g.d_cf.p;
             p.cfidx = (const int*)g.d_cfidx.p;

@@ -42,6 +42,9 @@ struct StagePtrs {
     void* ugd_out;
     void* ggd_out;
     void* gsd_out;
+    // the register-line stage kernels as programmatic dependent launches
+    // (each may become resident while the kernel before it finishes)
+    int pdl;
 };
 
 // Buffers and data of the full-metric passes (fullmetric.cuh).

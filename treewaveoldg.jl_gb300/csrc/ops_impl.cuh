@@ -331,8 +331,8 @@ public:
                 if (k == 1 && (E == 2 || E == 4) && mode != MODE_RHS && p.ugd_out) {
                     a.cf = p.cf;
                     a.cfidx = p.cfidx;
-                    if (E == 2) return stage3r_cf_launch<T, P, 2, COMP>(a, tb_, ct_, grid, mode, s);
-                    return stage3r_cf_launch<T, P, 4, COMP>(a, tb_, ct_, grid, mode, s);
+                    if (E == 2) return stage3r_cf_launch<T, P, 2, COMP>(a, tb_, ct_, grid, mode, s, p.pdl);
+                    return stage3r_cf_launch<T, P, 4, COMP>(a, tb_, ct_, grid, mode, s, p.pdl);
                 }
             }
             cudaError_t e = cf_ghosts(p.cf, p.ncf, E, p.fu_in, p.fog_in, const_cast<void*>(p.ugd), nullptr,
@@ -340,12 +340,12 @@ public:
             if (e != cudaSuccess) return e;
         }
         if constexpr (D == 3 && kShaped) {
-            if (k == 1 && E == 2) return launch3r<2>(a, grid, mode, s);
-            if (k == 1 && E == 4) return launch3r<4>(a, grid, mode, s);
+            if (k == 1 && E == 2) return launch3r<2>(a, grid, mode, s, p.pdl);
+            if (k == 1 && E == 4) return launch3r<4>(a, grid, mode, s, p.pdl);
         }
         if constexpr (D == 2 && kShaped) {
-            if (k == 1 && E == 2) return launch2r<2>(a, grid, mode, s);
-            if (k == 1 && E == 4) return launch2r<4>(a, grid, mode, s);
+            if (k == 1 && E == 2) return launch2r<2>(a, grid, mode, s, p.pdl);
+            if (k == 1 && E == 4) return launch2r<4>(a, grid, mode, s, p.pdl);
         }
         if constexpr (kShaped) {
             if (k == 2 && E == 2) {
@@ -366,34 +366,39 @@ public:
     // CTA per SM, every other stage without the compensation array.
     // One instantiation per stage (its data flow compiled in, no other's).
     template <int E>
-    cudaError_t launch3r(const StageArgs<T>& a, int grid, int mode, cudaStream_t s) const {
+    cudaError_t launch3r(const StageArgs<T>& a, int grid, int mode, cudaStream_t s, bool pdl) const {
         if constexpr (D == 3) {
             using SL = Stage3R<T, P, E, false, true>;
             using S0 = Stage3R<T, P, E, false>;
             using SC = Stage3R<T, P, E, true>;
             const size_t m0 = S0::words * sizeof(T);
+            auto go = [&](auto kern, int nt, size_t sm) {
+                StageArgs<T> b = a;
+                b.release = pdl && release_early(kern, grid, nt, sm);
+                return launch_kernel(kern, grid, nt, sm, s, pdl, b, tb_, ct_);
+            };
             if constexpr (COMP) {
                 if (mode == MODE_STAGE4) {
-                    stage3r_kernel<T, P, E, true, false, 4><<<grid, SC::NT, SC::words * sizeof(T), s>>>(a, tb_, ct_);
+                    go(stage3r_kernel<T, P, E, true, false, 4>, SC::NT, SC::words * sizeof(T));
                     return cudaGetLastError();
                 }
             }
             if (mode == MODE_STAGE1) {
                 if constexpr (SL::MINB > S0::MINB)
-                    stage3r_kernel<T, P, E, false, true, 1><<<grid, SL::NT, SL::words * sizeof(T), s>>>(a, tb_, ct_);
+                    go(stage3r_kernel<T, P, E, false, true, 1>, SL::NT, SL::words * sizeof(T));
                 else
-                    stage3r_kernel<T, P, E, false, false, 1><<<grid, S0::NT, m0, s>>>(a, tb_, ct_);
+                    go(stage3r_kernel<T, P, E, false, false, 1>, S0::NT, m0);
             } else if (mode == 2) {
                 if constexpr (SL::MINB > S0::MINB)
-                    stage3r_kernel<T, P, E, false, true, 2><<<grid, SL::NT, SL::words * sizeof(T), s>>>(a, tb_, ct_);
+                    go(stage3r_kernel<T, P, E, false, true, 2>, SL::NT, SL::words * sizeof(T));
                 else
-                    stage3r_kernel<T, P, E, false, false, 2><<<grid, S0::NT, m0, s>>>(a, tb_, ct_);
+                    go(stage3r_kernel<T, P, E, false, false, 2>, S0::NT, m0);
             } else if (mode == 3) {
-                stage3r_kernel<T, P, E, false, false, 3><<<grid, S0::NT, m0, s>>>(a, tb_, ct_);
+                go(stage3r_kernel<T, P, E, false, false, 3>, S0::NT, m0);
             } else if (mode == MODE_STAGE4) {
-                stage3r_kernel<T, P, E, false, false, 4><<<grid, S0::NT, m0, s>>>(a, tb_, ct_);
+                go(stage3r_kernel<T, P, E, false, false, 4>, S0::NT, m0);
             } else {
-                stage3r_kernel<T, P, E, false><<<grid, S0::NT, m0, s>>>(a, tb_, ct_);
+                go(stage3r_kernel<T, P, E, false>, S0::NT, m0);
             }
         }
         return cudaGetLastError();
@@ -402,28 +407,33 @@ public:
     // over K (capped by the persistent layout's CTAs); stage 4 of the
     // compensated path with the compensation array.
     template <int E>
-    cudaError_t launch2r(const StageArgs<T>& a, int grid, int mode, cudaStream_t s) const {
+    cudaError_t launch2r(const StageArgs<T>& a, int grid, int mode, cudaStream_t s, bool pdl) const {
         if constexpr (D == 2) {
             using S0 = Stage2R<T, P, E, false>;
             using SC = Stage2R<T, P, E, true>;
             const int g = std::max(1, std::min(grid, (a.nitems + S0::K - 1) / S0::K));
             const size_t m0 = S0::words * sizeof(T);
+            auto go = [&](auto kern, int nt, size_t sm) {
+                StageArgs<T> b = a;
+                b.release = pdl && release_early(kern, g, nt, sm);
+                return launch_kernel(kern, g, nt, sm, s, pdl, b, tb_);
+            };
             if constexpr (COMP) {
                 if (mode == MODE_STAGE4) {
-                    stage2r_kernel<T, P, E, true, 4><<<g, SC::NT, SC::words * sizeof(T), s>>>(a, tb_);
+                    go(stage2r_kernel<T, P, E, true, 4>, SC::NT, SC::words * sizeof(T));
                     return cudaGetLastError();
                 }
             }
             if (mode == MODE_STAGE1)
-                stage2r_kernel<T, P, E, false, 1><<<g, S0::NT, m0, s>>>(a, tb_);
+                go(stage2r_kernel<T, P, E, false, 1>, S0::NT, m0);
             else if (mode == 2)
-                stage2r_kernel<T, P, E, false, 2><<<g, S0::NT, m0, s>>>(a, tb_);
+                go(stage2r_kernel<T, P, E, false, 2>, S0::NT, m0);
             else if (mode == 3)
-                stage2r_kernel<T, P, E, false, 3><<<g, S0::NT, m0, s>>>(a, tb_);
+                go(stage2r_kernel<T, P, E, false, 3>, S0::NT, m0);
             else if (mode == MODE_STAGE4)
-                stage2r_kernel<T, P, E, false, 4><<<g, S0::NT, m0, s>>>(a, tb_);
+                go(stage2r_kernel<T, P, E, false, 4>, S0::NT, m0);
             else
-                stage2r_kernel<T, P, E, false><<<g, S0::NT, m0, s>>>(a, tb_);
+                go(stage2r_kernel<T, P, E, false>, S0::NT, m0);
         }
         return cudaGetLastError();
     }

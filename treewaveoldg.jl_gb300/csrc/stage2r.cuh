@@ -128,6 +128,12 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
     const T* vsrc = mode == 2 ? a.y : ysrc;
     const bool final_comp = COMP && mode == MODE_STAGE4;
 
+    // the first blocks' operands are asked into L2 (a hint) before the wait
+    // on the previous stage, as in the 3D kernel
+    const int first = blockIdx.x * K + bs;
+    if (c == 0 && first < a.nitems) prefetch_stage3r<T>(a, first, NN, (int)gridDim.x * K);
+    grid_dependency_wait();
+    if (a.release) grid_dependents_launch();
     for (int base = blockIdx.x * K; base < a.nitems; base += gridDim.x * K) {
         const int item = base + bs;
         // every thread passes every barrier; a slot past the last item holds
@@ -142,7 +148,7 @@ __global__ void __launch_bounds__(Stage2R<T, P, E, COMP>::NT)
         if (live) {
             // the block's stage operands (and the next block this slot takes)
             // into L2 while the CTA computes
-            if (c == 0) prefetch_stage3r<T>(a, item, NN, (int)gridDim.x * K);
+            if (c == 0 && item != first) prefetch_stage3r<T>(a, item, NN, (int)gridDim.x * K);
             flags = it->flags;
             slot = it->slot;
 #pragma unroll

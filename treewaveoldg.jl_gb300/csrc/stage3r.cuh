@@ -327,6 +327,13 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
     const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1 || mode == 2) ? a.u : a.y;
     const T* vsrc = mode == 2 ? a.y : ysrc;
 
+    // the first block's operands are asked into L2 (a hint: L2 is where the
+    // previous stage's writes land, so nothing stale is read) before the
+    // wait on the previous stage, so that under a programmatic launch their
+    // reads overlap that stage's last CTAs
+    if (tid == 0 && (int)blockIdx.x < a.nitems) prefetch_stage3r<T>(a, blockIdx.x, NN);
+    grid_dependency_wait();
+    if (a.release) grid_dependents_launch();
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         const BlockItem& it = a.items[item];
         const uint32_t flags = it.flags;
@@ -339,7 +346,7 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
         const T inv_h = T(1) / hb;
         const T inv_h2 = inv_h * inv_h;
         const T* yu = ysrc + it.off;
-        if (tid == 0) prefetch_stage3r<T>(a, item, NN);
+        if (tid == 0 && item != (int)blockIdx.x) prefetch_stage3r<T>(a, item, NN);
         // every global load of the block's prologue at once: the column, the u
         // ghosts and the neighbours' gradient parts at this face point
         T line[N + 2];
@@ -594,11 +601,11 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
 // The register-line stage of a forest with refinement (CFP), instantiated
 // per order in a translation unit of its own (kernels_d3_p<P>_cf.cu): its
 // shared-memory attributes, set once per device, and a launch of RK stage
-// `mode` (1 to 4).
+// `mode` (1 to 4), as a programmatic dependent launch when `pdl` is set.
 template <typename T, int P, bool COMP>
 void stage3r_cf_attrs(int max_smem);
 template <typename T, int P, int E, bool COMP>
 cudaError_t stage3r_cf_launch(const StageArgs<T>& a, const Tab<T, P>& tb, const CfTab<T, P>& ct, int grid,
-                              int mode, cudaStream_t s);
+                              int mode, cudaStream_t s, bool pdl);
 
 }  // namespace twoldg

@@ -37,32 +37,37 @@ void stage3r_cf_attrs(int max_smem) {
 }
 
 // Every RK stage in the plain register budget (the lean stage 1 and 2
-// variants of the uniform forests are left out here); the right-hand side of
-// a forest with refinement runs the plain kernel after a launch that fills
-// its ghost planes.
+// variants of the uniform forests are left out here), as a programmatic
+// dependent launch when `pdl` is set; the right-hand side of a forest with
+// refinement runs the plain kernel after a launch that fills its ghost planes.
 template <typename T, int P, int E, bool COMP>
 cudaError_t stage3r_cf_launch(const StageArgs<T>& a, const Tab<T, P>& tb, const CfTab<T, P>& ct, int grid,
-                              int mode, cudaStream_t s) {
+                              int mode, cudaStream_t s, bool pdl) {
     if constexpr (!Stage3R<T, P, E, false>::usable) {
         return cudaErrorInvalidConfiguration;
     } else {
         using S0 = Stage3R<T, P, E, false>;
         using SC = Stage3R<T, P, E, true>;
         const size_t m0 = S0::words * sizeof(T);
+        auto go = [&](auto kern, int nt, size_t sm) {
+            StageArgs<T> b = a;
+            b.release = pdl && release_early(kern, grid, nt, sm);
+            return launch_kernel(kern, grid, nt, sm, s, pdl, b, tb, ct);
+        };
         if constexpr (COMP) {
             if (mode == MODE_STAGE4) {
-                stage3r_kernel<T, P, E, true, false, 4, true><<<grid, SC::NT, SC::words * sizeof(T), s>>>(a, tb, ct);
+                go(stage3r_kernel<T, P, E, true, false, 4, true>, SC::NT, SC::words * sizeof(T));
                 return cudaGetLastError();
             }
         }
         if (mode == MODE_STAGE1)
-            stage3r_kernel<T, P, E, false, false, 1, true><<<grid, S0::NT, m0, s>>>(a, tb, ct);
+            go(stage3r_kernel<T, P, E, false, false, 1, true>, S0::NT, m0);
         else if (mode == 2)
-            stage3r_kernel<T, P, E, false, false, 2, true><<<grid, S0::NT, m0, s>>>(a, tb, ct);
+            go(stage3r_kernel<T, P, E, false, false, 2, true>, S0::NT, m0);
         else if (mode == 3)
-            stage3r_kernel<T, P, E, false, false, 3, true><<<grid, S0::NT, m0, s>>>(a, tb, ct);
+            go(stage3r_kernel<T, P, E, false, false, 3, true>, S0::NT, m0);
         else if (mode == MODE_STAGE4)
-            stage3r_kernel<T, P, E, false, false, 4, true><<<grid, S0::NT, m0, s>>>(a, tb, ct);
+            go(stage3r_kernel<T, P, E, false, false, 4, true>, S0::NT, m0);
         else
             return cudaErrorInvalidValue;
         return cudaGetLastError();
@@ -74,7 +79,7 @@ cudaError_t stage3r_cf_launch(const StageArgs<T>& a, const Tab<T, P>& tb, const 
 // which measured faster there).
 #define TWOLDG_STAGE3R_CF_E(T, P, E, COMP)                                                                      \
     template cudaError_t stage3r_cf_launch<T, P, E, COMP>(const StageArgs<T>&, const Tab<T, P>&,              \
-                                                           const CfTab<T, P>&, int, int, cudaStream_t);
+                                                           const CfTab<T, P>&, int, int, cudaStream_t, bool);
 #define TWOLDG_STAGE3R_CF(P)                                \
     template void stage3r_cf_attrs<float, P, false>(int);  \
     template void stage3r_cf_attrs<float, P, true>(int);   \
