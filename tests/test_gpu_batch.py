@@ -1,7 +1,9 @@
 """The batched ensemble (twoldg_batch_*): independent 2D periodic problems
 of uneven P, E and roots stepped together, one work list per shape and one
 graph per step. Each member must equal the same problem stepped alone, bit
-for bit (the same kernels and arithmetic), and the FP64 members the oracle."""
+for bit (the same kernels and arithmetic; alone, a problem's stage kernels
+run as programmatic dependent launches, in the batch as plain ones), and the
+FP64 members the oracle."""
 import ctypes
 import math
 

@@ -1299,6 +1299,15 @@ __global__ void __launch_bounds__(256) energy_kernel(StageArgs<T> a, Tab<T, P> t
 // Quadrature p-norm parts (src/layout.jl:100-122, 223-235): per block
 // sum w |x - ref|^p over the selected variables and sum w * nvars; p = 0
 // means the largest |x - ref|.
+//
+// A thread takes columns along the slowest dimension (consecutive threads,
+// consecutive columns: coalesced loads), so the weight's factor of the other
+// dimensions is one product a column, and the slowest dimension's factor
+// wq[q] multiplies P+1 running sums (one per node position q of an element)
+// once at the end: a node costs its difference and one FP64 FMA a variable,
+// no integer division and no weight product. Every sum stays FP64. A block
+// of fewer columns than threads splits each column's elements among
+// blockDim / C threads.
 template <typename T, int D, int P>
 __global__ void norm_kernel(const BlockItem* items, int nitems, int E, const T* u, const T* ref, int p,
                             int vars_mask, Tab<T, P> tb, double* part_num, double* part_vol, const T* coef,
@@ -1307,33 +1316,74 @@ __global__ void norm_kernel(const BlockItem* items, int nitems, int E, const T* 
     constexpr int P1 = P + 1;
     const int N = E * P1;
     const int NN = ipow(N, D);
+    const int C = NN / N;   // columns a block: N^(D-1)
     double wqd[P1];
+    double wsum = 0;
 #pragma unroll
-    for (int i = 0; i < P1; ++i) wqd[i] = (double)tb.wq[i];
+    for (int i = 0; i < P1; ++i) {
+        wqd[i] = (double)tb.wq[i];
+        wsum += wqd[i];
+    }
+    const int nvars = (vars_mask & 1) + ((vars_mask >> 1) & 1);
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         const BlockItem it = items[item];
         // the weights' block factor wscale^D multiplies the sums once
         const double wscale = it.h * P1 / 2.0;
         double wsD = 1.0;
         for (int k = 0; k < D; ++k) wsD *= wscale;
+        const T* cw = coef ? coef + (int64_t)item * ncoef * NN : nullptr;
         double num = 0, vol = 0;
-        for (int n = threadIdx.x; n < NN; n += blockDim.x) {
-            int m = n;
-            double w = wqd[(m % N) % P1];
-            m /= N;
-            for (int k = 1; k < D; ++k) { w *= wqd[(m % N) % P1]; m /= N; }
-            // on a geometry the norm is weighted by sqrt(g): the physical volume
-            if (coef) w *= (double)coef[(int64_t)item * ncoef * NN + n];
-            for (int var = 0; var < 2; ++var) {
-                if (!(vars_mask & (1 << var))) continue;
-                int64_t o = it.off + (int64_t)var * NN + n;
-                double x = (double)u[o];
-                if (ref) x -= (double)ref[o];
-                x = fabs(x);
-                if (p == 0) num = fmax(num, x);
-                else if (p == 2) num += w * x * x;
-                else num += w * pow(x, (double)p);
-                vol += w;
+        const bool wide = C >= (int)blockDim.x;
+        const int S = wide ? 1 : (int)blockDim.x / C;              // slices of a column's elements
+        const int sl = wide ? 0 : (int)threadIdx.x / C;            // this thread's slice
+        const int cstep = wide ? (int)blockDim.x : C;
+        for (int c = wide ? (int)threadIdx.x : (int)threadIdx.x % C; sl < S && c < C; c += cstep) {
+            // the column's weight over the dimensions but the slowest
+            double wc = 1.0;
+            int m = c;
+            for (int k = 1; k < D; ++k) {
+                wc *= wqd[(m % N) % P1];
+                m /= N;
+            }
+            double acc[P1], accv[P1];
+#pragma unroll
+            for (int q = 0; q < P1; ++q) acc[q] = accv[q] = 0.0;
+            double mx = 0;
+            int ne = 0;
+            for (int e = sl; e < E; e += S) {
+                ++ne;
+#pragma unroll
+                for (int q = 0; q < P1; ++q) {
+                    const int n = c + C * (e * P1 + q);
+                    const double g = cw ? (double)cw[n] : 1.0;
+                    if (cw) accv[q] += g;
+#pragma unroll
+                    for (int var = 0; var < 2; ++var) {
+                        if (!(vars_mask & (1 << var))) continue;
+                        const int64_t o = it.off + (int64_t)var * NN + n;
+                        double x = (double)u[o];
+                        if (ref) x -= (double)ref[o];
+                        if (p == 0) mx = fmax(mx, fabs(x));
+                        else if (p == 2) acc[q] += (cw ? g * x : x) * x;
+                        else acc[q] += g * pow(fabs(x), (double)p);
+                    }
+                }
+            }
+            if (p == 0) {
+                num = fmax(num, mx);
+            } else {
+                double s = 0;
+#pragma unroll
+                for (int q = 0; q < P1; ++q) s += wqd[q] * acc[q];
+                num += wc * s;
+            }
+            if (cw) {
+                double sv = 0;
+#pragma unroll
+                for (int q = 0; q < P1; ++q) sv += wqd[q] * accv[q];
+                vol += wc * sv * nvars;
+            } else {
+                vol += wc * wsum * ne * nvars;
             }
         }
         double s;
