@@ -542,6 +542,9 @@ struct twoldg_runner {
 
     FmPtrs fptrs(Group& g, void* u, int in) {
         FmPtrs p{};
+        // a full-metric problem is one group: its passes as programmatic
+        // dependent launches, as the flat stage kernels of a one-group problem
+        p.pdl = groups.size() == 1;
         p.u = u;
         p.y = y.p;
         p.acc = acc.p;

@@ -50,30 +50,39 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, false>::NT, (FmStageR<T, P, E
     const int s2 = (ca + 1) + SX * (cb + 1);       // z column (x0, x1) = (ca, cb)
     const int mode = FM;
     const T* ysrc = (mode == MODE_STAGE1) ? a.u : a.y;
+    // a block's operands into L2 (a hint): the fluxes, sqrt(g), the stage
+    // operands and the block's projection tables
+    auto prefetch = [&](int item) {
+        const int64_t off = a.items[item].off;
+        const size_t b = (size_t)NN * sizeof(T);
+        prefetch_l2(a.V + (int64_t)item * 3 * NN, 3 * b);
+        prefetch_l2(a.coef + (int64_t)item * 10 * NN, b);
+        prefetch_l2(ysrc + off, 2 * b);
+        if (mode != MODE_STAGE1) {
+            prefetch_l2(a.u + off, 2 * b);
+            prefetch_l2(a.acc + off, 2 * b);
+            if (COMP && mode == MODE_STAGE4) prefetch_l2(a.comp + off, 2 * b);
+        }
+        const int es = a.eslot[item];
+        if (a.truncate && es > 0) {
+            constexpr int n3 = (P + 1) * (P + 1) * (P + 1), m3 = P * P * P;
+            constexpr size_t EE = (size_t)E * E * E;
+            prefetch_l2(a.ew + (int64_t)(es - 1) * n3 * EE, n3 * EE * sizeof(T));
+            prefetch_l2(a.echol + (int64_t)(es - 1) * m3 * m3 * EE, (size_t)m3 * m3 * EE * sizeof(T));
+        }
+    };
+    // the first block's before the wait on the gradient pass, as in the flat
+    // stage kernel (L2 is where that pass's writes land: nothing stale is read)
+    if (tid == 0 && (int)blockIdx.x < a.nitems) prefetch(blockIdx.x);
+    grid_dependency_wait();
+    if (a.release) grid_dependents_launch();
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         const BlockItem& it = a.items[item];
         const T inv_h = T(1) / T(it.h);
         const double t = stage_time(a.tinfo, it.problem, mode);
         const T* cf = a.coef + (int64_t)item * 10 * NN;
         const T* Fb = a.V + (int64_t)item * 3 * NN;
-        if (tid == 0) {
-            const size_t b = (size_t)NN * sizeof(T);
-            prefetch_l2(Fb, 3 * b);
-            prefetch_l2(cf, b);
-            prefetch_l2(ysrc + it.off, 2 * b);
-            if (mode != MODE_STAGE1) {
-                prefetch_l2(a.u + it.off, 2 * b);
-                prefetch_l2(a.acc + it.off, 2 * b);
-                if (COMP && mode == MODE_STAGE4) prefetch_l2(a.comp + it.off, 2 * b);
-            }
-            const int es = a.eslot[item];
-            if (a.truncate && es > 0) {
-                constexpr int n3 = (P + 1) * (P + 1) * (P + 1), m3 = P * P * P;
-                constexpr size_t EE = (size_t)E * E * E;
-                prefetch_l2(a.ew + (int64_t)(es - 1) * n3 * EE, n3 * EE * sizeof(T));
-                prefetch_l2(a.echol + (int64_t)(es - 1) * m3 * m3 * EE, (size_t)m3 * m3 * EE * sizeof(T));
-            }
-        }
+        if (tid == 0 && item != (int)blockIdx.x) prefetch(item);
         // D_z F^z down the column, in registers
         T lapz[N];
         {
@@ -197,16 +206,21 @@ size_t fm_stage_r_smem() {
 
 template <typename T, int P, int E, bool COMP>
 cudaError_t fm_stage_r_launch(const FmArgs<T>& a, const Tab<T, P>& tb, const FmTab<T, P>& ft, int grid, int mode,
-                              cudaStream_t s) {
+                              cudaStream_t s, bool pdl) {
     if constexpr (!Stage3R<T, P, E, false>::usable) {
         return cudaErrorInvalidConfiguration;
     } else {
         constexpr int NT = Stage3R<T, P, E, false>::NT;
         const size_t smem = fm_stage_r_smem<T, P, E, COMP>();
-        if (mode == MODE_STAGE1) fm_stage_r_kernel<T, P, E, COMP, 1><<<grid, NT, smem, s>>>(a, tb, ft);
-        else if (mode == 2) fm_stage_r_kernel<T, P, E, COMP, 2><<<grid, NT, smem, s>>>(a, tb, ft);
-        else if (mode == 3) fm_stage_r_kernel<T, P, E, COMP, 3><<<grid, NT, smem, s>>>(a, tb, ft);
-        else if (mode == MODE_STAGE4) fm_stage_r_kernel<T, P, E, COMP, 4><<<grid, NT, smem, s>>>(a, tb, ft);
+        auto go = [&](auto kern) {
+            FmArgs<T> b = a;
+            b.release = pdl && release_early(kern, grid, NT, smem);
+            return launch_kernel(kern, grid, NT, smem, s, pdl, b, tb, ft);
+        };
+        if (mode == MODE_STAGE1) go(fm_stage_r_kernel<T, P, E, COMP, 1>);
+        else if (mode == 2) go(fm_stage_r_kernel<T, P, E, COMP, 2>);
+        else if (mode == 3) go(fm_stage_r_kernel<T, P, E, COMP, 3>);
+        else if (mode == MODE_STAGE4) go(fm_stage_r_kernel<T, P, E, COMP, 4>);
         else return cudaErrorInvalidValue;
         return cudaGetLastError();
     }
@@ -217,7 +231,7 @@ cudaError_t fm_stage_r_launch(const FmArgs<T>& a, const Tab<T, P>& tb, const FmT
     template void fm_stage_r_attrs<T, P, E, COMP>(int);                                                          \
     template size_t fm_stage_r_smem<T, P, E, COMP>();                                                            \
     template cudaError_t fm_stage_r_launch<T, P, E, COMP>(const FmArgs<T>&, const Tab<T, P>&, const FmTab<T, P>&, \
-                                                           int, int, cudaStream_t);
+                                                           int, int, cudaStream_t, bool);
 #define TWOLDG_FMSTAGE_R(P)                  \
     TWOLDG_FMSTAGE_R_E(double, P, 2, false) \
     TWOLDG_FMSTAGE_R_E(double, P, 4, false) \

@@ -80,6 +80,9 @@ struct FmArgs {
     // u's ghosts (N^2 per slot) and V's ((3, N^2) per slot)
     const T* ugd;
     const T* vgd;
+    // under a programmatic dependent launch: 1 where the pass lets the next
+    // kernel launch from its start, 0 where it does so at its end
+    int release;
 };
 
 template <typename T, int P>
@@ -288,15 +291,21 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, false>::NT) fm_gradient_r_ker
     const int l0 = LX * ca + LXY * cb, l1 = ca + LXY * cb, l2 = ca + LX * cb;
     const int mode = a.mode;
     const T* ysrc = (mode == MODE_RHS || mode == MODE_STAGE1 || mode == MODE_ENERGY) ? a.u : a.y;
+    // the block's metric (written once, at setup) into L2: the first block's
+    // before the wait on the previous kernel
+    auto prefetch = [&](int item) {
+        prefetch_l2(a.M + (int64_t)item * 6 * NN, 6 * (size_t)NN * sizeof(T));
+        prefetch_l2(a.coef + (int64_t)item * 10 * NN, (size_t)NN * sizeof(T));
+    };
+    if (tid == 0 && (int)blockIdx.x < a.nitems) prefetch(blockIdx.x);
+    grid_dependency_wait();
+    if (a.release) grid_dependents_launch();
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         const BlockItem& it = a.items[item];
         const T inv_h = T(1) / T(it.h);
         const double t = stage_time(a.tinfo, it.problem, mode == MODE_ENERGY ? 0 : mode);
         const T* yu = ysrc + it.off;
-        if (tid == 0) {
-            prefetch_l2(a.M + (int64_t)item * 6 * NN, 6 * (size_t)NN * sizeof(T));
-            prefetch_l2(a.coef + (int64_t)item * 10 * NN, (size_t)NN * sizeof(T));
-        }
+        if (tid == 0 && item != (int)blockIdx.x) prefetch(item);
         T line[N + 2];
 #pragma unroll
         for (int j = 0; j < N; ++j) {
@@ -928,7 +937,7 @@ template <typename T, int P, int E, bool COMP>
 size_t fm_stage_r_smem();
 template <typename T, int P, int E, bool COMP>
 cudaError_t fm_stage_r_launch(const FmArgs<T>& a, const Tab<T, P>& tb, const FmTab<T, P>& ft, int grid, int mode,
-                              cudaStream_t s);
+                              cudaStream_t s, bool pdl);
 
 // The standalone truncation of the full metric (twoldg_truncate).
 template <typename T, int P>

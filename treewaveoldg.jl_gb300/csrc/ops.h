@@ -83,6 +83,7 @@ struct FmPtrs {
     const BoundaryTable* btab;
     const void* ugd;    // coarse-fine faces (a refined brick patch): u's ghosts per slot (N^2)
     const void* vgd;    // and V's, (3, N^2) per slot
+    int pdl;            // the register-line passes as programmatic dependent launches
 };
 
 // A launch layout of the stage kernel. kernel: 0 the shape's default, 1 the

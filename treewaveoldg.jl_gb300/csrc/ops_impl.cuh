@@ -560,19 +560,19 @@ public:
             const int g = std::min(nitems, kMaxGrid);
             if constexpr (kShaped) {
                 // the register-line pass for the compile-time shapes
-                if (E == 2 && Stage3R<T, P, 2, false>::usable) {
-                    fm_gradient_r_kernel<T, P, 2><<<g, Stage3R<T, P, 2, false>::NT,
-                                                    FmGradR<T, P, 2>::words * sizeof(T), s>>>(
-                        fm_args(items, nitems, E, mode, 0, p), tb_);
+                auto go = [&](auto kern, int nt, size_t sm) {
+                    FmArgs<T> b = fm_args(items, nitems, E, mode, 0, p);
+                    b.release = p.pdl && release_early(kern, g, nt, sm);
+                    launch_kernel(kern, g, nt, sm, s, p.pdl != 0, b, tb_);
                     return cudaGetLastError();
-                }
+                };
+                if (E == 2 && Stage3R<T, P, 2, false>::usable)
+                    return go(fm_gradient_r_kernel<T, P, 2>, Stage3R<T, P, 2, false>::NT,
+                              FmGradR<T, P, 2>::words * sizeof(T));
                 if (E == 4 && Stage3R<T, P, 4, false>::usable &&
-                    FmGradR<T, P, 4>::words * sizeof(T) <= (size_t)max_smem_) {
-                    fm_gradient_r_kernel<T, P, 4><<<g, Stage3R<T, P, 4, false>::NT,
-                                                    FmGradR<T, P, 4>::words * sizeof(T), s>>>(
-                        fm_args(items, nitems, E, mode, 0, p), tb_);
-                    return cudaGetLastError();
-                }
+                    FmGradR<T, P, 4>::words * sizeof(T) <= (size_t)max_smem_)
+                    return go(fm_gradient_r_kernel<T, P, 4>, Stage3R<T, P, 4, false>::NT,
+                              FmGradR<T, P, 4>::words * sizeof(T));
             }
             size_t smem = fm_grad_smem(E);
             if (smem > (size_t)max_smem_) return cudaErrorInvalidConfiguration;
@@ -593,10 +593,10 @@ public:
                 if (mode >= MODE_STAGE1 && mode <= MODE_STAGE4) {
                     if (E == 2 && Stage3R<T, P, 2, false>::usable &&
                         fm_stage_r_smem<T, P, 2, COMP>() <= (size_t)max_smem_)
-                        return fm_stage_r_launch<T, P, 2, COMP>(fa, tb_, ft_, g, mode, s);
+                        return fm_stage_r_launch<T, P, 2, COMP>(fa, tb_, ft_, g, mode, s, p.pdl != 0);
                     if (E == 4 && Stage3R<T, P, 4, false>::usable &&
                         fm_stage_r_smem<T, P, 4, COMP>() <= (size_t)max_smem_)
-                        return fm_stage_r_launch<T, P, 4, COMP>(fa, tb_, ft_, g, mode, s);
+                        return fm_stage_r_launch<T, P, 4, COMP>(fa, tb_, ft_, g, mode, s, p.pdl != 0);
                 }
             }
             // one instantiation per stage
