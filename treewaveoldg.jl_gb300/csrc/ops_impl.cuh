@@ -553,6 +553,16 @@ public:
     // coefficients per element: P^3 (per-element projection) or (P+1) P^2 (factored)
     static size_t fm_cbuf_words(int E) { return (size_t)E * E * E * (P + 1) * P * P; }
     static size_t fm_stage_smem(int E) { return (padded_words(E) + 2 * plain_words(E) + fm_cbuf_words(E)) * sizeof(T); }
+    // Whether the register-line full-metric passes on 8^3 blocks (64 threads a
+    // CTA) have threads enough to fill the GPU: in FP32 a forest whose blocks
+    // give every SM fewer than 1024 threads (half what it holds) runs the
+    // run-time-shape passes of 256 threads a CTA instead (the seven-patch
+    // ball, 448 blocks: 0.245 against 0.269 ms a step), while FP64, held by
+    // its pipe, keeps the register-line passes at any size (0.463 against
+    // 0.616 ms there).
+    bool fm_r_fills(int nitems) const {
+        return sizeof(T) == 8 || (int64_t)nitems * 64 >= (int64_t)nsm_ * 1024;
+    }
     cudaError_t fm_gradient(const BlockItem* items, int nitems, int E, int mode, const FmPtrs& p,
                             cudaStream_t s) const override {
         if constexpr (D != 3) return cudaErrorNotSupported;
@@ -566,7 +576,7 @@ public:
                     launch_kernel(kern, g, nt, sm, s, p.pdl != 0, b, tb_);
                     return cudaGetLastError();
                 };
-                if (E == 2 && Stage3R<T, P, 2, false>::usable)
+                if (E == 2 && Stage3R<T, P, 2, false>::usable && fm_r_fills(nitems))
                     return go(fm_gradient_r_kernel<T, P, 2>, Stage3R<T, P, 2, false>::NT,
                               FmGradR<T, P, 2>::words * sizeof(T));
                 if (E == 4 && Stage3R<T, P, 4, false>::usable &&
@@ -591,7 +601,7 @@ public:
             if constexpr (kShaped) {
                 // the register-line pass for the compile-time shapes' RK stages
                 if (mode >= MODE_STAGE1 && mode <= MODE_STAGE4) {
-                    if (E == 2 && Stage3R<T, P, 2, false>::usable &&
+                    if (E == 2 && Stage3R<T, P, 2, false>::usable && fm_r_fills(nitems) &&
                         fm_stage_r_smem<T, P, 2, COMP>() <= (size_t)max_smem_)
                         return fm_stage_r_launch<T, P, 2, COMP>(fa, tb_, ft_, g, mode, s, p.pdl != 0);
                     if (E == 4 && Stage3R<T, P, 4, false>::usable &&
