@@ -185,10 +185,11 @@ int twoldg_truncate(twoldg_problem* p, void* u);
 
 /* `nsteps` classic RK4 steps of size dt from time t, in place on u, with the
  * truncation as stage and step limiter -- wave_integrator + solve!
- * (src/stepping.jl:72-78, src/evolution.jl:1408-1430). The step is a CUDA
- * graph captured on the first call for a state pointer; the graphs of the
- * four most recently used pointers are kept (a caller may alternate state
- * buffers), and a new dt changes only the coefficients the graph reads.
+ * (src/stepping.jl:72-78, src/evolution.jl:1408-1430). The steps run from
+ * CUDA graphs of up to 16 steps (a call's remainder in a graph of its own),
+ * captured on first use for a (state pointer, step count) pair; the six most
+ * recently used graphs are kept (a caller may alternate state buffers), and
+ * a new dt changes only the coefficients the graphs read.
  * For TWOLDG_F32C the compensation words persist between calls on the same
  * u and are cleared when u changes or by twoldg_reset_compensation. */
 int twoldg_rk4_step(twoldg_problem* p, void* u, double t, double dt, int32_t nsteps);
@@ -421,8 +422,8 @@ int twoldg_support_elements(twoldg_transfer_plan* plan, int32_t k, int32_t* out,
 int twoldg_transfer_table(int32_t order, int32_t precision, const char* name, int32_t q, void* out);
 
 /* Batched ensemble: n independent problems stepped together, the blocks of
- * all of them as one work list per (dim, order, elems) group and one RK4
- * step per CUDA graph launch. No reference counterpart (the reference runs
+ * all of them as one work list per (dim, order, elems) group and up to 16
+ * RK4 steps per CUDA graph launch. No reference counterpart (the reference runs
  * one forest per WaveProblem); each member behaves as twoldg_rk4_step on its
  * own problem. States are one device buffer: member k's state starts at word
  * offsets[k] (as returned by twoldg_batch_offsets). */

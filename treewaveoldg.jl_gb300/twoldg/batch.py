@@ -1,6 +1,6 @@
 """The batched ensemble over libtwoldg's twoldg_batch_* entry points: many
 independent problems of uneven (P, E, roots) stepped together, one work list
-per shape and one CUDA graph launch per RK4 step. No reference counterpart:
+per shape and up to 16 RK4 steps per CUDA graph launch. No reference counterpart:
 the reference runs one forest per WaveProblem."""
 import ctypes
 import math
