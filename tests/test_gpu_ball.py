@@ -52,6 +52,24 @@ def test_ball_parity_f64(native, P, E, roots, truncate):
                                                                           rel=1e-12)
 
 
+def test_ball_steps_past_one_graph(native):
+    # 19 steps in one call: a graph of 16 steps and one of 3, the problem's
+    # time advanced on the device after each step inside the graph, the
+    # passes chained as programmatic dependent launches; against the oracle
+    import torch
+    import twoldg
+    P, E, roots = 3, 2, (2, 2)
+    forest, geo, wave, tables, o = ball_setup(P, E, roots, True)
+    p = problem(forest, P, wave, True)
+    f = lambda x, v: np.sin(0.4 * x[0] + v) * np.cos(0.3 * x[1] - 0.2 * x[2]) + 0.1 * x[2] * v
+    u0 = o.truncate(ball_state(forest, tables, f))
+    dt = 0.5 * tables["hspeed"] / (P + 1)
+    integ = twoldg.wave_integrator(p, torch.from_numpy(u0).cuda(), 0.1, 0.1 + 19 * dt, dt)
+    integ.nsteps = 19
+    integ.solve()
+    assert rel(integ.u.cpu().numpy(), o.rk4(u0, dt, 19, 0.1)) < 1e-12
+
+
 def test_sevenpatch_errors_match_published(native):
     # reference CODE.md:4247-4252, P = 3, truncated, roots (2, 2): u 8.83e-3, v 1.14e-2
     import twoldg

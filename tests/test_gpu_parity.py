@@ -178,16 +178,29 @@ def test_f32_paths_against_f64_oracle(native, case):
         assert rel(integ.u.cpu().numpy(), ref) < 1e-4, prec
 
 
-def test_steps_in_one_call_equal_steps_one_by_one(native):
-    # the captured graph replays the same arithmetic: bitwise equal
-    forest, p, o, u = build(CASES[6])
-    dt = 0.5 * forest.minimum_spacing() / 4
-    a = native.wave_integrator(p, dev(p, o.truncate(u)), 0.0, 4 * dt, dt)
+@pytest.mark.parametrize("case", [CASES[3], CASES[6], CASES[10]], ids=ids)
+@pytest.mark.parametrize("prec", ["f64", "f32c"])
+def test_steps_in_one_call_equal_steps_one_by_one(native, case, prec):
+    # 19 steps in one call run one graph of 16 steps and one of 3, the stage
+    # kernels chained as programmatic dependent launches across the steps;
+    # one step a call runs a graph of one. The same arithmetic: bitwise equal.
+    # Except in FP32 on a refined forest: there a call's first stage reads
+    # coarse-fine planes that a launch forms whole from the face exports,
+    # where the later stages read them as the two sides' epilogues wrote them
+    # (the other side's part plus this side's), which rounds differently
+    dtype = np.float64 if prec == "f64" else np.float32
+    forest, p, o, u = build(case, dtype=dtype, precision=prec)
+    dt = 0.5 * forest.minimum_spacing() / (case[1] + 1)
+    a = native.wave_integrator(p, dev(p, o.truncate(u)), 0.0, 19 * dt, dt)
+    a.nsteps = 19
     a.solve()
-    b = native.wave_integrator(p, dev(p, o.truncate(u)), 0.0, 4 * dt, dt)
-    for _ in range(4):
+    b = native.wave_integrator(p, dev(p, o.truncate(u)), 0.0, 19 * dt, dt)
+    for _ in range(19):
         b.step()
-    assert np.array_equal(a.u.cpu().numpy(), b.u.cpu().numpy())
+    if case[5] and prec != "f64":
+        assert rel(a.u.cpu().numpy(), b.u.cpu().numpy().astype(np.float64)) < 1e-5
+    else:
+        assert np.array_equal(a.u.cpu().numpy(), b.u.cpu().numpy())
 
 
 def test_wave_errors_2d_p4_against_oracle_and_published(native):
