@@ -371,7 +371,13 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
                 gp[f] = a.fog_in[(int64_t)nb[f] * F + tid];
             }
         }
-        // ---- z: the column in registers
+        // ---- z: the column in registers (stage 1 keeps a copy: its RK
+        // combination reads u^n's u, which is this column, from registers)
+        T col[FM == 1 ? N : 1];
+        if constexpr (FM == 1) {
+#pragma unroll
+            for (int j = 0; j < N; ++j) col[j] = line[1 + j];
+        }
         {
 #pragma unroll
             for (int j = 0; j < N; ++j) su[s2 + SXY * j] = line[1 + j];
@@ -471,9 +477,11 @@ __global__ void __launch_bounds__(Stage3R<T, P, E, COMP, LEAN>::NT, Stage3R<T, P
                 const int n = tid + F * (ez * P1 + q);
                 y[q] = yv[n];
                 if (mode == MODE_STAGE1) {
-                    // the stage input is u^n: its u is the column in shared
-                    // memory, its v the value just loaded
-                    uu[q] = su[s2 + SXY * (ez * P1 + q)];
+                    // the stage input is u^n: its u is the column (kept in
+                    // registers by the stage-1 instantiation, else in shared
+                    // memory), its v the value just loaded
+                    if constexpr (FM == 1) uu[q] = col[ez * P1 + q];
+                    else uu[q] = su[s2 + SXY * (ez * P1 + q)];
                     uv[q] = y[q];
                 } else {
                     uu[q] = un[n];
