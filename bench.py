@@ -588,7 +588,7 @@ def ball13_run(twoldg, torch, roots, steps, warmup, repeats=3):
                       "ns_per_node_step": mps * 1e6 / nodes, "stage_ms": [float(x) for x in st],
                       "nodes": nodes, "dt": dt, "clocks": clocks,
                       "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                                   "note": "the survey's algorithmic bytes of the flat step; the full metric reads "
+                                   "note": "the flat step's algorithmic bytes (the minimum RK4 data flow); the full metric reads "
                                            "fluxes and sqrt(g) besides"},
                       "energy0": e0, "energy": twoldg.wave_energy(p, u, t=t1)}
         final[prec] = (p, u)
@@ -1022,8 +1022,9 @@ def main():
         "accuracy": {"fp64": acc64, "f32c": acc32},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_kind": peak_kind, "kernel": kname, "layout": head["layout"],
-                     "achieved_from": "the timed region: 152 B/node-step x nodes / ms_per_step, i.e. the survey's "
-                                      "algorithmic bytes per stage launch over the average launch (a quarter step)",
+                     "achieved_from": "the timed region: 152 B/node-step x nodes / ms_per_step, i.e. the minimum RK4 "
+                                      "data flow's algorithmic bytes per stage launch over the average launch (a "
+                                      "quarter step)",
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per stage launch, "
                                        "profiles/stage3r_f32c_256cube.md",
                      "stage_ms": [float(x) for x in stage],

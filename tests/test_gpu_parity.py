@@ -1,5 +1,5 @@
 """Parity of libtwoldg (CUDA, through the C ABI) with the CPU oracle, on the
-same seeded inputs: FP64 to 1e-12 relative (the benchmark spec's bar), float32
+same seeded inputs: FP64 to 1e-12 relative (the parity bar), float32
 paths within stated tolerances. Marked gpu."""
 import math
 

@@ -1,5 +1,5 @@
 """The bench on the CPU: its N > 1 path, which runs independent replicas (the
-field step has no collective; the survey's multi-GPU row plans replicas only),
+field step has no collective: each GPU runs a replica of the problem),
 where two gloo ranks take the barrier and the maximum of their times and the
 reference arm runs on rank 0 alone; the reference arm's JSON line; and the
 clock summary of the timed region."""
